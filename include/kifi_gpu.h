@@ -1,0 +1,176 @@
+/*
+ * kifi_gpu.h -- C ABI of the GB300 (sm_103a) depth-fusion library
+ * (libkifi_gpu.so), a drop-in for the per-frame fusion path of
+ * denniskb/merge_fusion's kifi library (KinectFission/kifi).
+ *
+ * Every entry point below names the reference interface it replaces.  The
+ * reference has no FFI of its own; its boundary is the C++ class API that
+ * kifi::Pipeline and the unit tests call.  include/kifi_gpu.hpp wraps these
+ * functions in classes with the reference's names and signatures.
+ *
+ * Conventions
+ *  - Plain pointers and sizes; no CUDA or C++ types in signatures.  A
+ *    `stream` argument or field is a cudaStream_t passed as void*.
+ *  - Matrices are 16 floats in kifi's util::float4x4 memory order: four
+ *    columns of four floats (KinectFission/kifi/util/math.h:59-61), so a
+ *    kifi float4x4 can be passed by address.
+ *  - Volumes hold sorted 30-bit linear voxel keys, key = z<<20 | y<<10 | x
+ *    (util::pack, math.h:442-445), and per voxel a (distance-sum, weight)
+ *    pair of floats (kifi::Voxel, Voxel.h:9-21).
+ *  - Every call returns a kifi_status; nothing throws across the ABI.  The
+ *    reference signals misuse only through assert(); here misuse returns
+ *    KIFI_ERR_INVALID_ARGUMENT.
+ *  - Threading: a volume (or ICP context) is not safe for concurrent calls;
+ *    different handles are independent.  All device work of a handle runs on
+ *    its own CUDA stream.
+ */
+#ifndef KIFI_GPU_H
+#define KIFI_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define KIFI_API __attribute__((visibility("default")))
+#else
+#define KIFI_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum kifi_status {
+    KIFI_OK = 0,
+    KIFI_ERR_INVALID_ARGUMENT = 1,
+    KIFI_ERR_OUT_OF_MEMORY = 2,
+    KIFI_ERR_CUDA = 3,
+    KIFI_ERR_CAPACITY = 4,     /* an output buffer or volume capacity is too small */
+    KIFI_ERR_TIMEOUT = 5,      /* a bounded device-side wait gave up */
+    KIFI_ERR_UNSUPPORTED = 6,
+    KIFI_ERR_NO_DEVICE = 7,
+    KIFI_ERR_IO = 8,
+    KIFI_ERR_FORMAT = 9,
+    KIFI_ERR_END_OF_STREAM = 10
+} kifi_status;
+
+/* Replaces kifi::DepthSensorParams (KinectFission/kifi/DepthSensorParams.h:23-52):
+ * resolution, focal length and principal point in pixels, and the sensible
+ * depth range in metres (used only by EyeToClipRH, DepthSensorParams.cpp:47-63). */
+typedef struct kifi_camera {
+    int width, height;
+    float fx, fy;
+    float cx, cy;
+    float znear_m, zfar_m;
+} kifi_camera;
+
+/* Replaces the arguments of kifi::Volume::Volume(int resolution,
+ * float sideLength, float truncationMargin) (KinectFission/kifi/Volume.h:15,
+ * Volume.cpp:12-37).  resolution: power of two in [2, 1024].  The volume is a
+ * cube of side_length_m centred at the world origin (Volume.cpp:63-71). */
+typedef struct kifi_volume_desc {
+    int resolution;
+    float side_length_m;
+    float truncation_m;
+    size_t initial_capacity; /* voxels to reserve up front; 0 = library default */
+    int device;              /* CUDA device ordinal */
+    void* stream;            /* cudaStream_t to run on, or NULL for a library-owned stream */
+} kifi_volume_desc;
+
+typedef struct kifi_volume kifi_volume;
+
+/* Human-readable name of a status code. */
+KIFI_API const char* kifi_status_string(kifi_status status);
+
+/* Detail of the last failing call on this thread (empty when none). */
+KIFI_API const char* kifi_last_error(void);
+
+/* Number of CUDA devices visible to the library (0 when there is none). */
+KIFI_API kifi_status kifi_device_count(int* count);
+
+/* kifi::Volume::Volume (Volume.h:15).  Allocates the device-resident sorted
+ * key/value arrays and the occupancy bitmap of the volume. */
+KIFI_API kifi_status kifi_volume_create(const kifi_volume_desc* desc, kifi_volume** out);
+
+/* kifi::Volume::~Volume */
+KIFI_API kifi_status kifi_volume_destroy(kifi_volume* vol);
+
+/* kifi::Volume::Data().size() (flat_map.h:199-203).  Waits for queued work. */
+KIFI_API kifi_status kifi_volume_size(kifi_volume* vol, size_t* n);
+
+/* Reads the volume back: the sorted keys (flat_map keys_cbegin..keys_cend,
+ * flat_map.h:27-30) and the voxels as (distance-sum, weight) float pairs
+ * (values_cbegin.., flat_map.h:32-37).  On KIFI_ERR_CAPACITY *n holds the
+ * size needed.  Waits for queued work. */
+KIFI_API kifi_status kifi_volume_export(kifi_volume* vol, uint32_t* keys, float* values, size_t capacity,
+                               size_t* n);
+
+/* kifi::util::flat_map::insert (flat_map.h:164-197) on the volume's map:
+ * the set union of the resident voxels with `keys` (sorted, unique), where
+ * resident voxels keep their value.  values may be NULL for Voxel() = (0,0),
+ * as Integrator::Integrate inserts (Integrator.cpp:60-63). */
+KIFI_API kifi_status kifi_volume_insert(kifi_volume* vol, const uint32_t* keys, const float* values,
+                               size_t n);
+
+/* kifi::util::flat_map::clear (flat_map.h:157-162) */
+KIFI_API kifi_status kifi_volume_clear(kifi_volume* vol);
+
+/* Grows the device capacity to at least `capacity` voxels (no reference
+ * counterpart: flat_map grows its std::vectors implicitly). */
+KIFI_API kifi_status kifi_volume_reserve(kifi_volume* vol, size_t capacity);
+
+/* Waits for the volume's stream and reports any error raised on the device
+ * by asynchronous calls since the last sync. */
+KIFI_API kifi_status kifi_volume_sync(kifi_volume* vol);
+
+/* The cudaStream_t (as void*) the volume's device work runs on. */
+KIFI_API void* kifi_volume_stream(kifi_volume* vol);
+
+/* kifi::Integrator::Integrate(Volume&, vector2d<float> const& frame,
+ * DepthSensorParams const&, float4x4 const& worldToEye)
+ * (KinectFission/kifi/Integrator.h:19-26, Integrator.cpp:26-71): splat the
+ * frame's pixels to voxel keys, dilate them by {0,1}^3, merge them into the
+ * resident volume and update the TSDF of every resident voxel.
+ * depth_m: width*height floats, row-major, metres, 0 = no measurement.
+ * Synchronous: returns when the volume is updated. */
+KIFI_API kifi_status kifi_integrate_f32(kifi_volume* vol, const float* depth_m, const kifi_camera* cam,
+                               const float world_to_eye[16]);
+
+/* Same, from 16-bit millimetre texels converted exactly as
+ * kifi::DepthStream::NextFrame does (value * 0.001f, DepthStream.cpp:81-92). */
+KIFI_API kifi_status kifi_integrate_u16(kifi_volume* vol, const uint16_t* depth_mm, const kifi_camera* cam,
+                               const float world_to_eye[16]);
+
+/* Same, with the frame already in device memory (float metres, or uint16
+ * millimetres when depth_is_u16 != 0).  Asynchronous: only enqueues work on
+ * the volume's stream; errors surface at kifi_volume_sync. */
+KIFI_API kifi_status kifi_integrate_device(kifi_volume* vol, const void* depth_dev, int depth_is_u16,
+                                  const kifi_camera* cam, const float world_to_eye[16]);
+
+/* kifi::Mesher::Mesh (KinectFission/kifi/Mesher.h:17-18, Mesher.cpp:14-45):
+ * sparse marching cubes over the resident voxels.
+ * with_indices = 0: Mesh(volume, verts) -- vertices only, in the reference's
+ *   generation order; indices is not written.
+ * with_indices = 1: Mesh(volume, verts, indices) -- vertices ordered by
+ *   their edge id, triangle indices in generation order.
+ * verts receives 3 floats per vertex.  When a capacity is too small the call
+ * returns KIFI_ERR_CAPACITY with the required counts in *n_verts/*n_indices
+ * and writes nothing. */
+KIFI_API kifi_status kifi_mesh(kifi_volume* vol, int with_indices, float* verts, size_t vert_capacity,
+                      uint32_t* indices, size_t index_capacity, size_t* n_verts,
+                      size_t* n_indices);
+
+/* kifi::util::radix_sort(T* first, T* last, void* scratch)
+ * (KinectFission/kifi/util/algorithm.h:63-91) on the GPU: stable LSD sort of
+ * n 32-bit keys held in host memory, in place. */
+KIFI_API kifi_status kifi_radix_sort_u32(uint32_t* keys, size_t n);
+
+/* kifi::util::radix_sort(keys, keys_last, values, scratch)
+ * (algorithm.h:93-134): stable sort of 32-bit keys carrying 32-bit values. */
+KIFI_API kifi_status kifi_radix_sort_pairs_u32(uint32_t* keys, uint32_t* values, size_t n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KIFI_GPU_H */

@@ -1,0 +1,91 @@
+"""ctypes binding of libkifi_gpu.so (include/kifi_gpu.h).
+
+Loading fails loudly when the library has not been built: there is no CPU
+fallback for any entry point.
+"""
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libkifi_gpu.so")
+
+KIFI_OK = 0
+STATUS_NAMES = {
+    0: "KIFI_OK", 1: "KIFI_ERR_INVALID_ARGUMENT", 2: "KIFI_ERR_OUT_OF_MEMORY", 3: "KIFI_ERR_CUDA",
+    4: "KIFI_ERR_CAPACITY", 5: "KIFI_ERR_TIMEOUT", 6: "KIFI_ERR_UNSUPPORTED",
+    7: "KIFI_ERR_NO_DEVICE", 8: "KIFI_ERR_IO", 9: "KIFI_ERR_FORMAT", 10: "KIFI_ERR_END_OF_STREAM",
+}
+
+
+class KifiError(RuntimeError):
+    def __init__(self, status, detail=""):
+        self.status = status
+        super().__init__("%s (%d): %s" % (STATUS_NAMES.get(status, "?"), status, detail))
+
+
+class Camera(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("fx", C.c_float), ("fy", C.c_float),
+                ("cx", C.c_float), ("cy", C.c_float), ("znear_m", C.c_float),
+                ("zfar_m", C.c_float)]
+
+
+class VolumeDesc(C.Structure):
+    _fields_ = [("resolution", C.c_int), ("side_length_m", C.c_float),
+                ("truncation_m", C.c_float), ("initial_capacity", C.c_size_t),
+                ("device", C.c_int), ("stream", C.c_void_p)]
+
+
+# name -> (restype, argtypes); every exported symbol of include/kifi_gpu.h
+SIGNATURES = {
+    "kifi_status_string": (C.c_char_p, [C.c_int]),
+    "kifi_last_error": (C.c_char_p, []),
+    "kifi_device_count": (C.c_int, [C.POINTER(C.c_int)]),
+    "kifi_volume_create": (C.c_int, [C.POINTER(VolumeDesc), C.POINTER(C.c_void_p)]),
+    "kifi_volume_destroy": (C.c_int, [C.c_void_p]),
+    "kifi_volume_size": (C.c_int, [C.c_void_p, C.POINTER(C.c_size_t)]),
+    "kifi_volume_export": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t,
+                                     C.POINTER(C.c_size_t)]),
+    "kifi_volume_insert": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t]),
+    "kifi_volume_clear": (C.c_int, [C.c_void_p]),
+    "kifi_volume_reserve": (C.c_int, [C.c_void_p, C.c_size_t]),
+    "kifi_volume_sync": (C.c_int, [C.c_void_p]),
+    "kifi_volume_stream": (C.c_void_p, [C.c_void_p]),
+    "kifi_integrate_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(Camera), C.c_void_p]),
+    "kifi_integrate_u16": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(Camera), C.c_void_p]),
+    "kifi_integrate_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.POINTER(Camera),
+                                        C.c_void_p]),
+    "kifi_mesh": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t,
+                            C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
+    "kifi_radix_sort_u32": (C.c_int, [C.c_void_p, C.c_size_t]),
+    "kifi_radix_sort_pairs_u32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+}
+
+_lib = None
+
+
+def load():
+    """The loaded library; raises OSError when it is missing."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise OSError("libkifi_gpu.so is not built (%s); run "
+                          "`python -m merge_fusion_gb300.build`" % LIB_PATH)
+        lib = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(lib, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def check(status, what=""):
+    if status != KIFI_OK:
+        detail = load().kifi_last_error().decode(errors="replace")
+        raise KifiError(status, (what + ": " if what else "") + detail)
+
+
+def device_count():
+    n = C.c_int(0)
+    check(load().kifi_device_count(C.byref(n)))
+    return n.value

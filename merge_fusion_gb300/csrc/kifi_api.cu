@@ -1,0 +1,569 @@
+// kifi_api.cu -- the C ABI of libkifi_gpu.so (include/kifi_gpu.h): volume
+// handles, device memory and stream management, and the host side of
+// Integrator::Integrate, flat_map::insert, Mesher::Mesh and
+// util::radix_sort.  Host code only; every computation runs in the kernels
+// of kifi_integrate.cu, kifi_sort.cu and kifi_mesh.cu.
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "kifi_internal.h"
+
+using namespace kifi;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+kifi_status fail(kifi_status s, const char* what) {
+    g_last_error = what;
+    return s;
+}
+
+kifi_status cuda_fail(cudaError_t e, const char* what) {
+    g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    if (e == cudaErrorMemoryAllocation) return KIFI_ERR_OUT_OF_MEMORY;
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return KIFI_ERR_NO_DEVICE;
+    return KIFI_ERR_CUDA;
+}
+
+#define KIFI_CUDA(call)                                   \
+    do {                                                  \
+        cudaError_t kifi_e_ = (call);                     \
+        if (kifi_e_ != cudaSuccess) return cuda_fail(kifi_e_, #call); \
+    } while (0)
+
+constexpr size_t kPad = 64;  // slack elements behind every device array
+
+bool is_pow2(int x) { return x > 0 && !(x & (x - 1)); }
+
+bool camera_ok(const kifi_camera* c) {
+    return c && c->width > 0 && c->height > 0 && c->fx != 0.0f && c->fy != 0.0f &&
+           (size_t)c->width * c->height <= (size_t)1 << 26;
+}
+
+kifi_status launch_shape(int device, LaunchShape* ls) {
+    int sms = 0;
+    KIFI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    ls->sms = sms;
+    ls->sort_ctas = sms * 4;
+    ls->merge_ctas = sms * 4;
+    ls->splat_ctas = sms * 4;
+    return KIFI_OK;
+}
+
+}  // namespace
+
+struct kifi_volume {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    Geom g{};
+    DeviceCtl* ctl = nullptr;       // device
+    DeviceCtl* ctl_host = nullptr;  // pinned mirror for read-backs
+    VolumeBuffers vb{};
+    SortScratch ss{};
+    MeshScratch ms{};
+    LaunchShape ls{};
+    void* depth_dev = nullptr;
+    size_t depth_dev_bytes = 0;
+    void* depth_pinned = nullptr;
+    size_t depth_pinned_bytes = 0;
+    size_t n_upper = 0;  // upper bound of the resident count of queued work
+    float* mesh_verts = nullptr;
+    size_t mesh_verts_cap = 0;
+    uint32_t* mesh_idx = nullptr;
+    size_t mesh_idx_cap = 0;
+};
+
+namespace {
+
+void free_volume_buffers(VolumeBuffers& vb) {
+    for (int i = 0; i < 2; ++i) {
+        cudaFree(vb.keys[i]);
+        cudaFree(vb.vals[i]);
+        vb.keys[i] = nullptr;
+        vb.vals[i] = nullptr;
+    }
+}
+
+// Reads the device control block (waits for the stream).
+kifi_status read_ctl(kifi_volume* v) {
+    KIFI_CUDA(cudaMemcpyAsync(v->ctl_host, v->ctl, sizeof(DeviceCtl), cudaMemcpyDeviceToHost,
+                              v->stream));
+    KIFI_CUDA(cudaStreamSynchronize(v->stream));
+    v->n_upper = (size_t)v->ctl_host->n[v->ctl_host->cur];
+    return KIFI_OK;
+}
+
+// Turns device-raised status bits into a status code and clears them.
+kifi_status take_device_status(kifi_volume* v) {
+    unsigned int st = v->ctl_host->status;
+    if (!st) return KIFI_OK;
+    KIFI_CUDA(cudaMemsetAsync(&v->ctl->status, 0, sizeof(unsigned int), v->stream));
+    KIFI_CUDA(cudaStreamSynchronize(v->stream));
+    if (st & KIFI_DEV_ERR_TIMEOUT) return fail(KIFI_ERR_TIMEOUT, "a bounded device wait gave up");
+    return fail(KIFI_ERR_CAPACITY, "volume capacity exceeded on the device");
+}
+
+kifi_status grow_volume(kifi_volume* v, size_t need) {
+    if (need <= v->vb.cap) return KIFI_OK;
+    kifi_status s = read_ctl(v);
+    if (s) return s;
+    size_t cap = v->vb.cap * 2;
+    if (cap < need) cap = need;
+    const unsigned int cur = v->ctl_host->cur;
+    const size_t n = (size_t)v->ctl_host->n[cur];
+    VolumeBuffers nb = v->vb;
+    for (int i = 0; i < 2; ++i) {
+        nb.keys[i] = nullptr;
+        nb.vals[i] = nullptr;
+    }
+    for (int i = 0; i < 2; ++i) {
+        cudaError_t e1 = cudaMalloc(&nb.keys[i], (cap + kPad) * sizeof(uint32_t));
+        cudaError_t e2 = e1 ? e1 : cudaMalloc(&nb.vals[i], (cap + kPad) * sizeof(float2));
+        if (e1 || e2) {
+            free_volume_buffers(nb);
+            return cuda_fail(e1 ? e1 : e2, "growing the volume");
+        }
+    }
+    KIFI_CUDA(cudaMemcpyAsync(nb.keys[cur], v->vb.keys[cur], n * sizeof(uint32_t),
+                              cudaMemcpyDeviceToDevice, v->stream));
+    KIFI_CUDA(cudaMemcpyAsync(nb.vals[cur], v->vb.vals[cur], n * sizeof(float2),
+                              cudaMemcpyDeviceToDevice, v->stream));
+    KIFI_CUDA(cudaStreamSynchronize(v->stream));
+    free_volume_buffers(v->vb);
+    v->vb.keys[0] = nb.keys[0];
+    v->vb.keys[1] = nb.keys[1];
+    v->vb.vals[0] = nb.vals[0];
+    v->vb.vals[1] = nb.vals[1];
+    v->vb.cap = cap;
+    return KIFI_OK;
+}
+
+// Room for `n_new` keys new to the volume per call (8 per pixel for frames).
+kifi_status reserve_new(kifi_volume* v, size_t n_new) {
+    if (n_new <= v->vb.new_cap) return KIFI_OK;
+    KIFI_CUDA(cudaStreamSynchronize(v->stream));
+    cudaFree(v->vb.new_keys);
+    cudaFree(v->vb.new_idx);
+    v->vb.new_keys = v->vb.new_idx = nullptr;
+    v->vb.new_cap = 0;
+    sort_scratch_free(&v->ss);
+    KIFI_CUDA(cudaMalloc(&v->vb.new_keys, (n_new + kPad) * sizeof(uint32_t)));
+    KIFI_CUDA(cudaMalloc(&v->vb.new_idx, (n_new + kPad) * sizeof(uint32_t)));
+    KIFI_CUDA(sort_scratch_alloc(&v->ss, n_new));
+    v->vb.new_cap = n_new;
+    return KIFI_OK;
+}
+
+kifi_status reserve_depth(kifi_volume* v, size_t bytes) {
+    if (bytes > v->depth_dev_bytes) {
+        KIFI_CUDA(cudaStreamSynchronize(v->stream));
+        cudaFree(v->depth_dev);
+        v->depth_dev = nullptr;
+        v->depth_dev_bytes = 0;
+        KIFI_CUDA(cudaMalloc(&v->depth_dev, bytes));
+        v->depth_dev_bytes = bytes;
+    }
+    return KIFI_OK;
+}
+
+kifi_status frame_prologue(kifi_volume* v, const kifi_camera* cam) {
+    const size_t P = (size_t)cam->width * cam->height;
+    kifi_status s = reserve_new(v, 8 * P);
+    if (s) return s;
+    if (v->n_upper + 8 * P > v->vb.cap) {
+        if ((s = read_ctl(v))) return s;
+        if (v->n_upper + 8 * P > v->vb.cap && (s = grow_volume(v, v->n_upper + 8 * P))) return s;
+    }
+    return KIFI_OK;
+}
+
+Mat4 load_mat(const float* m) {
+    Mat4 r;
+    std::memcpy(r.m, m, 64);
+    return r;
+}
+
+// Host frame -> device: straight from page-locked memory, else staged
+// through the volume's pinned buffer.
+kifi_status upload_depth(kifi_volume* v, const void* src, size_t bytes) {
+    kifi_status s = reserve_depth(v, bytes);
+    if (s) return s;
+    cudaPointerAttributes attr;
+    bool pinned = cudaPointerGetAttributes(&attr, src) == cudaSuccess &&
+                  (attr.type == cudaMemoryTypeHost);
+    cudaGetLastError();
+    if (!pinned) {
+        if (bytes > v->depth_pinned_bytes) {
+            KIFI_CUDA(cudaStreamSynchronize(v->stream));
+            cudaFreeHost(v->depth_pinned);
+            v->depth_pinned = nullptr;
+            v->depth_pinned_bytes = 0;
+            KIFI_CUDA(cudaMallocHost(&v->depth_pinned, bytes));
+            v->depth_pinned_bytes = bytes;
+        } else {
+            // the previous frame's copy out of the staging buffer must be done
+            KIFI_CUDA(cudaStreamSynchronize(v->stream));
+        }
+        std::memcpy(v->depth_pinned, src, bytes);
+        src = v->depth_pinned;
+    }
+    KIFI_CUDA(cudaMemcpyAsync(v->depth_dev, src, bytes, cudaMemcpyHostToDevice, v->stream));
+    return KIFI_OK;
+}
+
+kifi_status integrate_sync(kifi_volume* v, const void* host_depth, bool u16,
+                           const kifi_camera* cam, const float* w2e) {
+    if (!v || !host_depth || !camera_ok(cam) || !w2e)
+        return fail(KIFI_ERR_INVALID_ARGUMENT, "integrate: bad argument");
+    KIFI_CUDA(cudaSetDevice(v->device));
+    kifi_status s = frame_prologue(v, cam);
+    if (s) return s;
+    const size_t bytes = (size_t)cam->width * cam->height * (u16 ? 2 : 4);
+    if ((s = upload_depth(v, host_depth, bytes))) return s;
+    KIFI_CUDA(integrate_enqueue(v->ctl, v->g, v->vb, v->ss, v->depth_dev, u16, nullptr, *cam,
+                                load_mat(w2e), v->ls, v->stream));
+    if ((s = read_ctl(v))) return s;
+    return take_device_status(v);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* kifi_status_string(kifi_status s) {
+    switch (s) {
+        case KIFI_OK: return "ok";
+        case KIFI_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case KIFI_ERR_OUT_OF_MEMORY: return "out of memory";
+        case KIFI_ERR_CUDA: return "CUDA error";
+        case KIFI_ERR_CAPACITY: return "capacity exceeded";
+        case KIFI_ERR_TIMEOUT: return "device wait timed out";
+        case KIFI_ERR_UNSUPPORTED: return "unsupported";
+        case KIFI_ERR_NO_DEVICE: return "no CUDA device";
+        case KIFI_ERR_IO: return "I/O error";
+        case KIFI_ERR_FORMAT: return "bad file format";
+        case KIFI_ERR_END_OF_STREAM: return "end of stream";
+    }
+    return "unknown status";
+}
+
+const char* kifi_last_error(void) { return g_last_error.c_str(); }
+
+kifi_status kifi_device_count(int* count) {
+    if (!count) return fail(KIFI_ERR_INVALID_ARGUMENT, "null count");
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        n = 0;
+    }
+    *count = n;
+    return KIFI_OK;
+}
+
+kifi_status kifi_volume_create(const kifi_volume_desc* d, kifi_volume** out) {
+    if (!d || !out) return fail(KIFI_ERR_INVALID_ARGUMENT, "null argument");
+    *out = nullptr;
+    // Volume.cpp:22-26
+    if (!(d->resolution >= 2 && d->resolution <= 1024 && is_pow2(d->resolution)))
+        return fail(KIFI_ERR_INVALID_ARGUMENT, "resolution must be a power of two in [2, 1024]");
+    if (!(d->side_length_m > 0.0f) || !(d->truncation_m > 0.0f))
+        return fail(KIFI_ERR_INVALID_ARGUMENT, "side length and truncation must be > 0");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(KIFI_ERR_NO_DEVICE, "no CUDA device");
+    }
+    if (d->device < 0 || d->device >= ndev) return fail(KIFI_ERR_INVALID_ARGUMENT, "bad device");
+    kifi_volume* v = new (std::nothrow) kifi_volume();
+    if (!v) return fail(KIFI_ERR_OUT_OF_MEMORY, "host allocation");
+    v->device = d->device;
+    kifi_status s = KIFI_OK;
+    auto bail = [&](kifi_status st) {
+        kifi_volume_destroy(v);
+        return st;
+    };
+    if (cudaSetDevice(v->device) != cudaSuccess) return bail(cuda_fail(cudaGetLastError(), "cudaSetDevice"));
+    if (d->stream) {
+        v->stream = (cudaStream_t)d->stream;
+    } else {
+        cudaError_t e = cudaStreamCreateWithFlags(&v->stream, cudaStreamNonBlocking);
+        if (e) return bail(cuda_fail(e, "cudaStreamCreate"));
+        v->own_stream = true;
+    }
+    v->g = make_geom(d->resolution, d->side_length_m, d->truncation_m);
+    if ((s = launch_shape(v->device, &v->ls))) return bail(s);
+    cudaError_t e;
+    if ((e = cudaMalloc(&v->ctl, sizeof(DeviceCtl)))) return bail(cuda_fail(e, "control block"));
+    if ((e = cudaMemset(v->ctl, 0, sizeof(DeviceCtl)))) return bail(cuda_fail(e, "control block"));
+    if ((e = cudaMallocHost(&v->ctl_host, sizeof(DeviceCtl)))) return bail(cuda_fail(e, "pinned"));
+    std::memset(v->ctl_host, 0, sizeof(DeviceCtl));
+    const size_t r = (size_t)d->resolution;
+    v->vb.bitmap_words = (r * r * r + 31) / 32;
+    if ((e = cudaMalloc(&v->vb.bitmap, v->vb.bitmap_words * 4))) return bail(cuda_fail(e, "bitmap"));
+    if ((e = cudaMemset(v->vb.bitmap, 0, v->vb.bitmap_words * 4))) return bail(cuda_fail(e, "bitmap"));
+    size_t cap = d->initial_capacity;
+    if (cap == 0) cap = r * r * r < ((size_t)1 << 22) ? r * r * r : ((size_t)1 << 22);
+    for (int i = 0; i < 2; ++i) {
+        if ((e = cudaMalloc(&v->vb.keys[i], (cap + kPad) * sizeof(uint32_t))))
+            return bail(cuda_fail(e, "volume keys"));
+        if ((e = cudaMalloc(&v->vb.vals[i], (cap + kPad) * sizeof(float2))))
+            return bail(cuda_fail(e, "volume values"));
+    }
+    v->vb.cap = cap;
+    if ((s = reserve_new(v, 8 * 640 * 480))) return bail(s);
+    *out = v;
+    return KIFI_OK;
+}
+
+kifi_status kifi_volume_destroy(kifi_volume* v) {
+    if (!v) return KIFI_OK;
+    cudaSetDevice(v->device);
+    if (v->stream) cudaStreamSynchronize(v->stream);
+    free_volume_buffers(v->vb);
+    cudaFree(v->vb.bitmap);
+    cudaFree(v->vb.new_keys);
+    cudaFree(v->vb.new_idx);
+    sort_scratch_free(&v->ss);
+    mesh_scratch_free(&v->ms);
+    cudaFree(v->ctl);
+    cudaFreeHost(v->ctl_host);
+    cudaFree(v->depth_dev);
+    cudaFreeHost(v->depth_pinned);
+    cudaFree(v->mesh_verts);
+    cudaFree(v->mesh_idx);
+    if (v->own_stream && v->stream) cudaStreamDestroy(v->stream);
+    delete v;
+    return KIFI_OK;
+}
+
+kifi_status kifi_volume_sync(kifi_volume* v) {
+    if (!v) return fail(KIFI_ERR_INVALID_ARGUMENT, "null volume");
+    KIFI_CUDA(cudaSetDevice(v->device));
+    kifi_status s = read_ctl(v);
+    if (s) return s;
+    return take_device_status(v);
+}
+
+void* kifi_volume_stream(kifi_volume* v) { return v ? (void*)v->stream : nullptr; }
+
+kifi_status kifi_volume_size(kifi_volume* v, size_t* n) {
+    if (!v || !n) return fail(KIFI_ERR_INVALID_ARGUMENT, "null argument");
+    kifi_status s = kifi_volume_sync(v);
+    *n = v->n_upper;
+    return s;
+}
+
+kifi_status kifi_volume_export(kifi_volume* v, uint32_t* keys, float* values, size_t capacity,
+                               size_t* n) {
+    if (!v || !n) return fail(KIFI_ERR_INVALID_ARGUMENT, "null argument");
+    kifi_status s = kifi_volume_sync(v);
+    if (s) return s;
+    const size_t cnt = v->n_upper;
+    *n = cnt;
+    if (cnt > capacity) return fail(KIFI_ERR_CAPACITY, "export buffer too small");
+    if (cnt == 0) return KIFI_OK;
+    const unsigned int cur = v->ctl_host->cur;
+    if (keys)
+        KIFI_CUDA(cudaMemcpyAsync(keys, v->vb.keys[cur], cnt * 4, cudaMemcpyDeviceToHost, v->stream));
+    if (values)
+        KIFI_CUDA(cudaMemcpyAsync(values, v->vb.vals[cur], cnt * 8, cudaMemcpyDeviceToHost, v->stream));
+    KIFI_CUDA(cudaStreamSynchronize(v->stream));
+    return KIFI_OK;
+}
+
+kifi_status kifi_volume_clear(kifi_volume* v) {
+    if (!v) return fail(KIFI_ERR_INVALID_ARGUMENT, "null volume");
+    KIFI_CUDA(cudaSetDevice(v->device));
+    KIFI_CUDA(cudaMemsetAsync(v->vb.bitmap, 0, v->vb.bitmap_words * 4, v->stream));
+    KIFI_CUDA(cudaMemsetAsync(v->ctl, 0, sizeof(DeviceCtl), v->stream));
+    KIFI_CUDA(cudaStreamSynchronize(v->stream));
+    v->n_upper = 0;
+    return KIFI_OK;
+}
+
+kifi_status kifi_volume_reserve(kifi_volume* v, size_t capacity) {
+    if (!v) return fail(KIFI_ERR_INVALID_ARGUMENT, "null volume");
+    KIFI_CUDA(cudaSetDevice(v->device));
+    return grow_volume(v, capacity);
+}
+
+kifi_status kifi_volume_insert(kifi_volume* v, const uint32_t* keys, const float* values, size_t n) {
+    if (!v || (n && !keys)) return fail(KIFI_ERR_INVALID_ARGUMENT, "null argument");
+    if (n == 0) return KIFI_OK;
+    if (n >= ((size_t)1 << 30)) return fail(KIFI_ERR_INVALID_ARGUMENT, "too many keys");
+    const uint32_t res = (uint32_t)v->g.res;
+    for (size_t i = 0; i < n; ++i) {
+        const uint32_t k = keys[i];
+        if (k >> 30 || key_x(k) >= res || key_y(k) >= res || key_z(k) >= res)
+            return fail(KIFI_ERR_INVALID_ARGUMENT, "key outside the volume");
+        if (i && keys[i - 1] >= k) return fail(KIFI_ERR_INVALID_ARGUMENT, "keys not sorted/unique");
+    }
+    KIFI_CUDA(cudaSetDevice(v->device));
+    kifi_status s = reserve_new(v, n);
+    if (s) return s;
+    if ((s = read_ctl(v))) return s;
+    if ((s = grow_volume(v, v->n_upper + n))) return s;
+    uint32_t* dk = nullptr;
+    float2* dv = nullptr;
+    unsigned int* dn = nullptr;
+    auto cleanup = [&]() {
+        cudaFree(dk);
+        cudaFree(dv);
+        cudaFree(dn);
+    };
+    cudaError_t e = cudaMalloc(&dk, n * 4);
+    if (!e && values) e = cudaMalloc(&dv, n * 8);
+    if (!e) e = cudaMalloc(&dn, 4);
+    if (e) {
+        cleanup();
+        return cuda_fail(e, "insert staging");
+    }
+    const unsigned int n32 = (unsigned int)n;
+    e = cudaMemcpyAsync(dk, keys, n * 4, cudaMemcpyHostToDevice, v->stream);
+    if (!e && values) e = cudaMemcpyAsync(dv, values, n * 8, cudaMemcpyHostToDevice, v->stream);
+    if (!e) e = cudaMemcpyAsync(dn, &n32, 4, cudaMemcpyHostToDevice, v->stream);
+    if (!e) e = insert_filter_enqueue(v->ctl, v->g, v->vb, dk, dn, v->ls, v->stream);
+    if (!e) e = sort_u32(v->vb.new_keys, v->vb.new_idx, &v->ctl->n_new, v->ss, &v->ctl->status,
+                         v->ls.sort_ctas, v->stream);
+    if (!e) e = insert_merge_enqueue(v->ctl, v->g, v->vb, dv, v->ls, v->stream);
+    if (!e) e = cudaStreamSynchronize(v->stream);
+    cleanup();
+    if (e) return cuda_fail(e, "insert");
+    if ((s = read_ctl(v))) return s;
+    return take_device_status(v);
+}
+
+kifi_status kifi_integrate_f32(kifi_volume* v, const float* depth_m, const kifi_camera* cam,
+                               const float world_to_eye[16]) {
+    return integrate_sync(v, depth_m, false, cam, world_to_eye);
+}
+
+kifi_status kifi_integrate_u16(kifi_volume* v, const uint16_t* depth_mm, const kifi_camera* cam,
+                               const float world_to_eye[16]) {
+    return integrate_sync(v, depth_mm, true, cam, world_to_eye);
+}
+
+kifi_status kifi_integrate_device(kifi_volume* v, const void* depth_dev, int depth_is_u16,
+                                  const kifi_camera* cam, const float world_to_eye[16]) {
+    if (!v || !depth_dev || !camera_ok(cam) || !world_to_eye)
+        return fail(KIFI_ERR_INVALID_ARGUMENT, "integrate: bad argument");
+    KIFI_CUDA(cudaSetDevice(v->device));
+    kifi_status s = frame_prologue(v, cam);
+    if (s) return s;
+    KIFI_CUDA(integrate_enqueue(v->ctl, v->g, v->vb, v->ss, depth_dev, depth_is_u16 != 0, nullptr,
+                                *cam, load_mat(world_to_eye), v->ls, v->stream));
+    v->n_upper += 8 * (size_t)cam->width * cam->height;
+    return KIFI_OK;
+}
+
+kifi_status kifi_mesh(kifi_volume* v, int with_indices, float* verts, size_t vert_capacity,
+                      uint32_t* indices, size_t index_capacity, size_t* n_verts,
+                      size_t* n_indices) {
+    if (!v || !n_verts || !n_indices) return fail(KIFI_ERR_INVALID_ARGUMENT, "null argument");
+    *n_verts = *n_indices = 0;
+    kifi_status s = kifi_volume_sync(v);
+    if (s) return s;
+    const size_t n = v->n_upper;
+    if (n < 2) return KIFI_OK;  // the reference's loop starts at size-2
+    if (n >= ((size_t)1 << 28)) return fail(KIFI_ERR_UNSUPPORTED, "mesh of more than 2^28 voxels");
+    const unsigned int cur = v->ctl_host->cur;
+    KIFI_CUDA(mesh_scratch_reserve(&v->ms, n));
+    KIFI_CUDA(mesh_count_enqueue(v->vb.keys[cur], v->vb.vals[cur], n, with_indices ? 1 : 0, v->ms,
+                                 v->ls.sms, v->stream));
+    MeshCounts mc;
+    KIFI_CUDA(cudaMemcpyAsync(&mc, v->ms.counts, sizeof mc, cudaMemcpyDeviceToHost, v->stream));
+    KIFI_CUDA(cudaStreamSynchronize(v->stream));
+    const size_t nv = (size_t)mc.n_verts, ni = with_indices ? (size_t)mc.n_idx : 0;
+    *n_verts = nv;
+    *n_indices = ni;
+    if (nv > vert_capacity || ni > index_capacity || (nv && !verts) || (ni && !indices))
+        return fail(KIFI_ERR_CAPACITY, "mesh output buffers too small");
+    if (nv > v->mesh_verts_cap) {
+        cudaFree(v->mesh_verts);
+        v->mesh_verts = nullptr;
+        v->mesh_verts_cap = 0;
+        KIFI_CUDA(cudaMalloc(&v->mesh_verts, (nv + kPad) * 12));
+        v->mesh_verts_cap = nv;
+    }
+    if (ni > v->mesh_idx_cap) {
+        cudaFree(v->mesh_idx);
+        v->mesh_idx = nullptr;
+        v->mesh_idx_cap = 0;
+        KIFI_CUDA(cudaMalloc(&v->mesh_idx, (ni + kPad) * 4));
+        v->mesh_idx_cap = ni;
+    }
+    KIFI_CUDA(mesh_emit_enqueue(v->g, v->vb.keys[cur], v->vb.vals[cur], n, with_indices ? 1 : 0,
+                                v->ms, nv, ni, 0xffffffffu, v->mesh_verts, v->mesh_idx, v->ls.sms,
+                                v->stream));
+    if (with_indices) {
+        unsigned int missing = 0;
+        KIFI_CUDA(cudaMemcpyAsync(&missing, &v->ms.counts->missing_min, 4, cudaMemcpyDeviceToHost,
+                                  v->stream));
+        KIFI_CUDA(cudaStreamSynchronize(v->stream));
+        if (missing != 0xffffffffu)
+            KIFI_CUDA(mesh_emit_enqueue(v->g, v->vb.keys[cur], v->vb.vals[cur], n, 1, v->ms, nv, ni,
+                                        missing, v->mesh_verts, v->mesh_idx, v->ls.sms, v->stream));
+    }
+    if (nv)
+        KIFI_CUDA(cudaMemcpyAsync(verts, v->mesh_verts, nv * 12, cudaMemcpyDeviceToHost, v->stream));
+    if (ni)
+        KIFI_CUDA(cudaMemcpyAsync(indices, v->mesh_idx, ni * 4, cudaMemcpyDeviceToHost, v->stream));
+    KIFI_CUDA(cudaStreamSynchronize(v->stream));
+    return KIFI_OK;
+}
+
+static kifi_status radix_sort_host(uint32_t* keys, uint32_t* values, size_t n) {
+    if (n == 0) return KIFI_OK;
+    if (!keys) return fail(KIFI_ERR_INVALID_ARGUMENT, "null keys");
+    if (n >= ((size_t)1 << 30)) return fail(KIFI_ERR_UNSUPPORTED, "sort of 2^30 or more keys");
+    int dev = 0;
+    KIFI_CUDA(cudaGetDevice(&dev));
+    LaunchShape ls;
+    kifi_status s = launch_shape(dev, &ls);
+    if (s) return s;
+    cudaStream_t st;
+    KIFI_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    SortScratch ss;
+    uint32_t *dk = nullptr, *dv = nullptr;
+    unsigned int *dn = nullptr, *dstatus = nullptr;
+    const unsigned int n32 = (unsigned int)n;
+    unsigned int status = 0;
+    cudaError_t e = sort_scratch_alloc(&ss, n);
+    if (!e) e = cudaMalloc(&dk, (n + kPad) * 4);
+    if (!e && values) e = cudaMalloc(&dv, (n + kPad) * 4);
+    if (!e) e = cudaMalloc(&dn, 4);
+    if (!e) e = cudaMalloc(&dstatus, 4);
+    if (!e) e = cudaMemsetAsync(dstatus, 0, 4, st);
+    if (!e) e = cudaMemcpyAsync(dk, keys, n * 4, cudaMemcpyHostToDevice, st);
+    if (!e && values) e = cudaMemcpyAsync(dv, values, n * 4, cudaMemcpyHostToDevice, st);
+    if (!e) e = cudaMemcpyAsync(dn, &n32, 4, cudaMemcpyHostToDevice, st);
+    if (!e) e = sort_u32(dk, dv, dn, ss, dstatus, ls.sort_ctas, st);
+    if (!e) e = cudaMemcpyAsync(keys, dk, n * 4, cudaMemcpyDeviceToHost, st);
+    if (!e && values) e = cudaMemcpyAsync(values, dv, n * 4, cudaMemcpyDeviceToHost, st);
+    if (!e) e = cudaMemcpyAsync(&status, dstatus, 4, cudaMemcpyDeviceToHost, st);
+    if (!e) e = cudaStreamSynchronize(st);
+    sort_scratch_free(&ss);
+    cudaFree(dk);
+    cudaFree(dv);
+    cudaFree(dn);
+    cudaFree(dstatus);
+    cudaStreamDestroy(st);
+    if (e) return cuda_fail(e, "radix sort");
+    if (status) return fail(KIFI_ERR_TIMEOUT, "radix sort look-back gave up");
+    return KIFI_OK;
+}
+
+kifi_status kifi_radix_sort_u32(uint32_t* keys, size_t n) { return radix_sort_host(keys, nullptr, n); }
+
+kifi_status kifi_radix_sort_pairs_u32(uint32_t* keys, uint32_t* values, size_t n) {
+    if (n && !values) return fail(KIFI_ERR_INVALID_ARGUMENT, "null values");
+    return radix_sort_host(keys, values, n);
+}
+
+}  // extern "C"

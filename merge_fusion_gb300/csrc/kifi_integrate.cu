@@ -1,0 +1,414 @@
+// kifi_integrate.cu -- one Integrator::Integrate (KinectFission/kifi/
+// Integrator.cpp:26-71) on sm_103a, as four kernels on one stream:
+//
+//  k_frame_setup   derive eyeToWorld / worldToClip and the projection
+//                  constants from the pose (Integrator.cpp:41-42), reset the
+//                  per-frame counters.
+//  k_splat_emit    DepthMap2PointCloud (Integrator.cpp:76-183) fused with
+//                  ExpandChunks (:186-250) and the de-duplication of
+//                  std::unique (:50-55): every valid pixel's voxel key and its
+//                  seven {0,1}^3 neighbours are tested against the volume's
+//                  occupancy bitmap (one bit per voxel of the res^3 grid); the
+//                  thread whose atomicOr flips a bit owns that key and appends
+//                  it to the frame's list of keys NEW to the volume.
+//  (radix sort)    the new keys are sorted (kifi_sort.cu).
+//  k_merge_update  flat_map::insert (flat_map.h:164-197) as a merge-path
+//                  merge of the sorted resident keys with the sorted new keys
+//                  into the other half of the ping-pong buffers, fused with
+//                  UpdateVoxels (Integrator.cpp:253-358): every output voxel is
+//                  projected into the frame and its (distance-sum, weight)
+//                  updated before it is written -- one read and one write of
+//                  the volume per frame.
+//
+// Set semantics.  The reference dilates the sorted unique splat keys U with
+// three set unions: S2 = U + {0, dz, dy, dy+dz}, then the +x step adds s+1
+// for every s in S2 except the largest (its loop never emits the successor of
+// the last key).  Keys never carry between fields because a valid splat has
+// every coordinate <= res-2 (Integrator.cpp:151-154), so the dilated set is
+// exactly U + {0,1}^3 minus the single key max(U) + pack(1,1,1).  The emit
+// kernel records that key (an atomicMax over the splats); if it turns out to
+// be new it is the largest new key, and k_merge_update drops it and clears
+// its bit.
+//
+// Resident voxels keep their value in the union, new ones start at
+// Voxel() = (0, 0) (Integrator.cpp:60-63).  The update visits the first
+// n/4*4 voxels of the merged volume only -- the reference's 4-wide loop drops
+// the n%4 tail (Integrator.cpp:269) -- which the merge kernel can apply
+// directly because the merged size n = N0 + #new is known before it runs.
+#include "kifi_internal.h"
+
+namespace kifi {
+namespace {
+
+constexpr int kEmitThreads = 256;
+constexpr int kMergeThreads = 256;
+constexpr int kMergeItems = 8;                            // outputs per thread
+constexpr int kMergeTile = kMergeThreads * kMergeItems;   // 2048 outputs per tile
+constexpr uint16_t kFromB = 0x8000u;
+
+__global__ void k_frame_setup(DeviceCtl* ctl, kifi_camera cam, Mat4 w2e, int res) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        ctl->fc = make_frame_const(cam, w2e, res);
+        ctl->n_new = 0u;
+        ctl->excluded_key = 0u;
+    }
+}
+
+__device__ __forceinline__ float load_depth(const void* depth, size_t i, bool u16) {
+    // DepthStream::NextFrame converts 16-bit millimetres with value * 0.001f
+    // (DepthStream.cpp:89-90)
+    if (u16) return fmul((float)(unsigned int)__ldg((const unsigned short*)depth + i), 0.001f);
+    return __ldg((const float*)depth + i);
+}
+
+__device__ __forceinline__ size_t bit_index(uint32_t key, int res) {
+    return (size_t)key_x(key) + (size_t)res * ((size_t)key_y(key) + (size_t)res * key_z(key));
+}
+
+// Splat of one pixel (Integrator.cpp:121-154 for one SSE lane).
+__device__ __forceinline__ bool splat_pixel(const FrameConst& fc, const Geom& g, int u, int v,
+                                            float d, uint32_t* key) {
+    if (!(d > 0.0f)) return false;
+    float p[4];
+    // point = (u, -v, -1, 0) + 0; point * flInv + ppOverFl; point * depth + (0,0,0,1)
+    p[0] = fadd(fmul(fadd(fmul((float)u, fc.fl_inv_x), fc.pp_x), d), 0.0f);
+    p[1] = fadd(fmul(fadd(fmul(fadd(0.0f, -(float)v), fc.fl_inv_y), fc.pp_y), d), 0.0f);
+    p[2] = fadd(fmul(fadd(fmul(-1.0f, 1.0f), 0.0f), d), 0.0f);
+    p[3] = fadd(fmul(fadd(fmul(0.0f, 1.0f), 0.0f), d), 1.0f);
+    float w[4];
+    mat_vec(fc.eye_to_world.m, p, w);
+    // VoxelIndex(world) - 0.5 (Volume.cpp:90-93); the w lane uses (1, 0)
+    float ix = fsub(fadd(fmul(w[0], g.vlen_inv), g.index_off), 0.5f);
+    float iy = fsub(fadd(fmul(w[1], g.vlen_inv), g.index_off), 0.5f);
+    float iz = fsub(fadd(fmul(w[2], g.vlen_inv), g.index_off), 0.5f);
+    float iw = fsub(fadd(fmul(w[3], 1.0f), 0.0f), 0.5f);
+    const float mx = fc.max_index;
+    if (!(ix >= 0.0f && ix < mx && iy >= 0.0f && iy < mx && iz >= 0.0f && iz < mx && iw >= 0.0f &&
+          iw < mx))
+        return false;
+    *key = pack30((uint32_t)ix, (uint32_t)iy, (uint32_t)iz);
+    return true;
+}
+
+template <bool kU16>
+__global__ void __launch_bounds__(kEmitThreads) k_splat_emit(DeviceCtl* __restrict__ ctl, Geom g,
+                                                             const void* __restrict__ depth,
+                                                             uint32_t* __restrict__ bitmap,
+                                                             uint32_t* __restrict__ new_keys,
+                                                             unsigned int new_cap) {
+    const FrameConst fc = ctl->fc;
+    const int W = fc.width, H = fc.height;
+    const size_t P = (size_t)W * H;
+    const int lane = threadIdx.x & 31;
+    const size_t stride = (size_t)gridDim.x * kEmitThreads;
+    const size_t P_round = (P + 31) / 32 * 32;  // warp-uniform trip count
+    for (size_t i = (size_t)blockIdx.x * kEmitThreads + threadIdx.x; i < P_round; i += stride) {
+        uint32_t key = 0;
+        bool valid = false;
+        if (i < P) {
+            int u = (int)(i % (size_t)W), v = (int)(i / (size_t)W);
+            valid = splat_pixel(fc, g, u, v, load_depth(depth, i, kU16), &key);
+        }
+        // the excluded key of the dilation: max splat + pack(1,1,1)
+        unsigned int ex = __reduce_max_sync(0xffffffffu, valid ? key + pack30(1, 1, 1) : 0u);
+        if (lane == 0 && ex) atomicMax(&ctl->excluded_key, ex);
+        // neighbouring pixels often land in one voxel: one emitter per key
+        unsigned int peers = __match_any_sync(0xffffffffu, valid ? key : 0xffffffffu);
+        bool emitter = valid && (lane == __ffs(peers) - 1);
+#pragma unroll
+        for (int o = 0; o < 8; ++o) {
+            bool mine = false;
+            uint32_t nk = key + pack30(o & 1, (o >> 1) & 1, o >> 2);
+            if (emitter) {
+                size_t b = bit_index(nk, g.res);
+                uint32_t mask = 1u << (b & 31);
+                uint32_t* word = bitmap + (b >> 5);
+                if (!(*(volatile uint32_t*)word & mask)) mine = !(atomicOr(word, mask) & mask);
+            }
+            unsigned int ballot = __ballot_sync(0xffffffffu, mine);
+            if (!ballot) continue;
+            unsigned int base = 0;
+            if (lane == __ffs(ballot) - 1) base = atomicAdd(&ctl->n_new, (unsigned int)__popc(ballot));
+            base = __shfl_sync(0xffffffffu, base, __ffs(ballot) - 1);
+            if (mine) {
+                unsigned int at = base + __popc(ballot & ((1u << lane) - 1u));
+                if (at < new_cap) new_keys[at] = nk;
+                else atomicOr(&ctl->status, KIFI_DEV_ERR_CAPACITY);
+            }
+        }
+    }
+}
+
+// UpdateVoxels for one voxel (Integrator.cpp:273-322 for one SSE lane).
+template <bool kU16>
+__device__ __forceinline__ void update_voxel(uint32_t key, float2& val, const FrameConst& fc,
+                                             const Geom& g, const void* depth) {
+    // VoxelCenter: index * (vlen, vlen, vlen, 1) + (off, off, off, 0)
+    float c[4];
+    c[0] = fadd(fmul((float)key_x(key), g.vlen), g.center_off);
+    c[1] = fadd(fmul((float)key_y(key), g.vlen), g.center_off);
+    c[2] = fadd(fmul((float)key_z(key), g.vlen), g.center_off);
+    c[3] = 1.0f;  // 1 * 1 + 0
+    float cl[4];
+    mat_vec(fc.world_to_clip.m, c, cl);
+    const float w = cl[3];
+    // lane w: (w/w) * 0 + 0 lies in [-FLT_MAX, FLT_MAX) iff w/w is finite,
+    // i.e. iff w is finite and non-zero (w/w is then exactly 1).
+    if (!(isfinite(w) && w != 0.0f)) return;
+    // lane z: (z/w) * 0 + 0 lies in [-1, 1) iff z/w is finite.  With w finite
+    // and non-zero that needs z finite and no overflow of the quotient; the
+    // bounds below rule overflow out without dividing, else divide exactly.
+    const float z = cl[2];
+    if (!isfinite(z)) return;
+    if (!(fabsf(z) <= 1e18f && fabsf(w) >= 1e-18f) && !isfinite(fdiv(z, w))) return;
+    const float u = fadd(fmul(fdiv(cl[0], w), fc.half_w), fc.half_w);
+    const float v = fadd(fmul(fdiv(cl[1], w), fc.half_h), fc.half_h);
+    if (!(u >= 0.0f && u < (float)fc.width && v >= 0.0f && v < (float)fc.height)) return;
+    const size_t px = (uint32_t)u;
+    const size_t py = (size_t)fc.height - (uint32_t)v - 1;
+    const float d = load_depth(depth, py * (size_t)fc.width + px, kU16);
+    const float sd = fsub(d, w);
+    if (d > 0.0f && sd >= -g.trunc) {
+        // Voxel::Update(std::min(signedDist, trunc)) (Voxel.h:53-57)
+        val.x = fadd(val.x, (g.trunc < sd) ? g.trunc : sd);
+        val.y = fadd(val.y, 1.0f);
+    }
+}
+
+// number of A elements among the first d outputs of merge(A, B); A and B
+// are sorted and disjoint.
+__device__ __forceinline__ unsigned long long merge_path(const uint32_t* __restrict__ A,
+                                                         unsigned long long na,
+                                                         const uint32_t* __restrict__ B,
+                                                         unsigned long long nb,
+                                                         unsigned long long d) {
+    unsigned long long lo = d > nb ? d - nb : 0, hi = d < na ? d : na;
+    while (lo < hi) {
+        unsigned long long mid = (lo + hi) >> 1;
+        if (A[mid] < B[d - 1 - mid]) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+struct MergeInputs {
+    const uint32_t* b_keys;   // sorted new keys
+    const uint32_t* b_index;  // optional: b's position in b_vals (inserts)
+    const float2* b_vals;     // optional values of new keys; null = Voxel()
+    const unsigned int* b_count;
+    bool update;              // run UpdateVoxels on the merged volume
+};
+
+template <bool kU16>
+__global__ void __launch_bounds__(kMergeThreads) k_merge_update(DeviceCtl* __restrict__ ctl, Geom g,
+                                                                VolumeBuffers vb, MergeInputs in,
+                                                                const void* __restrict__ depth) {
+    __shared__ uint32_t sA_k[kMergeTile + 8];
+    __shared__ float2 sA_v[kMergeTile + 4];
+    __shared__ uint32_t sB_k[kMergeTile];
+    __shared__ uint16_t sSrc[kMergeTile];
+    __shared__ unsigned long long sSplit[2];
+
+    const unsigned int cur = ctl->cur, out = cur ^ 1u;
+    const unsigned long long N0 = ctl->n[cur];
+    unsigned long long e = *in.b_count;
+    const uint32_t* __restrict__ A = vb.keys[cur];
+    const float2* __restrict__ Av = vb.vals[cur];
+    const uint32_t* __restrict__ B = in.b_keys;
+    const uint32_t excluded = ctl->excluded_key;
+    bool drop = false;
+    if (e > 0 && excluded != 0u && B[e - 1] == excluded) {
+        drop = true;
+        --e;
+    }
+    const unsigned long long N1 = N0 + e;
+    if (N1 > vb.cap) {
+        // no room: leave the volume as it was and take the new keys back out
+        // of the occupancy bitmap; the host grows the buffers and retries.
+        for (unsigned long long i = (unsigned long long)blockIdx.x * kMergeThreads + threadIdx.x;
+             i < e + (drop ? 1 : 0); i += (unsigned long long)gridDim.x * kMergeThreads) {
+            size_t b = bit_index(B[i], g.res);
+            atomicAnd(vb.bitmap + (b >> 5), ~(1u << (b & 31)));
+        }
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&ctl->status, KIFI_DEV_ERR_CAPACITY);
+        return;
+    }
+    if (drop && blockIdx.x == 0 && threadIdx.x == 0) {
+        size_t b = bit_index(excluded, g.res);
+        atomicAnd(vb.bitmap + (b >> 5), ~(1u << (b & 31)));
+    }
+    const FrameConst fc = ctl->fc;
+    const unsigned long long upd_end = in.update ? (N1 / 4 * 4) : 0ull;
+    uint32_t* __restrict__ outK = vb.keys[out];
+    float2* __restrict__ outV = vb.vals[out];
+    const unsigned long long n_tiles = (N1 + kMergeTile - 1) / kMergeTile;
+
+    for (unsigned long long t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+        const unsigned long long d0 = t * kMergeTile;
+        const unsigned long long d1 = (d0 + kMergeTile < N1) ? d0 + kMergeTile : N1;
+        const int len = (int)(d1 - d0);
+        if (threadIdx.x < 2) sSplit[threadIdx.x] = merge_path(A, N0, B, e, threadIdx.x ? d1 : d0);
+        __syncthreads();
+        const unsigned long long a0 = sSplit[0], a1 = sSplit[1];
+        const int na = (int)(a1 - a0), nb = len - na;
+        const unsigned long long b0 = d0 - a0;
+        // stage the A range through shared memory with aligned 16-byte loads
+        const unsigned long long ka = a0 & ~3ull;
+        const int koff = (int)(a0 - ka);
+        for (int i = threadIdx.x * 4; i < koff + na; i += kMergeThreads * 4)
+            *(uint4*)&sA_k[i] = __ldcs((const uint4*)(A + ka + i));
+        const unsigned long long va = a0 & ~1ull;
+        const int voff = (int)(a0 - va);
+        for (int i = threadIdx.x * 2; i < voff + na; i += kMergeThreads * 2)
+            *(float4*)&sA_v[i] = __ldcs((const float4*)(Av + va + i));
+        for (int i = threadIdx.x; i < nb; i += kMergeThreads) sB_k[i] = B[b0 + i];
+        __syncthreads();
+        if (nb > 0) {
+            // per-thread merge path inside the tile, kMergeItems outputs each
+            const int dd = threadIdx.x * kMergeItems;
+            if (dd < len) {
+                int lo = dd > nb ? dd - nb : 0, hi = dd < na ? dd : na;
+                while (lo < hi) {
+                    int mid = (lo + hi) >> 1;
+                    if (sA_k[koff + mid] < sB_k[dd - 1 - mid]) lo = mid + 1;
+                    else hi = mid;
+                }
+                int ia = lo, ib = dd - lo;
+                const int end = dd + kMergeItems < len ? dd + kMergeItems : len;
+                for (int j = dd; j < end; ++j) {
+                    bool takeA = ib >= nb || (ia < na && sA_k[koff + ia] < sB_k[ib]);
+                    sSrc[j] = takeA ? (uint16_t)ia++ : (uint16_t)(kFromB | ib++);
+                }
+            }
+            __syncthreads();
+        }
+        // striped pass: 4 consecutive outputs per thread per round
+        for (int j0 = threadIdx.x * 4; j0 < len; j0 += kMergeThreads * 4) {
+            uint32_t ko[4];
+            float2 vo[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int j = j0 + q;
+                if (j >= len) break;
+                uint32_t key;
+                float2 val;
+                uint16_t src = nb > 0 ? sSrc[j] : (uint16_t)j;
+                if (!(src & kFromB)) {
+                    key = sA_k[koff + src];
+                    val = sA_v[voff + src];
+                } else {
+                    const int ib = src & ~kFromB;
+                    key = sB_k[ib];
+                    if (in.b_vals) val = in.b_vals[in.b_index ? in.b_index[b0 + ib] : b0 + ib];
+                    else val = make_float2(0.0f, 0.0f);
+                }
+                if (d0 + j < upd_end) update_voxel<kU16>(key, val, fc, g, depth);
+                ko[q] = key;
+                vo[q] = val;
+            }
+            if (j0 + 4 <= len) {
+                __stcs((uint4*)(outK + d0 + j0), make_uint4(ko[0], ko[1], ko[2], ko[3]));
+                __stcs((float4*)(outV + d0 + j0), make_float4(vo[0].x, vo[0].y, vo[1].x, vo[1].y));
+                __stcs((float4*)(outV + d0 + j0 + 2), make_float4(vo[2].x, vo[2].y, vo[3].x, vo[3].y));
+            } else {
+                for (int q = 0; q < 4 && j0 + q < len; ++q) {
+                    outK[d0 + j0 + q] = ko[q];
+                    outV[d0 + j0 + q] = vo[q];
+                }
+            }
+        }
+        __syncthreads();
+    }
+    // the last CTA to finish publishes the new volume
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        unsigned int prev = atomicAdd(&ctl->tile_counter[7], 1u);
+        if (prev == gridDim.x - 1) {
+            ctl->n[out] = N1;
+            ctl->cur = out;
+            ctl->tile_counter[7] = 0u;
+            ctl->frames += 1ull;
+            __threadfence();
+        }
+    }
+}
+
+// inserts: keep keys not yet in the volume (flat_map::insert keeps resident
+// values), appending (key, position) pairs for the sort.
+__global__ void k_insert_filter(DeviceCtl* ctl, Geom g, uint32_t* bitmap, const uint32_t* keys,
+                                const unsigned int* n_ptr, uint32_t* out_keys, uint32_t* out_idx) {
+    const unsigned int n = *n_ptr;
+    const int lane = threadIdx.x & 31;
+    const unsigned int n_round = (n + 31) / 32 * 32;
+    for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_round;
+         i += gridDim.x * blockDim.x) {
+        bool mine = false;
+        uint32_t k = 0;
+        if (i < n) {
+            k = keys[i];
+            size_t b = bit_index(k, g.res);
+            uint32_t mask = 1u << (b & 31);
+            mine = !(atomicOr(bitmap + (b >> 5), mask) & mask);
+        }
+        unsigned int ballot = __ballot_sync(0xffffffffu, mine);
+        if (!ballot) continue;
+        unsigned int base = 0;
+        if (lane == __ffs(ballot) - 1) base = atomicAdd(&ctl->n_new, (unsigned int)__popc(ballot));
+        base = __shfl_sync(0xffffffffu, base, __ffs(ballot) - 1);
+        if (mine) {
+            unsigned int at = base + __popc(ballot & ((1u << lane) - 1u));
+            out_keys[at] = k;
+            out_idx[at] = i;
+        }
+    }
+}
+
+__global__ void k_reset_new(DeviceCtl* ctl) {
+    ctl->n_new = 0u;
+    ctl->excluded_key = 0u;
+}
+
+}  // namespace
+
+cudaError_t integrate_enqueue(DeviceCtl* ctl, const Geom& g, VolumeBuffers& vb, SortScratch& ss,
+                              const void* depth_dev, bool depth_u16, float* /*depth_f32_dev*/,
+                              const kifi_camera& cam, const Mat4& world_to_eye,
+                              const LaunchShape& ls, cudaStream_t st) {
+    k_frame_setup<<<1, 32, 0, st>>>(ctl, cam, world_to_eye, g.res);
+    const unsigned int new_cap = (unsigned int)vb.new_cap;
+    if (depth_u16)
+        k_splat_emit<true><<<ls.splat_ctas, kEmitThreads, 0, st>>>(ctl, g, depth_dev, vb.bitmap,
+                                                                   vb.new_keys, new_cap);
+    else
+        k_splat_emit<false><<<ls.splat_ctas, kEmitThreads, 0, st>>>(ctl, g, depth_dev, vb.bitmap,
+                                                                    vb.new_keys, new_cap);
+    cudaError_t e = sort_u32(vb.new_keys, nullptr, &ctl->n_new, ss, &ctl->status, ls.sort_ctas, st);
+    if (e != cudaSuccess) return e;
+    MergeInputs in{vb.new_keys, nullptr, nullptr, &ctl->n_new, true};
+    if (depth_u16)
+        k_merge_update<true><<<ls.merge_ctas, kMergeThreads, 0, st>>>(ctl, g, vb, in, depth_dev);
+    else
+        k_merge_update<false><<<ls.merge_ctas, kMergeThreads, 0, st>>>(ctl, g, vb, in, depth_dev);
+    return cudaGetLastError();
+}
+
+cudaError_t insert_filter_enqueue(DeviceCtl* ctl, const Geom& g, VolumeBuffers& vb,
+                                  const uint32_t* keys_dev, const unsigned int* n_dev,
+                                  const LaunchShape& ls, cudaStream_t st) {
+    k_reset_new<<<1, 1, 0, st>>>(ctl);
+    k_insert_filter<<<ls.splat_ctas, 256, 0, st>>>(ctl, g, vb.bitmap, keys_dev, n_dev, vb.new_keys,
+                                                   vb.new_idx);
+    return cudaGetLastError();
+}
+
+// Merge of the filtered, (key, index)-sorted insert keys; values are taken
+// from vals_dev[index], or Voxel() when vals_dev is null.
+cudaError_t insert_merge_enqueue(DeviceCtl* ctl, const Geom& g, VolumeBuffers& vb,
+                                 const float2* vals_dev, const LaunchShape& ls, cudaStream_t st) {
+    MergeInputs in{vb.new_keys, vb.new_idx, vals_dev, &ctl->n_new, false};
+    k_merge_update<false><<<ls.merge_ctas, kMergeThreads, 0, st>>>(ctl, g, vb, in, nullptr);
+    return cudaGetLastError();
+}
+
+}  // namespace kifi

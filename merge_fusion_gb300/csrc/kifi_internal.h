@@ -1,0 +1,94 @@
+// kifi_internal.h -- declarations shared between the library's translation
+// units (not part of the public ABI).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "kifi_common.cuh"
+
+namespace kifi {
+
+// ------------------------------------------------------------ radix sort
+struct SortScratch {
+    unsigned int* hist = nullptr;           // [4][256] digit counts
+    unsigned int* tile_counter = nullptr;   // [4] dynamic tile ids per pass
+    unsigned long long* epoch = nullptr;    // look-back generation tag
+    unsigned long long* lookback = nullptr; // [4][max_tiles][256]
+    uint32_t* alt_keys = nullptr;           // ping-pong buffers, max_n (+pad)
+    uint32_t* alt_vals = nullptr;
+    unsigned int* status = nullptr;         // where timeouts are reported
+    size_t max_tiles = 0, max_n = 0;
+};
+
+size_t sort_max_tiles(size_t max_n);
+cudaError_t sort_scratch_alloc(SortScratch* s, size_t max_n);
+void sort_scratch_free(SortScratch* s);
+cudaError_t sort_u32(uint32_t* keys, uint32_t* vals, const unsigned int* n_dev, SortScratch& s,
+                     unsigned int* status, int grid_ctas, cudaStream_t st);
+
+// ------------------------------------------------------------- integrate
+struct VolumeBuffers {
+    uint32_t* keys[2] = {nullptr, nullptr};
+    float2* vals[2] = {nullptr, nullptr};
+    size_t cap = 0;                 // voxels per buffer (arrays hold cap + pad)
+    uint32_t* bitmap = nullptr;     // res^3 occupancy bits
+    size_t bitmap_words = 0;
+    uint32_t* new_keys = nullptr;   // keys new to the volume in this frame
+    uint32_t* new_idx = nullptr;    // insert path: source position of each new key
+    size_t new_cap = 0;
+};
+
+struct LaunchShape {
+    int sms = 0;          // multiprocessors of the device
+    int sort_ctas = 0;    // persistent CTAs of the sort passes
+    int merge_ctas = 0;   // persistent CTAs of the merge/update kernel
+    int splat_ctas = 0;
+};
+
+// Enqueues one Integrator::Integrate on `st`.  depth_dev holds the frame
+// (float metres, or uint16 millimetres when depth_u16).
+cudaError_t integrate_enqueue(DeviceCtl* ctl, const Geom& g, VolumeBuffers& vb, SortScratch& ss,
+                              const void* depth_dev, bool depth_u16, float* depth_f32_dev,
+                              const kifi_camera& cam, const Mat4& world_to_eye,
+                              const LaunchShape& ls, cudaStream_t st);
+
+// flat_map::insert of n sorted unique device keys: filter out resident keys
+// (their values win) and collect (key, index) of the rest in new_keys /
+// new_idx; the caller sorts those pairs and then merges.
+cudaError_t insert_filter_enqueue(DeviceCtl* ctl, const Geom& g, VolumeBuffers& vb,
+                                  const uint32_t* keys_dev, const unsigned int* n_dev,
+                                  const LaunchShape& ls, cudaStream_t st);
+cudaError_t insert_merge_enqueue(DeviceCtl* ctl, const Geom& g, VolumeBuffers& vb,
+                                 const float2* vals_dev, const LaunchShape& ls, cudaStream_t st);
+
+// ---------------------------------------------------------------- mesher
+struct MeshCounts {
+    unsigned long long n_verts;
+    unsigned long long n_idx;
+    unsigned int missing_min;  // smallest triangle edge id without a vertex (or ~0u)
+    unsigned int pad;
+};
+
+struct MeshScratch {
+    unsigned int* vflags = nullptr;        // per voxel: vertex axes | index count<<8 | case<<16
+    unsigned long long* vscan = nullptr;   // per voxel packed (index count << 32 | vertex count)
+    unsigned long long* tscan = nullptr;   // exclusive scan of vscan
+    unsigned long long* block_sums = nullptr;
+    unsigned int* rows = nullptr;          // start index of each (z, y) key row
+    MeshCounts* counts = nullptr;
+    size_t cap = 0;
+};
+
+cudaError_t mesh_scratch_reserve(MeshScratch* m, size_t n);
+void mesh_scratch_free(MeshScratch* m);
+cudaError_t mesh_count_enqueue(const uint32_t* keys, const float2* vals, size_t n,
+                               int with_indices, MeshScratch& ms, int sms, cudaStream_t st);
+cudaError_t mesh_emit_enqueue(const Geom& g, const uint32_t* keys, const float2* vals, size_t n,
+                              int with_indices, MeshScratch& ms, unsigned long long n_verts,
+                              unsigned long long n_idx, unsigned int missing_bound, float* verts_dev,
+                              uint32_t* idx_dev, int sms, cudaStream_t st);
+
+}  // namespace kifi

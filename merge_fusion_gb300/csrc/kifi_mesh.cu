@@ -1,0 +1,403 @@
+// kifi_mesh.cu -- sparse marching cubes over the sorted voxel keys on
+// sm_103a: kifi::Mesher::Mesh (KinectFission/kifi/Mesher.cpp:14-45) and
+// Mesher::Generate<bool> (:85-229).
+//
+// The reference walks the sorted volume backwards (voxels n-2 .. 0) with
+// three neighbour pointers (+y, +z, +yz) that start at n-2 and only move down.
+// After the walk for voxel i each pointer sits at
+//     min(n-2, upper_bound(keys, key_i + delta) - 1),
+// a closed form that depends on voxel i alone, so every voxel is handled by
+// its own thread:
+//
+//  k_row_directory  start index of every (y, z) key row (key >> 10); a
+//                   neighbour search then only scans one row of keys.
+//  k_mesh_classify  per voxel i in [0, n-2] with weight > 0: which of its
+//                   +x/+y/+z edges carry a vertex (Mesher.cpp:140-168) and,
+//                   for Mesh(verts, indices), the cube's marching-cubes case
+//                   and triangle count (:172-226).
+//  (scan)           one exclusive scan of the packed (vertex, index) counts
+//                   in ascending voxel order.
+//  k_mesh_emit      writes the vertices and the triangle indices.
+//
+// Output order equals the reference's:
+//  * Mesh(verts): vertices in generation order -- voxels descending, axes
+//    x, y, z -- so voxel i's vertices start after those of all voxels j > i.
+//  * Mesh(verts, indices): vertices sorted by id 3*key+axis (Mesher.cpp:25-26),
+//    which is ascending voxel order; triangles in generation order (voxels
+//    descending, table order), each index mapped to its vertex's rank
+//    (:28-44).  That mapping walk stops at the first index id that has no
+//    vertex; every index id at or above it keeps its raw id.  k_mesh_emit
+//    reproduces this: it records the smallest missing id, and when one exists
+//    the host runs it again with that bound.
+#include "kifi_internal.h"
+#include "mc_table.cuh"
+
+namespace kifi {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr unsigned int kRows = 1u << 20;  // (z, y) rows of 10-bit fields
+
+__device__ __forceinline__ unsigned long long lower_bound_u32(const uint32_t* __restrict__ k,
+                                                              unsigned long long n, uint32_t t) {
+    unsigned long long lo = 0, hi = n;
+    while (lo < hi) {
+        unsigned long long mid = (lo + hi) >> 1;
+        if (k[mid] < t) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// row_start[r] = first index whose key >> 10 >= r, for r in [0, 2^20]
+__global__ void k_row_directory(const uint32_t* __restrict__ keys, unsigned long long n,
+                                unsigned int* __restrict__ row_start) {
+    for (unsigned int r = blockIdx.x * blockDim.x + threadIdx.x; r <= kRows;
+         r += gridDim.x * blockDim.x)
+        row_start[r] = (unsigned int)lower_bound_u32(keys, n, r << 10);
+}
+
+// upper_bound(keys, t) using the row directory: keys of t's row lie in
+// [row_start[r], row_start[r+1]) sorted by x.
+__device__ __forceinline__ unsigned int upper_bound_row(const uint32_t* __restrict__ keys,
+                                                        const unsigned int* __restrict__ rs,
+                                                        uint32_t t, unsigned int n) {
+    const unsigned int r = t >> 10;
+    // a neighbour of a voxel on the last z slice lies past every key
+    if (r >= kRows) return n;
+    unsigned int lo = rs[r], hi = rs[r + 1];
+    while (lo < hi) {
+        unsigned int mid = (lo + hi) >> 1;
+        if (keys[mid] <= t) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// neighbour pointer position after the reference's walk (see file comment)
+__device__ __forceinline__ unsigned int walk_ptr(const uint32_t* keys, const unsigned int* rs,
+                                                 uint32_t t, unsigned int n) {
+    unsigned int p = upper_bound_row(keys, rs, t, n) - 1u;
+    return p < n - 2 ? p : n - 2;
+}
+
+__device__ __forceinline__ float vdist(float2 v) { return fdiv(v.x, v.y); }  // Voxel::Distance
+
+struct Cube {
+    unsigned int idx[8];  // voxel index of each corner (valid where found)
+    float2 val[8];        // Voxel() = (0,0) where not found
+};
+
+// Corner lookups of Mesher.cpp:122-132 (corners 0,1,2,4) and, when
+// kTris, :174-181 (corners 3,5,6,7).  Corner c = (c&1, c>>1&1, c>>2) in the
+// reference's voxels[] numbering: self, +x, +y, +xy, +z, +xz, +yz, +xyz.
+template <bool kTris>
+__device__ __forceinline__ void load_cube(const uint32_t* __restrict__ keys,
+                                          const float2* __restrict__ vals,
+                                          const unsigned int* __restrict__ rs, unsigned int n,
+                                          unsigned int i, Cube& c) {
+    const uint32_t key = keys[i];
+    const float2 zero = make_float2(0.0f, 0.0f);
+    c.idx[0] = i;
+    c.val[0] = vals[i];
+    c.idx[1] = i + 1;
+    c.val[1] = keys[i + 1] == key + pack30(1, 0, 0) ? vals[i + 1] : zero;
+    const unsigned int iTop = walk_ptr(keys, rs, key + pack30(0, 1, 0), n);
+    const unsigned int iFront = walk_ptr(keys, rs, key + pack30(0, 0, 1), n);
+    c.idx[2] = iTop;
+    c.val[2] = keys[iTop] == key + pack30(0, 1, 0) ? vals[iTop] : zero;
+    c.idx[4] = iFront;
+    c.val[4] = keys[iFront] == key + pack30(0, 0, 1) ? vals[iFront] : zero;
+    if (kTris) {
+        const unsigned int iFT = walk_ptr(keys, rs, key + pack30(0, 1, 1), n);
+        c.idx[6] = iFT;
+        c.val[6] = keys[iFT] == key + pack30(0, 1, 1) ? vals[iFT] : zero;
+        c.idx[3] = iTop + 1;
+        c.val[3] = keys[iTop + 1] == key + pack30(1, 1, 0) ? vals[iTop + 1] : zero;
+        c.idx[5] = iFront + 1;
+        c.val[5] = keys[iFront + 1] == key + pack30(1, 0, 1) ? vals[iFront + 1] : zero;
+        c.idx[7] = iFT + 1;
+        c.val[7] = keys[iFT + 1] == key + pack30(1, 1, 1) ? vals[iFT + 1] : zero;
+    }
+}
+
+// vertex axes of a voxel: bit a set when edge +a carries a vertex
+__device__ __forceinline__ unsigned int vertex_axes(const Cube& c) {
+    const float dself = vdist(c.val[0]);
+    unsigned int axes = 0;
+    const int nb[3] = {1, 2, 4};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float2 o = c.val[nb[a]];
+        if (o.y > 0.0f && fmul(dself, vdist(o)) <= 0.0f) axes |= 1u << a;
+    }
+    return axes;
+}
+
+// marching-cubes case with the reference's corner bit order (Mesher.cpp:191-199)
+__device__ __forceinline__ int cube_case(const Cube& c) {
+    return (vdist(c.val[0]) < 0.0f) << 2 | (vdist(c.val[1]) < 0.0f) << 3 |
+           (vdist(c.val[2]) < 0.0f) << 6 | (vdist(c.val[3]) < 0.0f) << 7 |
+           (vdist(c.val[4]) < 0.0f) << 1 | (vdist(c.val[5]) < 0.0f) << 0 |
+           (vdist(c.val[6]) < 0.0f) << 5 | (vdist(c.val[7]) < 0.0f) << 4;
+}
+
+// flags per voxel: bits 0-2 vertex axes, bits 8-15 index count, 16-23 case
+template <bool kTris>
+__global__ void __launch_bounds__(kThreads) k_mesh_classify(const uint32_t* __restrict__ keys,
+                                                            const float2* __restrict__ vals,
+                                                            const unsigned int* __restrict__ rs,
+                                                            unsigned int n,
+                                                            unsigned int* __restrict__ flags,
+                                                            unsigned long long* __restrict__ counts) {
+    for (unsigned int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+        unsigned int f = 0, nv = 0, ni = 0;
+        if (i + 1 < n && vals[i].y != 0.0f) {
+            Cube c;
+            load_cube<kTris>(keys, vals, rs, n, i, c);
+            const unsigned int axes = vertex_axes(c);
+            nv = __popc(axes);
+            f = axes;
+            if (kTris) {
+                bool skip = false;
+#pragma unroll
+                for (int q = 1; q < 8; ++q) skip |= (0.0f == c.val[q].y);
+                if (!skip) {
+                    const int lut = cube_case(c);
+                    ni = 3u * mc_tri_count(lut);
+                    f |= ni << 8 | (unsigned int)lut << 16;
+                }
+            }
+        }
+        flags[i] = f;
+        counts[i] = (unsigned long long)ni << 32 | nv;
+    }
+}
+
+// edge e of the cube -> (corner, axis), from localToGlobal (Mesher.cpp:206-218)
+__constant__ unsigned char kEdgeCorner[12] = {4, 0, 0, 1, 6, 2, 2, 3, 5, 4, 0, 1};
+__constant__ unsigned char kEdgeAxis[12] = {0, 2, 0, 2, 0, 2, 0, 2, 1, 1, 1, 1};
+
+template <bool kTris>
+__global__ void __launch_bounds__(kThreads) k_mesh_emit(const uint32_t* __restrict__ keys,
+                                                        const float2* __restrict__ vals,
+                                                        const unsigned int* __restrict__ rs,
+                                                        unsigned int n, Geom g,
+                                                        const unsigned int* __restrict__ flags,
+                                                        const unsigned long long* __restrict__ scan,
+                                                        unsigned long long n_verts,
+                                                        unsigned long long n_idx,
+                                                        unsigned int missing_bound,
+                                                        float* __restrict__ verts,
+                                                        uint32_t* __restrict__ idx,
+                                                        unsigned int* __restrict__ missing_min) {
+    for (unsigned int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+        const unsigned int f = flags[i];
+        if (f == 0) continue;
+        Cube c;
+        load_cube<kTris>(keys, vals, rs, n, i, c);
+        const uint32_t key = keys[i];
+        const unsigned long long s = scan[i];
+        const unsigned int vbase = (unsigned int)(s & 0xffffffffu);
+        const unsigned int axes = f & 7u;
+        // vertices (Mesher.cpp:134-168)
+        if (axes) {
+            const unsigned int nv = __popc(axes);
+            const unsigned long long first =
+                kTris ? vbase : n_verts - vbase - nv;  // ascending ids / generation order
+            const float cx = fadd(fmul((float)(int)key_x(key), g.vlen), g.center_off);
+            const float cy = fadd(fmul((float)(int)key_y(key), g.vlen), g.center_off);
+            const float cz = fadd(fmul((float)(int)key_z(key), g.vlen), g.center_off);
+            const float dself = vdist(c.val[0]);
+            const int nb[3] = {1, 2, 4};
+            unsigned int r = 0;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                if (!(axes >> a & 1u)) continue;
+                const float dn = vdist(c.val[nb[a]]);
+                const float t = fmul(fdiv(fabsf(dself), fadd(fabsf(dself), fabsf(dn))), g.vlen);
+                float p[3] = {cx, cy, cz};
+                p[a] = fadd(p[a], t);
+                float* o = verts + 3 * (first + r);
+                o[0] = p[0];
+                o[1] = p[1];
+                o[2] = p[2];
+                ++r;
+            }
+        }
+        if (!kTris) continue;
+        const unsigned int ni = (f >> 8) & 0xffu;
+        if (!ni) continue;
+        const int lut = (int)(f >> 16 & 0xffu);
+        const unsigned int ibase = (unsigned int)(s >> 32);
+        const unsigned long long first = n_idx - ibase - ni;  // generation order
+        unsigned int local_min = 0xffffffffu;
+        for (unsigned int t = 0; t < ni; ++t) {
+            const int e = mc_tri_edge(lut, (int)t);
+            const int corner = kEdgeCorner[e], axis = kEdgeAxis[e];
+            const unsigned int ci = c.idx[corner];
+            const uint32_t id = 3u * keys[ci] + (uint32_t)axis;
+            const unsigned int cf = flags[ci];
+            uint32_t outv;
+            if (cf >> axis & 1u) {
+                outv = (unsigned int)(scan[ci] & 0xffffffffu) + __popc(cf & 7u & ((1u << axis) - 1u));
+            } else {
+                outv = id;
+                local_min = min(local_min, id);
+            }
+            if (id >= missing_bound) outv = id;
+            idx[first + t] = outv;
+        }
+        if (local_min != 0xffffffffu) atomicMin(missing_min, local_min);
+    }
+}
+
+// -------------------------------------------------------- exclusive scan
+// Two-level exclusive scan of packed 64-bit (index count << 32 | vertex
+// count) values; both halves stay below 2^32 for volumes under 2^28 voxels.
+constexpr int kScanItems = 4;
+constexpr int kScanTile = kThreads * kScanItems;
+
+__device__ __forceinline__ unsigned long long block_exclusive_scan(unsigned long long x,
+                                                                   unsigned long long* total) {
+    __shared__ unsigned long long warp_sums[kThreads / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned long long inc = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        unsigned long long y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+    }
+    if (lane == 31) warp_sums[warp] = inc;
+    __syncthreads();
+    unsigned long long before = 0, all = 0;
+#pragma unroll
+    for (int w = 0; w < kThreads / 32; ++w) {
+        if (w < warp) before += warp_sums[w];
+        all += warp_sums[w];
+    }
+    __syncthreads();
+    *total = all;
+    return before + inc - x;
+}
+
+__global__ void __launch_bounds__(kThreads) k_scan_tiles(const unsigned long long* __restrict__ in,
+                                                         unsigned long long* __restrict__ out,
+                                                         unsigned long long* __restrict__ tile_sums,
+                                                         unsigned int n) {
+    const unsigned int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    unsigned long long v[kScanItems], s = 0;
+#pragma unroll
+    for (int q = 0; q < kScanItems; ++q) {
+        v[q] = base + q < n ? in[base + q] : 0ull;
+        s += v[q];
+    }
+    unsigned long long total;
+    unsigned long long run = block_exclusive_scan(s, &total);
+#pragma unroll
+    for (int q = 0; q < kScanItems; ++q) {
+        if (base + q < n) out[base + q] = run;
+        run += v[q];
+    }
+    if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
+}
+
+// single CTA: exclusive scan of the tile sums, total to counts
+__global__ void __launch_bounds__(kThreads) k_scan_sums(unsigned long long* __restrict__ sums,
+                                                        unsigned int n_tiles,
+                                                        MeshCounts* __restrict__ counts) {
+    unsigned long long carry = 0;
+    for (unsigned int b = 0; b < n_tiles; b += kThreads) {
+        const unsigned int i = b + threadIdx.x;
+        unsigned long long x = i < n_tiles ? sums[i] : 0ull, total;
+        unsigned long long ex = block_exclusive_scan(x, &total);
+        if (i < n_tiles) sums[i] = carry + ex;
+        carry += total;
+    }
+    if (threadIdx.x == 0) {
+        counts->n_verts = carry & 0xffffffffull;
+        counts->n_idx = carry >> 32;
+        counts->missing_min = 0xffffffffu;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_scan_add(unsigned long long* __restrict__ out,
+                                                       const unsigned long long* __restrict__ sums,
+                                                       unsigned int n) {
+    const unsigned int base = blockIdx.x * kScanTile;
+    const unsigned long long add = sums[blockIdx.x];
+    for (int q = threadIdx.x; q < kScanTile; q += kThreads)
+        if (base + q < n) out[base + q] += add;
+}
+
+}  // namespace
+
+cudaError_t mesh_scratch_reserve(MeshScratch* m, size_t n) {
+    if (m->cap >= n && m->vflags) return cudaSuccess;
+    mesh_scratch_free(m);
+    size_t cap = n < 1024 ? 1024 : n;
+    cudaError_t e;
+    if ((e = cudaMalloc(&m->vflags, cap * sizeof(unsigned int)))) return e;
+    if ((e = cudaMalloc(&m->vscan, cap * sizeof(unsigned long long)))) return e;
+    if ((e = cudaMalloc(&m->tscan, cap * sizeof(unsigned long long)))) return e;
+    if ((e = cudaMalloc(&m->block_sums, ((cap + kScanTile - 1) / kScanTile + 1) * 8))) return e;
+    if ((e = cudaMalloc(&m->rows, (kRows + 1) * sizeof(unsigned int)))) return e;
+    if ((e = cudaMalloc(&m->counts, sizeof(MeshCounts)))) return e;
+    m->cap = cap;
+    return cudaSuccess;
+}
+
+void mesh_scratch_free(MeshScratch* m) {
+    cudaFree(m->vflags);
+    cudaFree(m->vscan);
+    cudaFree(m->tscan);
+    cudaFree(m->block_sums);
+    cudaFree(m->rows);
+    cudaFree(m->counts);
+    *m = MeshScratch{};
+}
+
+static int grid_for(size_t n, int sms) {
+    size_t b = (n + kThreads - 1) / kThreads;
+    size_t cap = (size_t)sms * 8;
+    return (int)(b < 1 ? 1 : (b > cap ? cap : b));
+}
+
+cudaError_t mesh_count_enqueue(const uint32_t* keys, const float2* vals, size_t n,
+                               int with_indices, MeshScratch& ms, int sms, cudaStream_t st) {
+    // vscan holds the per-voxel packed counts, tscan their exclusive scan
+    unsigned long long* cnt = ms.vscan;
+    unsigned long long* scan = ms.tscan;
+    k_row_directory<<<grid_for(kRows + 1, sms), kThreads, 0, st>>>(keys, n, ms.rows);
+    if (with_indices)
+        k_mesh_classify<true><<<grid_for(n, sms), kThreads, 0, st>>>(keys, vals, ms.rows,
+                                                                      (unsigned int)n, ms.vflags, cnt);
+    else
+        k_mesh_classify<false><<<grid_for(n, sms), kThreads, 0, st>>>(keys, vals, ms.rows,
+                                                                       (unsigned int)n, ms.vflags, cnt);
+    const unsigned int n_tiles = (unsigned int)((n + kScanTile - 1) / kScanTile);
+    k_scan_tiles<<<n_tiles ? n_tiles : 1, kThreads, 0, st>>>(cnt, scan, ms.block_sums,
+                                                             (unsigned int)n);
+    k_scan_sums<<<1, kThreads, 0, st>>>(ms.block_sums, n_tiles ? n_tiles : 1, ms.counts);
+    k_scan_add<<<n_tiles ? n_tiles : 1, kThreads, 0, st>>>(scan, ms.block_sums, (unsigned int)n);
+    return cudaGetLastError();
+}
+
+cudaError_t mesh_emit_enqueue(const Geom& g, const uint32_t* keys, const float2* vals, size_t n,
+                              int with_indices, MeshScratch& ms, unsigned long long n_verts,
+                              unsigned long long n_idx, unsigned int missing_bound, float* verts_dev,
+                              uint32_t* idx_dev, int sms, cudaStream_t st) {
+    const unsigned long long* scan = ms.tscan;
+    unsigned int* mm = &ms.counts->missing_min;
+    if (with_indices)
+        k_mesh_emit<true><<<grid_for(n, sms), kThreads, 0, st>>>(
+            keys, vals, ms.rows, (unsigned int)n, g, ms.vflags, scan, n_verts, n_idx, missing_bound,
+            verts_dev, idx_dev, mm);
+    else
+        k_mesh_emit<false><<<grid_for(n, sms), kThreads, 0, st>>>(
+            keys, vals, ms.rows, (unsigned int)n, g, ms.vflags, scan, n_verts, n_idx, missing_bound,
+            verts_dev, idx_dev, mm);
+    return cudaGetLastError();
+}
+
+}  // namespace kifi

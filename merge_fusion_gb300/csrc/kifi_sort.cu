@@ -1,0 +1,255 @@
+// kifi_sort.cu -- stable LSD radix sort of 32-bit keys (optionally carrying
+// 32-bit values) on sm_103a, the GPU counterpart of kifi::util::radix_sort
+// (KinectFission/kifi/util/algorithm.h:63-134: four stable 8-bit passes,
+// each an exclusive scan of 256 digit counts, numeric.h:78-108).
+//
+// The key count is read from device memory, so a sort can be enqueued
+// behind the kernel that produces the keys without a host round trip and
+// captured in a CUDA graph.
+//
+// Structure (one "onesweep" kernel per digit pass):
+//  * k_sort_prepare: zero the digit histograms and the dynamic tile
+//    counters, bump the look-back generation tag.
+//  * k_sort_histogram: one read of the keys builds all four 256-bin digit
+//    histograms (shared-memory counters, then one global atomic per bin).
+//  * k_sort_pass: persistent CTAs take 2048-key tiles in increasing order
+//    from an atomic counter.  Each warp ranks its keys with
+//    __match_any_sync (a stable rank among lanes holding the same digit),
+//    per-warp digit counts are scanned across warps in shared memory, the
+//    tile's counts are published to a decoupled look-back array and the
+//    tile's global offsets are resolved by walking back over predecessor
+//    tiles.  Keys (and values) are scattered to their final position of the
+//    pass.
+// The look-back words pack {generation:32 | status:2 | count:30}, so the
+// count and its flag are one atomic 64-bit store and stale words of an
+// earlier sort are ignored without clearing.  Every wait on a predecessor is
+// bounded: after kSpinLimit polls the kernel raises KIFI_DEV_ERR_TIMEOUT in
+// the volume's status word and carries on with what it has, so a broken
+// invariant can never hang the GPU.
+#include "kifi_internal.h"
+
+namespace kifi {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kKeysPerThread = 8;
+constexpr int kTile = kThreads * kKeysPerThread;  // 2048
+constexpr int kRadix = 256;
+constexpr unsigned long long kSpinLimit = 1ull << 22;
+
+constexpr unsigned long long kFlagAggregate = 1ull << 30;
+constexpr unsigned long long kFlagInclusive = 2ull << 30;
+constexpr unsigned long long kCountMask = (1ull << 30) - 1;
+
+__global__ void k_sort_prepare(SortScratch s) {
+    for (int i = threadIdx.x; i < 4 * kRadix; i += blockDim.x) s.hist[i] = 0u;
+    if (threadIdx.x < 4) s.tile_counter[threadIdx.x] = 0u;
+    if (threadIdx.x == 0) *s.epoch += 1ull;
+}
+
+__global__ void __launch_bounds__(kThreads) k_sort_histogram(const uint32_t* __restrict__ keys,
+                                                             const unsigned int* __restrict__ n_ptr,
+                                                             SortScratch s) {
+    __shared__ unsigned int h[4][kRadix];
+    for (int i = threadIdx.x; i < 4 * kRadix; i += kThreads) (&h[0][0])[i] = 0u;
+    __syncthreads();
+    const size_t n = min((size_t)*n_ptr, s.max_n);
+    for (size_t i = (size_t)blockIdx.x * kThreads + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * kThreads) {
+        uint32_t k = keys[i];
+        atomicAdd(&h[0][k & 0xffu], 1u);
+        atomicAdd(&h[1][(k >> 8) & 0xffu], 1u);
+        atomicAdd(&h[2][(k >> 16) & 0xffu], 1u);
+        atomicAdd(&h[3][k >> 24], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 4 * kRadix; i += kThreads) {
+        unsigned int c = (&h[0][0])[i];
+        if (c) atomicAdd(&s.hist[i], c);
+    }
+}
+
+__device__ __forceinline__ unsigned int lanemask_lt() {
+    unsigned int m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+__device__ __forceinline__ unsigned long long ld_volatile_u64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_volatile_u64(unsigned long long* p, unsigned long long v) {
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+template <bool kWithValues>
+__global__ void __launch_bounds__(kThreads) k_sort_pass(const uint32_t* __restrict__ keys_in,
+                                                        uint32_t* __restrict__ keys_out,
+                                                        const uint32_t* __restrict__ vals_in,
+                                                        uint32_t* __restrict__ vals_out,
+                                                        const unsigned int* __restrict__ n_ptr,
+                                                        SortScratch s, int pass) {
+    __shared__ unsigned int warp_hist[kWarps][kRadix + 1];  // last column: out-of-range keys
+    __shared__ unsigned int digit_base[kRadix];
+    __shared__ unsigned int pass_offset[kRadix];
+    __shared__ unsigned int tile_id;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned int n = (unsigned int)min((size_t)*n_ptr, s.max_n);
+    const unsigned int n_tiles = (n + kTile - 1) / kTile;
+    const int shift = pass * 8;
+    const unsigned long long gen = (*s.epoch & 0xffffffffull) << 32;
+    unsigned long long* lb = s.lookback + (size_t)pass * s.max_tiles * kRadix;
+
+    // exclusive scan of this pass's global digit histogram (256 entries)
+    {
+        unsigned int c = s.hist[pass * kRadix + threadIdx.x];
+        unsigned int x = c;
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned int y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        __shared__ unsigned int wsum[kWarps];
+        if (lane == 31) wsum[warp] = x;
+        __syncthreads();
+        unsigned int before = 0;
+        for (int w = 0; w < warp; ++w) before += wsum[w];
+        pass_offset[threadIdx.x] = before + x - c;
+    }
+
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) tile_id = atomicAdd(&s.tile_counter[pass], 1u);
+        for (int i = threadIdx.x; i < kWarps * (kRadix + 1); i += kThreads)
+            (&warp_hist[0][0])[i] = 0u;
+        __syncthreads();
+        const unsigned int tile = tile_id;
+        if (tile >= n_tiles) break;
+
+        const unsigned int base = tile * kTile + warp * (32 * kKeysPerThread);
+        uint32_t k[kKeysPerThread], v[kKeysPerThread];
+        unsigned int rank[kKeysPerThread];
+        int dig[kKeysPerThread];
+#pragma unroll
+        for (int j = 0; j < kKeysPerThread; ++j) {
+            unsigned int i = base + j * 32 + lane;
+            bool ok = i < n;
+            k[j] = ok ? keys_in[i] : 0u;
+            if (kWithValues) v[j] = ok ? vals_in[i] : 0u;
+            dig[j] = ok ? (int)((k[j] >> shift) & 0xffu) : kRadix;
+        }
+        // stable warp-local ranks: lanes with equal digits, in (j, lane) order
+#pragma unroll
+        for (int j = 0; j < kKeysPerThread; ++j) {
+            unsigned int peers = __match_any_sync(0xffffffffu, dig[j]);
+            unsigned int before = warp_hist[warp][dig[j]];
+            rank[j] = before + __popc(peers & lanemask_lt());
+            __syncwarp();
+            if (lane == __ffs(peers) - 1) warp_hist[warp][dig[j]] = before + __popc(peers);
+            __syncwarp();
+        }
+        __syncthreads();
+        // per digit: counts across warps -> exclusive prefix over warps
+        const int d = threadIdx.x;
+        unsigned int tile_count = 0;
+        for (int w = 0; w < kWarps; ++w) {
+            unsigned int c = warp_hist[w][d];
+            warp_hist[w][d] = tile_count;
+            tile_count += c;
+        }
+        // decoupled look-back for digit d
+        unsigned long long* my = lb + (size_t)tile * kRadix + d;
+        if (tile == 0) {
+            st_volatile_u64(my, gen | kFlagInclusive | tile_count);
+            digit_base[d] = pass_offset[d];
+        } else {
+            st_volatile_u64(my, gen | kFlagAggregate | tile_count);
+            unsigned int excl = 0;
+            int t = (int)tile - 1;
+            unsigned long long spins = 0;
+            while (t >= 0) {
+                unsigned long long w = ld_volatile_u64(lb + (size_t)t * kRadix + d);
+                if ((w & 0xffffffff00000000ull) != gen || (w & (3ull << 30)) == 0) {
+                    if (++spins > kSpinLimit) {
+                        atomicOr(s.status, KIFI_DEV_ERR_TIMEOUT);
+                        break;
+                    }
+                    continue;
+                }
+                excl += (unsigned int)(w & kCountMask);
+                if (w & kFlagInclusive) break;
+                --t;
+            }
+            st_volatile_u64(my, gen | kFlagInclusive | ((excl + tile_count) & kCountMask));
+            digit_base[d] = pass_offset[d] + excl;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < kKeysPerThread; ++j) {
+            if (dig[j] == kRadix) continue;
+            unsigned int pos = digit_base[dig[j]] + warp_hist[warp][dig[j]] + rank[j];
+            if (pos >= n) {  // only reachable after a timed-out look-back
+                atomicOr(s.status, KIFI_DEV_ERR_TIMEOUT);
+                continue;
+            }
+            keys_out[pos] = k[j];
+            if (kWithValues) vals_out[pos] = v[j];
+        }
+    }
+}
+
+}  // namespace
+
+size_t sort_max_tiles(size_t max_n) { return (max_n + kTile - 1) / kTile + 1; }
+
+cudaError_t sort_scratch_alloc(SortScratch* s, size_t max_n) {
+    *s = SortScratch{};
+    s->max_tiles = sort_max_tiles(max_n);
+    s->max_n = max_n;
+    cudaError_t e;
+    if ((e = cudaMalloc(&s->hist, 4 * kRadix * sizeof(unsigned int) + 64))) return e;
+    if ((e = cudaMalloc(&s->tile_counter, 8 * sizeof(unsigned int)))) return e;
+    if ((e = cudaMalloc(&s->epoch, sizeof(unsigned long long)))) return e;
+    if ((e = cudaMemset(s->epoch, 0, sizeof(unsigned long long)))) return e;
+    size_t lb = 4 * s->max_tiles * kRadix * sizeof(unsigned long long);
+    if ((e = cudaMalloc(&s->lookback, lb))) return e;
+    if ((e = cudaMemset(s->lookback, 0, lb))) return e;
+    if ((e = cudaMalloc(&s->alt_keys, (max_n + 64) * sizeof(uint32_t)))) return e;
+    if ((e = cudaMalloc(&s->alt_vals, (max_n + 64) * sizeof(uint32_t)))) return e;
+    return cudaSuccess;
+}
+
+void sort_scratch_free(SortScratch* s) {
+    cudaFree(s->hist);
+    cudaFree(s->tile_counter);
+    cudaFree(s->epoch);
+    cudaFree(s->lookback);
+    cudaFree(s->alt_keys);
+    cudaFree(s->alt_vals);
+    *s = SortScratch{};
+}
+
+// Sorts keys[0..*n_dev) (and vals, when not null) in place.  *n_dev must not
+// exceed s->max_n.  Four passes leave the result in the caller's buffers.
+cudaError_t sort_u32(uint32_t* keys, uint32_t* vals, const unsigned int* n_dev, SortScratch& s,
+                     unsigned int* status, int grid_ctas, cudaStream_t st) {
+    s.status = status;
+    k_sort_prepare<<<1, 256, 0, st>>>(s);
+    k_sort_histogram<<<grid_ctas, kThreads, 0, st>>>(keys, n_dev, s);
+    uint32_t *ki = keys, *ko = s.alt_keys, *vi = vals, *vo = s.alt_vals;
+    for (int pass = 0; pass < 4; ++pass) {
+        if (vals)
+            k_sort_pass<true><<<grid_ctas, kThreads, 0, st>>>(ki, ko, vi, vo, n_dev, s, pass);
+        else
+            k_sort_pass<false><<<grid_ctas, kThreads, 0, st>>>(ki, ko, nullptr, nullptr, n_dev, s,
+                                                               pass);
+        uint32_t* t = ki; ki = ko; ko = t;
+        t = vi; vi = vo; vo = t;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace kifi

@@ -1,0 +1,227 @@
+"""Python mirror of kifi's fusion interface (denniskb/merge_fusion,
+KinectFission/kifi), backed by libkifi_gpu.so through its C ABI.
+
+Names, argument meanings and results follow the reference classes:
+
+* ``DepthSensorParams``  -- KinectFission/kifi/DepthSensorParams.h:23-52
+* ``Volume``             -- KinectFission/kifi/Volume.h:12-51
+* ``Integrator``         -- KinectFission/kifi/Integrator.h:16-63
+* ``Mesher``             -- KinectFission/kifi/Mesher.h:14-38
+
+Matrices: a (16,) float array is taken in kifi's float4x4 memory order
+(four columns, KinectFission/kifi/util/math.h:59-61); a (4, 4) array is taken
+as the matrix itself (element [row, col]).
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import Camera, KifiError, VolumeDesc, check
+
+
+def as_kifi_matrix(m):
+    """(16,) float32 in kifi float4x4 memory order (column-major)."""
+    a = np.asarray(m, dtype=np.float32)
+    if a.shape == (4, 4):
+        return np.ascontiguousarray(a.T).reshape(16)
+    if a.shape == (16,):
+        return np.ascontiguousarray(a)
+    raise ValueError("expected a (16,) kifi matrix or a (4, 4) matrix")
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class DepthSensorParams:
+    """Camera intrinsics (DepthSensorParams.h:23-52)."""
+
+    def __init__(self, resolution, focal_length, principal_point, sensible_range):
+        self.resolution = (int(resolution[0]), int(resolution[1]))
+        self.focal_length = (float(focal_length[0]), float(focal_length[1]))
+        self.principal_point = (float(principal_point[0]), float(principal_point[1]))
+        self.sensible_range = (float(sensible_range[0]), float(sensible_range[1]))
+
+    def ResolutionPixels(self):
+        return self.resolution
+
+    def FocalLengthPixels(self):
+        return self.focal_length
+
+    def PrincipalPointPixels(self):
+        return self.principal_point
+
+    def SensibleRangeMeters(self):
+        return self.sensible_range
+
+    @staticmethod
+    def KinectParams(resolution_640x480=True, near_mode=False):
+        """DepthSensorParams::KinectParams (DepthSensorParams.cpp:67-82)."""
+        w, h = (640, 480) if resolution_640x480 else (320, 240)
+        fl = np.float32(571.26) if resolution_640x480 else np.float32(285.63)
+        rng = (0.4, 3.0) if near_mode else (0.8, 4.0)
+        return DepthSensorParams((w, h), (fl, fl), (w * 0.5, h * 0.5), rng)
+
+    def camera(self):
+        c = Camera()
+        c.width, c.height = self.resolution
+        c.fx, c.fy = self.focal_length
+        c.cx, c.cy = self.principal_point
+        c.znear_m, c.zfar_m = self.sensible_range
+        return c
+
+    def as_tuple(self):
+        return (self.resolution[0], self.resolution[1]) + self.focal_length + \
+            self.principal_point + self.sensible_range
+
+
+class Volume:
+    """Sparse TSDF volume resident on the GPU (Volume.h:12-51).
+
+    ``Volume(resolution, sideLength, truncationMargin)``; the cube is centred
+    at the world origin.  Voxels are (distance-sum, weight) pairs keyed by
+    30-bit linear keys z<<20 | y<<10 | x."""
+
+    def __init__(self, resolution, side_length, truncation_margin, device=0, capacity=0,
+                 stream=None):
+        self._h = None
+        d = VolumeDesc()
+        d.resolution = int(resolution)
+        d.side_length_m = float(side_length)
+        d.truncation_m = float(truncation_margin)
+        d.initial_capacity = int(capacity)
+        d.device = int(device)
+        d.stream = stream
+        h = C.c_void_p()
+        check(_lib.load().kifi_volume_create(C.byref(d), C.byref(h)), "Volume")
+        self._h = h
+        self._res = int(resolution)
+        self._side = np.float32(side_length)
+        self._trunc = np.float32(truncation_margin)
+
+    def __del__(self):
+        self.close()
+
+    def close(self):
+        if self._h is not None:
+            _lib.load().kifi_volume_destroy(self._h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    # Volume.cpp:41-71
+    def Resolution(self):
+        return self._res
+
+    def VoxelLength(self):
+        return np.float32(self._side / np.float32(self._res))
+
+    def SideLength(self):
+        return self._side
+
+    def TruncationMargin(self):
+        return self._trunc
+
+    def Minimum(self):
+        return np.float32(-0.5) * self._side
+
+    def Maximum(self):
+        return np.float32(0.5) * self._side
+
+    def size(self):
+        n = C.c_size_t()
+        check(_lib.load().kifi_volume_size(self._h, C.byref(n)), "size")
+        return n.value
+
+    def export(self):
+        """(keys uint32 (n,), values float32 (n, 2) = (distance-sum, weight))."""
+        n = self.size()
+        keys = np.zeros(n + 1, np.uint32)
+        vals = np.zeros((n + 1, 2), np.float32)
+        got = C.c_size_t()
+        check(_lib.load().kifi_volume_export(self._h, _ptr(keys), _ptr(vals), n + 1,
+                                             C.byref(got)), "export")
+        return keys[:got.value].copy(), vals[:got.value].copy()
+
+    def insert(self, keys, values=None):
+        """flat_map::insert: union with sorted unique keys; resident voxels win."""
+        k = np.ascontiguousarray(keys, dtype=np.uint32)
+        v = None if values is None else np.ascontiguousarray(values, dtype=np.float32)
+        check(_lib.load().kifi_volume_insert(self._h, _ptr(k), None if v is None else _ptr(v),
+                                             k.size), "insert")
+
+    def clear(self):
+        check(_lib.load().kifi_volume_clear(self._h), "clear")
+
+    def reserve(self, capacity):
+        check(_lib.load().kifi_volume_reserve(self._h, int(capacity)), "reserve")
+
+    def sync(self):
+        check(_lib.load().kifi_volume_sync(self._h), "sync")
+
+    def stream(self):
+        return _lib.load().kifi_volume_stream(self._h)
+
+
+class Integrator:
+    """Integrator::Integrate (Integrator.h:19-26)."""
+
+    def Integrate(self, volume, frame, camera_params, world_to_eye):
+        """frame: (h, w) float32 metres, or uint16 millimetres."""
+        f = np.ascontiguousarray(frame)
+        cam = camera_params.camera()
+        if f.shape != (cam.height, cam.width):
+            raise ValueError("frame shape does not match the camera resolution")
+        m = as_kifi_matrix(world_to_eye)
+        lib = _lib.load()
+        if f.dtype == np.uint16:
+            check(lib.kifi_integrate_u16(volume.handle, _ptr(f), C.byref(cam), _ptr(m)), "Integrate")
+        else:
+            f = np.ascontiguousarray(f, dtype=np.float32)
+            check(lib.kifi_integrate_f32(volume.handle, _ptr(f), C.byref(cam), _ptr(m)), "Integrate")
+
+    def IntegrateDevice(self, volume, depth_ptr, is_u16, camera_params, world_to_eye):
+        """Asynchronous variant over a frame already in device memory."""
+        cam = camera_params.camera()
+        m = as_kifi_matrix(world_to_eye)
+        check(_lib.load().kifi_integrate_device(volume.handle, C.c_void_p(depth_ptr),
+                                                1 if is_u16 else 0, C.byref(cam), _ptr(m)),
+              "IntegrateDevice")
+
+
+class Mesher:
+    """Mesher::Mesh (Mesher.h:17-18)."""
+
+    def Mesh(self, volume, with_indices=True):
+        """Returns (vertices float32 (V, 3), indices uint32 (I,)); without
+        indices the vertices come in the reference's generation order."""
+        lib = _lib.load()
+        nv, ni = C.c_size_t(), C.c_size_t()
+        st = lib.kifi_mesh(volume.handle, 1 if with_indices else 0, None, 0, None, 0,
+                           C.byref(nv), C.byref(ni))
+        if st not in (0, 4):
+            check(st, "Mesh")
+        verts = np.zeros((nv.value + 1, 3), np.float32)
+        idx = np.zeros(ni.value + 1, np.uint32)
+        check(lib.kifi_mesh(volume.handle, 1 if with_indices else 0, _ptr(verts), nv.value + 1,
+                            _ptr(idx), ni.value + 1, C.byref(nv), C.byref(ni)), "Mesh")
+        return verts[:nv.value].copy(), idx[:ni.value].copy()
+
+
+def radix_sort(keys, values=None):
+    """util::radix_sort on the GPU (algorithm.h:63-134)."""
+    k = np.ascontiguousarray(keys, dtype=np.uint32).copy()
+    lib = _lib.load()
+    if values is None:
+        check(lib.kifi_radix_sort_u32(_ptr(k), k.size), "radix_sort")
+        return k
+    v = np.ascontiguousarray(values, dtype=np.uint32).copy()
+    check(lib.kifi_radix_sort_pairs_u32(_ptr(k), _ptr(v), k.size), "radix_sort")
+    return k, v
+
+
+__all__ = ["DepthSensorParams", "Volume", "Integrator", "Mesher", "radix_sort", "KifiError",
+           "as_kifi_matrix"]
