@@ -40,7 +40,14 @@ VOLUMES = [(256, 2.0, 0.02), (512, 4.0, 0.02), (1024, 4.096, 0.02)]
 
 
 def digest(a):
-    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+    """SHA-256 of the array bytes; float32 NaNs are canonicalised to
+    0x7FC00000 first because NaN payloads differ between platforms."""
+    a = np.ascontiguousarray(a)
+    if a.dtype == np.float32:
+        b = a.view(np.uint32).copy()
+        b[np.isnan(a)] = 0x7FC00000
+        a = b
+    return hashlib.sha256(a.tobytes()).hexdigest()
 
 
 def posed(view, off):

@@ -1,17 +1,11 @@
 """Integrator::Integrate on the GPU against the oracle (bit-exact keys and
 TSDF values) and against the reference's golden digests."""
-import hashlib
-
 import numpy as np
 import pytest
 
-from tests.helpers import assert_volume_equal, cam_params, posed
+from tests.helpers import assert_volume_equal, cam_params, canon_bits, digest, posed
 
 pytestmark = pytest.mark.gpu
-
-
-def digest(a):
-    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
 
 
 def test_imrod_matches_golden_and_oracle(gpu, oracle_cpu, golden):

@@ -5,14 +5,10 @@
 * against the reference's own code compiled by oracle/build_ref.py -- runs
   where that build exists (skipped otherwise).
 """
-import hashlib
-
 import numpy as np
 import pytest
 
-
-def digest(a):
-    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+from tests.helpers import canon_bits, digest
 
 
 def posed(view, off):
@@ -82,11 +78,11 @@ def test_oracle_matches_reference_stagewise(oracle_cpu, oracle_ref, golden):
             ov.integrate(depth, cam, v)
             rk, rvals = rv.export()
             assert np.array_equal(rk, ov.keys)
-            assert np.array_equal(rvals.view(np.uint32), ov.values.view(np.uint32))
+            assert np.array_equal(canon_bits(rvals), canon_bits(ov.values))
         for wi in (False, True):
             va, ia = rv.mesh(wi)
             vb, ib = ov.mesh(wi)
-            assert np.array_equal(va.view(np.uint32), vb.view(np.uint32))
+            assert np.array_equal(canon_bits(va), canon_bits(vb))
             assert np.array_equal(ia, ib)
 
 
@@ -123,10 +119,10 @@ def test_oracle_matches_reference_synthetic_scenes(oracle_cpu, oracle_ref):
             ov.integrate(seq.depth_m(i), cam, seq.world_to_eye_f32(i))
         rk, rvals = rv.export()
         assert np.array_equal(rk, ov.keys)
-        assert np.array_equal(rvals.view(np.uint32), ov.values.view(np.uint32))
+        assert np.array_equal(canon_bits(rvals), canon_bits(ov.values))
         va, ia = rv.mesh(True)
         vb, ib = ov.mesh(True)
-        assert np.array_equal(va.view(np.uint32), vb.view(np.uint32)) and np.array_equal(ia, ib)
+        assert np.array_equal(canon_bits(va), canon_bits(vb)) and np.array_equal(ia, ib)
 
 
 def test_oracle_icp_matches_reference_on_sphere(oracle_cpu, oracle_ref):
