@@ -169,6 +169,61 @@ KIFI_API kifi_status kifi_radix_sort_u32(uint32_t* keys, size_t n);
  * (algorithm.h:93-134): stable sort of 32-bit keys carrying 32-bit values. */
 KIFI_API kifi_status kifi_radix_sort_pairs_u32(uint32_t* keys, uint32_t* values, size_t n);
 
+/* ------------------------------------------------------------------ ICP */
+
+/* Context of kifi::ICP (KinectFission/kifi/ICP.h:15-42): device buffers for
+ * the source frame, the target point buffer and the association pairs, and
+ * the pose estimate (kept in double on the device). */
+typedef struct kifi_icp kifi_icp;
+
+KIFI_API kifi_status kifi_icp_create(int device, void* stream, kifi_icp** out);
+KIFI_API kifi_status kifi_icp_destroy(kifi_icp* icp);
+KIFI_API void* kifi_icp_stream(kifi_icp* icp);
+
+/* The synthetic target of ICP::Align (ICP.h:23-24): a width x height
+ * row-major buffer of world points (3 floats each, (0,0,0) = no point) and
+ * the eye-to-world pose of the camera that produced it. */
+KIFI_API kifi_status kifi_icp_set_target(kifi_icp* icp, const float* points, int width, int height,
+                                         const float synth_eye_to_world[16]);
+
+/* Target from a depth frame (host or device memory): every pixel
+ * back-projected to world space with the frame's eye-to-world pose, using
+ * the back-projection of Integrator::DepthMap2PointCloud
+ * (Integrator.cpp:121-144) -- "ICP between consecutive frames". */
+KIFI_API kifi_status kifi_icp_set_target_from_depth(kifi_icp* icp, const void* depth, int on_device,
+                                                    int depth_is_u16, const kifi_camera* cam,
+                                                    const float eye_to_world[16]);
+
+/* kifi::ICP::Align (ICP.h:18-27, ICP.cpp:9-31) against the current target,
+ * with a caller-chosen iteration count (the reference fixes 4): each
+ * iteration is one AlignStep (ICP.cpp:35-265) -- projective association in a
+ * 21x21 window, Horn's closed form -- and the step is left-multiplied onto
+ * the pose.  depth_m: host float metres.  Synchronous. */
+KIFI_API kifi_status kifi_icp_align(kifi_icp* icp, const float* depth_m, const kifi_camera* cam,
+                                    const float eye_to_world_guess[16], int iterations,
+                                    float out_eye_to_world[16]);
+
+/* Same on a device-resident frame; asynchronous (read with kifi_icp_result). */
+KIFI_API kifi_status kifi_icp_align_device(kifi_icp* icp, const void* depth_dev, int depth_is_u16,
+                                           const kifi_camera* cam,
+                                           const float eye_to_world_guess[16], int iterations);
+
+/* Waits and reads the last alignment: the pose (float, and optionally the
+ * double it was rounded from), per-iteration association counts and RMS
+ * residuals (up to `capacity` entries; the reference prints the count,
+ * ICP.cpp:133) and the iteration count.  Pointers may be NULL. */
+KIFI_API kifi_status kifi_icp_result(kifi_icp* icp, float out_eye_to_world[16],
+                                     double out_eye_to_world_d[16], int* n_assoc, double* rms,
+                                     int capacity, int* iterations);
+
+/* kifi::Renderer::Bin (KinectFission/kifi/Renderer.h:23-29,
+ * Renderer.cpp:39-80): z-buffered splat of n world points (3 floats each,
+ * host memory) through world_to_clip into a width x height float3 buffer;
+ * per pixel the first point with the smallest clip z wins, empty pixels are
+ * (0,0,0). */
+KIFI_API kifi_status kifi_bin(const float* points, size_t n, const float world_to_clip[16],
+                              float* out, int width, int height);
+
 #ifdef __cplusplus
 }
 #endif

@@ -58,6 +58,19 @@ SIGNATURES = {
                             C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
     "kifi_radix_sort_u32": (C.c_int, [C.c_void_p, C.c_size_t]),
     "kifi_radix_sort_pairs_u32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "kifi_icp_create": (C.c_int, [C.c_int, C.c_void_p, C.POINTER(C.c_void_p)]),
+    "kifi_icp_destroy": (C.c_int, [C.c_void_p]),
+    "kifi_icp_stream": (C.c_void_p, [C.c_void_p]),
+    "kifi_icp_set_target": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_void_p]),
+    "kifi_icp_set_target_from_depth": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int,
+                                                 C.POINTER(Camera), C.c_void_p]),
+    "kifi_icp_align": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(Camera), C.c_void_p, C.c_int,
+                                 C.c_void_p]),
+    "kifi_icp_align_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.POINTER(Camera),
+                                        C.c_void_p, C.c_int]),
+    "kifi_icp_result": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                  C.c_int, C.POINTER(C.c_int)]),
+    "kifi_bin": (C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
 }
 
 _lib = None

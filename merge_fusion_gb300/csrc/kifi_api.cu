@@ -9,12 +9,11 @@
 #include <new>
 #include <string>
 
-#include "kifi_internal.h"
+#include "kifi_api_util.h"
 
 using namespace kifi;
 
-namespace {
-
+namespace kifi {
 thread_local std::string g_last_error;
 
 kifi_status fail(kifi_status s, const char* what) {
@@ -29,21 +28,6 @@ kifi_status cuda_fail(cudaError_t e, const char* what) {
     return KIFI_ERR_CUDA;
 }
 
-#define KIFI_CUDA(call)                                   \
-    do {                                                  \
-        cudaError_t kifi_e_ = (call);                     \
-        if (kifi_e_ != cudaSuccess) return cuda_fail(kifi_e_, #call); \
-    } while (0)
-
-constexpr size_t kPad = 64;  // slack elements behind every device array
-
-bool is_pow2(int x) { return x > 0 && !(x & (x - 1)); }
-
-bool camera_ok(const kifi_camera* c) {
-    return c && c->width > 0 && c->height > 0 && c->fx != 0.0f && c->fy != 0.0f &&
-           (size_t)c->width * c->height <= (size_t)1 << 26;
-}
-
 kifi_status launch_shape(int device, LaunchShape* ls) {
     int sms = 0;
     KIFI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
@@ -53,6 +37,16 @@ kifi_status launch_shape(int device, LaunchShape* ls) {
     ls->splat_ctas = sms * 4;
     return KIFI_OK;
 }
+
+bool camera_ok(const kifi_camera* c) {
+    return c && c->width > 0 && c->height > 0 && c->fx != 0.0f && c->fy != 0.0f &&
+           (size_t)c->width * c->height <= (size_t)1 << 26;
+}
+}  // namespace kifi
+
+namespace {
+
+bool is_pow2(int x) { return x > 0 && !(x & (x - 1)); }
 
 }  // namespace
 
@@ -180,12 +174,6 @@ kifi_status frame_prologue(kifi_volume* v, const kifi_camera* cam) {
         if (v->n_upper + 8 * P > v->vb.cap && (s = grow_volume(v, v->n_upper + 8 * P))) return s;
     }
     return KIFI_OK;
-}
-
-Mat4 load_mat(const float* m) {
-    Mat4 r;
-    std::memcpy(r.m, m, 64);
-    return r;
 }
 
 // Host frame -> device: straight from page-locked memory, else staged

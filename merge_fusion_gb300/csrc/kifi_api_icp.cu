@@ -1,0 +1,276 @@
+// kifi_api_icp.cu -- C ABI of the ICP context and of Renderer::Bin
+// (include/kifi_gpu.h).  Host code; the kernels live in kifi_icp.cu.
+#include <cstring>
+#include <new>
+
+#include "kifi_api_util.h"
+
+using namespace kifi;
+
+struct kifi_icp {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    LaunchShape ls{};
+    IcpState* st = nullptr;
+    void* depth_dev = nullptr;
+    size_t depth_bytes = 0;
+    float* synth = nullptr;
+    size_t synth_cap = 0;  // floats
+    int sw = 0, sh = 0;
+    Mat4 synth_e2w{};
+    bool have_target = false;
+    float4* src = nullptr;
+    float4* dst = nullptr;
+    size_t n_src_cap = 0;
+    int last_iters = 0;
+};
+
+namespace {
+
+int icp_ctas(const kifi_icp* c, size_t n_src) {
+    size_t b = (n_src + 255) / 256;
+    size_t cap = (size_t)c->ls.sms * 2;
+    if (cap > (size_t)kIcpMaxCtas) cap = kIcpMaxCtas;
+    return (int)(b < 1 ? 1 : (b > cap ? cap : b));
+}
+
+kifi_status reserve_bytes(void** p, size_t* cap, size_t bytes, cudaStream_t st) {
+    if (bytes <= *cap) return KIFI_OK;
+    KIFI_CUDA(cudaStreamSynchronize(st));
+    cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    KIFI_CUDA(cudaMalloc(p, bytes));
+    *cap = bytes;
+    return KIFI_OK;
+}
+
+kifi_status reserve_target(kifi_icp* c, int w, int h) {
+    size_t floats = (size_t)w * h * 3;
+    size_t cap = c->synth_cap * 4;
+    kifi_status s = reserve_bytes((void**)&c->synth, &cap, floats * 4, c->stream);
+    c->synth_cap = cap / 4;
+    return s;
+}
+
+kifi_status enqueue_align(kifi_icp* c, const void* depth_dev, bool u16, const kifi_camera* cam,
+                          const float* guess, int iterations) {
+    if (!c->have_target) return fail(KIFI_ERR_INVALID_ARGUMENT, "ICP target not set");
+    if (iterations < 0 || iterations > kIcpMaxStats)
+        return fail(KIFI_ERR_INVALID_ARGUMENT, "iterations must be in [0, 64]");
+    const size_t n_src = (size_t)((cam->width + 3) / 4) * cam->height;
+    if (n_src > c->n_src_cap) {
+        KIFI_CUDA(cudaStreamSynchronize(c->stream));
+        cudaFree(c->src);
+        cudaFree(c->dst);
+        c->src = c->dst = nullptr;
+        c->n_src_cap = 0;
+        KIFI_CUDA(cudaMalloc(&c->src, n_src * sizeof(float4)));
+        KIFI_CUDA(cudaMalloc(&c->dst, n_src * sizeof(float4)));
+        c->n_src_cap = n_src;
+    }
+    IcpArgs a{};
+    a.depth = depth_dev;
+    a.depth_u16 = u16 ? 1 : 0;
+    a.width = cam->width;
+    a.height = cam->height;
+    // ICP.cpp:48-57: flInv, ppOverFl, and EyeToClipRH * inverse(synth pose)
+    a.fl_inv_x = fdiv(1.0f, cam->fx);
+    a.fl_inv_y = fdiv(1.0f, cam->fy);
+    a.pp_x = fmul(fsub(0.5f, cam->cx), a.fl_inv_x);
+    a.pp_y = fmul(fsub(cam->cy, 0.5f), a.fl_inv_y);
+    Mat4 proj = mat_mul(eye_to_clip(*cam), invert_transform(c->synth_e2w));
+    std::memcpy(a.proj, proj.m, 64);
+    a.synth = c->synth;
+    a.synth_w = c->sw;
+    a.synth_h = c->sh;
+    a.src = c->src;
+    a.dst = c->dst;
+    KIFI_CUDA(icp_align_enqueue(a, c->st, load_mat(guess), iterations, icp_ctas(c, n_src),
+                                c->stream));
+    c->last_iters = iterations;
+    return KIFI_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+kifi_status kifi_icp_create(int device, void* stream, kifi_icp** out) {
+    if (!out) return fail(KIFI_ERR_INVALID_ARGUMENT, "null argument");
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(KIFI_ERR_NO_DEVICE, "no CUDA device");
+    }
+    if (device < 0 || device >= ndev) return fail(KIFI_ERR_INVALID_ARGUMENT, "bad device");
+    kifi_icp* c = new (std::nothrow) kifi_icp();
+    if (!c) return fail(KIFI_ERR_OUT_OF_MEMORY, "host allocation");
+    c->device = device;
+    kifi_status s;
+    cudaError_t e = cudaSetDevice(device);
+    if (!e) {
+        if (stream) c->stream = (cudaStream_t)stream;
+        else {
+            e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+            c->own_stream = !e;
+        }
+    }
+    if (!e) e = cudaMalloc(&c->st, sizeof(IcpState));
+    if (!e) e = cudaMemset(c->st, 0, sizeof(IcpState));
+    if (e) {
+        kifi_icp_destroy(c);
+        return cuda_fail(e, "ICP context");
+    }
+    if ((s = launch_shape(device, &c->ls))) {
+        kifi_icp_destroy(c);
+        return s;
+    }
+    *out = c;
+    return KIFI_OK;
+}
+
+kifi_status kifi_icp_destroy(kifi_icp* c) {
+    if (!c) return KIFI_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    cudaFree(c->st);
+    cudaFree(c->depth_dev);
+    cudaFree(c->synth);
+    cudaFree(c->src);
+    cudaFree(c->dst);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return KIFI_OK;
+}
+
+void* kifi_icp_stream(kifi_icp* c) { return c ? (void*)c->stream : nullptr; }
+
+kifi_status kifi_icp_set_target(kifi_icp* c, const float* points, int width, int height,
+                                const float synth_eye_to_world[16]) {
+    if (!c || !points || width <= 0 || height <= 0 || !synth_eye_to_world)
+        return fail(KIFI_ERR_INVALID_ARGUMENT, "bad argument");
+    KIFI_CUDA(cudaSetDevice(c->device));
+    kifi_status s = reserve_target(c, width, height);
+    if (s) return s;
+    KIFI_CUDA(cudaMemcpyAsync(c->synth, points, (size_t)width * height * 12, cudaMemcpyHostToDevice,
+                              c->stream));
+    KIFI_CUDA(cudaStreamSynchronize(c->stream));
+    c->sw = width;
+    c->sh = height;
+    c->synth_e2w = load_mat(synth_eye_to_world);
+    c->have_target = true;
+    return KIFI_OK;
+}
+
+kifi_status kifi_icp_set_target_from_depth(kifi_icp* c, const void* depth, int on_device,
+                                           int depth_is_u16, const kifi_camera* cam,
+                                           const float eye_to_world[16]) {
+    if (!c || !depth || !camera_ok(cam) || !eye_to_world)
+        return fail(KIFI_ERR_INVALID_ARGUMENT, "bad argument");
+    KIFI_CUDA(cudaSetDevice(c->device));
+    kifi_status s = reserve_target(c, cam->width, cam->height);
+    if (s) return s;
+    const void* src = depth;
+    if (!on_device) {
+        const size_t bytes = (size_t)cam->width * cam->height * (depth_is_u16 ? 2 : 4);
+        if ((s = reserve_bytes(&c->depth_dev, &c->depth_bytes, bytes, c->stream))) return s;
+        KIFI_CUDA(cudaMemcpyAsync(c->depth_dev, depth, bytes, cudaMemcpyHostToDevice, c->stream));
+        src = c->depth_dev;
+    }
+    const Mat4 e2w = load_mat(eye_to_world);
+    KIFI_CUDA(backproject_enqueue(src, depth_is_u16 != 0, *cam, e2w, c->synth, c->ls.sms * 4,
+                                  c->stream));
+    if (!on_device) KIFI_CUDA(cudaStreamSynchronize(c->stream));
+    c->sw = cam->width;
+    c->sh = cam->height;
+    c->synth_e2w = e2w;
+    c->have_target = true;
+    return KIFI_OK;
+}
+
+kifi_status kifi_icp_align(kifi_icp* c, const float* depth_m, const kifi_camera* cam,
+                           const float eye_to_world_guess[16], int iterations,
+                           float out_eye_to_world[16]) {
+    if (!c || !depth_m || !camera_ok(cam) || !eye_to_world_guess || !out_eye_to_world)
+        return fail(KIFI_ERR_INVALID_ARGUMENT, "bad argument");
+    KIFI_CUDA(cudaSetDevice(c->device));
+    const size_t bytes = (size_t)cam->width * cam->height * 4;
+    kifi_status s = reserve_bytes(&c->depth_dev, &c->depth_bytes, bytes, c->stream);
+    if (s) return s;
+    KIFI_CUDA(cudaMemcpyAsync(c->depth_dev, depth_m, bytes, cudaMemcpyHostToDevice, c->stream));
+    if ((s = enqueue_align(c, c->depth_dev, false, cam, eye_to_world_guess, iterations))) return s;
+    return kifi_icp_result(c, out_eye_to_world, nullptr, nullptr, nullptr, 0, nullptr);
+}
+
+kifi_status kifi_icp_align_device(kifi_icp* c, const void* depth_dev, int depth_is_u16,
+                                  const kifi_camera* cam, const float eye_to_world_guess[16],
+                                  int iterations) {
+    if (!c || !depth_dev || !camera_ok(cam) || !eye_to_world_guess)
+        return fail(KIFI_ERR_INVALID_ARGUMENT, "bad argument");
+    KIFI_CUDA(cudaSetDevice(c->device));
+    return enqueue_align(c, depth_dev, depth_is_u16 != 0, cam, eye_to_world_guess, iterations);
+}
+
+kifi_status kifi_icp_result(kifi_icp* c, float out_eye_to_world[16], double out_eye_to_world_d[16],
+                            int* n_assoc, double* rms, int capacity, int* iterations) {
+    if (!c) return fail(KIFI_ERR_INVALID_ARGUMENT, "null context");
+    KIFI_CUDA(cudaSetDevice(c->device));
+    // read the head of the state: poses and per-iteration statistics
+    const size_t head = offsetof(IcpState, part);
+    IcpState* h = (IcpState*)std::malloc(head);
+    if (!h) return fail(KIFI_ERR_OUT_OF_MEMORY, "host allocation");
+    cudaError_t e = cudaMemcpyAsync(h, c->st, head, cudaMemcpyDeviceToHost, c->stream);
+    if (!e) e = cudaStreamSynchronize(c->stream);
+    if (e) {
+        std::free(h);
+        return cuda_fail(e, "ICP result");
+    }
+    if (out_eye_to_world) std::memcpy(out_eye_to_world, h->pose_f, 64);
+    if (out_eye_to_world_d)
+        for (int r = 0; r < 4; ++r)
+            for (int col = 0; col < 4; ++col) out_eye_to_world_d[4 * col + r] = h->pose[4 * r + col];
+    const int it = h->iter < kIcpMaxStats ? h->iter : kIcpMaxStats;
+    if (iterations) *iterations = h->iter;
+    for (int i = 0; i < it && i < capacity; ++i) {
+        if (n_assoc) n_assoc[i] = h->stats[i].n_assoc;
+        if (rms) rms[i] = h->stats[i].rms;
+    }
+    std::free(h);
+    return KIFI_OK;
+}
+
+kifi_status kifi_bin(const float* points, size_t n, const float world_to_clip[16], float* out,
+                     int width, int height) {
+    if ((n && !points) || !world_to_clip || !out || width <= 0 || height <= 0)
+        return fail(KIFI_ERR_INVALID_ARGUMENT, "bad argument");
+    if (n >= ((size_t)1 << 32)) return fail(KIFI_ERR_UNSUPPORTED, "more than 2^32 points");
+    int dev = 0;
+    KIFI_CUDA(cudaGetDevice(&dev));
+    LaunchShape ls;
+    kifi_status s = launch_shape(dev, &ls);
+    if (s) return s;
+    cudaStream_t st;
+    KIFI_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    float *dp = nullptr, *dout = nullptr;
+    unsigned long long* zb = nullptr;
+    const size_t pix = (size_t)width * height;
+    cudaError_t e = cudaMalloc(&dp, n * 12 + 16);
+    if (!e) e = cudaMalloc(&dout, pix * 12);
+    if (!e) e = cudaMalloc(&zb, pix * 8);
+    if (!e && n) e = cudaMemcpyAsync(dp, points, n * 12, cudaMemcpyHostToDevice, st);
+    if (!e) e = bin_enqueue(dp, (unsigned int)n, load_mat(world_to_clip), width, height, zb, dout,
+                            ls.sms * 4, st);
+    if (!e) e = cudaMemcpyAsync(out, dout, pix * 12, cudaMemcpyDeviceToHost, st);
+    if (!e) e = cudaStreamSynchronize(st);
+    cudaFree(dp);
+    cudaFree(dout);
+    cudaFree(zb);
+    cudaStreamDestroy(st);
+    if (e) return cuda_fail(e, "bin");
+    return KIFI_OK;
+}
+
+}  // extern "C"

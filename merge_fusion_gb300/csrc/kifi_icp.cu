@@ -1,0 +1,446 @@
+// kifi_icp.cu -- projective ICP on sm_103a: kifi::ICP::Align / AlignStep
+// (KinectFission/kifi/ICP.cpp:9-265) and its target producers,
+// Renderer::Bin (Renderer.cpp:39-80) and a depth back-projection.
+//
+// One AlignStep is two kernels, both ending in a last-CTA-done finisher, so a
+// whole Align (any iteration count) is a fixed launch sequence with no host
+// round trip:
+//
+//  k_icp_associate   one thread per source pixel of every row and every 4th
+//                    column (ICP.cpp:66-67): back-project with the current
+//                    pose estimate, project into the target camera, search
+//                    the 21x21 window for the nearest valid target point
+//                    within len^2 < 0.01 (:100-131; first minimum in scan
+//                    order wins).  The pairs are stored; counts and the
+//                    centroid sums are reduced with compensated float
+//                    arithmetic per thread and warp (Kahan / TwoSum) and in
+//                    double across CTAs.  The last CTA forms the centroids
+//                    (:166-167).
+//  k_icp_horn        the centred 3x3 cross-covariance (:169-197) with the
+//                    same compensated reduction; the last CTA builds Horn's
+//                    symmetric 4x4 matrix (:199-213) in double, solves it with
+//                    a cyclic Jacobi eigen-decomposition in double (Golub &
+//                    Van Loan, sec. 8.5; warm-started from the previous
+//                    step's eigenvectors), turns the dominant eigenvector into
+//                    R and t (:218-256) and accumulates the pose
+//                    step * pose in double (:23-28).  The float pose the next
+//                    association uses is that double pose rounded.
+//
+// The per-point arithmetic follows the reference's float expression order
+// and x86 float-to-int conversion (CVTTSS2SI: truncation, INT_MIN for NaN or
+// out-of-range); the reference's 640x480 window clamp (:108-109) is kept,
+// with reads past the end of a smaller target buffer treated as invalid
+// points.
+#include "kifi_internal.h"
+
+namespace kifi {
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ int cvt_i32_x86(float f) {
+    if (f >= -2147483648.0f && f < 2147483648.0f) return __float2int_rz(f);
+    return INT_MIN;
+}
+__device__ __forceinline__ int wrap_sub(int a, int b) { return (int)((unsigned int)a - (unsigned int)b); }
+
+// compensated float accumulator (Kahan; kahan_sum, numeric.h:59-68)
+struct KahanF {
+    float s = 0.0f, c = 0.0f;
+    __device__ __forceinline__ void add(float x) {
+        float y = fsub(x, c);
+        float t = fadd(s, y);
+        c = fsub(fsub(t, s), y);
+        s = t;
+    }
+};
+
+// TwoSum-based warp reduction of a compensated pair (s, c)
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = fadd(a, b);
+    float bb = fsub(s, a);
+    e = fadd(fsub(a, fsub(s, bb)), fsub(b, bb));
+}
+__device__ __forceinline__ double warp_sum_comp(float s, float c) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        float s2 = __shfl_xor_sync(0xffffffffu, s, o);
+        float c2 = __shfl_xor_sync(0xffffffffu, c, o);
+        float ns, e;
+        two_sum(s, s2, ns, e);
+        c = fadd(fadd(c, c2), e);
+        s = ns;
+    }
+    return (double)s + (double)c;
+}
+
+// block reduction of NV compensated values to double partials (thread 0 gets them)
+template <int NV>
+__device__ __forceinline__ void block_reduce(const KahanF (&k)[NV], double (&out)[NV]) {
+    __shared__ double sh[kThreads / 32][NV];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+        double w = warp_sum_comp(k[i].s, -k[i].c);
+        if (lane == 0) sh[warp][i] = w;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            double a = 0.0;
+            for (int w = 0; w < kThreads / 32; ++w) a += sh[w][i];
+            out[i] = a;
+        }
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ float load_depth(const void* depth, size_t i, bool u16) {
+    if (u16) return fmul((float)(unsigned int)__ldg((const unsigned short*)depth + i), 0.001f);
+    return __ldg((const float*)depth + i);
+}
+
+// last CTA to arrive returns true (after a fence); resets the counter
+__device__ __forceinline__ bool last_cta(unsigned int* counter) {
+    __shared__ bool last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        unsigned int prev = atomicAdd(counter, 1u);
+        last = (prev == gridDim.x - 1);
+        if (last) *counter = 0u;
+    }
+    __syncthreads();
+    if (last) __threadfence();
+    return last;
+}
+
+__global__ void __launch_bounds__(kThreads) k_icp_associate(IcpArgs a, IcpState* __restrict__ st) {
+    const int n_cols = (a.width + 3) / 4;
+    const int n_src = n_cols * a.height;
+    const float* pose = st->pose_f;
+    // counts, src xyzw, dst xyz, sum of min len^2
+    KahanF acc[9];
+    const float half_w = fmul((float)a.synth_w, 0.5f), half_h = fmul((float)a.synth_h, 0.5f);
+    const size_t n_synth = (size_t)a.synth_w * a.synth_h;
+    for (int s = blockIdx.x * kThreads + threadIdx.x; s < n_src; s += gridDim.x * kThreads) {
+        const int y = s / n_cols, x = (s - y * n_cols) * 4;
+        float4 p1 = make_float4(0.f, 0.f, 0.f, 0.f), p2 = make_float4(0.f, 0.f, 0.f, 0.f);
+        const float d = load_depth(a.depth, (size_t)y * a.width + x, a.depth_u16);
+        if (0.0f != d) {
+            float pt[4];
+            pt[0] = fmul(fadd(fmul((float)x, a.fl_inv_x), a.pp_x), d);
+            pt[1] = fmul(fadd(fmul(-(float)y, a.fl_inv_y), a.pp_y), d);
+            pt[2] = fmul(fadd(fmul(-1.0f, 1.0f), 0.0f), d);
+            pt[3] = 1.0f;
+            float wp[4], cl[4];
+            mat_vec(pose, pt, wp);
+            mat_vec(a.proj, wp, cl);
+            const float ux = fdiv(cl[0], cl[3]), uy = fdiv(cl[1], cl[3]);
+            int u = wrap_sub(cvt_i32_x86(fadd(fmul(ux, half_w), half_w)), 10);
+            int v = wrap_sub(wrap_sub(a.synth_h - 1, cvt_i32_x86(fadd(fmul(uy, half_h), half_h))), 10);
+            u = max(0, u);
+            v = max(0, v);
+            float mind = 0.01f;
+            float3 best = make_float3(0.f, 0.f, 0.f);
+            const int yend = (int)min(480ll, (long long)v + 21), xend = (int)min(640ll, (long long)u + 21);
+            const float dw = fsub(1.0f, wp[3]);
+            const float dw2 = fmul(dw, dw);
+            for (int y1 = v; y1 < yend; ++y1) {
+                const size_t row = (size_t)y1 * a.synth_w;
+                for (int x1 = u; x1 < xend; ++x1) {
+                    const size_t at = row + x1;
+                    if (at >= n_synth) continue;
+                    const float* q = a.synth + 3 * at;
+                    const float qx = __ldg(q), qy = __ldg(q + 1), qz = __ldg(q + 2);
+                    if (qx == 0.0f && qy == 0.0f && qz == 0.0f) continue;
+                    const float dx = fsub(qx, wp[0]), dy = fsub(qy, wp[1]), dz = fsub(qz, wp[2]);
+                    const float l2 = fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fadd(fmul(dz, dz), dw2));
+                    if (l2 < mind) {
+                        mind = l2;
+                        best = make_float3(qx, qy, qz);
+                    }
+                }
+            }
+            if (mind < 0.01f) {
+                p1 = make_float4(wp[0], wp[1], wp[2], wp[3]);
+                p2 = make_float4(best.x, best.y, best.z, 1.0f);
+                acc[0].add(1.0f);
+                acc[1].add(p1.x); acc[2].add(p1.y); acc[3].add(p1.z); acc[4].add(p1.w);
+                acc[5].add(p2.x); acc[6].add(p2.y); acc[7].add(p2.z);
+                acc[8].add(mind);
+            }
+        }
+        a.src[s] = p1;
+        a.dst[s] = p2;  // w = 1 marks an association
+    }
+    double part[9];
+    block_reduce<9>(acc, part);
+    if (threadIdx.x == 0)
+        for (int i = 0; i < 9; ++i) st->part[blockIdx.x * 16 + i] = part[i];
+    if (!last_cta(&st->done)) return;
+    if (threadIdx.x == 0) {
+        double tot[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        for (unsigned int b = 0; b < gridDim.x; ++b)
+            for (int i = 0; i < 9; ++i) tot[i] += st->part[b * 16 + i];
+        const int n = (int)(tot[0] + 0.5);
+        const float nf = (float)n;
+        // srcMedianSum / float4(n) (ICP.cpp:166-167)
+        for (int i = 0; i < 4; ++i) st->mu_s[i] = fdiv((float)tot[1 + i], nf);
+        for (int i = 0; i < 3; ++i) st->mu_d[i] = fdiv((float)tot[5 + i], nf);
+        st->mu_d[3] = fdiv(nf, nf);
+        st->n_assoc = n;
+        st->sum_l2 = tot[8];
+    }
+}
+
+// ------------------------------------------------------ FP64 Horn solve
+// Cyclic Jacobi on a symmetric 4x4 (row-major) in double; V accumulates the
+// rotations (columns are eigenvectors).  Starting from V0 (the previous
+// solve's eigenvectors) the matrix is first rotated into that basis.
+__device__ void jacobi4(double* A, double* V, const double* V0, bool warm) {
+    double a[16];
+    if (warm) {
+        double t[16];
+        for (int i = 0; i < 4; ++i)
+            for (int j = 0; j < 4; ++j) {
+                double s = 0.0;
+                for (int k = 0; k < 4; ++k) s += A[4 * i + k] * V0[4 * k + j];
+                t[4 * i + j] = s;
+            }
+        for (int i = 0; i < 4; ++i)
+            for (int j = 0; j < 4; ++j) {
+                double s = 0.0;
+                for (int k = 0; k < 4; ++k) s += V0[4 * k + i] * t[4 * k + j];
+                a[4 * i + j] = s;
+            }
+        for (int i = 0; i < 16; ++i) V[i] = V0[i];
+    } else {
+        for (int i = 0; i < 16; ++i) {
+            a[i] = A[i];
+            V[i] = (i % 5 == 0) ? 1.0 : 0.0;
+        }
+    }
+    double scale = 0.0;
+    for (int i = 0; i < 16; ++i) scale += a[i] * a[i];
+    for (int sweep = 0; sweep < 32; ++sweep) {
+        double off = 0.0;
+        for (int p = 0; p < 4; ++p)
+            for (int q = p + 1; q < 4; ++q) off += a[4 * p + q] * a[4 * p + q];
+        if (!(off > 1e-32 * scale)) break;
+        for (int p = 0; p < 3; ++p)
+            for (int q = p + 1; q < 4; ++q) {
+                const double apq = a[4 * p + q];
+                if (apq == 0.0) continue;
+                const double theta = (a[4 * q + q] - a[4 * p + p]) / (2.0 * apq);
+                const double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+                const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+                for (int k = 0; k < 4; ++k) {
+                    const double akp = a[4 * k + p], akq = a[4 * k + q];
+                    a[4 * k + p] = c * akp - s * akq;
+                    a[4 * k + q] = s * akp + c * akq;
+                }
+                for (int k = 0; k < 4; ++k) {
+                    const double apk = a[4 * p + k], aqk = a[4 * q + k];
+                    a[4 * p + k] = c * apk - s * aqk;
+                    a[4 * q + k] = s * apk + c * aqk;
+                }
+                for (int k = 0; k < 4; ++k) {
+                    const double vkp = V[4 * k + p], vkq = V[4 * k + q];
+                    V[4 * k + p] = c * vkp - s * vkq;
+                    V[4 * k + q] = s * vkp + c * vkq;
+                }
+            }
+    }
+    for (int i = 0; i < 4; ++i) A[i] = a[5 * i];  // eigenvalues into A[0..3]
+}
+
+__global__ void __launch_bounds__(kThreads) k_icp_horn(IcpArgs a, IcpState* __restrict__ st) {
+    const int n_cols = (a.width + 3) / 4;
+    const int n_src = n_cols * a.height;
+    const float ms0 = st->mu_s[0], ms1 = st->mu_s[1], ms2 = st->mu_s[2];
+    const float md0 = st->mu_d[0], md1 = st->mu_d[1], md2 = st->mu_d[2];
+    KahanF acc[9];
+    for (int s = blockIdx.x * kThreads + threadIdx.x; s < n_src; s += gridDim.x * kThreads) {
+        const float4 q = a.dst[s];
+        if (q.w == 0.0f) continue;
+        const float4 p = a.src[s];
+        // src = float4(p1, 1) - srcMedian, dst likewise (ICP.cpp:180-184)
+        const float sx = fsub(p.x, ms0), sy = fsub(p.y, ms1), sz = fsub(p.z, ms2);
+        const float dx = fsub(q.x, md0), dy = fsub(q.y, md1), dz = fsub(q.z, md2);
+        acc[0].add(fmul(sx, dx)); acc[1].add(fmul(sx, dy)); acc[2].add(fmul(sx, dz));
+        acc[3].add(fmul(sy, dx)); acc[4].add(fmul(sy, dy)); acc[5].add(fmul(sy, dz));
+        acc[6].add(fmul(sz, dx)); acc[7].add(fmul(sz, dy)); acc[8].add(fmul(sz, dz));
+    }
+    double part[9];
+    block_reduce<9>(acc, part);
+    if (threadIdx.x == 0)
+        for (int i = 0; i < 9; ++i) st->part[blockIdx.x * 16 + i] = part[i];
+    if (!last_cta(&st->done)) return;
+    if (threadIdx.x != 0) return;
+    double S[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (unsigned int b = 0; b < gridDim.x; ++b)
+        for (int i = 0; i < 9; ++i) S[i] += st->part[b * 16 + i];
+    const double Sxx = S[0], Sxy = S[1], Sxz = S[2], Syx = S[3], Syy = S[4], Syz = S[5],
+                 Szx = S[6], Szy = S[7], Szz = S[8];
+    // Horn's N (ICP.cpp:199-213), symmetric
+    double N[16] = {Sxx + Syy + Szz, Syz - Szy, Szx - Sxz, Sxy - Syx,
+                    Syz - Szy, Sxx - Syy - Szz, Sxy + Syx, Szx + Sxz,
+                    Szx - Sxz, Sxy + Syx, Syy - Sxx - Szz, Syz + Szy,
+                    Sxy - Syx, Szx + Sxz, Syz + Szy, Szz - Sxx - Syy};
+    double V[16];
+    jacobi4(N, V, st->V, st->have_V != 0);
+    for (int i = 0; i < 16; ++i) st->V[i] = V[i];
+    st->have_V = 1;
+    int imax = 0;
+    for (int i = 1; i < 4; ++i)
+        if (N[i] > N[imax]) imax = i;
+    double q[4] = {V[0 + imax], V[4 + imax], V[8 + imax], V[12 + imax]};
+    const double ql = sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+    for (int i = 0; i < 4; ++i) q[i] /= ql;
+    // quaternion (x = scalar part) to rotation (ICP.cpp:233-254)
+    const double xy = q[0] * q[1], xz = q[0] * q[2], xw = q[0] * q[3], yy = q[1] * q[1],
+                 yz = q[1] * q[2], yw = q[1] * q[3], zz = q[2] * q[2], zw = q[2] * q[3],
+                 ww = q[3] * q[3];
+    const double R[9] = {1.0 - 2.0 * (zz + ww), 2.0 * (yz - xw),       2.0 * (yw + xz),
+                         2.0 * (yz + xw),       1.0 - 2.0 * (yy + ww), 2.0 * (zw - xy),
+                         2.0 * (yw - xz),       2.0 * (zw + xy),       1.0 - 2.0 * (yy + zz)};
+    double T[16];  // step = T * R, row-major
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) T[4 * r + c] = (r == c) ? 1.0 : 0.0;
+    const double ms[3] = {(double)ms0, (double)ms1, (double)ms2};
+    const double md[3] = {(double)md0, (double)md1, (double)md2};
+    for (int r = 0; r < 3; ++r) {
+        double t = md[r];
+        for (int c = 0; c < 3; ++c) {
+            T[4 * r + c] = R[3 * r + c];
+            t -= R[3 * r + c] * ms[c];
+        }
+        T[4 * r + 3] = t;
+    }
+    double P[16];
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) {
+            double s = 0.0;
+            for (int k = 0; k < 4; ++k) s += T[4 * r + k] * st->pose[4 * k + c];
+            P[4 * r + c] = s;
+        }
+    for (int i = 0; i < 16; ++i) st->pose[i] = P[i];
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) st->pose_f[4 * c + r] = (float)P[4 * r + c];
+    const int it = st->iter;
+    if (it < kIcpMaxStats) {
+        st->stats[it].n_assoc = st->n_assoc;
+        st->stats[it].rms = st->n_assoc > 0 ? sqrt(st->sum_l2 / st->n_assoc) : 0.0;
+    }
+    st->iter = it + 1;
+}
+
+__global__ void k_icp_begin(IcpState* st, Mat4 guess) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) st->pose[4 * r + c] = (double)guess.m[4 * c + r];
+    for (int i = 0; i < 16; ++i) st->pose_f[i] = guess.m[i];
+    st->iter = 0;
+    st->have_V = 0;
+    st->done = 0u;
+}
+
+// World points of a depth frame: the back-projection of
+// DepthMap2PointCloud (Integrator.cpp:121-144) without the voxel step;
+// pixels without depth get (0,0,0), the reference's "invalid" target value.
+__global__ void k_backproject(const void* __restrict__ depth, int u16, int width, int height,
+                              float fl_inv_x, float fl_inv_y, float pp_x, float pp_y, Mat4 e2w,
+                              float* __restrict__ out) {
+    const int n = width * height;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int v = i / width, u = i - v * width;
+        const float d = load_depth(depth, i, u16 != 0);
+        float w[4] = {0.f, 0.f, 0.f, 0.f};
+        if (d > 0.0f) {
+            float p[4];
+            p[0] = fadd(fmul(fadd(fmul((float)u, fl_inv_x), pp_x), d), 0.0f);
+            p[1] = fadd(fmul(fadd(fmul(fadd(0.0f, -(float)v), fl_inv_y), pp_y), d), 0.0f);
+            p[2] = fadd(fmul(fadd(fmul(-1.0f, 1.0f), 0.0f), d), 0.0f);
+            p[3] = fadd(fmul(fadd(fmul(0.0f, 1.0f), 0.0f), d), 1.0f);
+            mat_vec(e2w.m, p, w);
+        }
+        out[3 * i] = w[0];
+        out[3 * i + 1] = w[1];
+        out[3 * i + 2] = w[2];
+    }
+}
+
+// Renderer::Bin: a z-buffered splat.  The first point (in input order) with
+// the smallest clip-space z wins a pixel, as the reference's sequential
+// strict "<" test does; a 64-bit atomicMin over (ordered z, point index)
+// gives the same winner in parallel.
+__device__ __forceinline__ unsigned int ordered_bits(float z) {
+    if (z == 0.0f) z = 0.0f;  // -0 and +0 compare equal
+    unsigned int b = __float_as_uint(z);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+
+__global__ void k_bin_splat(const float* __restrict__ pts, unsigned int n, Mat4 w2c, int width,
+                            int height, unsigned long long* __restrict__ zbuf) {
+    const float hw = fmul((float)width, 0.5f), hh = fmul((float)height, 0.5f);
+    for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float p[4] = {pts[3 * i], pts[3 * i + 1], pts[3 * i + 2], 1.0f}, c[4];
+        mat_vec(w2c.m, p, c);
+        const float x = fdiv(c[0], c[3]), y = fdiv(c[1], c[3]), z = fdiv(c[2], c[3]);
+        const int u = cvt_i32_x86(fadd(fmul(x, hw), hw));
+        const int v = wrap_sub(height - 1, cvt_i32_x86(fadd(fmul(y, hh), hh)));
+        if (u >= 0 && u < width && v >= 0 && v < height && z >= -1.0f && z <= 1.0f)
+            atomicMin(zbuf + (size_t)v * width + u, (unsigned long long)ordered_bits(z) << 32 | i);
+    }
+}
+
+__global__ void k_bin_resolve(const float* __restrict__ pts, const unsigned long long* __restrict__ zbuf,
+                              int n_pix, float* __restrict__ out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_pix; i += gridDim.x * blockDim.x) {
+        const unsigned long long z = zbuf[i];
+        float x = 0.f, y = 0.f, w = 0.f;
+        if (z != ~0ull) {
+            const unsigned int j = (unsigned int)(z & 0xffffffffu);
+            x = pts[3 * j];
+            y = pts[3 * j + 1];
+            w = pts[3 * j + 2];
+        }
+        out[3 * i] = x;
+        out[3 * i + 1] = y;
+        out[3 * i + 2] = w;
+    }
+}
+
+}  // namespace
+
+cudaError_t icp_align_enqueue(const IcpArgs& a, IcpState* st, const Mat4& guess, int iterations,
+                              int ctas, cudaStream_t stream) {
+    k_icp_begin<<<1, 32, 0, stream>>>(st, guess);
+    for (int it = 0; it < iterations; ++it) {
+        k_icp_associate<<<ctas, kThreads, 0, stream>>>(a, st);
+        k_icp_horn<<<ctas, kThreads, 0, stream>>>(a, st);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t backproject_enqueue(const void* depth, bool u16, const kifi_camera& cam,
+                                const Mat4& eye_to_world, float* out, int ctas, cudaStream_t st) {
+    const float fix = fdiv(1.0f, cam.fx), fiy = fdiv(1.0f, cam.fy);
+    const float ppx = fmul(fsub(0.5f, cam.cx), fix), ppy = fmul(fsub(cam.cy, 0.5f), fiy);
+    k_backproject<<<ctas, kThreads, 0, st>>>(depth, u16 ? 1 : 0, cam.width, cam.height, fix, fiy,
+                                             ppx, ppy, eye_to_world, out);
+    return cudaGetLastError();
+}
+
+cudaError_t bin_enqueue(const float* pts, unsigned int n, const Mat4& w2c, int width, int height,
+                        unsigned long long* zbuf, float* out, int ctas, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(zbuf, 0xff, (size_t)width * height * 8, st);
+    if (e) return e;
+    if (n) k_bin_splat<<<ctas, kThreads, 0, st>>>(pts, n, w2c, width, height, zbuf);
+    k_bin_resolve<<<ctas, kThreads, 0, st>>>(pts, zbuf, width * height, out);
+    return cudaGetLastError();
+}
+
+}  // namespace kifi

@@ -91,4 +91,47 @@ cudaError_t mesh_emit_enqueue(const Geom& g, const uint32_t* keys, const float2*
                               unsigned long long n_idx, unsigned int missing_bound, float* verts_dev,
                               uint32_t* idx_dev, int sms, cudaStream_t st);
 
+// ------------------------------------------------------------------ ICP
+constexpr int kIcpMaxStats = 64;
+constexpr int kIcpMaxCtas = 2048;
+
+struct IcpArgs {
+    const void* depth;      // source frame (float metres or uint16 mm)
+    int depth_u16;
+    int width, height;
+    float fl_inv_x, fl_inv_y, pp_x, pp_y;
+    float proj[16];         // EyeToClipRH * inverse(synth eye-to-world), kifi order
+    const float* synth;     // target world points, synth_w * synth_h float3
+    int synth_w, synth_h;
+    float4* src;            // per source pixel: associated point (w = pose row 3)
+    float4* dst;            // per source pixel: target point, w = 1 when associated
+};
+
+struct IcpIterStats {
+    int n_assoc;
+    int pad;
+    double rms;  // sqrt(mean of the associated squared distances)
+};
+
+struct IcpState {
+    double pose[16];    // eye-to-world estimate, row-major double
+    float pose_f[16];   // the same rounded to float, kifi order
+    double V[16];       // eigenvectors of the previous Horn solve (warm start)
+    int have_V;
+    unsigned int done;  // last-CTA counter
+    float mu_s[4], mu_d[4];
+    int n_assoc;
+    int iter;
+    double sum_l2;
+    IcpIterStats stats[kIcpMaxStats];
+    double part[kIcpMaxCtas * 16];  // per-CTA partial sums
+};
+
+cudaError_t icp_align_enqueue(const IcpArgs& a, IcpState* st, const Mat4& guess, int iterations,
+                              int ctas, cudaStream_t stream);
+cudaError_t backproject_enqueue(const void* depth, bool u16, const kifi_camera& cam,
+                                const Mat4& eye_to_world, float* out, int ctas, cudaStream_t st);
+cudaError_t bin_enqueue(const float* pts, unsigned int n, const Mat4& w2c, int width, int height,
+                        unsigned long long* zbuf, float* out, int ctas, cudaStream_t st);
+
 }  // namespace kifi

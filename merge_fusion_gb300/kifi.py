@@ -211,6 +211,90 @@ class Mesher:
         return verts[:nv.value].copy(), idx[:ni.value].copy()
 
 
+class ICP:
+    """ICP::Align (ICP.h:18-27) on the GPU.
+
+    ``Align(rawDepthMap, eyeToWorldGuess, synthBuffer, synthEyeToWorld,
+    cameraParams, iterations=4)`` -- the reference's parameter names say
+    worldToEye but carry eye-to-world poses (ICP.cpp:12-15, :79); the
+    reference fixes 4 iterations (ICP.cpp:22).  Returns the eye-to-world pose
+    as a (16,) kifi matrix."""
+
+    def __init__(self, device=0, stream=None):
+        self._h = None
+        h = C.c_void_p()
+        check(_lib.load().kifi_icp_create(int(device), stream, C.byref(h)), "ICP")
+        self._h = h
+
+    def __del__(self):
+        self.close()
+
+    def close(self):
+        if self._h is not None:
+            _lib.load().kifi_icp_destroy(self._h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def SetTarget(self, synth_points, synth_eye_to_world):
+        p = np.ascontiguousarray(synth_points, dtype=np.float32)
+        if p.ndim != 3 or p.shape[2] != 3:
+            raise ValueError("target must be (h, w, 3)")
+        m = as_kifi_matrix(synth_eye_to_world)
+        check(_lib.load().kifi_icp_set_target(self._h, _ptr(p), p.shape[1], p.shape[0], _ptr(m)),
+              "SetTarget")
+
+    def SetTargetFromDepth(self, frame, camera_params, eye_to_world):
+        f = np.ascontiguousarray(frame)
+        u16 = f.dtype == np.uint16
+        if not u16:
+            f = np.ascontiguousarray(f, dtype=np.float32)
+        cam = camera_params.camera()
+        m = as_kifi_matrix(eye_to_world)
+        check(_lib.load().kifi_icp_set_target_from_depth(self._h, _ptr(f), 0, 1 if u16 else 0,
+                                                         C.byref(cam), _ptr(m)), "SetTargetFromDepth")
+
+    def Align(self, raw_depth, eye_to_world_guess, synth_points, synth_eye_to_world,
+              camera_params, iterations=4):
+        self.SetTarget(synth_points, synth_eye_to_world)
+        return self.AlignToTarget(raw_depth, eye_to_world_guess, camera_params, iterations)
+
+    def AlignToTarget(self, raw_depth, eye_to_world_guess, camera_params, iterations=4):
+        d = np.ascontiguousarray(raw_depth, dtype=np.float32)
+        cam = camera_params.camera()
+        g = as_kifi_matrix(eye_to_world_guess)
+        out = np.zeros(16, np.float32)
+        check(_lib.load().kifi_icp_align(self._h, _ptr(d), C.byref(cam), _ptr(g), int(iterations),
+                                         _ptr(out)), "Align")
+        return out
+
+    def Result(self):
+        """(pose float (16,), pose double (16,), n_assoc per iteration, rms per iteration)."""
+        pf = np.zeros(16, np.float32)
+        pd = np.zeros(16, np.float64)
+        na = np.zeros(64, np.int32)
+        rms = np.zeros(64, np.float64)
+        it = C.c_int()
+        check(_lib.load().kifi_icp_result(self._h, _ptr(pf), _ptr(pd), _ptr(na), _ptr(rms), 64,
+                                          C.byref(it)), "Result")
+        n = min(it.value, 64)
+        return pf, pd, na[:n].copy(), rms[:n].copy()
+
+
+class Renderer:
+    """Renderer::Bin (Renderer.h:23-29)."""
+
+    def Bin(self, point_cloud, world_to_clip, width, height):
+        p = np.ascontiguousarray(point_cloud, dtype=np.float32).reshape(-1, 3)
+        m = as_kifi_matrix(world_to_clip)
+        out = np.zeros((height, width, 3), np.float32)
+        check(_lib.load().kifi_bin(_ptr(p), p.shape[0], _ptr(m), _ptr(out), int(width),
+                                   int(height)), "Bin")
+        return out
+
+
 def radix_sort(keys, values=None):
     """util::radix_sort on the GPU (algorithm.h:63-134)."""
     k = np.ascontiguousarray(keys, dtype=np.uint32).copy()
@@ -223,5 +307,5 @@ def radix_sort(keys, values=None):
     return k, v
 
 
-__all__ = ["DepthSensorParams", "Volume", "Integrator", "Mesher", "radix_sort", "KifiError",
-           "as_kifi_matrix"]
+__all__ = ["DepthSensorParams", "Volume", "Integrator", "Mesher", "ICP", "Renderer", "radix_sort",
+           "KifiError", "as_kifi_matrix"]

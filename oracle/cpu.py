@@ -184,3 +184,12 @@ def bin_points(points, world_to_clip, w, h):
     out = np.zeros((h, w, 3), np.float32)
     lib().or_bin(_p(pts), C.c_size_t(pts.size // 3), _p(w2c), _p(out), C.c_int(w), C.c_int(h))
     return out
+
+
+def backproject(depth, cam, eye_to_world):
+    """(h, w, 3) float32 world points of a frame; (0,0,0) where depth <= 0."""
+    d = f32(depth)
+    m = f32(eye_to_world)
+    out = np.zeros((cam[1], cam[0], 3), np.float32)
+    lib().or_backproject(_p(d), C.byref(cam_struct(cam)), _p(m), _p(out))
+    return out

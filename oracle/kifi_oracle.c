@@ -7,7 +7,7 @@
  * produce expected results.  The shipped library never links, loads or calls
  * it, and no product code path falls back to it.
  *
- * Parity is pinned: tests/test_oracle_vs_reference.py checks this file
+ * Parity is pinned: tests/test_oracle_pinned.py checks this file
  * bit-for-bit against the reference's own code compiled by
  * oracle/build_ref.py, and tests/golden/ holds fixtures generated from the
  * reference (tests/golden/make_golden.py).
@@ -709,6 +709,35 @@ void or_bin(const float* pts, size_t n, const float* world_to_clip, float* out, 
         }
     }
     free(zb);
+}
+
+/* World points of a depth frame (0,0,0 where there is no depth), with the
+ * back-projection arithmetic of DepthMap2PointCloud (Integrator.cpp:121-144)
+ * -- the target buffer for ICP between consecutive frames. */
+void or_backproject(const float* depth, const or_camera* cam, const float* eye_to_world,
+                    float* out) {
+    float fl_inv_x = 1.0f / cam->fx, fl_inv_y = 1.0f / cam->fy;
+    float pp_x = (0.5f - cam->cx) * fl_inv_x;
+    float pp_y = (cam->cy - 0.5f) * fl_inv_y;
+    for (int v = 0; v < cam->height; ++v) {
+        float row = 0.0f + -(float)v;
+        for (int u = 0; u < cam->width; ++u) {
+            size_t i = (size_t)v * cam->width + u;
+            float d = depth[i];
+            float w[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+            if (d > 0.0f) {
+                float p[4];
+                p[0] = ((float)u * fl_inv_x + pp_x) * d + 0.0f;
+                p[1] = (row * fl_inv_y + pp_y) * d + 0.0f;
+                p[2] = (-1.0f * 1.0f + 0.0f) * d + 0.0f;
+                p[3] = (0.0f * 1.0f + 0.0f) * d + 1.0f;
+                or_mat_vec(eye_to_world, p, w);
+            }
+            out[3 * i] = w[0];
+            out[3 * i + 1] = w[1];
+            out[3 * i + 2] = w[2];
+        }
+    }
 }
 
 /* kahan_sum<float> over a range -- numeric.h:52-74 */

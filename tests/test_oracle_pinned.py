@@ -8,13 +8,7 @@
 import numpy as np
 import pytest
 
-from tests.helpers import canon_bits, digest
-
-
-def posed(view, off):
-    v = view.copy()
-    v[12:15] += np.asarray(off, np.float32)
-    return v
+from tests.helpers import canon_bits, digest, posed
 
 
 def test_oracle_matches_golden_integration_and_mesh(oracle_cpu, golden):
@@ -134,5 +128,36 @@ def test_oracle_icp_matches_reference_on_sphere(oracle_cpu, oracle_ref):
     guess = seq.eye_to_world_f32(0)  # previous pose as the initial guess
     r = oracle_ref.icp_align(seq.depth_m(1), cam, guess, target, seq.eye_to_world_f32(0), 10)
     o, od, n = oracle_cpu.icp_align(seq.depth_m(1), cam, guess, target, seq.eye_to_world_f32(0), 10)
+    assert n > 100
+    assert np.abs(r - o).max() < 1e-5
+
+
+def test_oracle_bin_matches_reference(oracle_cpu, oracle_ref, golden):
+    # Renderer::Bin of the fixture's mesh vertices through the frame's camera,
+    # into the 1024x768 buffer Pipeline uses (Pipeline.cpp:48-52)
+    depth, view, cam = golden["depth"], golden["view"], golden["camera"]
+    vol = oracle_cpu.Volume(256, 2.0, 0.02)
+    vol.integrate(depth, cam, view)
+    verts, _ = vol.mesh(False)
+    w2c = oracle_cpu.mat_mul(oracle_cpu.eye_to_clip(cam), view)
+    for w, h in ((1024, 768), (640, 480), (97, 61)):
+        a = oracle_cpu.bin_points(verts, w2c, w, h)
+        b = oracle_ref.bin_points(verts, w2c, w, h)
+        assert np.array_equal(canon_bits(a), canon_bits(b))
+        assert (a != 0).any()
+
+
+def test_oracle_icp_on_bin_target_matches_reference(oracle_cpu, oracle_ref, golden):
+    # the reference's intended pipeline (Pipeline.cpp:36-55): mesh -> Bin -> ICP
+    depth, view, cam = golden["depth"], golden["view"], golden["camera"]
+    vol = oracle_cpu.Volume(256, 2.0, 0.02)
+    vol.integrate(depth, cam, view)
+    verts, _ = vol.mesh(False)
+    w2c = oracle_cpu.mat_mul(oracle_cpu.eye_to_clip(cam), view)
+    target = oracle_cpu.bin_points(verts, w2c, 1024, 768)
+    e2w = oracle_cpu.invert_transform(view)
+    guess = posed(e2w, (0.004, -0.003, 0.002))
+    r = oracle_ref.icp_align(depth, cam, guess, target, e2w, 5)
+    o, od, n = oracle_cpu.icp_align(depth, cam, guess, target, e2w, 5)
     assert n > 100
     assert np.abs(r - o).max() < 1e-5
