@@ -160,6 +160,29 @@ KIFI_API kifi_status kifi_mesh(kifi_volume* vol, int with_indices, float* verts,
                       uint32_t* indices, size_t index_capacity, size_t* n_verts,
                       size_t* n_indices);
 
+/* Mesher::Mesh into device memory owned by the volume: the same output as
+ * kifi_mesh, left on the GPU.  *verts_dev / *indices_dev stay valid until
+ * the next mesh call on the volume or its destruction.  Either pointer
+ * argument may be NULL. */
+KIFI_API kifi_status kifi_mesh_device(kifi_volume* vol, int with_indices, size_t* n_verts,
+                                      size_t* n_indices, const float** verts_dev,
+                                      const uint32_t** indices_dev);
+
+/* Stage timers, the GPU counterpart of the stop_watch the reference wires
+ * into Integrator::Integrate (Integrator.cpp:45-70, "tmerge"/"tupd"): while
+ * on, every integrated frame records CUDA events around splat+emit, the sort
+ * of the new keys, and the fused merge+update.  kifi_volume_stage_times
+ * waits for them, returns the summed milliseconds of the three stages and
+ * the number of frames, and resets the accumulation. */
+KIFI_API kifi_status kifi_volume_set_profiling(kifi_volume* vol, int on);
+KIFI_API kifi_status kifi_volume_stage_times(kifi_volume* vol, double out_ms[3], int* frames);
+
+/* Sizes of the most recent merges (up to 64, oldest first): resident voxels
+ * before, keys new to the volume, resident voxels after.  No reference
+ * counterpart; it sizes the bytes each merge moves. */
+KIFI_API kifi_status kifi_volume_frame_log(kifi_volume* vol, uint64_t* n_before, uint64_t* n_new,
+                                           uint64_t* n_after, int capacity, int* count);
+
 /* kifi::util::radix_sort(T* first, T* last, void* scratch)
  * (KinectFission/kifi/util/algorithm.h:63-91) on the GPU: stable LSD sort of
  * n 32-bit keys held in host memory, in place. */
@@ -223,6 +246,56 @@ KIFI_API kifi_status kifi_icp_result(kifi_icp* icp, float out_eye_to_world[16],
  * (0,0,0). */
 KIFI_API kifi_status kifi_bin(const float* points, size_t n, const float world_to_clip[16],
                               float* out, int width, int height);
+
+/* ------------------------------------------------------------ pipeline */
+
+/* Arguments of kifi::Pipeline::Pipeline(cameraParams, volumeResolution,
+ * volumeSideLength, truncationMargin) (KinectFission/kifi/Pipeline.h:19-26)
+ * plus the tracking and meshing cadence. */
+typedef struct kifi_pipeline_desc {
+    kifi_camera camera;
+    int resolution;
+    float side_length_m;
+    float truncation_m;
+    int icp_iterations;     /* ICP iterations per frame against the previous frame; 0 = off */
+    int mesh_every;         /* extract the mesh every N frames (device-resident); 0 = never */
+    int mesh_with_indices;  /* Mesh(verts, indices) rather than Mesh(verts) */
+    size_t initial_capacity;
+    int device;
+} kifi_pipeline_desc;
+
+typedef struct kifi_pipeline kifi_pipeline;
+
+KIFI_API kifi_status kifi_pipeline_create(const kifi_pipeline_desc* desc, kifi_pipeline** out);
+KIFI_API kifi_status kifi_pipeline_destroy(kifi_pipeline* p);
+KIFI_API kifi_volume* kifi_pipeline_volume(kifi_pipeline* p);
+KIFI_API kifi_icp* kifi_pipeline_icp(kifi_pipeline* p);
+
+/* kifi::Pipeline::Integrate(rawDepthMap, worldToEye) (Pipeline.h:31-35,
+ * Pipeline.cpp:26-56): fuses the frame with its given pose (the live path,
+ * :32-35) and, when icp_iterations > 0, tracks it by ICP against the
+ * previous frame's back-projection with the previous pose as the guess (the
+ * reference's tracking path, :36-55); every mesh_every frames the mesh is
+ * extracted on the device.  Host frame (uint16 mm or float m); returns when
+ * done, with the tracked eye-to-world pose in out_eye_to_world (the given
+ * pose's inverse for the first frame or when tracking is off; may be NULL). */
+KIFI_API kifi_status kifi_pipeline_integrate(kifi_pipeline* p, const void* depth_host,
+                                             int depth_is_u16, const float world_to_eye[16],
+                                             float out_eye_to_world[16]);
+
+/* Same with the frame in device memory; asynchronous (the frame must stay
+ * valid until the next kifi_pipeline_sync). */
+KIFI_API kifi_status kifi_pipeline_integrate_device(kifi_pipeline* p, const void* depth_dev,
+                                                    int depth_is_u16,
+                                                    const float world_to_eye[16]);
+
+/* Waits for all queued frames; reports device errors and the last tracked
+ * pose (may be NULL). */
+KIFI_API kifi_status kifi_pipeline_sync(kifi_pipeline* p, float out_eye_to_world[16]);
+
+/* Vertex and index counts of the last mesh the pipeline extracted. */
+KIFI_API kifi_status kifi_pipeline_mesh_counts(kifi_pipeline* p, size_t* n_verts,
+                                               size_t* n_indices);
 
 #ifdef __cplusplus
 }

@@ -29,6 +29,13 @@ class Camera(C.Structure):
                 ("zfar_m", C.c_float)]
 
 
+class PipelineDesc(C.Structure):
+    _fields_ = [("camera", Camera), ("resolution", C.c_int), ("side_length_m", C.c_float),
+                ("truncation_m", C.c_float), ("icp_iterations", C.c_int), ("mesh_every", C.c_int),
+                ("mesh_with_indices", C.c_int), ("initial_capacity", C.c_size_t),
+                ("device", C.c_int)]
+
+
 class VolumeDesc(C.Structure):
     _fields_ = [("resolution", C.c_int), ("side_length_m", C.c_float),
                 ("truncation_m", C.c_float), ("initial_capacity", C.c_size_t),
@@ -71,6 +78,21 @@ SIGNATURES = {
     "kifi_icp_result": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                   C.c_int, C.POINTER(C.c_int)]),
     "kifi_bin": (C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
+    "kifi_mesh_device": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_size_t),
+                                   C.POINTER(C.c_size_t), C.c_void_p, C.c_void_p]),
+    "kifi_volume_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
+    "kifi_volume_stage_times": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int)]),
+    "kifi_volume_frame_log": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                        C.POINTER(C.c_int)]),
+    "kifi_pipeline_create": (C.c_int, [C.POINTER(PipelineDesc), C.POINTER(C.c_void_p)]),
+    "kifi_pipeline_destroy": (C.c_int, [C.c_void_p]),
+    "kifi_pipeline_volume": (C.c_void_p, [C.c_void_p]),
+    "kifi_pipeline_icp": (C.c_void_p, [C.c_void_p]),
+    "kifi_pipeline_integrate": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "kifi_pipeline_integrate_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
+    "kifi_pipeline_sync": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "kifi_pipeline_mesh_counts": (C.c_int, [C.c_void_p, C.POINTER(C.c_size_t),
+                                            C.POINTER(C.c_size_t)]),
 }
 
 _lib = None

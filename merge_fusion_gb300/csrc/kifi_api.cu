@@ -50,28 +50,6 @@ bool is_pow2(int x) { return x > 0 && !(x & (x - 1)); }
 
 }  // namespace
 
-struct kifi_volume {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    bool own_stream = false;
-    Geom g{};
-    DeviceCtl* ctl = nullptr;       // device
-    DeviceCtl* ctl_host = nullptr;  // pinned mirror for read-backs
-    VolumeBuffers vb{};
-    SortScratch ss{};
-    MeshScratch ms{};
-    LaunchShape ls{};
-    void* depth_dev = nullptr;
-    size_t depth_dev_bytes = 0;
-    void* depth_pinned = nullptr;
-    size_t depth_pinned_bytes = 0;
-    size_t n_upper = 0;  // upper bound of the resident count of queued work
-    float* mesh_verts = nullptr;
-    size_t mesh_verts_cap = 0;
-    uint32_t* mesh_idx = nullptr;
-    size_t mesh_idx_cap = 0;
-};
-
 namespace {
 
 void free_volume_buffers(VolumeBuffers& vb) {
@@ -213,13 +191,36 @@ kifi_status integrate_sync(kifi_volume* v, const void* host_depth, bool u16,
     if (s) return s;
     const size_t bytes = (size_t)cam->width * cam->height * (u16 ? 2 : 4);
     if ((s = upload_depth(v, host_depth, bytes))) return s;
-    KIFI_CUDA(integrate_enqueue(v->ctl, v->g, v->vb, v->ss, v->depth_dev, u16, nullptr, *cam,
-                                load_mat(w2e), v->ls, v->stream));
+    if ((s = kifi_volume_enqueue_frame(v, v->depth_dev, u16, cam, w2e))) return s;
     if ((s = read_ctl(v))) return s;
     return take_device_status(v);
 }
 
 }  // namespace
+
+kifi_status kifi_volume_enqueue_frame(kifi_volume* v, const void* depth_dev, bool u16,
+                                      const kifi_camera* cam, const float* w2e) {
+    cudaEvent_t* ev = nullptr;
+    std::array<cudaEvent_t, 4> evs{};
+    if (v->profiling) {
+        for (int k = 0; k < 4; ++k) {
+            if (v->event_pool.empty()) {
+                cudaEvent_t e;
+                KIFI_CUDA(cudaEventCreate(&e));
+                v->event_pool.push_back(e);
+            }
+            evs[k] = v->event_pool.back();
+            v->event_pool.pop_back();
+        }
+        ev = evs.data();
+    }
+    cudaError_t e = integrate_enqueue(v->ctl, v->g, v->vb, v->ss, depth_dev, u16, *cam,
+                                      load_mat(w2e), v->ls, v->stream, ev);
+    if (ev) v->pending.push_back(evs);
+    if (e != cudaSuccess) return cuda_fail(e, "integrate");
+    v->n_upper += 8 * (size_t)cam->width * cam->height;
+    return KIFI_OK;
+}
 
 extern "C" {
 
@@ -325,6 +326,9 @@ kifi_status kifi_volume_destroy(kifi_volume* v) {
     cudaFreeHost(v->depth_pinned);
     cudaFree(v->mesh_verts);
     cudaFree(v->mesh_idx);
+    for (auto e : v->event_pool) cudaEventDestroy(e);
+    for (auto& ev : v->pending)
+        for (auto e : ev) cudaEventDestroy(e);
     if (v->own_stream && v->stream) cudaStreamDestroy(v->stream);
     delete v;
     return KIFI_OK;
@@ -444,16 +448,56 @@ kifi_status kifi_integrate_device(kifi_volume* v, const void* depth_dev, int dep
     KIFI_CUDA(cudaSetDevice(v->device));
     kifi_status s = frame_prologue(v, cam);
     if (s) return s;
-    KIFI_CUDA(integrate_enqueue(v->ctl, v->g, v->vb, v->ss, depth_dev, depth_is_u16 != 0, nullptr,
-                                *cam, load_mat(world_to_eye), v->ls, v->stream));
-    v->n_upper += 8 * (size_t)cam->width * cam->height;
+    return kifi_volume_enqueue_frame(v, depth_dev, depth_is_u16 != 0, cam, world_to_eye);
+}
+
+kifi_status kifi_volume_set_profiling(kifi_volume* v, int on) {
+    if (!v) return fail(KIFI_ERR_INVALID_ARGUMENT, "null volume");
+    v->profiling = on != 0;
     return KIFI_OK;
 }
 
-kifi_status kifi_mesh(kifi_volume* v, int with_indices, float* verts, size_t vert_capacity,
-                      uint32_t* indices, size_t index_capacity, size_t* n_verts,
-                      size_t* n_indices) {
-    if (!v || !n_verts || !n_indices) return fail(KIFI_ERR_INVALID_ARGUMENT, "null argument");
+kifi_status kifi_volume_stage_times(kifi_volume* v, double out_ms[3], int* frames) {
+    if (!v || !out_ms) return fail(KIFI_ERR_INVALID_ARGUMENT, "null argument");
+    KIFI_CUDA(cudaSetDevice(v->device));
+    out_ms[0] = out_ms[1] = out_ms[2] = 0.0;
+    const int n = (int)v->pending.size();
+    for (auto& ev : v->pending) {
+        KIFI_CUDA(cudaEventSynchronize(ev[3]));
+        for (int k = 0; k < 3; ++k) {
+            float ms = 0.0f;
+            KIFI_CUDA(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
+            out_ms[k] += ms;
+        }
+        for (int k = 0; k < 4; ++k) v->event_pool.push_back(ev[k]);
+    }
+    v->pending.clear();
+    if (frames) *frames = n;
+    return KIFI_OK;
+}
+
+kifi_status kifi_volume_frame_log(kifi_volume* v, uint64_t* n_before, uint64_t* n_new,
+                                  uint64_t* n_after, int capacity, int* count) {
+    if (!v || !count) return fail(KIFI_ERR_INVALID_ARGUMENT, "null argument");
+    kifi_status s = kifi_volume_sync(v);
+    if (s) return s;
+    const DeviceCtl* h = v->ctl_host;
+    const unsigned long long total = h->frames;
+    int n = (int)(total < (unsigned long long)kFrameLog ? total : kFrameLog);
+    if (n > capacity) n = capacity;
+    for (int i = 0; i < n; ++i) {
+        const unsigned int slot = (unsigned int)((total - n + i) % kFrameLog);
+        if (n_before) n_before[i] = h->log_n0[slot];
+        if (n_new) n_new[i] = h->log_new[slot];
+        if (n_after) n_after[i] = h->log_n1[slot];
+    }
+    *count = n;
+    return KIFI_OK;
+}
+
+// Meshes into the volume's device buffers; returns the counts.
+static kifi_status mesh_to_device(kifi_volume* v, int with_indices, size_t* n_verts,
+                                  size_t* n_indices) {
     *n_verts = *n_indices = 0;
     kifi_status s = kifi_volume_sync(v);
     if (s) return s;
@@ -464,14 +508,11 @@ kifi_status kifi_mesh(kifi_volume* v, int with_indices, float* verts, size_t ver
     KIFI_CUDA(mesh_scratch_reserve(&v->ms, n));
     KIFI_CUDA(mesh_count_enqueue(v->vb.keys[cur], v->vb.vals[cur], n, with_indices ? 1 : 0, v->ms,
                                  v->ls.sms, v->stream));
-    MeshCounts mc;
-    KIFI_CUDA(cudaMemcpyAsync(&mc, v->ms.counts, sizeof mc, cudaMemcpyDeviceToHost, v->stream));
+    MeshCounts* mc = &v->ctl_host_mesh;
+    KIFI_CUDA(cudaMemcpyAsync(mc, v->ms.counts, sizeof(MeshCounts), cudaMemcpyDeviceToHost,
+                              v->stream));
     KIFI_CUDA(cudaStreamSynchronize(v->stream));
-    const size_t nv = (size_t)mc.n_verts, ni = with_indices ? (size_t)mc.n_idx : 0;
-    *n_verts = nv;
-    *n_indices = ni;
-    if (nv > vert_capacity || ni > index_capacity || (nv && !verts) || (ni && !indices))
-        return fail(KIFI_ERR_CAPACITY, "mesh output buffers too small");
+    const size_t nv = (size_t)mc->n_verts, ni = with_indices ? (size_t)mc->n_idx : 0;
     if (nv > v->mesh_verts_cap) {
         cudaFree(v->mesh_verts);
         v->mesh_verts = nullptr;
@@ -490,19 +531,48 @@ kifi_status kifi_mesh(kifi_volume* v, int with_indices, float* verts, size_t ver
                                 v->ms, nv, ni, 0xffffffffu, v->mesh_verts, v->mesh_idx, v->ls.sms,
                                 v->stream));
     if (with_indices) {
-        unsigned int missing = 0;
-        KIFI_CUDA(cudaMemcpyAsync(&missing, &v->ms.counts->missing_min, 4, cudaMemcpyDeviceToHost,
-                                  v->stream));
+        KIFI_CUDA(cudaMemcpyAsync(&mc->missing_min, &v->ms.counts->missing_min, 4,
+                                  cudaMemcpyDeviceToHost, v->stream));
         KIFI_CUDA(cudaStreamSynchronize(v->stream));
-        if (missing != 0xffffffffu)
+        if (mc->missing_min != 0xffffffffu)
             KIFI_CUDA(mesh_emit_enqueue(v->g, v->vb.keys[cur], v->vb.vals[cur], n, 1, v->ms, nv, ni,
-                                        missing, v->mesh_verts, v->mesh_idx, v->ls.sms, v->stream));
+                                        mc->missing_min, v->mesh_verts, v->mesh_idx, v->ls.sms,
+                                        v->stream));
     }
+    *n_verts = nv;
+    *n_indices = ni;
+    v->mesh_counts_valid = true;
+    return KIFI_OK;
+}
+
+kifi_status kifi_mesh(kifi_volume* v, int with_indices, float* verts, size_t vert_capacity,
+                      uint32_t* indices, size_t index_capacity, size_t* n_verts,
+                      size_t* n_indices) {
+    if (!v || !n_verts || !n_indices) return fail(KIFI_ERR_INVALID_ARGUMENT, "null argument");
+    KIFI_CUDA(cudaSetDevice(v->device));
+    size_t nv = 0, ni = 0;
+    kifi_status s = mesh_to_device(v, with_indices, &nv, &ni);
+    *n_verts = nv;
+    *n_indices = ni;
+    if (s) return s;
+    if (nv > vert_capacity || ni > index_capacity || (nv && !verts) || (ni && !indices))
+        return fail(KIFI_ERR_CAPACITY, "mesh output buffers too small");
     if (nv)
         KIFI_CUDA(cudaMemcpyAsync(verts, v->mesh_verts, nv * 12, cudaMemcpyDeviceToHost, v->stream));
     if (ni)
         KIFI_CUDA(cudaMemcpyAsync(indices, v->mesh_idx, ni * 4, cudaMemcpyDeviceToHost, v->stream));
     KIFI_CUDA(cudaStreamSynchronize(v->stream));
+    return KIFI_OK;
+}
+
+kifi_status kifi_mesh_device(kifi_volume* v, int with_indices, size_t* n_verts, size_t* n_indices,
+                             const float** verts_dev, const uint32_t** indices_dev) {
+    if (!v || !n_verts || !n_indices) return fail(KIFI_ERR_INVALID_ARGUMENT, "null argument");
+    KIFI_CUDA(cudaSetDevice(v->device));
+    kifi_status s = mesh_to_device(v, with_indices, n_verts, n_indices);
+    if (s) return s;
+    if (verts_dev) *verts_dev = v->mesh_verts;
+    if (indices_dev) *indices_dev = v->mesh_idx;
     return KIFI_OK;
 }
 

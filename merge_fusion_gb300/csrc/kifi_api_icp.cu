@@ -29,8 +29,8 @@ struct kifi_icp {
 namespace {
 
 int icp_ctas(const kifi_icp* c, size_t n_src) {
-    size_t b = (n_src + 255) / 256;
-    size_t cap = (size_t)c->ls.sms * 2;
+    size_t b = (n_src + 7) / 8;  // association: one warp per source, 8 warps per CTA
+    size_t cap = (size_t)c->ls.sms * 8;
     if (cap > (size_t)kIcpMaxCtas) cap = kIcpMaxCtas;
     return (int)(b < 1 ? 1 : (b > cap ? cap : b));
 }

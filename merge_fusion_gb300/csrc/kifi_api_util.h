@@ -2,7 +2,9 @@
 // units (kifi_api.cu, kifi_api_icp.cu).
 #pragma once
 
+#include <array>
 #include <string>
+#include <vector>
 
 #include "kifi_internal.h"
 
@@ -26,6 +28,41 @@ inline Mat4 load_mat(const float* m) {
 }
 
 }  // namespace kifi
+
+// A volume handle (include/kifi_gpu.h): device state of one kifi::Volume.
+struct kifi_volume {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    kifi::Geom g{};
+    kifi::DeviceCtl* ctl = nullptr;       // device
+    kifi::DeviceCtl* ctl_host = nullptr;  // pinned mirror for read-backs
+    kifi::VolumeBuffers vb{};
+    kifi::SortScratch ss{};
+    kifi::MeshScratch ms{};
+    kifi::LaunchShape ls{};
+    void* depth_dev = nullptr;
+    size_t depth_dev_bytes = 0;
+    void* depth_pinned = nullptr;
+    size_t depth_pinned_bytes = 0;
+    size_t n_upper = 0;  // upper bound of the resident count of queued work
+    float* mesh_verts = nullptr;
+    size_t mesh_verts_cap = 0;
+    uint32_t* mesh_idx = nullptr;
+    size_t mesh_idx_cap = 0;
+    kifi::MeshCounts ctl_host_mesh{};
+    bool mesh_counts_valid = false;
+    // stage timers (kifi_volume_set_profiling): per integrated frame four
+    // events around splat+emit, sort and merge+update
+    bool profiling = false;
+    std::vector<cudaEvent_t> event_pool;
+    std::vector<std::array<cudaEvent_t, 4>> pending;
+};
+
+// integrate entry shared by the ABI translation units: enqueues one frame
+// (device depth) on the volume's stream, growing buffers first when needed.
+kifi_status kifi_volume_enqueue_frame(kifi_volume* v, const void* depth_dev, bool u16,
+                                      const kifi_camera* cam, const float* world_to_eye);
 
 #define KIFI_CUDA(call)                                                 \
     do {                                                                \

@@ -172,8 +172,11 @@ struct DeviceCtl {
     unsigned long long sort_epoch; // generation tag of the sort look-back words
     unsigned int tile_counter[8];  // dynamic tile ids (one per sort pass / merge)
     FrameConst fc;                 // constants of the frame being integrated
-    unsigned long long frames;     // frames integrated
+    unsigned long long frames;     // merges committed (frames integrated + inserts)
+    // sizes of the last kFrameLog merges: resident before, new, resident after
+    unsigned long long log_n0[64], log_new[64], log_n1[64];
 };
+constexpr int kFrameLog = 64;
 
 // status bits raised on the device (reported through kifi_volume_sync)
 enum : unsigned int {

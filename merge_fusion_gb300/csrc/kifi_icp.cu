@@ -116,18 +116,38 @@ __device__ __forceinline__ bool last_cta(unsigned int* counter) {
     return last;
 }
 
+// Sums the per-CTA partials of NV components (thread c sums component c in
+// CTA order, so the result does not depend on scheduling) into out[].
+template <int NV>
+__device__ __forceinline__ void finish_partials(const IcpState* st, double* out) {
+    if (threadIdx.x < NV) {
+        double a = 0.0;
+        for (unsigned int b = 0; b < gridDim.x; ++b) a += st->part[b * 16 + threadIdx.x];
+        out[threadIdx.x] = a;
+    }
+    __syncthreads();
+}
+
+// One warp per source pixel: the lanes split the 21x21 window and the
+// nearest candidate is chosen by a lexicographic (len^2, scan position)
+// minimum, which is the reference's "first strict minimum in row-major scan
+// order" (ICP.cpp:108-125).
 __global__ void __launch_bounds__(kThreads) k_icp_associate(IcpArgs a, IcpState* __restrict__ st) {
     const int n_cols = (a.width + 3) / 4;
     const int n_src = n_cols * a.height;
-    const float* pose = st->pose_f;
-    // counts, src xyzw, dst xyz, sum of min len^2
+    const int lane = threadIdx.x & 31;
+    const int warps = gridDim.x * (kThreads / 32);
+    float pose[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) pose[i] = st->pose_f[i];
+    // counts, src xyzw, dst xyz, sum of min len^2 (lane 0 of each warp)
     KahanF acc[9];
     const float half_w = fmul((float)a.synth_w, 0.5f), half_h = fmul((float)a.synth_h, 0.5f);
     const size_t n_synth = (size_t)a.synth_w * a.synth_h;
-    for (int s = blockIdx.x * kThreads + threadIdx.x; s < n_src; s += gridDim.x * kThreads) {
+    for (int s = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5); s < n_src; s += warps) {
         const int y = s / n_cols, x = (s - y * n_cols) * 4;
-        float4 p1 = make_float4(0.f, 0.f, 0.f, 0.f), p2 = make_float4(0.f, 0.f, 0.f, 0.f);
         const float d = load_depth(a.depth, (size_t)y * a.width + x, a.depth_u16);
+        float4 p1 = make_float4(0.f, 0.f, 0.f, 0.f), p2 = make_float4(0.f, 0.f, 0.f, 0.f);
         if (0.0f != d) {
             float pt[4];
             pt[0] = fmul(fadd(fmul((float)x, a.fl_inv_x), a.pp_x), d);
@@ -142,48 +162,74 @@ __global__ void __launch_bounds__(kThreads) k_icp_associate(IcpArgs a, IcpState*
             int v = wrap_sub(wrap_sub(a.synth_h - 1, cvt_i32_x86(fadd(fmul(uy, half_h), half_h))), 10);
             u = max(0, u);
             v = max(0, v);
-            float mind = 0.01f;
-            float3 best = make_float3(0.f, 0.f, 0.f);
-            const int yend = (int)min(480ll, (long long)v + 21), xend = (int)min(640ll, (long long)u + 21);
+            const int nr = (int)min(480ll, (long long)v + 21) - v;
+            const int nc = (int)min(640ll, (long long)u + 21) - u;
             const float dw = fsub(1.0f, wp[3]);
             const float dw2 = fmul(dw, dw);
-            for (int y1 = v; y1 < yend; ++y1) {
-                const size_t row = (size_t)y1 * a.synth_w;
-                for (int x1 = u; x1 < xend; ++x1) {
-                    const size_t at = row + x1;
-                    if (at >= n_synth) continue;
-                    const float* q = a.synth + 3 * at;
-                    const float qx = __ldg(q), qy = __ldg(q + 1), qz = __ldg(q + 2);
-                    if (qx == 0.0f && qy == 0.0f && qz == 0.0f) continue;
-                    const float dx = fsub(qx, wp[0]), dy = fsub(qy, wp[1]), dz = fsub(qz, wp[2]);
-                    const float l2 = fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fadd(fmul(dz, dz), dw2));
-                    if (l2 < mind) {
-                        mind = l2;
-                        best = make_float3(qx, qy, qz);
+            float best = 0.01f;
+            int best_i = 0x7fffffff;
+            if (nr > 0 && nc > 0) {
+                const int total = nr * nc;
+                int r = lane / nc, c = lane - (lane / nc) * nc;
+                const int step_r = 32 / nc, step_c = 32 - step_r * nc;
+                for (int i = lane; i < total; i += 32) {
+                    const size_t at = (size_t)(v + r) * a.synth_w + (u + c);
+                    if (at < n_synth) {
+                        const float* q = a.synth + 3 * at;
+                        const float qx = __ldg(q), qy = __ldg(q + 1), qz = __ldg(q + 2);
+                        if (!(qx == 0.0f && qy == 0.0f && qz == 0.0f)) {
+                            const float dx = fsub(qx, wp[0]), dy = fsub(qy, wp[1]), dz = fsub(qz, wp[2]);
+                            const float l2 = fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fadd(fmul(dz, dz), dw2));
+                            if (l2 < best) {  // scan order within the lane is increasing
+                                best = l2;
+                                best_i = i;
+                            }
+                        }
+                    }
+                    r += step_r;
+                    c += step_c;
+                    if (c >= nc) {
+                        c -= nc;
+                        ++r;
                     }
                 }
             }
-            if (mind < 0.01f) {
+            // lexicographic (len^2, scan index) minimum over the warp
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, best_i, o);
+                if (ob < best || (ob == best && oi < best_i)) {
+                    best = ob;
+                    best_i = oi;
+                }
+            }
+            if (best_i != 0x7fffffff) {
+                const int br = best_i / nc, bc = best_i - br * nc;
+                const float* q = a.synth + 3 * ((size_t)(v + br) * a.synth_w + (u + bc));
                 p1 = make_float4(wp[0], wp[1], wp[2], wp[3]);
-                p2 = make_float4(best.x, best.y, best.z, 1.0f);
-                acc[0].add(1.0f);
-                acc[1].add(p1.x); acc[2].add(p1.y); acc[3].add(p1.z); acc[4].add(p1.w);
-                acc[5].add(p2.x); acc[6].add(p2.y); acc[7].add(p2.z);
-                acc[8].add(mind);
+                p2 = make_float4(__ldg(q), __ldg(q + 1), __ldg(q + 2), 1.0f);
+                if (lane == 0) {
+                    acc[0].add(1.0f);
+                    acc[1].add(p1.x); acc[2].add(p1.y); acc[3].add(p1.z); acc[4].add(p1.w);
+                    acc[5].add(p2.x); acc[6].add(p2.y); acc[7].add(p2.z);
+                    acc[8].add(best);
+                }
             }
         }
-        a.src[s] = p1;
-        a.dst[s] = p2;  // w = 1 marks an association
+        if (lane == 0) {
+            a.src[s] = p1;
+            a.dst[s] = p2;  // w = 1 marks an association
+        }
     }
     double part[9];
     block_reduce<9>(acc, part);
     if (threadIdx.x == 0)
         for (int i = 0; i < 9; ++i) st->part[blockIdx.x * 16 + i] = part[i];
     if (!last_cta(&st->done)) return;
+    __shared__ double tot[9];
+    finish_partials<9>(st, tot);
     if (threadIdx.x == 0) {
-        double tot[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-        for (unsigned int b = 0; b < gridDim.x; ++b)
-            for (int i = 0; i < 9; ++i) tot[i] += st->part[b * 16 + i];
         const int n = (int)(tot[0] + 0.5);
         const float nf = (float)n;
         // srcMedianSum / float4(n) (ICP.cpp:166-167)
@@ -278,10 +324,9 @@ __global__ void __launch_bounds__(kThreads) k_icp_horn(IcpArgs a, IcpState* __re
     if (threadIdx.x == 0)
         for (int i = 0; i < 9; ++i) st->part[blockIdx.x * 16 + i] = part[i];
     if (!last_cta(&st->done)) return;
+    __shared__ double S[9];
+    finish_partials<9>(st, S);
     if (threadIdx.x != 0) return;
-    double S[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (unsigned int b = 0; b < gridDim.x; ++b)
-        for (int i = 0; i < 9; ++i) S[i] += st->part[b * 16 + i];
     const double Sxx = S[0], Sxy = S[1], Sxz = S[2], Syx = S[3], Syy = S[4], Syz = S[5],
                  Szx = S[6], Szy = S[7], Szz = S[8];
     // Horn's N (ICP.cpp:199-213), symmetric

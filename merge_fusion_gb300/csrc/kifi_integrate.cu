@@ -328,6 +328,10 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_update(DeviceCtl* __res
             ctl->n[out] = N1;
             ctl->cur = out;
             ctl->tile_counter[7] = 0u;
+            const unsigned int slot = (unsigned int)(ctl->frames % kFrameLog);
+            ctl->log_n0[slot] = N0;
+            ctl->log_new[slot] = e;
+            ctl->log_n1[slot] = N1;
             ctl->frames += 1ull;
             __threadfence();
         }
@@ -372,9 +376,10 @@ __global__ void k_reset_new(DeviceCtl* ctl) {
 }  // namespace
 
 cudaError_t integrate_enqueue(DeviceCtl* ctl, const Geom& g, VolumeBuffers& vb, SortScratch& ss,
-                              const void* depth_dev, bool depth_u16, float* /*depth_f32_dev*/,
-                              const kifi_camera& cam, const Mat4& world_to_eye,
-                              const LaunchShape& ls, cudaStream_t st) {
+                              const void* depth_dev, bool depth_u16, const kifi_camera& cam,
+                              const Mat4& world_to_eye, const LaunchShape& ls, cudaStream_t st,
+                              cudaEvent_t* events) {
+    if (events) cudaEventRecord(events[0], st);
     k_frame_setup<<<1, 32, 0, st>>>(ctl, cam, world_to_eye, g.res);
     const unsigned int new_cap = (unsigned int)vb.new_cap;
     if (depth_u16)
@@ -383,13 +388,16 @@ cudaError_t integrate_enqueue(DeviceCtl* ctl, const Geom& g, VolumeBuffers& vb, 
     else
         k_splat_emit<false><<<ls.splat_ctas, kEmitThreads, 0, st>>>(ctl, g, depth_dev, vb.bitmap,
                                                                     vb.new_keys, new_cap);
+    if (events) cudaEventRecord(events[1], st);
     cudaError_t e = sort_u32(vb.new_keys, nullptr, &ctl->n_new, ss, &ctl->status, ls.sort_ctas, st);
     if (e != cudaSuccess) return e;
+    if (events) cudaEventRecord(events[2], st);
     MergeInputs in{vb.new_keys, nullptr, nullptr, &ctl->n_new, true};
     if (depth_u16)
         k_merge_update<true><<<ls.merge_ctas, kMergeThreads, 0, st>>>(ctl, g, vb, in, depth_dev);
     else
         k_merge_update<false><<<ls.merge_ctas, kMergeThreads, 0, st>>>(ctl, g, vb, in, depth_dev);
+    if (events) cudaEventRecord(events[3], st);
     return cudaGetLastError();
 }
 

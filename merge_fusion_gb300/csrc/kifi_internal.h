@@ -50,10 +50,12 @@ struct LaunchShape {
 
 // Enqueues one Integrator::Integrate on `st`.  depth_dev holds the frame
 // (float metres, or uint16 millimetres when depth_u16).
+// `events` (optional, 4 entries) are recorded before the frame set-up, after
+// splat+emit, after the sort and after merge+update.
 cudaError_t integrate_enqueue(DeviceCtl* ctl, const Geom& g, VolumeBuffers& vb, SortScratch& ss,
-                              const void* depth_dev, bool depth_u16, float* depth_f32_dev,
-                              const kifi_camera& cam, const Mat4& world_to_eye,
-                              const LaunchShape& ls, cudaStream_t st);
+                              const void* depth_dev, bool depth_u16, const kifi_camera& cam,
+                              const Mat4& world_to_eye, const LaunchShape& ls, cudaStream_t st,
+                              cudaEvent_t* events);
 
 // flat_map::insert of n sorted unique device keys: filter out resident keys
 // (their values win) and collect (key, index) of the rest in new_keys /

@@ -217,3 +217,106 @@ def room_scene(n_frames=300, seed=0, width=640, height=480, f=585.0, scale=1.0, 
         rng = np.random.default_rng([seed, first_frame + i])
         frames.append(_render(rays, pose, layout, rng, 0.4, 4.0, dropout))
     return Sequence(width, height, fx, fy, cx, cy, 0.4, 4.0, frames, poses)
+
+
+# ------------------------------------------------------------ torch renderer
+# Input generation for long sequences (benchmarks): the same scenes and
+# trajectories ray-cast with torch, on the GPU or the CPU.  Noise and
+# dropout come from a counter-based integer hash, so the random stream is
+# the same on either device.
+
+def _hash32(x):
+    """lowbias32-style integer hash of int64 tensors holding 32-bit values."""
+    def mul32(a, m):
+        lo = a & 0xFFFF
+        hi = a >> 16
+        return (lo * m + (((hi * m) & 0xFFFF) << 16)) & 0xFFFFFFFF
+    x = x & 0xFFFFFFFF
+    x = x ^ (x >> 16)
+    x = mul32(x, 0x7FEB352D)
+    x = x ^ (x >> 15)
+    x = mul32(x, 0x846CA68B)
+    x = x ^ (x >> 16)
+    return x
+
+
+def _uniform(torch, seed, frame, pix, stream):
+    key = _hash32(pix + _hash32(torch.full_like(pix, (seed * 7919 + frame * 104729 + stream * 31337)
+                                                & 0xFFFFFFFF)))
+    return (key.to(torch.float32) + 0.5) * (1.0 / 4294967296.0)
+
+
+def render_room_torch(n_frames, seed=0, width=640, height=480, f=585.0, scale=1.0, dropout=0.02,
+                      first_frame=0, device="cuda", chunk=1 << 16):
+    """Frames first_frame .. first_frame+n_frames-1 of room_scene(seed) as a
+    uint16 tensor (n, h, w) on `device`, and their eye-to-world poses."""
+    import torch
+    layout = room_layout(seed, scale)
+    poses = room_trajectory(first_frame + n_frames, seed, scale)[first_frame:]
+    fx = fy = f
+    cx, cy = width / 2.0, height / 2.0
+    dev = torch.device(device)
+    u = torch.arange(width, device=dev, dtype=torch.float32)
+    v = torch.arange(height, device=dev, dtype=torch.float32)
+    vv, uu = torch.meshgrid(v, u, indexing="ij")
+    rays = torch.stack([(uu + 0.5 - cx) / fx, (cy - 0.5 - vv) / fy, -torch.ones_like(uu)], -1)
+    rays = rays.reshape(-1, 3)
+    half = torch.tensor(layout["half"], device=dev, dtype=torch.float32)
+    blo = torch.tensor(np.array(layout["box_lo"]), device=dev, dtype=torch.float32)
+    bhi = torch.tensor(np.array(layout["box_hi"]), device=dev, dtype=torch.float32)
+    sc = torch.tensor(np.array(layout["sph_c"]), device=dev, dtype=torch.float32)
+    sr = torch.tensor(np.array(layout["sph_r"]), device=dev, dtype=torch.float32)
+    pix = torch.arange(width * height, device=dev, dtype=torch.int64)
+    out = torch.zeros((n_frames, height, width), dtype=torch.int16, device=dev)
+    inf = float("inf")
+    for i, pose in enumerate(poses):
+        R = torch.tensor(pose[:3, :3], device=dev, dtype=torch.float32)
+        o = torch.tensor(pose[:3, 3], device=dev, dtype=torch.float32)
+        z = torch.empty(width * height, device=dev, dtype=torch.float32)
+        for s0 in range(0, width * height, chunk):
+            d = rays[s0:s0 + chunk] @ R.T
+            # room walls from inside
+            tpos = torch.where(d > 0, (half - o) / d, torch.full_like(d, inf))
+            tneg = torch.where(d < 0, (-half - o) / d, torch.full_like(d, inf))
+            t = torch.minimum(tpos, tneg).amin(1)
+            # boxes (slabs)
+            inv = 1.0 / torch.where(d == 0, torch.full_like(d, 1e-30), d)
+            t1 = (blo[None] - o) * inv[:, None]
+            t2 = (bhi[None] - o) * inv[:, None]
+            tn = torch.minimum(t1, t2).amax(2)
+            tf = torch.maximum(t1, t2).amin(2)
+            th = torch.where(tn > 1e-6, tn, tf)
+            hit = (tn <= tf) & (tf > 1e-6)
+            t = torch.minimum(t, torch.where(hit, th, torch.full_like(th, inf)).amin(1))
+            # spheres
+            oc = o[None] - sc                       # (S, 3)
+            b = d @ oc.T                            # (P, S)
+            cc = (oc * oc).sum(1) - sr * sr         # (S,)
+            a = (d * d).sum(1, keepdim=True)        # (P, 1)
+            disc = b * b - a * cc[None]
+            sq = torch.sqrt(torch.clamp(disc, min=0))
+            t0 = (-b - sq) / a
+            t1s = (-b + sq) / a
+            ts = torch.where(t0 > 1e-6, t0, t1s)
+            ok = (disc >= 0) & (ts > 1e-6)
+            t = torch.minimum(t, torch.where(ok, ts, torch.full_like(ts, inf)).amin(1))
+            z[s0:s0 + chunk] = t
+        gidx = first_frame + i
+        u1 = _uniform(torch, seed, gidx, pix, 1)
+        u2 = _uniform(torch, seed, gidx, pix, 2)
+        u3 = _uniform(torch, seed, gidx, pix, 3)
+        hitm = torch.isfinite(z)
+        zz = torch.where(hitm, z, torch.zeros_like(z))
+        sigma = 0.0012 + 0.0019 * (zz - 0.4) ** 2
+        gauss = torch.sqrt(-2.0 * torch.log(u1)) * torch.cos(6.283185307179586 * u2)
+        zz = zz + sigma * gauss
+        mm = torch.round(zz * 1000.0)
+        valid = hitm & (zz >= 0.4) & (zz <= 4.0) & (u3 >= dropout)
+        mm = torch.where(valid, torch.clamp(mm, 0, 65535), torch.zeros_like(mm))
+        out[i] = mm.to(torch.int32).to(torch.int16).reshape(height, width)  # bit pattern of uint16
+    return out, poses
+
+
+def kifi_matrix(m):
+    """4x4 matrix -> (16,) float32 in kifi float4x4 memory order."""
+    return np.ascontiguousarray(np.asarray(m, np.float32).T).reshape(16)

@@ -1,0 +1,84 @@
+"""kifi::Pipeline on the GPU: fuse + track + mesh through kifi_pipeline_*,
+checked against the volume/ICP entry points it composes and the oracle."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from tests.helpers import cam_params, canon_bits
+
+pytestmark = pytest.mark.gpu
+
+
+def test_pipeline_matches_components_and_oracle(gpu, oracle_cpu):
+    from merge_fusion_gb300 import _lib, kifi, scenes
+    from merge_fusion_gb300._lib import Camera, PipelineDesc, check
+    lib = _lib.load()
+    seq = scenes.room_scene(n_frames=4, seed=3)
+    cam = seq.camera
+    d = PipelineDesc()
+    d.camera = cam_params(cam).camera()
+    d.resolution, d.side_length_m, d.truncation_m = 1024, 4.096, 0.02
+    d.icp_iterations, d.mesh_every, d.mesh_with_indices = 15, 2, 1
+    d.device = 0
+    pipe = C.c_void_p()
+    check(lib.kifi_pipeline_create(C.byref(d), C.byref(pipe)))
+    ov = oracle_cpu.Volume(1024, 4.096, 0.02)
+    out = np.zeros(16, np.float32)
+    try:
+        for i in range(4):
+            frame = np.ascontiguousarray(seq.frames[i])
+            w2e = seq.world_to_eye_f32(i)
+            check(lib.kifi_pipeline_integrate(pipe, frame.ctypes.data_as(C.c_void_p), 1,
+                                              w2e.ctypes.data_as(C.c_void_p),
+                                              out.ctypes.data_as(C.c_void_p)))
+            ov.integrate(seq.depth_m(i), cam, w2e)
+            if i > 0:
+                prev = seq.eye_to_world_f32(i - 1)
+                target = oracle_cpu.backproject(seq.depth_m(i - 1), cam, prev)
+                o, _, n = oracle_cpu.icp_align(seq.depth_m(i), cam, prev, target, prev, 15)
+                assert np.abs(out - o).max() < 1e-5, (i, np.abs(out - o).max())
+            else:
+                assert np.array_equal(out, seq.eye_to_world_f32(0)) or \
+                    np.abs(out - seq.eye_to_world_f32(0)).max() < 1e-6
+        vol = lib.kifi_pipeline_volume(pipe)
+        n = C.c_size_t()
+        check(lib.kifi_volume_size(vol, C.byref(n)))
+        k = np.zeros(n.value, np.uint32)
+        v = np.zeros((n.value, 2), np.float32)
+        got = C.c_size_t()
+        check(lib.kifi_volume_export(vol, k.ctypes.data_as(C.c_void_p),
+                                     v.ctypes.data_as(C.c_void_p), n.value, C.byref(got)))
+        assert np.array_equal(k, ov.keys)
+        assert np.array_equal(canon_bits(v), canon_bits(ov.values))
+        nv, ni = C.c_size_t(), C.c_size_t()
+        check(lib.kifi_pipeline_mesh_counts(pipe, C.byref(nv), C.byref(ni)))
+        vb, ib = ov.mesh(True)
+        assert (nv.value, ni.value) == (vb.shape[0], ib.size)
+    finally:
+        lib.kifi_pipeline_destroy(pipe)
+
+
+def test_stage_timers_and_frame_log(gpu, golden):
+    from merge_fusion_gb300 import _lib, kifi
+    from merge_fusion_gb300._lib import check
+    lib = _lib.load()
+    depth, view, cam = golden["depth"], golden["view"], golden["camera"]
+    vol = kifi.Volume(256, 2.0, 0.02)
+    check(lib.kifi_volume_set_profiling(vol.handle, 1))
+    for i in range(3):
+        kifi.Integrator().Integrate(vol, depth, cam_params(cam), view)
+    ms = np.zeros(3)
+    nf = C.c_int()
+    check(lib.kifi_volume_stage_times(vol.handle, ms.ctypes.data_as(C.c_void_p), C.byref(nf)))
+    assert nf.value == 3 and (ms > 0).all()
+    n0 = np.zeros(64, np.uint64)
+    ne = np.zeros(64, np.uint64)
+    n1 = np.zeros(64, np.uint64)
+    cnt = C.c_int()
+    check(lib.kifi_volume_frame_log(vol.handle, n0.ctypes.data_as(C.c_void_p),
+                                    ne.ctypes.data_as(C.c_void_p), n1.ctypes.data_as(C.c_void_p),
+                                    64, C.byref(cnt)))
+    assert cnt.value == 3
+    assert n0[0] == 0 and n1[0] == golden["cases"][0]["voxels"]
+    assert (n1[:3] == n0[:3] + ne[:3]).all() and n0[1] == n1[0]
