@@ -424,6 +424,9 @@ def run_reference(args, rank, world):
 def main():
     args = parse()
     rank, world, local = dist_env()
+    # in-tree build (no-op when up to date); the GPU arm fails loudly without it
+    from merge_fusion_gb300 import build
+    build.build()
     if args.impl == "reference":
         run_reference(args, rank, world)
     else:
