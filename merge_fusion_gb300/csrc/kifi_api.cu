@@ -33,7 +33,7 @@ kifi_status launch_shape(int device, LaunchShape* ls) {
     KIFI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
     ls->sms = sms;
     ls->sort_ctas = sms * 4;
-    ls->merge_ctas = sms * 4;
+    ls->merge_ctas = sms * merge_blocks_per_sm();
     ls->splat_ctas = sms * 4;
     return KIFI_OK;
 }
@@ -59,7 +59,11 @@ void free_volume_buffers(VolumeBuffers& vb) {
         vb.keys[i] = nullptr;
         vb.vals[i] = nullptr;
     }
+    cudaFree(vb.splits);
+    vb.splits = nullptr;
 }
+
+size_t split_count(size_t cap) { return cap / 2048 + 4; }
 
 // Reads the device control block (waits for the stream).
 kifi_status read_ctl(kifi_volume* v) {
@@ -93,6 +97,7 @@ kifi_status grow_volume(kifi_volume* v, size_t need) {
         nb.keys[i] = nullptr;
         nb.vals[i] = nullptr;
     }
+    nb.splits = nullptr;
     for (int i = 0; i < 2; ++i) {
         cudaError_t e1 = cudaMalloc(&nb.keys[i], (cap + kPad) * sizeof(uint32_t));
         cudaError_t e2 = e1 ? e1 : cudaMalloc(&nb.vals[i], (cap + kPad) * sizeof(float2));
@@ -100,6 +105,11 @@ kifi_status grow_volume(kifi_volume* v, size_t need) {
             free_volume_buffers(nb);
             return cuda_fail(e1 ? e1 : e2, "growing the volume");
         }
+    }
+    cudaError_t es = cudaMalloc(&nb.splits, split_count(cap) * sizeof(unsigned long long));
+    if (es) {
+        free_volume_buffers(nb);
+        return cuda_fail(es, "growing the volume");
     }
     KIFI_CUDA(cudaMemcpyAsync(nb.keys[cur], v->vb.keys[cur], n * sizeof(uint32_t),
                               cudaMemcpyDeviceToDevice, v->stream));
@@ -111,6 +121,7 @@ kifi_status grow_volume(kifi_volume* v, size_t need) {
     v->vb.keys[1] = nb.keys[1];
     v->vb.vals[0] = nb.vals[0];
     v->vb.vals[1] = nb.vals[1];
+    v->vb.splits = nb.splits;
     v->vb.cap = cap;
     return KIFI_OK;
 }
@@ -304,6 +315,8 @@ kifi_status kifi_volume_create(const kifi_volume_desc* d, kifi_volume** out) {
         if ((e = cudaMalloc(&v->vb.vals[i], (cap + kPad) * sizeof(float2))))
             return bail(cuda_fail(e, "volume values"));
     }
+    if ((e = cudaMalloc(&v->vb.splits, split_count(cap) * sizeof(unsigned long long))))
+        return bail(cuda_fail(e, "merge splits"));
     v->vb.cap = cap;
     if ((s = reserve_new(v, 8 * 640 * 480))) return bail(s);
     *out = v;

@@ -15,8 +15,10 @@ struct kifi_icp {
     IcpState* st = nullptr;
     void* depth_dev = nullptr;
     size_t depth_bytes = 0;
-    float* synth = nullptr;
-    size_t synth_cap = 0;  // floats
+    float4* synth = nullptr;  // target in the association's float4 layout
+    size_t synth_cap = 0;     // bytes
+    void* staging = nullptr;  // host float3 targets on their way in
+    size_t staging_cap = 0;
     int sw = 0, sh = 0;
     Mat4 synth_e2w{};
     bool have_target = false;
@@ -47,11 +49,8 @@ kifi_status reserve_bytes(void** p, size_t* cap, size_t bytes, cudaStream_t st) 
 }
 
 kifi_status reserve_target(kifi_icp* c, int w, int h) {
-    size_t floats = (size_t)w * h * 3;
-    size_t cap = c->synth_cap * 4;
-    kifi_status s = reserve_bytes((void**)&c->synth, &cap, floats * 4, c->stream);
-    c->synth_cap = cap / 4;
-    return s;
+    return reserve_bytes((void**)&c->synth, &c->synth_cap, (size_t)w * h * sizeof(float4),
+                         c->stream);
 }
 
 kifi_status enqueue_align(kifi_icp* c, const void* depth_dev, bool u16, const kifi_camera* cam,
@@ -139,6 +138,7 @@ kifi_status kifi_icp_destroy(kifi_icp* c) {
     cudaFree(c->st);
     cudaFree(c->depth_dev);
     cudaFree(c->synth);
+    cudaFree(c->staging);
     cudaFree(c->src);
     cudaFree(c->dst);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -155,8 +155,11 @@ kifi_status kifi_icp_set_target(kifi_icp* c, const float* points, int width, int
     KIFI_CUDA(cudaSetDevice(c->device));
     kifi_status s = reserve_target(c, width, height);
     if (s) return s;
-    KIFI_CUDA(cudaMemcpyAsync(c->synth, points, (size_t)width * height * 12, cudaMemcpyHostToDevice,
-                              c->stream));
+    const size_t bytes = (size_t)width * height * 12;
+    if ((s = reserve_bytes(&c->staging, &c->staging_cap, bytes, c->stream))) return s;
+    KIFI_CUDA(cudaMemcpyAsync(c->staging, points, bytes, cudaMemcpyHostToDevice, c->stream));
+    KIFI_CUDA(expand_target_enqueue((const float*)c->staging, width * height, c->synth,
+                                    c->ls.sms * 4, c->stream));
     KIFI_CUDA(cudaStreamSynchronize(c->stream));
     c->sw = width;
     c->sh = height;

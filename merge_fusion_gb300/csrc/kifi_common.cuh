@@ -171,7 +171,9 @@ struct DeviceCtl {
     unsigned int status;           // KIFI_ERR_* bits raised on the device
     unsigned long long sort_epoch; // generation tag of the sort look-back words
     unsigned int tile_counter[8];  // dynamic tile ids (one per sort pass / merge)
-    FrameConst fc;                 // constants of the frame being integrated
+    unsigned long long merge_e;    // settled merge: keys new to the volume,
+    unsigned long long merge_n1;   //   resident voxels after it,
+    unsigned int merge_ok;         //   and whether they fit the capacity
     unsigned long long frames;     // merges committed (frames integrated + inserts)
     // sizes of the last kFrameLog merges: resident before, new, resident after
     unsigned long long log_n0[64], log_new[64], log_n1[64];

@@ -116,85 +116,107 @@ __device__ __forceinline__ bool last_cta(unsigned int* counter) {
     return last;
 }
 
-// Sums the per-CTA partials of NV components (thread c sums component c in
-// CTA order, so the result does not depend on scheduling) into out[].
+// Sums the per-CTA double partials of NV components with the whole (last)
+// CTA: thread t adds CTAs t, t+256, ... and a fixed-shape tree combines the
+// threads, so the result does not depend on scheduling.
 template <int NV>
 __device__ __forceinline__ void finish_partials(const IcpState* st, double* out) {
-    if (threadIdx.x < NV) {
+    __shared__ double red[kThreads];
+    for (int c = 0; c < NV; ++c) {
         double a = 0.0;
-        for (unsigned int b = 0; b < gridDim.x; ++b) a += st->part[b * 16 + threadIdx.x];
-        out[threadIdx.x] = a;
+        for (unsigned int b = threadIdx.x; b < gridDim.x; b += kThreads) a += st->part[b * 16 + c];
+        red[threadIdx.x] = a;
+        __syncthreads();
+        for (int w = kThreads / 2; w > 0; w >>= 1) {
+            if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) out[c] = red[0];
+        __syncthreads();
     }
-    __syncthreads();
 }
 
-// One warp per source pixel: the lanes split the 21x21 window and the
-// nearest candidate is chosen by a lexicographic (len^2, scan position)
-// minimum, which is the reference's "first strict minimum in row-major scan
-// order" (ICP.cpp:108-125).
+// Association, one warp per batch of 32 consecutive source pixels: lane k
+// back-projects and projects source k (ICP.cpp:69-81, 100-104); then for each
+// source of the batch the whole warp scans its 21x21 window (lanes split the
+// candidates) and a lexicographic (len^2, scan position) minimum reproduces
+// the reference's "first strict minimum in row-major scan order"
+// (ICP.cpp:108-125).  Lane k keeps source k's result, so the stores and the
+// centroid sums are lane-parallel again.
 __global__ void __launch_bounds__(kThreads) k_icp_associate(IcpArgs a, IcpState* __restrict__ st) {
     const int n_cols = (a.width + 3) / 4;
     const int n_src = n_cols * a.height;
     const int lane = threadIdx.x & 31;
+    const int n_batches = (n_src + 31) / 32;
     const int warps = gridDim.x * (kThreads / 32);
-    float pose[16];
-#pragma unroll
-    for (int i = 0; i < 16; ++i) pose[i] = st->pose_f[i];
-    // counts, src xyzw, dst xyz, sum of min len^2 (lane 0 of each warp)
-    KahanF acc[9];
     const float half_w = fmul((float)a.synth_w, 0.5f), half_h = fmul((float)a.synth_h, 0.5f);
     const size_t n_synth = (size_t)a.synth_w * a.synth_h;
-    for (int s = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5); s < n_src; s += warps) {
-        const int y = s / n_cols, x = (s - y * n_cols) * 4;
-        const float d = load_depth(a.depth, (size_t)y * a.width + x, a.depth_u16);
-        float4 p1 = make_float4(0.f, 0.f, 0.f, 0.f), p2 = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (0.0f != d) {
-            float pt[4];
-            pt[0] = fmul(fadd(fmul((float)x, a.fl_inv_x), a.pp_x), d);
-            pt[1] = fmul(fadd(fmul(-(float)y, a.fl_inv_y), a.pp_y), d);
-            pt[2] = fmul(fadd(fmul(-1.0f, 1.0f), 0.0f), d);
-            pt[3] = 1.0f;
-            float wp[4], cl[4];
-            mat_vec(pose, pt, wp);
-            mat_vec(a.proj, wp, cl);
-            const float ux = fdiv(cl[0], cl[3]), uy = fdiv(cl[1], cl[3]);
-            int u = wrap_sub(cvt_i32_x86(fadd(fmul(ux, half_w), half_w)), 10);
-            int v = wrap_sub(wrap_sub(a.synth_h - 1, cvt_i32_x86(fadd(fmul(uy, half_h), half_h))), 10);
-            u = max(0, u);
-            v = max(0, v);
-            const int nr = (int)min(480ll, (long long)v + 21) - v;
-            const int nc = (int)min(640ll, (long long)u + 21) - u;
-            const float dw = fsub(1.0f, wp[3]);
+    KahanF acc[9];  // count, src xyzw, dst xyz, sum of min len^2
+    for (int batch = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5); batch < n_batches;
+         batch += warps) {
+        const int s = batch * 32 + lane;
+        // per-lane set-up of source s
+        float wp[4] = {0.f, 0.f, 0.f, 0.f};
+        int u = 0, v = 0, nr = 0, nc = 0;
+        if (s < n_src) {
+            const int y = s / n_cols, x = (s - y * n_cols) * 4;
+            const float d = load_depth(a.depth, (size_t)y * a.width + x, a.depth_u16);
+            if (0.0f != d) {
+                float pt[4], cl[4];
+                pt[0] = fmul(fadd(fmul((float)x, a.fl_inv_x), a.pp_x), d);
+                pt[1] = fmul(fadd(fmul(-(float)y, a.fl_inv_y), a.pp_y), d);
+                pt[2] = fmul(fadd(fmul(-1.0f, 1.0f), 0.0f), d);
+                pt[3] = 1.0f;
+                mat_vec(st->pose_f, pt, wp);
+                mat_vec(a.proj, wp, cl);
+                const float ux = fdiv(cl[0], cl[3]), uy = fdiv(cl[1], cl[3]);
+                u = wrap_sub(cvt_i32_x86(fadd(fmul(ux, half_w), half_w)), 10);
+                v = wrap_sub(wrap_sub(a.synth_h - 1, cvt_i32_x86(fadd(fmul(uy, half_h), half_h))), 10);
+                u = max(0, u);
+                v = max(0, v);
+                nr = (int)min(480ll, (long long)v + 21) - v;
+                nc = (int)min(640ll, (long long)u + 21) - u;
+                if (nr <= 0 || nc <= 0) nr = nc = 0;
+            }
+        }
+        float my_best = 0.01f;
+        int my_idx = 0x7fffffff;
+        for (int k = 0; k < 32; ++k) {
+            const int knr = __shfl_sync(0xffffffffu, nr, k);
+            if (knr == 0) continue;  // warp-uniform
+            const int knc = __shfl_sync(0xffffffffu, nc, k);
+            const int ku = __shfl_sync(0xffffffffu, u, k), kv = __shfl_sync(0xffffffffu, v, k);
+            const float px = __shfl_sync(0xffffffffu, wp[0], k);
+            const float py = __shfl_sync(0xffffffffu, wp[1], k);
+            const float pz = __shfl_sync(0xffffffffu, wp[2], k);
+            const float pw = __shfl_sync(0xffffffffu, wp[3], k);
+            const float dw = fsub(1.0f, pw);
             const float dw2 = fmul(dw, dw);
+            const int total = knr * knc;
+            int r = lane / knc, c = lane - r * knc;
+            const int step_r = 32 / knc, step_c = 32 - step_r * knc;
             float best = 0.01f;
             int best_i = 0x7fffffff;
-            if (nr > 0 && nc > 0) {
-                const int total = nr * nc;
-                int r = lane / nc, c = lane - (lane / nc) * nc;
-                const int step_r = 32 / nc, step_c = 32 - step_r * nc;
-                for (int i = lane; i < total; i += 32) {
-                    const size_t at = (size_t)(v + r) * a.synth_w + (u + c);
-                    if (at < n_synth) {
-                        const float* q = a.synth + 3 * at;
-                        const float qx = __ldg(q), qy = __ldg(q + 1), qz = __ldg(q + 2);
-                        if (!(qx == 0.0f && qy == 0.0f && qz == 0.0f)) {
-                            const float dx = fsub(qx, wp[0]), dy = fsub(qy, wp[1]), dz = fsub(qz, wp[2]);
-                            const float l2 = fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fadd(fmul(dz, dz), dw2));
-                            if (l2 < best) {  // scan order within the lane is increasing
-                                best = l2;
-                                best_i = i;
-                            }
+            for (int i = lane; i < total; i += 32) {
+                const size_t at = (size_t)(kv + r) * a.synth_w + (ku + c);
+                if (at < n_synth) {
+                    const float4 q = __ldg(a.synth + at);
+                    if (!(q.x == 0.0f && q.y == 0.0f && q.z == 0.0f)) {
+                        const float dx = fsub(q.x, px), dy = fsub(q.y, py), dz = fsub(q.z, pz);
+                        const float l2 = fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fadd(fmul(dz, dz), dw2));
+                        if (l2 < best) {  // scan order within a lane is increasing
+                            best = l2;
+                            best_i = i;
                         }
                     }
-                    r += step_r;
-                    c += step_c;
-                    if (c >= nc) {
-                        c -= nc;
-                        ++r;
-                    }
+                }
+                r += step_r;
+                c += step_c;
+                if (c >= knc) {
+                    c -= knc;
+                    ++r;
                 }
             }
-            // lexicographic (len^2, scan index) minimum over the warp
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 const float ob = __shfl_xor_sync(0xffffffffu, best, o);
@@ -204,20 +226,23 @@ __global__ void __launch_bounds__(kThreads) k_icp_associate(IcpArgs a, IcpState*
                     best_i = oi;
                 }
             }
-            if (best_i != 0x7fffffff) {
-                const int br = best_i / nc, bc = best_i - br * nc;
-                const float* q = a.synth + 3 * ((size_t)(v + br) * a.synth_w + (u + bc));
-                p1 = make_float4(wp[0], wp[1], wp[2], wp[3]);
-                p2 = make_float4(__ldg(q), __ldg(q + 1), __ldg(q + 2), 1.0f);
-                if (lane == 0) {
-                    acc[0].add(1.0f);
-                    acc[1].add(p1.x); acc[2].add(p1.y); acc[3].add(p1.z); acc[4].add(p1.w);
-                    acc[5].add(p2.x); acc[6].add(p2.y); acc[7].add(p2.z);
-                    acc[8].add(best);
-                }
+            if (lane == k) {
+                my_best = best;
+                my_idx = best_i;
             }
         }
-        if (lane == 0) {
+        if (s < n_src) {
+            float4 p1 = make_float4(0.f, 0.f, 0.f, 0.f), p2 = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (my_idx != 0x7fffffff) {
+                const int br = my_idx / nc, bc = my_idx - br * nc;
+                const float4 q = __ldg(a.synth + (size_t)(v + br) * a.synth_w + (u + bc));
+                p1 = make_float4(wp[0], wp[1], wp[2], wp[3]);
+                p2 = make_float4(q.x, q.y, q.z, 1.0f);
+                acc[0].add(1.0f);
+                acc[1].add(p1.x); acc[2].add(p1.y); acc[3].add(p1.z); acc[4].add(p1.w);
+                acc[5].add(p2.x); acc[6].add(p2.y); acc[7].add(p2.z);
+                acc[8].add(my_best);
+            }
             a.src[s] = p1;
             a.dst[s] = p2;  // w = 1 marks an association
         }
@@ -397,7 +422,7 @@ __global__ void k_icp_begin(IcpState* st, Mat4 guess) {
 // pixels without depth get (0,0,0), the reference's "invalid" target value.
 __global__ void k_backproject(const void* __restrict__ depth, int u16, int width, int height,
                               float fl_inv_x, float fl_inv_y, float pp_x, float pp_y, Mat4 e2w,
-                              float* __restrict__ out) {
+                              float4* __restrict__ out) {
     const int n = width * height;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int v = i / width, u = i - v * width;
@@ -411,10 +436,15 @@ __global__ void k_backproject(const void* __restrict__ depth, int u16, int width
             p[3] = fadd(fmul(fadd(fmul(0.0f, 1.0f), 0.0f), d), 1.0f);
             mat_vec(e2w.m, p, w);
         }
-        out[3 * i] = w[0];
-        out[3 * i + 1] = w[1];
-        out[3 * i + 2] = w[2];
+        out[i] = make_float4(w[0], w[1], w[2], 0.0f);
     }
+}
+
+// host float3 target -> the float4 layout the association reads (one
+// 16-byte load per candidate)
+__global__ void k_expand_target(const float* __restrict__ in, int n, float4* __restrict__ out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        out[i] = make_float4(in[3 * i], in[3 * i + 1], in[3 * i + 2], 0.0f);
 }
 
 // Renderer::Bin: a z-buffered splat.  The first point (in input order) with
@@ -463,15 +493,24 @@ __global__ void k_bin_resolve(const float* __restrict__ pts, const unsigned long
 cudaError_t icp_align_enqueue(const IcpArgs& a, IcpState* st, const Mat4& guess, int iterations,
                               int ctas, cudaStream_t stream) {
     k_icp_begin<<<1, 32, 0, stream>>>(st, guess);
+    const int n_src = ((a.width + 3) / 4) * a.height;
+    int horn_ctas = (n_src + kThreads * 4 - 1) / (kThreads * 4);
+    if (horn_ctas > ctas) horn_ctas = ctas;
+    if (horn_ctas < 1) horn_ctas = 1;
     for (int it = 0; it < iterations; ++it) {
         k_icp_associate<<<ctas, kThreads, 0, stream>>>(a, st);
-        k_icp_horn<<<ctas, kThreads, 0, stream>>>(a, st);
+        k_icp_horn<<<horn_ctas, kThreads, 0, stream>>>(a, st);
     }
     return cudaGetLastError();
 }
 
+cudaError_t expand_target_enqueue(const float* in, int n, float4* out, int ctas, cudaStream_t st) {
+    k_expand_target<<<ctas, kThreads, 0, st>>>(in, n, out);
+    return cudaGetLastError();
+}
+
 cudaError_t backproject_enqueue(const void* depth, bool u16, const kifi_camera& cam,
-                                const Mat4& eye_to_world, float* out, int ctas, cudaStream_t st) {
+                                const Mat4& eye_to_world, float4* out, int ctas, cudaStream_t st) {
     const float fix = fdiv(1.0f, cam.fx), fiy = fdiv(1.0f, cam.fy);
     const float ppx = fmul(fsub(0.5f, cam.cx), fix), ppy = fmul(fsub(cam.cy, 0.5f), fiy);
     k_backproject<<<ctas, kThreads, 0, st>>>(depth, u16 ? 1 : 0, cam.width, cam.height, fix, fiy,

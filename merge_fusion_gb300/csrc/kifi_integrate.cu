@@ -46,9 +46,8 @@ constexpr int kMergeItems = 8;                            // outputs per thread
 constexpr int kMergeTile = kMergeThreads * kMergeItems;   // 2048 outputs per tile
 constexpr uint16_t kFromB = 0x8000u;
 
-__global__ void k_frame_setup(DeviceCtl* ctl, kifi_camera cam, Mat4 w2e, int res) {
+__global__ void k_frame_setup(DeviceCtl* ctl) {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
-        ctl->fc = make_frame_const(cam, w2e, res);
         ctl->n_new = 0u;
         ctl->excluded_key = 0u;
     }
@@ -66,8 +65,8 @@ __device__ __forceinline__ size_t bit_index(uint32_t key, int res) {
 }
 
 // Splat of one pixel (Integrator.cpp:121-154 for one SSE lane).
-__device__ __forceinline__ bool splat_pixel(const FrameConst& fc, const Geom& g, int u, int v,
-                                            float d, uint32_t* key) {
+__device__ __forceinline__ bool splat_pixel(const FrameConst& fc, const float (&e2w)[16],
+                                            const Geom& g, int u, int v, float d, uint32_t* key) {
     if (!(d > 0.0f)) return false;
     float p[4];
     // point = (u, -v, -1, 0) + 0; point * flInv + ppOverFl; point * depth + (0,0,0,1)
@@ -76,7 +75,7 @@ __device__ __forceinline__ bool splat_pixel(const FrameConst& fc, const Geom& g,
     p[2] = fadd(fmul(fadd(fmul(-1.0f, 1.0f), 0.0f), d), 0.0f);
     p[3] = fadd(fmul(fadd(fmul(0.0f, 1.0f), 0.0f), d), 1.0f);
     float w[4];
-    mat_vec(fc.eye_to_world.m, p, w);
+    mat_vec(e2w, p, w);
     // VoxelIndex(world) - 0.5 (Volume.cpp:90-93); the w lane uses (1, 0)
     float ix = fsub(fadd(fmul(w[0], g.vlen_inv), g.index_off), 0.5f);
     float iy = fsub(fadd(fmul(w[1], g.vlen_inv), g.index_off), 0.5f);
@@ -95,11 +94,14 @@ __global__ void __launch_bounds__(kEmitThreads) k_splat_emit(DeviceCtl* __restri
                                                              const void* __restrict__ depth,
                                                              uint32_t* __restrict__ bitmap,
                                                              uint32_t* __restrict__ new_keys,
-                                                             unsigned int new_cap) {
-    const FrameConst fc = ctl->fc;
+                                                             unsigned int new_cap,
+                                                             const FrameConst fc) {
     const int W = fc.width, H = fc.height;
     const size_t P = (size_t)W * H;
     const int lane = threadIdx.x & 31;
+    float e2w[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) e2w[i] = fc.eye_to_world.m[i];
     const size_t stride = (size_t)gridDim.x * kEmitThreads;
     const size_t P_round = (P + 31) / 32 * 32;  // warp-uniform trip count
     for (size_t i = (size_t)blockIdx.x * kEmitThreads + threadIdx.x; i < P_round; i += stride) {
@@ -107,7 +109,7 @@ __global__ void __launch_bounds__(kEmitThreads) k_splat_emit(DeviceCtl* __restri
         bool valid = false;
         if (i < P) {
             int u = (int)(i % (size_t)W), v = (int)(i / (size_t)W);
-            valid = splat_pixel(fc, g, u, v, load_depth(depth, i, kU16), &key);
+            valid = splat_pixel(fc, e2w, g, u, v, load_depth(depth, i, kU16), &key);
         }
         // the excluded key of the dilation: max splat + pack(1,1,1)
         unsigned int ex = __reduce_max_sync(0xffffffffu, valid ? key + pack30(1, 1, 1) : 0u);
@@ -142,7 +144,8 @@ __global__ void __launch_bounds__(kEmitThreads) k_splat_emit(DeviceCtl* __restri
 // UpdateVoxels for one voxel (Integrator.cpp:273-322 for one SSE lane).
 template <bool kU16>
 __device__ __forceinline__ void update_voxel(uint32_t key, float2& val, const FrameConst& fc,
-                                             const Geom& g, const void* depth) {
+                                             const float (&w2c)[16], const Geom& g,
+                                             const void* depth) {
     // VoxelCenter: index * (vlen, vlen, vlen, 1) + (off, off, off, 0)
     float c[4];
     c[0] = fadd(fmul((float)key_x(key), g.vlen), g.center_off);
@@ -150,7 +153,7 @@ __device__ __forceinline__ void update_voxel(uint32_t key, float2& val, const Fr
     c[2] = fadd(fmul((float)key_z(key), g.vlen), g.center_off);
     c[3] = 1.0f;  // 1 * 1 + 0
     float cl[4];
-    mat_vec(fc.world_to_clip.m, c, cl);
+    mat_vec(w2c, c, cl);
     const float w = cl[3];
     // lane w: (w/w) * 0 + 0 lies in [-FLT_MAX, FLT_MAX) iff w/w is finite,
     // i.e. iff w is finite and non-zero (w/w is then exactly 1).
@@ -199,60 +202,151 @@ struct MergeInputs {
     bool update;              // run UpdateVoxels on the merged volume
 };
 
+// Merge set-up and partition.  Thread 0 settles the merge: drops the
+// dilation's excluded key when it is the largest new key (clearing its
+// occupancy bit), checks the capacity and publishes (e, N1).  Every thread t
+// then computes the merge-path split of output tile t: the number of resident
+// keys among the first t*kMergeTile outputs.  The binary searches of all
+// tiles run in parallel here instead of serialising the merge kernel's tiles.
+__global__ void __launch_bounds__(256) k_merge_partition(DeviceCtl* __restrict__ ctl, Geom g,
+                                                          VolumeBuffers vb, MergeInputs in,
+                                                          unsigned long long* __restrict__ splits,
+                                                          unsigned int max_tiles) {
+    __shared__ unsigned long long s_e, s_n1;
+    __shared__ int s_ok;
+    const unsigned int cur = ctl->cur;
+    const unsigned long long N0 = ctl->n[cur];
+    // select rather than index: a runtime index into a parameter array
+    // would force the array into local memory
+    const uint32_t* __restrict__ A = cur ? vb.keys[1] : vb.keys[0];
+    const uint32_t* __restrict__ B = in.b_keys;
+    if (threadIdx.x == 0) {
+        unsigned long long e = *in.b_count;
+        const uint32_t excluded = ctl->excluded_key;
+        const bool drop = e > 0 && excluded != 0u && B[e - 1] == excluded;
+        if (drop) --e;
+        const bool ok = N0 + e <= vb.cap;
+        s_e = e;
+        s_n1 = N0 + e;
+        s_ok = ok;
+        if (blockIdx.x == 0) {
+            ctl->merge_e = e;
+            ctl->merge_n1 = N0 + e;
+            ctl->merge_ok = ok ? 1u : 0u;
+            if (drop) {
+                size_t b = bit_index(excluded, g.res);
+                atomicAnd(vb.bitmap + (b >> 5), ~(1u << (b & 31)));
+            }
+            if (!ok) atomicOr(&ctl->status, KIFI_DEV_ERR_CAPACITY);
+        }
+    }
+    __syncthreads();
+    const unsigned long long e = s_e, N1 = s_n1;
+    if (!s_ok) {
+        // no room: leave the volume as it was and take the new keys back out
+        // of the occupancy bitmap; the host grows the buffers and retries.
+        for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < e;
+             i += (unsigned long long)gridDim.x * blockDim.x) {
+            size_t b = bit_index(B[i], g.res);
+            atomicAnd(vb.bitmap + (b >> 5), ~(1u << (b & 31)));
+        }
+        return;
+    }
+    const unsigned long long n_tiles = (N1 + kMergeTile - 1) / kMergeTile;
+    for (unsigned long long t = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+         t <= n_tiles && t < max_tiles; t += (unsigned long long)gridDim.x * blockDim.x) {
+        const unsigned long long d = t * kMergeTile < N1 ? t * kMergeTile : N1;
+        splits[t] = merge_path(A, N0, B, e, d);
+    }
+}
+
+// One output voxel: value from A or Voxel(), TSDF update when inside the
+// reference's update range.
+template <bool kU16>
+__device__ __forceinline__ void finish_voxel(uint32_t key, float2& val, unsigned long long pos,
+                                             unsigned long long upd_end, const FrameConst& fc,
+                                             const float (&w2c)[16], const Geom& g,
+                                             const void* depth) {
+    if (pos < upd_end) update_voxel<kU16>(key, val, fc, w2c, g, depth);
+}
+
 template <bool kU16>
 __global__ void __launch_bounds__(kMergeThreads) k_merge_update(DeviceCtl* __restrict__ ctl, Geom g,
                                                                 VolumeBuffers vb, MergeInputs in,
-                                                                const void* __restrict__ depth) {
+                                                                const void* __restrict__ depth,
+                                                                const unsigned long long* __restrict__ splits,
+                                                                const FrameConst fc) {
     __shared__ uint32_t sA_k[kMergeTile + 8];
     __shared__ float2 sA_v[kMergeTile + 4];
     __shared__ uint32_t sB_k[kMergeTile];
     __shared__ uint16_t sSrc[kMergeTile];
-    __shared__ unsigned long long sSplit[2];
 
+    if (!ctl->merge_ok) return;
     const unsigned int cur = ctl->cur, out = cur ^ 1u;
     const unsigned long long N0 = ctl->n[cur];
-    unsigned long long e = *in.b_count;
-    const uint32_t* __restrict__ A = vb.keys[cur];
-    const float2* __restrict__ Av = vb.vals[cur];
+    const unsigned long long e = ctl->merge_e;
+    const unsigned long long N1 = ctl->merge_n1;
+    const uint32_t* __restrict__ A = cur ? vb.keys[1] : vb.keys[0];
+    const float2* __restrict__ Av = cur ? vb.vals[1] : vb.vals[0];
     const uint32_t* __restrict__ B = in.b_keys;
-    const uint32_t excluded = ctl->excluded_key;
-    bool drop = false;
-    if (e > 0 && excluded != 0u && B[e - 1] == excluded) {
-        drop = true;
-        --e;
-    }
-    const unsigned long long N1 = N0 + e;
-    if (N1 > vb.cap) {
-        // no room: leave the volume as it was and take the new keys back out
-        // of the occupancy bitmap; the host grows the buffers and retries.
-        for (unsigned long long i = (unsigned long long)blockIdx.x * kMergeThreads + threadIdx.x;
-             i < e + (drop ? 1 : 0); i += (unsigned long long)gridDim.x * kMergeThreads) {
-            size_t b = bit_index(B[i], g.res);
-            atomicAnd(vb.bitmap + (b >> 5), ~(1u << (b & 31)));
-        }
-        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&ctl->status, KIFI_DEV_ERR_CAPACITY);
-        return;
-    }
-    if (drop && blockIdx.x == 0 && threadIdx.x == 0) {
-        size_t b = bit_index(excluded, g.res);
-        atomicAnd(vb.bitmap + (b >> 5), ~(1u << (b & 31)));
-    }
-    const FrameConst fc = ctl->fc;
     const unsigned long long upd_end = in.update ? (N1 / 4 * 4) : 0ull;
-    uint32_t* __restrict__ outK = vb.keys[out];
-    float2* __restrict__ outV = vb.vals[out];
+    uint32_t* __restrict__ outK = out ? vb.keys[1] : vb.keys[0];
+    float2* __restrict__ outV = out ? vb.vals[1] : vb.vals[0];
     const unsigned long long n_tiles = (N1 + kMergeTile - 1) / kMergeTile;
+    float w2c[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) w2c[i] = fc.world_to_clip.m[i];
 
     for (unsigned long long t = blockIdx.x; t < n_tiles; t += gridDim.x) {
         const unsigned long long d0 = t * kMergeTile;
         const unsigned long long d1 = (d0 + kMergeTile < N1) ? d0 + kMergeTile : N1;
         const int len = (int)(d1 - d0);
-        if (threadIdx.x < 2) sSplit[threadIdx.x] = merge_path(A, N0, B, e, threadIdx.x ? d1 : d0);
-        __syncthreads();
-        const unsigned long long a0 = sSplit[0], a1 = sSplit[1];
+        const unsigned long long a0 = splits[t], a1 = splits[t + 1];
         const int na = (int)(a1 - a0), nb = len - na;
+        if (nb == 0) {
+            // only resident voxels in this tile: straight streaming, no barrier
+            const bool vec = (a0 & 3ull) == 0;
+#pragma unroll
+            for (int r = 0; r < kMergeItems / 4; ++r) {
+                const int j0 = threadIdx.x * 4 + r * kMergeThreads * 4;
+                if (j0 >= len) break;
+                uint32_t k0, k1, k2, k3;
+                float2 v0, v1, v2, v3;
+                const unsigned long long ia = a0 + j0;
+                if (vec && j0 + 4 <= len) {
+                    const uint4 kk = __ldcs((const uint4*)(A + ia));
+                    const float4 va = __ldcs((const float4*)(Av + ia));
+                    const float4 vb4 = __ldcs((const float4*)(Av + ia + 2));
+                    k0 = kk.x; k1 = kk.y; k2 = kk.z; k3 = kk.w;
+                    v0 = make_float2(va.x, va.y); v1 = make_float2(va.z, va.w);
+                    v2 = make_float2(vb4.x, vb4.y); v3 = make_float2(vb4.z, vb4.w);
+                } else {
+                    const int m = len - j0;
+                    k0 = __ldcs(A + ia); v0 = __ldcs(Av + ia);
+                    k1 = m > 1 ? __ldcs(A + ia + 1) : 0u; v1 = m > 1 ? __ldcs(Av + ia + 1) : v0;
+                    k2 = m > 2 ? __ldcs(A + ia + 2) : 0u; v2 = m > 2 ? __ldcs(Av + ia + 2) : v0;
+                    k3 = m > 3 ? __ldcs(A + ia + 3) : 0u; v3 = m > 3 ? __ldcs(Av + ia + 3) : v0;
+                }
+                const unsigned long long p = d0 + j0;
+                finish_voxel<kU16>(k0, v0, p, upd_end, fc, w2c, g, depth);
+                finish_voxel<kU16>(k1, v1, p + 1, upd_end, fc, w2c, g, depth);
+                finish_voxel<kU16>(k2, v2, p + 2, upd_end, fc, w2c, g, depth);
+                finish_voxel<kU16>(k3, v3, p + 3, upd_end, fc, w2c, g, depth);
+                if (j0 + 4 <= len) {
+                    __stcs((uint4*)(outK + p), make_uint4(k0, k1, k2, k3));
+                    __stcs((float4*)(outV + p), make_float4(v0.x, v0.y, v1.x, v1.y));
+                    __stcs((float4*)(outV + p + 2), make_float4(v2.x, v2.y, v3.x, v3.y));
+                } else {
+                    const int m = len - j0;
+                    outK[p] = k0; outV[p] = v0;
+                    if (m > 1) { outK[p + 1] = k1; outV[p + 1] = v1; }
+                    if (m > 2) { outK[p + 2] = k2; outV[p + 2] = v2; }
+                }
+            }
+            continue;
+        }
+        // mixed tile: stage both ranges in shared memory and merge there
         const unsigned long long b0 = d0 - a0;
-        // stage the A range through shared memory with aligned 16-byte loads
         const unsigned long long ka = a0 & ~3ull;
         const int koff = (int)(a0 - ka);
         for (int i = threadIdx.x * 4; i < koff + na; i += kMergeThreads * 4)
@@ -263,8 +357,7 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_update(DeviceCtl* __res
             *(float4*)&sA_v[i] = __ldcs((const float4*)(Av + va + i));
         for (int i = threadIdx.x; i < nb; i += kMergeThreads) sB_k[i] = B[b0 + i];
         __syncthreads();
-        if (nb > 0) {
-            // per-thread merge path inside the tile, kMergeItems outputs each
+        {
             const int dd = threadIdx.x * kMergeItems;
             if (dd < len) {
                 int lo = dd > nb ? dd - nb : 0, hi = dd < na ? dd : na;
@@ -280,42 +373,24 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_update(DeviceCtl* __res
                     sSrc[j] = takeA ? (uint16_t)ia++ : (uint16_t)(kFromB | ib++);
                 }
             }
-            __syncthreads();
         }
-        // striped pass: 4 consecutive outputs per thread per round
-        for (int j0 = threadIdx.x * 4; j0 < len; j0 += kMergeThreads * 4) {
-            uint32_t ko[4];
-            float2 vo[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int j = j0 + q;
-                if (j >= len) break;
-                uint32_t key;
-                float2 val;
-                uint16_t src = nb > 0 ? sSrc[j] : (uint16_t)j;
-                if (!(src & kFromB)) {
-                    key = sA_k[koff + src];
-                    val = sA_v[voff + src];
-                } else {
-                    const int ib = src & ~kFromB;
-                    key = sB_k[ib];
-                    if (in.b_vals) val = in.b_vals[in.b_index ? in.b_index[b0 + ib] : b0 + ib];
-                    else val = make_float2(0.0f, 0.0f);
-                }
-                if (d0 + j < upd_end) update_voxel<kU16>(key, val, fc, g, depth);
-                ko[q] = key;
-                vo[q] = val;
-            }
-            if (j0 + 4 <= len) {
-                __stcs((uint4*)(outK + d0 + j0), make_uint4(ko[0], ko[1], ko[2], ko[3]));
-                __stcs((float4*)(outV + d0 + j0), make_float4(vo[0].x, vo[0].y, vo[1].x, vo[1].y));
-                __stcs((float4*)(outV + d0 + j0 + 2), make_float4(vo[2].x, vo[2].y, vo[3].x, vo[3].y));
+        __syncthreads();
+        for (int j = threadIdx.x; j < len; j += kMergeThreads) {
+            const uint16_t src = sSrc[j];
+            uint32_t key;
+            float2 val;
+            if (!(src & kFromB)) {
+                key = sA_k[koff + src];
+                val = sA_v[voff + src];
             } else {
-                for (int q = 0; q < 4 && j0 + q < len; ++q) {
-                    outK[d0 + j0 + q] = ko[q];
-                    outV[d0 + j0 + q] = vo[q];
-                }
+                const int ib = src & ~kFromB;
+                key = sB_k[ib];
+                if (in.b_vals) val = in.b_vals[in.b_index ? in.b_index[b0 + ib] : b0 + ib];
+                else val = make_float2(0.0f, 0.0f);
             }
+            finish_voxel<kU16>(key, val, d0 + j, upd_end, fc, w2c, g, depth);
+            __stcs(outK + d0 + j, key);
+            __stcs(outV + d0 + j, val);
         }
         __syncthreads();
     }
@@ -375,30 +450,56 @@ __global__ void k_reset_new(DeviceCtl* ctl) {
 
 }  // namespace
 
+int merge_blocks_per_sm() {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_merge_update<true>, kMergeThreads, 0) !=
+            cudaSuccess ||
+        n < 1)
+        n = 4;
+    return n;
+}
+
+static unsigned int max_tiles_of(const VolumeBuffers& vb) {
+    return (unsigned int)((vb.cap + kMergeTile - 1) / kMergeTile + 2);
+}
+
+static cudaError_t merge_enqueue(DeviceCtl* ctl, const Geom& g, VolumeBuffers& vb,
+                                 const MergeInputs& in, const void* depth, bool u16,
+                                 const FrameConst& fc, const LaunchShape& ls, cudaStream_t st) {
+    const unsigned int mt = max_tiles_of(vb);
+    k_merge_partition<<<(mt + 255) / 256, 256, 0, st>>>(ctl, g, vb, in, vb.splits, mt);
+    if (u16)
+        k_merge_update<true><<<ls.merge_ctas, kMergeThreads, 0, st>>>(ctl, g, vb, in, depth,
+                                                                     vb.splits, fc);
+    else
+        k_merge_update<false><<<ls.merge_ctas, kMergeThreads, 0, st>>>(ctl, g, vb, in, depth,
+                                                                      vb.splits, fc);
+    return cudaGetLastError();
+}
+
 cudaError_t integrate_enqueue(DeviceCtl* ctl, const Geom& g, VolumeBuffers& vb, SortScratch& ss,
                               const void* depth_dev, bool depth_u16, const kifi_camera& cam,
                               const Mat4& world_to_eye, const LaunchShape& ls, cudaStream_t st,
                               cudaEvent_t* events) {
+    // frame constants on the host, in the reference's float order
+    const FrameConst fc = make_frame_const(cam, world_to_eye, g.res);
     if (events) cudaEventRecord(events[0], st);
-    k_frame_setup<<<1, 32, 0, st>>>(ctl, cam, world_to_eye, g.res);
+    k_frame_setup<<<1, 32, 0, st>>>(ctl);
     const unsigned int new_cap = (unsigned int)vb.new_cap;
     if (depth_u16)
         k_splat_emit<true><<<ls.splat_ctas, kEmitThreads, 0, st>>>(ctl, g, depth_dev, vb.bitmap,
-                                                                   vb.new_keys, new_cap);
+                                                                   vb.new_keys, new_cap, fc);
     else
         k_splat_emit<false><<<ls.splat_ctas, kEmitThreads, 0, st>>>(ctl, g, depth_dev, vb.bitmap,
-                                                                    vb.new_keys, new_cap);
+                                                                    vb.new_keys, new_cap, fc);
     if (events) cudaEventRecord(events[1], st);
     cudaError_t e = sort_u32(vb.new_keys, nullptr, &ctl->n_new, ss, &ctl->status, ls.sort_ctas, st);
     if (e != cudaSuccess) return e;
     if (events) cudaEventRecord(events[2], st);
     MergeInputs in{vb.new_keys, nullptr, nullptr, &ctl->n_new, true};
-    if (depth_u16)
-        k_merge_update<true><<<ls.merge_ctas, kMergeThreads, 0, st>>>(ctl, g, vb, in, depth_dev);
-    else
-        k_merge_update<false><<<ls.merge_ctas, kMergeThreads, 0, st>>>(ctl, g, vb, in, depth_dev);
+    e = merge_enqueue(ctl, g, vb, in, depth_dev, depth_u16, fc, ls, st);
     if (events) cudaEventRecord(events[3], st);
-    return cudaGetLastError();
+    return e;
 }
 
 cudaError_t insert_filter_enqueue(DeviceCtl* ctl, const Geom& g, VolumeBuffers& vb,
@@ -415,8 +516,8 @@ cudaError_t insert_filter_enqueue(DeviceCtl* ctl, const Geom& g, VolumeBuffers& 
 cudaError_t insert_merge_enqueue(DeviceCtl* ctl, const Geom& g, VolumeBuffers& vb,
                                  const float2* vals_dev, const LaunchShape& ls, cudaStream_t st) {
     MergeInputs in{vb.new_keys, vb.new_idx, vals_dev, &ctl->n_new, false};
-    k_merge_update<false><<<ls.merge_ctas, kMergeThreads, 0, st>>>(ctl, g, vb, in, nullptr);
-    return cudaGetLastError();
+    FrameConst fc{};
+    return merge_enqueue(ctl, g, vb, in, nullptr, false, fc, ls, st);
 }
 
 }  // namespace kifi

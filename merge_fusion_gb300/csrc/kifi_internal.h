@@ -39,6 +39,7 @@ struct VolumeBuffers {
     uint32_t* new_keys = nullptr;   // keys new to the volume in this frame
     uint32_t* new_idx = nullptr;    // insert path: source position of each new key
     size_t new_cap = 0;
+    unsigned long long* splits = nullptr;  // merge-path split of every output tile
 };
 
 struct LaunchShape {
@@ -56,6 +57,9 @@ cudaError_t integrate_enqueue(DeviceCtl* ctl, const Geom& g, VolumeBuffers& vb, 
                               const void* depth_dev, bool depth_u16, const kifi_camera& cam,
                               const Mat4& world_to_eye, const LaunchShape& ls, cudaStream_t st,
                               cudaEvent_t* events);
+
+// resident CTAs per SM of the merge/update kernel (occupancy API)
+int merge_blocks_per_sm();
 
 // flat_map::insert of n sorted unique device keys: filter out resident keys
 // (their values win) and collect (key, index) of the rest in new_keys /
@@ -103,7 +107,7 @@ struct IcpArgs {
     int width, height;
     float fl_inv_x, fl_inv_y, pp_x, pp_y;
     float proj[16];         // EyeToClipRH * inverse(synth eye-to-world), kifi order
-    const float* synth;     // target world points, synth_w * synth_h float3
+    const float4* synth;    // target world points (w unused), synth_w * synth_h
     int synth_w, synth_h;
     float4* src;            // per source pixel: associated point (w = pose row 3)
     float4* dst;            // per source pixel: target point, w = 1 when associated
@@ -132,7 +136,8 @@ struct IcpState {
 cudaError_t icp_align_enqueue(const IcpArgs& a, IcpState* st, const Mat4& guess, int iterations,
                               int ctas, cudaStream_t stream);
 cudaError_t backproject_enqueue(const void* depth, bool u16, const kifi_camera& cam,
-                                const Mat4& eye_to_world, float* out, int ctas, cudaStream_t st);
+                                const Mat4& eye_to_world, float4* out, int ctas, cudaStream_t st);
+cudaError_t expand_target_enqueue(const float* in, int n, float4* out, int ctas, cudaStream_t st);
 cudaError_t bin_enqueue(const float* pts, unsigned int n, const Mat4& w2c, int width, int height,
                         unsigned long long* zbuf, float* out, int ctas, cudaStream_t st);
 
