@@ -136,30 +136,45 @@ __device__ __forceinline__ void finish_partials(const IcpState* st, double* out)
     }
 }
 
-// Association, one warp per batch of 32 consecutive source pixels: lane k
-// back-projects and projects source k (ICP.cpp:69-81, 100-104); then for each
-// source of the batch the whole warp scans its 21x21 window (lanes split the
-// candidates) and a lexicographic (len^2, scan position) minimum reproduces
-// the reference's "first strict minimum in row-major scan order"
-// (ICP.cpp:108-125).  Lane k keeps source k's result, so the stores and the
-// centroid sums are lane-parallel again.
+// Association (ICP.cpp:66-131).  A CTA owns a tile of 8 source columns x
+// 32 source rows; warp w takes source column w of the tile and lane l source
+// row l, so the 32 lanes of a warp are vertically adjacent sources whose
+// windows sit about one image row apart.  Each thread back-projects and
+// projects its source, the CTA takes the bounding box of the tile's 21x21
+// windows and stages that target region in shared memory as three float
+// planes with an odd row pitch (lanes then hit distinct banks), and every
+// thread scans its own window row by row -- the reference's loop order, so
+// the first strict minimum wins exactly as there.  A region too large for
+// the staging buffer (fast motion) falls back to reading the target from
+// global memory.  Target pixel (y1, x1) is fetched from linear index
+// y1 * synth_w + x1 as in the reference; indices past the buffer's end read
+// as invalid points.
+constexpr int kTileCols = 8, kTileRows = 32;
+constexpr int kStagePixels = 6144;
+
 __global__ void __launch_bounds__(kThreads) k_icp_associate(IcpArgs a, IcpState* __restrict__ st) {
+    extern __shared__ float stage[];  // 3 planes of kStagePixels floats
+    __shared__ int s_box[4];
     const int n_cols = (a.width + 3) / 4;
     const int n_src = n_cols * a.height;
-    const int lane = threadIdx.x & 31;
-    const int n_batches = (n_src + 31) / 32;
-    const int warps = gridDim.x * (kThreads / 32);
+    const int tiles_x = (n_cols + kTileCols - 1) / kTileCols;
+    const int tiles_y = (a.height + kTileRows - 1) / kTileRows;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const float half_w = fmul((float)a.synth_w, 0.5f), half_h = fmul((float)a.synth_h, 0.5f);
     const size_t n_synth = (size_t)a.synth_w * a.synth_h;
+    float pose[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) pose[i] = st->pose_f[i];
     KahanF acc[9];  // count, src xyzw, dst xyz, sum of min len^2
-    for (int batch = blockIdx.x * (kThreads / 32) + (threadIdx.x >> 5); batch < n_batches;
-         batch += warps) {
-        const int s = batch * 32 + lane;
-        // per-lane set-up of source s
+    for (int tile = blockIdx.x; tile < tiles_x * tiles_y; tile += gridDim.x) {
+        const int tx = tile % tiles_x, ty = tile / tiles_x;
+        const int col = tx * kTileCols + warp, y = ty * kTileRows + lane;
+        const bool mine = col < n_cols && y < a.height;
+        const int s = y * n_cols + col;
         float wp[4] = {0.f, 0.f, 0.f, 0.f};
         int u = 0, v = 0, nr = 0, nc = 0;
-        if (s < n_src) {
-            const int y = s / n_cols, x = (s - y * n_cols) * 4;
+        if (mine) {
+            const int x = col * 4;
             const float d = load_depth(a.depth, (size_t)y * a.width + x, a.depth_u16);
             if (0.0f != d) {
                 float pt[4], cl[4];
@@ -167,7 +182,7 @@ __global__ void __launch_bounds__(kThreads) k_icp_associate(IcpArgs a, IcpState*
                 pt[1] = fmul(fadd(fmul(-(float)y, a.fl_inv_y), a.pp_y), d);
                 pt[2] = fmul(fadd(fmul(-1.0f, 1.0f), 0.0f), d);
                 pt[3] = 1.0f;
-                mat_vec(st->pose_f, pt, wp);
+                mat_vec(pose, pt, wp);
                 mat_vec(a.proj, wp, cl);
                 const float ux = fdiv(cl[0], cl[3]), uy = fdiv(cl[1], cl[3]);
                 u = wrap_sub(cvt_i32_x86(fadd(fmul(ux, half_w), half_w)), 10);
@@ -179,73 +194,90 @@ __global__ void __launch_bounds__(kThreads) k_icp_associate(IcpArgs a, IcpState*
                 if (nr <= 0 || nc <= 0) nr = nc = 0;
             }
         }
-        float my_best = 0.01f;
-        int my_idx = 0x7fffffff;
-        for (int k = 0; k < 32; ++k) {
-            const int knr = __shfl_sync(0xffffffffu, nr, k);
-            if (knr == 0) continue;  // warp-uniform
-            const int knc = __shfl_sync(0xffffffffu, nc, k);
-            const int ku = __shfl_sync(0xffffffffu, u, k), kv = __shfl_sync(0xffffffffu, v, k);
-            const float px = __shfl_sync(0xffffffffu, wp[0], k);
-            const float py = __shfl_sync(0xffffffffu, wp[1], k);
-            const float pz = __shfl_sync(0xffffffffu, wp[2], k);
-            const float pw = __shfl_sync(0xffffffffu, wp[3], k);
-            const float dw = fsub(1.0f, pw);
+        // bounding box of the tile's windows
+        if (threadIdx.x == 0) {
+            s_box[0] = 0x7fffffff; s_box[1] = 0x7fffffff; s_box[2] = -1; s_box[3] = -1;
+        }
+        __syncthreads();
+        if (nr > 0) {
+            atomicMin(&s_box[0], u);
+            atomicMin(&s_box[1], v);
+            atomicMax(&s_box[2], u + nc);
+            atomicMax(&s_box[3], v + nr);
+        }
+        __syncthreads();
+        const int bx0 = s_box[0], by0 = s_box[1], bx1 = s_box[2], by1 = s_box[3];
+        const int bw = bx1 - bx0, bh = by1 - by0;
+        const int pitch = bw | 1;  // odd pitch: vertically adjacent windows hit distinct banks
+        const bool staged = bx1 >= 0 && pitch * bh <= kStagePixels;
+        if (staged) {
+            float* sx = stage;
+            float* sy = stage + kStagePixels;
+            float* sz = stage + 2 * kStagePixels;
+            for (int i = threadIdx.x; i < bw * bh; i += kThreads) {
+                const int ry = i / bw, rx = i - ry * bw;
+                const size_t at = (size_t)(by0 + ry) * a.synth_w + (bx0 + rx);
+                float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (at < n_synth) q = __ldg(a.synth + at);
+                sx[ry * pitch + rx] = q.x;
+                sy[ry * pitch + rx] = q.y;
+                sz[ry * pitch + rx] = q.z;
+            }
+        }
+        __syncthreads();
+        float best = 0.01f;
+        float3 bq = make_float3(0.f, 0.f, 0.f);
+        if (nr > 0) {
+            const float dw = fsub(1.0f, wp[3]);
             const float dw2 = fmul(dw, dw);
-            const int total = knr * knc;
-            int r = lane / knc, c = lane - r * knc;
-            const int step_r = 32 / knc, step_c = 32 - step_r * knc;
-            float best = 0.01f;
-            int best_i = 0x7fffffff;
-            for (int i = lane; i < total; i += 32) {
-                const size_t at = (size_t)(kv + r) * a.synth_w + (ku + c);
-                if (at < n_synth) {
-                    const float4 q = __ldg(a.synth + at);
-                    if (!(q.x == 0.0f && q.y == 0.0f && q.z == 0.0f)) {
-                        const float dx = fsub(q.x, px), dy = fsub(q.y, py), dz = fsub(q.z, pz);
+            if (staged) {
+                const float* sx = stage;
+                const float* sy = stage + kStagePixels;
+                const float* sz = stage + 2 * kStagePixels;
+                int base = (v - by0) * pitch + (u - bx0);
+                for (int r = 0; r < nr; ++r, base += pitch) {
+                    for (int c = 0; c < nc; ++c) {
+                        const float qx = sx[base + c], qy = sy[base + c], qz = sz[base + c];
+                        if (qx == 0.0f && qy == 0.0f && qz == 0.0f) continue;
+                        const float dx = fsub(qx, wp[0]), dy = fsub(qy, wp[1]), dz = fsub(qz, wp[2]);
                         const float l2 = fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fadd(fmul(dz, dz), dw2));
-                        if (l2 < best) {  // scan order within a lane is increasing
+                        if (l2 < best) {
                             best = l2;
-                            best_i = i;
+                            bq = make_float3(qx, qy, qz);
                         }
                     }
                 }
-                r += step_r;
-                c += step_c;
-                if (c >= knc) {
-                    c -= knc;
-                    ++r;
+            } else {
+                for (int r = 0; r < nr; ++r) {
+                    for (int c = 0; c < nc; ++c) {
+                        const size_t at = (size_t)(v + r) * a.synth_w + (u + c);
+                        if (at >= n_synth) continue;
+                        const float4 q = __ldg(a.synth + at);
+                        if (q.x == 0.0f && q.y == 0.0f && q.z == 0.0f) continue;
+                        const float dx = fsub(q.x, wp[0]), dy = fsub(q.y, wp[1]), dz = fsub(q.z, wp[2]);
+                        const float l2 = fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fadd(fmul(dz, dz), dw2));
+                        if (l2 < best) {
+                            best = l2;
+                            bq = make_float3(q.x, q.y, q.z);
+                        }
+                    }
                 }
-            }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const float ob = __shfl_xor_sync(0xffffffffu, best, o);
-                const int oi = __shfl_xor_sync(0xffffffffu, best_i, o);
-                if (ob < best || (ob == best && oi < best_i)) {
-                    best = ob;
-                    best_i = oi;
-                }
-            }
-            if (lane == k) {
-                my_best = best;
-                my_idx = best_i;
             }
         }
-        if (s < n_src) {
+        if (mine) {
             float4 p1 = make_float4(0.f, 0.f, 0.f, 0.f), p2 = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (my_idx != 0x7fffffff) {
-                const int br = my_idx / nc, bc = my_idx - br * nc;
-                const float4 q = __ldg(a.synth + (size_t)(v + br) * a.synth_w + (u + bc));
+            if (best < 0.01f) {
                 p1 = make_float4(wp[0], wp[1], wp[2], wp[3]);
-                p2 = make_float4(q.x, q.y, q.z, 1.0f);
+                p2 = make_float4(bq.x, bq.y, bq.z, 1.0f);
                 acc[0].add(1.0f);
                 acc[1].add(p1.x); acc[2].add(p1.y); acc[3].add(p1.z); acc[4].add(p1.w);
                 acc[5].add(p2.x); acc[6].add(p2.y); acc[7].add(p2.z);
-                acc[8].add(my_best);
+                acc[8].add(best);
             }
             a.src[s] = p1;
             a.dst[s] = p2;  // w = 1 marks an association
         }
+        __syncthreads();  // the staging buffer is reused by the next tile
     }
     double part[9];
     block_reduce<9>(acc, part);
@@ -264,6 +296,7 @@ __global__ void __launch_bounds__(kThreads) k_icp_associate(IcpArgs a, IcpState*
         st->n_assoc = n;
         st->sum_l2 = tot[8];
     }
+    (void)n_src;
 }
 
 // ------------------------------------------------------ FP64 Horn solve
@@ -295,11 +328,13 @@ __device__ void jacobi4(double* A, double* V, const double* V0, bool warm) {
     }
     double scale = 0.0;
     for (int i = 0; i < 16; ++i) scale += a[i] * a[i];
+    // converged once the off-diagonal mass is below (1e-13)^2 of the total:
+    // tighter bounds sit at double rounding noise and never terminate early
     for (int sweep = 0; sweep < 32; ++sweep) {
         double off = 0.0;
         for (int p = 0; p < 4; ++p)
             for (int q = p + 1; q < 4; ++q) off += a[4 * p + q] * a[4 * p + q];
-        if (!(off > 1e-32 * scale)) break;
+        if (!(off > 1e-26 * scale)) break;
         for (int p = 0; p < 3; ++p)
             for (int q = p + 1; q < 4; ++q) {
                 const double apq = a[4 * p + q];
@@ -493,12 +528,19 @@ __global__ void k_bin_resolve(const float* __restrict__ pts, const unsigned long
 cudaError_t icp_align_enqueue(const IcpArgs& a, IcpState* st, const Mat4& guess, int iterations,
                               int ctas, cudaStream_t stream) {
     k_icp_begin<<<1, 32, 0, stream>>>(st, guess);
-    const int n_src = ((a.width + 3) / 4) * a.height;
+    const int n_cols = (a.width + 3) / 4;
+    const int n_src = n_cols * a.height;
     int horn_ctas = (n_src + kThreads * 4 - 1) / (kThreads * 4);
     if (horn_ctas > ctas) horn_ctas = ctas;
     if (horn_ctas < 1) horn_ctas = 1;
+    const int tiles = ((n_cols + kTileCols - 1) / kTileCols) * ((a.height + kTileRows - 1) / kTileRows);
+    int assoc_ctas = tiles < kIcpMaxCtas ? tiles : kIcpMaxCtas;
+    const size_t smem = 3 * kStagePixels * sizeof(float);
+    cudaError_t e = cudaFuncSetAttribute(k_icp_associate, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
     for (int it = 0; it < iterations; ++it) {
-        k_icp_associate<<<ctas, kThreads, 0, stream>>>(a, st);
+        k_icp_associate<<<assoc_ctas, kThreads, smem, stream>>>(a, st);
         k_icp_horn<<<horn_ctas, kThreads, 0, stream>>>(a, st);
     }
     return cudaGetLastError();
