@@ -18,10 +18,10 @@
 //                    (:166-167).
 //  k_icp_horn        the centred 3x3 cross-covariance (:169-197) with the
 //                    same compensated reduction; the last CTA builds Horn's
-//                    symmetric 4x4 matrix (:199-213) in double, solves it with
-//                    a cyclic Jacobi eigen-decomposition in double (Golub &
-//                    Van Loan, sec. 8.5; warm-started from the previous
-//                    step's eigenvectors), turns the dominant eigenvector into
+//                    symmetric 4x4 matrix (:199-213) in double, finds its
+//                    dominant eigenvector in double by Horn's closed form
+//                    (characteristic quartic, Newton, adjugate; a cyclic
+//                    Jacobi solve for degenerate spectra), turns it into
 //                    R and t (:218-256) and accumulates the pose
 //                    step * pose in double (:23-28).  The float pose the next
 //                    association uses is that double pose rounded.
@@ -121,19 +121,27 @@ __device__ __forceinline__ bool last_cta(unsigned int* counter) {
 // threads, so the result does not depend on scheduling.
 template <int NV>
 __device__ __forceinline__ void finish_partials(const IcpState* st, double* out) {
-    __shared__ double red[kThreads];
-    for (int c = 0; c < NV; ++c) {
-        double a = 0.0;
-        for (unsigned int b = threadIdx.x; b < gridDim.x; b += kThreads) a += st->part[b * 16 + c];
-        red[threadIdx.x] = a;
-        __syncthreads();
-        for (int w = kThreads / 2; w > 0; w >>= 1) {
-            if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-            __syncthreads();
-        }
-        if (threadIdx.x == 0) out[c] = red[0];
-        __syncthreads();
+    __shared__ double red[kThreads / 32][NV];
+    double a[NV];
+#pragma unroll
+    for (int c = 0; c < NV; ++c) a[c] = 0.0;
+    for (unsigned int b = threadIdx.x; b < gridDim.x; b += kThreads)
+#pragma unroll
+        for (int c = 0; c < NV; ++c) a[c] += st->part[b * 16 + c];
+#pragma unroll
+    for (int c = 0; c < NV; ++c)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) a[c] += __shfl_xor_sync(0xffffffffu, a[c], o);
+    if ((threadIdx.x & 31) == 0)
+#pragma unroll
+        for (int c = 0; c < NV; ++c) red[threadIdx.x >> 5][c] = a[c];
+    __syncthreads();
+    if (threadIdx.x < NV) {
+        double t = 0.0;
+        for (int w = 0; w < kThreads / 32; ++w) t += red[w][threadIdx.x];
+        out[threadIdx.x] = t;
     }
+    __syncthreads();
 }
 
 // Association (ICP.cpp:66-131).  A CTA owns a tile of 8 source columns x
@@ -362,6 +370,85 @@ __device__ void jacobi4(double* A, double* V, const double* V0, bool warm) {
     for (int i = 0; i < 4; ++i) A[i] = a[5 * i];  // eigenvalues into A[0..3]
 }
 
+// Dominant eigenvector of Horn's symmetric 4x4 N in double by Horn's closed
+// form (B. K. P. Horn, "Closed-form solution of absolute orientation using
+// unit quaternions", JOSA A 4(4), 1987, sec. 3.E-F): the characteristic
+// polynomial det(lambda I - N) from the Faddeev-LeVerrier recursion, its
+// largest root by Newton's method started above the spectrum (the Frobenius
+// norm bounds every eigenvalue; the polynomial is increasing and convex to
+// the right of its largest root, so the iterates decrease monotonically onto
+// it), and the eigenvector as the largest column of adj(N - lambda I), which
+// for a simple eigenvalue is rank one and proportional to it.  Returns false
+// when that column vanishes (a repeated largest eigenvalue); the caller then
+// falls back to the Jacobi solver.
+__device__ bool horn_eigen(const double* N, double* q, double* lambda_out) {
+    double fro = 0.0;
+    for (int i = 0; i < 16; ++i) fro += N[i] * N[i];
+    fro = sqrt(fro);
+    if (!(fro > 0.0)) return false;
+    // Faddeev-LeVerrier: p(l) = l^4 + c3 l^3 + c2 l^2 + c1 l + c0
+    double M[16], T[16], c[4];
+    for (int i = 0; i < 16; ++i) M[i] = N[i];
+    c[3] = -(M[0] + M[5] + M[10] + M[15]);
+    for (int k = 2; k <= 4; ++k) {
+        // M <- N (M + c_{5-k} I)
+        const double ck = c[5 - k];
+        for (int i = 0; i < 4; ++i) M[5 * i] += ck;
+        for (int i = 0; i < 4; ++i)
+            for (int j = 0; j < 4; ++j) {
+                double sum = 0.0;
+                for (int t = 0; t < 4; ++t) sum += N[4 * i + t] * M[4 * t + j];
+                T[4 * i + j] = sum;
+            }
+        for (int i = 0; i < 16; ++i) M[i] = T[i];
+        c[4 - k] = -(M[0] + M[5] + M[10] + M[15]) / (double)k;
+    }
+    double l = fro;
+    for (int it = 0; it < 100; ++it) {
+        const double p = (((l + c[3]) * l + c[2]) * l + c[1]) * l + c[0];
+        const double dp = ((4.0 * l + 3.0 * c[3]) * l + 2.0 * c[2]) * l + c[1];
+        if (!(dp > 0.0)) break;
+        const double step = p / dp;
+        l -= step;
+        if (!(fabs(step) > 1e-15 * fro)) break;
+    }
+    // adjugate column of A = N - l I with the largest diagonal cofactor
+    double A[16];
+    for (int i = 0; i < 16; ++i) A[i] = N[i];
+    for (int i = 0; i < 4; ++i) A[5 * i] -= l;
+    auto cof = [&](int r, int col) {  // (r, col) cofactor of A
+        int rr[3], cc[3], n = 0, m = 0;
+        for (int i = 0; i < 4; ++i)
+            if (i != r) rr[n++] = i;
+        for (int j = 0; j < 4; ++j)
+            if (j != col) cc[m++] = j;
+        const double d =
+            A[4 * rr[0] + cc[0]] * (A[4 * rr[1] + cc[1]] * A[4 * rr[2] + cc[2]] - A[4 * rr[1] + cc[2]] * A[4 * rr[2] + cc[1]]) -
+            A[4 * rr[0] + cc[1]] * (A[4 * rr[1] + cc[0]] * A[4 * rr[2] + cc[2]] - A[4 * rr[1] + cc[2]] * A[4 * rr[2] + cc[0]]) +
+            A[4 * rr[0] + cc[2]] * (A[4 * rr[1] + cc[0]] * A[4 * rr[2] + cc[1]] - A[4 * rr[1] + cc[1]] * A[4 * rr[2] + cc[0]]);
+        return ((r + col) & 1) ? -d : d;
+    };
+    int best = 0;
+    double bd = -1.0;
+    for (int j = 0; j < 4; ++j) {
+        const double d = fabs(cof(j, j));
+        if (d > bd) {
+            bd = d;
+            best = j;
+        }
+    }
+    if (!(bd > 1e-24 * fro * fro * fro)) return false;
+    double nrm = 0.0;
+    for (int k = 0; k < 4; ++k) {
+        q[k] = cof(k, best);  // column `best` of adj(A) = cofactors (best, k) transposed
+        nrm += q[k] * q[k];
+    }
+    nrm = sqrt(nrm);
+    for (int k = 0; k < 4; ++k) q[k] /= nrm;
+    *lambda_out = l;
+    return true;
+}
+
 __global__ void __launch_bounds__(kThreads) k_icp_horn(IcpArgs a, IcpState* __restrict__ st) {
     const int n_cols = (a.width + 3) / 4;
     const int n_src = n_cols * a.height;
@@ -394,16 +481,17 @@ __global__ void __launch_bounds__(kThreads) k_icp_horn(IcpArgs a, IcpState* __re
                     Syz - Szy, Sxx - Syy - Szz, Sxy + Syx, Szx + Sxz,
                     Szx - Sxz, Sxy + Syx, Syy - Sxx - Szz, Syz + Szy,
                     Sxy - Syx, Szx + Sxz, Syz + Szy, Szz - Sxx - Syy};
-    double V[16];
-    jacobi4(N, V, st->V, st->have_V != 0);
-    for (int i = 0; i < 16; ++i) st->V[i] = V[i];
-    st->have_V = 1;
-    int imax = 0;
-    for (int i = 1; i < 4; ++i)
-        if (N[i] > N[imax]) imax = i;
-    double q[4] = {V[0 + imax], V[4 + imax], V[8 + imax], V[12 + imax]};
-    const double ql = sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
-    for (int i = 0; i < 4; ++i) q[i] /= ql;
+    double q[4], lmax;
+    if (!horn_eigen(N, q, &lmax)) {
+        double V[16];
+        jacobi4(N, V, st->V, false);
+        int imax = 0;
+        for (int i = 1; i < 4; ++i)
+            if (N[i] > N[imax]) imax = i;
+        for (int i = 0; i < 4; ++i) q[i] = V[4 * i + imax];
+        const double ql = sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+        for (int i = 0; i < 4; ++i) q[i] /= ql;
+    }
     // quaternion (x = scalar part) to rotation (ICP.cpp:233-254)
     const double xy = q[0] * q[1], xz = q[0] * q[2], xw = q[0] * q[3], yy = q[1] * q[1],
                  yz = q[1] * q[2], yw = q[1] * q[3], zz = q[2] * q[2], zw = q[2] * q[3],
