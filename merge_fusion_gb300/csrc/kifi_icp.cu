@@ -158,22 +158,66 @@ __device__ __forceinline__ void finish_partials(const IcpState* st, double* out)
 // y1 * synth_w + x1 as in the reference; indices past the buffer's end read
 // as invalid points.
 constexpr int kTileCols = 8, kTileRows = 32;
-constexpr int kStagePixels = 6144;
+constexpr int kStagePixels = 4096;
 
+// Scan of one thread's window in the staged region: rows nr, columns nc,
+// plane offset `base` of its first candidate.  Invalid target points were
+// staged with x = NaN, which can never pass `l2 < best`.  Returns the best
+// squared distance (0.01 when none) and its candidate number r * 32 + c.
+template <bool kW>
+__device__ __forceinline__ float scan_staged(const float* __restrict__ sx,
+                                             const float* __restrict__ sy,
+                                             const float* __restrict__ sz, int base, int pitch,
+                                             int nr, int nc, float px, float py, float pz,
+                                             float dw2, int* best_rc) {
+    float best = 0.01f;
+    int bi = -1;
+    auto cand = [&](int at, int rc) {
+        const float dx = fsub(sx[at], px), dy = fsub(sy[at], py), dz = fsub(sz[at], pz);
+        const float zz = kW ? fadd(fmul(dz, dz), dw2) : fmul(dz, dz);
+        const float l2 = fadd(fadd(fmul(dx, dx), fmul(dy, dy)), zz);
+        if (l2 < best) {
+            best = l2;
+            bi = rc;
+        }
+    };
+    if (nc == 21) {
+        for (int r = 0; r < nr; ++r, base += pitch) {
+#pragma unroll
+            for (int c = 0; c < 21; ++c) cand(base + c, r * 32 + c);
+        }
+    } else {
+        for (int r = 0; r < nr; ++r, base += pitch)
+            for (int c = 0; c < nc; ++c) cand(base + c, r * 32 + c);
+    }
+    *best_rc = bi;
+    return best;
+}
+
+// Association (ICP.cpp:66-131).  A CTA owns a tile of 8 source columns x
+// 32 source rows; warp w takes source column w of the tile and lane l source
+// row l, so the 32 lanes of a warp are vertically adjacent sources whose
+// windows sit about one image row apart.  Each thread back-projects and
+// projects its source, the CTA takes the bounding box of the tile's 21x21
+// windows and stages that target region in shared memory as three float
+// planes with an odd row pitch (lanes then hit distinct banks), and every
+// thread scans its own window row by row -- the reference's loop order, so
+// the first strict minimum wins exactly as there.  A region too large for
+// the staging buffer (fast motion) falls back to reading the target from
+// global memory.  Target pixel (y1, x1) is fetched from linear index
+// y1 * synth_w + x1 as in the reference; indices past the buffer's end read
+// as invalid points.
 __global__ void __launch_bounds__(kThreads) k_icp_associate(IcpArgs a, IcpState* __restrict__ st) {
     extern __shared__ float stage[];  // 3 planes of kStagePixels floats
     __shared__ int s_box[4];
+    __shared__ float s_acc[kThreads / 32][9][2];  // per-warp compensated sums
     const int n_cols = (a.width + 3) / 4;
-    const int n_src = n_cols * a.height;
     const int tiles_x = (n_cols + kTileCols - 1) / kTileCols;
     const int tiles_y = (a.height + kTileRows - 1) / kTileRows;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const float half_w = fmul((float)a.synth_w, 0.5f), half_h = fmul((float)a.synth_h, 0.5f);
     const size_t n_synth = (size_t)a.synth_w * a.synth_h;
-    float pose[16];
-#pragma unroll
-    for (int i = 0; i < 16; ++i) pose[i] = st->pose_f[i];
-    KahanF acc[9];  // count, src xyzw, dst xyz, sum of min len^2
+    if (lane < 9) s_acc[warp][lane][0] = s_acc[warp][lane][1] = 0.0f;
     for (int tile = blockIdx.x; tile < tiles_x * tiles_y; tile += gridDim.x) {
         const int tx = tile % tiles_x, ty = tile / tiles_x;
         const int col = tx * kTileCols + warp, y = ty * kTileRows + lane;
@@ -190,7 +234,7 @@ __global__ void __launch_bounds__(kThreads) k_icp_associate(IcpArgs a, IcpState*
                 pt[1] = fmul(fadd(fmul(-(float)y, a.fl_inv_y), a.pp_y), d);
                 pt[2] = fmul(fadd(fmul(-1.0f, 1.0f), 0.0f), d);
                 pt[3] = 1.0f;
-                mat_vec(pose, pt, wp);
+                mat_vec(st->pose_f, pt, wp);
                 mat_vec(a.proj, wp, cl);
                 const float ux = fdiv(cl[0], cl[3]), uy = fdiv(cl[1], cl[3]);
                 u = wrap_sub(cvt_i32_x86(fadd(fmul(ux, half_w), half_w)), 10);
@@ -218,15 +262,17 @@ __global__ void __launch_bounds__(kThreads) k_icp_associate(IcpArgs a, IcpState*
         const int bw = bx1 - bx0, bh = by1 - by0;
         const int pitch = bw | 1;  // odd pitch: vertically adjacent windows hit distinct banks
         const bool staged = bx1 >= 0 && pitch * bh <= kStagePixels;
+        float* sx = stage;
+        float* sy = stage + kStagePixels;
+        float* sz = stage + 2 * kStagePixels;
         if (staged) {
-            float* sx = stage;
-            float* sy = stage + kStagePixels;
-            float* sz = stage + 2 * kStagePixels;
             for (int i = threadIdx.x; i < bw * bh; i += kThreads) {
                 const int ry = i / bw, rx = i - ry * bw;
                 const size_t at = (size_t)(by0 + ry) * a.synth_w + (bx0 + rx);
                 float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
                 if (at < n_synth) q = __ldg(a.synth + at);
+                // (0,0,0) = no point (ICP.cpp:112): stage it as NaN
+                if (q.x == 0.0f && q.y == 0.0f && q.z == 0.0f) q.x = __int_as_float(0x7fffffff);
                 sx[ry * pitch + rx] = q.x;
                 sy[ry * pitch + rx] = q.y;
                 sz[ry * pitch + rx] = q.z;
@@ -239,21 +285,15 @@ __global__ void __launch_bounds__(kThreads) k_icp_associate(IcpArgs a, IcpState*
             const float dw = fsub(1.0f, wp[3]);
             const float dw2 = fmul(dw, dw);
             if (staged) {
-                const float* sx = stage;
-                const float* sy = stage + kStagePixels;
-                const float* sz = stage + 2 * kStagePixels;
-                int base = (v - by0) * pitch + (u - bx0);
-                for (int r = 0; r < nr; ++r, base += pitch) {
-                    for (int c = 0; c < nc; ++c) {
-                        const float qx = sx[base + c], qy = sy[base + c], qz = sz[base + c];
-                        if (qx == 0.0f && qy == 0.0f && qz == 0.0f) continue;
-                        const float dx = fsub(qx, wp[0]), dy = fsub(qy, wp[1]), dz = fsub(qz, wp[2]);
-                        const float l2 = fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fadd(fmul(dz, dz), dw2));
-                        if (l2 < best) {
-                            best = l2;
-                            bq = make_float3(qx, qy, qz);
-                        }
-                    }
+                const int base = (v - by0) * pitch + (u - bx0);
+                int rc;
+                // dz^2 + dw^2 == dz^2 exactly when dw == 0 (dz^2 >= 0)
+                best = dw2 != 0.0f
+                           ? scan_staged<true>(sx, sy, sz, base, pitch, nr, nc, wp[0], wp[1], wp[2], dw2, &rc)
+                           : scan_staged<false>(sx, sy, sz, base, pitch, nr, nc, wp[0], wp[1], wp[2], dw2, &rc);
+                if (rc >= 0) {
+                    const int at = base + (rc >> 5) * pitch + (rc & 31);
+                    bq = make_float3(sx[at], sy[at], sz[at]);
                 }
             } else {
                 for (int r = 0; r < nr; ++r) {
@@ -272,25 +312,44 @@ __global__ void __launch_bounds__(kThreads) k_icp_associate(IcpArgs a, IcpState*
                 }
             }
         }
+        const bool hit = mine && best < 0.01f;
         if (mine) {
             float4 p1 = make_float4(0.f, 0.f, 0.f, 0.f), p2 = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (best < 0.01f) {
+            if (hit) {
                 p1 = make_float4(wp[0], wp[1], wp[2], wp[3]);
                 p2 = make_float4(bq.x, bq.y, bq.z, 1.0f);
-                acc[0].add(1.0f);
-                acc[1].add(p1.x); acc[2].add(p1.y); acc[3].add(p1.z); acc[4].add(p1.w);
-                acc[5].add(p2.x); acc[6].add(p2.y); acc[7].add(p2.z);
-                acc[8].add(best);
             }
             a.src[s] = p1;
             a.dst[s] = p2;  // w = 1 marks an association
         }
+        // this tile's contribution to the centroid sums: compensated warp
+        // sums folded into the warp's Kahan accumulators
+        if (__any_sync(0xffffffffu, hit)) {
+            const float vals[9] = {hit ? 1.0f : 0.0f, hit ? wp[0] : 0.0f, hit ? wp[1] : 0.0f,
+                                   hit ? wp[2] : 0.0f, hit ? wp[3] : 0.0f, hit ? bq.x : 0.0f,
+                                   hit ? bq.y : 0.0f, hit ? bq.z : 0.0f, hit ? best : 0.0f};
+#pragma unroll
+            for (int i = 0; i < 9; ++i) {
+                const double w = warp_sum_comp(vals[i], 0.0f);
+                if (lane == 0) {
+                    KahanF k{s_acc[warp][i][0], s_acc[warp][i][1]};
+                    const float hi = (float)w;
+                    k.add(hi);
+                    k.add((float)(w - (double)hi));
+                    s_acc[warp][i][0] = k.s;
+                    s_acc[warp][i][1] = k.c;
+                }
+            }
+        }
         __syncthreads();  // the staging buffer is reused by the next tile
     }
-    double part[9];
-    block_reduce<9>(acc, part);
-    if (threadIdx.x == 0)
-        for (int i = 0; i < 9; ++i) st->part[blockIdx.x * 16 + i] = part[i];
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < 9; ++i) {
+            double t = 0.0;
+            for (int w = 0; w < kThreads / 32; ++w) t += (double)s_acc[w][i][0] - (double)s_acc[w][i][1];
+            st->part[blockIdx.x * 16 + i] = t;
+        }
+    }
     if (!last_cta(&st->done)) return;
     __shared__ double tot[9];
     finish_partials<9>(st, tot);
@@ -304,7 +363,6 @@ __global__ void __launch_bounds__(kThreads) k_icp_associate(IcpArgs a, IcpState*
         st->n_assoc = n;
         st->sum_l2 = tot[8];
     }
-    (void)n_src;
 }
 
 // ------------------------------------------------------ FP64 Horn solve
@@ -370,83 +428,150 @@ __device__ void jacobi4(double* A, double* V, const double* V0, bool warm) {
     for (int i = 0; i < 4; ++i) A[i] = a[5 * i];  // eigenvalues into A[0..3]
 }
 
-// Dominant eigenvector of Horn's symmetric 4x4 N in double by Horn's closed
-// form (B. K. P. Horn, "Closed-form solution of absolute orientation using
-// unit quaternions", JOSA A 4(4), 1987, sec. 3.E-F): the characteristic
+// Warp 0 of the finishing CTA: Horn's N from S in double, its dominant
+// eigenvector by Horn's closed form (B. K. P. Horn, "Closed-form solution of absolute
+// orientation using unit quaternions", JOSA A 4(4), 1987): the characteristic
 // polynomial det(lambda I - N) from the Faddeev-LeVerrier recursion, its
-// largest root by Newton's method started above the spectrum (the Frobenius
-// norm bounds every eigenvalue; the polynomial is increasing and convex to
-// the right of its largest root, so the iterates decrease monotonically onto
-// it), and the eigenvector as the largest column of adj(N - lambda I), which
-// for a simple eigenvalue is rank one and proportional to it.  Returns false
-// when that column vanishes (a repeated largest eigenvalue); the caller then
-// falls back to the Jacobi solver.
-__device__ bool horn_eigen(const double* N, double* q, double* lambda_out) {
-    double fro = 0.0;
-    for (int i = 0; i < 16; ++i) fro += N[i] * N[i];
-    fro = sqrt(fro);
-    if (!(fro > 0.0)) return false;
-    // Faddeev-LeVerrier: p(l) = l^4 + c3 l^3 + c2 l^2 + c1 l + c0
-    double M[16], T[16], c[4];
-    for (int i = 0; i < 16; ++i) M[i] = N[i];
-    c[3] = -(M[0] + M[5] + M[10] + M[15]);
+// largest root by Newton's method from the Frobenius norm (an upper bound of
+// the spectrum; the polynomial is increasing and convex right of its largest
+// root, so the iterates fall monotonically onto it), and the eigenvector as
+// the largest column of adj(N - lambda I), rank one for a simple eigenvalue.
+// A repeated largest eigenvalue falls back to the Jacobi solver.  Matrix
+// products and cofactors are spread over lanes (GB300's double-precision units are few, so a
+// shorter dependent chain matters more than the operation count), then R, t
+// and pose <- (T R) pose in double (ICP.cpp:199-264, :23-28).
+__device__ void horn_solve_warp(const double* S, IcpState* __restrict__ st, float ms0, float ms1,
+                                float ms2, float md0, float md1, float md2) {
+    __shared__ double sN[16], sM[16], sA[16], sq[4], sT[16];
+    __shared__ int s_ok;
+    const int lane = threadIdx.x;
+    if (lane == 0) {
+        const double Sxx = S[0], Sxy = S[1], Sxz = S[2], Syx = S[3], Syy = S[4], Syz = S[5],
+                     Szx = S[6], Szy = S[7], Szz = S[8];
+        const double N[16] = {Sxx + Syy + Szz, Syz - Szy, Szx - Sxz, Sxy - Syx,
+                              Syz - Szy, Sxx - Syy - Szz, Sxy + Syx, Szx + Sxz,
+                              Szx - Sxz, Sxy + Syx, Syy - Sxx - Szz, Syz + Szy,
+                              Sxy - Syx, Szx + Sxz, Syz + Szy, Szz - Sxx - Syy};
+        for (int i = 0; i < 16; ++i) sN[i] = sM[i] = N[i];
+    }
+    __syncwarp();
+    const int r = (lane >> 2) & 3, c = lane & 3;
+    double x = lane < 16 ? sN[lane] * sN[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    const double fro = sqrt(x);
+    auto trace_of = [&](const double* m) {
+        return (m[0] + m[5]) + (m[10] + m[15]);
+    };
+    double cf[4];
+    cf[3] = -trace_of(sM);
     for (int k = 2; k <= 4; ++k) {
-        // M <- N (M + c_{5-k} I)
-        const double ck = c[5 - k];
-        for (int i = 0; i < 4; ++i) M[5 * i] += ck;
-        for (int i = 0; i < 4; ++i)
-            for (int j = 0; j < 4; ++j) {
-                double sum = 0.0;
-                for (int t = 0; t < 4; ++t) sum += N[4 * i + t] * M[4 * t + j];
-                T[4 * i + j] = sum;
-            }
-        for (int i = 0; i < 16; ++i) M[i] = T[i];
-        c[4 - k] = -(M[0] + M[5] + M[10] + M[15]) / (double)k;
+        const double ck = cf[5 - k];
+        double t = 0.0;
+        if (lane < 16)
+            for (int j = 0; j < 4; ++j) t += sN[4 * r + j] * (sM[4 * j + c] + (j == c ? ck : 0.0));
+        __syncwarp();
+        if (lane < 16) sM[lane] = t;
+        __syncwarp();
+        cf[4 - k] = -trace_of(sM) / (double)k;
     }
     double l = fro;
     for (int it = 0; it < 100; ++it) {
-        const double p = (((l + c[3]) * l + c[2]) * l + c[1]) * l + c[0];
-        const double dp = ((4.0 * l + 3.0 * c[3]) * l + 2.0 * c[2]) * l + c[1];
+        const double p = (((l + cf[3]) * l + cf[2]) * l + cf[1]) * l + cf[0];
+        const double dp = ((4.0 * l + 3.0 * cf[3]) * l + 2.0 * cf[2]) * l + cf[1];
         if (!(dp > 0.0)) break;
         const double step = p / dp;
         l -= step;
         if (!(fabs(step) > 1e-15 * fro)) break;
     }
-    // adjugate column of A = N - l I with the largest diagonal cofactor
-    double A[16];
-    for (int i = 0; i < 16; ++i) A[i] = N[i];
-    for (int i = 0; i < 4; ++i) A[5 * i] -= l;
-    auto cof = [&](int r, int col) {  // (r, col) cofactor of A
+    if (lane < 16) sA[lane] = sN[lane] - (r == c ? l : 0.0);
+    __syncwarp();
+    // (row, col) cofactor of A
+    auto cof = [&](int row, int col) {
         int rr[3], cc[3], n = 0, m = 0;
         for (int i = 0; i < 4; ++i)
-            if (i != r) rr[n++] = i;
+            if (i != row) rr[n++] = i;
         for (int j = 0; j < 4; ++j)
             if (j != col) cc[m++] = j;
         const double d =
-            A[4 * rr[0] + cc[0]] * (A[4 * rr[1] + cc[1]] * A[4 * rr[2] + cc[2]] - A[4 * rr[1] + cc[2]] * A[4 * rr[2] + cc[1]]) -
-            A[4 * rr[0] + cc[1]] * (A[4 * rr[1] + cc[0]] * A[4 * rr[2] + cc[2]] - A[4 * rr[1] + cc[2]] * A[4 * rr[2] + cc[0]]) +
-            A[4 * rr[0] + cc[2]] * (A[4 * rr[1] + cc[0]] * A[4 * rr[2] + cc[1]] - A[4 * rr[1] + cc[1]] * A[4 * rr[2] + cc[0]]);
-        return ((r + col) & 1) ? -d : d;
+            sA[4 * rr[0] + cc[0]] * (sA[4 * rr[1] + cc[1]] * sA[4 * rr[2] + cc[2]] - sA[4 * rr[1] + cc[2]] * sA[4 * rr[2] + cc[1]]) -
+            sA[4 * rr[0] + cc[1]] * (sA[4 * rr[1] + cc[0]] * sA[4 * rr[2] + cc[2]] - sA[4 * rr[1] + cc[2]] * sA[4 * rr[2] + cc[0]]) +
+            sA[4 * rr[0] + cc[2]] * (sA[4 * rr[1] + cc[0]] * sA[4 * rr[2] + cc[1]] - sA[4 * rr[1] + cc[1]] * sA[4 * rr[2] + cc[0]]);
+        return ((row + col) & 1) ? -d : d;
     };
-    int best = 0;
-    double bd = -1.0;
-    for (int j = 0; j < 4; ++j) {
-        const double d = fabs(cof(j, j));
-        if (d > bd) {
-            bd = d;
-            best = j;
+    // the largest diagonal cofactor selects the adjugate column
+    double dj = lane < 4 ? fabs(cof(lane, lane)) : -1.0;
+    int bj = lane;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const double od = __shfl_xor_sync(0xffffffffu, dj, o);
+        const int oj = __shfl_xor_sync(0xffffffffu, bj, o);
+        if (od > dj || (od == dj && oj < bj)) {
+            dj = od;
+            bj = oj;
         }
     }
-    if (!(bd > 1e-24 * fro * fro * fro)) return false;
-    double nrm = 0.0;
-    for (int k = 0; k < 4; ++k) {
-        q[k] = cof(k, best);  // column `best` of adj(A) = cofactors (best, k) transposed
-        nrm += q[k] * q[k];
+    const bool ok = dj > 1e-24 * fro * fro * fro;
+    double qk = (ok && lane < 4) ? cof(lane, bj) : 0.0;
+    double n2 = qk * qk;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) n2 += __shfl_xor_sync(0xffffffffu, n2, o);
+    if (lane < 4) sq[lane] = qk / sqrt(n2);
+    if (lane == 0) s_ok = ok;
+    __syncwarp();
+    if (!s_ok && lane == 0) {
+        // repeated largest eigenvalue: cyclic Jacobi in double
+        double A[16], V[16];
+        for (int i = 0; i < 16; ++i) A[i] = sN[i];
+        jacobi4(A, V, V, false);
+        int imax = 0;
+        for (int i = 1; i < 4; ++i)
+            if (A[i] > A[imax]) imax = i;
+        double nn = 0.0;
+        for (int i = 0; i < 4; ++i) nn += V[4 * i + imax] * V[4 * i + imax];
+        nn = sqrt(nn);
+        for (int i = 0; i < 4; ++i) sq[i] = V[4 * i + imax] / nn;
     }
-    nrm = sqrt(nrm);
-    for (int k = 0; k < 4; ++k) q[k] /= nrm;
-    *lambda_out = l;
-    return true;
+    __syncwarp();
+    if (lane == 0) {
+        const double q[4] = {sq[0], sq[1], sq[2], sq[3]};
+        // quaternion (x = scalar part) to rotation (ICP.cpp:233-254)
+        const double xy = q[0] * q[1], xz = q[0] * q[2], xw = q[0] * q[3], yy = q[1] * q[1],
+                     yz = q[1] * q[2], yw = q[1] * q[3], zz = q[2] * q[2], zw = q[2] * q[3],
+                     ww = q[3] * q[3];
+        const double R[9] = {1.0 - 2.0 * (zz + ww), 2.0 * (yz - xw),       2.0 * (yw + xz),
+                             2.0 * (yz + xw),       1.0 - 2.0 * (yy + ww), 2.0 * (zw - xy),
+                             2.0 * (yw - xz),       2.0 * (zw + xy),       1.0 - 2.0 * (yy + zz)};
+        const double ms[3] = {(double)ms0, (double)ms1, (double)ms2};
+        const double md[3] = {(double)md0, (double)md1, (double)md2};
+        for (int i = 0; i < 16; ++i) sT[i] = (i % 5 == 0) ? 1.0 : 0.0;
+        for (int rr = 0; rr < 3; ++rr) {
+            double t = md[rr];
+            for (int cc = 0; cc < 3; ++cc) {
+                sT[4 * rr + cc] = R[3 * rr + cc];
+                t -= R[3 * rr + cc] * ms[cc];
+            }
+            sT[4 * rr + 3] = t;
+        }
+    }
+    __syncwarp();
+    // pose <- step * pose, one entry per lane
+    double pnew = 0.0;
+    if (lane < 16)
+        for (int k = 0; k < 4; ++k) pnew += sT[4 * r + k] * st->pose[4 * k + c];
+    __syncwarp();
+    if (lane < 16) {
+        st->pose[lane] = pnew;
+        st->pose_f[4 * c + r] = (float)pnew;
+    }
+    if (lane == 0) {
+        const int it = st->iter;
+        if (it < kIcpMaxStats) {
+            st->stats[it].n_assoc = st->n_assoc;
+            st->stats[it].rms = st->n_assoc > 0 ? sqrt(st->sum_l2 / st->n_assoc) : 0.0;
+        }
+        st->iter = it + 1;
+    }
 }
 
 __global__ void __launch_bounds__(kThreads) k_icp_horn(IcpArgs a, IcpState* __restrict__ st) {
@@ -473,61 +598,8 @@ __global__ void __launch_bounds__(kThreads) k_icp_horn(IcpArgs a, IcpState* __re
     if (!last_cta(&st->done)) return;
     __shared__ double S[9];
     finish_partials<9>(st, S);
-    if (threadIdx.x != 0) return;
-    const double Sxx = S[0], Sxy = S[1], Sxz = S[2], Syx = S[3], Syy = S[4], Syz = S[5],
-                 Szx = S[6], Szy = S[7], Szz = S[8];
-    // Horn's N (ICP.cpp:199-213), symmetric
-    double N[16] = {Sxx + Syy + Szz, Syz - Szy, Szx - Sxz, Sxy - Syx,
-                    Syz - Szy, Sxx - Syy - Szz, Sxy + Syx, Szx + Sxz,
-                    Szx - Sxz, Sxy + Syx, Syy - Sxx - Szz, Syz + Szy,
-                    Sxy - Syx, Szx + Sxz, Syz + Szy, Szz - Sxx - Syy};
-    double q[4], lmax;
-    if (!horn_eigen(N, q, &lmax)) {
-        double V[16];
-        jacobi4(N, V, st->V, false);
-        int imax = 0;
-        for (int i = 1; i < 4; ++i)
-            if (N[i] > N[imax]) imax = i;
-        for (int i = 0; i < 4; ++i) q[i] = V[4 * i + imax];
-        const double ql = sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
-        for (int i = 0; i < 4; ++i) q[i] /= ql;
-    }
-    // quaternion (x = scalar part) to rotation (ICP.cpp:233-254)
-    const double xy = q[0] * q[1], xz = q[0] * q[2], xw = q[0] * q[3], yy = q[1] * q[1],
-                 yz = q[1] * q[2], yw = q[1] * q[3], zz = q[2] * q[2], zw = q[2] * q[3],
-                 ww = q[3] * q[3];
-    const double R[9] = {1.0 - 2.0 * (zz + ww), 2.0 * (yz - xw),       2.0 * (yw + xz),
-                         2.0 * (yz + xw),       1.0 - 2.0 * (yy + ww), 2.0 * (zw - xy),
-                         2.0 * (yw - xz),       2.0 * (zw + xy),       1.0 - 2.0 * (yy + zz)};
-    double T[16];  // step = T * R, row-major
-    for (int r = 0; r < 4; ++r)
-        for (int c = 0; c < 4; ++c) T[4 * r + c] = (r == c) ? 1.0 : 0.0;
-    const double ms[3] = {(double)ms0, (double)ms1, (double)ms2};
-    const double md[3] = {(double)md0, (double)md1, (double)md2};
-    for (int r = 0; r < 3; ++r) {
-        double t = md[r];
-        for (int c = 0; c < 3; ++c) {
-            T[4 * r + c] = R[3 * r + c];
-            t -= R[3 * r + c] * ms[c];
-        }
-        T[4 * r + 3] = t;
-    }
-    double P[16];
-    for (int r = 0; r < 4; ++r)
-        for (int c = 0; c < 4; ++c) {
-            double s = 0.0;
-            for (int k = 0; k < 4; ++k) s += T[4 * r + k] * st->pose[4 * k + c];
-            P[4 * r + c] = s;
-        }
-    for (int i = 0; i < 16; ++i) st->pose[i] = P[i];
-    for (int r = 0; r < 4; ++r)
-        for (int c = 0; c < 4; ++c) st->pose_f[4 * c + r] = (float)P[4 * r + c];
-    const int it = st->iter;
-    if (it < kIcpMaxStats) {
-        st->stats[it].n_assoc = st->n_assoc;
-        st->stats[it].rms = st->n_assoc > 0 ? sqrt(st->sum_l2 / st->n_assoc) : 0.0;
-    }
-    st->iter = it + 1;
+    if (threadIdx.x >= 32) return;
+    horn_solve_warp(S, st, ms0, ms1, ms2, md0, md1, md2);
 }
 
 __global__ void k_icp_begin(IcpState* st, Mat4 guess) {
@@ -618,7 +690,7 @@ cudaError_t icp_align_enqueue(const IcpArgs& a, IcpState* st, const Mat4& guess,
     k_icp_begin<<<1, 32, 0, stream>>>(st, guess);
     const int n_cols = (a.width + 3) / 4;
     const int n_src = n_cols * a.height;
-    int horn_ctas = (n_src + kThreads * 4 - 1) / (kThreads * 4);
+    int horn_ctas = (n_src + kThreads - 1) / kThreads;
     if (horn_ctas > ctas) horn_ctas = ctas;
     if (horn_ctas < 1) horn_ctas = 1;
     const int tiles = ((n_cols + kTileCols - 1) / kTileCols) * ((a.height + kTileRows - 1) / kTileRows);
