@@ -55,45 +55,54 @@ struct KahanF {
     }
 };
 
-// TwoSum-based warp reduction of a compensated pair (s, c)
+// Float-float (double-single) sums: a value is hi + lo with |lo| <= ulp(hi)/2.
+// GB300 runs double precision at a small fraction of the float rate, so the
+// compensated reductions stay in float pairs and only the final cross-CTA
+// total is formed in double.
+struct FF {
+    float hi, lo;
+};
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
     s = fadd(a, b);
     float bb = fsub(s, a);
     e = fadd(fsub(a, fsub(s, bb)), fsub(b, bb));
 }
-__device__ __forceinline__ double warp_sum_comp(float s, float c) {
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+    float s, e;
+    two_sum(a.hi, b.hi, s, e);
+    e = fadd(e, fadd(a.lo, b.lo));
+    const float hi = fadd(s, e);
+    return FF{hi, fsub(e, fsub(hi, s))};
+}
+__device__ __forceinline__ FF warp_sum_ff(FF v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        float s2 = __shfl_xor_sync(0xffffffffu, s, o);
-        float c2 = __shfl_xor_sync(0xffffffffu, c, o);
-        float ns, e;
-        two_sum(s, s2, ns, e);
-        c = fadd(fadd(c, c2), e);
-        s = ns;
+        FF w{__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+        v = ff_add(v, w);
     }
-    return (double)s + (double)c;
+    return v;
 }
+__device__ __forceinline__ FF ff_of(const KahanF& k) { return FF{k.s, -k.c}; }
 
-// block reduction of NV compensated values to double partials (thread 0 gets them)
+// Block reduction of NV Kahan accumulators into this CTA's float-float
+// partials in st->part (2 floats per component).
 template <int NV>
-__device__ __forceinline__ void block_reduce(const KahanF (&k)[NV], double (&out)[NV]) {
-    __shared__ double sh[kThreads / 32][NV];
+__device__ __forceinline__ void block_partials(const KahanF (&k)[NV], float* part) {
+    __shared__ FF sh[kThreads / 32][NV];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int i = 0; i < NV; ++i) {
-        double w = warp_sum_comp(k[i].s, -k[i].c);
+        FF w = warp_sum_ff(ff_of(k[i]));
         if (lane == 0) sh[warp][i] = w;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-#pragma unroll
-        for (int i = 0; i < NV; ++i) {
-            double a = 0.0;
-            for (int w = 0; w < kThreads / 32; ++w) a += sh[w][i];
-            out[i] = a;
-        }
+    if (threadIdx.x < NV) {
+        FF t = sh[0][threadIdx.x];
+        for (int w = 1; w < kThreads / 32; ++w) t = ff_add(t, sh[w][threadIdx.x]);
+        part[2 * threadIdx.x] = t.hi;
+        part[2 * threadIdx.x + 1] = t.lo;
+        __threadfence();  // publish before the CTA signals completion
     }
-    __syncthreads();
 }
 
 __device__ __forceinline__ float load_depth(const void* depth, size_t i, bool u16) {
@@ -116,82 +125,85 @@ __device__ __forceinline__ bool last_cta(unsigned int* counter) {
     return last;
 }
 
-// Sums the per-CTA double partials of NV components with the whole (last)
-// CTA: thread t adds CTAs t, t+256, ... and a fixed-shape tree combines the
-// threads, so the result does not depend on scheduling.
+// Sums the per-CTA float-float partials of NV components with the whole
+// (last) CTA: thread t adds CTAs t, t+256, ... in float-float, warps combine
+// with shuffles, and the 8 warp totals are added in double -- a fixed order,
+// so the result does not depend on scheduling.
 template <int NV>
 __device__ __forceinline__ void finish_partials(const IcpState* st, double* out) {
-    __shared__ double red[kThreads / 32][NV];
-    double a[NV];
+    __shared__ FF red[kThreads / 32][NV];
+    FF a[NV];
 #pragma unroll
-    for (int c = 0; c < NV; ++c) a[c] = 0.0;
+    for (int c = 0; c < NV; ++c) a[c] = FF{0.0f, 0.0f};
     for (unsigned int b = threadIdx.x; b < gridDim.x; b += kThreads)
 #pragma unroll
-        for (int c = 0; c < NV; ++c) a[c] += st->part[b * 16 + c];
+        for (int c = 0; c < NV; ++c)
+            a[c] = ff_add(a[c], FF{st->part[b * 32 + 2 * c], st->part[b * 32 + 2 * c + 1]});
 #pragma unroll
-    for (int c = 0; c < NV; ++c)
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) a[c] += __shfl_xor_sync(0xffffffffu, a[c], o);
+    for (int c = 0; c < NV; ++c) a[c] = warp_sum_ff(a[c]);
     if ((threadIdx.x & 31) == 0)
 #pragma unroll
         for (int c = 0; c < NV; ++c) red[threadIdx.x >> 5][c] = a[c];
     __syncthreads();
     if (threadIdx.x < NV) {
         double t = 0.0;
-        for (int w = 0; w < kThreads / 32; ++w) t += red[w][threadIdx.x];
+        for (int w = 0; w < kThreads / 32; ++w)
+            t += (double)red[w][threadIdx.x].hi + (double)red[w][threadIdx.x].lo;
         out[threadIdx.x] = t;
     }
     __syncthreads();
 }
 
-// Association (ICP.cpp:66-131).  A CTA owns a tile of 8 source columns x
-// 32 source rows; warp w takes source column w of the tile and lane l source
-// row l, so the 32 lanes of a warp are vertically adjacent sources whose
-// windows sit about one image row apart.  Each thread back-projects and
-// projects its source, the CTA takes the bounding box of the tile's 21x21
-// windows and stages that target region in shared memory as three float
-// planes with an odd row pitch (lanes then hit distinct banks), and every
-// thread scans its own window row by row -- the reference's loop order, so
-// the first strict minimum wins exactly as there.  A region too large for
-// the staging buffer (fast motion) falls back to reading the target from
-// global memory.  Target pixel (y1, x1) is fetched from linear index
-// y1 * synth_w + x1 as in the reference; indices past the buffer's end read
-// as invalid points.
 constexpr int kTileCols = 8, kTileRows = 32;
-constexpr int kStagePixels = 4096;
+constexpr int kStagePixels = 3840;  // float4 per pixel: 60 KB
 
-// Scan of one thread's window in the staged region: rows nr, columns nc,
-// plane offset `base` of its first candidate.  Invalid target points were
-// staged with x = NaN, which can never pass `l2 < best`.  Returns the best
-// squared distance (0.01 when none) and its candidate number r * 32 + c.
+// Scan of one thread's window in the staged region (float4 per pixel,
+// `base` = its first candidate, odd row pitch).  Invalid target points were
+// staged with x = NaN, which never passes `l2 < best`.  Three interleaved
+// chains (columns mod 3) keep their own first strict minimum so that the
+// compare/select dependencies overlap; the lexicographic (l2, candidate)
+// minimum of the chains is the first strict minimum of the row-major scan.
+// Returns the best squared distance (0.01 when none) and its candidate
+// number r * 32 + c (-1 when none).
 template <bool kW>
-__device__ __forceinline__ float scan_staged(const float* __restrict__ sx,
-                                             const float* __restrict__ sy,
-                                             const float* __restrict__ sz, int base, int pitch,
+__device__ __forceinline__ float scan_staged(const float4* __restrict__ sp, int base, int pitch,
                                              int nr, int nc, float px, float py, float pz,
                                              float dw2, int* best_rc) {
-    float best = 0.01f;
-    int bi = -1;
-    auto cand = [&](int at, int rc) {
-        const float dx = fsub(sx[at], px), dy = fsub(sy[at], py), dz = fsub(sz[at], pz);
+    float b0 = 0.01f, b1 = 0.01f, b2 = 0.01f;
+    int i0 = 0x7fffffff, i1 = 0x7fffffff, i2 = 0x7fffffff;
+    auto cand = [&](int at, int rc, float& b, int& bi) {
+        const float4 q = sp[at];
+        const float dx = fsub(q.x, px), dy = fsub(q.y, py), dz = fsub(q.z, pz);
         const float zz = kW ? fadd(fmul(dz, dz), dw2) : fmul(dz, dz);
         const float l2 = fadd(fadd(fmul(dx, dx), fmul(dy, dy)), zz);
-        if (l2 < best) {
-            best = l2;
+        if (l2 < b) {
+            b = l2;
             bi = rc;
         }
     };
     if (nc == 21) {
         for (int r = 0; r < nr; ++r, base += pitch) {
 #pragma unroll
-            for (int c = 0; c < 21; ++c) cand(base + c, r * 32 + c);
+            for (int c = 0; c < 21; c += 3) {
+                cand(base + c, r * 32 + c, b0, i0);
+                cand(base + c + 1, r * 32 + c + 1, b1, i1);
+                cand(base + c + 2, r * 32 + c + 2, b2, i2);
+            }
         }
     } else {
         for (int r = 0; r < nr; ++r, base += pitch)
-            for (int c = 0; c < nc; ++c) cand(base + c, r * 32 + c);
+            for (int c = 0; c < nc; ++c) cand(base + c, r * 32 + c, b0, i0);
     }
-    *best_rc = bi;
-    return best;
+    if (b1 < b0 || (b1 == b0 && i1 < i0)) {
+        b0 = b1;
+        i0 = i1;
+    }
+    if (b2 < b0 || (b2 == b0 && i2 < i0)) {
+        b0 = b2;
+        i0 = i2;
+    }
+    *best_rc = i0 == 0x7fffffff ? -1 : i0;
+    return b0;
 }
 
 // Association (ICP.cpp:66-131).  A CTA owns a tile of 8 source columns x
@@ -208,16 +220,16 @@ __device__ __forceinline__ float scan_staged(const float* __restrict__ sx,
 // y1 * synth_w + x1 as in the reference; indices past the buffer's end read
 // as invalid points.
 __global__ void __launch_bounds__(kThreads) k_icp_associate(IcpArgs a, IcpState* __restrict__ st) {
-    extern __shared__ float stage[];  // 3 planes of kStagePixels floats
+    extern __shared__ float4 stage[];  // kStagePixels target points
     __shared__ int s_box[4];
-    __shared__ float s_acc[kThreads / 32][9][2];  // per-warp compensated sums
+    __shared__ FF s_acc[kThreads / 32][9];  // per-warp float-float sums
     const int n_cols = (a.width + 3) / 4;
     const int tiles_x = (n_cols + kTileCols - 1) / kTileCols;
     const int tiles_y = (a.height + kTileRows - 1) / kTileRows;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const float half_w = fmul((float)a.synth_w, 0.5f), half_h = fmul((float)a.synth_h, 0.5f);
     const size_t n_synth = (size_t)a.synth_w * a.synth_h;
-    if (lane < 9) s_acc[warp][lane][0] = s_acc[warp][lane][1] = 0.0f;
+    if (lane < 9) s_acc[warp][lane] = FF{0.0f, 0.0f};
     for (int tile = blockIdx.x; tile < tiles_x * tiles_y; tile += gridDim.x) {
         const int tx = tile % tiles_x, ty = tile / tiles_x;
         const int col = tx * kTileCols + warp, y = ty * kTileRows + lane;
@@ -262,9 +274,6 @@ __global__ void __launch_bounds__(kThreads) k_icp_associate(IcpArgs a, IcpState*
         const int bw = bx1 - bx0, bh = by1 - by0;
         const int pitch = bw | 1;  // odd pitch: vertically adjacent windows hit distinct banks
         const bool staged = bx1 >= 0 && pitch * bh <= kStagePixels;
-        float* sx = stage;
-        float* sy = stage + kStagePixels;
-        float* sz = stage + 2 * kStagePixels;
         if (staged) {
             for (int i = threadIdx.x; i < bw * bh; i += kThreads) {
                 const int ry = i / bw, rx = i - ry * bw;
@@ -273,9 +282,7 @@ __global__ void __launch_bounds__(kThreads) k_icp_associate(IcpArgs a, IcpState*
                 if (at < n_synth) q = __ldg(a.synth + at);
                 // (0,0,0) = no point (ICP.cpp:112): stage it as NaN
                 if (q.x == 0.0f && q.y == 0.0f && q.z == 0.0f) q.x = __int_as_float(0x7fffffff);
-                sx[ry * pitch + rx] = q.x;
-                sy[ry * pitch + rx] = q.y;
-                sz[ry * pitch + rx] = q.z;
+                stage[ry * pitch + rx] = q;
             }
         }
         __syncthreads();
@@ -289,11 +296,11 @@ __global__ void __launch_bounds__(kThreads) k_icp_associate(IcpArgs a, IcpState*
                 int rc;
                 // dz^2 + dw^2 == dz^2 exactly when dw == 0 (dz^2 >= 0)
                 best = dw2 != 0.0f
-                           ? scan_staged<true>(sx, sy, sz, base, pitch, nr, nc, wp[0], wp[1], wp[2], dw2, &rc)
-                           : scan_staged<false>(sx, sy, sz, base, pitch, nr, nc, wp[0], wp[1], wp[2], dw2, &rc);
+                           ? scan_staged<true>(stage, base, pitch, nr, nc, wp[0], wp[1], wp[2], dw2, &rc)
+                           : scan_staged<false>(stage, base, pitch, nr, nc, wp[0], wp[1], wp[2], dw2, &rc);
                 if (rc >= 0) {
-                    const int at = base + (rc >> 5) * pitch + (rc & 31);
-                    bq = make_float3(sx[at], sy[at], sz[at]);
+                    const float4 q = stage[base + (rc >> 5) * pitch + (rc & 31)];
+                    bq = make_float3(q.x, q.y, q.z);
                 }
             } else {
                 for (int r = 0; r < nr; ++r) {
@@ -330,25 +337,19 @@ __global__ void __launch_bounds__(kThreads) k_icp_associate(IcpArgs a, IcpState*
                                    hit ? bq.y : 0.0f, hit ? bq.z : 0.0f, hit ? best : 0.0f};
 #pragma unroll
             for (int i = 0; i < 9; ++i) {
-                const double w = warp_sum_comp(vals[i], 0.0f);
-                if (lane == 0) {
-                    KahanF k{s_acc[warp][i][0], s_acc[warp][i][1]};
-                    const float hi = (float)w;
-                    k.add(hi);
-                    k.add((float)(w - (double)hi));
-                    s_acc[warp][i][0] = k.s;
-                    s_acc[warp][i][1] = k.c;
-                }
+                const FF w = warp_sum_ff(FF{vals[i], 0.0f});
+                if (lane == 0) s_acc[warp][i] = ff_add(s_acc[warp][i], w);
             }
         }
         __syncthreads();  // the staging buffer is reused by the next tile
     }
-    if (threadIdx.x == 0) {
-        for (int i = 0; i < 9; ++i) {
-            double t = 0.0;
-            for (int w = 0; w < kThreads / 32; ++w) t += (double)s_acc[w][i][0] - (double)s_acc[w][i][1];
-            st->part[blockIdx.x * 16 + i] = t;
-        }
+    __syncthreads();
+    if (threadIdx.x < 9) {
+        FF t = s_acc[0][threadIdx.x];
+        for (int w = 1; w < kThreads / 32; ++w) t = ff_add(t, s_acc[w][threadIdx.x]);
+        st->part[blockIdx.x * 32 + 2 * threadIdx.x] = t.hi;
+        st->part[blockIdx.x * 32 + 2 * threadIdx.x + 1] = t.lo;
+        __threadfence();  // publish before the CTA signals completion
     }
     if (!last_cta(&st->done)) return;
     __shared__ double tot[9];
@@ -591,10 +592,7 @@ __global__ void __launch_bounds__(kThreads) k_icp_horn(IcpArgs a, IcpState* __re
         acc[3].add(fmul(sy, dx)); acc[4].add(fmul(sy, dy)); acc[5].add(fmul(sy, dz));
         acc[6].add(fmul(sz, dx)); acc[7].add(fmul(sz, dy)); acc[8].add(fmul(sz, dz));
     }
-    double part[9];
-    block_reduce<9>(acc, part);
-    if (threadIdx.x == 0)
-        for (int i = 0; i < 9; ++i) st->part[blockIdx.x * 16 + i] = part[i];
+    block_partials<9>(acc, st->part + blockIdx.x * 32);
     if (!last_cta(&st->done)) return;
     __shared__ double S[9];
     finish_partials<9>(st, S);
@@ -695,7 +693,7 @@ cudaError_t icp_align_enqueue(const IcpArgs& a, IcpState* st, const Mat4& guess,
     if (horn_ctas < 1) horn_ctas = 1;
     const int tiles = ((n_cols + kTileCols - 1) / kTileCols) * ((a.height + kTileRows - 1) / kTileRows);
     int assoc_ctas = tiles < kIcpMaxCtas ? tiles : kIcpMaxCtas;
-    const size_t smem = 3 * kStagePixels * sizeof(float);
+    const size_t smem = kStagePixels * sizeof(float4);
     cudaError_t e = cudaFuncSetAttribute(k_icp_associate, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
