@@ -44,17 +44,6 @@ __device__ __forceinline__ int cvt_i32_x86(float f) {
 }
 __device__ __forceinline__ int wrap_sub(int a, int b) { return (int)((unsigned int)a - (unsigned int)b); }
 
-// compensated float accumulator (Kahan; kahan_sum, numeric.h:59-68)
-struct KahanF {
-    float s = 0.0f, c = 0.0f;
-    __device__ __forceinline__ void add(float x) {
-        float y = fsub(x, c);
-        float t = fadd(s, y);
-        c = fsub(fsub(t, s), y);
-        s = t;
-    }
-};
-
 // Float-float (double-single) sums: a value is hi + lo with |lo| <= ulp(hi)/2.
 // GB300 runs double precision at a small fraction of the float rate, so the
 // compensated reductions stay in float pairs and only the final cross-CTA
@@ -82,29 +71,6 @@ __device__ __forceinline__ FF warp_sum_ff(FF v) {
     }
     return v;
 }
-__device__ __forceinline__ FF ff_of(const KahanF& k) { return FF{k.s, -k.c}; }
-
-// Block reduction of NV Kahan accumulators into this CTA's float-float
-// partials in st->part (2 floats per component).
-template <int NV>
-__device__ __forceinline__ void block_partials(const KahanF (&k)[NV], float* part) {
-    __shared__ FF sh[kThreads / 32][NV];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int i = 0; i < NV; ++i) {
-        FF w = warp_sum_ff(ff_of(k[i]));
-        if (lane == 0) sh[warp][i] = w;
-    }
-    __syncthreads();
-    if (threadIdx.x < NV) {
-        FF t = sh[0][threadIdx.x];
-        for (int w = 1; w < kThreads / 32; ++w) t = ff_add(t, sh[w][threadIdx.x]);
-        part[2 * threadIdx.x] = t.hi;
-        part[2 * threadIdx.x + 1] = t.lo;
-        __threadfence();  // publish before the CTA signals completion
-    }
-}
-
 __device__ __forceinline__ float load_depth(const void* depth, size_t i, bool u16) {
     if (u16) return fmul((float)(unsigned int)__ldg((const unsigned short*)depth + i), 0.001f);
     return __ldg((const float*)depth + i);
@@ -131,14 +97,14 @@ __device__ __forceinline__ bool last_cta(unsigned int* counter) {
 // so the result does not depend on scheduling.
 template <int NV>
 __device__ __forceinline__ void finish_partials(const IcpState* st, double* out) {
-    __shared__ FF red[kThreads / 32][NV];
+    __shared__ FF red[32][NV];
     FF a[NV];
 #pragma unroll
     for (int c = 0; c < NV; ++c) a[c] = FF{0.0f, 0.0f};
-    for (unsigned int b = threadIdx.x; b < gridDim.x; b += kThreads)
+    for (unsigned int b = threadIdx.x; b < gridDim.x; b += blockDim.x)
 #pragma unroll
         for (int c = 0; c < NV; ++c)
-            a[c] = ff_add(a[c], FF{st->part[b * 32 + 2 * c], st->part[b * 32 + 2 * c + 1]});
+            a[c] = ff_add(a[c], FF{st->part[b * 48 + 2 * c], st->part[b * 48 + 2 * c + 1]});
 #pragma unroll
     for (int c = 0; c < NV; ++c) a[c] = warp_sum_ff(a[c]);
     if ((threadIdx.x & 31) == 0)
@@ -147,7 +113,7 @@ __device__ __forceinline__ void finish_partials(const IcpState* st, double* out)
     __syncthreads();
     if (threadIdx.x < NV) {
         double t = 0.0;
-        for (int w = 0; w < kThreads / 32; ++w)
+        for (int w = 0; w < (int)(blockDim.x / 32); ++w)
             t += (double)red[w][threadIdx.x].hi + (double)red[w][threadIdx.x].lo;
         out[threadIdx.x] = t;
     }
@@ -206,35 +172,59 @@ __device__ __forceinline__ float scan_staged(const float4* __restrict__ sp, int 
     return b0;
 }
 
-// Association (ICP.cpp:66-131).  A CTA owns a tile of 8 source columns x
-// 32 source rows; warp w takes source column w of the tile and lane l source
-// row l, so the 32 lanes of a warp are vertically adjacent sources whose
-// windows sit about one image row apart.  Each thread back-projects and
-// projects its source, the CTA takes the bounding box of the tile's 21x21
-// windows and stages that target region in shared memory as three float
-// planes with an odd row pitch (lanes then hit distinct banks), and every
-// thread scans its own window row by row -- the reference's loop order, so
-// the first strict minimum wins exactly as there.  A region too large for
-// the staging buffer (fast motion) falls back to reading the target from
-// global memory.  Target pixel (y1, x1) is fetched from linear index
-// y1 * synth_w + x1 as in the reference; indices past the buffer's end read
-// as invalid points.
-__global__ void __launch_bounds__(kThreads) k_icp_associate(IcpArgs a, IcpState* __restrict__ st) {
+__device__ __noinline__ void horn_solve_warp(const double* S, IcpState* __restrict__ st,
+                                             const double* mu);
+
+// One ICP::AlignStep (ICP.cpp:35-265) as one kernel.
+//
+// Association (:66-131): a CTA owns a tile of 8 source columns x 32 source
+// rows.  Warp w takes source column w/2 of the tile and lane l source row l,
+// so a warp's lanes are vertically adjacent sources whose windows sit about
+// one image row apart; the two warps of a column split each 21x21 window
+// into rows 0-10 and 11-20.  Each thread back-projects and projects its
+// source, the CTA stages the bounding box of the tile's windows in shared
+// memory (float4 per pixel, odd row pitch: lanes hit distinct banks) and each
+// thread scans its rows in the reference's loop order; the halves are merged
+// by (len^2, scan position), so the first strict minimum wins as in the
+// reference.  A region too large for the staging buffer (fast motion) is
+// read from global memory instead.  Target pixel (y1, x1) is linear index
+// y1 * synth_w + x1 as in the reference; indices past the buffer's end are
+// invalid points.
+//
+// Horn's sums: instead of a second pass over the pairs for the centred
+// cross-covariance (:169-197), the kernel accumulates the raw moments --
+// count, sum p, sum q, sum p_r q_c (each product split exactly into a
+// float-float pair by an FMA) and the squared distances -- in float-float
+// per warp and CTA; the last CTA to finish totals them in double, forms the
+// centroids and S = sum p q^T - n mu_p mu_q^T in double, and runs the Horn
+// solve.  Algebraically this is the reference's two-pass sum; numerically it
+// is at least as accurate.
+constexpr int kAssocThreads = 512;
+constexpr int kMoments = 17;  // n, p xyz, q xyz, p q^T (9), len^2
+
+__device__ __forceinline__ FF two_prod(float a, float b) {
+    const float p = fmul(a, b);
+    return FF{p, __fmaf_rn(a, b, -p)};  // exact remainder of the product
+}
+
+__global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step(IcpArgs a, IcpState* __restrict__ st) {
     extern __shared__ float4 stage[];  // kStagePixels target points
     __shared__ int s_box[4];
-    __shared__ FF s_acc[kThreads / 32][9];  // per-warp float-float sums
+    __shared__ float s_hb[kTileCols][32];  // lower half's best len^2 per source
+    __shared__ int s_hi[kTileCols][32];    // and its candidate number
+    __shared__ FF s_acc[kTileCols][kMoments];
     const int n_cols = (a.width + 3) / 4;
     const int tiles_x = (n_cols + kTileCols - 1) / kTileCols;
     const int tiles_y = (a.height + kTileRows - 1) / kTileRows;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int wcol = warp >> 1, half = warp & 1;
     const float half_w = fmul((float)a.synth_w, 0.5f), half_h = fmul((float)a.synth_h, 0.5f);
     const size_t n_synth = (size_t)a.synth_w * a.synth_h;
-    if (lane < 9) s_acc[warp][lane] = FF{0.0f, 0.0f};
+    if (half == 0 && lane < kMoments) s_acc[wcol][lane] = FF{0.0f, 0.0f};
     for (int tile = blockIdx.x; tile < tiles_x * tiles_y; tile += gridDim.x) {
         const int tx = tile % tiles_x, ty = tile / tiles_x;
-        const int col = tx * kTileCols + warp, y = ty * kTileRows + lane;
+        const int col = tx * kTileCols + wcol, y = ty * kTileRows + lane;
         const bool mine = col < n_cols && y < a.height;
-        const int s = y * n_cols + col;
         float wp[4] = {0.f, 0.f, 0.f, 0.f};
         int u = 0, v = 0, nr = 0, nc = 0;
         if (mine) {
@@ -263,7 +253,7 @@ __global__ void __launch_bounds__(kThreads) k_icp_associate(IcpArgs a, IcpState*
             s_box[0] = 0x7fffffff; s_box[1] = 0x7fffffff; s_box[2] = -1; s_box[3] = -1;
         }
         __syncthreads();
-        if (nr > 0) {
+        if (nr > 0 && half == 0) {
             atomicMin(&s_box[0], u);
             atomicMin(&s_box[1], v);
             atomicMax(&s_box[2], u + nc);
@@ -275,7 +265,7 @@ __global__ void __launch_bounds__(kThreads) k_icp_associate(IcpArgs a, IcpState*
         const int pitch = bw | 1;  // odd pitch: vertically adjacent windows hit distinct banks
         const bool staged = bx1 >= 0 && pitch * bh <= kStagePixels;
         if (staged) {
-            for (int i = threadIdx.x; i < bw * bh; i += kThreads) {
+            for (int i = threadIdx.x; i < bw * bh; i += kAssocThreads) {
                 const int ry = i / bw, rx = i - ry * bw;
                 const size_t at = (size_t)(by0 + ry) * a.synth_w + (bx0 + rx);
                 float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -286,24 +276,27 @@ __global__ void __launch_bounds__(kThreads) k_icp_associate(IcpArgs a, IcpState*
             }
         }
         __syncthreads();
+        // this thread's rows of the window
+        const int r0 = half ? 11 : 0, r1 = half ? nr : min(nr, 11);
         float best = 0.01f;
+        int rc = -1;
         float3 bq = make_float3(0.f, 0.f, 0.f);
-        if (nr > 0) {
+        if (r1 > r0) {
             const float dw = fsub(1.0f, wp[3]);
             const float dw2 = fmul(dw, dw);
             if (staged) {
-                const int base = (v - by0) * pitch + (u - bx0);
-                int rc;
+                const int base = (v + r0 - by0) * pitch + (u - bx0);
                 // dz^2 + dw^2 == dz^2 exactly when dw == 0 (dz^2 >= 0)
                 best = dw2 != 0.0f
-                           ? scan_staged<true>(stage, base, pitch, nr, nc, wp[0], wp[1], wp[2], dw2, &rc)
-                           : scan_staged<false>(stage, base, pitch, nr, nc, wp[0], wp[1], wp[2], dw2, &rc);
+                           ? scan_staged<true>(stage, base, pitch, r1 - r0, nc, wp[0], wp[1], wp[2], dw2, &rc)
+                           : scan_staged<false>(stage, base, pitch, r1 - r0, nc, wp[0], wp[1], wp[2], dw2, &rc);
                 if (rc >= 0) {
                     const float4 q = stage[base + (rc >> 5) * pitch + (rc & 31)];
                     bq = make_float3(q.x, q.y, q.z);
+                    rc += r0 * 32;
                 }
             } else {
-                for (int r = 0; r < nr; ++r) {
+                for (int r = r0; r < r1; ++r) {
                     for (int c = 0; c < nc; ++c) {
                         const size_t at = (size_t)(v + r) * a.synth_w + (u + c);
                         if (at >= n_synth) continue;
@@ -313,64 +306,86 @@ __global__ void __launch_bounds__(kThreads) k_icp_associate(IcpArgs a, IcpState*
                         const float l2 = fadd(fadd(fmul(dx, dx), fmul(dy, dy)), fadd(fmul(dz, dz), dw2));
                         if (l2 < best) {
                             best = l2;
+                            rc = r * 32 + c;
                             bq = make_float3(q.x, q.y, q.z);
                         }
                     }
                 }
             }
         }
-        const bool hit = mine && best < 0.01f;
-        if (mine) {
-            float4 p1 = make_float4(0.f, 0.f, 0.f, 0.f), p2 = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (hit) {
-                p1 = make_float4(wp[0], wp[1], wp[2], wp[3]);
-                p2 = make_float4(bq.x, bq.y, bq.z, 1.0f);
-            }
-            a.src[s] = p1;
-            a.dst[s] = p2;  // w = 1 marks an association
+        // merge the halves: the upper rows come earlier in scan order
+        if (half == 1) {
+            s_hb[wcol][lane] = best;
+            s_hi[wcol][lane] = rc;
         }
-        // this tile's contribution to the centroid sums: compensated warp
-        // sums folded into the warp's Kahan accumulators
-        if (__any_sync(0xffffffffu, hit)) {
-            const float vals[9] = {hit ? 1.0f : 0.0f, hit ? wp[0] : 0.0f, hit ? wp[1] : 0.0f,
-                                   hit ? wp[2] : 0.0f, hit ? wp[3] : 0.0f, hit ? bq.x : 0.0f,
-                                   hit ? bq.y : 0.0f, hit ? bq.z : 0.0f, hit ? best : 0.0f};
+        __syncthreads();
+        if (half == 0) {
+            const float ob = s_hb[wcol][lane];
+            const int oi = s_hi[wcol][lane];
+            if (oi >= 0 && (rc < 0 || ob < best)) {
+                best = ob;
+                rc = oi;
+                const size_t at = (size_t)(v + (oi >> 5)) * a.synth_w + (u + (oi & 31));
+                const float4 q = staged ? stage[(v + (oi >> 5) - by0) * pitch + (u + (oi & 31) - bx0)]
+                                        : __ldg(a.synth + at);
+                bq = make_float3(q.x, q.y, q.z);
+            }
+            const bool hit = mine && rc >= 0;
+            // this tile's raw moments, folded into the warp's accumulators
+            if (__any_sync(0xffffffffu, hit)) {
+                const float px = hit ? wp[0] : 0.f, py = hit ? wp[1] : 0.f, pz = hit ? wp[2] : 0.f;
+                const float qx = hit ? bq.x : 0.f, qy = hit ? bq.y : 0.f, qz = hit ? bq.z : 0.f;
+                const float pv[3] = {px, py, pz}, qv[3] = {qx, qy, qz};
 #pragma unroll
-            for (int i = 0; i < 9; ++i) {
-                const FF w = warp_sum_ff(FF{vals[i], 0.0f});
-                if (lane == 0) s_acc[warp][i] = ff_add(s_acc[warp][i], w);
+                for (int i = 0; i < kMoments; ++i) {
+                    FF m;
+                    if (i == 0) m = FF{hit ? 1.0f : 0.0f, 0.0f};
+                    else if (i < 4) m = FF{pv[i - 1], 0.0f};
+                    else if (i < 7) m = FF{qv[i - 4], 0.0f};
+                    else if (i < 16) m = two_prod(pv[(i - 7) / 3], qv[(i - 7) % 3]);
+                    else m = FF{hit ? best : 0.0f, 0.0f};
+                    const FF w = warp_sum_ff(m);
+                    if (lane == 0) s_acc[wcol][i] = ff_add(s_acc[wcol][i], w);
+                }
             }
         }
-        __syncthreads();  // the staging buffer is reused by the next tile
+        __syncthreads();  // staging buffer and half results are reused by the next tile
     }
-    __syncthreads();
-    if (threadIdx.x < 9) {
+    if (threadIdx.x < kMoments) {
         FF t = s_acc[0][threadIdx.x];
-        for (int w = 1; w < kThreads / 32; ++w) t = ff_add(t, s_acc[w][threadIdx.x]);
-        st->part[blockIdx.x * 32 + 2 * threadIdx.x] = t.hi;
-        st->part[blockIdx.x * 32 + 2 * threadIdx.x + 1] = t.lo;
+        for (int w = 1; w < kTileCols; ++w) t = ff_add(t, s_acc[w][threadIdx.x]);
+        st->part[blockIdx.x * 48 + 2 * threadIdx.x] = t.hi;
+        st->part[blockIdx.x * 48 + 2 * threadIdx.x + 1] = t.lo;
         __threadfence();  // publish before the CTA signals completion
     }
     if (!last_cta(&st->done)) return;
-    __shared__ double tot[9];
-    finish_partials<9>(st, tot);
+    __shared__ double tot[kMoments];
+    finish_partials<kMoments>(st, tot);
+    if (threadIdx.x >= 32) return;
+    // centroids and the centred cross-covariance (ICP.cpp:166-197)
+    const double n = tot[0];
+    __shared__ double S[9];
+    __shared__ double mu[6];
     if (threadIdx.x == 0) {
-        const int n = (int)(tot[0] + 0.5);
-        const float nf = (float)n;
-        // srcMedianSum / float4(n) (ICP.cpp:166-167)
-        for (int i = 0; i < 4; ++i) st->mu_s[i] = fdiv((float)tot[1 + i], nf);
-        for (int i = 0; i < 3; ++i) st->mu_d[i] = fdiv((float)tot[5 + i], nf);
-        st->mu_d[3] = fdiv(nf, nf);
-        st->n_assoc = n;
-        st->sum_l2 = tot[8];
+        for (int i = 0; i < 6; ++i) mu[i] = tot[1 + i] / n;
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) S[3 * r + c] = tot[7 + 3 * r + c] - n * mu[r] * mu[3 + c];
+        st->n_assoc = (int)(n + 0.5);
+        st->sum_l2 = tot[16];
+        for (int i = 0; i < 3; ++i) {
+            st->mu_s[i] = (float)mu[i];
+            st->mu_d[i] = (float)mu[3 + i];
+        }
     }
+    __syncwarp();
+    horn_solve_warp(S, st, mu);
 }
 
 // ------------------------------------------------------ FP64 Horn solve
 // Cyclic Jacobi on a symmetric 4x4 (row-major) in double; V accumulates the
 // rotations (columns are eigenvectors).  Starting from V0 (the previous
 // solve's eigenvectors) the matrix is first rotated into that basis.
-__device__ void jacobi4(double* A, double* V, const double* V0, bool warm) {
+__device__ __noinline__ void jacobi4(double* A, double* V, const double* V0, bool warm) {
     double a[16];
     if (warm) {
         double t[16];
@@ -441,8 +456,8 @@ __device__ void jacobi4(double* A, double* V, const double* V0, bool warm) {
 // products and cofactors are spread over lanes (GB300's double-precision units are few, so a
 // shorter dependent chain matters more than the operation count), then R, t
 // and pose <- (T R) pose in double (ICP.cpp:199-264, :23-28).
-__device__ void horn_solve_warp(const double* S, IcpState* __restrict__ st, float ms0, float ms1,
-                                float ms2, float md0, float md1, float md2) {
+__device__ __noinline__ void horn_solve_warp(const double* S, IcpState* __restrict__ st,
+                                             const double* mu) {
     __shared__ double sN[16], sM[16], sA[16], sq[4], sT[16];
     __shared__ int s_ok;
     const int lane = threadIdx.x;
@@ -543,8 +558,8 @@ __device__ void horn_solve_warp(const double* S, IcpState* __restrict__ st, floa
         const double R[9] = {1.0 - 2.0 * (zz + ww), 2.0 * (yz - xw),       2.0 * (yw + xz),
                              2.0 * (yz + xw),       1.0 - 2.0 * (yy + ww), 2.0 * (zw - xy),
                              2.0 * (yw - xz),       2.0 * (zw + xy),       1.0 - 2.0 * (yy + zz)};
-        const double ms[3] = {(double)ms0, (double)ms1, (double)ms2};
-        const double md[3] = {(double)md0, (double)md1, (double)md2};
+        const double ms[3] = {mu[0], mu[1], mu[2]};
+        const double md[3] = {mu[3], mu[4], mu[5]};
         for (int i = 0; i < 16; ++i) sT[i] = (i % 5 == 0) ? 1.0 : 0.0;
         for (int rr = 0; rr < 3; ++rr) {
             double t = md[rr];
@@ -573,31 +588,6 @@ __device__ void horn_solve_warp(const double* S, IcpState* __restrict__ st, floa
         }
         st->iter = it + 1;
     }
-}
-
-__global__ void __launch_bounds__(kThreads) k_icp_horn(IcpArgs a, IcpState* __restrict__ st) {
-    const int n_cols = (a.width + 3) / 4;
-    const int n_src = n_cols * a.height;
-    const float ms0 = st->mu_s[0], ms1 = st->mu_s[1], ms2 = st->mu_s[2];
-    const float md0 = st->mu_d[0], md1 = st->mu_d[1], md2 = st->mu_d[2];
-    KahanF acc[9];
-    for (int s = blockIdx.x * kThreads + threadIdx.x; s < n_src; s += gridDim.x * kThreads) {
-        const float4 q = a.dst[s];
-        if (q.w == 0.0f) continue;
-        const float4 p = a.src[s];
-        // src = float4(p1, 1) - srcMedian, dst likewise (ICP.cpp:180-184)
-        const float sx = fsub(p.x, ms0), sy = fsub(p.y, ms1), sz = fsub(p.z, ms2);
-        const float dx = fsub(q.x, md0), dy = fsub(q.y, md1), dz = fsub(q.z, md2);
-        acc[0].add(fmul(sx, dx)); acc[1].add(fmul(sx, dy)); acc[2].add(fmul(sx, dz));
-        acc[3].add(fmul(sy, dx)); acc[4].add(fmul(sy, dy)); acc[5].add(fmul(sy, dz));
-        acc[6].add(fmul(sz, dx)); acc[7].add(fmul(sz, dy)); acc[8].add(fmul(sz, dz));
-    }
-    block_partials<9>(acc, st->part + blockIdx.x * 32);
-    if (!last_cta(&st->done)) return;
-    __shared__ double S[9];
-    finish_partials<9>(st, S);
-    if (threadIdx.x >= 32) return;
-    horn_solve_warp(S, st, ms0, ms1, ms2, md0, md1, md2);
 }
 
 __global__ void k_icp_begin(IcpState* st, Mat4 guess) {
@@ -684,23 +674,16 @@ __global__ void k_bin_resolve(const float* __restrict__ pts, const unsigned long
 }  // namespace
 
 cudaError_t icp_align_enqueue(const IcpArgs& a, IcpState* st, const Mat4& guess, int iterations,
-                              int ctas, cudaStream_t stream) {
+                              int /*ctas*/, cudaStream_t stream) {
     k_icp_begin<<<1, 32, 0, stream>>>(st, guess);
     const int n_cols = (a.width + 3) / 4;
-    const int n_src = n_cols * a.height;
-    int horn_ctas = (n_src + kThreads - 1) / kThreads;
-    if (horn_ctas > ctas) horn_ctas = ctas;
-    if (horn_ctas < 1) horn_ctas = 1;
     const int tiles = ((n_cols + kTileCols - 1) / kTileCols) * ((a.height + kTileRows - 1) / kTileRows);
-    int assoc_ctas = tiles < kIcpMaxCtas ? tiles : kIcpMaxCtas;
+    const int ctas = tiles < kIcpMaxCtas ? tiles : kIcpMaxCtas;
     const size_t smem = kStagePixels * sizeof(float4);
-    cudaError_t e = cudaFuncSetAttribute(k_icp_associate, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+    cudaError_t e =
+        cudaFuncSetAttribute(k_icp_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    for (int it = 0; it < iterations; ++it) {
-        k_icp_associate<<<assoc_ctas, kThreads, smem, stream>>>(a, st);
-        k_icp_horn<<<horn_ctas, kThreads, 0, stream>>>(a, st);
-    }
+    for (int it = 0; it < iterations; ++it) k_icp_step<<<ctas, kAssocThreads, smem, stream>>>(a, st);
     return cudaGetLastError();
 }
 

@@ -130,7 +130,7 @@ struct IcpState {
     int iter;
     double sum_l2;
     IcpIterStats stats[kIcpMaxStats];
-    float part[kIcpMaxCtas * 32];   // per-CTA float-float partial sums (16 components)
+    float part[kIcpMaxCtas * 48];   // per-CTA float-float partial sums (24 components)
 };
 
 cudaError_t icp_align_enqueue(const IcpArgs& a, IcpState* st, const Mat4& guess, int iterations,
