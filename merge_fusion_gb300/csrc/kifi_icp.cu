@@ -253,11 +253,18 @@ __global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step(IcpArgs a, IcpSta
             s_box[0] = 0x7fffffff; s_box[1] = 0x7fffffff; s_box[2] = -1; s_box[3] = -1;
         }
         __syncthreads();
-        if (nr > 0 && half == 0) {
-            atomicMin(&s_box[0], u);
-            atomicMin(&s_box[1], v);
-            atomicMax(&s_box[2], u + nc);
-            atomicMax(&s_box[3], v + nr);
+        if (half == 0) {  // warp-uniform; one shared atomic per warp and bound
+            const bool has = nr > 0;
+            const int mu0 = (int)__reduce_min_sync(0xffffffffu, has ? (unsigned)u : 0x7fffffffu);
+            const int mv0 = (int)__reduce_min_sync(0xffffffffu, has ? (unsigned)v : 0x7fffffffu);
+            const int mu1 = __reduce_max_sync(0xffffffffu, has ? u + nc : -1);
+            const int mv1 = __reduce_max_sync(0xffffffffu, has ? v + nr : -1);
+            if (lane == 0 && mu1 >= 0) {
+                atomicMin(&s_box[0], mu0);
+                atomicMin(&s_box[1], mv0);
+                atomicMax(&s_box[2], mu1);
+                atomicMax(&s_box[3], mv1);
+            }
         }
         __syncthreads();
         const int bx0 = s_box[0], by0 = s_box[1], bx1 = s_box[2], by1 = s_box[3];

@@ -116,26 +116,66 @@ __global__ void __launch_bounds__(kEmitThreads) k_splat_emit(DeviceCtl* __restri
         if (lane == 0 && ex) atomicMax(&ctl->excluded_key, ex);
         // neighbouring pixels often land in one voxel: one emitter per key
         unsigned int peers = __match_any_sync(0xffffffffu, valid ? key : 0xffffffffu);
-        bool emitter = valid && (lane == __ffs(peers) - 1);
+        const bool emitter = valid && (lane == __ffs(peers) - 1);
+        // The dilation's 8 keys are 4 (y, z) rows of an (x, x+1) pair.  The
+        // pair's bits are adjacent in the bitmap, so one word probe covers
+        // both unless x is the last bit of its word.  All probes are issued
+        // before any decision; atomics only for bits still clear.
+        uint32_t got[4] = {0u, 0u, 0u, 0u};   // bit 0: key + dx=0 new, bit 1: dx=1 new
+        if (emitter) {
+            uint32_t* wp[4];
+            uint32_t* wq[4];
+            uint32_t m0[4], m1[4], pre0[4], pre1[4];
 #pragma unroll
-        for (int o = 0; o < 8; ++o) {
-            bool mine = false;
-            uint32_t nk = key + pack30(o & 1, (o >> 1) & 1, o >> 2);
-            if (emitter) {
-                size_t b = bit_index(nk, g.res);
-                uint32_t mask = 1u << (b & 31);
-                uint32_t* word = bitmap + (b >> 5);
-                if (!(*(volatile uint32_t*)word & mask)) mine = !(atomicOr(word, mask) & mask);
+            for (int o = 0; o < 4; ++o) {
+                const uint32_t k0 = key + pack30(0, o & 1, o >> 1);
+                const size_t b = bit_index(k0, g.res);
+                const uint32_t sh = (uint32_t)(b & 31);
+                wp[o] = bitmap + (b >> 5);
+                wq[o] = bitmap + ((b + 1) >> 5);
+                m0[o] = sh == 31 ? 0x80000000u : (3u << sh);
+                m1[o] = sh == 31 ? 1u : 0u;
+                pre0[o] = __ldcg(wp[o]);
+                pre1[o] = sh == 31 ? __ldcg(wq[o]) : 0u;
             }
-            unsigned int ballot = __ballot_sync(0xffffffffu, mine);
-            if (!ballot) continue;
+#pragma unroll
+            for (int o = 0; o < 4; ++o) {
+                const uint32_t sh = m0[o] == 0x80000000u && m1[o] ? 31u : (uint32_t)(__ffs(m0[o]) - 1);
+                uint32_t need0 = m0[o] & ~pre0[o];
+                uint32_t need1 = m1[o] & ~pre1[o];
+                uint32_t flipped0 = 0u, flipped1 = 0u;
+                if (need0) flipped0 = need0 & ~atomicOr(wp[o], need0);
+                if (need1) flipped1 = need1 & ~atomicOr(wq[o], need1);
+                // dx = 0 is bit sh of word 0; dx = 1 is bit sh+1 of word 0, or bit 0 of word 1
+                const uint32_t n0 = (flipped0 >> sh) & 1u;
+                const uint32_t n1 = m1[o] ? (flipped1 & 1u) : ((flipped0 >> (sh + 1)) & 1u);
+                got[o] = n0 | (n1 << 1);
+            }
+        }
+        // warp-aggregated append: one atomic per warp
+        const unsigned int cnt = __popc(got[0] | (got[1] << 2) | (got[2] << 4) | (got[3] << 6));
+        unsigned int incl = cnt;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const unsigned int y = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= d) incl += y;
+        }
+        const unsigned int total = __shfl_sync(0xffffffffu, incl, 31);
+        if (total) {
             unsigned int base = 0;
-            if (lane == __ffs(ballot) - 1) base = atomicAdd(&ctl->n_new, (unsigned int)__popc(ballot));
-            base = __shfl_sync(0xffffffffu, base, __ffs(ballot) - 1);
-            if (mine) {
-                unsigned int at = base + __popc(ballot & ((1u << lane) - 1u));
-                if (at < new_cap) new_keys[at] = nk;
-                else atomicOr(&ctl->status, KIFI_DEV_ERR_CAPACITY);
+            if (lane == 31) base = atomicAdd(&ctl->n_new, total);
+            base = __shfl_sync(0xffffffffu, base, 31);
+            unsigned int at = base + incl - cnt;
+#pragma unroll
+            for (int o = 0; o < 4; ++o) {
+                const uint32_t k0 = key + pack30(0, o & 1, o >> 1);
+#pragma unroll
+                for (int dx = 0; dx < 2; ++dx) {
+                    if (!((got[o] >> dx) & 1u)) continue;
+                    if (at < new_cap) new_keys[at] = k0 + (uint32_t)dx;
+                    else atomicOr(&ctl->status, KIFI_DEV_ERR_CAPACITY);
+                    ++at;
+                }
             }
         }
     }
