@@ -141,6 +141,8 @@ struct FrameConst {
     float half_w, half_h;      // width*0.5, height*0.5
     float max_index;           // res - 1
     int width, height;
+    int z_bounded;             // |clip z| <= 1e18 for every voxel centre of the volume
+    int fast_uv;               // frame small enough for the reciprocal fast path
 };
 
 KIFI_HD FrameConst make_frame_const(const kifi_camera& cam, const Mat4& world_to_eye, int res) {
@@ -156,7 +158,21 @@ KIFI_HD FrameConst make_frame_const(const kifi_camera& cam, const Mat4& world_to
     f.max_index = (float)(res - 1);
     f.width = cam.width;
     f.height = cam.height;
+    f.z_bounded = 0;
+    f.fast_uv = (cam.width <= 4096 && cam.height <= 4096) ? 1 : 0;
     return f;
+}
+
+// Host-side bound for UpdateVoxels' z lane: voxel centres lie in the cube
+// [-side/2, side/2]^3 with w = 1, so |clip z| <= sum_j |m[2][j]| * side/2
+// + |m[2][3]| (with slack for the float roundings of the four products).
+inline int clip_z_bounded(const Mat4& w2c, float side) {
+    double b = 0.0;
+    for (int j = 0; j < 3; ++j) b += fabs((double)w2c.m[4 * j + 2]) * (0.5 * side + 1.0);
+    b += fabs((double)w2c.m[14]);
+    for (int i = 0; i < 16; ++i)
+        if (!(fabs((double)w2c.m[i]) < 1e30)) return 0;
+    return b * 1.001 <= 1e18 ? 1 : 0;
 }
 
 // --------------------------------------------------- device control block

@@ -172,8 +172,7 @@ __device__ __forceinline__ float scan_staged(const float4* __restrict__ sp, int 
     return b0;
 }
 
-__device__ __noinline__ void horn_solve_warp(const double* S, IcpState* __restrict__ st,
-                                             const double* mu);
+__device__ __noinline__ void finish_step(IcpState* __restrict__ st, unsigned int n_ctas);
 
 // One ICP::AlignStep (ICP.cpp:35-265) as one kernel.
 //
@@ -366,26 +365,7 @@ __global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step(IcpArgs a, IcpSta
         __threadfence();  // publish before the CTA signals completion
     }
     if (!last_cta(&st->done)) return;
-    __shared__ double tot[kMoments];
-    finish_partials<kMoments>(st, tot);
-    if (threadIdx.x >= 32) return;
-    // centroids and the centred cross-covariance (ICP.cpp:166-197)
-    const double n = tot[0];
-    __shared__ double S[9];
-    __shared__ double mu[6];
-    if (threadIdx.x == 0) {
-        for (int i = 0; i < 6; ++i) mu[i] = tot[1 + i] / n;
-        for (int r = 0; r < 3; ++r)
-            for (int c = 0; c < 3; ++c) S[3 * r + c] = tot[7 + 3 * r + c] - n * mu[r] * mu[3 + c];
-        st->n_assoc = (int)(n + 0.5);
-        st->sum_l2 = tot[16];
-        for (int i = 0; i < 3; ++i) {
-            st->mu_s[i] = (float)mu[i];
-            st->mu_d[i] = (float)mu[3 + i];
-        }
-    }
-    __syncwarp();
-    horn_solve_warp(S, st, mu);
+    if (threadIdx.x < 32) finish_step(st, gridDim.x);
 }
 
 // ------------------------------------------------------ FP64 Horn solve
@@ -451,43 +431,101 @@ __device__ __noinline__ void jacobi4(double* A, double* V, const double* V0, boo
     for (int i = 0; i < 4; ++i) A[i] = a[5 * i];  // eigenvalues into A[0..3]
 }
 
-// Warp 0 of the finishing CTA: Horn's N from S in double, its dominant
-// eigenvector by Horn's closed form (B. K. P. Horn, "Closed-form solution of absolute
-// orientation using unit quaternions", JOSA A 4(4), 1987): the characteristic
-// polynomial det(lambda I - N) from the Faddeev-LeVerrier recursion, its
-// largest root by Newton's method from the Frobenius norm (an upper bound of
-// the spectrum; the polynomial is increasing and convex right of its largest
-// root, so the iterates fall monotonically onto it), and the eigenvector as
-// the largest column of adj(N - lambda I), rank one for a simple eigenvalue.
-// A repeated largest eigenvalue falls back to the Jacobi solver.  Matrix
-// products and cofactors are spread over lanes (GB300's double-precision units are few, so a
-// shorter dependent chain matters more than the operation count), then R, t
-// and pose <- (T R) pose in double (ICP.cpp:199-264, :23-28).
-__device__ __noinline__ void horn_solve_warp(const double* S, IcpState* __restrict__ st,
-                                             const double* mu) {
-    __shared__ double sN[16], sM[16], sA[16], sq[4], sT[16];
+// Warp 0 of the last CTA of an AlignStep: totals of the raw moments, the
+// centroids and the centred cross-covariance S (ICP.cpp:166-197), Horn's
+// symmetric N (:199-213), its dominant eigenvector, R and t (:215-256) and
+// pose <- (T R) pose (:23-28) -- all in double.
+//
+// GB300 executes double precision at a small fraction of the float rate, and
+// this tail runs on one SM while the others wait, so it is written for a
+// short dependent chain: every quantity with independent entries gets a lane
+// of its own, sums are shuffle trees, and divisions / square roots start from
+// a float approximation refined by Newton steps in double.
+//
+// The eigenvector is Horn's closed form (B. K. P. Horn, "Closed-form solution
+// of absolute orientation using unit quaternions", JOSA A 4(4), 1987): the
+// characteristic polynomial det(lambda I - N) from the Faddeev-LeVerrier
+// recursion, its largest root by Newton's method started from an upper bound
+// of the spectrum (Gershgorin, or the Frobenius norm; right of its largest
+// root the polynomial is increasing and convex, so the iterates fall
+// monotonically onto the root), and the largest column of adj(N - lambda I),
+// which is proportional to the eigenvector when the root is simple.  A
+// repeated largest root falls back to the cyclic Jacobi solver.
+__device__ __forceinline__ double warp_sum_d(double x) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    return x;
+}
+__device__ __forceinline__ double recip_d(double x) {  // 1/x to double accuracy
+    double r = (double)(1.0f / (float)x);
+    r = r * (2.0 - x * r);
+    return r * (2.0 - x * r);
+}
+__device__ __forceinline__ double rsqrt_d(double x) {  // 1/sqrt(x) to double accuracy
+    double y = (double)rsqrtf((float)x);
+    y = y * (1.5 - 0.5 * x * y * y);
+    return y * (1.5 - 0.5 * x * y * y);
+}
+
+__device__ __noinline__ void finish_step(IcpState* __restrict__ st, unsigned int n_ctas) {
+    __shared__ double sN[16], sM[16], sA[16], sT[16], sq[4];
     __shared__ int s_ok;
     const int lane = threadIdx.x;
-    if (lane == 0) {
-        const double Sxx = S[0], Sxy = S[1], Sxz = S[2], Syx = S[3], Syy = S[4], Syz = S[5],
-                     Szx = S[6], Szy = S[7], Szz = S[8];
+    // moment totals: float-float per lane over its CTAs, then a double tree
+    double tot[kMoments];
+#pragma unroll
+    for (int c = 0; c < kMoments; ++c) {
+        FF acc{0.0f, 0.0f};
+        for (unsigned int b = lane; b < n_ctas; b += 32)
+            acc = ff_add(acc, FF{st->part[b * 48 + 2 * c], st->part[b * 48 + 2 * c + 1]});
+        tot[c] = warp_sum_d((double)acc.hi + (double)acc.lo);
+    }
+    const double n = tot[0];
+    const double inv_n = recip_d(n);
+    // S_rc = sum p_r q_c - n mu_r nu_c, lane j < 9 holds S_j
+    const int jr = lane < 9 ? lane / 3 : 0, jc = lane < 9 ? lane % 3 : 0;
+    double mu[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) mu[i] = tot[1 + i] * inv_n;
+    double pq = tot[7];
+#pragma unroll
+    for (int i = 1; i < 9; ++i)
+        if (lane == i) pq = tot[7 + i];
+    const double Sj = pq - n * mu[jr] * mu[3 + jc];
+    double S[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) S[i] = __shfl_sync(0xffffffffu, Sj, i);
+    const double Sxx = S[0], Sxy = S[1], Sxz = S[2], Syx = S[3], Syy = S[4], Syz = S[5],
+                 Szx = S[6], Szy = S[7], Szz = S[8];
+    if (lane < 16) {
         const double N[16] = {Sxx + Syy + Szz, Syz - Szy, Szx - Sxz, Sxy - Syx,
                               Syz - Szy, Sxx - Syy - Szz, Sxy + Syx, Szx + Sxz,
                               Szx - Sxz, Sxy + Syx, Syy - Sxx - Szz, Syz + Szy,
                               Sxy - Syx, Szx + Sxz, Syz + Szy, Szz - Sxx - Syy};
-        for (int i = 0; i < 16; ++i) sN[i] = sM[i] = N[i];
+        double v = N[0];
+#pragma unroll
+        for (int i = 1; i < 16; ++i)
+            if (lane == i) v = N[i];
+        sN[lane] = sM[lane] = v;
     }
     __syncwarp();
     const int r = (lane >> 2) & 3, c = lane & 3;
-    double x = lane < 16 ? sN[lane] * sN[lane] : 0.0;
+    // upper bounds of the spectrum: Frobenius norm and Gershgorin rows
+    const double fro2 = warp_sum_d(lane < 16 ? sN[lane] * sN[lane] : 0.0);
+    const double fro = (double)sqrtf((float)fro2) * (1.0 + 1e-6);
+    double gr = lane < 4 ? sN[5 * lane] : -1e300;
+    if (lane < 4)
+        for (int j = 0; j < 4; ++j)
+            if (j != lane) gr += fabs(sN[4 * lane + j]);
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-    const double fro = sqrt(x);
-    auto trace_of = [&](const double* m) {
-        return (m[0] + m[5]) + (m[10] + m[15]);
+    for (int o = 16; o > 0; o >>= 1) gr = fmax(gr, __shfl_xor_sync(0xffffffffu, gr, o));
+    // Faddeev-LeVerrier: p(l) = l^4 + c3 l^3 + c2 l^2 + c1 l + c0
+    auto trace4 = [&](double mine) {  // sum of the diagonal lanes 0, 5, 10, 15
+        double t = (lane < 16 && r == c) ? mine : 0.0;
+        return warp_sum_d(t);
     };
     double cf[4];
-    cf[3] = -trace_of(sM);
+    cf[3] = -trace4(lane < 16 ? sM[lane] : 0.0);
     for (int k = 2; k <= 4; ++k) {
         const double ck = cf[5 - k];
         double t = 0.0;
@@ -496,24 +534,23 @@ __device__ __noinline__ void horn_solve_warp(const double* S, IcpState* __restri
         __syncwarp();
         if (lane < 16) sM[lane] = t;
         __syncwarp();
-        cf[4 - k] = -trace_of(sM) / (double)k;
+        cf[4 - k] = -trace4(t) * (k == 2 ? 0.5 : (k == 3 ? (1.0 / 3.0) : 0.25));
     }
-    double l = fro;
-    for (int it = 0; it < 100; ++it) {
+    double l = fmin(fro, gr);
+    for (int it = 0; it < 60; ++it) {
         const double p = (((l + cf[3]) * l + cf[2]) * l + cf[1]) * l + cf[0];
         const double dp = ((4.0 * l + 3.0 * cf[3]) * l + 2.0 * cf[2]) * l + cf[1];
         if (!(dp > 0.0)) break;
-        const double step = p / dp;
+        const double step = p * recip_d(dp);
         l -= step;
         if (!(fabs(step) > 1e-15 * fro)) break;
     }
     if (lane < 16) sA[lane] = sN[lane] - (r == c ? l : 0.0);
     __syncwarp();
-    // (row, col) cofactor of A
-    auto cof = [&](int row, int col) {
-        int rr[3], cc[3], n = 0, m = 0;
+    auto cof = [&](int row, int col) {  // (row, col) cofactor of A
+        int rr[3], cc[3], nn = 0, m = 0;
         for (int i = 0; i < 4; ++i)
-            if (i != row) rr[n++] = i;
+            if (i != row) rr[nn++] = i;
         for (int j = 0; j < 4; ++j)
             if (j != col) cc[m++] = j;
         const double d =
@@ -522,7 +559,6 @@ __device__ __noinline__ void horn_solve_warp(const double* S, IcpState* __restri
             sA[4 * rr[0] + cc[2]] * (sA[4 * rr[1] + cc[0]] * sA[4 * rr[2] + cc[1]] - sA[4 * rr[1] + cc[1]] * sA[4 * rr[2] + cc[0]]);
         return ((row + col) & 1) ? -d : d;
     };
-    // the largest diagonal cofactor selects the adjugate column
     double dj = lane < 4 ? fabs(cof(lane, lane)) : -1.0;
     int bj = lane;
 #pragma unroll
@@ -535,15 +571,12 @@ __device__ __noinline__ void horn_solve_warp(const double* S, IcpState* __restri
         }
     }
     const bool ok = dj > 1e-24 * fro * fro * fro;
-    double qk = (ok && lane < 4) ? cof(lane, bj) : 0.0;
-    double n2 = qk * qk;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) n2 += __shfl_xor_sync(0xffffffffu, n2, o);
-    if (lane < 4) sq[lane] = qk / sqrt(n2);
+    const double qk = (ok && lane < 4) ? cof(lane, bj) : 0.0;
+    const double inv_norm = rsqrt_d(warp_sum_d(qk * qk));
+    if (lane < 4) sq[lane] = qk * inv_norm;
     if (lane == 0) s_ok = ok;
     __syncwarp();
     if (!s_ok && lane == 0) {
-        // repeated largest eigenvalue: cyclic Jacobi in double
         double A[16], V[16];
         for (int i = 0; i < 16; ++i) A[i] = sN[i];
         jacobi4(A, V, V, false);
@@ -556,29 +589,33 @@ __device__ __noinline__ void horn_solve_warp(const double* S, IcpState* __restri
         for (int i = 0; i < 4; ++i) sq[i] = V[4 * i + imax] / nn;
     }
     __syncwarp();
-    if (lane == 0) {
-        const double q[4] = {sq[0], sq[1], sq[2], sq[3]};
-        // quaternion (x = scalar part) to rotation (ICP.cpp:233-254)
-        const double xy = q[0] * q[1], xz = q[0] * q[2], xw = q[0] * q[3], yy = q[1] * q[1],
-                     yz = q[1] * q[2], yw = q[1] * q[3], zz = q[2] * q[2], zw = q[2] * q[3],
-                     ww = q[3] * q[3];
-        const double R[9] = {1.0 - 2.0 * (zz + ww), 2.0 * (yz - xw),       2.0 * (yw + xz),
-                             2.0 * (yz + xw),       1.0 - 2.0 * (yy + ww), 2.0 * (zw - xy),
-                             2.0 * (yw - xz),       2.0 * (zw + xy),       1.0 - 2.0 * (yy + zz)};
-        const double ms[3] = {mu[0], mu[1], mu[2]};
-        const double md[3] = {mu[3], mu[4], mu[5]};
-        for (int i = 0; i < 16; ++i) sT[i] = (i % 5 == 0) ? 1.0 : 0.0;
-        for (int rr = 0; rr < 3; ++rr) {
-            double t = md[rr];
-            for (int cc = 0; cc < 3; ++cc) {
-                sT[4 * rr + cc] = R[3 * rr + cc];
-                t -= R[3 * rr + cc] * ms[cc];
-            }
-            sT[4 * rr + 3] = t;
-        }
+    // R from the quaternion (x = scalar part, ICP.cpp:233-254), one entry per lane
+    const double qx = sq[0], qy = sq[1], qz = sq[2], qw = sq[3];
+    double Rj = 0.0;
+    switch (lane) {
+        case 0: Rj = 1.0 - 2.0 * (qz * qz + qw * qw); break;
+        case 1: Rj = 2.0 * (qy * qz - qx * qw); break;
+        case 2: Rj = 2.0 * (qy * qw + qx * qz); break;
+        case 3: Rj = 2.0 * (qy * qz + qx * qw); break;
+        case 4: Rj = 1.0 - 2.0 * (qy * qy + qw * qw); break;
+        case 5: Rj = 2.0 * (qz * qw - qx * qy); break;
+        case 6: Rj = 2.0 * (qy * qw - qx * qz); break;
+        case 7: Rj = 2.0 * (qz * qw + qx * qy); break;
+        case 8: Rj = 1.0 - 2.0 * (qy * qy + qz * qz); break;
+        default: break;
+    }
+    double R[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) R[i] = __shfl_sync(0xffffffffu, Rj, i);
+    // step = T * R with t = mu_q - R mu_p (row-major 4x4), one entry per lane
+    if (lane < 16) {
+        double v;
+        if (r == 3) v = (c == 3) ? 1.0 : 0.0;
+        else if (c < 3) v = R[3 * r + c];
+        else v = mu[3 + r] - (R[3 * r] * mu[0] + R[3 * r + 1] * mu[1] + R[3 * r + 2] * mu[2]);
+        sT[lane] = v;
     }
     __syncwarp();
-    // pose <- step * pose, one entry per lane
     double pnew = 0.0;
     if (lane < 16)
         for (int k = 0; k < 4; ++k) pnew += sT[4 * r + k] * st->pose[4 * k + c];
@@ -588,10 +625,16 @@ __device__ __noinline__ void horn_solve_warp(const double* S, IcpState* __restri
         st->pose_f[4 * c + r] = (float)pnew;
     }
     if (lane == 0) {
+        st->n_assoc = (int)(n + 0.5);
+        st->sum_l2 = tot[16];
+        for (int i = 0; i < 3; ++i) {
+            st->mu_s[i] = (float)mu[i];
+            st->mu_d[i] = (float)mu[3 + i];
+        }
         const int it = st->iter;
         if (it < kIcpMaxStats) {
-            st->stats[it].n_assoc = st->n_assoc;
-            st->stats[it].rms = st->n_assoc > 0 ? sqrt(st->sum_l2 / st->n_assoc) : 0.0;
+            st->stats[it].n_assoc = (int)(n + 0.5);
+            st->stats[it].rms = n > 0.0 ? (double)sqrtf((float)(tot[16] * inv_n)) : 0.0;
         }
         st->iter = it + 1;
     }

@@ -192,21 +192,61 @@ __device__ __forceinline__ void update_voxel(uint32_t key, float2& val, const Fr
     c[1] = fadd(fmul((float)key_y(key), g.vlen), g.center_off);
     c[2] = fadd(fmul((float)key_z(key), g.vlen), g.center_off);
     c[3] = 1.0f;  // 1 * 1 + 0
-    float cl[4];
-    mat_vec(w2c, c, cl);
-    const float w = cl[3];
+    // rows 0, 1, 3 of worldToClip * c (mat_vec's order); row 2 below
+    auto row = [&](int i) {
+        return fadd(fadd(fmul(w2c[i], c[0]), fmul(w2c[4 + i], c[1])),
+                    fadd(fmul(w2c[8 + i], c[2]), fmul(w2c[12 + i], c[3])));
+    };
+    const float x = row(0), y = row(1), w = row(3);
     // lane w: (w/w) * 0 + 0 lies in [-FLT_MAX, FLT_MAX) iff w/w is finite,
     // i.e. iff w is finite and non-zero (w/w is then exactly 1).
     if (!(isfinite(w) && w != 0.0f)) return;
-    // lane z: (z/w) * 0 + 0 lies in [-1, 1) iff z/w is finite.  With w finite
-    // and non-zero that needs z finite and no overflow of the quotient; the
-    // bounds below rule overflow out without dividing, else divide exactly.
-    const float z = cl[2];
-    if (!isfinite(z)) return;
-    if (!(fabsf(z) <= 1e18f && fabsf(w) >= 1e-18f) && !isfinite(fdiv(z, w))) return;
-    const float u = fadd(fmul(fdiv(cl[0], w), fc.half_w), fc.half_w);
-    const float v = fadd(fmul(fdiv(cl[1], w), fc.half_h), fc.half_h);
-    if (!(u >= 0.0f && u < (float)fc.width && v >= 0.0f && v < (float)fc.height)) return;
+    // lane z: (z/w) * 0 + 0 lies in [-1, 1) iff z/w is finite.  When the
+    // host has bounded |z| by 1e18 over the whole volume (fc.z_bounded), any
+    // |w| >= 1e-18 keeps the quotient finite and z need not be formed.
+    if (!(fc.z_bounded && fabsf(w) >= 1e-18f)) {
+        const float z = row(2);
+        if (!isfinite(z)) return;
+        if (!(fabsf(z) <= 1e18f && fabsf(w) >= 1e-18f) && !isfinite(fdiv(z, w))) return;
+    }
+    // u = (x/w) * W/2 + W/2 and v likewise, IEEE-exact.  Only floor(u),
+    // floor(v) and the range tests use them, so first try a fast reciprocal
+    // (__fdividef: at most 2 ulp).  For frames up to 4096 pixels on a side
+    // the approximate u' differs from u by less than 2.5e-3 wherever
+    // u' lies in [-0.5, W + 0.5] (relative error of x * rcp(w) against the
+    // rounded x/w at most 3.6e-7 + 6e-8, times |u - W/2| <= 4097, plus the
+    // roundings of the two remaining operations), so when u' is at least
+    // 1/256 away from every integer, floor(u') = floor(u) and every range test
+    // agrees; otherwise the exact division decides.
+    if (!fc.fast_uv) {
+        const float u = fadd(fmul(fdiv(x, w), fc.half_w), fc.half_w);
+        const float v = fadd(fmul(fdiv(y, w), fc.half_h), fc.half_h);
+        if (!(u >= 0.0f && u < (float)fc.width && v >= 0.0f && v < (float)fc.height)) return;
+        const size_t px = (uint32_t)u;
+        const size_t py = (size_t)fc.height - (uint32_t)v - 1;
+        const float d = load_depth(depth, py * (size_t)fc.width + px, kU16);
+        const float sd = fsub(d, w);
+        if (d > 0.0f && sd >= -g.trunc) {
+            val.x = fadd(val.x, (g.trunc < sd) ? g.trunc : sd);
+            val.y = fadd(val.y, 1.0f);
+        }
+        return;
+    }
+    const float rw = __fdividef(1.0f, w);
+    const float ua = fadd(fmul(fmul(x, rw), fc.half_w), fc.half_w);
+    const float va = fadd(fmul(fmul(y, rw), fc.half_h), fc.half_h);
+    const float Wf = (float)fc.width, Hf = (float)fc.height;
+    if (!(ua >= -0.5f && ua <= Wf + 0.5f && va >= -0.5f && va <= Hf + 0.5f)) return;
+    constexpr float kE = 1.0f / 256.0f;
+    float u, v;
+    {
+        const float fu = floorf(ua), fv = floorf(va);
+        const bool su = ua - fu >= kE && fu + 1.0f - ua >= kE;
+        const bool sv = va - fv >= kE && fv + 1.0f - va >= kE;
+        u = su ? fu + 0.5f : fadd(fmul(fdiv(x, w), fc.half_w), fc.half_w);
+        v = sv ? fv + 0.5f : fadd(fmul(fdiv(y, w), fc.half_h), fc.half_h);
+    }
+    if (!(u >= 0.0f && u < Wf && v >= 0.0f && v < Hf)) return;
     const size_t px = (uint32_t)u;
     const size_t py = (size_t)fc.height - (uint32_t)v - 1;
     const float d = load_depth(depth, py * (size_t)fc.width + px, kU16);
@@ -522,7 +562,8 @@ cudaError_t integrate_enqueue(DeviceCtl* ctl, const Geom& g, VolumeBuffers& vb, 
                               const Mat4& world_to_eye, const LaunchShape& ls, cudaStream_t st,
                               cudaEvent_t* events) {
     // frame constants on the host, in the reference's float order
-    const FrameConst fc = make_frame_const(cam, world_to_eye, g.res);
+    FrameConst fc = make_frame_const(cam, world_to_eye, g.res);
+    fc.z_bounded = clip_z_bounded(fc.world_to_clip, g.side);
     if (events) cudaEventRecord(events[0], st);
     k_frame_setup<<<1, 32, 0, st>>>(ctl);
     const unsigned int new_cap = (unsigned int)vb.new_cap;
