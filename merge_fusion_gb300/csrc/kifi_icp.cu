@@ -91,20 +91,26 @@ __device__ __forceinline__ bool last_cta(unsigned int* counter) {
     return last;
 }
 
-// Sums the per-CTA float-float partials of NV components with the whole
-// (last) CTA: thread t adds CTAs t, t+256, ... in float-float, warps combine
-// with shuffles, and the 8 warp totals are added in double -- a fixed order,
-// so the result does not depend on scheduling.
+// Totals of the per-CTA float-float partials of NV components, computed by
+// the whole (last) CTA: thread t loads CTA t's partials (one round of
+// independent loads), warps combine with float-float shuffles, and lane c of
+// warp 0 adds the warp totals of component c in float-float and forms the
+// double total.  Fixed order: independent of scheduling.  Double precision
+// enters only at the end -- on GB300 a dependent double add costs about 64
+// cycles against under 6 for a float one.
 template <int NV>
-__device__ __forceinline__ void finish_partials(const IcpState* st, double* out) {
+__device__ __forceinline__ void moments_total(const IcpState* st, double* out) {
     __shared__ FF red[32][NV];
     FF a[NV];
 #pragma unroll
     for (int c = 0; c < NV; ++c) a[c] = FF{0.0f, 0.0f};
-    for (unsigned int b = threadIdx.x; b < gridDim.x; b += blockDim.x)
+    for (unsigned int b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+        float v[2 * NV];
 #pragma unroll
-        for (int c = 0; c < NV; ++c)
-            a[c] = ff_add(a[c], FF{st->part[b * 48 + 2 * c], st->part[b * 48 + 2 * c + 1]});
+        for (int c = 0; c < 2 * NV; ++c) v[c] = st->part[b * 48 + c];
+#pragma unroll
+        for (int c = 0; c < NV; ++c) a[c] = ff_add(a[c], FF{v[2 * c], v[2 * c + 1]});
+    }
 #pragma unroll
     for (int c = 0; c < NV; ++c) a[c] = warp_sum_ff(a[c]);
     if ((threadIdx.x & 31) == 0)
@@ -112,10 +118,9 @@ __device__ __forceinline__ void finish_partials(const IcpState* st, double* out)
         for (int c = 0; c < NV; ++c) red[threadIdx.x >> 5][c] = a[c];
     __syncthreads();
     if (threadIdx.x < NV) {
-        double t = 0.0;
-        for (int w = 0; w < (int)(blockDim.x / 32); ++w)
-            t += (double)red[w][threadIdx.x].hi + (double)red[w][threadIdx.x].lo;
-        out[threadIdx.x] = t;
+        FF t = red[0][threadIdx.x];
+        for (int w = 1; w < (int)(blockDim.x / 32); ++w) t = ff_add(t, red[w][threadIdx.x]);
+        out[threadIdx.x] = (double)t.hi + (double)t.lo;
     }
     __syncthreads();
 }
@@ -172,7 +177,7 @@ __device__ __forceinline__ float scan_staged(const float4* __restrict__ sp, int 
     return b0;
 }
 
-__device__ __noinline__ void finish_step(IcpState* __restrict__ st, unsigned int n_ctas);
+__device__ __noinline__ void finish_step(IcpState* __restrict__ st, const double* tot);
 
 // One ICP::AlignStep (ICP.cpp:35-265) as one kernel.
 //
@@ -365,7 +370,9 @@ __global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step(IcpArgs a, IcpSta
         __threadfence();  // publish before the CTA signals completion
     }
     if (!last_cta(&st->done)) return;
-    if (threadIdx.x < 32) finish_step(st, gridDim.x);
+    __shared__ double tot[kMoments];
+    moments_total<kMoments>(st, tot);
+    if (threadIdx.x < 32) finish_step(st, tot);
 }
 
 // ------------------------------------------------------ FP64 Horn solve
@@ -467,19 +474,10 @@ __device__ __forceinline__ double rsqrt_d(double x) {  // 1/sqrt(x) to double ac
     return y * (1.5 - 0.5 * x * y * y);
 }
 
-__device__ __noinline__ void finish_step(IcpState* __restrict__ st, unsigned int n_ctas) {
+__device__ __noinline__ void finish_step(IcpState* __restrict__ st, const double* tot) {
     __shared__ double sN[16], sM[16], sA[16], sT[16], sq[4];
     __shared__ int s_ok;
     const int lane = threadIdx.x;
-    // moment totals: float-float per lane over its CTAs, then a double tree
-    double tot[kMoments];
-#pragma unroll
-    for (int c = 0; c < kMoments; ++c) {
-        FF acc{0.0f, 0.0f};
-        for (unsigned int b = lane; b < n_ctas; b += 32)
-            acc = ff_add(acc, FF{st->part[b * 48 + 2 * c], st->part[b * 48 + 2 * c + 1]});
-        tot[c] = warp_sum_d((double)acc.hi + (double)acc.lo);
-    }
     const double n = tot[0];
     const double inv_n = recip_d(n);
     // S_rc = sum p_r q_c - n mu_r nu_c, lane j < 9 holds S_j
@@ -487,10 +485,7 @@ __device__ __noinline__ void finish_step(IcpState* __restrict__ st, unsigned int
     double mu[6];
 #pragma unroll
     for (int i = 0; i < 6; ++i) mu[i] = tot[1 + i] * inv_n;
-    double pq = tot[7];
-#pragma unroll
-    for (int i = 1; i < 9; ++i)
-        if (lane == i) pq = tot[7 + i];
+    const double pq = tot[7 + (lane < 9 ? lane : 0)];
     const double Sj = pq - n * mu[jr] * mu[3 + jc];
     double S[9];
 #pragma unroll
