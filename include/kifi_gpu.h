@@ -239,6 +239,13 @@ KIFI_API kifi_status kifi_icp_result(kifi_icp* icp, float out_eye_to_world[16],
                                      double out_eye_to_world_d[16], int* n_assoc, double* rms,
                                      int capacity, int* iterations);
 
+/* Per-iteration device timings of the last alignment (the GPU counterpart
+ * of the reference's stop_watch telemetry): microseconds from the first CTA's
+ * start to the last CTA's end of the association, and from there to the
+ * updated pose (the reduction and Horn solve).  Pointers may be NULL. */
+KIFI_API kifi_status kifi_icp_iteration_times(kifi_icp* icp, float* body_us, float* tail_us,
+                                              int capacity, int* iterations);
+
 /* kifi::Renderer::Bin (KinectFission/kifi/Renderer.h:23-29,
  * Renderer.cpp:39-80): z-buffered splat of n world points (3 floats each,
  * host memory) through world_to_clip into a width x height float3 buffer;

@@ -245,6 +245,29 @@ kifi_status kifi_icp_result(kifi_icp* c, float out_eye_to_world[16], double out_
     return KIFI_OK;
 }
 
+kifi_status kifi_icp_iteration_times(kifi_icp* c, float* body_us, float* tail_us, int capacity,
+                                     int* iterations) {
+    if (!c) return fail(KIFI_ERR_INVALID_ARGUMENT, "null context");
+    KIFI_CUDA(cudaSetDevice(c->device));
+    const size_t head = offsetof(IcpState, part);
+    IcpState* h = (IcpState*)std::malloc(head);
+    if (!h) return fail(KIFI_ERR_OUT_OF_MEMORY, "host allocation");
+    cudaError_t e = cudaMemcpyAsync(h, c->st, head, cudaMemcpyDeviceToHost, c->stream);
+    if (!e) e = cudaStreamSynchronize(c->stream);
+    if (e) {
+        std::free(h);
+        return cuda_fail(e, "ICP timings");
+    }
+    const int it = h->iter < kIcpMaxStats ? h->iter : kIcpMaxStats;
+    if (iterations) *iterations = h->iter;
+    for (int i = 0; i < it && i < capacity; ++i) {
+        if (body_us) body_us[i] = h->stats[i].body_us;
+        if (tail_us) tail_us[i] = h->stats[i].tail_us;
+    }
+    std::free(h);
+    return KIFI_OK;
+}
+
 kifi_status kifi_bin(const float* points, size_t n, const float world_to_clip[16], float* out,
                      int width, int height) {
     if ((n && !points) || !world_to_clip || !out || width <= 0 || height <= 0)

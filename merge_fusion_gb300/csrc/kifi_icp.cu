@@ -206,6 +206,12 @@ __device__ __noinline__ void finish_step(IcpState* __restrict__ st, const double
 constexpr int kAssocThreads = 512;
 constexpr int kMoments = 17;  // n, p xyz, q xyz, p q^T (9), len^2
 
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 __device__ __forceinline__ FF two_prod(float a, float b) {
     const float p = fmul(a, b);
     return FF{p, __fmaf_rn(a, b, -p)};  // exact remainder of the product
@@ -225,6 +231,7 @@ __global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step(IcpArgs a, IcpSta
     const float half_w = fmul((float)a.synth_w, 0.5f), half_h = fmul((float)a.synth_h, 0.5f);
     const size_t n_synth = (size_t)a.synth_w * a.synth_h;
     if (half == 0 && lane < kMoments) s_acc[wcol][lane] = FF{0.0f, 0.0f};
+    if (threadIdx.x == 0) atomicMin(&st->t_start, global_ns());
     for (int tile = blockIdx.x; tile < tiles_x * tiles_y; tile += gridDim.x) {
         const int tx = tile % tiles_x, ty = tile / tiles_x;
         const int col = tx * kTileCols + wcol, y = ty * kTileRows + lane;
@@ -369,6 +376,7 @@ __global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step(IcpArgs a, IcpSta
         st->part[blockIdx.x * 48 + 2 * threadIdx.x + 1] = t.lo;
         __threadfence();  // publish before the CTA signals completion
     }
+    if (threadIdx.x == 0) atomicMax(&st->t_body, global_ns());
     if (!last_cta(&st->done)) return;
     __shared__ double tot[kMoments];
     moments_total<kMoments>(st, tot);
@@ -630,7 +638,12 @@ __device__ __noinline__ void finish_step(IcpState* __restrict__ st, const double
         if (it < kIcpMaxStats) {
             st->stats[it].n_assoc = (int)(n + 0.5);
             st->stats[it].rms = n > 0.0 ? (double)sqrtf((float)(tot[16] * inv_n)) : 0.0;
+            const unsigned long long t_end = global_ns();
+            st->stats[it].body_us = (float)(st->t_body - st->t_start) * 1e-3f;
+            st->stats[it].tail_us = (float)(t_end - st->t_body) * 1e-3f;
         }
+        st->t_start = ~0ull;
+        st->t_body = 0ull;
         st->iter = it + 1;
     }
 }
@@ -643,6 +656,8 @@ __global__ void k_icp_begin(IcpState* st, Mat4 guess) {
     st->iter = 0;
     st->have_V = 0;
     st->done = 0u;
+    st->t_start = ~0ull;
+    st->t_body = 0ull;
 }
 
 // World points of a depth frame: the back-projection of

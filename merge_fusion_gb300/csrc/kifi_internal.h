@@ -116,7 +116,9 @@ struct IcpArgs {
 struct IcpIterStats {
     int n_assoc;
     int pad;
-    double rms;  // sqrt(mean of the associated squared distances)
+    double rms;       // sqrt(mean of the associated squared distances)
+    float body_us;    // first CTA start to last CTA end of the association
+    float tail_us;    // last CTA end to the updated pose
 };
 
 struct IcpState {
@@ -129,6 +131,7 @@ struct IcpState {
     int n_assoc;
     int iter;
     double sum_l2;
+    unsigned long long t_start, t_body;  // globaltimer stamps of the running step
     IcpIterStats stats[kIcpMaxStats];
     float part[kIcpMaxCtas * 48];   // per-CTA float-float partial sums (24 components)
 };
