@@ -231,8 +231,9 @@ KIFI_API kifi_status kifi_icp_align_device(kifi_icp* icp, const void* depth_dev,
                                            const kifi_camera* cam,
                                            const float eye_to_world_guess[16], int iterations);
 
-/* Waits and reads the last alignment: the pose (float, and optionally the
- * double it was rounded from), per-iteration association counts and RMS
+/* Waits and reads the last alignment: the pose (float, as the reference
+ * composes it, and optionally the same widened to double), per-iteration
+ * association counts and RMS
  * residuals (up to `capacity` entries; the reference prints the count,
  * ICP.cpp:133) and the iteration count.  Pointers may be NULL. */
 KIFI_API kifi_status kifi_icp_result(kifi_icp* icp, float out_eye_to_world[16],

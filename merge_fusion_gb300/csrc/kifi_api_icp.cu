@@ -233,8 +233,7 @@ kifi_status kifi_icp_result(kifi_icp* c, float out_eye_to_world[16], double out_
     }
     if (out_eye_to_world) std::memcpy(out_eye_to_world, h->pose_f, 64);
     if (out_eye_to_world_d)
-        for (int r = 0; r < 4; ++r)
-            for (int col = 0; col < 4; ++col) out_eye_to_world_d[4 * col + r] = h->pose[4 * r + col];
+        for (int i = 0; i < 16; ++i) out_eye_to_world_d[i] = (double)h->pose_f[i];
     const int it = h->iter < kIcpMaxStats ? h->iter : kIcpMaxStats;
     if (iterations) *iterations = h->iter;
     for (int i = 0; i < it && i < capacity; ++i) {

@@ -63,6 +63,27 @@ __device__ __forceinline__ FF ff_add(FF a, FF b) {
     const float hi = fadd(s, e);
     return FF{hi, fsub(e, fsub(hi, s))};
 }
+__device__ __forceinline__ FF ff_norm(float hi, float lo) {  // |lo| may exceed ulp(hi)/2
+    const float s = fadd(hi, lo);
+    return FF{s, fsub(lo, fsub(s, hi))};
+}
+__device__ __forceinline__ FF operator+(FF a, FF b) { return ff_add(a, b); }
+__device__ __forceinline__ FF operator-(FF a, FF b) { return ff_add(a, FF{-b.hi, -b.lo}); }
+__device__ __forceinline__ FF operator-(FF a) { return FF{-a.hi, -a.lo}; }
+__device__ __forceinline__ FF operator*(FF a, FF b) {
+    const float p = fmul(a.hi, b.hi);
+    const float e = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, __fmaf_rn(a.hi, b.hi, -p)));
+    return ff_norm(p, e);
+}
+__device__ __forceinline__ FF operator*(FF a, float b) {
+    const float p = fmul(a.hi, b);
+    return ff_norm(p, __fmaf_rn(a.lo, b, __fmaf_rn(a.hi, b, -p)));
+}
+__device__ __forceinline__ FF ff_div(FF a, FF b) {  // a / b, b != 0
+    const float q1 = fdiv(a.hi, b.hi);
+    const FF r = a - b * q1;
+    return ff_norm(q1, fdiv(r.hi, b.hi));
+}
 __device__ __forceinline__ FF warp_sum_ff(FF v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -76,51 +97,62 @@ __device__ __forceinline__ float load_depth(const void* depth, size_t i, bool u1
     return __ldg((const float*)depth + i);
 }
 
-// last CTA to arrive returns true (after a fence); resets the counter
+// Last CTA to arrive returns true; resets the counter.  Thread 0's fences
+// order the whole CTA's earlier stores (the barrier makes them visible to it)
+// before the count, and the count before the last CTA's reads.
 __device__ __forceinline__ bool last_cta(unsigned int* counter) {
     __shared__ bool last;
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
-        unsigned int prev = atomicAdd(counter, 1u);
+        const unsigned int prev = atomicAdd(counter, 1u);
         last = (prev == gridDim.x - 1);
-        if (last) *counter = 0u;
+        if (last) {
+            *counter = 0u;
+            __threadfence();
+        }
     }
     __syncthreads();
-    if (last) __threadfence();
     return last;
 }
 
-// Totals of the per-CTA float-float partials of NV components, computed by
-// the whole (last) CTA: thread t loads CTA t's partials (one round of
-// independent loads), warps combine with float-float shuffles, and lane c of
-// warp 0 adds the warp totals of component c in float-float and forms the
-// double total.  Fixed order: independent of scheduling.  Double precision
-// enters only at the end -- on GB300 a dependent double add costs about 64
-// cycles against under 6 for a float one.
-template <int NV>
-__device__ __forceinline__ void moments_total(const IcpState* st, double* out) {
-    __shared__ FF red[32][NV];
-    FF a[NV];
+// Totals of the per-CTA float-float partials, by the whole (last) CTA.  The
+// partials are stored component-major (hi row, then lo row, each
+// kIcpMaxCtas long), so warp w reduces components w and w + 16 with
+// coalesced loads: lane l adds CTAs l, l + 32, ... in float-float -- all of a
+// lane's loads (up to 320 CTAs) issued in one round -- then a shuffle tree.
+// Fixed order: independent of scheduling.  The loads bypass L1 (the partials
+// were written by other SMs during this launch).
+constexpr int kTotalsPerLane = 10;
+__device__ __forceinline__ FF lane_partials(const float* ph, int b0, int G) {
+    float h[kTotalsPerLane], l[kTotalsPerLane];
 #pragma unroll
-    for (int c = 0; c < NV; ++c) a[c] = FF{0.0f, 0.0f};
-    for (unsigned int b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
-        float v[2 * NV];
-#pragma unroll
-        for (int c = 0; c < 2 * NV; ++c) v[c] = st->part[b * 48 + c];
-#pragma unroll
-        for (int c = 0; c < NV; ++c) a[c] = ff_add(a[c], FF{v[2 * c], v[2 * c + 1]});
+    for (int k = 0; k < kTotalsPerLane; ++k) {
+        const int b = b0 + 32 * k;
+        h[k] = b < G ? __ldcg(ph + b) : 0.0f;
+        l[k] = b < G ? __ldcg(ph + kIcpMaxCtas + b) : 0.0f;
     }
+    FF acc{h[0], l[0]};
 #pragma unroll
-    for (int c = 0; c < NV; ++c) a[c] = warp_sum_ff(a[c]);
-    if ((threadIdx.x & 31) == 0)
-#pragma unroll
-        for (int c = 0; c < NV; ++c) red[threadIdx.x >> 5][c] = a[c];
-    __syncthreads();
-    if (threadIdx.x < NV) {
-        FF t = red[0][threadIdx.x];
-        for (int w = 1; w < (int)(blockDim.x / 32); ++w) t = ff_add(t, red[w][threadIdx.x]);
-        out[threadIdx.x] = (double)t.hi + (double)t.lo;
+    for (int k = 1; k < kTotalsPerLane; ++k) acc = ff_add(acc, FF{h[k], l[k]});
+    return acc;
+}
+template <int NV>
+__device__ __forceinline__ void moments_total(const IcpState* st, FF* out) {
+    const int lane = threadIdx.x & 31, c0 = threadIdx.x >> 5, c1 = c0 + (blockDim.x >> 5);
+    const int G = gridDim.x;
+    if (c0 < NV) {
+        FF a0{0.0f, 0.0f}, a1{0.0f, 0.0f};
+        for (int b0 = lane; b0 < G; b0 += 32 * kTotalsPerLane) {
+            a0 = ff_add(a0, lane_partials(st->part + (size_t)(2 * c0) * kIcpMaxCtas, b0, G));
+            if (c1 < NV) a1 = ff_add(a1, lane_partials(st->part + (size_t)(2 * c1) * kIcpMaxCtas, b0, G));
+        }
+        a0 = warp_sum_ff(a0);
+        if (lane == 0) out[c0] = a0;
+        if (c1 < NV) {
+            a1 = warp_sum_ff(a1);
+            if (lane == 0) out[c1] = a1;
+        }
     }
     __syncthreads();
 }
@@ -177,7 +209,7 @@ __device__ __forceinline__ float scan_staged(const float4* __restrict__ sp, int 
     return b0;
 }
 
-__device__ __noinline__ void finish_step(IcpState* __restrict__ st, const double* tot);
+__device__ __noinline__ void finish_step(IcpState* __restrict__ st, const FF* __restrict__ tot);
 
 // One ICP::AlignStep (ICP.cpp:35-265) as one kernel.
 //
@@ -372,43 +404,25 @@ __global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step(IcpArgs a, IcpSta
     if (threadIdx.x < kMoments) {
         FF t = s_acc[0][threadIdx.x];
         for (int w = 1; w < kTileCols; ++w) t = ff_add(t, s_acc[w][threadIdx.x]);
-        st->part[blockIdx.x * 48 + 2 * threadIdx.x] = t.hi;
-        st->part[blockIdx.x * 48 + 2 * threadIdx.x + 1] = t.lo;
-        __threadfence();  // publish before the CTA signals completion
+        st->part[(size_t)(2 * threadIdx.x) * kIcpMaxCtas + blockIdx.x] = t.hi;
+        st->part[(size_t)(2 * threadIdx.x + 1) * kIcpMaxCtas + blockIdx.x] = t.lo;
     }
     if (threadIdx.x == 0) atomicMax(&st->t_body, global_ns());
     if (!last_cta(&st->done)) return;
-    __shared__ double tot[kMoments];
+    __shared__ FF tot[kMoments];
     moments_total<kMoments>(st, tot);
-    if (threadIdx.x < 32) finish_step(st, tot);
+    if (threadIdx.x == 0) finish_step(st, tot);
 }
 
-// ------------------------------------------------------ FP64 Horn solve
+// ------------------------------------------------------------- Horn solve
 // Cyclic Jacobi on a symmetric 4x4 (row-major) in double; V accumulates the
-// rotations (columns are eigenvectors).  Starting from V0 (the previous
-// solve's eigenvectors) the matrix is first rotated into that basis.
-__device__ __noinline__ void jacobi4(double* A, double* V, const double* V0, bool warm) {
+// rotations (columns are eigenvectors), the eigenvalues end in A[0..3].  The
+// fallback for spectra whose largest eigenvalue is (nearly) repeated.
+__device__ __noinline__ void jacobi4(double* A, double* V) {
     double a[16];
-    if (warm) {
-        double t[16];
-        for (int i = 0; i < 4; ++i)
-            for (int j = 0; j < 4; ++j) {
-                double s = 0.0;
-                for (int k = 0; k < 4; ++k) s += A[4 * i + k] * V0[4 * k + j];
-                t[4 * i + j] = s;
-            }
-        for (int i = 0; i < 4; ++i)
-            for (int j = 0; j < 4; ++j) {
-                double s = 0.0;
-                for (int k = 0; k < 4; ++k) s += V0[4 * k + i] * t[4 * k + j];
-                a[4 * i + j] = s;
-            }
-        for (int i = 0; i < 16; ++i) V[i] = V0[i];
-    } else {
-        for (int i = 0; i < 16; ++i) {
-            a[i] = A[i];
-            V[i] = (i % 5 == 0) ? 1.0 : 0.0;
-        }
+    for (int i = 0; i < 16; ++i) {
+        a[i] = A[i];
+        V[i] = (i % 5 == 0) ? 1.0 : 0.0;
     }
     double scale = 0.0;
     for (int i = 0; i < 16; ++i) scale += a[i] * a[i];
@@ -443,218 +457,269 @@ __device__ __noinline__ void jacobi4(double* A, double* V, const double* V0, boo
                 }
             }
     }
-    for (int i = 0; i < 4; ++i) A[i] = a[5 * i];  // eigenvalues into A[0..3]
+    for (int i = 0; i < 4; ++i) A[i] = a[5 * i];
 }
 
-// Warp 0 of the last CTA of an AlignStep: totals of the raw moments, the
-// centroids and the centred cross-covariance S (ICP.cpp:166-197), Horn's
-// symmetric N (:199-213), its dominant eigenvector, R and t (:215-256) and
-// pose <- (T R) pose (:23-28) -- all in double.
+// Horn's closed form (B. K. P. Horn, "Closed-form solution of absolute
+// orientation using unit quaternions", JOSA A 4(4), 1987), written for one
+// thread and without double precision: GB300 issues a double instruction
+// (conversions included) at about one per 64 cycles per SM sub-partition,
+// even for a single thread, and this tail runs on one SM while the others
+// wait.  Precision comes from float-float (FF) arithmetic where it matters.
 //
-// GB300 executes double precision at a small fraction of the float rate, and
-// this tail runs on one SM while the others wait, so it is written for a
-// short dependent chain: every quantity with independent entries gets a lane
-// of its own, sums are shuffle trees, and divisions / square roots start from
-// a float approximation refined by Newton steps in double.
+//  1. FF: centroids, the centred cross-covariance S = sum p q^T - (sum p)
+//     mu_q^T (the raw moments cancel heavily) and Horn's symmetric N, scaled
+//     by a power of two to unit size (exact).
+//  2. float: the characteristic polynomial of N by the Faddeev-LeVerrier
+//     recursion, its largest root by Newton's method from an upper bound of
+//     the spectrum (Gershgorin or the Frobenius norm; right of the largest
+//     root the polynomial is increasing and convex, so the iterates fall
+//     monotonically onto it), and the largest diagonal entry j of
+//     adj(N - lambda I), whose column j is then proportional to the
+//     eigenvector.
+//  3. FF: one step of Rayleigh-quotient inverse iteration -- rho = q'Nq / q'q,
+//     q <- column j of adj(N - rho I) -- which converges cubically, so the
+//     float-accurate start lands well below float rounding (two steps when
+//     the eigen-gaps are small).
+//  4. A spectrum whose gap product (the adjugate diagonal above) is tiny --
+//     a nearly repeated largest eigenvalue -- goes to the double Jacobi
+//     solver instead.
 //
-// The eigenvector is Horn's closed form (B. K. P. Horn, "Closed-form solution
-// of absolute orientation using unit quaternions", JOSA A 4(4), 1987): the
-// characteristic polynomial det(lambda I - N) from the Faddeev-LeVerrier
-// recursion, its largest root by Newton's method started from an upper bound
-// of the spectrum (Gershgorin, or the Frobenius norm; right of its largest
-// root the polynomial is increasing and convex, so the iterates fall
-// monotonically onto the root), and the largest column of adj(N - lambda I),
-// which is proportional to the eigenvector when the root is simple.  A
-// repeated largest root falls back to the cyclic Jacobi solver.
-__device__ __forceinline__ double warp_sum_d(double x) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-    return x;
+// R, t and the pose update are then float, in the reference's expression
+// order (ICP.cpp:233-263 and :20-28).
+//
+// Symmetric 4x4 matrices are held as their upper triangle, row by row.
+__host__ __device__ constexpr int sym(int i, int j) {
+    return i <= j ? (i * (7 - i)) / 2 + j : (j * (7 - j)) / 2 + i;
 }
-__device__ __forceinline__ double recip_d(double x) {  // 1/x to double accuracy
-    double r = (double)(1.0f / (float)x);
-    r = r * (2.0 - x * r);
-    return r * (2.0 - x * r);
+template <typename T>
+__device__ __forceinline__ T shifted(const T* n, T s, int i, int j) {
+    return i == j ? n[sym(i, i)] - s : n[sym(i, j)];
 }
-__device__ __forceinline__ double rsqrt_d(double x) {  // 1/sqrt(x) to double accuracy
-    double y = (double)rsqrtf((float)x);
-    y = y * (1.5 - 0.5 * x * y * y);
-    return y * (1.5 - 0.5 * x * y * y);
+// determinant of rows r0..r2 and columns k0..k2 of N - s I
+template <typename T>
+__device__ __forceinline__ T minor3(const T* n, T s, int r0, int r1, int r2, int k0, int k1, int k2) {
+    const T a00 = shifted(n, s, r0, k0), a01 = shifted(n, s, r0, k1), a02 = shifted(n, s, r0, k2);
+    const T a10 = shifted(n, s, r1, k0), a11 = shifted(n, s, r1, k1), a12 = shifted(n, s, r1, k2);
+    const T a20 = shifted(n, s, r2, k0), a21 = shifted(n, s, r2, k1), a22 = shifted(n, s, r2, k2);
+    return a00 * (a11 * a22 - a12 * a21) - a01 * (a10 * a22 - a12 * a20) + a02 * (a10 * a21 - a11 * a20);
 }
-
-__device__ __noinline__ void finish_step(IcpState* __restrict__ st, const double* tot) {
-    __shared__ double sN[16], sM[16], sA[16], sT[16], sq[4];
-    __shared__ int s_ok;
-    const int lane = threadIdx.x;
-    const double n = tot[0];
-    const double inv_n = recip_d(n);
-    // S_rc = sum p_r q_c - n mu_r nu_c, lane j < 9 holds S_j
-    const int jr = lane < 9 ? lane / 3 : 0, jc = lane < 9 ? lane % 3 : 0;
-    double mu[6];
-#pragma unroll
-    for (int i = 0; i < 6; ++i) mu[i] = tot[1 + i] * inv_n;
-    const double pq = tot[7 + (lane < 9 ? lane : 0)];
-    const double Sj = pq - n * mu[jr] * mu[3 + jc];
-    double S[9];
-#pragma unroll
-    for (int i = 0; i < 9; ++i) S[i] = __shfl_sync(0xffffffffu, Sj, i);
-    const double Sxx = S[0], Sxy = S[1], Sxz = S[2], Syx = S[3], Syy = S[4], Syz = S[5],
-                 Szx = S[6], Szy = S[7], Szz = S[8];
-    if (lane < 16) {
-        const double N[16] = {Sxx + Syy + Szz, Syz - Szy, Szx - Sxz, Sxy - Syx,
-                              Syz - Szy, Sxx - Syy - Szz, Sxy + Syx, Szx + Sxz,
-                              Szx - Sxz, Sxy + Syx, Syy - Sxx - Szz, Syz + Szy,
-                              Sxy - Syx, Szx + Sxz, Syz + Szy, Szz - Sxx - Syy};
-        double v = N[0];
-#pragma unroll
-        for (int i = 1; i < 16; ++i)
-            if (lane == i) v = N[i];
-        sN[lane] = sM[lane] = v;
+// column j of adj(N - s I) (the matrix is symmetric, so cofactor (i, j))
+template <typename T>
+__device__ __forceinline__ void adj_column(const T* n, T s, int j, T* q) {
+    switch (j) {
+        case 0:
+            q[0] = minor3(n, s, 1, 2, 3, 1, 2, 3);
+            q[1] = -minor3(n, s, 1, 2, 3, 0, 2, 3);
+            q[2] = minor3(n, s, 1, 2, 3, 0, 1, 3);
+            q[3] = -minor3(n, s, 1, 2, 3, 0, 1, 2);
+            break;
+        case 1:
+            q[0] = -minor3(n, s, 0, 2, 3, 1, 2, 3);
+            q[1] = minor3(n, s, 0, 2, 3, 0, 2, 3);
+            q[2] = -minor3(n, s, 0, 2, 3, 0, 1, 3);
+            q[3] = minor3(n, s, 0, 2, 3, 0, 1, 2);
+            break;
+        case 2:
+            q[0] = minor3(n, s, 0, 1, 3, 1, 2, 3);
+            q[1] = -minor3(n, s, 0, 1, 3, 0, 2, 3);
+            q[2] = minor3(n, s, 0, 1, 3, 0, 1, 3);
+            q[3] = -minor3(n, s, 0, 1, 3, 0, 1, 2);
+            break;
+        default:
+            q[0] = -minor3(n, s, 0, 1, 2, 1, 2, 3);
+            q[1] = minor3(n, s, 0, 1, 2, 0, 2, 3);
+            q[2] = -minor3(n, s, 0, 1, 2, 0, 1, 3);
+            q[3] = minor3(n, s, 0, 1, 2, 0, 1, 2);
+            break;
     }
-    __syncwarp();
-    const int r = (lane >> 2) & 3, c = lane & 3;
-    // upper bounds of the spectrum: Frobenius norm and Gershgorin rows
-    const double fro2 = warp_sum_d(lane < 16 ? sN[lane] * sN[lane] : 0.0);
-    const double fro = (double)sqrtf((float)fro2) * (1.0 + 1e-6);
-    double gr = lane < 4 ? sN[5 * lane] : -1e300;
-    if (lane < 4)
-        for (int j = 0; j < 4; ++j)
-            if (j != lane) gr += fabs(sN[4 * lane + j]);
+}
+// out = n (p + c I); symmetric because p is a polynomial in n
+__device__ __forceinline__ void sym_mul_shift(const float* n, const float* p, float c, float* out) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) gr = fmax(gr, __shfl_xor_sync(0xffffffffu, gr, o));
-    // Faddeev-LeVerrier: p(l) = l^4 + c3 l^3 + c2 l^2 + c1 l + c0
-    auto trace4 = [&](double mine) {  // sum of the diagonal lanes 0, 5, 10, 15
-        double t = (lane < 16 && r == c) ? mine : 0.0;
-        return warp_sum_d(t);
-    };
-    double cf[4];
-    cf[3] = -trace4(lane < 16 ? sM[lane] : 0.0);
-    for (int k = 2; k <= 4; ++k) {
-        const double ck = cf[5 - k];
-        double t = 0.0;
-        if (lane < 16)
-            for (int j = 0; j < 4; ++j) t += sN[4 * r + j] * (sM[4 * j + c] + (j == c ? ck : 0.0));
-        __syncwarp();
-        if (lane < 16) sM[lane] = t;
-        __syncwarp();
-        cf[4 - k] = -trace4(t) * (k == 2 ? 0.5 : (k == 3 ? (1.0 / 3.0) : 0.25));
-    }
-    double l = fmin(fro, gr);
-    for (int it = 0; it < 60; ++it) {
-        const double p = (((l + cf[3]) * l + cf[2]) * l + cf[1]) * l + cf[0];
-        const double dp = ((4.0 * l + 3.0 * cf[3]) * l + 2.0 * cf[2]) * l + cf[1];
-        if (!(dp > 0.0)) break;
-        const double step = p * recip_d(dp);
-        l -= step;
-        if (!(fabs(step) > 1e-15 * fro)) break;
-    }
-    if (lane < 16) sA[lane] = sN[lane] - (r == c ? l : 0.0);
-    __syncwarp();
-    auto cof = [&](int row, int col) {  // (row, col) cofactor of A
-        int rr[3], cc[3], nn = 0, m = 0;
-        for (int i = 0; i < 4; ++i)
-            if (i != row) rr[nn++] = i;
-        for (int j = 0; j < 4; ++j)
-            if (j != col) cc[m++] = j;
-        const double d =
-            sA[4 * rr[0] + cc[0]] * (sA[4 * rr[1] + cc[1]] * sA[4 * rr[2] + cc[2]] - sA[4 * rr[1] + cc[2]] * sA[4 * rr[2] + cc[1]]) -
-            sA[4 * rr[0] + cc[1]] * (sA[4 * rr[1] + cc[0]] * sA[4 * rr[2] + cc[2]] - sA[4 * rr[1] + cc[2]] * sA[4 * rr[2] + cc[0]]) +
-            sA[4 * rr[0] + cc[2]] * (sA[4 * rr[1] + cc[0]] * sA[4 * rr[2] + cc[1]] - sA[4 * rr[1] + cc[1]] * sA[4 * rr[2] + cc[0]]);
-        return ((row + col) & 1) ? -d : d;
-    };
-    double dj = lane < 4 ? fabs(cof(lane, lane)) : -1.0;
-    int bj = lane;
+    for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const double od = __shfl_xor_sync(0xffffffffu, dj, o);
-        const int oj = __shfl_xor_sync(0xffffffffu, bj, o);
-        if (od > dj || (od == dj && oj < bj)) {
-            dj = od;
-            bj = oj;
+        for (int j = i; j < 4; ++j) {
+            float t = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) t = fmaf(n[sym(i, k)], k == j ? p[sym(k, j)] + c : p[sym(k, j)], t);
+            out[sym(i, j)] = t;
         }
+}
+
+// Thread 0 of the last CTA of an AlignStep: from the totals of the raw
+// moments, the centroids and S (ICP.cpp:166-197), N (:199-213), its dominant
+// eigenvector (above), R and t (:215-256) and pose <- (T R) pose (:20-28).
+__device__ __noinline__ void finish_step(IcpState* __restrict__ st, const FF* __restrict__ tot) {
+    // 1. centroids, S and N in FF
+    const float n = fadd(tot[0].hi, tot[0].lo);  // an exact count below 2^24
+    FF mu[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        const float h = fdiv(tot[1 + i].hi, n);
+        const float r = fadd(__fmaf_rn(-h, n, tot[1 + i].hi), tot[1 + i].lo);  // exact remainder + lo
+        mu[i] = ff_norm(h, fdiv(r, n));
     }
-    const bool ok = dj > 1e-24 * fro * fro * fro;
-    const double qk = (ok && lane < 4) ? cof(lane, bj) : 0.0;
-    const double inv_norm = rsqrt_d(warp_sum_d(qk * qk));
-    if (lane < 4) sq[lane] = qk * inv_norm;
-    if (lane == 0) s_ok = ok;
-    __syncwarp();
-    if (!s_ok && lane == 0) {
+    FF S[9];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) S[3 * r + c] = tot[7 + 3 * r + c] - tot[1 + r] * mu[3 + c];
+    const FF Sxx = S[0], Sxy = S[1], Sxz = S[2], Syx = S[3], Syy = S[4], Syz = S[5],
+             Szx = S[6], Szy = S[7], Szz = S[8];
+    FF nf[10] = {Sxx + Syy + Szz, Syz - Szy,       Szx - Sxz,       Sxy - Syx,
+                 Sxx - Syy - Szz, Sxy + Syx,       Szx + Sxz,
+                 Syy - Sxx - Szz, Syz + Szy,
+                 Szz - Sxx - Syy};
+    float f2 = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 10; ++i) {
+        const bool diag = i == 0 || i == 4 || i == 7 || i == 9;
+        f2 = fmaf(diag ? nf[i].hi : 2.0f * nf[i].hi, nf[i].hi, f2);
+    }
+    // power-of-two scale 2^-e/2 with f2 = m 2^e: N's Frobenius norm lands in [0.5, 1.5)
+    const int e = ((__float_as_int(f2) >> 23) & 0xff) - 127;
+    const float sc = __int_as_float((127 - (e >> 1)) << 23);
+    const bool finite = f2 > 1e-30f && f2 < 1e30f;
+    float f[10];
+#pragma unroll
+    for (int i = 0; i < 10; ++i) {
+        nf[i] = FF{nf[i].hi * sc, nf[i].lo * sc};
+        f[i] = nf[i].hi;
+    }
+    // 2. float search
+    float gmax = -1e30f;  // Gershgorin: the largest row bound
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        float t = f[sym(i, i)];
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (j != i) t += fabsf(f[sym(i, j)]);
+        gmax = fmaxf(gmax, t);
+    }
+    // start just above the smaller of the Gershgorin and Frobenius bounds
+    float l = fminf(gmax, sqrtf(f2 * sc * sc)) * 1.00001f + 1e-6f;
+    float m[10], w[10];
+    const float c3 = -(f[0] + f[4] + f[7] + f[9]);
+    sym_mul_shift(f, f, c3, m);
+    const float c2 = -0.5f * (m[0] + m[4] + m[7] + m[9]);
+    sym_mul_shift(f, m, c2, w);
+    const float c1 = -(w[0] + w[4] + w[7] + w[9]) * (1.0f / 3.0f);
+    float tr = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int k = 0; k < 4; ++k) tr = fmaf(f[sym(i, k)], k == i ? w[sym(k, i)] + c1 : w[sym(k, i)], tr);
+    const float c0 = -0.25f * tr;
+    for (int it = 0; it < 32; ++it) {
+        const float p = fmaf(fmaf(fmaf(l + c3, l, c2), l, c1), l, c0);
+        const float dp = fmaf(fmaf(fmaf(4.0f, l, 3.0f * c3), l, 2.0f * c2), l, c1);
+        if (!(dp > 0.0f)) break;
+        const float step = __fdividef(p, dp);
+        if (!(step > 0.0f)) break;
+        l -= step;
+        if (step <= 1e-7f * fabsf(l)) break;
+    }
+    const float d0 = fabsf(minor3(f, l, 1, 2, 3, 1, 2, 3)), d1 = fabsf(minor3(f, l, 0, 2, 3, 0, 2, 3));
+    const float d2 = fabsf(minor3(f, l, 0, 1, 3, 0, 1, 3)), d3 = fabsf(minor3(f, l, 0, 1, 2, 0, 1, 2));
+    int j = 0;
+    float dj = d0;
+    if (d1 > dj) { j = 1; dj = d1; }
+    if (d2 > dj) { j = 2; dj = d2; }
+    if (d3 > dj) { j = 3; dj = d3; }
+    float q[4];
+    int solver = 0;
+    if (finite && dj > 1e-4f) {
+        // 3. Rayleigh-quotient inverse iteration in FF
+        adj_column(f, l, j, q);
+        const int steps = dj < 1e-2f ? 2 : 1;
+        for (int s = 0; s < steps; ++s) {
+            FF num{0.0f, 0.0f}, qq{0.0f, 0.0f};
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                FF t{0.0f, 0.0f};
+#pragma unroll
+                for (int c = 0; c < 4; ++c) t = t + nf[sym(r, c)] * q[c];
+                num = num + t * q[r];
+                qq = qq + FF{q[r], 0.0f} * q[r];
+            }
+            FF qn[4];
+            adj_column(nf, ff_div(num, qq), j, qn);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) q[i] = qn[i].hi;
+        }
+    } else {
+        // 4. nearly repeated largest eigenvalue (or no finite solution)
+        solver = 1;
         double A[16], V[16];
-        for (int i = 0; i < 16; ++i) A[i] = sN[i];
-        jacobi4(A, V, V, false);
+        for (int r = 0; r < 4; ++r)
+            for (int c = 0; c < 4; ++c) A[4 * r + c] = (double)nf[sym(r, c)].hi + (double)nf[sym(r, c)].lo;
+        jacobi4(A, V);
         int imax = 0;
         for (int i = 1; i < 4; ++i)
             if (A[i] > A[imax]) imax = i;
-        double nn = 0.0;
-        for (int i = 0; i < 4; ++i) nn += V[4 * i + imax] * V[4 * i + imax];
-        nn = sqrt(nn);
-        for (int i = 0; i < 4; ++i) sq[i] = V[4 * i + imax] / nn;
+        for (int i = 0; i < 4; ++i) q[i] = (float)V[4 * i + imax];
     }
-    __syncwarp();
-    // R from the quaternion (x = scalar part, ICP.cpp:233-254), one entry per lane
-    const double qx = sq[0], qy = sq[1], qz = sq[2], qw = sq[3];
-    double Rj = 0.0;
-    switch (lane) {
-        case 0: Rj = 1.0 - 2.0 * (qz * qz + qw * qw); break;
-        case 1: Rj = 2.0 * (qy * qz - qx * qw); break;
-        case 2: Rj = 2.0 * (qy * qw + qx * qz); break;
-        case 3: Rj = 2.0 * (qy * qz + qx * qw); break;
-        case 4: Rj = 1.0 - 2.0 * (qy * qy + qw * qw); break;
-        case 5: Rj = 2.0 * (qz * qw - qx * qy); break;
-        case 6: Rj = 2.0 * (qy * qw - qx * qz); break;
-        case 7: Rj = 2.0 * (qz * qw + qx * qy); break;
-        case 8: Rj = 1.0 - 2.0 * (qy * qy + qz * qz); break;
-        default: break;
-    }
-    double R[9];
+    // q = normalize(q) (:231); one Newton step refines the reciprocal square root
+    const float qq = fmaf(q[0], q[0], fmaf(q[1], q[1], fmaf(q[2], q[2], q[3] * q[3])));
+    float ri = rsqrtf(qq);
+    ri = ri * fmaf(-0.5f * qq * ri, ri, 1.5f);
 #pragma unroll
-    for (int i = 0; i < 9; ++i) R[i] = __shfl_sync(0xffffffffu, Rj, i);
-    // step = T * R with t = mu_q - R mu_p (row-major 4x4), one entry per lane
-    if (lane < 16) {
-        double v;
-        if (r == 3) v = (c == 3) ? 1.0 : 0.0;
-        else if (c < 3) v = R[3 * r + c];
-        else v = mu[3 + r] - (R[3 * r] * mu[0] + R[3 * r + 1] * mu[1] + R[3 * r + 2] * mu[2]);
-        sT[lane] = v;
+    for (int i = 0; i < 4; ++i) q[i] *= ri;
+    // R from the quaternion, x = scalar part (:233-254)
+    const float xy = fmul(q[0], q[1]), xz = fmul(q[0], q[2]), xw = fmul(q[0], q[3]);
+    const float yy = fmul(q[1], q[1]), yz = fmul(q[1], q[2]), yw = fmul(q[1], q[3]);
+    const float zz = fmul(q[2], q[2]), zw = fmul(q[2], q[3]), ww = fmul(q[3], q[3]);
+    Mat4 R{};
+    R.m[0] = fsub(1.0f, fmul(2.0f, fadd(zz, ww)));
+    R.m[4] = fmul(2.0f, fsub(yz, xw));
+    R.m[8] = fmul(2.0f, fadd(yw, xz));
+    R.m[1] = fmul(2.0f, fadd(yz, xw));
+    R.m[5] = fsub(1.0f, fmul(2.0f, fadd(yy, ww)));
+    R.m[9] = fmul(2.0f, fsub(zw, xy));
+    R.m[2] = fmul(2.0f, fsub(yw, xz));
+    R.m[6] = fmul(2.0f, fadd(zw, xy));
+    R.m[10] = fsub(1.0f, fmul(2.0f, fadd(yy, zz)));
+    R.m[15] = 1.0f;
+    // t = dstMedian - R srcMedian (:256), T = [I t] (:259-261), step = T R (:263)
+    const float mp[4] = {fadd(mu[0].hi, mu[0].lo), fadd(mu[1].hi, mu[1].lo), fadd(mu[2].hi, mu[2].lo), 1.0f};
+    float rmp[4];
+    mat_vec(R.m, mp, rmp);
+    Mat4 T{};
+    T.m[0] = T.m[5] = T.m[10] = T.m[15] = 1.0f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) T.m[12 + i] = fsub(fadd(mu[3 + i].hi, mu[3 + i].lo), rmp[i]);
+    Mat4 P;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) P.m[i] = st->pose_f[i];
+    const Mat4 out = mat_mul(mat_mul(T, R), P);
+#pragma unroll
+    for (int i = 0; i < 16; ++i) st->pose_f[i] = out.m[i];
+    st->n_assoc = (int)n;
+    st->sum_l2 = (double)fadd(tot[16].hi, tot[16].lo);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        st->mu_s[i] = mp[i];
+        st->mu_d[i] = fadd(mu[3 + i].hi, mu[3 + i].lo);
     }
-    __syncwarp();
-    double pnew = 0.0;
-    if (lane < 16)
-        for (int k = 0; k < 4; ++k) pnew += sT[4 * r + k] * st->pose[4 * k + c];
-    __syncwarp();
-    if (lane < 16) {
-        st->pose[lane] = pnew;
-        st->pose_f[4 * c + r] = (float)pnew;
+    const int it = st->iter;
+    if (it < kIcpMaxStats) {
+        st->stats[it].n_assoc = (int)n;
+        st->stats[it].solver = solver;
+        st->stats[it].rms = n > 0.0f ? (double)sqrtf(fdiv(fadd(tot[16].hi, tot[16].lo), n)) : 0.0;
+        const unsigned long long t_end = global_ns();
+        st->stats[it].body_us = (float)(st->t_body - st->t_start) * 1e-3f;
+        st->stats[it].tail_us = (float)(t_end - st->t_body) * 1e-3f;
     }
-    if (lane == 0) {
-        st->n_assoc = (int)(n + 0.5);
-        st->sum_l2 = tot[16];
-        for (int i = 0; i < 3; ++i) {
-            st->mu_s[i] = (float)mu[i];
-            st->mu_d[i] = (float)mu[3 + i];
-        }
-        const int it = st->iter;
-        if (it < kIcpMaxStats) {
-            st->stats[it].n_assoc = (int)(n + 0.5);
-            st->stats[it].rms = n > 0.0 ? (double)sqrtf((float)(tot[16] * inv_n)) : 0.0;
-            const unsigned long long t_end = global_ns();
-            st->stats[it].body_us = (float)(st->t_body - st->t_start) * 1e-3f;
-            st->stats[it].tail_us = (float)(t_end - st->t_body) * 1e-3f;
-        }
-        st->t_start = ~0ull;
-        st->t_body = 0ull;
-        st->iter = it + 1;
-    }
+    st->t_start = ~0ull;
+    st->t_body = 0ull;
+    st->iter = it + 1;
 }
 
 __global__ void k_icp_begin(IcpState* st, Mat4 guess) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    for (int r = 0; r < 4; ++r)
-        for (int c = 0; c < 4; ++c) st->pose[4 * r + c] = (double)guess.m[4 * c + r];
     for (int i = 0; i < 16; ++i) st->pose_f[i] = guess.m[i];
     st->iter = 0;
-    st->have_V = 0;
     st->done = 0u;
     st->t_start = ~0ull;
     st->t_body = 0ull;

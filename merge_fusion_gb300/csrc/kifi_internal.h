@@ -115,17 +115,14 @@ struct IcpArgs {
 
 struct IcpIterStats {
     int n_assoc;
-    int pad;
+    int solver;       // Horn's eigenvector: 0 closed form, 1 Jacobi fallback
     double rms;       // sqrt(mean of the associated squared distances)
     float body_us;    // first CTA start to last CTA end of the association
     float tail_us;    // last CTA end to the updated pose
 };
 
 struct IcpState {
-    double pose[16];    // eye-to-world estimate, row-major double
-    float pose_f[16];   // the same rounded to float, kifi order
-    double V[16];       // eigenvectors of the previous Horn solve (warm start)
-    int have_V;
+    float pose_f[16];   // eye-to-world estimate, kifi order
     unsigned int done;  // last-CTA counter
     float mu_s[4], mu_d[4];
     int n_assoc;
@@ -133,7 +130,7 @@ struct IcpState {
     double sum_l2;
     unsigned long long t_start, t_body;  // globaltimer stamps of the running step
     IcpIterStats stats[kIcpMaxStats];
-    float part[kIcpMaxCtas * 48];   // per-CTA float-float partial sums (24 components)
+    float part[34 * kIcpMaxCtas];   // per-CTA float-float partials: hi, lo rows of 17 components
 };
 
 cudaError_t icp_align_enqueue(const IcpArgs& a, IcpState* st, const Mat4& guess, int iterations,
