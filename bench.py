@@ -45,7 +45,7 @@ CAM = (W, H, F_PX, F_PX, W / 2.0, H / 2.0, 0.4, 4.0)
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--steps", type=int, default=95)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--prefill", type=int, default=100)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
@@ -96,7 +96,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -256,7 +256,7 @@ def run_gpu(args, rank, world, local):
     # ---- device-resident timed region
     check(lib.kifi_volume_set_profiling(vol, 1))
     t0 = Fp + Wu
-    ms_stage = np.zeros(3)
+    ms_stage = np.zeros(4)
     nst = C.c_int()
     check(lib.kifi_volume_stage_times(vol, ptr(ms_stage), C.byref(nst)))  # reset
     if world > 1:
@@ -316,14 +316,17 @@ def run_gpu(args, rank, world, local):
     value = world * K / (ms / 1e3)
     P = W * H
     algo_bytes = (12.0 * n0.astype(np.float64) + 4.0 * ne + 12.0 * n1 + 2.0 * P)
-    merge_ms = ms_stage[2] / max(nst.value, 1)
+    merge_ms = ms_stage[3] / max(nst.value, 1)
     achieved = float(algo_bytes.mean()) / (merge_ms / 1e3) / 1e9
     peak, peak_kind = measured_peak()
     traffic = None
     tr = ncu_traffic_per_voxel()
     if tr:
         traffic = float(tr["bytes_per_voxel"] * float((n0 + n1).mean()) + tr.get("bytes_fixed", 0.0))
-    launches_per_frame = 9 + (2 * ICP_ITERS + 2)
+    # per frame: frame set-up, splat+emit, sort (prepare, histogram, 4 passes),
+    # merge partition, merge+update; ICP: begin, one step per iteration, the
+    # next target's back-projection; a mesh call is 6 launches
+    launches_per_frame = 10 + (ICP_ITERS + 2)
     gpu_launches = K * launches_per_frame + (K // MESH_EVERY) * 6
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
@@ -343,6 +346,7 @@ def run_gpu(args, rank, world, local):
                      "ms_per_launch": merge_ms},
         "stage_ms_per_frame": {"splat_emit": ms_stage[0] / max(nst.value, 1),
                                "sort": ms_stage[1] / max(nst.value, 1),
+                               "merge_partition": ms_stage[2] / max(nst.value, 1),
                                "merge_update": merge_ms},
         "e2e": {"value": world * K / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 2 * P + 64,
                 "d2h_bytes_per_step": 64 + 1024},

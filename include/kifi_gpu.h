@@ -171,11 +171,11 @@ KIFI_API kifi_status kifi_mesh_device(kifi_volume* vol, int with_indices, size_t
 /* Stage timers, the GPU counterpart of the stop_watch the reference wires
  * into Integrator::Integrate (Integrator.cpp:45-70, "tmerge"/"tupd"): while
  * on, every integrated frame records CUDA events around splat+emit, the sort
- * of the new keys, and the fused merge+update.  kifi_volume_stage_times
- * waits for them, returns the summed milliseconds of the three stages and
- * the number of frames, and resets the accumulation. */
+ * of the new keys, the merge partition and the fused merge+update.
+ * kifi_volume_stage_times waits for them, returns the summed milliseconds of
+ * the four stages and the number of frames, and resets the accumulation. */
 KIFI_API kifi_status kifi_volume_set_profiling(kifi_volume* vol, int on);
-KIFI_API kifi_status kifi_volume_stage_times(kifi_volume* vol, double out_ms[3], int* frames);
+KIFI_API kifi_status kifi_volume_stage_times(kifi_volume* vol, double out_ms[4], int* frames);
 
 /* Sizes of the most recent merges (up to 64, oldest first): resident voxels
  * before, keys new to the volume, resident voxels after.  No reference
@@ -231,8 +231,8 @@ KIFI_API kifi_status kifi_icp_align_device(kifi_icp* icp, const void* depth_dev,
                                            const kifi_camera* cam,
                                            const float eye_to_world_guess[16], int iterations);
 
-/* Waits and reads the last alignment: the pose (float, as the reference
- * composes it, and optionally the same widened to double), per-iteration
+/* Waits and reads the last alignment: the pose (float, and optionally the
+ * float-float value it was rounded from, as a double), per-iteration
  * association counts and RMS
  * residuals (up to `capacity` entries; the reference prints the count,
  * ICP.cpp:133) and the iteration count.  Pointers may be NULL. */

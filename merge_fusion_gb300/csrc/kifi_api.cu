@@ -212,9 +212,9 @@ kifi_status integrate_sync(kifi_volume* v, const void* host_depth, bool u16,
 kifi_status kifi_volume_enqueue_frame(kifi_volume* v, const void* depth_dev, bool u16,
                                       const kifi_camera* cam, const float* w2e) {
     cudaEvent_t* ev = nullptr;
-    std::array<cudaEvent_t, 4> evs{};
+    std::array<cudaEvent_t, kStageEvents> evs{};
     if (v->profiling) {
-        for (int k = 0; k < 4; ++k) {
+        for (int k = 0; k < kStageEvents; ++k) {
             if (v->event_pool.empty()) {
                 cudaEvent_t e;
                 KIFI_CUDA(cudaEventCreate(&e));
@@ -470,19 +470,19 @@ kifi_status kifi_volume_set_profiling(kifi_volume* v, int on) {
     return KIFI_OK;
 }
 
-kifi_status kifi_volume_stage_times(kifi_volume* v, double out_ms[3], int* frames) {
+kifi_status kifi_volume_stage_times(kifi_volume* v, double out_ms[4], int* frames) {
     if (!v || !out_ms) return fail(KIFI_ERR_INVALID_ARGUMENT, "null argument");
     KIFI_CUDA(cudaSetDevice(v->device));
-    out_ms[0] = out_ms[1] = out_ms[2] = 0.0;
+    for (int k = 0; k < kStageEvents - 1; ++k) out_ms[k] = 0.0;
     const int n = (int)v->pending.size();
     for (auto& ev : v->pending) {
-        KIFI_CUDA(cudaEventSynchronize(ev[3]));
-        for (int k = 0; k < 3; ++k) {
+        KIFI_CUDA(cudaEventSynchronize(ev[kStageEvents - 1]));
+        for (int k = 0; k < kStageEvents - 1; ++k) {
             float ms = 0.0f;
             KIFI_CUDA(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
             out_ms[k] += ms;
         }
-        for (int k = 0; k < 4; ++k) v->event_pool.push_back(ev[k]);
+        for (int k = 0; k < kStageEvents; ++k) v->event_pool.push_back(ev[k]);
     }
     v->pending.clear();
     if (frames) *frames = n;

@@ -233,7 +233,7 @@ kifi_status kifi_icp_result(kifi_icp* c, float out_eye_to_world[16], double out_
     }
     if (out_eye_to_world) std::memcpy(out_eye_to_world, h->pose_f, 64);
     if (out_eye_to_world_d)
-        for (int i = 0; i < 16; ++i) out_eye_to_world_d[i] = (double)h->pose_f[i];
+        for (int i = 0; i < 16; ++i) out_eye_to_world_d[i] = (double)h->pose_f[i] + (double)h->pose_lo[i];
     const int it = h->iter < kIcpMaxStats ? h->iter : kIcpMaxStats;
     if (iterations) *iterations = h->iter;
     for (int i = 0; i < it && i < capacity; ++i) {

@@ -30,6 +30,10 @@ inline Mat4 load_mat(const float* m) {
 }  // namespace kifi
 
 // A volume handle (include/kifi_gpu.h): device state of one kifi::Volume.
+// stage timer events per frame: start, after splat+emit, after the sort,
+// after the merge partition, after the merge+update
+constexpr int kStageEvents = 5;
+
 struct kifi_volume {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -56,7 +60,7 @@ struct kifi_volume {
     // events around splat+emit, sort and merge+update
     bool profiling = false;
     std::vector<cudaEvent_t> event_pool;
-    std::vector<std::array<cudaEvent_t, 4>> pending;
+    std::vector<std::array<cudaEvent_t, kStageEvents>> pending;
 };
 
 // integrate entry shared by the ABI translation units: enqueues one frame

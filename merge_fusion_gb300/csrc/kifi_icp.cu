@@ -2,29 +2,26 @@
 // (KinectFission/kifi/ICP.cpp:9-265) and its target producers,
 // Renderer::Bin (Renderer.cpp:39-80) and a depth back-projection.
 //
-// One AlignStep is two kernels, both ending in a last-CTA-done finisher, so a
-// whole Align (any iteration count) is a fixed launch sequence with no host
-// round trip:
+// One AlignStep is one kernel, k_icp_step, ending in a last-CTA-done
+// finisher, so a whole Align (any iteration count) is a fixed launch sequence
+// with no host round trip:
 //
-//  k_icp_associate   one thread per source pixel of every row and every 4th
-//                    column (ICP.cpp:66-67): back-project with the current
-//                    pose estimate, project into the target camera, search
-//                    the 21x21 window for the nearest valid target point
-//                    within len^2 < 0.01 (:100-131; first minimum in scan
-//                    order wins).  The pairs are stored; counts and the
-//                    centroid sums are reduced with compensated float
-//                    arithmetic per thread and warp (Kahan / TwoSum) and in
-//                    double across CTAs.  The last CTA forms the centroids
-//                    (:166-167).
-//  k_icp_horn        the centred 3x3 cross-covariance (:169-197) with the
-//                    same compensated reduction; the last CTA builds Horn's
-//                    symmetric 4x4 matrix (:199-213) in double, finds its
-//                    dominant eigenvector in double by Horn's closed form
-//                    (characteristic quartic, Newton, adjugate; a cyclic
-//                    Jacobi solve for degenerate spectra), turns it into
-//                    R and t (:218-256) and accumulates the pose
-//                    step * pose in double (:23-28).  The float pose the next
-//                    association uses is that double pose rounded.
+//  association   every row and every 4th column (ICP.cpp:66-67) is a source
+//                pixel: back-project it with the current pose estimate,
+//                project into the target camera, search the 21x21 window for
+//                the nearest valid target point within len^2 < 0.01
+//                (:100-131; the first minimum in scan order wins).  CTAs own
+//                tiles of sources and stage the union of their windows in
+//                shared memory.
+//  moments       the associated pairs are not stored: count, sum p, sum q,
+//                sum p q^T and the squared distances are accumulated per
+//                CTA in float-float, each product split exactly by an FMA.
+//  finisher      the last CTA totals the per-CTA partials, and one thread
+//                forms the centroids and the centred cross-covariance
+//                (:166-197), Horn's matrix (:199-213), its dominant
+//                eigenvector (:215-231), R and t (:233-261) and the pose
+//                update (:20-28), without double precision (see the Horn
+//                solve below).
 //
 // The per-point arithmetic follows the reference's float expression order
 // and x86 float-to-int conversion (CVTTSS2SI: truncation, INT_MIN for NaN or
@@ -44,10 +41,10 @@ __device__ __forceinline__ int cvt_i32_x86(float f) {
 }
 __device__ __forceinline__ int wrap_sub(int a, int b) { return (int)((unsigned int)a - (unsigned int)b); }
 
-// Float-float (double-single) sums: a value is hi + lo with |lo| <= ulp(hi)/2.
-// GB300 runs double precision at a small fraction of the float rate, so the
-// compensated reductions stay in float pairs and only the final cross-CTA
-// total is formed in double.
+// Float-float (double-single) arithmetic: a value is hi + lo with |lo| about
+// ulp(hi)/2 or less -- a 48-bit significand.  GB300 issues double precision
+// at a small fraction of the float rate, so every compensated sum and the
+// Horn solve's precise steps use float pairs instead.
 struct FF {
     float hi, lo;
 };
@@ -231,10 +228,10 @@ __device__ __noinline__ void finish_step(IcpState* __restrict__ st, const FF* __
 // cross-covariance (:169-197), the kernel accumulates the raw moments --
 // count, sum p, sum q, sum p_r q_c (each product split exactly into a
 // float-float pair by an FMA) and the squared distances -- in float-float
-// per warp and CTA; the last CTA to finish totals them in double, forms the
-// centroids and S = sum p q^T - n mu_p mu_q^T in double, and runs the Horn
+// per warp and CTA; the last CTA to finish totals them, forms the centroids
+// and S = sum p q^T - (sum p) mu_q^T in float-float, and runs the Horn
 // solve.  Algebraically this is the reference's two-pass sum; numerically it
-// is at least as accurate.
+// is more accurate than the reference's float Kahan sums.
 constexpr int kAssocThreads = 512;
 constexpr int kMoments = 17;  // n, p xyz, q xyz, p q^T (9), len^2
 
@@ -485,8 +482,8 @@ __device__ __noinline__ void jacobi4(double* A, double* V) {
 //     a nearly repeated largest eigenvalue -- goes to the double Jacobi
 //     solver instead.
 //
-// R, t and the pose update are then float, in the reference's expression
-// order (ICP.cpp:233-263 and :20-28).
+// R, t and the accumulated pose are FF as well; the float pose the next
+// association uses is the FF pose rounded (its high part).
 //
 // Symmetric 4x4 matrices are held as their upper triangle, row by row.
 __host__ __device__ constexpr int sym(int i, int j) {
@@ -627,11 +624,12 @@ __device__ __noinline__ void finish_step(IcpState* __restrict__ st, const FF* __
     if (d1 > dj) { j = 1; dj = d1; }
     if (d2 > dj) { j = 2; dj = d2; }
     if (d3 > dj) { j = 3; dj = d3; }
-    float q[4];
+    FF q[4];
     int solver = 0;
     if (finite && dj > 1e-4f) {
         // 3. Rayleigh-quotient inverse iteration in FF
-        adj_column(f, l, j, q);
+        float qf[4];
+        adj_column(f, l, j, qf);
         const int steps = dj < 1e-2f ? 2 : 1;
         for (int s = 0; s < steps; ++s) {
             FF num{0.0f, 0.0f}, qq{0.0f, 0.0f};
@@ -639,14 +637,13 @@ __device__ __noinline__ void finish_step(IcpState* __restrict__ st, const FF* __
             for (int r = 0; r < 4; ++r) {
                 FF t{0.0f, 0.0f};
 #pragma unroll
-                for (int c = 0; c < 4; ++c) t = t + nf[sym(r, c)] * q[c];
-                num = num + t * q[r];
-                qq = qq + FF{q[r], 0.0f} * q[r];
+                for (int c = 0; c < 4; ++c) t = t + nf[sym(r, c)] * qf[c];
+                num = num + t * qf[r];
+                qq = qq + FF{qf[r], 0.0f} * qf[r];
             }
-            FF qn[4];
-            adj_column(nf, ff_div(num, qq), j, qn);
+            adj_column(nf, ff_div(num, qq), j, q);
 #pragma unroll
-            for (int i = 0; i < 4; ++i) q[i] = qn[i].hi;
+            for (int i = 0; i < 4; ++i) qf[i] = q[i].hi;
         }
     } else {
         // 4. nearly repeated largest eigenvalue (or no finite solution)
@@ -658,43 +655,43 @@ __device__ __noinline__ void finish_step(IcpState* __restrict__ st, const FF* __
         int imax = 0;
         for (int i = 1; i < 4; ++i)
             if (A[i] > A[imax]) imax = i;
-        for (int i = 0; i < 4; ++i) q[i] = (float)V[4 * i + imax];
+        for (int i = 0; i < 4; ++i) {
+            const double v = V[4 * i + imax];
+            q[i] = FF{(float)v, (float)(v - (double)(float)v)};
+        }
     }
-    // q = normalize(q) (:231); one Newton step refines the reciprocal square root
-    const float qq = fmaf(q[0], q[0], fmaf(q[1], q[1], fmaf(q[2], q[2], q[3] * q[3])));
-    float ri = rsqrtf(qq);
-    ri = ri * fmaf(-0.5f * qq * ri, ri, 1.5f);
+    // q = normalize(q) (:231): 1/sqrt(q'q) from a float estimate and one FF Newton step
+    const FF qq = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
+    const float r0 = rsqrtf(qq.hi);
+    const FF corr = (FF{1.0f, 0.0f} - qq * r0 * r0) * (0.5f * r0);
+    const FF ri = FF{r0, 0.0f} + corr;
 #pragma unroll
-    for (int i = 0; i < 4; ++i) q[i] *= ri;
-    // R from the quaternion, x = scalar part (:233-254)
-    const float xy = fmul(q[0], q[1]), xz = fmul(q[0], q[2]), xw = fmul(q[0], q[3]);
-    const float yy = fmul(q[1], q[1]), yz = fmul(q[1], q[2]), yw = fmul(q[1], q[3]);
-    const float zz = fmul(q[2], q[2]), zw = fmul(q[2], q[3]), ww = fmul(q[3], q[3]);
-    Mat4 R{};
-    R.m[0] = fsub(1.0f, fmul(2.0f, fadd(zz, ww)));
-    R.m[4] = fmul(2.0f, fsub(yz, xw));
-    R.m[8] = fmul(2.0f, fadd(yw, xz));
-    R.m[1] = fmul(2.0f, fadd(yz, xw));
-    R.m[5] = fsub(1.0f, fmul(2.0f, fadd(yy, ww)));
-    R.m[9] = fmul(2.0f, fsub(zw, xy));
-    R.m[2] = fmul(2.0f, fsub(yw, xz));
-    R.m[6] = fmul(2.0f, fadd(zw, xy));
-    R.m[10] = fsub(1.0f, fmul(2.0f, fadd(yy, zz)));
-    R.m[15] = 1.0f;
-    // t = dstMedian - R srcMedian (:256), T = [I t] (:259-261), step = T R (:263)
-    const float mp[4] = {fadd(mu[0].hi, mu[0].lo), fadd(mu[1].hi, mu[1].lo), fadd(mu[2].hi, mu[2].lo), 1.0f};
-    float rmp[4];
-    mat_vec(R.m, mp, rmp);
-    Mat4 T{};
-    T.m[0] = T.m[5] = T.m[10] = T.m[15] = 1.0f;
+    for (int i = 0; i < 4; ++i) q[i] = q[i] * ri;
+    // R from the quaternion, x = scalar part (:233-254), in FF
+    const FF xy = q[0] * q[1], xz = q[0] * q[2], xw = q[0] * q[3];
+    const FF yy = q[1] * q[1], yz = q[1] * q[2], yw = q[1] * q[3];
+    const FF zz = q[2] * q[2], zw = q[2] * q[3], ww = q[3] * q[3];
+    const FF one{1.0f, 0.0f};
+    const FF R[9] = {one - (zz + ww) * 2.0f, (yz - xw) * 2.0f,       (yw + xz) * 2.0f,
+                     (yz + xw) * 2.0f,       one - (yy + ww) * 2.0f, (zw - xy) * 2.0f,
+                     (yw - xz) * 2.0f,       (zw + xy) * 2.0f,       one - (yy + zz) * 2.0f};
+    // t = dstMedian - R srcMedian (:256); pose <- [R t; 0 1] pose (:259-263, :20-28)
+    FF t[3];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) T.m[12 + i] = fsub(fadd(mu[3 + i].hi, mu[3 + i].lo), rmp[i]);
-    Mat4 P;
+    for (int r = 0; r < 3; ++r) t[r] = mu[3 + r] - (R[3 * r] * mu[0] + R[3 * r + 1] * mu[1] + R[3 * r + 2] * mu[2]);
+    FF P[16];  // kifi order: entry (row r, column c) at 4c + r
 #pragma unroll
-    for (int i = 0; i < 16; ++i) P.m[i] = st->pose_f[i];
-    const Mat4 out = mat_mul(mat_mul(T, R), P);
+    for (int i = 0; i < 16; ++i) P[i] = FF{st->pose_f[i], st->pose_lo[i]};
 #pragma unroll
-    for (int i = 0; i < 16; ++i) st->pose_f[i] = out.m[i];
+    for (int c = 0; c < 4; ++c)
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            const FF v = R[3 * r] * P[4 * c] + R[3 * r + 1] * P[4 * c + 1] + R[3 * r + 2] * P[4 * c + 2] +
+                         t[r] * P[4 * c + 3];
+            st->pose_f[4 * c + r] = v.hi;
+            st->pose_lo[4 * c + r] = v.lo;
+        }
+    const float mp[3] = {fadd(mu[0].hi, mu[0].lo), fadd(mu[1].hi, mu[1].lo), fadd(mu[2].hi, mu[2].lo)};
     st->n_assoc = (int)n;
     st->sum_l2 = (double)fadd(tot[16].hi, tot[16].lo);
 #pragma unroll
@@ -718,7 +715,10 @@ __device__ __noinline__ void finish_step(IcpState* __restrict__ st, const FF* __
 
 __global__ void k_icp_begin(IcpState* st, Mat4 guess) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    for (int i = 0; i < 16; ++i) st->pose_f[i] = guess.m[i];
+    for (int i = 0; i < 16; ++i) {
+        st->pose_f[i] = guess.m[i];
+        st->pose_lo[i] = 0.0f;
+    }
     st->iter = 0;
     st->done = 0u;
     st->t_start = ~0ull;

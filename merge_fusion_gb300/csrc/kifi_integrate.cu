@@ -545,9 +545,11 @@ static unsigned int max_tiles_of(const VolumeBuffers& vb) {
 
 static cudaError_t merge_enqueue(DeviceCtl* ctl, const Geom& g, VolumeBuffers& vb,
                                  const MergeInputs& in, const void* depth, bool u16,
-                                 const FrameConst& fc, const LaunchShape& ls, cudaStream_t st) {
+                                 const FrameConst& fc, const LaunchShape& ls, cudaStream_t st,
+                                 cudaEvent_t after_partition = nullptr) {
     const unsigned int mt = max_tiles_of(vb);
     k_merge_partition<<<(mt + 255) / 256, 256, 0, st>>>(ctl, g, vb, in, vb.splits, mt);
+    if (after_partition) cudaEventRecord(after_partition, st);
     if (u16)
         k_merge_update<true><<<ls.merge_ctas, kMergeThreads, 0, st>>>(ctl, g, vb, in, depth,
                                                                      vb.splits, fc);
@@ -578,8 +580,8 @@ cudaError_t integrate_enqueue(DeviceCtl* ctl, const Geom& g, VolumeBuffers& vb, 
     if (e != cudaSuccess) return e;
     if (events) cudaEventRecord(events[2], st);
     MergeInputs in{vb.new_keys, nullptr, nullptr, &ctl->n_new, true};
-    e = merge_enqueue(ctl, g, vb, in, depth_dev, depth_u16, fc, ls, st);
-    if (events) cudaEventRecord(events[3], st);
+    e = merge_enqueue(ctl, g, vb, in, depth_dev, depth_u16, fc, ls, st, events ? events[3] : nullptr);
+    if (events) cudaEventRecord(events[4], st);
     return e;
 }
 

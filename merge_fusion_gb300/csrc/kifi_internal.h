@@ -122,7 +122,8 @@ struct IcpIterStats {
 };
 
 struct IcpState {
-    float pose_f[16];   // eye-to-world estimate, kifi order
+    float pose_f[16];   // eye-to-world estimate, kifi order (float-float high part)
+    float pose_lo[16];  // and its low part
     unsigned int done;  // last-CTA counter
     float mu_s[4], mu_d[4];
     int n_assoc;

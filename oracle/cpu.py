@@ -165,16 +165,20 @@ class Volume:
         return verts[:nv.value].copy(), idx[:ni.value].copy()
 
 
-def icp_align(depth, cam, e2w_guess, synth, synth_e2w, iters):
-    """Returns (float pose (16,), double pose (16,), n_assoc of last step)."""
+def icp_align(depth, cam, e2w_guess, synth, synth_e2w, iters, fp64=False):
+    """Returns (float pose (16,), double pose (16,), n_assoc of last step).
+    fp64: sums, cross-covariance and Horn's matrix in double instead of the
+    reference's float Kahan sums (the FP64 reference solution)."""
     depth, guess, se2w = f32(depth), f32(e2w_guess), f32(synth_e2w)
     synth = f32(synth)
     sh, sw = synth.shape[0], synth.shape[1]
     out = np.zeros(16, np.float32)
     outd = np.zeros(16, np.float64)
     st = _IcpStats()
+    lib().or_icp_set_fp64(C.c_int(1 if fp64 else 0))
     lib().or_icp_align(_p(depth), C.byref(cam_struct(cam)), _p(guess), _p(synth), C.c_int(sw),
                        C.c_int(sh), _p(se2w), C.c_int(iters), _p(out), _p(outd), C.byref(st))
+    lib().or_icp_set_fp64(C.c_int(0))
     return out, outd, st.n_assoc
 
 

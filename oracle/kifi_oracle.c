@@ -534,6 +534,21 @@ typedef struct {
     double sums[15];      /* last iteration: src sum (3), dst sum (3), S (9) */
 } or_icp_stats;
 
+/* quaternion (x = scalar part) to rotation -- ICP.cpp:233-254 */
+static void or_quat_to_rot(const double* q, double* R) {
+    double xy = q[0] * q[1], xz = q[0] * q[2], xw = q[0] * q[3], yy = q[1] * q[1],
+           yz = q[1] * q[2], yw = q[1] * q[3], zz = q[2] * q[2], zw = q[2] * q[3], ww = q[3] * q[3];
+    R[0] = 1.0 - 2.0 * (zz + ww); R[1] = 2.0 * (yz - xw);       R[2] = 2.0 * (yw + xz);
+    R[3] = 2.0 * (yz + xw);       R[4] = 1.0 - 2.0 * (yy + ww); R[5] = 2.0 * (zw - xy);
+    R[6] = 2.0 * (yw - xz);       R[7] = 2.0 * (zw + xy);       R[8] = 1.0 - 2.0 * (yy + zz);
+}
+
+/* 0: the reference's float Kahan sums and float N (parity mode);
+ * 1: every sum, the centred cross-covariance and N in double (the FP64
+ *    reference solution the GPU's float-float solve is measured against). */
+static int g_icp_fp64 = 0;
+void or_icp_set_fp64(int on) { g_icp_fp64 = on; }
+
 /* One ICP::AlignStep (ICP.cpp:35-265) with the Horn solve in double.
  *
  * Association, Kahan centroid and cross-covariance sums follow the reference
@@ -601,6 +616,46 @@ int or_icp_step(const float* depth, const or_camera* cam, const float* e2w_guess
                 kahan_add(&dsum[3], 1.0f);
             }
         }
+    if (g_icp_fp64) {
+        /* FP64 reference solution of the same associations: double sums,
+         * two-pass centred cross-covariance, N in double */
+        double ms[3] = {0, 0, 0}, md[3] = {0, 0, 0}, Sd[9] = {0};
+        for (size_t i = 0; i < na; ++i)
+            for (int l = 0; l < 3; ++l) { ms[l] += assoc[6 * i + l]; md[l] += assoc[6 * i + 3 + l]; }
+        for (int l = 0; l < 3; ++l) { ms[l] /= (double)na; md[l] /= (double)na; }
+        for (size_t i = 0; i < na; ++i)
+            for (int r = 0; r < 3; ++r)
+                for (int c = 0; c < 3; ++c)
+                    Sd[3 * r + c] += ((double)assoc[6 * i + r] - ms[r]) * ((double)assoc[6 * i + 3 + c] - md[c]);
+        free(assoc);
+        double Xx = Sd[0], Xy = Sd[1], Xz = Sd[2], Yx = Sd[3], Yy = Sd[4], Yz = Sd[5], Zx = Sd[6], Zy = Sd[7], Zz = Sd[8];
+        double a[16] = {Xx + Yy + Zz, Yz - Zy, Zx - Xz, Xy - Yx,
+                        Yz - Zy, Xx - Yy - Zz, Xy + Yx, Zx + Xz,
+                        Zx - Xz, Xy + Yx, Yy - Xx - Zz, Yz + Zy,
+                        Xy - Yx, Zx + Xz, Yz + Zy, Zz - Xx - Yy};
+        double ev[4], V[16];
+        or_jacobi4(a, ev, V);
+        int imax = 0;
+        for (int i = 1; i < 4; ++i)
+            if (ev[i] > ev[imax]) imax = i;
+        double q[4] = {V[0 + imax], V[4 + imax], V[8 + imax], V[12 + imax]};
+        double ql = sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+        for (int l = 0; l < 4; ++l) q[l] /= ql;
+        double R[9];
+        or_quat_to_rot(q, R);
+        for (int r = 0; r < 4; ++r)
+            for (int c = 0; c < 4; ++c) step[4 * r + c] = (r == c) ? 1.0 : 0.0;
+        for (int r = 0; r < 3; ++r) {
+            double t = md[r];
+            for (int c = 0; c < 3; ++c) {
+                step[4 * r + c] = R[3 * r + c];
+                t -= R[3 * r + c] * ms[c];
+            }
+            step[4 * r + 3] = t;
+        }
+        if (stats) stats->n_assoc = (int)na;
+        return na > 0 ? 0 : 1;
+    }
     float nf = (float)na;
     float sm[4], dm[4];
     for (int l = 0; l < 4; ++l) { sm[l] = ssum[l].s / nf; dm[l] = dsum[l].s / nf; }
@@ -629,12 +684,8 @@ int or_icp_step(const float* depth, const or_camera* cam, const float* e2w_guess
     double q[4] = {V[0 + imax], V[4 + imax], V[8 + imax], V[12 + imax]};
     double ql = sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
     for (int l = 0; l < 4; ++l) q[l] /= ql;
-    /* quaternion (x = scalar part) to rotation -- ICP.cpp:233-254 */
-    double xy = q[0] * q[1], xz = q[0] * q[2], xw = q[0] * q[3], yy = q[1] * q[1],
-           yz = q[1] * q[2], yw = q[1] * q[3], zz = q[2] * q[2], zw = q[2] * q[3], ww = q[3] * q[3];
-    double R[9] = {1.0 - 2.0 * (zz + ww), 2.0 * (yz - xw),       2.0 * (yw + xz),
-                   2.0 * (yz + xw),       1.0 - 2.0 * (yy + ww), 2.0 * (zw - xy),
-                   2.0 * (yw - xz),       2.0 * (zw + xy),       1.0 - 2.0 * (yy + zz)};
+    double R[9];
+    or_quat_to_rot(q, R);
     for (int r = 0; r < 4; ++r)
         for (int c = 0; c < 4; ++c) step[4 * r + c] = (r == c) ? 1.0 : 0.0;
     for (int r = 0; r < 3; ++r) {

@@ -116,3 +116,32 @@ def test_icp_on_bin_target(gpu, oracle_cpu, golden):
     pose = kifi.ICP().Align(depth, guess, target, e2w, cam_params(cam), 5)
     o, od, n = oracle_cpu.icp_align(depth, cam, guess, target, e2w, 5)
     assert np.abs(pose - o).max() < POSE_TOL
+
+
+def test_icp_error_vs_fp64_oracle(gpu, oracle_cpu, golden):
+    # The float-float Horn solve and pose accumulation against the FP64
+    # reference solution of the same associations (double sums, two-pass
+    # cross-covariance, double Jacobi, double pose).
+    from merge_fusion_gb300 import kifi, scenes
+    worst = 0.0
+    depth, view, cam = golden["depth"], golden["view"], golden["camera"]
+    e2w = oracle_cpu.invert_transform(view)
+    target = oracle_cpu.backproject(depth, cam, e2w)
+    icp = kifi.ICP()
+    for case in golden["icp"]:
+        guess = posed(e2w, case["guess_offset"])
+        icp.Align(depth, guess, target, e2w, cam_params(cam), case["iterations"])
+        _, pd, _, _ = icp.Result()
+        _, od, _ = oracle_cpu.icp_align(depth, cam, guess, target, e2w, case["iterations"], fp64=True)
+        worst = max(worst, float(np.abs(pd - od).max()))
+    seq = scenes.room_scene(n_frames=3, seed=2)
+    rc = seq.camera
+    for i in (1, 2):
+        prev = seq.eye_to_world_f32(i - 1)
+        icp.SetTargetFromDepth(seq.frames[i - 1], cam_params(rc), prev)
+        tgt = oracle_cpu.backproject(seq.depth_m(i - 1), rc, prev)
+        icp.AlignToTarget(seq.depth_m(i), prev, cam_params(rc), iterations=15)
+        _, pd, _, _ = icp.Result()
+        _, od, _ = oracle_cpu.icp_align(seq.depth_m(i), rc, prev, tgt, prev, 15, fp64=True)
+        worst = max(worst, float(np.abs(pd - od).max()))
+    assert worst < POSE_TOL, worst

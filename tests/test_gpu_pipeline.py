@@ -68,7 +68,7 @@ def test_stage_timers_and_frame_log(gpu, golden):
     check(lib.kifi_volume_set_profiling(vol.handle, 1))
     for i in range(3):
         kifi.Integrator().Integrate(vol, depth, cam_params(cam), view)
-    ms = np.zeros(3)
+    ms = np.zeros(4)
     nf = C.c_int()
     check(lib.kifi_volume_stage_times(vol.handle, ms.ctypes.data_as(C.c_void_p), C.byref(nf)))
     assert nf.value == 3 and (ms > 0).all()

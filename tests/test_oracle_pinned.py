@@ -52,6 +52,11 @@ def test_oracle_icp_matches_golden(oracle_cpu, golden):
         # float Horn solve in the reference vs double Jacobi here: 1e-5 m / rad
         assert np.abs(pose - ref).max() < 1e-5
         assert n > 1000
+        # the FP64 reference solution (double sums and N) stays within the
+        # same budget of the reference's float result
+        pose64, _, n64 = oracle_cpu.icp_align(depth, cam, guess, synth, e2w, case["iterations"], fp64=True)
+        assert np.abs(pose64 - ref).max() < 1e-5
+        assert abs(n64 - n) <= max(3, n // 1000)
 
 
 def test_oracle_matches_reference_stagewise(oracle_cpu, oracle_ref, golden):
