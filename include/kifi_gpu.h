@@ -192,6 +192,34 @@ KIFI_API kifi_status kifi_radix_sort_u32(uint32_t* keys, size_t n);
  * (algorithm.h:93-134): stable sort of 32-bit keys carrying 32-bit values. */
 KIFI_API kifi_status kifi_radix_sort_pairs_u32(uint32_t* keys, uint32_t* values, size_t n);
 
+/* No counterpart in the reference.  The radix sort of
+ * kifi_radix_sort_pairs_u32 for callers that must not allocate device
+ * memory: it sorts keys_dev[0..n) -- and values_dev[0..n) with them when
+ * values_dev is not NULL -- in place, in device memory, on `stream` (a
+ * cudaStream_t; NULL for the default stream), with results identical to
+ * kifi_radix_sort_pairs_u32.  Its scratch is a fixed area of static device
+ * memory built into the library (12.0 MiB, present once the library's
+ * module is loaded); it calls no cudaMalloc, cudaFree or other allocating
+ * routine.  It is meant for processes whose device memory is handed out by
+ * their own pool, and for frame loops that cannot pay for cudaMalloc /
+ * cudaFree, which synchronise the device and stall its other streams.
+ *  - n <= KIFI_RADIX_SORT_STATIC_MAX; a larger n returns
+ *    KIFI_ERR_INVALID_ARGUMENT and does nothing.
+ *  - The first call on a device (the device current at the call) looks up
+ *    the scratch area's address; make that first call before any stream
+ *    capture.
+ *  - There is one scratch area per device: calls that overlap in time (from
+ *    several host threads, or on several streams) race on it and corrupt
+ *    each other's results.  Serialise them.  The call returns only when the
+ *    sort has finished on `stream`, so calls made one after another from
+ *    one thread never overlap.
+ *  - The caller zeroes nothing: the scratch state that must start at zero
+ *    is zero when the library is loaded, and the rest is reset by each call.
+ *  - KIFI_ERR_TIMEOUT when a bounded device wait gave up. */
+#define KIFI_RADIX_SORT_STATIC_MAX (1u << 20)
+KIFI_API kifi_status kifi_radix_sort_pairs_u32_static(uint32_t* keys_dev, uint32_t* values_dev, size_t n,
+                                                      void* stream);
+
 /* ------------------------------------------------------------------ ICP */
 
 /* Context of kifi::ICP (KinectFission/kifi/ICP.h:15-42): device buffers for

@@ -77,6 +77,7 @@ SIGNATURES = {
                                         C.c_void_p, C.c_int]),
     "kifi_icp_result": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                   C.c_int, C.POINTER(C.c_int)]),
+    "kifi_radix_sort_pairs_u32_static": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
     "kifi_icp_iteration_times": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                            C.POINTER(C.c_int)]),
     "kifi_bin": (C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
