@@ -155,6 +155,8 @@ __device__ __forceinline__ void moments_total(const IcpState* st, FF* out) {
 }
 
 constexpr int kTileCols = 8, kTileRows = 32;
+constexpr int kSplitRow = 10;   // window rows [0, 10) to the lower half-warp set, [10, 21) to the upper
+constexpr int kStageBatch = 4;  // staging loads in flight per thread
 constexpr int kStagePixels = 3840;  // float4 per pixel: 60 KB
 
 // Scan of one thread's window in the staged region (float4 per pixel,
@@ -234,6 +236,7 @@ __device__ __noinline__ void finish_step(IcpState* __restrict__ st, const FF* __
 // is more accurate than the reference's float Kahan sums.
 constexpr int kAssocThreads = 512;
 constexpr int kMoments = 17;  // n, p xyz, q xyz, p q^T (9), len^2
+static_assert(kAssocThreads / 32 == kMoments - 1, "one warp per moment after the count");
 
 __device__ __forceinline__ unsigned long long global_ns() {
     unsigned long long t;
@@ -251,7 +254,9 @@ __global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step(IcpArgs a, IcpSta
     __shared__ int s_box[4];
     __shared__ float s_hb[kTileCols][32];  // lower half's best len^2 per source
     __shared__ int s_hi[kTileCols][32];    // and its candidate number
-    __shared__ FF s_acc[kTileCols][kMoments];
+    __shared__ FF s_acc[kMoments];             // this CTA's moments (index 0 unused: s_count)
+    __shared__ float s_rec[7][kTileCols * 32];  // per source: p xyz, q xyz, len^2 (0 when no pair)
+    __shared__ unsigned int s_count;
     const int n_cols = (a.width + 3) / 4;
     const int tiles_x = (n_cols + kTileCols - 1) / kTileCols;
     const int tiles_y = (a.height + kTileRows - 1) / kTileRows;
@@ -259,7 +264,8 @@ __global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step(IcpArgs a, IcpSta
     const int wcol = warp >> 1, half = warp & 1;
     const float half_w = fmul((float)a.synth_w, 0.5f), half_h = fmul((float)a.synth_h, 0.5f);
     const size_t n_synth = (size_t)a.synth_w * a.synth_h;
-    if (half == 0 && lane < kMoments) s_acc[wcol][lane] = FF{0.0f, 0.0f};
+    if (threadIdx.x < kMoments) s_acc[threadIdx.x] = FF{0.0f, 0.0f};
+    if (threadIdx.x == 0) s_count = 0u;
     if (threadIdx.x == 0) atomicMin(&st->t_start, global_ns());
     for (int tile = blockIdx.x; tile < tiles_x * tiles_y; tile += gridDim.x) {
         const int tx = tile % tiles_x, ty = tile / tiles_x;
@@ -312,19 +318,35 @@ __global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step(IcpArgs a, IcpSta
         const int pitch = bw | 1;  // odd pitch: vertically adjacent windows hit distinct banks
         const bool staged = bx1 >= 0 && pitch * bh <= kStagePixels;
         if (staged) {
-            for (int i = threadIdx.x; i < bw * bh; i += kAssocThreads) {
-                const int ry = i / bw, rx = i - ry * bw;
-                const size_t at = (size_t)(by0 + ry) * a.synth_w + (bx0 + rx);
-                float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (at < n_synth) q = __ldg(a.synth + at);
-                // (0,0,0) = no point (ICP.cpp:112): stage it as NaN
-                if (q.x == 0.0f && q.y == 0.0f && q.z == 0.0f) q.x = __int_as_float(0x7fffffff);
-                stage[ry * pitch + rx] = q;
+            // kStageBatch independent loads in flight per thread, then the stores
+            const int total = bw * bh;
+            for (int i0 = threadIdx.x; i0 < total; i0 += kStageBatch * kAssocThreads) {
+                float4 q[kStageBatch];
+#pragma unroll
+                for (int k = 0; k < kStageBatch; ++k) {
+                    const int i = i0 + k * kAssocThreads;
+                    q[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (i < total) {
+                        const int ry = i / bw, rx = i - ry * bw;
+                        const size_t at = (size_t)(by0 + ry) * a.synth_w + (bx0 + rx);
+                        if (at < n_synth) q[k] = __ldg(a.synth + at);
+                    }
+                }
+#pragma unroll
+                for (int k = 0; k < kStageBatch; ++k) {
+                    const int i = i0 + k * kAssocThreads;
+                    if (i < total) {
+                        const int ry = i / bw, rx = i - ry * bw;
+                        // (0,0,0) = no point (ICP.cpp:112): stage it as NaN
+                        if (q[k].x == 0.0f && q[k].y == 0.0f && q[k].z == 0.0f) q[k].x = __int_as_float(0x7fffffff);
+                        stage[ry * pitch + rx] = q[k];
+                    }
+                }
             }
         }
         __syncthreads();
         // this thread's rows of the window
-        const int r0 = half ? 11 : 0, r1 = half ? nr : min(nr, 11);
+        const int r0 = half ? kSplitRow : 0, r1 = half ? nr : min(nr, kSplitRow);
         float best = 0.01f;
         int rc = -1;
         float3 bq = make_float3(0.f, 0.f, 0.f);
@@ -378,29 +400,40 @@ __global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step(IcpArgs a, IcpSta
                 bq = make_float3(q.x, q.y, q.z);
             }
             const bool hit = mine && rc >= 0;
-            // this tile's raw moments, folded into the warp's accumulators
-            if (__any_sync(0xffffffffu, hit)) {
-                const float px = hit ? wp[0] : 0.f, py = hit ? wp[1] : 0.f, pz = hit ? wp[2] : 0.f;
-                const float qx = hit ? bq.x : 0.f, qy = hit ? bq.y : 0.f, qz = hit ? bq.z : 0.f;
-                const float pv[3] = {px, py, pz}, qv[3] = {qx, qy, qz};
-#pragma unroll
-                for (int i = 0; i < kMoments; ++i) {
-                    FF m;
-                    if (i == 0) m = FF{hit ? 1.0f : 0.0f, 0.0f};
-                    else if (i < 4) m = FF{pv[i - 1], 0.0f};
-                    else if (i < 7) m = FF{qv[i - 4], 0.0f};
-                    else if (i < 16) m = two_prod(pv[(i - 7) / 3], qv[(i - 7) % 3]);
-                    else m = FF{hit ? best : 0.0f, 0.0f};
-                    const FF w = warp_sum_ff(m);
-                    if (lane == 0) s_acc[wcol][i] = ff_add(s_acc[wcol][i], w);
-                }
-            }
+            // this source's pair for the tile's moments (zeros when none)
+            const int sidx = wcol * 32 + lane;
+            s_rec[0][sidx] = hit ? wp[0] : 0.f;
+            s_rec[1][sidx] = hit ? wp[1] : 0.f;
+            s_rec[2][sidx] = hit ? wp[2] : 0.f;
+            s_rec[3][sidx] = hit ? bq.x : 0.f;
+            s_rec[4][sidx] = hit ? bq.y : 0.f;
+            s_rec[5][sidx] = hit ? bq.z : 0.f;
+            s_rec[6][sidx] = hit ? best : 0.f;
+            const unsigned int nh = __popc(__ballot_sync(0xffffffffu, hit));
+            if (lane == 0 && nh) atomicAdd(&s_count, nh);
         }
-        __syncthreads();  // staging buffer and half results are reused by the next tile
+        __syncthreads();
+        // the tile's raw moments: warp w reduces moment w + 1 over the 256
+        // sources (lane l takes sources l, l + 32, ...), in float-float
+        {
+            const int c = warp + 1;
+            FF acc{0.0f, 0.0f};
+#pragma unroll
+            for (int k = 0; k < kTileCols; ++k) {
+                const int sidx = lane + 32 * k;
+                FF m;
+                if (c < 7) m = FF{s_rec[c - 1][sidx], 0.0f};
+                else if (c < 16) m = two_prod(s_rec[(c - 7) / 3][sidx], s_rec[3 + (c - 7) % 3][sidx]);
+                else m = FF{s_rec[6][sidx], 0.0f};
+                acc = ff_add(acc, m);
+            }
+            acc = warp_sum_ff(acc);
+            if (lane == 0) s_acc[c] = ff_add(s_acc[c], acc);
+        }
+        __syncthreads();  // staging buffer, half results and records are reused by the next tile
     }
     if (threadIdx.x < kMoments) {
-        FF t = s_acc[0][threadIdx.x];
-        for (int w = 1; w < kTileCols; ++w) t = ff_add(t, s_acc[w][threadIdx.x]);
+        const FF t = threadIdx.x == 0 ? FF{(float)s_count, 0.0f} : s_acc[threadIdx.x];
         st->part[(size_t)(2 * threadIdx.x) * kIcpMaxCtas + blockIdx.x] = t.hi;
         st->part[(size_t)(2 * threadIdx.x + 1) * kIcpMaxCtas + blockIdx.x] = t.lo;
     }
