@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0,
                     help="bounded CPU-baseline sample (seconds of CPU work)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--graphs", action="store_true",
+                    help="one CUDA graph per frame (kifi_pipeline_set_graphs) instead of plain launches")
     return ap.parse_args()
 
 
@@ -226,6 +228,7 @@ def run_gpu(args, rank, world, local):
     d.device = local
     pipe = C.c_void_p()
     check(lib.kifi_pipeline_create(C.byref(d), C.byref(pipe)), "pipeline")
+    check(lib.kifi_pipeline_set_graphs(pipe, 1 if args.graphs else 0))
     vol = lib.kifi_pipeline_volume(pipe)
     vs = torch.cuda.ExternalStream(lib.kifi_volume_stream(vol))
     ist = torch.cuda.ExternalStream(lib.kifi_icp_stream(lib.kifi_pipeline_icp(pipe)))
@@ -305,6 +308,8 @@ def run_gpu(args, rank, world, local):
     e2e_s = float(e2e_t.item())
     nv, ni = C.c_size_t(), C.c_size_t()
     check(lib.kifi_pipeline_mesh_counts(pipe, C.byref(nv), C.byref(ni)))
+    gb, gu = C.c_longlong(), C.c_longlong()
+    check(lib.kifi_pipeline_graph_stats(pipe, C.byref(gb), C.byref(gu)))
     check(lib.kifi_volume_size(vol, C.byref(n_resident)))
 
     if rank != 0:
@@ -351,6 +356,7 @@ def run_gpu(args, rank, world, local):
         "e2e": {"value": world * K / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 2 * P + 64,
                 "d2h_bytes_per_step": 64 + 1024},
         "gpu_launches": gpu_launches,
+        "graphs": {"on": bool(args.graphs), "instantiated": int(gb.value), "updated": int(gu.value)},
         "mesh": {"vertices": nv.value, "indices": ni.value},
     }
     line["clocks"] = clocks.summary()

@@ -283,6 +283,45 @@ KIFI_API kifi_status kifi_icp_iteration_times(kifi_icp* icp, float* body_us, flo
 KIFI_API kifi_status kifi_bin(const float* points, size_t n, const float world_to_clip[16],
                               float* out, int width, int height);
 
+/* ----------------------------------------------------------------- I/O */
+
+/* kifi::DepthStream (KinectFission/kifi/DepthStream.h:13-45,
+ * DepthStream.cpp:15-102): a .depth v1 (640x480, 16-bit mm) or v2 (width,
+ * height, 16-bit mm or float m) recording.  Header errors return
+ * KIFI_ERR_FORMAT (the reference asserts). */
+typedef struct kifi_depthstream kifi_depthstream;
+KIFI_API kifi_status kifi_depthstream_open(const char* path, kifi_depthstream** out);
+KIFI_API kifi_status kifi_depthstream_close(kifi_depthstream* stream);
+/* DepthStream::FrameCount (DepthStream.h:24) plus the frame geometry */
+KIFI_API kifi_status kifi_depthstream_info(kifi_depthstream* stream, int* width, int* height,
+                                           int* texel_is_u16, int* frame_count);
+/* DepthStream::NextFrame (DepthStream.cpp:55-98): the next frame as float
+ * metres (width*height, row-major; 16-bit texels * 0.001f) and its view
+ * matrix (world to eye, kifi column order).  KIFI_ERR_END_OF_STREAM after
+ * the last frame (the reference returns false); KIFI_ERR_FORMAT on a
+ * truncated frame. */
+KIFI_API kifi_status kifi_depthstream_next_frame(kifi_depthstream* stream, float* out_depth_m,
+                                                 float out_view[16]);
+/* The same frame copied raw -- 16-bit millimetres or float metres, as
+ * kifi_depthstream_info reports -- into device memory, asynchronously on
+ * `stream` (a cudaStream_t) through pinned double-buffered staging; pass the
+ * buffer to the *_device integrate calls with the matching depth_is_u16.
+ * The view is returned at once. */
+KIFI_API kifi_status kifi_depthstream_next_frame_device(kifi_depthstream* stream, void* depth_dev,
+                                                        float out_view[16], void* cuda_stream);
+
+/* kifi::Mesher::Mesh2Obj (Mesher.h:20-25, Mesher.cpp:50-78): "v x y z" lines
+ * (printf %f) then "f a b c" lines with 1-based indices. */
+KIFI_API kifi_status kifi_mesh_to_obj(const float* verts, size_t n_verts, const uint32_t* indices,
+                                      size_t n_indices, const char* path);
+
+/* Volume checkpoints; no counterpart in the reference.  kifi_volume_save
+ * writes the geometry, the sorted keys and the (distance-sum, weight) voxels;
+ * kifi_volume_load creates a volume on `device` holding exactly those
+ * voxels, so integration resumes where it stopped. */
+KIFI_API kifi_status kifi_volume_save(kifi_volume* vol, const char* path);
+KIFI_API kifi_status kifi_volume_load(const char* path, int device, kifi_volume** out);
+
 /* ------------------------------------------------------------ pipeline */
 
 /* Arguments of kifi::Pipeline::Pipeline(cameraParams, volumeResolution,
@@ -330,6 +369,17 @@ KIFI_API kifi_status kifi_pipeline_integrate_device(kifi_pipeline* p, const void
 KIFI_API kifi_status kifi_pipeline_sync(kifi_pipeline* p, float out_eye_to_world[16]);
 
 /* Vertex and index counts of the last mesh the pipeline extracted. */
+/* No counterpart in the reference.  With graphs on, each frame -- the upload
+ * of a page-locked host frame, the fusion launches and the tracking launches
+ * on both streams -- runs as one CUDA graph: captured, applied to the
+ * instantiated graph with cudaGraphExecUpdate and launched once.  Results
+ * are identical to graphs off.  Frames from pageable host memory are uploaded
+ * outside the graph.  kifi_pipeline_graph_stats counts instantiations and
+ * in-place updates. */
+KIFI_API kifi_status kifi_pipeline_set_graphs(kifi_pipeline* p, int on);
+KIFI_API kifi_status kifi_pipeline_graph_stats(kifi_pipeline* p, long long* instantiated,
+                                               long long* updated);
+
 KIFI_API kifi_status kifi_pipeline_mesh_counts(kifi_pipeline* p, size_t* n_verts,
                                                size_t* n_indices);
 

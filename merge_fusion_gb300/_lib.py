@@ -77,6 +77,17 @@ SIGNATURES = {
                                         C.c_void_p, C.c_int]),
     "kifi_icp_result": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                   C.c_int, C.POINTER(C.c_int)]),
+    "kifi_pipeline_set_graphs": (C.c_int, [C.c_void_p, C.c_int]),
+    "kifi_pipeline_graph_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
+    "kifi_depthstream_open": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),
+    "kifi_depthstream_close": (C.c_int, [C.c_void_p]),
+    "kifi_depthstream_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                        C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "kifi_depthstream_next_frame": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "kifi_depthstream_next_frame_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "kifi_mesh_to_obj": (C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.c_char_p]),
+    "kifi_volume_save": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "kifi_volume_load": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_void_p)]),
     "kifi_radix_sort_pairs_u32_static": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
     "kifi_icp_iteration_times": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                            C.POINTER(C.c_int)]),

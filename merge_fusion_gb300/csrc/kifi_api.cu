@@ -165,6 +165,12 @@ kifi_status frame_prologue(kifi_volume* v, const kifi_camera* cam) {
     return KIFI_OK;
 }
 
+}  // namespace
+
+kifi_status kifi_volume_prepare_frame(kifi_volume* v, const kifi_camera* cam) { return frame_prologue(v, cam); }
+
+namespace {
+
 // Host frame -> device: straight from page-locked memory, else staged
 // through the volume's pinned buffer.
 kifi_status upload_depth(kifi_volume* v, const void* src, size_t bytes) {

@@ -22,9 +22,6 @@ struct kifi_icp {
     int sw = 0, sh = 0;
     Mat4 synth_e2w{};
     bool have_target = false;
-    float4* src = nullptr;
-    float4* dst = nullptr;
-    size_t n_src_cap = 0;
     int last_iters = 0;
 };
 
@@ -59,16 +56,6 @@ kifi_status enqueue_align(kifi_icp* c, const void* depth_dev, bool u16, const ki
     if (iterations < 0 || iterations > kIcpMaxStats)
         return fail(KIFI_ERR_INVALID_ARGUMENT, "iterations must be in [0, 64]");
     const size_t n_src = (size_t)((cam->width + 3) / 4) * cam->height;
-    if (n_src > c->n_src_cap) {
-        KIFI_CUDA(cudaStreamSynchronize(c->stream));
-        cudaFree(c->src);
-        cudaFree(c->dst);
-        c->src = c->dst = nullptr;
-        c->n_src_cap = 0;
-        KIFI_CUDA(cudaMalloc(&c->src, n_src * sizeof(float4)));
-        KIFI_CUDA(cudaMalloc(&c->dst, n_src * sizeof(float4)));
-        c->n_src_cap = n_src;
-    }
     IcpArgs a{};
     a.depth = depth_dev;
     a.depth_u16 = u16 ? 1 : 0;
@@ -84,8 +71,6 @@ kifi_status enqueue_align(kifi_icp* c, const void* depth_dev, bool u16, const ki
     a.synth = c->synth;
     a.synth_w = c->sw;
     a.synth_h = c->sh;
-    a.src = c->src;
-    a.dst = c->dst;
     KIFI_CUDA(icp_align_enqueue(a, c->st, load_mat(guess), iterations, icp_ctas(c, n_src),
                                 c->stream));
     c->last_iters = iterations;
@@ -93,6 +78,12 @@ kifi_status enqueue_align(kifi_icp* c, const void* depth_dev, bool u16, const ki
 }
 
 }  // namespace
+
+// Everything an alignment against a target of the camera's size may need to
+// allocate, done ahead (outside any stream capture).
+kifi_status kifi_icp_prepare_frame(kifi_icp* c, const kifi_camera* cam) {
+    return reserve_target(c, cam->width, cam->height);
+}
 
 extern "C" {
 
@@ -127,6 +118,10 @@ kifi_status kifi_icp_create(int device, void* stream, kifi_icp** out) {
         kifi_icp_destroy(c);
         return s;
     }
+    if ((e = icp_init_device())) {
+        kifi_icp_destroy(c);
+        return cuda_fail(e, "ICP kernel attributes");
+    }
     *out = c;
     return KIFI_OK;
 }
@@ -139,8 +134,6 @@ kifi_status kifi_icp_destroy(kifi_icp* c) {
     cudaFree(c->depth_dev);
     cudaFree(c->synth);
     cudaFree(c->staging);
-    cudaFree(c->src);
-    cudaFree(c->dst);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return KIFI_OK;

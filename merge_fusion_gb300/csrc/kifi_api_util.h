@@ -65,6 +65,10 @@ struct kifi_volume {
 
 // integrate entry shared by the ABI translation units: enqueues one frame
 // (device depth) on the volume's stream, growing buffers first when needed.
+// Host-side capacity checks (and growth) a frame of `cam` may need, done
+// ahead of enqueueing it -- nothing in kifi_volume_enqueue_frame then waits.
+kifi_status kifi_volume_prepare_frame(kifi_volume* v, const kifi_camera* cam);
+kifi_status kifi_icp_prepare_frame(kifi_icp* c, const kifi_camera* cam);
 kifi_status kifi_volume_enqueue_frame(kifi_volume* v, const void* depth_dev, bool u16,
                                       const kifi_camera* cam, const float* world_to_eye);
 

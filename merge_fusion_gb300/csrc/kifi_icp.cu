@@ -838,11 +838,15 @@ cudaError_t icp_align_enqueue(const IcpArgs& a, IcpState* st, const Mat4& guess,
     const int tiles = ((n_cols + kTileCols - 1) / kTileCols) * ((a.height + kTileRows - 1) / kTileRows);
     const int ctas = tiles < kIcpMaxCtas ? tiles : kIcpMaxCtas;
     const size_t smem = kStagePixels * sizeof(float4);
-    cudaError_t e =
-        cudaFuncSetAttribute(k_icp_step, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
     for (int it = 0; it < iterations; ++it) k_icp_step<<<ctas, kAssocThreads, smem, stream>>>(a, st);
     return cudaGetLastError();
+}
+
+// The association's dynamic shared memory above the default 48 KB limit; set
+// once per device, outside any stream capture.
+cudaError_t icp_init_device() {
+    return cudaFuncSetAttribute(k_icp_step, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(kStagePixels * sizeof(float4)));
 }
 
 cudaError_t expand_target_enqueue(const float* in, int n, float4* out, int ctas, cudaStream_t st) {

@@ -109,8 +109,6 @@ struct IcpArgs {
     float proj[16];         // EyeToClipRH * inverse(synth eye-to-world), kifi order
     const float4* synth;    // target world points (w unused), synth_w * synth_h
     int synth_w, synth_h;
-    float4* src;            // per source pixel: associated point (w = pose row 3)
-    float4* dst;            // per source pixel: target point, w = 1 when associated
 };
 
 struct IcpIterStats {
@@ -134,6 +132,7 @@ struct IcpState {
     float part[34 * kIcpMaxCtas];   // per-CTA float-float partials: hi, lo rows of 17 components
 };
 
+cudaError_t icp_init_device();
 cudaError_t icp_align_enqueue(const IcpArgs& a, IcpState* st, const Mat4& guess, int iterations,
                               int ctas, cudaStream_t stream);
 cudaError_t backproject_enqueue(const void* depth, bool u16, const kifi_camera& cam,

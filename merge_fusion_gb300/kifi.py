@@ -13,6 +13,7 @@ Matrices: a (16,) float array is taken in kifi's float4x4 memory order
 as the matrix itself (element [row, col]).
 """
 import ctypes as C
+import os
 
 import numpy as np
 
@@ -165,6 +166,25 @@ class Volume:
     def stream(self):
         return _lib.load().kifi_volume_stream(self._h)
 
+    def save(self, path):
+        """Checkpoint: geometry, keys and voxels (no reference counterpart)."""
+        check(_lib.load().kifi_volume_save(self._h, os.fsencode(path)), "save")
+
+    @classmethod
+    def load(cls, path, device=0):
+        """A new volume holding exactly the voxels of a checkpoint."""
+        h = C.c_void_p()
+        lib = _lib.load()
+        check(lib.kifi_volume_load(os.fsencode(path), int(device), C.byref(h)), "load")
+        self = cls.__new__(cls)
+        self._h = h
+        with open(path, "rb") as f:
+            hdr = f.read(20)
+        self._res = int(np.frombuffer(hdr[8:12], np.int32)[0])
+        self._side = np.frombuffer(hdr[12:16], np.float32)[0]
+        self._trunc = np.frombuffer(hdr[16:20], np.float32)[0]
+        return self
+
 
 class Integrator:
     """Integrator::Integrate (Integrator.h:19-26)."""
@@ -193,7 +213,14 @@ class Integrator:
 
 
 class Mesher:
-    """Mesher::Mesh (Mesher.h:17-18)."""
+    """Mesher::Mesh (Mesher.h:17-18) and Mesher::Mesh2Obj (Mesher.h:20-25)."""
+
+    @staticmethod
+    def Mesh2Obj(vertices, indices, out_obj_file_name):
+        v = np.ascontiguousarray(vertices, dtype=np.float32).reshape(-1, 3)
+        i = np.ascontiguousarray(indices, dtype=np.uint32).reshape(-1)
+        check(_lib.load().kifi_mesh_to_obj(_ptr(v), v.shape[0], _ptr(i), i.size,
+                                           os.fsencode(out_obj_file_name)), "Mesh2Obj")
 
     def Mesh(self, volume, with_indices=True):
         """Returns (vertices float32 (V, 3), indices uint32 (I,)); without
@@ -309,3 +336,50 @@ def radix_sort(keys, values=None):
 
 __all__ = ["DepthSensorParams", "Volume", "Integrator", "Mesher", "ICP", "Renderer", "radix_sort",
            "KifiError", "as_kifi_matrix"]
+
+
+class DepthStream:
+    """DepthStream (DepthStream.h:13-45): a .depth v1/v2 recording."""
+
+    def __init__(self, file_name):
+        self._h = None
+        h = C.c_void_p()
+        check(_lib.load().kifi_depthstream_open(os.fsencode(file_name), C.byref(h)), "DepthStream")
+        self._h = h
+        w, hh, u16, n = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        check(_lib.load().kifi_depthstream_info(h, C.byref(w), C.byref(hh), C.byref(u16), C.byref(n)),
+              "DepthStream")
+        self.width, self.height, self.texel_is_u16, self._n = w.value, hh.value, bool(u16.value), n.value
+
+    def __del__(self):
+        self.close()
+
+    def close(self):
+        if self._h is not None:
+            _lib.load().kifi_depthstream_close(self._h)
+            self._h = None
+
+    def FrameCount(self):
+        return self._n
+
+    def NextFrame(self):
+        """(frame float32 (height, width) metres, view (16,) kifi order), or
+        None after the last frame (the reference returns false)."""
+        frame = np.zeros((self.height, self.width), np.float32)
+        view = np.zeros(16, np.float32)
+        st = _lib.load().kifi_depthstream_next_frame(self._h, _ptr(frame), _ptr(view))
+        if st == 10:  # KIFI_ERR_END_OF_STREAM
+            return None
+        check(st, "NextFrame")
+        return frame, view
+
+    def NextFrameDevice(self, depth_dev_ptr, cuda_stream=None):
+        """Raw texels of the next frame into device memory (async on the
+        stream); returns the view, or None after the last frame."""
+        view = np.zeros(16, np.float32)
+        st = _lib.load().kifi_depthstream_next_frame_device(self._h, C.c_void_p(depth_dev_ptr),
+                                                            _ptr(view), cuda_stream)
+        if st == 10:
+            return None
+        check(st, "NextFrameDevice")
+        return view

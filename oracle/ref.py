@@ -196,3 +196,10 @@ def read_depthstream(path):
         return frames
     finally:
         lib().kref_depthstream_close(h)
+
+
+def mesh2obj(verts, indices, path):
+    """Mesher::Mesh2Obj (Mesher.cpp:50-78) of the reference on the given arrays."""
+    v = np.ascontiguousarray(verts, np.float32).reshape(-1, 3)
+    i = np.ascontiguousarray(indices, np.uint32).reshape(-1)
+    lib().kref_mesh2obj(_p(v), C.c_size_t(v.shape[0]), _p(i), C.c_size_t(i.size), str(path).encode())

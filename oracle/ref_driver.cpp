@@ -250,6 +250,14 @@ void kref_invert_transform(const float* in, float* out) {
 void* kref_depthstream_open(const char* path) { return new DepthStream(path); }
 void kref_depthstream_close(void* h) { delete static_cast<DepthStream*>(h); }
 int kref_depthstream_frame_count(void* h) { return static_cast<DepthStream*>(h)->FrameCount(); }
+// Mesher::Mesh2Obj (Mesher.cpp:50-78)
+void kref_mesh2obj(const float* verts, size_t nv, const unsigned* idx, size_t ni, const char* path) {
+    std::vector<util::float3> v(nv);
+    std::memcpy(v.data(), verts, 12 * nv);
+    std::vector<unsigned> i(idx, idx + ni);
+    Mesher::Mesh2Obj(v, i, path);
+}
+
 int kref_depthstream_next(void* h, float* depth, int capacity, int* w, int* hgt, float* view) {
     util::vector2d<float> frame;
     util::float4x4 v;

@@ -82,3 +82,65 @@ def test_stage_timers_and_frame_log(gpu, golden):
     assert cnt.value == 3
     assert n0[0] == 0 and n1[0] == golden["cases"][0]["voxels"]
     assert (n1[:3] == n0[:3] + ne[:3]).all() and n0[1] == n1[0]
+
+
+def _run_pipeline(lib, seq, graphs, device_frames):
+    import torch
+    from merge_fusion_gb300._lib import PipelineDesc, check
+    d = PipelineDesc()
+    d.camera = cam_params(seq.camera).camera()
+    d.resolution, d.side_length_m, d.truncation_m = 1024, 4.096, 0.02
+    d.icp_iterations, d.mesh_every, d.mesh_with_indices = 15, 3, 1
+    d.device = 0
+    pipe = C.c_void_p()
+    check(lib.kifi_pipeline_create(C.byref(d), C.byref(pipe)))
+    check(lib.kifi_pipeline_set_graphs(pipe, 1 if graphs else 0))
+    poses = []
+    out = np.zeros(16, np.float32)
+    try:
+        pinned = [torch.from_numpy(np.ascontiguousarray(f).view(np.int16)).pin_memory() for f in seq.frames]
+        dev = [p.cuda() for p in pinned]
+        torch.cuda.synchronize()
+        for i in range(len(seq.frames)):
+            w2e = seq.world_to_eye_f32(i)
+            if device_frames:
+                check(lib.kifi_pipeline_integrate_device(pipe, C.c_void_p(dev[i].data_ptr()), 1,
+                                                         w2e.ctypes.data_as(C.c_void_p)))
+                check(lib.kifi_pipeline_sync(pipe, out.ctypes.data_as(C.c_void_p)))
+            else:
+                check(lib.kifi_pipeline_integrate(pipe, C.c_void_p(pinned[i].data_ptr()), 1,
+                                                  w2e.ctypes.data_as(C.c_void_p),
+                                                  out.ctypes.data_as(C.c_void_p)))
+            poses.append(out.copy())
+        vol = lib.kifi_pipeline_volume(pipe)
+        n = C.c_size_t()
+        check(lib.kifi_volume_size(vol, C.byref(n)))
+        k = np.zeros(n.value, np.uint32)
+        v = np.zeros((n.value, 2), np.float32)
+        got = C.c_size_t()
+        check(lib.kifi_volume_export(vol, k.ctypes.data_as(C.c_void_p), v.ctypes.data_as(C.c_void_p),
+                                     n.value, C.byref(got)))
+        nv, ni = C.c_size_t(), C.c_size_t()
+        check(lib.kifi_pipeline_mesh_counts(pipe, C.byref(nv), C.byref(ni)))
+        built, updated = C.c_longlong(), C.c_longlong()
+        check(lib.kifi_pipeline_graph_stats(pipe, C.byref(built), C.byref(updated)))
+        return k, v, poses, (nv.value, ni.value), (built.value, updated.value)
+    finally:
+        lib.kifi_pipeline_destroy(pipe)
+
+
+@pytest.mark.parametrize("device_frames", [False, True])
+def test_pipeline_graphs_match_plain_launches(gpu, device_frames):
+    from merge_fusion_gb300 import _lib, scenes
+    lib = _lib.load()
+    seq = scenes.room_scene(n_frames=6, seed=5)
+    k0, v0, p0, m0, _ = _run_pipeline(lib, seq, False, device_frames)
+    k1, v1, p1, m1, (built, updated) = _run_pipeline(lib, seq, True, device_frames)
+    assert np.array_equal(k0, k1)
+    assert np.array_equal(canon_bits(v0), canon_bits(v1))
+    for a, b in zip(p0, p1):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    assert m0 == m1
+    # the first frame (no tracking) and the first tracked frame instantiate;
+    # the rest update the instantiated graph in place
+    assert built + updated == 6 and updated >= 3, (built, updated)
