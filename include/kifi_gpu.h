@@ -322,6 +322,18 @@ KIFI_API kifi_status kifi_mesh_to_obj(const float* verts, size_t n_verts, const 
 KIFI_API kifi_status kifi_volume_save(kifi_volume* vol, const char* path);
 KIFI_API kifi_status kifi_volume_load(const char* path, int device, kifi_volume** out);
 
+/* ------------------------------------------------------- learned proposer */
+
+/* No counterpart in the reference.  The pose proposer's tensor-core GEMM:
+ * C[m x n] = A[m x k] * B[n x k]^T (or C += with accumulate != 0), A and B
+ * BF16 in device memory with K contiguous (row strides lda, ldb elements),
+ * C FP32 (row stride ldc), accumulated in FP32 on the tcgen05 tensor cores.
+ * k, lda, ldb and k_split must be multiples of 8 and A, B 16-byte aligned;
+ * k_split > 0 splits K across CTAs (requires accumulate).  Synchronous on
+ * `stream`. */
+KIFI_API kifi_status kifi_gemm_bf16(const void* a_dev, const void* b_dev, float* c_dev, int m, int n, int k,
+                                    int lda, int ldb, int ldc, int k_split, int accumulate, void* stream);
+
 /* ------------------------------------------------------------ pipeline */
 
 /* Arguments of kifi::Pipeline::Pipeline(cameraParams, volumeResolution,

@@ -77,6 +77,8 @@ SIGNATURES = {
                                         C.c_void_p, C.c_int]),
     "kifi_icp_result": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                   C.c_int, C.POINTER(C.c_int)]),
+    "kifi_gemm_bf16": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
+                                 C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]),
     "kifi_pipeline_set_graphs": (C.c_int, [C.c_void_p, C.c_int]),
     "kifi_pipeline_graph_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
     "kifi_depthstream_open": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),

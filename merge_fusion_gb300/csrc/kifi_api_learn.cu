@@ -1,0 +1,37 @@
+// kifi_api_learn.cu -- C ABI of the learned pose proposer's tensor-core
+// building blocks (no counterpart in the reference).
+#include <mutex>
+
+#include "kifi_api_util.h"
+
+using namespace kifi;
+
+namespace {
+__device__ unsigned int g_gemm_status;
+}
+
+extern "C" {
+
+kifi_status kifi_gemm_bf16(const void* a_dev, const void* b_dev, float* c_dev, int m, int n, int k, int lda,
+                           int ldb, int ldc, int k_split, int accumulate, void* stream) {
+    if (!a_dev || !b_dev || !c_dev || m < 0 || n < 0 || k < 0) return fail(KIFI_ERR_INVALID_ARGUMENT, "bad argument");
+    if (k % 8 || lda % 8 || ldb % 8 || (k_split > 0 && k_split % 8) || ((uintptr_t)a_dev | (uintptr_t)b_dev) % 16 ||
+        lda < k || ldb < k || ldc < n)
+        return fail(KIFI_ERR_INVALID_ARGUMENT, "gemm: K, lda, ldb and the split must be multiples of 8, "
+                                                "operands 16-byte aligned");
+    if (k_split > 0 && k_split < k && !accumulate)
+        return fail(KIFI_ERR_INVALID_ARGUMENT, "gemm: a split K accumulates into C");
+    if (m == 0 || n == 0) return KIFI_OK;
+    unsigned int* status = nullptr;
+    KIFI_CUDA(cudaGetSymbolAddress((void**)&status, g_gemm_status));
+    cudaStream_t st = (cudaStream_t)stream;
+    KIFI_CUDA(cudaMemsetAsync(status, 0, sizeof(unsigned int), st));
+    KIFI_CUDA(gemm_bf16_enqueue(a_dev, b_dev, c_dev, m, n, k, lda, ldb, ldc, k_split, accumulate != 0, status, st));
+    unsigned int h = 0;
+    KIFI_CUDA(cudaMemcpyAsync(&h, status, sizeof h, cudaMemcpyDeviceToHost, st));
+    KIFI_CUDA(cudaStreamSynchronize(st));
+    if (h) return fail(KIFI_ERR_TIMEOUT, "gemm: a bounded device wait gave up");
+    return KIFI_OK;
+}
+
+}  // extern "C"

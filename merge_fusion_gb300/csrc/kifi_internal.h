@@ -141,4 +141,10 @@ cudaError_t expand_target_enqueue(const float* in, int n, float4* out, int ctas,
 cudaError_t bin_enqueue(const float* pts, unsigned int n, const Mat4& w2c, int width, int height,
                         unsigned long long* zbuf, float* out, int ctas, cudaStream_t st);
 
+// C[M x N] (+)= A[M x K] * B[N x K]^T, BF16 in, FP32 out, on tcgen05 tensor
+// cores (kifi_tc_gemm.cu).  k_split > 0 splits K across CTAs that add into C
+// atomically (atomic must then be true and C pre-initialised).
+cudaError_t gemm_bf16_enqueue(const void* A, const void* B, float* C, int M, int N, int K, int lda, int ldb,
+                              int ldc, int k_split, bool atomic, unsigned int* status, cudaStream_t st);
+
 }  // namespace kifi
