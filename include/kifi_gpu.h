@@ -334,6 +334,40 @@ KIFI_API kifi_status kifi_volume_load(const char* path, int device, kifi_volume*
 KIFI_API kifi_status kifi_gemm_bf16(const void* a_dev, const void* b_dev, float* c_dev, int m, int n, int k,
                                     int lda, int ldb, int ldc, int k_split, int accumulate, void* stream);
 
+/* No counterpart in the reference: the learned ICP pose proposer -- a small
+ * convolutional network (4 conv 3x3/2 layers 32-64-64-128, global average
+ * pool, MLP 128-64-6) mapping two depth frames box-downsampled to 80 x 60 to
+ * the 6-DoF twist (rotation vector, translation; camera frame of the first
+ * frame) of the second frame's pose relative to the first, used to
+ * warm-start ICP.  BF16 weights and activations, FP32 accumulation on the
+ * tcgen05 tensor cores (kifi_gemm_bf16), FP32 master weights and Adam.
+ * Inputs are NHWC FP16 [batch][60][80][2] (metres, 0 = no depth); batches
+ * are multiples of 8 up to max_batch.  Parameters are one FP32 vector of
+ * kifi_proposer_param_count entries (layer by layer: weights [out][in],
+ * then biases, each padded to a multiple of 8). */
+typedef struct kifi_proposer kifi_proposer;
+KIFI_API kifi_status kifi_proposer_create(int device, int max_batch, kifi_proposer** out);
+KIFI_API kifi_status kifi_proposer_destroy(kifi_proposer* pr);
+KIFI_API kifi_status kifi_proposer_param_count(kifi_proposer* pr, size_t* n);
+KIFI_API kifi_status kifi_proposer_set_params(kifi_proposer* pr, const float* host, size_t n);
+KIFI_API kifi_status kifi_proposer_get_params(kifi_proposer* pr, float* host, size_t n);
+/* one network input from two device depth frames (width, height multiples
+ * of 80 and 60): per 8x8 block the mean of the non-zero depths, or 0 */
+KIFI_API kifi_status kifi_proposer_make_input(kifi_proposer* pr, const void* depth_a_dev,
+                                              const void* depth_b_dev, int depth_is_u16, int width,
+                                              int height, void* out_fp16_dev);
+KIFI_API kifi_status kifi_proposer_set_inputs(kifi_proposer* pr, const void* inputs_fp16_dev, int batch);
+KIFI_API kifi_status kifi_proposer_get_inputs(kifi_proposer* pr, void* out_fp16_dev, int batch);
+/* forward pass on the inputs set: batch x 6 twists into host memory */
+KIFI_API kifi_status kifi_proposer_predict(kifi_proposer* pr, int batch, float* out_twists_host);
+/* forward + mean-squared-error loss against targets (device, batch x 6) +
+ * backward; the loss and the gradient vector (optional) into host memory */
+KIFI_API kifi_status kifi_proposer_gradients(kifi_proposer* pr, const float* targets_dev, int batch,
+                                             float* out_loss, float* out_grads_host);
+/* kifi_proposer_gradients followed by one Adam step (beta 0.9 / 0.999) */
+KIFI_API kifi_status kifi_proposer_train_step(kifi_proposer* pr, const float* targets_dev, int batch,
+                                              float lr, float* out_loss);
+
 /* ------------------------------------------------------------ pipeline */
 
 /* Arguments of kifi::Pipeline::Pipeline(cameraParams, volumeResolution,

@@ -79,6 +79,18 @@ SIGNATURES = {
                                   C.c_int, C.POINTER(C.c_int)]),
     "kifi_gemm_bf16": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
                                  C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]),
+    "kifi_proposer_create": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
+    "kifi_proposer_destroy": (C.c_int, [C.c_void_p]),
+    "kifi_proposer_param_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_size_t)]),
+    "kifi_proposer_set_params": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "kifi_proposer_get_params": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "kifi_proposer_make_input": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int,
+                                           C.c_void_p]),
+    "kifi_proposer_set_inputs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    "kifi_proposer_get_inputs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
+    "kifi_proposer_predict": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "kifi_proposer_gradients": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "kifi_proposer_train_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_float, C.c_void_p]),
     "kifi_pipeline_set_graphs": (C.c_int, [C.c_void_p, C.c_int]),
     "kifi_pipeline_graph_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
     "kifi_depthstream_open": (C.c_int, [C.c_char_p, C.POINTER(C.c_void_p)]),

@@ -1,0 +1,99 @@
+"""The learned pose proposer on the GPU (tcgen05 GEMMs, BF16 weights and
+activations, FP32 accumulation) against its CPU oracle (oracle/proposer.py,
+float64 with BF16 rounding at the same points)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _inputs(b, seed):
+    import torch
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(0.4, 4.0, (b, 60, 80, 2)).astype(np.float16)
+    x[rng.uniform(size=x.shape) < 0.1] = 0
+    return x, torch.from_numpy(x).cuda()
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+
+
+def test_param_layout_roundtrip(gpu):
+    from merge_fusion_gb300 import proposer as mp
+    from oracle import proposer as op
+    pr = mp.PoseProposer(max_batch=16)
+    _, total = op.layout()
+    assert pr.n_params == total
+    p = mp.init_params(3)
+    assert np.array_equal(p, op.init_params(3))
+    pr.set_params(p)
+    assert np.array_equal(pr.get_params(), p)
+
+
+def test_forward_and_gradients_match_oracle(gpu):
+    import torch
+    from merge_fusion_gb300 import proposer as mp
+    from oracle import proposer as op
+    b = 16
+    pr = mp.PoseProposer(max_batch=32)
+    rng = np.random.default_rng(5)
+    p = mp.init_params(5)
+    p = (p + 0.02 * rng.normal(size=p.shape).astype(np.float32) * op.trainable_mask()).astype(np.float32)
+    pr.set_params(p)
+    x, xd = _inputs(b, 6)
+    t = rng.normal(size=(b, 6)).astype(np.float32)
+    out, cache = op.forward(p.astype(np.float64), x.astype(np.float64), quantize=True)
+    loss_o, g_o = op.backward(cache, t)
+    pred = pr.predict(xd)
+    assert _rel(pred, out[:, :6]) < 2e-3, _rel(pred, out[:, :6])
+    loss, g = pr.gradients(xd, torch.from_numpy(t).cuda())
+    assert abs(loss - loss_o) <= 2e-3 * loss_o, (loss, loss_o)
+    lay, _ = op.layout()
+    for i, (off, shp) in enumerate(lay):
+        n = int(np.prod(shp))
+        r = _rel(g[off:off + n], g_o[off:off + n])
+        assert r < 2e-2, (i, r)
+    assert np.all(g[~op.trainable_mask()] == 0)
+
+
+def test_make_input_is_the_box_mean(gpu):
+    import torch
+    from merge_fusion_gb300 import proposer as mp
+    pr = mp.PoseProposer(max_batch=8)
+    rng = np.random.default_rng(2)
+    da = rng.integers(0, 4000, (480, 640)).astype(np.uint16)
+    db = rng.integers(0, 4000, (480, 640)).astype(np.uint16)
+    da[rng.uniform(size=da.shape) < 0.3] = 0
+    db[:8, :8] = 0  # a block with no depth
+    ta, tb = (torch.from_numpy(d.view(np.int16)).cuda() for d in (da, db))
+    out = torch.zeros((60, 80, 2), dtype=torch.float16, device="cuda")
+    pr.make_input(ta.data_ptr(), tb.data_ptr(), True, 640, 480, out.data_ptr())
+    got = out.cpu().numpy().astype(np.float32)
+    for f, d in enumerate((da, db)):
+        z = (d.astype(np.float32) * np.float32(0.001)).reshape(60, 8, 80, 8)
+        cnt = (z > 0).sum(axis=(1, 3))
+        want = np.where(cnt > 0, z.sum(axis=(1, 3)) / np.maximum(cnt, 1), 0).astype(np.float16)
+        assert np.abs(got[..., f] - want.astype(np.float32)).max() <= 2e-3
+    assert got[0, 0, 1] == 0
+
+
+def test_training_reduces_loss(gpu):
+    import torch
+    from merge_fusion_gb300 import proposer as mp
+    pr = mp.PoseProposer(max_batch=64)
+    pr.set_params(mp.init_params(0))
+    x, xd = _inputs(64, 9)
+    # a learnable target: smooth functions of the two frames' depth statistics
+    m = x.astype(np.float32).reshape(64, -1, 2)
+    t = np.stack([m[:, :, 0].mean(1), m[:, :, 1].mean(1), m[:, :2400, 0].mean(1) - m[:, 2400:, 0].mean(1),
+                  m[:, :, 0].std(1), m[:, :, 1].std(1), m[:, :, 0].mean(1) - m[:, :, 1].mean(1)], 1)
+    t = ((t - t.mean(0)) / (t.std(0) + 1e-6)).astype(np.float32)
+    td = torch.from_numpy(t).cuda()
+    first = pr.train_step(xd, td, 1e-3)
+    for _ in range(150):
+        last = pr.train_step(xd, td, 1e-3)
+    assert last < 0.3 * first, (first, last)
+    p = pr.get_params()
+    from oracle import proposer as op
+    assert np.all(p[~op.trainable_mask()] == 0)
