@@ -184,7 +184,7 @@ def iterations_to_converge(rms, tol=1e-4):
     return len(rms)
 
 
-def make_pairs(proposer, seeds, frames_per_traj, steps=(1, 2, 3), icp_iters=20, device="cuda"):
+def make_pairs(proposer, seeds, frames_per_traj, steps=(1, 2, 3), icp_iters=40, device="cuda"):
     """Inputs [N, 60, 80, 2] FP16 on the device, labels [N, 6] (relative pose
     vectors from converged plain ICP) and per-pair (seed, a, b, pose a)."""
     import torch
@@ -231,13 +231,14 @@ def train(proposer, x, y, steps=3000, batch=256, lr=1e-3, seed=0, log_every=250)
     return mean, std, hist
 
 
-def evaluate(proposer, mean, std, seeds, frames_per_traj, steps=(1, 2, 3), icp_iters=20, max_pairs=1000,
+def evaluate(proposer, mean, std, seeds, frames_per_traj, steps=(1, 2, 3), icp_iters=60, max_pairs=1000,
              device="cuda"):
     """Plain vs learned-warm-started ICP on held-out trajectories: iterations
     to converge (RMS change < 1e-4 m), the final pose difference, fallbacks."""
     import torch
     icp = _Icp()
-    it_plain, it_learned, diffs, fallbacks, n = [], [], [], 0, 0
+    it_plain, it_learned, diffs, spread, fallbacks, n = [], [], [], [], 0, 0
+    rng = np.random.default_rng(12345)
     try:
         for seed in seeds:
             frames, poses = scenes.render_room_torch(frames_per_traj, seed=seed, device=device)
@@ -257,6 +258,11 @@ def evaluate(proposer, mean, std, seeds, frames_per_traj, steps=(1, 2, 3), icp_i
                     icp.set_target(frames[a].data_ptr(), e2w[a])
                     Tp, _, rp = icp.align(frames[b].data_ptr(), e2w[a], icp_iters)
                     Tl, _, rl = icp.align(frames[b].data_ptr(), warm, icp_iters)
+                    # the method's own spread: plain ICP from a start moved by 1 mm / 0.05 deg
+                    jig = vec_to_pose(np.concatenate([rng.normal(size=3) * (8.7e-4 / math.sqrt(3)),
+                                                      rng.normal(size=3) * (1e-3 / math.sqrt(3))]))
+                    Tj, _, _ = icp.align(frames[b].data_ptr(), scenes.kifi_matrix(guess @ jig), icp_iters)
+                    spread.append(float(np.abs(Tj - Tp).max()))
                     kp, kl = iterations_to_converge(rp), iterations_to_converge(rl)
                     if rl[-1] > 1.5 * rp[-1]:  # fallback to the plain result
                         fallbacks += 1
@@ -270,11 +276,15 @@ def evaluate(proposer, mean, std, seeds, frames_per_traj, steps=(1, 2, 3), icp_i
                 break
     finally:
         icp.close()
+    diffs = np.asarray(diffs)
     return {"pairs": n, "plain_iterations": float(np.mean(it_plain)),
             "learned_iterations": float(np.mean(it_learned)),
             "ratio": float(np.mean(it_learned) / max(np.mean(it_plain), 1e-12)),
-            "fallbacks": fallbacks, "max_pose_diff": float(np.max(diffs)),
-            "p99_pose_diff": float(np.quantile(diffs, 0.99))}
+            "fallbacks": fallbacks, "max_pose_diff": float(diffs.max()),
+            "median_pose_diff": float(np.median(diffs)),
+            "same_pose_1e-5": float((diffs <= 1e-5).mean()),
+            "plain_spread_median": float(np.median(spread)), "plain_spread_max": float(np.max(spread)),
+            "icp_iterations_run": icp_iters}
 
 
 def save(path, params, mean, std, info):
