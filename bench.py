@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0,
                     help="bounded CPU-baseline sample (seconds of CPU work)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-vs-plain ICP measurement")
     ap.add_argument("--graphs", action="store_true",
                     help="one CUDA graph per frame (kifi_pipeline_set_graphs) instead of plain launches")
     return ap.parse_args()
@@ -368,6 +369,8 @@ def run_gpu(args, rank, world, local):
                                           "over 10 frames; single-threaded, as the reference is"
                                           % (nfr, tmesh)}
     lib.kifi_pipeline_destroy(pipe)
+    if not args.no_learned:
+        line["icp_iterations"] = learned_vs_plain()
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
@@ -376,6 +379,26 @@ def run_gpu(args, rank, world, local):
 # ------------------------------------------------------------ reference arm
 
 REF_MAX_TIMED_FRAMES = 12  # about 16 s of the reference's single-threaded CPU work
+
+
+def learned_vs_plain():
+    """ICP iterations to converge (RMS change < 1e-4 m) with the learned warm
+    start vs plain identity-initialised ICP, on held-out room trajectories
+    (seeds the training never saw), with the trained weights in the repo."""
+    from merge_fusion_gb300 import proposer as mp
+    path = os.path.join(ROOT, "merge_fusion_gb300", "weights", "proposer_room.npz")
+    if not os.path.exists(path):
+        return None
+    net = mp.PoseProposer(max_batch=8)
+    params, mean, std = mp.load(path)
+    net.set_params(params)
+    seeds = [SEED + 21000, SEED + 21001]
+    res = mp.evaluate(net, mean, std, seeds, 40, max_pairs=96)
+    net.close()
+    return {"plain": res["plain_iterations"], "learned": res["learned_iterations"], "ratio": res["ratio"],
+            "pairs": res["pairs"], "fallbacks": res["fallbacks"], "criterion": "RMS change < 1e-4 m",
+            "held_out": "room trajectories %d-%d, pairs (a, a+k), k = 1..3" % (seeds[0], seeds[-1]),
+            "median_pose_diff": res["median_pose_diff"], "plain_spread_median": res["plain_spread_median"]}
 
 
 def run_reference(args, rank, world):
