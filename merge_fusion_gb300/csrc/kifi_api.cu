@@ -525,8 +525,10 @@ static kifi_status mesh_to_device(kifi_volume* v, int with_indices, size_t* n_ve
     if (n >= ((size_t)1 << 28)) return fail(KIFI_ERR_UNSUPPORTED, "mesh of more than 2^28 voxels");
     const unsigned int cur = v->ctl_host->cur;
     KIFI_CUDA(mesh_scratch_reserve(&v->ms, n));
-    KIFI_CUDA(mesh_count_enqueue(v->vb.keys[cur], v->vb.vals[cur], n, with_indices ? 1 : 0, v->ms,
-                                 v->ls.sms, v->stream));
+    const unsigned int n32 = (unsigned int)n;
+    KIFI_CUDA(cudaMemcpyAsync(v->ms.n_dev, &n32, sizeof n32, cudaMemcpyHostToDevice, v->stream));
+    KIFI_CUDA(mesh_count_enqueue(v->vb.keys[cur], v->vb.vals[cur], n, with_indices ? 1 : 0, v->ms, v->ls.sms,
+                                 v->stream));
     MeshCounts* mc = &v->ctl_host_mesh;
     KIFI_CUDA(cudaMemcpyAsync(mc, v->ms.counts, sizeof(MeshCounts), cudaMemcpyDeviceToHost,
                               v->stream));
@@ -546,18 +548,8 @@ static kifi_status mesh_to_device(kifi_volume* v, int with_indices, size_t* n_ve
         KIFI_CUDA(cudaMalloc(&v->mesh_idx, (ni + kPad) * 4));
         v->mesh_idx_cap = ni;
     }
-    KIFI_CUDA(mesh_emit_enqueue(v->g, v->vb.keys[cur], v->vb.vals[cur], n, with_indices ? 1 : 0,
-                                v->ms, nv, ni, 0xffffffffu, v->mesh_verts, v->mesh_idx, v->ls.sms,
-                                v->stream));
-    if (with_indices) {
-        KIFI_CUDA(cudaMemcpyAsync(&mc->missing_min, &v->ms.counts->missing_min, 4,
-                                  cudaMemcpyDeviceToHost, v->stream));
-        KIFI_CUDA(cudaStreamSynchronize(v->stream));
-        if (mc->missing_min != 0xffffffffu)
-            KIFI_CUDA(mesh_emit_enqueue(v->g, v->vb.keys[cur], v->vb.vals[cur], n, 1, v->ms, nv, ni,
-                                        mc->missing_min, v->mesh_verts, v->mesh_idx, v->ls.sms,
-                                        v->stream));
-    }
+    KIFI_CUDA(mesh_emit_enqueue(v->g, v->vb.keys[cur], v->vb.vals[cur], n, with_indices ? 1 : 0, v->ms, nv, ni,
+                                v->mesh_verts, v->mesh_idx, v->ls.sms, v->stream));
     *n_verts = nv;
     *n_indices = ni;
     v->mesh_counts_valid = true;

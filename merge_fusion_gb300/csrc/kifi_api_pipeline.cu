@@ -18,6 +18,15 @@
 // instantiated graph with cudaGraphExecUpdate, and it is launched as one
 // unit.  A frame whose captured topology differs (the first tracked frame,
 // a grown volume) instantiates anew.  Meshing stays outside the graph.
+//
+// Meshing every N frames never blocks the host: on a mesh frame a third
+// stream waits for that frame's fusion, copies the resident voxels into a
+// snapshot (count and buffer read on the device) and runs the counting
+// passes; the volume stream only waits for the copy before fusing the next
+// frame.  Later pipeline calls poll the counts without blocking and, once
+// they are in, size the outputs (stream-ordered allocation) and enqueue the
+// vertex/index emission on the mesh stream.  kifi_pipeline_mesh_counts waits
+// for the latest mesh.
 #include <cstring>
 #include <new>
 
@@ -40,6 +49,18 @@ struct kifi_pipeline {
     bool have_prev = false;
     size_t mesh_verts = 0, mesh_indices = 0;
     bool graphs = false;
+    // asynchronous meshing
+    cudaStream_t ms = nullptr;
+    MeshScratch mscr{};
+    uint32_t* snap_keys = nullptr;
+    float2* snap_vals = nullptr;
+    size_t snap_cap = 0, snap_n = 0;
+    float* mverts = nullptr;
+    uint32_t* midx = nullptr;
+    size_t mverts_cap = 0, midx_cap = 0;
+    MeshCounts* counts_host = nullptr;  // page-locked
+    cudaEvent_t frame_done = nullptr, snap_done = nullptr, counts_ready = nullptr;
+    bool counting = false;
     cudaGraphExec_t exec = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr, after = nullptr;
     long long graph_builds = 0, graph_updates = 0;
@@ -47,10 +68,82 @@ struct kifi_pipeline {
 
 namespace {
 
+// counts of the snapshot in: size the outputs and enqueue the emission
+kifi_status mesh_emit(kifi_pipeline* p) {
+    const MeshCounts& c = *p->counts_host;
+    const size_t nv = (size_t)c.n_verts, ni = p->desc.mesh_with_indices ? (size_t)c.n_idx : 0;
+    if (nv + kPad > p->mverts_cap) {
+        if (p->mverts) KIFI_CUDA(cudaFreeAsync(p->mverts, p->ms));
+        p->mverts_cap = (nv + kPad) + (nv + kPad) / 4;
+        KIFI_CUDA(cudaMallocAsync((void**)&p->mverts, p->mverts_cap * 12, p->ms));
+    }
+    if (ni + kPad > p->midx_cap) {
+        if (p->midx) KIFI_CUDA(cudaFreeAsync(p->midx, p->ms));
+        p->midx_cap = (ni + kPad) + (ni + kPad) / 4;
+        KIFI_CUDA(cudaMallocAsync((void**)&p->midx, p->midx_cap * 4, p->ms));
+    }
+    KIFI_CUDA(mesh_emit_enqueue(p->vol->g, p->snap_keys, p->snap_vals, p->snap_n, p->desc.mesh_with_indices,
+                                p->mscr, nv, ni, p->mverts, p->midx, p->vol->ls.sms, p->ms));
+    p->mesh_verts = nv;
+    p->mesh_indices = ni;
+    p->counting = false;
+    return KIFI_OK;
+}
+
+// a mesh whose counts are in gets its emission; with `wait`, wait for them
+kifi_status mesh_poll(kifi_pipeline* p, bool wait) {
+    if (!p->counting) return KIFI_OK;
+    if (wait) {
+        KIFI_CUDA(cudaEventSynchronize(p->counts_ready));
+    } else {
+        const cudaError_t q = cudaEventQuery(p->counts_ready);
+        if (q == cudaErrorNotReady) return KIFI_OK;
+        if (q != cudaSuccess) return cuda_fail(q, "mesh counts");
+    }
+    return mesh_emit(p);
+}
+
+// snapshot + counting passes of the volume as of the frame just enqueued
+kifi_status mesh_begin(kifi_pipeline* p) {
+    kifi_status s = mesh_poll(p, true);  // one mesh at a time
+    if (s) return s;
+    kifi_volume* v = p->vol;
+    if (p->snap_cap < v->vb.cap) {
+        KIFI_CUDA(cudaStreamSynchronize(p->ms));
+        cudaFree(p->snap_keys);
+        cudaFree(p->snap_vals);
+        p->snap_keys = nullptr;
+        p->snap_vals = nullptr;
+        p->snap_cap = 0;
+        KIFI_CUDA(cudaMalloc(&p->snap_keys, (v->vb.cap + kPad) * 4));
+        KIFI_CUDA(cudaMalloc(&p->snap_vals, (v->vb.cap + kPad) * 8));
+        p->snap_cap = v->vb.cap;
+    }
+    // the passes' grids cover the host's upper bound of the voxel count
+    p->snap_n = v->n_upper < p->snap_cap ? v->n_upper : p->snap_cap;
+    if (p->mscr.cap < p->snap_n) {  // with headroom: freeing scratch waits for the device
+        const size_t want = p->snap_n + p->snap_n / 4;
+        KIFI_CUDA(mesh_scratch_reserve(&p->mscr, want < p->snap_cap ? want : p->snap_cap));
+    }
+    KIFI_CUDA(cudaEventRecord(p->frame_done, p->vs));
+    KIFI_CUDA(cudaStreamWaitEvent(p->ms, p->frame_done, 0));
+    KIFI_CUDA(mesh_snapshot_enqueue(v->ctl, v->vb, p->snap_keys, p->snap_vals, p->snap_n, p->mscr.n_dev, v->ls.sms,
+                                    p->ms));
+    KIFI_CUDA(cudaEventRecord(p->snap_done, p->ms));
+    KIFI_CUDA(cudaStreamWaitEvent(p->vs, p->snap_done, 0));  // fusion may overwrite the buffers after the copy
+    KIFI_CUDA(mesh_count_enqueue(p->snap_keys, p->snap_vals, p->snap_n, p->desc.mesh_with_indices, p->mscr,
+                                 v->ls.sms, p->ms));
+    KIFI_CUDA(cudaMemcpyAsync(p->counts_host, p->mscr.counts, sizeof(MeshCounts), cudaMemcpyDeviceToHost, p->ms));
+    KIFI_CUDA(cudaEventRecord(p->counts_ready, p->ms));
+    p->counting = true;
+    return KIFI_OK;
+}
+
 kifi_status track_and_fuse(kifi_pipeline* p, const void* depth_dev, bool u16, int k,
                            const float* world_to_eye) {
     const kifi_camera& cam = p->desc.camera;
-    kifi_status s;
+    kifi_status s = mesh_poll(p, false);
+    if (s) return s;
     // fusion on the volume's stream
     if ((s = kifi_integrate_device(p->vol, depth_dev, u16 ? 1 : 0, &cam, world_to_eye))) return s;
     // tracking on the ICP stream, once the frame is on the device
@@ -69,11 +162,7 @@ kifi_status track_and_fuse(kifi_pipeline* p, const void* depth_dev, bool u16, in
     std::memcpy(p->prev_e2w, e2w.m, 64);
     p->have_prev = true;
     ++p->frame;
-    if (p->desc.mesh_every > 0 && p->frame % p->desc.mesh_every == 0) {
-        if ((s = kifi_mesh_device(p->vol, p->desc.mesh_with_indices, &p->mesh_verts,
-                                  &p->mesh_indices, nullptr, nullptr)))
-            return s;
-    }
+    if (p->desc.mesh_every > 0 && p->frame % p->desc.mesh_every == 0 && (s = mesh_begin(p))) return s;
     return KIFI_OK;
 }
 
@@ -83,8 +172,9 @@ kifi_status frame_graph(kifi_pipeline* p, const void* host_src, size_t bytes, co
                         const float* world_to_eye) {
     const kifi_camera& cam = p->desc.camera;
     const bool track = p->desc.icp_iterations > 0;
-    kifi_status s = kifi_volume_prepare_frame(p->vol, &cam);
+    kifi_status s = mesh_poll(p, false);
     if (s) return s;
+    if ((s = kifi_volume_prepare_frame(p->vol, &cam))) return s;
     if (track && (s = kifi_icp_prepare_frame(p->icp, &cam))) return s;
     const Mat4 e2w = invert_transform(load_mat(world_to_eye));
     // stage timer events cannot be waited on once captured: none in the graph
@@ -136,11 +226,7 @@ kifi_status frame_graph(kifi_pipeline* p, const void* host_src, size_t bytes, co
     std::memcpy(p->prev_e2w, e2w.m, 64);
     p->have_prev = true;
     ++p->frame;
-    if (p->desc.mesh_every > 0 && p->frame % p->desc.mesh_every == 0) {
-        if ((s = kifi_mesh_device(p->vol, p->desc.mesh_with_indices, &p->mesh_verts, &p->mesh_indices,
-                                  nullptr, nullptr)))
-            return s;
-    }
+    if (p->desc.mesh_every > 0 && p->frame % p->desc.mesh_every == 0 && (s = mesh_begin(p))) return s;
     return KIFI_OK;
 }
 
@@ -178,6 +264,11 @@ kifi_status kifi_pipeline_create(const kifi_pipeline_desc* d, kifi_pipeline** ou
     }
     if (!e) e = cudaEventCreateWithFlags(&p->fused, cudaEventDisableTiming);
     if (!e) e = cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming);
+    if (!e) e = cudaStreamCreateWithFlags(&p->ms, cudaStreamNonBlocking);
+    if (!e) e = cudaEventCreateWithFlags(&p->frame_done, cudaEventDisableTiming);
+    if (!e) e = cudaEventCreateWithFlags(&p->snap_done, cudaEventDisableTiming);
+    if (!e) e = cudaEventCreateWithFlags(&p->counts_ready, cudaEventDisableTiming);
+    if (!e) e = cudaHostAlloc((void**)&p->counts_host, sizeof(MeshCounts), cudaHostAllocDefault);
     if (!e) e = cudaEventCreateWithFlags(&p->join, cudaEventDisableTiming);
     if (!e) e = cudaEventCreateWithFlags(&p->after, cudaEventDisableTiming);
     if (e) {
@@ -202,6 +293,20 @@ kifi_status kifi_pipeline_destroy(kifi_pipeline* p) {
     if (p->join) cudaEventDestroy(p->join);
     if (p->after) cudaEventDestroy(p->after);
     if (p->exec) cudaGraphExecDestroy(p->exec);
+    if (p->ms) {
+        cudaStreamSynchronize(p->ms);
+        if (p->mverts) cudaFreeAsync(p->mverts, p->ms);
+        if (p->midx) cudaFreeAsync(p->midx, p->ms);
+        cudaStreamSynchronize(p->ms);
+        cudaStreamDestroy(p->ms);
+    }
+    mesh_scratch_free(&p->mscr);
+    cudaFree(p->snap_keys);
+    cudaFree(p->snap_vals);
+    if (p->counts_host) cudaFreeHost(p->counts_host);
+    if (p->frame_done) cudaEventDestroy(p->frame_done);
+    if (p->snap_done) cudaEventDestroy(p->snap_done);
+    if (p->counts_ready) cudaEventDestroy(p->counts_ready);
     kifi_icp_destroy(p->icp);
     kifi_volume_destroy(p->vol);
     delete p;
@@ -286,6 +391,10 @@ kifi_status kifi_pipeline_graph_stats(kifi_pipeline* p, long long* instantiated,
 
 kifi_status kifi_pipeline_mesh_counts(kifi_pipeline* p, size_t* n_verts, size_t* n_indices) {
     if (!p || !n_verts || !n_indices) return fail(KIFI_ERR_INVALID_ARGUMENT, "null argument");
+    KIFI_CUDA(cudaSetDevice(p->desc.device));
+    kifi_status s = mesh_poll(p, true);
+    if (s) return s;
+    KIFI_CUDA(cudaStreamSynchronize(p->ms));
     *n_verts = p->mesh_verts;
     *n_indices = p->mesh_indices;
     return KIFI_OK;

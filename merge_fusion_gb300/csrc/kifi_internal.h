@@ -85,17 +85,20 @@ struct MeshScratch {
     unsigned long long* block_sums = nullptr;
     unsigned int* rows = nullptr;          // start index of each (z, y) key row
     MeshCounts* counts = nullptr;
+    unsigned int* n_dev = nullptr;         // the voxel count the passes read
     size_t cap = 0;
 };
 
 cudaError_t mesh_scratch_reserve(MeshScratch* m, size_t n);
 void mesh_scratch_free(MeshScratch* m);
-cudaError_t mesh_count_enqueue(const uint32_t* keys, const float2* vals, size_t n,
-                               int with_indices, MeshScratch& ms, int sms, cudaStream_t st);
-cudaError_t mesh_emit_enqueue(const Geom& g, const uint32_t* keys, const float2* vals, size_t n,
+cudaError_t mesh_count_enqueue(const uint32_t* keys, const float2* vals, size_t n_cap, int with_indices,
+                               MeshScratch& ms, int sms, cudaStream_t st);
+cudaError_t mesh_emit_enqueue(const Geom& g, const uint32_t* keys, const float2* vals, size_t n_cap,
                               int with_indices, MeshScratch& ms, unsigned long long n_verts,
-                              unsigned long long n_idx, unsigned int missing_bound, float* verts_dev,
-                              uint32_t* idx_dev, int sms, cudaStream_t st);
+                              unsigned long long n_idx, float* verts_dev, uint32_t* idx_dev, int sms,
+                              cudaStream_t st);
+cudaError_t mesh_snapshot_enqueue(const DeviceCtl* ctl, const VolumeBuffers& vb, uint32_t* keys, float2* vals,
+                                  size_t cap, unsigned int* n_dev, int sms, cudaStream_t st);
 
 // ------------------------------------------------------------------ ICP
 constexpr int kIcpMaxStats = 64;

@@ -50,8 +50,9 @@ __device__ __forceinline__ unsigned long long lower_bound_u32(const uint32_t* __
 }
 
 // row_start[r] = first index whose key >> 10 >= r, for r in [0, 2^20]
-__global__ void k_row_directory(const uint32_t* __restrict__ keys, unsigned long long n,
+__global__ void k_row_directory(const uint32_t* __restrict__ keys, const unsigned int* __restrict__ n_dev,
                                 unsigned int* __restrict__ row_start) {
+    const unsigned long long n = *n_dev;
     for (unsigned int r = blockIdx.x * blockDim.x + threadIdx.x; r <= kRows;
          r += gridDim.x * blockDim.x)
         row_start[r] = (unsigned int)lower_bound_u32(keys, n, r << 10);
@@ -147,9 +148,10 @@ template <bool kTris>
 __global__ void __launch_bounds__(kThreads) k_mesh_classify(const uint32_t* __restrict__ keys,
                                                             const float2* __restrict__ vals,
                                                             const unsigned int* __restrict__ rs,
-                                                            unsigned int n,
+                                                            const unsigned int* __restrict__ n_dev,
                                                             unsigned int* __restrict__ flags,
                                                             unsigned long long* __restrict__ counts) {
+    const unsigned int n = *n_dev;
     for (unsigned int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
         unsigned int f = 0, nv = 0, ni = 0;
         if (i + 1 < n && vals[i].y != 0.0f) {
@@ -182,15 +184,23 @@ template <bool kTris>
 __global__ void __launch_bounds__(kThreads) k_mesh_emit(const uint32_t* __restrict__ keys,
                                                         const float2* __restrict__ vals,
                                                         const unsigned int* __restrict__ rs,
-                                                        unsigned int n, Geom g,
+                                                        const unsigned int* __restrict__ n_dev, Geom g,
                                                         const unsigned int* __restrict__ flags,
                                                         const unsigned long long* __restrict__ scan,
                                                         unsigned long long n_verts,
                                                         unsigned long long n_idx,
                                                         unsigned int missing_bound,
+                                                        const unsigned int* __restrict__ missing_bound_dev,
                                                         float* __restrict__ verts,
                                                         uint32_t* __restrict__ idx,
                                                         unsigned int* __restrict__ missing_min) {
+    const unsigned int n = *n_dev;
+    // a re-run for the index mapping's stop rule takes its bound from the first run, and only
+    // when that run found a missing vertex
+    if (missing_bound_dev) {
+        missing_bound = *missing_bound_dev;
+        if (missing_bound == 0xffffffffu) return;
+    }
     for (unsigned int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
         const unsigned int f = flags[i];
         if (f == 0) continue;
@@ -248,7 +258,7 @@ __global__ void __launch_bounds__(kThreads) k_mesh_emit(const uint32_t* __restri
             if (id >= missing_bound) outv = id;
             idx[first + t] = outv;
         }
-        if (local_min != 0xffffffffu) atomicMin(missing_min, local_min);
+        if (local_min != 0xffffffffu && missing_min) atomicMin(missing_min, local_min);
     }
 }
 
@@ -284,7 +294,8 @@ __device__ __forceinline__ unsigned long long block_exclusive_scan(unsigned long
 __global__ void __launch_bounds__(kThreads) k_scan_tiles(const unsigned long long* __restrict__ in,
                                                          unsigned long long* __restrict__ out,
                                                          unsigned long long* __restrict__ tile_sums,
-                                                         unsigned int n) {
+                                                         const unsigned int* __restrict__ n_dev) {
+    const unsigned int n = *n_dev;
     const unsigned int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
     unsigned long long v[kScanItems], s = 0;
 #pragma unroll
@@ -305,7 +316,11 @@ __global__ void __launch_bounds__(kThreads) k_scan_tiles(const unsigned long lon
 // single CTA: exclusive scan of the tile sums, total to counts
 __global__ void __launch_bounds__(kThreads) k_scan_sums(unsigned long long* __restrict__ sums,
                                                         unsigned int n_tiles,
+                                                        const unsigned int* __restrict__ n_dev,
                                                         MeshCounts* __restrict__ counts) {
+    // only the tiles that hold voxels (the grid covers an upper bound)
+    const unsigned int used = (*n_dev + kScanTile - 1) / kScanTile;
+    if (used < n_tiles) n_tiles = used;
     unsigned long long carry = 0;
     for (unsigned int b = 0; b < n_tiles; b += kThreads) {
         const unsigned int i = b + threadIdx.x;
@@ -323,7 +338,8 @@ __global__ void __launch_bounds__(kThreads) k_scan_sums(unsigned long long* __re
 
 __global__ void __launch_bounds__(kThreads) k_scan_add(unsigned long long* __restrict__ out,
                                                        const unsigned long long* __restrict__ sums,
-                                                       unsigned int n) {
+                                                       const unsigned int* __restrict__ n_dev) {
+    const unsigned int n = *n_dev;
     const unsigned int base = blockIdx.x * kScanTile;
     const unsigned long long add = sums[blockIdx.x];
     for (int q = threadIdx.x; q < kScanTile; q += kThreads)
@@ -343,6 +359,7 @@ cudaError_t mesh_scratch_reserve(MeshScratch* m, size_t n) {
     if ((e = cudaMalloc(&m->block_sums, ((cap + kScanTile - 1) / kScanTile + 1) * 8))) return e;
     if ((e = cudaMalloc(&m->rows, (kRows + 1) * sizeof(unsigned int)))) return e;
     if ((e = cudaMalloc(&m->counts, sizeof(MeshCounts)))) return e;
+    if ((e = cudaMalloc(&m->n_dev, sizeof(unsigned int)))) return e;
     m->cap = cap;
     return cudaSuccess;
 }
@@ -354,6 +371,7 @@ void mesh_scratch_free(MeshScratch* m) {
     cudaFree(m->block_sums);
     cudaFree(m->rows);
     cudaFree(m->counts);
+    cudaFree(m->n_dev);
     *m = MeshScratch{};
 }
 
@@ -363,40 +381,71 @@ static int grid_for(size_t n, int sms) {
     return (int)(b < 1 ? 1 : (b > cap ? cap : b));
 }
 
-cudaError_t mesh_count_enqueue(const uint32_t* keys, const float2* vals, size_t n,
-                               int with_indices, MeshScratch& ms, int sms, cudaStream_t st) {
+// The voxel count is read on the device from ms.n_dev (<= n_cap, which sizes
+// the grids), so the passes can be enqueued before the count is known.
+cudaError_t mesh_count_enqueue(const uint32_t* keys, const float2* vals, size_t n_cap, int with_indices,
+                               MeshScratch& ms, int sms, cudaStream_t st) {
     // vscan holds the per-voxel packed counts, tscan their exclusive scan
     unsigned long long* cnt = ms.vscan;
     unsigned long long* scan = ms.tscan;
-    k_row_directory<<<grid_for(kRows + 1, sms), kThreads, 0, st>>>(keys, n, ms.rows);
+    k_row_directory<<<grid_for(kRows + 1, sms), kThreads, 0, st>>>(keys, ms.n_dev, ms.rows);
     if (with_indices)
-        k_mesh_classify<true><<<grid_for(n, sms), kThreads, 0, st>>>(keys, vals, ms.rows,
-                                                                      (unsigned int)n, ms.vflags, cnt);
+        k_mesh_classify<true><<<grid_for(n_cap, sms), kThreads, 0, st>>>(keys, vals, ms.rows, ms.n_dev, ms.vflags,
+                                                                          cnt);
     else
-        k_mesh_classify<false><<<grid_for(n, sms), kThreads, 0, st>>>(keys, vals, ms.rows,
-                                                                       (unsigned int)n, ms.vflags, cnt);
-    const unsigned int n_tiles = (unsigned int)((n + kScanTile - 1) / kScanTile);
-    k_scan_tiles<<<n_tiles ? n_tiles : 1, kThreads, 0, st>>>(cnt, scan, ms.block_sums,
-                                                             (unsigned int)n);
-    k_scan_sums<<<1, kThreads, 0, st>>>(ms.block_sums, n_tiles ? n_tiles : 1, ms.counts);
-    k_scan_add<<<n_tiles ? n_tiles : 1, kThreads, 0, st>>>(scan, ms.block_sums, (unsigned int)n);
+        k_mesh_classify<false><<<grid_for(n_cap, sms), kThreads, 0, st>>>(keys, vals, ms.rows, ms.n_dev, ms.vflags,
+                                                                           cnt);
+    const unsigned int n_tiles = (unsigned int)((n_cap + kScanTile - 1) / kScanTile);
+    k_scan_tiles<<<n_tiles ? n_tiles : 1, kThreads, 0, st>>>(cnt, scan, ms.block_sums, ms.n_dev);
+    k_scan_sums<<<1, kThreads, 0, st>>>(ms.block_sums, n_tiles ? n_tiles : 1, ms.n_dev, ms.counts);
+    k_scan_add<<<n_tiles ? n_tiles : 1, kThreads, 0, st>>>(scan, ms.block_sums, ms.n_dev);
     return cudaGetLastError();
 }
 
-cudaError_t mesh_emit_enqueue(const Geom& g, const uint32_t* keys, const float2* vals, size_t n,
+// Both emit passes: the first records the smallest edge id without a vertex
+// in ms.counts->missing_min; the second (the index mapping's stop rule)
+// re-emits with that bound and does nothing when the first found none.
+cudaError_t mesh_emit_enqueue(const Geom& g, const uint32_t* keys, const float2* vals, size_t n_cap,
                               int with_indices, MeshScratch& ms, unsigned long long n_verts,
-                              unsigned long long n_idx, unsigned int missing_bound, float* verts_dev,
-                              uint32_t* idx_dev, int sms, cudaStream_t st) {
+                              unsigned long long n_idx, float* verts_dev, uint32_t* idx_dev, int sms,
+                              cudaStream_t st) {
     const unsigned long long* scan = ms.tscan;
     unsigned int* mm = &ms.counts->missing_min;
-    if (with_indices)
-        k_mesh_emit<true><<<grid_for(n, sms), kThreads, 0, st>>>(
-            keys, vals, ms.rows, (unsigned int)n, g, ms.vflags, scan, n_verts, n_idx, missing_bound,
-            verts_dev, idx_dev, mm);
-    else
-        k_mesh_emit<false><<<grid_for(n, sms), kThreads, 0, st>>>(
-            keys, vals, ms.rows, (unsigned int)n, g, ms.vflags, scan, n_verts, n_idx, missing_bound,
-            verts_dev, idx_dev, mm);
+    if (with_indices) {
+        k_mesh_emit<true><<<grid_for(n_cap, sms), kThreads, 0, st>>>(keys, vals, ms.rows, ms.n_dev, g, ms.vflags,
+                                                                      scan, n_verts, n_idx, 0xffffffffu, nullptr,
+                                                                      verts_dev, idx_dev, mm);
+        k_mesh_emit<true><<<grid_for(n_cap, sms), kThreads, 0, st>>>(keys, vals, ms.rows, ms.n_dev, g, ms.vflags,
+                                                                      scan, n_verts, n_idx, 0u, mm, verts_dev,
+                                                                      idx_dev, nullptr);
+    } else {
+        k_mesh_emit<false><<<grid_for(n_cap, sms), kThreads, 0, st>>>(keys, vals, ms.rows, ms.n_dev, g, ms.vflags,
+                                                                       scan, n_verts, n_idx, 0xffffffffu, nullptr,
+                                                                       verts_dev, idx_dev, mm);
+    }
+    return cudaGetLastError();
+}
+
+// Copy of the resident voxels (buffer ctl->cur, ctl->n[cur] of them) for a
+// mesh that runs while fusion goes on; the count goes to *n_dev.
+__global__ void k_mesh_snapshot(const DeviceCtl* __restrict__ ctl, VolumeBuffers vb, uint32_t* __restrict__ keys,
+                                float2* __restrict__ vals, unsigned long long cap, unsigned int* __restrict__ n_dev) {
+    const unsigned int cur = ctl->cur;
+    unsigned long long n = ctl->n[cur];
+    if (n > cap) n = cap;
+    const uint32_t* sk = cur ? vb.keys[1] : vb.keys[0];
+    const float2* sv = cur ? vb.vals[1] : vb.vals[0];
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        keys[i] = __ldcs(sk + i);
+        vals[i] = __ldcs(sv + i);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *n_dev = (unsigned int)n;
+}
+
+cudaError_t mesh_snapshot_enqueue(const DeviceCtl* ctl, const VolumeBuffers& vb, uint32_t* keys, float2* vals,
+                                  size_t cap, unsigned int* n_dev, int sms, cudaStream_t st) {
+    k_mesh_snapshot<<<sms * 4, 256, 0, st>>>(ctl, vb, keys, vals, cap, n_dev);
     return cudaGetLastError();
 }
 
