@@ -53,6 +53,7 @@ def parse():
                     help="bounded CPU-baseline sample (seconds of CPU work)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-vs-plain ICP measurement")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
     ap.add_argument("--graphs", action="store_true",
                     help="one CUDA graph per frame (kifi_pipeline_set_graphs) instead of plain launches")
     return ap.parse_args()
@@ -244,6 +245,11 @@ def run_gpu(args, rank, world, local):
     for i in range(Fp + Wu):
         step_device(i)
     check(lib.kifi_pipeline_sync(pipe, None))
+    # launch shape of the fusion kernels, measured on the next frame (the volume is left unchanged)
+    tuned = np.zeros(3, np.int32)
+    if not args.no_autotune:
+        check(lib.kifi_volume_autotune(vol, C.c_void_p(frames[Fp + Wu].data_ptr()), 1, C.byref(cam),
+                                       ptr(w2e[Fp + Wu]), 1, ptr(tuned)), "autotune")
     n_resident = C.c_size_t()
     check(lib.kifi_volume_size(vol, C.byref(n_resident)))
 
@@ -358,6 +364,8 @@ def run_gpu(args, rank, world, local):
                 "d2h_bytes_per_step": 64 + 1024},
         "gpu_launches": gpu_launches,
         "graphs": {"on": bool(args.graphs), "instantiated": int(gb.value), "updated": int(gu.value)},
+        "autotune": None if args.no_autotune else {"splat_ctas": int(tuned[0]), "sort_ctas": int(tuned[1]),
+                                                   "merge_ctas": int(tuned[2])},
         "mesh": {"vertices": nv.value, "indices": ni.value},
     }
     line["clocks"] = clocks.summary()

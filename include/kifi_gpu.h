@@ -177,6 +177,18 @@ KIFI_API kifi_status kifi_mesh_device(kifi_volume* vol, int with_indices, size_t
 KIFI_API kifi_status kifi_volume_set_profiling(kifi_volume* vol, int on);
 KIFI_API kifi_status kifi_volume_stage_times(kifi_volume* vol, double out_ms[4], int* frames);
 
+/* No counterpart in the reference.  Picks the persistent CTA counts of the
+ * volume's splat+emit, sort and merge/update kernels by timing them on one
+ * frame (device memory) integrated from a snapshot of the volume, which is
+ * restored: the volume is unchanged and later results are identical for any
+ * choice.  The choice is cached per (GPU, resolution, frame size) for the
+ * process and, when the environment variable KIFI_AUTOTUNE_CACHE names a
+ * file, there; force != 0 re-measures.  out_ctas (may be NULL) receives the
+ * splat, sort and merge CTA counts. */
+KIFI_API kifi_status kifi_volume_autotune(kifi_volume* vol, const void* depth_dev, int depth_is_u16,
+                                          const kifi_camera* cam, const float world_to_eye[16], int force,
+                                          int out_ctas[3]);
+
 /* Sizes of the most recent merges (up to 64, oldest first): resident voxels
  * before, keys new to the volume, resident voxels after.  No reference
  * counterpart; it sizes the bytes each merge moves. */

@@ -166,6 +166,17 @@ class Volume:
     def stream(self):
         return _lib.load().kifi_volume_stream(self._h)
 
+    def autotune(self, depth_dev_ptr, depth_is_u16, camera_params, world_to_eye, force=False):
+        """Measures and sets the persistent CTA counts of the fusion kernels
+        on one device frame (kifi_volume_autotune); the volume is unchanged.
+        Returns {"splat": n, "sort": n, "merge": n}."""
+        cam = camera_params.camera()
+        m = as_kifi_matrix(world_to_eye)
+        out = np.zeros(3, np.int32)
+        check(_lib.load().kifi_volume_autotune(self._h, C.c_void_p(depth_dev_ptr), 1 if depth_is_u16 else 0,
+                                               C.byref(cam), _ptr(m), 1 if force else 0, _ptr(out)), "autotune")
+        return {"splat": int(out[0]), "sort": int(out[1]), "merge": int(out[2])}
+
     def save(self, path):
         """Checkpoint: geometry, keys and voxels (no reference counterpart)."""
         check(_lib.load().kifi_volume_save(self._h, os.fsencode(path)), "save")

@@ -1,0 +1,40 @@
+"""kifi_volume_autotune: tuning leaves the volume untouched, every tuned
+launch shape gives bit-identical results, and choices are cached."""
+import os
+
+import numpy as np
+import pytest
+
+from tests.helpers import cam_params
+
+pytestmark = pytest.mark.gpu
+
+
+def test_autotune_is_invisible_and_cached(gpu, golden, tmp_path):
+    import torch
+    from merge_fusion_gb300 import kifi
+    cache = tmp_path / "autotune.txt"
+    os.environ["KIFI_AUTOTUNE_CACHE"] = str(cache)
+    depth, view, cam = golden["depth"], golden["view"], golden["camera"]
+    params = cam_params(cam)
+    a = kifi.Volume(256, 2.0, 0.02)
+    b = kifi.Volume(256, 2.0, 0.02)
+    for v in (a, b):
+        kifi.Integrator().Integrate(v, depth, params, view)
+    shifted = view.copy()
+    shifted[12] += np.float32(0.013)
+    d = torch.from_numpy(np.ascontiguousarray(depth, np.float32)).cuda()
+    torch.cuda.synchronize()
+    k0, v0 = a.export()
+    shape = a.autotune(d.data_ptr(), False, params, shifted, force=True)
+    assert min(shape.values()) > 0
+    k1, v1 = a.export()
+    assert np.array_equal(k0, k1) and np.array_equal(v0.view(np.uint32), v1.view(np.uint32))
+    for v in (a, b):
+        kifi.Integrator().Integrate(v, depth, params, shifted)
+    ka, va = a.export()
+    kb, vb = b.export()
+    assert np.array_equal(ka, kb) and np.array_equal(va.view(np.uint32), vb.view(np.uint32))
+    # cached: the same choice without measuring, and written to the file
+    assert b.autotune(d.data_ptr(), False, params, shifted) == shape
+    assert cache.exists() and len(cache.read_text().split()) == 5
