@@ -75,6 +75,10 @@ typedef struct kifi_volume_desc {
     size_t initial_capacity; /* voxels to reserve up front; 0 = library default */
     int device;              /* CUDA device ordinal */
     void* stream;            /* cudaStream_t to run on, or NULL for a library-owned stream */
+    int key_bits;            /* 0: 32 up to 1024 voxels per axis, else 64; 32 or 64 to choose.
+                              * 32-bit keys are util::pack (math.h:442-457), z<<20|y<<10|x;
+                              * 64-bit keys are z<<2b|y<<b|x with b = max(10, log2 resolution),
+                              * so below 1024 voxels per axis both name a voxel alike. */
 } kifi_volume_desc;
 
 typedef struct kifi_volume kifi_volume;
@@ -105,12 +109,23 @@ KIFI_API kifi_status kifi_volume_size(kifi_volume* vol, size_t* n);
 KIFI_API kifi_status kifi_volume_export(kifi_volume* vol, uint32_t* keys, float* values, size_t capacity,
                                size_t* n);
 
+/* kifi_volume_export with 64-bit keys (any volume). */
+KIFI_API kifi_status kifi_volume_export64(kifi_volume* vol, uint64_t* keys, float* values, size_t capacity,
+                                          size_t* n);
+
+/* The volume's key width (32 or 64) and key bits per axis (b). */
+KIFI_API kifi_status kifi_volume_key_bits(kifi_volume* vol, int* key_bits, int* bits_per_axis);
+
 /* kifi::util::flat_map::insert (flat_map.h:164-197) on the volume's map:
  * the set union of the resident voxels with `keys` (sorted, unique), where
  * resident voxels keep their value.  values may be NULL for Voxel() = (0,0),
  * as Integrator::Integrate inserts (Integrator.cpp:60-63). */
 KIFI_API kifi_status kifi_volume_insert(kifi_volume* vol, const uint32_t* keys, const float* values,
                                size_t n);
+
+/* kifi_volume_insert with 64-bit keys (any volume). */
+KIFI_API kifi_status kifi_volume_insert64(kifi_volume* vol, const uint64_t* keys, const float* values,
+                                          size_t n);
 
 /* kifi::util::flat_map::clear (flat_map.h:157-162) */
 KIFI_API kifi_status kifi_volume_clear(kifi_volume* vol);
@@ -203,6 +218,11 @@ KIFI_API kifi_status kifi_radix_sort_u32(uint32_t* keys, size_t n);
 /* kifi::util::radix_sort(keys, keys_last, values, scratch)
  * (algorithm.h:93-134): stable sort of 32-bit keys carrying 32-bit values. */
 KIFI_API kifi_status kifi_radix_sort_pairs_u32(uint32_t* keys, uint32_t* values, size_t n);
+
+/* The same radix sort widened to 64-bit keys (eight 8-bit digit passes),
+ * the sort behind volumes with 64-bit keys. */
+KIFI_API kifi_status kifi_radix_sort_u64(uint64_t* keys, size_t n);
+KIFI_API kifi_status kifi_radix_sort_pairs_u64(uint64_t* keys, uint32_t* values, size_t n);
 
 /* No counterpart in the reference.  The radix sort of
  * kifi_radix_sort_pairs_u32 for callers that must not allocate device
@@ -395,6 +415,7 @@ typedef struct kifi_pipeline_desc {
     int mesh_with_indices;  /* Mesh(verts, indices) rather than Mesh(verts) */
     size_t initial_capacity;
     int device;
+    int key_bits;           /* as kifi_volume_desc::key_bits */
 } kifi_pipeline_desc;
 
 typedef struct kifi_pipeline kifi_pipeline;

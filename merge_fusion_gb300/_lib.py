@@ -33,13 +33,13 @@ class PipelineDesc(C.Structure):
     _fields_ = [("camera", Camera), ("resolution", C.c_int), ("side_length_m", C.c_float),
                 ("truncation_m", C.c_float), ("icp_iterations", C.c_int), ("mesh_every", C.c_int),
                 ("mesh_with_indices", C.c_int), ("initial_capacity", C.c_size_t),
-                ("device", C.c_int)]
+                ("device", C.c_int), ("key_bits", C.c_int)]
 
 
 class VolumeDesc(C.Structure):
     _fields_ = [("resolution", C.c_int), ("side_length_m", C.c_float),
                 ("truncation_m", C.c_float), ("initial_capacity", C.c_size_t),
-                ("device", C.c_int), ("stream", C.c_void_p)]
+                ("device", C.c_int), ("stream", C.c_void_p), ("key_bits", C.c_int)]
 
 
 # name -> (restype, argtypes); every exported symbol of include/kifi_gpu.h
@@ -53,6 +53,12 @@ SIGNATURES = {
     "kifi_volume_export": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t,
                                      C.POINTER(C.c_size_t)]),
     "kifi_volume_insert": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t]),
+    "kifi_volume_export64": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t,
+                                       C.POINTER(C.c_size_t)]),
+    "kifi_volume_insert64": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t]),
+    "kifi_volume_key_bits": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "kifi_radix_sort_u64": (C.c_int, [C.c_void_p, C.c_size_t]),
+    "kifi_radix_sort_pairs_u64": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "kifi_volume_clear": (C.c_int, [C.c_void_p]),
     "kifi_volume_reserve": (C.c_int, [C.c_void_p, C.c_size_t]),
     "kifi_volume_sync": (C.c_int, [C.c_void_p]),

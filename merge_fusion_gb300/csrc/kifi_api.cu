@@ -48,9 +48,14 @@ namespace {
 
 bool is_pow2(int x) { return x > 0 && !(x & (x - 1)); }
 
+// voxels per axis at most: 13-bit key fields, a 2^39-bit occupancy bitmap
+constexpr int kMaxResolution = 8192;
+
 }  // namespace
 
 namespace {
+
+size_t vb_key_bytes(const VolumeBuffers& vb) { return (size_t)vb.key_bytes; }
 
 void free_volume_buffers(VolumeBuffers& vb) {
     for (int i = 0; i < 2; ++i) {
@@ -63,7 +68,7 @@ void free_volume_buffers(VolumeBuffers& vb) {
     vb.splits = nullptr;
 }
 
-size_t split_count(size_t cap) { return cap / 2048 + 4; }
+size_t split_count(const VolumeBuffers& vb, size_t cap) { return merge_max_tiles(vb, cap) + 2; }
 
 // Reads the device control block (waits for the stream).
 kifi_status read_ctl(kifi_volume* v) {
@@ -99,19 +104,19 @@ kifi_status grow_volume(kifi_volume* v, size_t need) {
     }
     nb.splits = nullptr;
     for (int i = 0; i < 2; ++i) {
-        cudaError_t e1 = cudaMalloc(&nb.keys[i], (cap + kPad) * sizeof(uint32_t));
+        cudaError_t e1 = cudaMalloc(&nb.keys[i], (cap + kPad) * vb_key_bytes(v->vb));
         cudaError_t e2 = e1 ? e1 : cudaMalloc(&nb.vals[i], (cap + kPad) * sizeof(float2));
         if (e1 || e2) {
             free_volume_buffers(nb);
             return cuda_fail(e1 ? e1 : e2, "growing the volume");
         }
     }
-    cudaError_t es = cudaMalloc(&nb.splits, split_count(cap) * sizeof(unsigned long long));
+    cudaError_t es = cudaMalloc(&nb.splits, split_count(v->vb, cap) * sizeof(unsigned long long));
     if (es) {
         free_volume_buffers(nb);
         return cuda_fail(es, "growing the volume");
     }
-    KIFI_CUDA(cudaMemcpyAsync(nb.keys[cur], v->vb.keys[cur], n * sizeof(uint32_t),
+    KIFI_CUDA(cudaMemcpyAsync(nb.keys[cur], v->vb.keys[cur], n * vb_key_bytes(v->vb),
                               cudaMemcpyDeviceToDevice, v->stream));
     KIFI_CUDA(cudaMemcpyAsync(nb.vals[cur], v->vb.vals[cur], n * sizeof(float2),
                               cudaMemcpyDeviceToDevice, v->stream));
@@ -135,7 +140,7 @@ kifi_status reserve_new(kifi_volume* v, size_t n_new) {
     v->vb.new_keys = v->vb.new_idx = nullptr;
     v->vb.new_cap = 0;
     sort_scratch_free(&v->ss);
-    KIFI_CUDA(cudaMalloc(&v->vb.new_keys, (n_new + kPad) * sizeof(uint32_t)));
+    KIFI_CUDA(cudaMalloc(&v->vb.new_keys, (n_new + kPad) * vb_key_bytes(v->vb)));
     KIFI_CUDA(cudaMalloc(&v->vb.new_idx, (n_new + kPad) * sizeof(uint32_t)));
     KIFI_CUDA(sort_scratch_alloc(&v->ss, n_new));
     v->vb.new_cap = n_new;
@@ -275,9 +280,14 @@ kifi_status kifi_device_count(int* count) {
 kifi_status kifi_volume_create(const kifi_volume_desc* d, kifi_volume** out) {
     if (!d || !out) return fail(KIFI_ERR_INVALID_ARGUMENT, "null argument");
     *out = nullptr;
-    // Volume.cpp:22-26
-    if (!(d->resolution >= 2 && d->resolution <= 1024 && is_pow2(d->resolution)))
-        return fail(KIFI_ERR_INVALID_ARGUMENT, "resolution must be a power of two in [2, 1024]");
+    // Volume.cpp:22-26 (a power of two up to 1024 there: 30-bit keys); beyond
+    // 1024 voxels per axis the volume keys voxels with 64 bits
+    if (!(d->resolution >= 2 && d->resolution <= kMaxResolution && is_pow2(d->resolution)))
+        return fail(KIFI_ERR_INVALID_ARGUMENT, "resolution must be a power of two in [2, 8192]");
+    if (d->key_bits != 0 && d->key_bits != 32 && d->key_bits != 64)
+        return fail(KIFI_ERR_INVALID_ARGUMENT, "key_bits must be 0, 32 or 64");
+    if (d->key_bits == 32 && d->resolution > 1024)
+        return fail(KIFI_ERR_INVALID_ARGUMENT, "32-bit keys hold at most 1024 voxels per axis");
     if (!(d->side_length_m > 0.0f) || !(d->truncation_m > 0.0f))
         return fail(KIFI_ERR_INVALID_ARGUMENT, "side length and truncation must be > 0");
     int ndev = 0;
@@ -303,6 +313,14 @@ kifi_status kifi_volume_create(const kifi_volume_desc* d, kifi_volume** out) {
         v->own_stream = true;
     }
     v->g = make_geom(d->resolution, d->side_length_m, d->truncation_m);
+    if (d->key_bits == 64 || d->resolution > 1024) {
+        // b = max(10, log2 res): below 1024 voxels per axis the 64-bit key of a
+        // voxel is the number the 30-bit key would be
+        int b = 10;
+        while ((1 << b) < d->resolution) ++b;
+        v->g.kb = b;
+        v->vb.key_bytes = 8;
+    }
     if ((s = launch_shape(v->device, &v->ls))) return bail(s);
     cudaError_t e;
     if ((e = cudaMalloc(&v->ctl, sizeof(DeviceCtl)))) return bail(cuda_fail(e, "control block"));
@@ -316,12 +334,12 @@ kifi_status kifi_volume_create(const kifi_volume_desc* d, kifi_volume** out) {
     size_t cap = d->initial_capacity;
     if (cap == 0) cap = r * r * r < ((size_t)1 << 22) ? r * r * r : ((size_t)1 << 22);
     for (int i = 0; i < 2; ++i) {
-        if ((e = cudaMalloc(&v->vb.keys[i], (cap + kPad) * sizeof(uint32_t))))
+        if ((e = cudaMalloc(&v->vb.keys[i], (cap + kPad) * vb_key_bytes(v->vb))))
             return bail(cuda_fail(e, "volume keys"));
         if ((e = cudaMalloc(&v->vb.vals[i], (cap + kPad) * sizeof(float2))))
             return bail(cuda_fail(e, "volume values"));
     }
-    if ((e = cudaMalloc(&v->vb.splits, split_count(cap) * sizeof(unsigned long long))))
+    if ((e = cudaMalloc(&v->vb.splits, split_count(v->vb, cap) * sizeof(unsigned long long))))
         return bail(cuda_fail(e, "merge splits"));
     v->vb.cap = cap;
     if ((s = reserve_new(v, 8 * 640 * 480))) return bail(s);
@@ -370,9 +388,14 @@ kifi_status kifi_volume_size(kifi_volume* v, size_t* n) {
     return s;
 }
 
-kifi_status kifi_volume_export(kifi_volume* v, uint32_t* keys, float* values, size_t capacity,
+// Copies the resident keys to the host as `out_bytes`-wide numbers: a copy
+// when the widths agree, a narrowing through a host buffer when a 64-bit
+// volume's keys (b = 10) are read as 30-bit keys, a widening otherwise.
+static kifi_status export_keys(kifi_volume* v, void* keys, int out_bytes, float* values, size_t capacity,
                                size_t* n) {
     if (!v || !n) return fail(KIFI_ERR_INVALID_ARGUMENT, "null argument");
+    if (out_bytes == 4 && v->vb.key_bytes == 8 && v->g.kb != 10)
+        return fail(KIFI_ERR_UNSUPPORTED, "keys of this volume need 64 bits (kifi_volume_export64)");
     kifi_status s = kifi_volume_sync(v);
     if (s) return s;
     const size_t cnt = v->n_upper;
@@ -380,11 +403,39 @@ kifi_status kifi_volume_export(kifi_volume* v, uint32_t* keys, float* values, si
     if (cnt > capacity) return fail(KIFI_ERR_CAPACITY, "export buffer too small");
     if (cnt == 0) return KIFI_OK;
     const unsigned int cur = v->ctl_host->cur;
-    if (keys)
-        KIFI_CUDA(cudaMemcpyAsync(keys, v->vb.keys[cur], cnt * 4, cudaMemcpyDeviceToHost, v->stream));
+    std::vector<uint64_t> wide;
+    std::vector<uint32_t> narrow;
+    if (keys) {
+        if (out_bytes == v->vb.key_bytes) {
+            KIFI_CUDA(cudaMemcpyAsync(keys, v->vb.keys[cur], cnt * out_bytes, cudaMemcpyDeviceToHost, v->stream));
+        } else if (out_bytes == 4) {
+            wide.resize(cnt);
+            KIFI_CUDA(cudaMemcpyAsync(wide.data(), v->vb.keys[cur], cnt * 8, cudaMemcpyDeviceToHost, v->stream));
+        } else {
+            narrow.resize(cnt);
+            KIFI_CUDA(cudaMemcpyAsync(narrow.data(), v->vb.keys[cur], cnt * 4, cudaMemcpyDeviceToHost, v->stream));
+        }
+    }
     if (values)
         KIFI_CUDA(cudaMemcpyAsync(values, v->vb.vals[cur], cnt * 8, cudaMemcpyDeviceToHost, v->stream));
     KIFI_CUDA(cudaStreamSynchronize(v->stream));
+    for (size_t i = 0; i < wide.size(); ++i) ((uint32_t*)keys)[i] = (uint32_t)wide[i];
+    for (size_t i = 0; i < narrow.size(); ++i) ((uint64_t*)keys)[i] = narrow[i];
+    return KIFI_OK;
+}
+
+kifi_status kifi_volume_export(kifi_volume* v, uint32_t* keys, float* values, size_t capacity, size_t* n) {
+    return export_keys(v, keys, 4, values, capacity, n);
+}
+
+kifi_status kifi_volume_export64(kifi_volume* v, uint64_t* keys, float* values, size_t capacity, size_t* n) {
+    return export_keys(v, keys, 8, values, capacity, n);
+}
+
+kifi_status kifi_volume_key_bits(kifi_volume* v, int* key_bits, int* bits_per_axis) {
+    if (!v) return fail(KIFI_ERR_INVALID_ARGUMENT, "null volume");
+    if (key_bits) *key_bits = v->vb.key_bytes * 8;
+    if (bits_per_axis) *bits_per_axis = v->g.kb;
     return KIFI_OK;
 }
 
@@ -404,23 +455,41 @@ kifi_status kifi_volume_reserve(kifi_volume* v, size_t capacity) {
     return grow_volume(v, capacity);
 }
 
-kifi_status kifi_volume_insert(kifi_volume* v, const uint32_t* keys, const float* values, size_t n) {
-    if (!v || (n && !keys)) return fail(KIFI_ERR_INVALID_ARGUMENT, "null argument");
+// flat_map::insert of n sorted unique keys given `in_bytes` wide.
+static kifi_status insert_keys(kifi_volume* v, const void* keys_in, int in_bytes, const float* values, size_t n) {
+    if (!v || (n && !keys_in)) return fail(KIFI_ERR_INVALID_ARGUMENT, "null argument");
     if (n == 0) return KIFI_OK;
     if (n >= ((size_t)1 << 30)) return fail(KIFI_ERR_INVALID_ARGUMENT, "too many keys");
     const uint32_t res = (uint32_t)v->g.res;
+    const int b = in_bytes == 4 ? 10 : v->g.kb;
+    const uint64_t mask = ((uint64_t)1 << b) - 1;
+    // keys in the volume's width (the 64-bit key of a 30-bit key is the same number when b = 10)
+    std::vector<unsigned char> conv;
+    const void* src = keys_in;
+    if (in_bytes != v->vb.key_bytes) {
+        if (v->g.kb != 10) return fail(KIFI_ERR_UNSUPPORTED, "keys of this volume need 64 bits (kifi_volume_insert64)");
+        conv.resize(n * v->vb.key_bytes);
+        for (size_t i = 0; i < n; ++i) {
+            if (in_bytes == 4) ((uint64_t*)conv.data())[i] = ((const uint32_t*)keys_in)[i];
+            else ((uint32_t*)conv.data())[i] = (uint32_t)((const uint64_t*)keys_in)[i];
+        }
+        src = conv.data();
+    }
     for (size_t i = 0; i < n; ++i) {
-        const uint32_t k = keys[i];
-        if (k >> 30 || key_x(k) >= res || key_y(k) >= res || key_z(k) >= res)
+        const uint64_t k = in_bytes == 4 ? (uint64_t)((const uint32_t*)keys_in)[i] : ((const uint64_t*)keys_in)[i];
+        const uint64_t prev =
+            i ? (in_bytes == 4 ? (uint64_t)((const uint32_t*)keys_in)[i - 1] : ((const uint64_t*)keys_in)[i - 1]) : 0;
+        if (k >> (3 * b) || (k & mask) >= res || (k >> b & mask) >= res || (k >> (2 * b)) >= res)
             return fail(KIFI_ERR_INVALID_ARGUMENT, "key outside the volume");
-        if (i && keys[i - 1] >= k) return fail(KIFI_ERR_INVALID_ARGUMENT, "keys not sorted/unique");
+        if (i && prev >= k) return fail(KIFI_ERR_INVALID_ARGUMENT, "keys not sorted/unique");
     }
     KIFI_CUDA(cudaSetDevice(v->device));
     kifi_status s = reserve_new(v, n);
     if (s) return s;
     if ((s = read_ctl(v))) return s;
     if ((s = grow_volume(v, v->n_upper + n))) return s;
-    uint32_t* dk = nullptr;
+    const size_t kbytes = (size_t)v->vb.key_bytes;
+    void* dk = nullptr;
     float2* dv = nullptr;
     unsigned int* dn = nullptr;
     auto cleanup = [&]() {
@@ -428,7 +497,7 @@ kifi_status kifi_volume_insert(kifi_volume* v, const uint32_t* keys, const float
         cudaFree(dv);
         cudaFree(dn);
     };
-    cudaError_t e = cudaMalloc(&dk, n * 4);
+    cudaError_t e = cudaMalloc(&dk, n * kbytes);
     if (!e && values) e = cudaMalloc(&dv, n * 8);
     if (!e) e = cudaMalloc(&dn, 4);
     if (e) {
@@ -436,18 +505,26 @@ kifi_status kifi_volume_insert(kifi_volume* v, const uint32_t* keys, const float
         return cuda_fail(e, "insert staging");
     }
     const unsigned int n32 = (unsigned int)n;
-    e = cudaMemcpyAsync(dk, keys, n * 4, cudaMemcpyHostToDevice, v->stream);
+    e = cudaMemcpyAsync(dk, src, n * kbytes, cudaMemcpyHostToDevice, v->stream);
     if (!e && values) e = cudaMemcpyAsync(dv, values, n * 8, cudaMemcpyHostToDevice, v->stream);
     if (!e) e = cudaMemcpyAsync(dn, &n32, 4, cudaMemcpyHostToDevice, v->stream);
     if (!e) e = insert_filter_enqueue(v->ctl, v->g, v->vb, dk, dn, v->ls, v->stream);
-    if (!e) e = sort_u32(v->vb.new_keys, v->vb.new_idx, &v->ctl->n_new, v->ss, &v->ctl->status,
-                         v->ls.sort_ctas, v->stream);
+    if (!e) e = sort_keys(v->vb.new_keys, v->vb.key_bytes, 3 * v->g.kb, v->vb.new_idx, &v->ctl->n_new, v->ss,
+                          &v->ctl->status, v->ls.sort_ctas, v->stream);
     if (!e) e = insert_merge_enqueue(v->ctl, v->g, v->vb, dv, v->ls, v->stream);
     if (!e) e = cudaStreamSynchronize(v->stream);
     cleanup();
     if (e) return cuda_fail(e, "insert");
     if ((s = read_ctl(v))) return s;
     return take_device_status(v);
+}
+
+kifi_status kifi_volume_insert(kifi_volume* v, const uint32_t* keys, const float* values, size_t n) {
+    return insert_keys(v, keys, 4, values, n);
+}
+
+kifi_status kifi_volume_insert64(kifi_volume* v, const uint64_t* keys, const float* values, size_t n) {
+    return insert_keys(v, keys, 8, values, n);
 }
 
 kifi_status kifi_integrate_f32(kifi_volume* v, const float* depth_m, const kifi_camera* cam,
@@ -524,11 +601,11 @@ static kifi_status mesh_to_device(kifi_volume* v, int with_indices, size_t* n_ve
     if (n < 2) return KIFI_OK;  // the reference's loop starts at size-2
     if (n >= ((size_t)1 << 28)) return fail(KIFI_ERR_UNSUPPORTED, "mesh of more than 2^28 voxels");
     const unsigned int cur = v->ctl_host->cur;
-    KIFI_CUDA(mesh_scratch_reserve(&v->ms, n));
+    KIFI_CUDA(mesh_scratch_reserve(&v->ms, n, v->g.kb));
     const unsigned int n32 = (unsigned int)n;
     KIFI_CUDA(cudaMemcpyAsync(v->ms.n_dev, &n32, sizeof n32, cudaMemcpyHostToDevice, v->stream));
-    KIFI_CUDA(mesh_count_enqueue(v->vb.keys[cur], v->vb.vals[cur], n, with_indices ? 1 : 0, v->ms, v->ls.sms,
-                                 v->stream));
+    KIFI_CUDA(mesh_count_enqueue(v->vb.keys[cur], v->vb.key_bytes, v->vb.vals[cur], n, v->g.kb,
+                                 with_indices ? 1 : 0, v->ms, v->ls.sms, v->stream));
     MeshCounts* mc = &v->ctl_host_mesh;
     KIFI_CUDA(cudaMemcpyAsync(mc, v->ms.counts, sizeof(MeshCounts), cudaMemcpyDeviceToHost,
                               v->stream));
@@ -548,8 +625,8 @@ static kifi_status mesh_to_device(kifi_volume* v, int with_indices, size_t* n_ve
         KIFI_CUDA(cudaMalloc(&v->mesh_idx, (ni + kPad) * 4));
         v->mesh_idx_cap = ni;
     }
-    KIFI_CUDA(mesh_emit_enqueue(v->g, v->vb.keys[cur], v->vb.vals[cur], n, with_indices ? 1 : 0, v->ms, nv, ni,
-                                v->mesh_verts, v->mesh_idx, v->ls.sms, v->stream));
+    KIFI_CUDA(mesh_emit_enqueue(v->g, v->vb.keys[cur], v->vb.key_bytes, v->vb.vals[cur], n, with_indices ? 1 : 0,
+                                v->ms, nv, ni, v->mesh_verts, v->mesh_idx, v->ls.sms, v->stream));
     *n_verts = nv;
     *n_indices = ni;
     v->mesh_counts_valid = true;
@@ -587,7 +664,8 @@ kifi_status kifi_mesh_device(kifi_volume* v, int with_indices, size_t* n_verts, 
     return KIFI_OK;
 }
 
-static kifi_status radix_sort_host(uint32_t* keys, uint32_t* values, size_t n) {
+// keys of key_bytes (4 or 8) bytes, all bits significant
+static kifi_status radix_sort_host(void* keys, int key_bytes, uint32_t* values, size_t n) {
     if (n == 0) return KIFI_OK;
     if (!keys) return fail(KIFI_ERR_INVALID_ARGUMENT, "null keys");
     if (n >= ((size_t)1 << 30)) return fail(KIFI_ERR_UNSUPPORTED, "sort of 2^30 or more keys");
@@ -599,21 +677,23 @@ static kifi_status radix_sort_host(uint32_t* keys, uint32_t* values, size_t n) {
     cudaStream_t st;
     KIFI_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
     SortScratch ss;
-    uint32_t *dk = nullptr, *dv = nullptr;
+    void* dk = nullptr;
+    uint32_t* dv = nullptr;
     unsigned int *dn = nullptr, *dstatus = nullptr;
     const unsigned int n32 = (unsigned int)n;
+    const size_t kb = (size_t)key_bytes;
     unsigned int status = 0;
     cudaError_t e = sort_scratch_alloc(&ss, n);
-    if (!e) e = cudaMalloc(&dk, (n + kPad) * 4);
+    if (!e) e = cudaMalloc(&dk, (n + kPad) * kb);
     if (!e && values) e = cudaMalloc(&dv, (n + kPad) * 4);
     if (!e) e = cudaMalloc(&dn, 4);
     if (!e) e = cudaMalloc(&dstatus, 4);
     if (!e) e = cudaMemsetAsync(dstatus, 0, 4, st);
-    if (!e) e = cudaMemcpyAsync(dk, keys, n * 4, cudaMemcpyHostToDevice, st);
+    if (!e) e = cudaMemcpyAsync(dk, keys, n * kb, cudaMemcpyHostToDevice, st);
     if (!e && values) e = cudaMemcpyAsync(dv, values, n * 4, cudaMemcpyHostToDevice, st);
     if (!e) e = cudaMemcpyAsync(dn, &n32, 4, cudaMemcpyHostToDevice, st);
-    if (!e) e = sort_u32(dk, dv, dn, ss, dstatus, ls.sort_ctas, st);
-    if (!e) e = cudaMemcpyAsync(keys, dk, n * 4, cudaMemcpyDeviceToHost, st);
+    if (!e) e = sort_keys(dk, key_bytes, 8 * key_bytes, dv, dn, ss, dstatus, ls.sort_ctas, st);
+    if (!e) e = cudaMemcpyAsync(keys, dk, n * kb, cudaMemcpyDeviceToHost, st);
     if (!e && values) e = cudaMemcpyAsync(values, dv, n * 4, cudaMemcpyDeviceToHost, st);
     if (!e) e = cudaMemcpyAsync(&status, dstatus, 4, cudaMemcpyDeviceToHost, st);
     if (!e) e = cudaStreamSynchronize(st);
@@ -628,11 +708,18 @@ static kifi_status radix_sort_host(uint32_t* keys, uint32_t* values, size_t n) {
     return KIFI_OK;
 }
 
-kifi_status kifi_radix_sort_u32(uint32_t* keys, size_t n) { return radix_sort_host(keys, nullptr, n); }
+kifi_status kifi_radix_sort_u32(uint32_t* keys, size_t n) { return radix_sort_host(keys, 4, nullptr, n); }
 
 kifi_status kifi_radix_sort_pairs_u32(uint32_t* keys, uint32_t* values, size_t n) {
     if (n && !values) return fail(KIFI_ERR_INVALID_ARGUMENT, "null values");
-    return radix_sort_host(keys, values, n);
+    return radix_sort_host(keys, 4, values, n);
+}
+
+kifi_status kifi_radix_sort_u64(uint64_t* keys, size_t n) { return radix_sort_host(keys, 8, nullptr, n); }
+
+kifi_status kifi_radix_sort_pairs_u64(uint64_t* keys, uint32_t* values, size_t n) {
+    if (n && !values) return fail(KIFI_ERR_INVALID_ARGUMENT, "null values");
+    return radix_sort_host(keys, 8, values, n);
 }
 
 }  // extern "C"

@@ -8,8 +8,9 @@
 //    double-buffered staging, and the fusion kernels convert millimetres
 //    with the same `texel * 0.001f` as DepthStream.cpp:89-90.
 //  * kifi::Mesher::Mesh2Obj (Mesher.cpp:50-78): Wavefront OBJ text.
-//  * Volume checkpoints (no counterpart in the reference): the resident keys
-//    and voxels, restored by a set-union insert into a fresh volume.
+//  * Volume checkpoints (no counterpart in the reference): a header, the
+//    resident keys in the volume's width, and the voxels, restored by a
+//    set-union insert into a fresh volume of the same key width.
 //
 // .depth layout (poly2depth/README.txt, DepthStream.cpp:23-51): 15 bytes of
 // magic (not checked by the reference, not checked here), int version;
@@ -49,7 +50,7 @@ struct CheckpointHeader {
     int32_t resolution;
     float side_length_m;
     float truncation_m;
-    uint32_t reserved;
+    uint32_t key_bits;  // 0 (files before 64-bit keys) or 32: uint32 keys; 64: uint64 keys
     uint64_t n_voxels;
 };
 
@@ -200,19 +201,23 @@ kifi_status kifi_volume_save(kifi_volume* vol, const char* path) {
     size_t n = 0;
     kifi_status st = kifi_volume_size(vol, &n);
     if (st) return st;
-    std::vector<uint32_t> keys(n + 1);
+    const int kbytes = vol->vb.key_bytes;
+    std::vector<unsigned char> keys((n + 1) * kbytes);
     std::vector<float> values(2 * (n + 1));
     size_t got = 0;
-    if ((st = kifi_volume_export(vol, keys.data(), values.data(), n + 1, &got))) return st;
+    st = kbytes == 8 ? kifi_volume_export64(vol, (uint64_t*)keys.data(), values.data(), n + 1, &got)
+                     : kifi_volume_export(vol, (uint32_t*)keys.data(), values.data(), n + 1, &got);
+    if (st) return st;
     CheckpointHeader h{};
     std::memcpy(h.magic, kCheckpointMagic, 8);
     h.resolution = vol->g.res;
     h.side_length_m = vol->g.side;
     h.truncation_m = vol->g.trunc;
+    h.key_bits = (uint32_t)(8 * kbytes);
     h.n_voxels = got;
     std::FILE* f = std::fopen(path, "wb");
     if (!f) return fail(KIFI_ERR_IO, "cannot open the checkpoint file");
-    bool ok = std::fwrite(&h, sizeof h, 1, f) == 1 && std::fwrite(keys.data(), 4, got, f) == got &&
+    bool ok = std::fwrite(&h, sizeof h, 1, f) == 1 && std::fwrite(keys.data(), kbytes, got, f) == got &&
               std::fwrite(values.data(), 8, got, f) == got;
     ok = (std::fclose(f) == 0) && ok;
     return ok ? KIFI_OK : fail(KIFI_ERR_IO, "writing the checkpoint failed");
@@ -225,20 +230,34 @@ kifi_status kifi_volume_load(const char* path, int device, kifi_volume** out) {
     if (!f) return fail(KIFI_ERR_IO, "cannot open the checkpoint file");
     CheckpointHeader h{};
     bool ok = read_exact(f, &h, sizeof h) && std::memcmp(h.magic, kCheckpointMagic, 8) == 0 &&
-              h.n_voxels <= ((uint64_t)1 << 32);
-    std::vector<uint32_t> keys;
+              h.n_voxels <= ((uint64_t)1 << 32) && (h.key_bits == 0 || h.key_bits == 32 || h.key_bits == 64) &&
+              h.resolution >= 2 && h.resolution <= 8192 && !(h.resolution & (h.resolution - 1));
+    const bool wide = h.key_bits == 64;
+    std::vector<uint64_t> keys;
     std::vector<float> values;
     if (ok) {
         keys.resize(h.n_voxels);
         values.resize(2 * h.n_voxels);
-        ok = read_exact(f, keys.data(), 4 * h.n_voxels) && read_exact(f, values.data(), 8 * h.n_voxels);
+        if (wide) {
+            ok = read_exact(f, keys.data(), 8 * h.n_voxels);
+        } else {
+            std::vector<uint32_t> k32(h.n_voxels);
+            ok = read_exact(f, k32.data(), 4 * h.n_voxels);
+            for (size_t i = 0; ok && i < k32.size(); ++i) keys[i] = k32[i];
+        }
+        ok = ok && read_exact(f, values.data(), 8 * h.n_voxels);
     }
     std::fclose(f);
     if (!ok) return fail(KIFI_ERR_FORMAT, "not a volume checkpoint, or truncated");
-    const uint32_t r = (uint32_t)h.resolution;
+    const uint64_t r = (uint64_t)h.resolution;
+    int b = 10;
+    if (wide)
+        while ((1 << b) < h.resolution) ++b;
+    const uint64_t mask = ((uint64_t)1 << b) - 1;
     for (size_t i = 0; ok && i < keys.size(); ++i) {
-        ok = key_x(keys[i]) < r && key_y(keys[i]) < r && key_z(keys[i]) < r;
-        if (i) ok = ok && keys[i - 1] < keys[i];
+        const uint64_t k = keys[i];
+        ok = (k & mask) < r && (k >> b & mask) < r && (k >> (2 * b)) < r;
+        if (i) ok = ok && keys[i - 1] < k;
     }
     if (!ok) return fail(KIFI_ERR_FORMAT, "checkpoint keys not sorted, unique and inside the volume");
     kifi_volume_desc d{};
@@ -247,10 +266,11 @@ kifi_status kifi_volume_load(const char* path, int device, kifi_volume** out) {
     d.truncation_m = h.truncation_m;
     d.initial_capacity = keys.size() + 1;
     d.device = device;
+    d.key_bits = wide ? 64 : 32;
     kifi_volume* v = nullptr;
     kifi_status st = kifi_volume_create(&d, &v);
     if (st) return st;
-    if (!keys.empty() && (st = kifi_volume_insert(v, keys.data(), values.data(), keys.size()))) {
+    if (!keys.empty() && (st = kifi_volume_insert64(v, keys.data(), values.data(), keys.size()))) {
         kifi_volume_destroy(v);
         return st;
     }

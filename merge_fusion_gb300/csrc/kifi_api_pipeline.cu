@@ -52,7 +52,7 @@ struct kifi_pipeline {
     // asynchronous meshing
     cudaStream_t ms = nullptr;
     MeshScratch mscr{};
-    uint32_t* snap_keys = nullptr;
+    void* snap_keys = nullptr;  // the volume's key width
     float2* snap_vals = nullptr;
     size_t snap_cap = 0, snap_n = 0;
     float* mverts = nullptr;
@@ -82,8 +82,9 @@ kifi_status mesh_emit(kifi_pipeline* p) {
         p->midx_cap = (ni + kPad) + (ni + kPad) / 4;
         KIFI_CUDA(cudaMallocAsync((void**)&p->midx, p->midx_cap * 4, p->ms));
     }
-    KIFI_CUDA(mesh_emit_enqueue(p->vol->g, p->snap_keys, p->snap_vals, p->snap_n, p->desc.mesh_with_indices,
-                                p->mscr, nv, ni, p->mverts, p->midx, p->vol->ls.sms, p->ms));
+    KIFI_CUDA(mesh_emit_enqueue(p->vol->g, p->snap_keys, p->vol->vb.key_bytes, p->snap_vals, p->snap_n,
+                                p->desc.mesh_with_indices, p->mscr, nv, ni, p->mverts, p->midx, p->vol->ls.sms,
+                                p->ms));
     p->mesh_verts = nv;
     p->mesh_indices = ni;
     p->counting = false;
@@ -115,7 +116,7 @@ kifi_status mesh_begin(kifi_pipeline* p) {
         p->snap_keys = nullptr;
         p->snap_vals = nullptr;
         p->snap_cap = 0;
-        KIFI_CUDA(cudaMalloc(&p->snap_keys, (v->vb.cap + kPad) * 4));
+        KIFI_CUDA(cudaMalloc(&p->snap_keys, (v->vb.cap + kPad) * v->vb.key_bytes));
         KIFI_CUDA(cudaMalloc(&p->snap_vals, (v->vb.cap + kPad) * 8));
         p->snap_cap = v->vb.cap;
     }
@@ -123,7 +124,7 @@ kifi_status mesh_begin(kifi_pipeline* p) {
     p->snap_n = v->n_upper < p->snap_cap ? v->n_upper : p->snap_cap;
     if (p->mscr.cap < p->snap_n) {  // with headroom: freeing scratch waits for the device
         const size_t want = p->snap_n + p->snap_n / 4;
-        KIFI_CUDA(mesh_scratch_reserve(&p->mscr, want < p->snap_cap ? want : p->snap_cap));
+        KIFI_CUDA(mesh_scratch_reserve(&p->mscr, want < p->snap_cap ? want : p->snap_cap, v->g.kb));
     }
     KIFI_CUDA(cudaEventRecord(p->frame_done, p->vs));
     KIFI_CUDA(cudaStreamWaitEvent(p->ms, p->frame_done, 0));
@@ -131,8 +132,8 @@ kifi_status mesh_begin(kifi_pipeline* p) {
                                     p->ms));
     KIFI_CUDA(cudaEventRecord(p->snap_done, p->ms));
     KIFI_CUDA(cudaStreamWaitEvent(p->vs, p->snap_done, 0));  // fusion may overwrite the buffers after the copy
-    KIFI_CUDA(mesh_count_enqueue(p->snap_keys, p->snap_vals, p->snap_n, p->desc.mesh_with_indices, p->mscr,
-                                 v->ls.sms, p->ms));
+    KIFI_CUDA(mesh_count_enqueue(p->snap_keys, v->vb.key_bytes, p->snap_vals, p->snap_n, v->g.kb,
+                                 p->desc.mesh_with_indices, p->mscr, v->ls.sms, p->ms));
     KIFI_CUDA(cudaMemcpyAsync(p->counts_host, p->mscr.counts, sizeof(MeshCounts), cudaMemcpyDeviceToHost, p->ms));
     KIFI_CUDA(cudaEventRecord(p->counts_ready, p->ms));
     p->counting = true;
@@ -248,6 +249,7 @@ kifi_status kifi_pipeline_create(const kifi_pipeline_desc* d, kifi_pipeline** ou
     vd.truncation_m = d->truncation_m;
     vd.initial_capacity = d->initial_capacity;
     vd.device = d->device;
+    vd.key_bits = d->key_bits;
     kifi_status s = kifi_volume_create(&vd, &p->vol);
     if (!s) s = kifi_icp_create(d->device, nullptr, &p->icp);
     if (s) {

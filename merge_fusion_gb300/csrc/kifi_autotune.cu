@@ -35,7 +35,7 @@ std::mutex g_mu;
 std::map<std::string, LaunchShape> g_cache;
 bool g_loaded = false;
 
-std::string cache_key(int device, int res, int w, int h) {
+std::string cache_key(int device, int res, int key_bits, int w, int h) {
     cudaDeviceProp prop;
     if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) {
         cudaGetLastError();
@@ -43,7 +43,11 @@ std::string cache_key(int device, int res, int w, int h) {
         prop.multiProcessorCount = 0;
     }
     char buf[512];
-    std::snprintf(buf, sizeof buf, "%s|%d|%d|%dx%d", prop.name, prop.multiProcessorCount, res, w, h);
+    // 30-bit keys keep the key format of caches written before 64-bit keys
+    if (key_bits == 64)
+        std::snprintf(buf, sizeof buf, "%s|%d|%d|k64|%dx%d", prop.name, prop.multiProcessorCount, res, w, h);
+    else
+        std::snprintf(buf, sizeof buf, "%s|%d|%d|%dx%d", prop.name, prop.multiProcessorCount, res, w, h);
     for (char* c = buf; *c; ++c)
         if (*c == ' ') *c = '_';
     return buf;
@@ -95,7 +99,7 @@ extern "C" kifi_status kifi_volume_autotune(kifi_volume* v, const void* depth_de
     if (!v || !depth_dev || !camera_ok(cam) || !world_to_eye)
         return fail(KIFI_ERR_INVALID_ARGUMENT, "autotune: bad argument");
     KIFI_CUDA(cudaSetDevice(v->device));
-    const std::string key = cache_key(v->device, v->g.res, cam->width, cam->height);
+    const std::string key = cache_key(v->device, v->g.res, 8 * v->vb.key_bytes, cam->width, cam->height);
     {
         std::lock_guard<std::mutex> lock(g_mu);
         load_file();
@@ -117,17 +121,17 @@ extern "C" kifi_status kifi_volume_autotune(kifi_volume* v, const void* depth_de
     const size_t n = (size_t)v->ctl_host->n[cur];
     Snapshot snap;
     KIFI_CUDA(cudaMalloc(&snap.ctl, sizeof(DeviceCtl)));
-    KIFI_CUDA(cudaMalloc(&snap.keys, (n + kPad) * 4));
+    KIFI_CUDA(cudaMalloc(&snap.keys, (n + kPad) * v->vb.key_bytes));
     KIFI_CUDA(cudaMalloc(&snap.vals, (n + kPad) * 8));
     KIFI_CUDA(cudaMalloc(&snap.bitmap, v->vb.bitmap_words * 4));
     cudaStream_t st = v->stream;
     KIFI_CUDA(cudaMemcpyAsync(snap.ctl, v->ctl, sizeof(DeviceCtl), cudaMemcpyDeviceToDevice, st));
-    KIFI_CUDA(cudaMemcpyAsync(snap.keys, v->vb.keys[cur], n * 4, cudaMemcpyDeviceToDevice, st));
+    KIFI_CUDA(cudaMemcpyAsync(snap.keys, v->vb.keys[cur], n * v->vb.key_bytes, cudaMemcpyDeviceToDevice, st));
     KIFI_CUDA(cudaMemcpyAsync(snap.vals, v->vb.vals[cur], n * 8, cudaMemcpyDeviceToDevice, st));
     KIFI_CUDA(cudaMemcpyAsync(snap.bitmap, v->vb.bitmap, v->vb.bitmap_words * 4, cudaMemcpyDeviceToDevice, st));
     auto restore = [&]() -> kifi_status {
         KIFI_CUDA(cudaMemcpyAsync(v->ctl, snap.ctl, sizeof(DeviceCtl), cudaMemcpyDeviceToDevice, st));
-        KIFI_CUDA(cudaMemcpyAsync(v->vb.keys[cur], snap.keys, n * 4, cudaMemcpyDeviceToDevice, st));
+        KIFI_CUDA(cudaMemcpyAsync(v->vb.keys[cur], snap.keys, n * v->vb.key_bytes, cudaMemcpyDeviceToDevice, st));
         KIFI_CUDA(cudaMemcpyAsync(v->vb.vals[cur], snap.vals, n * 8, cudaMemcpyDeviceToDevice, st));
         KIFI_CUDA(cudaMemcpyAsync(v->vb.bitmap, snap.bitmap, v->vb.bitmap_words * 4, cudaMemcpyDeviceToDevice, st));
         return KIFI_OK;

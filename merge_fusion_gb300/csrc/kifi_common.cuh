@@ -106,10 +106,40 @@ KIFI_HD uint32_t key_x(uint32_t k) { return k & 0x3ffu; }
 KIFI_HD uint32_t key_y(uint32_t k) { return k >> 10 & 0x3ffu; }
 KIFI_HD uint32_t key_z(uint32_t k) { return k >> 20; }
 
+// The same linear order for volumes beyond 1024 voxels per axis: 64-bit keys
+// z << 2b | y << b | x with b = log2(res) bits per axis.  Codec<uint32_t> is
+// util::pack (b = 10, fixed at compile time); Codec<uint64_t> takes b at run
+// time.  With b = 10 both encode a voxel to the same number.
+template <typename K>
+struct Codec;
+template <>
+struct Codec<uint32_t> {
+    static constexpr int b = 10;
+    KIFI_HD explicit Codec(int) {}
+    KIFI_HD uint32_t pack(uint32_t x, uint32_t y, uint32_t z) const { return pack30(x, y, z); }
+    KIFI_HD uint32_t x(uint32_t k) const { return key_x(k); }
+    KIFI_HD uint32_t y(uint32_t k) const { return key_y(k); }
+    KIFI_HD uint32_t z(uint32_t k) const { return key_z(k); }
+    KIFI_HD uint32_t row(uint32_t k) const { return k >> 10; }  // (z, y) row
+};
+template <>
+struct Codec<uint64_t> {
+    int b;
+    KIFI_HD explicit Codec(int bits) : b(bits) {}
+    KIFI_HD uint64_t pack(uint32_t x, uint32_t y, uint32_t z) const {
+        return (uint64_t)z << (2 * b) | (uint64_t)y << b | (uint64_t)x;
+    }
+    KIFI_HD uint32_t x(uint64_t k) const { return (uint32_t)(k & ((1ull << b) - 1)); }
+    KIFI_HD uint32_t y(uint64_t k) const { return (uint32_t)((k >> b) & ((1ull << b) - 1)); }
+    KIFI_HD uint32_t z(uint64_t k) const { return (uint32_t)(k >> (2 * b)); }
+    KIFI_HD uint64_t row(uint64_t k) const { return k >> b; }
+};
+
 // ------------------------------------------------------- volume geometry
 // Volume's precomputed terms (Volume.cpp:12-37).
 struct Geom {
     int res;
+    int kb;            // key bits per axis: 10 (30-bit keys) or log2(res) (64-bit keys)
     float side, trunc;
     float vlen;        // side / res
     float center_off;  // vlen * 0.5 + min      (VoxelCenter)
@@ -120,6 +150,7 @@ struct Geom {
 KIFI_HD Geom make_geom(int res, float side, float trunc) {
     Geom g;
     g.res = res;
+    g.kb = 10;
     g.side = side;
     g.trunc = trunc;
     float mn = fmul(-0.5f, side);
@@ -183,7 +214,7 @@ struct DeviceCtl {
     unsigned long long n[2];       // voxel count of key/value buffer 0 and 1
     unsigned int cur;              // which buffer holds the resident volume
     unsigned int n_new;            // keys appended by the splat/emit kernel
-    unsigned int excluded_key;     // max splat key + pack(1,1,1), or 0
+    unsigned long long excluded_key;  // max splat key + pack(1,1,1), or 0
     unsigned int status;           // KIFI_ERR_* bits raised on the device
     unsigned long long sort_epoch; // generation tag of the sort look-back words
     unsigned int tile_counter[8];  // dynamic tile ids (one per sort pass / merge)

@@ -43,13 +43,16 @@ namespace {
 constexpr int kEmitThreads = 256;
 constexpr int kMergeThreads = 256;
 constexpr int kMergeItems = 8;                            // outputs per thread
-constexpr int kMergeTile = kMergeThreads * kMergeItems;   // 2048 outputs per tile
+constexpr int kMergeTile = kMergeThreads * kMergeItems;   // 2048 outputs per tile (30-bit keys)
+// outputs per merge tile: 64-bit keys halve it to stay within 48 KB of shared memory
+template <typename K>
+__host__ __device__ constexpr int merge_tile() { return sizeof(K) == 4 ? kMergeTile : kMergeTile / 2; }
 constexpr uint16_t kFromB = 0x8000u;
 
 __global__ void k_frame_setup(DeviceCtl* ctl) {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         ctl->n_new = 0u;
-        ctl->excluded_key = 0u;
+        ctl->excluded_key = 0ull;
     }
 }
 
@@ -60,13 +63,26 @@ __device__ __forceinline__ float load_depth(const void* depth, size_t i, bool u1
     return __ldg((const float*)depth + i);
 }
 
-__device__ __forceinline__ size_t bit_index(uint32_t key, int res) {
-    return (size_t)key_x(key) + (size_t)res * ((size_t)key_y(key) + (size_t)res * key_z(key));
+template <typename K>
+__device__ __forceinline__ size_t bit_index(K key, const Codec<K>& cd, int res) {
+    return (size_t)cd.x(key) + (size_t)res * ((size_t)cd.y(key) + (size_t)res * cd.z(key));
+}
+
+// maximum over the warp
+__device__ __forceinline__ uint32_t warp_max(uint32_t v) { return __reduce_max_sync(0xffffffffu, v); }
+__device__ __forceinline__ uint64_t warp_max(uint64_t v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const uint64_t w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
+    return v;
 }
 
 // Splat of one pixel (Integrator.cpp:121-154 for one SSE lane).
+template <typename K>
 __device__ __forceinline__ bool splat_pixel(const FrameConst& fc, const float (&e2w)[16],
-                                            const Geom& g, int u, int v, float d, uint32_t* key) {
+                                            const Geom& g, const Codec<K>& cd, int u, int v, float d, K* key) {
     if (!(d > 0.0f)) return false;
     float p[4];
     // point = (u, -v, -1, 0) + 0; point * flInv + ppOverFl; point * depth + (0,0,0,1)
@@ -85,17 +101,18 @@ __device__ __forceinline__ bool splat_pixel(const FrameConst& fc, const float (&
     if (!(ix >= 0.0f && ix < mx && iy >= 0.0f && iy < mx && iz >= 0.0f && iz < mx && iw >= 0.0f &&
           iw < mx))
         return false;
-    *key = pack30((uint32_t)ix, (uint32_t)iy, (uint32_t)iz);
+    *key = cd.pack((uint32_t)ix, (uint32_t)iy, (uint32_t)iz);
     return true;
 }
 
-template <bool kU16>
+template <bool kU16, typename K>
 __global__ void __launch_bounds__(kEmitThreads) k_splat_emit(DeviceCtl* __restrict__ ctl, Geom g,
                                                              const void* __restrict__ depth,
                                                              uint32_t* __restrict__ bitmap,
-                                                             uint32_t* __restrict__ new_keys,
+                                                             K* __restrict__ new_keys,
                                                              unsigned int new_cap,
                                                              const FrameConst fc) {
+    const Codec<K> cd(g.kb);
     const int W = fc.width, H = fc.height;
     const size_t P = (size_t)W * H;
     const int lane = threadIdx.x & 31;
@@ -105,17 +122,17 @@ __global__ void __launch_bounds__(kEmitThreads) k_splat_emit(DeviceCtl* __restri
     const size_t stride = (size_t)gridDim.x * kEmitThreads;
     const size_t P_round = (P + 31) / 32 * 32;  // warp-uniform trip count
     for (size_t i = (size_t)blockIdx.x * kEmitThreads + threadIdx.x; i < P_round; i += stride) {
-        uint32_t key = 0;
+        K key = 0;
         bool valid = false;
         if (i < P) {
             int u = (int)(i % (size_t)W), v = (int)(i / (size_t)W);
-            valid = splat_pixel(fc, e2w, g, u, v, load_depth(depth, i, kU16), &key);
+            valid = splat_pixel<K>(fc, e2w, g, cd, u, v, load_depth(depth, i, kU16), &key);
         }
         // the excluded key of the dilation: max splat + pack(1,1,1)
-        unsigned int ex = __reduce_max_sync(0xffffffffu, valid ? key + pack30(1, 1, 1) : 0u);
-        if (lane == 0 && ex) atomicMax(&ctl->excluded_key, ex);
+        const K ex = warp_max(valid ? (K)(key + cd.pack(1, 1, 1)) : (K)0);
+        if (lane == 0 && ex) atomicMax(&ctl->excluded_key, (unsigned long long)ex);
         // neighbouring pixels often land in one voxel: one emitter per key
-        unsigned int peers = __match_any_sync(0xffffffffu, valid ? key : 0xffffffffu);
+        unsigned int peers = __match_any_sync(0xffffffffu, valid ? key : ~(K)0);
         const bool emitter = valid && (lane == __ffs(peers) - 1);
         // The dilation's 8 keys are 4 (y, z) rows of an (x, x+1) pair.  The
         // pair's bits are adjacent in the bitmap, so one word probe covers
@@ -126,10 +143,11 @@ __global__ void __launch_bounds__(kEmitThreads) k_splat_emit(DeviceCtl* __restri
             uint32_t* wp[4];
             uint32_t* wq[4];
             uint32_t m0[4], m1[4], pre0[4], pre1[4];
+            const size_t kb0 = bit_index(key, cd, g.res);
+            const size_t res = (size_t)g.res;
 #pragma unroll
             for (int o = 0; o < 4; ++o) {
-                const uint32_t k0 = key + pack30(0, o & 1, o >> 1);
-                const size_t b = bit_index(k0, g.res);
+                const size_t b = kb0 + (size_t)(o & 1) * res + (size_t)(o >> 1) * res * res;
                 const uint32_t sh = (uint32_t)(b & 31);
                 wp[o] = bitmap + (b >> 5);
                 wq[o] = bitmap + ((b + 1) >> 5);
@@ -168,11 +186,11 @@ __global__ void __launch_bounds__(kEmitThreads) k_splat_emit(DeviceCtl* __restri
             unsigned int at = base + incl - cnt;
 #pragma unroll
             for (int o = 0; o < 4; ++o) {
-                const uint32_t k0 = key + pack30(0, o & 1, o >> 1);
+                const K k0 = key + cd.pack(0, o & 1, o >> 1);
 #pragma unroll
                 for (int dx = 0; dx < 2; ++dx) {
                     if (!((got[o] >> dx) & 1u)) continue;
-                    if (at < new_cap) new_keys[at] = k0 + (uint32_t)dx;
+                    if (at < new_cap) new_keys[at] = k0 + (K)dx;
                     else atomicOr(&ctl->status, KIFI_DEV_ERR_CAPACITY);
                     ++at;
                 }
@@ -182,15 +200,16 @@ __global__ void __launch_bounds__(kEmitThreads) k_splat_emit(DeviceCtl* __restri
 }
 
 // UpdateVoxels for one voxel (Integrator.cpp:273-322 for one SSE lane).
-template <bool kU16>
-__device__ __forceinline__ void update_voxel(uint32_t key, float2& val, const FrameConst& fc,
+template <bool kU16, typename K>
+__device__ __forceinline__ void update_voxel(K key, float2& val, const FrameConst& fc,
                                              const float (&w2c)[16], const Geom& g,
                                              const void* depth) {
+    const Codec<K> cd(g.kb);
     // VoxelCenter: index * (vlen, vlen, vlen, 1) + (off, off, off, 0)
     float c[4];
-    c[0] = fadd(fmul((float)key_x(key), g.vlen), g.center_off);
-    c[1] = fadd(fmul((float)key_y(key), g.vlen), g.center_off);
-    c[2] = fadd(fmul((float)key_z(key), g.vlen), g.center_off);
+    c[0] = fadd(fmul((float)cd.x(key), g.vlen), g.center_off);
+    c[1] = fadd(fmul((float)cd.y(key), g.vlen), g.center_off);
+    c[2] = fadd(fmul((float)cd.z(key), g.vlen), g.center_off);
     c[3] = 1.0f;  // 1 * 1 + 0
     // rows 0, 1, 3 of worldToClip * c (mat_vec's order); row 2 below
     auto row = [&](int i) {
@@ -260,9 +279,10 @@ __device__ __forceinline__ void update_voxel(uint32_t key, float2& val, const Fr
 
 // number of A elements among the first d outputs of merge(A, B); A and B
 // are sorted and disjoint.
-__device__ __forceinline__ unsigned long long merge_path(const uint32_t* __restrict__ A,
+template <typename K>
+__device__ __forceinline__ unsigned long long merge_path(const K* __restrict__ A,
                                                          unsigned long long na,
-                                                         const uint32_t* __restrict__ B,
+                                                         const K* __restrict__ B,
                                                          unsigned long long nb,
                                                          unsigned long long d) {
     unsigned long long lo = d > nb ? d - nb : 0, hi = d < na ? d : na;
@@ -274,8 +294,9 @@ __device__ __forceinline__ unsigned long long merge_path(const uint32_t* __restr
     return lo;
 }
 
+template <typename K>
 struct MergeInputs {
-    const uint32_t* b_keys;   // sorted new keys
+    const K* b_keys;          // sorted new keys
     const uint32_t* b_index;  // optional: b's position in b_vals (inserts)
     const float2* b_vals;     // optional values of new keys; null = Voxel()
     const unsigned int* b_count;
@@ -288,22 +309,25 @@ struct MergeInputs {
 // then computes the merge-path split of output tile t: the number of resident
 // keys among the first t*kMergeTile outputs.  The binary searches of all
 // tiles run in parallel here instead of serialising the merge kernel's tiles.
+template <typename K>
 __global__ void __launch_bounds__(256) k_merge_partition(DeviceCtl* __restrict__ ctl, Geom g,
-                                                          VolumeBuffers vb, MergeInputs in,
+                                                          VolumeBuffers vb, MergeInputs<K> in,
                                                           unsigned long long* __restrict__ splits,
                                                           unsigned int max_tiles) {
+    constexpr int kTile = merge_tile<K>();
+    const Codec<K> cd(g.kb);
     __shared__ unsigned long long s_e, s_n1;
     __shared__ int s_ok;
     const unsigned int cur = ctl->cur;
     const unsigned long long N0 = ctl->n[cur];
     // select rather than index: a runtime index into a parameter array
     // would force the array into local memory
-    const uint32_t* __restrict__ A = cur ? vb.keys[1] : vb.keys[0];
-    const uint32_t* __restrict__ B = in.b_keys;
+    const K* __restrict__ A = (const K*)(cur ? vb.keys[1] : vb.keys[0]);
+    const K* __restrict__ B = in.b_keys;
     if (threadIdx.x == 0) {
         unsigned long long e = *in.b_count;
-        const uint32_t excluded = ctl->excluded_key;
-        const bool drop = e > 0 && excluded != 0u && B[e - 1] == excluded;
+        const K excluded = (K)ctl->excluded_key;
+        const bool drop = e > 0 && excluded != 0 && B[e - 1] == excluded;
         if (drop) --e;
         const bool ok = N0 + e <= vb.cap;
         s_e = e;
@@ -314,7 +338,7 @@ __global__ void __launch_bounds__(256) k_merge_partition(DeviceCtl* __restrict__
             ctl->merge_n1 = N0 + e;
             ctl->merge_ok = ok ? 1u : 0u;
             if (drop) {
-                size_t b = bit_index(excluded, g.res);
+                size_t b = bit_index(excluded, cd, g.res);
                 atomicAnd(vb.bitmap + (b >> 5), ~(1u << (b & 31)));
             }
             if (!ok) atomicOr(&ctl->status, KIFI_DEV_ERR_CAPACITY);
@@ -327,59 +351,79 @@ __global__ void __launch_bounds__(256) k_merge_partition(DeviceCtl* __restrict__
         // of the occupancy bitmap; the host grows the buffers and retries.
         for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < e;
              i += (unsigned long long)gridDim.x * blockDim.x) {
-            size_t b = bit_index(B[i], g.res);
+            size_t b = bit_index(B[i], cd, g.res);
             atomicAnd(vb.bitmap + (b >> 5), ~(1u << (b & 31)));
         }
         return;
     }
-    const unsigned long long n_tiles = (N1 + kMergeTile - 1) / kMergeTile;
+    const unsigned long long n_tiles = (N1 + kTile - 1) / kTile;
     for (unsigned long long t = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
          t <= n_tiles && t < max_tiles; t += (unsigned long long)gridDim.x * blockDim.x) {
-        const unsigned long long d = t * kMergeTile < N1 ? t * kMergeTile : N1;
+        const unsigned long long d = t * kTile < N1 ? t * kTile : N1;
         splits[t] = merge_path(A, N0, B, e, d);
     }
 }
 
 // One output voxel: value from A or Voxel(), TSDF update when inside the
 // reference's update range.
-template <bool kU16>
-__device__ __forceinline__ void finish_voxel(uint32_t key, float2& val, unsigned long long pos,
+template <bool kU16, typename K>
+__device__ __forceinline__ void finish_voxel(K key, float2& val, unsigned long long pos,
                                              unsigned long long upd_end, const FrameConst& fc,
                                              const float (&w2c)[16], const Geom& g,
                                              const void* depth) {
-    if (pos < upd_end) update_voxel<kU16>(key, val, fc, w2c, g, depth);
+    if (pos < upd_end) update_voxel<kU16, K>(key, val, fc, w2c, g, depth);
 }
 
-template <bool kU16>
+// four consecutive keys, streamed (p 16-byte aligned for 32-bit keys,
+// 32-byte aligned for 64-bit keys)
+__device__ __forceinline__ void ld4(const uint32_t* p, uint32_t (&k)[4]) {
+    const uint4 v = __ldcs((const uint4*)p);
+    k[0] = v.x; k[1] = v.y; k[2] = v.z; k[3] = v.w;
+}
+__device__ __forceinline__ void ld4(const uint64_t* p, uint64_t (&k)[4]) {
+    const ulonglong2 a = __ldcs((const ulonglong2*)p), b = __ldcs((const ulonglong2*)(p + 2));
+    k[0] = a.x; k[1] = a.y; k[2] = b.x; k[3] = b.y;
+}
+__device__ __forceinline__ void st4(uint32_t* p, const uint32_t (&k)[4]) {
+    __stcs((uint4*)p, make_uint4(k[0], k[1], k[2], k[3]));
+}
+__device__ __forceinline__ void st4(uint64_t* p, const uint64_t (&k)[4]) {
+    __stcs((ulonglong2*)p, make_ulonglong2(k[0], k[1]));
+    __stcs((ulonglong2*)(p + 2), make_ulonglong2(k[2], k[3]));
+}
+
+template <bool kU16, typename K>
 __global__ void __launch_bounds__(kMergeThreads) k_merge_update(DeviceCtl* __restrict__ ctl, Geom g,
-                                                                VolumeBuffers vb, MergeInputs in,
+                                                                VolumeBuffers vb, MergeInputs<K> in,
                                                                 const void* __restrict__ depth,
                                                                 const unsigned long long* __restrict__ splits,
                                                                 const FrameConst fc) {
-    __shared__ uint32_t sA_k[kMergeTile + 8];
-    __shared__ float2 sA_v[kMergeTile + 4];
-    __shared__ uint32_t sB_k[kMergeTile];
-    __shared__ uint16_t sSrc[kMergeTile];
+    constexpr int kTile = merge_tile<K>();
+    constexpr int kItems = kTile / kMergeThreads;
+    __shared__ __align__(16) K sA_k[kTile + 8];
+    __shared__ float2 sA_v[kTile + 4];
+    __shared__ K sB_k[kTile];
+    __shared__ uint16_t sSrc[kTile];
 
     if (!ctl->merge_ok) return;
     const unsigned int cur = ctl->cur, out = cur ^ 1u;
     const unsigned long long N0 = ctl->n[cur];
     const unsigned long long e = ctl->merge_e;
     const unsigned long long N1 = ctl->merge_n1;
-    const uint32_t* __restrict__ A = cur ? vb.keys[1] : vb.keys[0];
+    const K* __restrict__ A = (const K*)(cur ? vb.keys[1] : vb.keys[0]);
     const float2* __restrict__ Av = cur ? vb.vals[1] : vb.vals[0];
-    const uint32_t* __restrict__ B = in.b_keys;
+    const K* __restrict__ B = in.b_keys;
     const unsigned long long upd_end = in.update ? (N1 / 4 * 4) : 0ull;
-    uint32_t* __restrict__ outK = out ? vb.keys[1] : vb.keys[0];
+    K* __restrict__ outK = (K*)(out ? vb.keys[1] : vb.keys[0]);
     float2* __restrict__ outV = out ? vb.vals[1] : vb.vals[0];
-    const unsigned long long n_tiles = (N1 + kMergeTile - 1) / kMergeTile;
+    const unsigned long long n_tiles = (N1 + kTile - 1) / kTile;
     float w2c[16];
 #pragma unroll
     for (int i = 0; i < 16; ++i) w2c[i] = fc.world_to_clip.m[i];
 
     for (unsigned long long t = blockIdx.x; t < n_tiles; t += gridDim.x) {
-        const unsigned long long d0 = t * kMergeTile;
-        const unsigned long long d1 = (d0 + kMergeTile < N1) ? d0 + kMergeTile : N1;
+        const unsigned long long d0 = t * kTile;
+        const unsigned long long d1 = (d0 + kTile < N1) ? d0 + kTile : N1;
         const int len = (int)(d1 - d0);
         const unsigned long long a0 = splits[t], a1 = splits[t + 1];
         const int na = (int)(a1 - a0), nb = len - na;
@@ -387,33 +431,35 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_update(DeviceCtl* __res
             // only resident voxels in this tile: straight streaming, no barrier
             const bool vec = (a0 & 3ull) == 0;
 #pragma unroll
-            for (int r = 0; r < kMergeItems / 4; ++r) {
+            for (int r = 0; r < kItems / 4; ++r) {
                 const int j0 = threadIdx.x * 4 + r * kMergeThreads * 4;
                 if (j0 >= len) break;
-                uint32_t k0, k1, k2, k3;
+                K k0, k1, k2, k3;
                 float2 v0, v1, v2, v3;
                 const unsigned long long ia = a0 + j0;
                 if (vec && j0 + 4 <= len) {
-                    const uint4 kk = __ldcs((const uint4*)(A + ia));
+                    K kk[4];
+                    ld4(A + ia, kk);
                     const float4 va = __ldcs((const float4*)(Av + ia));
                     const float4 vb4 = __ldcs((const float4*)(Av + ia + 2));
-                    k0 = kk.x; k1 = kk.y; k2 = kk.z; k3 = kk.w;
+                    k0 = kk[0]; k1 = kk[1]; k2 = kk[2]; k3 = kk[3];
                     v0 = make_float2(va.x, va.y); v1 = make_float2(va.z, va.w);
                     v2 = make_float2(vb4.x, vb4.y); v3 = make_float2(vb4.z, vb4.w);
                 } else {
                     const int m = len - j0;
                     k0 = __ldcs(A + ia); v0 = __ldcs(Av + ia);
-                    k1 = m > 1 ? __ldcs(A + ia + 1) : 0u; v1 = m > 1 ? __ldcs(Av + ia + 1) : v0;
-                    k2 = m > 2 ? __ldcs(A + ia + 2) : 0u; v2 = m > 2 ? __ldcs(Av + ia + 2) : v0;
-                    k3 = m > 3 ? __ldcs(A + ia + 3) : 0u; v3 = m > 3 ? __ldcs(Av + ia + 3) : v0;
+                    k1 = m > 1 ? __ldcs(A + ia + 1) : (K)0; v1 = m > 1 ? __ldcs(Av + ia + 1) : v0;
+                    k2 = m > 2 ? __ldcs(A + ia + 2) : (K)0; v2 = m > 2 ? __ldcs(Av + ia + 2) : v0;
+                    k3 = m > 3 ? __ldcs(A + ia + 3) : (K)0; v3 = m > 3 ? __ldcs(Av + ia + 3) : v0;
                 }
                 const unsigned long long p = d0 + j0;
-                finish_voxel<kU16>(k0, v0, p, upd_end, fc, w2c, g, depth);
-                finish_voxel<kU16>(k1, v1, p + 1, upd_end, fc, w2c, g, depth);
-                finish_voxel<kU16>(k2, v2, p + 2, upd_end, fc, w2c, g, depth);
-                finish_voxel<kU16>(k3, v3, p + 3, upd_end, fc, w2c, g, depth);
+                finish_voxel<kU16, K>(k0, v0, p, upd_end, fc, w2c, g, depth);
+                finish_voxel<kU16, K>(k1, v1, p + 1, upd_end, fc, w2c, g, depth);
+                finish_voxel<kU16, K>(k2, v2, p + 2, upd_end, fc, w2c, g, depth);
+                finish_voxel<kU16, K>(k3, v3, p + 3, upd_end, fc, w2c, g, depth);
                 if (j0 + 4 <= len) {
-                    __stcs((uint4*)(outK + p), make_uint4(k0, k1, k2, k3));
+                    const K kk[4] = {k0, k1, k2, k3};
+                    st4(outK + p, kk);
                     __stcs((float4*)(outV + p), make_float4(v0.x, v0.y, v1.x, v1.y));
                     __stcs((float4*)(outV + p + 2), make_float4(v2.x, v2.y, v3.x, v3.y));
                 } else {
@@ -429,8 +475,11 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_update(DeviceCtl* __res
         const unsigned long long b0 = d0 - a0;
         const unsigned long long ka = a0 & ~3ull;
         const int koff = (int)(a0 - ka);
-        for (int i = threadIdx.x * 4; i < koff + na; i += kMergeThreads * 4)
-            *(uint4*)&sA_k[i] = __ldcs((const uint4*)(A + ka + i));
+        for (int i = threadIdx.x * 4; i < koff + na; i += kMergeThreads * 4) {
+            K kk[4];
+            ld4(A + ka + i, kk);
+            sA_k[i] = kk[0]; sA_k[i + 1] = kk[1]; sA_k[i + 2] = kk[2]; sA_k[i + 3] = kk[3];
+        }
         const unsigned long long va = a0 & ~1ull;
         const int voff = (int)(a0 - va);
         for (int i = threadIdx.x * 2; i < voff + na; i += kMergeThreads * 2)
@@ -438,7 +487,7 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_update(DeviceCtl* __res
         for (int i = threadIdx.x; i < nb; i += kMergeThreads) sB_k[i] = B[b0 + i];
         __syncthreads();
         {
-            const int dd = threadIdx.x * kMergeItems;
+            const int dd = threadIdx.x * kItems;
             if (dd < len) {
                 int lo = dd > nb ? dd - nb : 0, hi = dd < na ? dd : na;
                 while (lo < hi) {
@@ -447,7 +496,7 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_update(DeviceCtl* __res
                     else hi = mid;
                 }
                 int ia = lo, ib = dd - lo;
-                const int end = dd + kMergeItems < len ? dd + kMergeItems : len;
+                const int end = dd + kItems < len ? dd + kItems : len;
                 for (int j = dd; j < end; ++j) {
                     bool takeA = ib >= nb || (ia < na && sA_k[koff + ia] < sB_k[ib]);
                     sSrc[j] = takeA ? (uint16_t)ia++ : (uint16_t)(kFromB | ib++);
@@ -457,7 +506,7 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_update(DeviceCtl* __res
         __syncthreads();
         for (int j = threadIdx.x; j < len; j += kMergeThreads) {
             const uint16_t src = sSrc[j];
-            uint32_t key;
+            K key;
             float2 val;
             if (!(src & kFromB)) {
                 key = sA_k[koff + src];
@@ -468,7 +517,7 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_update(DeviceCtl* __res
                 if (in.b_vals) val = in.b_vals[in.b_index ? in.b_index[b0 + ib] : b0 + ib];
                 else val = make_float2(0.0f, 0.0f);
             }
-            finish_voxel<kU16>(key, val, d0 + j, upd_end, fc, w2c, g, depth);
+            finish_voxel<kU16, K>(key, val, d0 + j, upd_end, fc, w2c, g, depth);
             __stcs(outK + d0 + j, key);
             __stcs(outV + d0 + j, val);
         }
@@ -495,18 +544,20 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_update(DeviceCtl* __res
 
 // inserts: keep keys not yet in the volume (flat_map::insert keeps resident
 // values), appending (key, position) pairs for the sort.
-__global__ void k_insert_filter(DeviceCtl* ctl, Geom g, uint32_t* bitmap, const uint32_t* keys,
-                                const unsigned int* n_ptr, uint32_t* out_keys, uint32_t* out_idx) {
+template <typename K>
+__global__ void k_insert_filter(DeviceCtl* ctl, Geom g, uint32_t* bitmap, const K* keys,
+                                const unsigned int* n_ptr, K* out_keys, uint32_t* out_idx) {
+    const Codec<K> cd(g.kb);
     const unsigned int n = *n_ptr;
     const int lane = threadIdx.x & 31;
     const unsigned int n_round = (n + 31) / 32 * 32;
     for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_round;
          i += gridDim.x * blockDim.x) {
         bool mine = false;
-        uint32_t k = 0;
+        K k = 0;
         if (i < n) {
             k = keys[i];
-            size_t b = bit_index(k, g.res);
+            size_t b = bit_index(k, cd, g.res);
             uint32_t mask = 1u << (b & 31);
             mine = !(atomicOr(bitmap + (b >> 5), mask) & mask);
         }
@@ -525,72 +576,91 @@ __global__ void k_insert_filter(DeviceCtl* ctl, Geom g, uint32_t* bitmap, const 
 
 __global__ void k_reset_new(DeviceCtl* ctl) {
     ctl->n_new = 0u;
-    ctl->excluded_key = 0u;
+    ctl->excluded_key = 0ull;
 }
 
 }  // namespace
 
 int merge_blocks_per_sm() {
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_merge_update<true>, kMergeThreads, 0) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_merge_update<true, uint32_t>, kMergeThreads, 0) !=
             cudaSuccess ||
         n < 1)
         n = 4;
     return n;
 }
 
+template <typename K>
 static unsigned int max_tiles_of(const VolumeBuffers& vb) {
-    return (unsigned int)((vb.cap + kMergeTile - 1) / kMergeTile + 2);
+    return (unsigned int)((vb.cap + merge_tile<K>() - 1) / merge_tile<K>() + 2);
 }
 
+size_t merge_max_tiles(const VolumeBuffers& vb, size_t cap) {
+    const int tile = vb.key_bytes == 8 ? merge_tile<uint64_t>() : merge_tile<uint32_t>();
+    return (cap + tile - 1) / tile + 2;
+}
+
+template <typename K>
 static cudaError_t merge_enqueue(DeviceCtl* ctl, const Geom& g, VolumeBuffers& vb,
-                                 const MergeInputs& in, const void* depth, bool u16,
+                                 const MergeInputs<K>& in, const void* depth, bool u16,
                                  const FrameConst& fc, const LaunchShape& ls, cudaStream_t st,
                                  cudaEvent_t after_partition = nullptr) {
-    const unsigned int mt = max_tiles_of(vb);
-    k_merge_partition<<<(mt + 255) / 256, 256, 0, st>>>(ctl, g, vb, in, vb.splits, mt);
+    const unsigned int mt = max_tiles_of<K>(vb);
+    k_merge_partition<K><<<(mt + 255) / 256, 256, 0, st>>>(ctl, g, vb, in, vb.splits, mt);
     if (after_partition) cudaEventRecord(after_partition, st);
     if (u16)
-        k_merge_update<true><<<ls.merge_ctas, kMergeThreads, 0, st>>>(ctl, g, vb, in, depth,
-                                                                     vb.splits, fc);
+        k_merge_update<true, K><<<ls.merge_ctas, kMergeThreads, 0, st>>>(ctl, g, vb, in, depth, vb.splits, fc);
     else
-        k_merge_update<false><<<ls.merge_ctas, kMergeThreads, 0, st>>>(ctl, g, vb, in, depth,
-                                                                      vb.splits, fc);
+        k_merge_update<false, K><<<ls.merge_ctas, kMergeThreads, 0, st>>>(ctl, g, vb, in, depth, vb.splits, fc);
     return cudaGetLastError();
 }
 
-cudaError_t integrate_enqueue(DeviceCtl* ctl, const Geom& g, VolumeBuffers& vb, SortScratch& ss,
-                              const void* depth_dev, bool depth_u16, const kifi_camera& cam,
-                              const Mat4& world_to_eye, const LaunchShape& ls, cudaStream_t st,
-                              cudaEvent_t* events) {
+template <typename K>
+static cudaError_t integrate_enqueue_t(DeviceCtl* ctl, const Geom& g, VolumeBuffers& vb, SortScratch& ss,
+                                       const void* depth_dev, bool depth_u16, const kifi_camera& cam,
+                                       const Mat4& world_to_eye, const LaunchShape& ls, cudaStream_t st,
+                                       cudaEvent_t* events) {
     // frame constants on the host, in the reference's float order
     FrameConst fc = make_frame_const(cam, world_to_eye, g.res);
     fc.z_bounded = clip_z_bounded(fc.world_to_clip, g.side);
     if (events) cudaEventRecord(events[0], st);
     k_frame_setup<<<1, 32, 0, st>>>(ctl);
     const unsigned int new_cap = (unsigned int)vb.new_cap;
+    K* nk = (K*)vb.new_keys;
     if (depth_u16)
-        k_splat_emit<true><<<ls.splat_ctas, kEmitThreads, 0, st>>>(ctl, g, depth_dev, vb.bitmap,
-                                                                   vb.new_keys, new_cap, fc);
+        k_splat_emit<true, K><<<ls.splat_ctas, kEmitThreads, 0, st>>>(ctl, g, depth_dev, vb.bitmap, nk, new_cap, fc);
     else
-        k_splat_emit<false><<<ls.splat_ctas, kEmitThreads, 0, st>>>(ctl, g, depth_dev, vb.bitmap,
-                                                                    vb.new_keys, new_cap, fc);
+        k_splat_emit<false, K><<<ls.splat_ctas, kEmitThreads, 0, st>>>(ctl, g, depth_dev, vb.bitmap, nk, new_cap, fc);
     if (events) cudaEventRecord(events[1], st);
-    cudaError_t e = sort_u32(vb.new_keys, nullptr, &ctl->n_new, ss, &ctl->status, ls.sort_ctas, st);
+    cudaError_t e = sort_keys(vb.new_keys, sizeof(K), 3 * g.kb, nullptr, &ctl->n_new, ss, &ctl->status,
+                              ls.sort_ctas, st);
     if (e != cudaSuccess) return e;
     if (events) cudaEventRecord(events[2], st);
-    MergeInputs in{vb.new_keys, nullptr, nullptr, &ctl->n_new, true};
-    e = merge_enqueue(ctl, g, vb, in, depth_dev, depth_u16, fc, ls, st, events ? events[3] : nullptr);
+    MergeInputs<K> in{nk, nullptr, nullptr, &ctl->n_new, true};
+    e = merge_enqueue<K>(ctl, g, vb, in, depth_dev, depth_u16, fc, ls, st, events ? events[3] : nullptr);
     if (events) cudaEventRecord(events[4], st);
     return e;
 }
 
-cudaError_t insert_filter_enqueue(DeviceCtl* ctl, const Geom& g, VolumeBuffers& vb,
-                                  const uint32_t* keys_dev, const unsigned int* n_dev,
-                                  const LaunchShape& ls, cudaStream_t st) {
+cudaError_t integrate_enqueue(DeviceCtl* ctl, const Geom& g, VolumeBuffers& vb, SortScratch& ss,
+                              const void* depth_dev, bool depth_u16, const kifi_camera& cam,
+                              const Mat4& world_to_eye, const LaunchShape& ls, cudaStream_t st,
+                              cudaEvent_t* events) {
+    if (vb.key_bytes == 8)
+        return integrate_enqueue_t<uint64_t>(ctl, g, vb, ss, depth_dev, depth_u16, cam, world_to_eye, ls, st,
+                                             events);
+    return integrate_enqueue_t<uint32_t>(ctl, g, vb, ss, depth_dev, depth_u16, cam, world_to_eye, ls, st, events);
+}
+
+cudaError_t insert_filter_enqueue(DeviceCtl* ctl, const Geom& g, VolumeBuffers& vb, const void* keys_dev,
+                                  const unsigned int* n_dev, const LaunchShape& ls, cudaStream_t st) {
     k_reset_new<<<1, 1, 0, st>>>(ctl);
-    k_insert_filter<<<ls.splat_ctas, 256, 0, st>>>(ctl, g, vb.bitmap, keys_dev, n_dev, vb.new_keys,
-                                                   vb.new_idx);
+    if (vb.key_bytes == 8)
+        k_insert_filter<uint64_t><<<ls.splat_ctas, 256, 0, st>>>(ctl, g, vb.bitmap, (const uint64_t*)keys_dev, n_dev,
+                                                                (uint64_t*)vb.new_keys, vb.new_idx);
+    else
+        k_insert_filter<uint32_t><<<ls.splat_ctas, 256, 0, st>>>(ctl, g, vb.bitmap, (const uint32_t*)keys_dev, n_dev,
+                                                                (uint32_t*)vb.new_keys, vb.new_idx);
     return cudaGetLastError();
 }
 
@@ -598,9 +668,13 @@ cudaError_t insert_filter_enqueue(DeviceCtl* ctl, const Geom& g, VolumeBuffers& 
 // from vals_dev[index], or Voxel() when vals_dev is null.
 cudaError_t insert_merge_enqueue(DeviceCtl* ctl, const Geom& g, VolumeBuffers& vb,
                                  const float2* vals_dev, const LaunchShape& ls, cudaStream_t st) {
-    MergeInputs in{vb.new_keys, vb.new_idx, vals_dev, &ctl->n_new, false};
     FrameConst fc{};
-    return merge_enqueue(ctl, g, vb, in, nullptr, false, fc, ls, st);
+    if (vb.key_bytes == 8) {
+        MergeInputs<uint64_t> in{(const uint64_t*)vb.new_keys, vb.new_idx, vals_dev, &ctl->n_new, false};
+        return merge_enqueue<uint64_t>(ctl, g, vb, in, nullptr, false, fc, ls, st);
+    }
+    MergeInputs<uint32_t> in{(const uint32_t*)vb.new_keys, vb.new_idx, vals_dev, &ctl->n_new, false};
+    return merge_enqueue<uint32_t>(ctl, g, vb, in, nullptr, false, fc, ls, st);
 }
 
 }  // namespace kifi

@@ -12,12 +12,14 @@
 namespace kifi {
 
 // ------------------------------------------------------------ radix sort
+// up to 8 digit passes: keys of up to 64 bits
+constexpr int kSortMaxPasses = 8;
 struct SortScratch {
-    unsigned int* hist = nullptr;           // [4][256] digit counts
-    unsigned int* tile_counter = nullptr;   // [4] dynamic tile ids per pass
+    unsigned int* hist = nullptr;           // [passes][256] digit counts
+    unsigned int* tile_counter = nullptr;   // [passes] dynamic tile ids per pass
     unsigned long long* epoch = nullptr;    // look-back generation tag
-    unsigned long long* lookback = nullptr; // [4][max_tiles][256]
-    uint32_t* alt_keys = nullptr;           // ping-pong buffers, max_n (+pad)
+    unsigned long long* lookback = nullptr; // [passes][max_tiles][256]
+    void* alt_keys = nullptr;               // ping-pong buffers, max_n (+pad), 8 bytes per key
     uint32_t* alt_vals = nullptr;
     unsigned int* status = nullptr;         // where timeouts are reported
     size_t max_tiles = 0, max_n = 0;
@@ -28,15 +30,21 @@ cudaError_t sort_scratch_alloc(SortScratch* s, size_t max_n);
 void sort_scratch_free(SortScratch* s);
 cudaError_t sort_u32(uint32_t* keys, uint32_t* vals, const unsigned int* n_dev, SortScratch& s,
                      unsigned int* status, int grid_ctas, cudaStream_t st);
+// keys of key_bytes (4 or 8) bytes holding key_bits significant bits: one
+// stable 8-bit digit pass per byte of significant bits, rounded up to an
+// even count so the result lands back in `keys`
+cudaError_t sort_keys(void* keys, int key_bytes, int key_bits, uint32_t* vals, const unsigned int* n_dev,
+                      SortScratch& s, unsigned int* status, int grid_ctas, cudaStream_t st);
 
 // ------------------------------------------------------------- integrate
 struct VolumeBuffers {
-    uint32_t* keys[2] = {nullptr, nullptr};
+    int key_bytes = 4;              // 4: 30-bit keys (uint32_t), 8: 64-bit keys (uint64_t)
+    void* keys[2] = {nullptr, nullptr};
     float2* vals[2] = {nullptr, nullptr};
     size_t cap = 0;                 // voxels per buffer (arrays hold cap + pad)
     uint32_t* bitmap = nullptr;     // res^3 occupancy bits
     size_t bitmap_words = 0;
-    uint32_t* new_keys = nullptr;   // keys new to the volume in this frame
+    void* new_keys = nullptr;       // keys new to the volume in this frame
     uint32_t* new_idx = nullptr;    // insert path: source position of each new key
     size_t new_cap = 0;
     unsigned long long* splits = nullptr;  // merge-path split of every output tile
@@ -64,8 +72,10 @@ int merge_blocks_per_sm();
 // flat_map::insert of n sorted unique device keys: filter out resident keys
 // (their values win) and collect (key, index) of the rest in new_keys /
 // new_idx; the caller sorts those pairs and then merges.
+// merge-path split slots a volume of `cap` voxels needs
+size_t merge_max_tiles(const VolumeBuffers& vb, size_t cap);
 cudaError_t insert_filter_enqueue(DeviceCtl* ctl, const Geom& g, VolumeBuffers& vb,
-                                  const uint32_t* keys_dev, const unsigned int* n_dev,
+                                  const void* keys_dev, const unsigned int* n_dev,
                                   const LaunchShape& ls, cudaStream_t st);
 cudaError_t insert_merge_enqueue(DeviceCtl* ctl, const Geom& g, VolumeBuffers& vb,
                                  const float2* vals_dev, const LaunchShape& ls, cudaStream_t st);
@@ -74,8 +84,7 @@ cudaError_t insert_merge_enqueue(DeviceCtl* ctl, const Geom& g, VolumeBuffers& v
 struct MeshCounts {
     unsigned long long n_verts;
     unsigned long long n_idx;
-    unsigned int missing_min;  // smallest triangle edge id without a vertex (or ~0u)
-    unsigned int pad;
+    unsigned long long missing_min;  // smallest triangle edge id without a vertex (or ~0)
 };
 
 struct MeshScratch {
@@ -86,18 +95,18 @@ struct MeshScratch {
     unsigned int* rows = nullptr;          // start index of each (z, y) key row
     MeshCounts* counts = nullptr;
     unsigned int* n_dev = nullptr;         // the voxel count the passes read
-    size_t cap = 0;
+    size_t cap = 0, rows_cap = 0;
 };
 
-cudaError_t mesh_scratch_reserve(MeshScratch* m, size_t n);
+cudaError_t mesh_scratch_reserve(MeshScratch* m, size_t n, int kb);
 void mesh_scratch_free(MeshScratch* m);
-cudaError_t mesh_count_enqueue(const uint32_t* keys, const float2* vals, size_t n_cap, int with_indices,
-                               MeshScratch& ms, int sms, cudaStream_t st);
-cudaError_t mesh_emit_enqueue(const Geom& g, const uint32_t* keys, const float2* vals, size_t n_cap,
+cudaError_t mesh_count_enqueue(const void* keys, int key_bytes, const float2* vals, size_t n_cap, int kb,
+                               int with_indices, MeshScratch& ms, int sms, cudaStream_t st);
+cudaError_t mesh_emit_enqueue(const Geom& g, const void* keys, int key_bytes, const float2* vals, size_t n_cap,
                               int with_indices, MeshScratch& ms, unsigned long long n_verts,
                               unsigned long long n_idx, float* verts_dev, uint32_t* idx_dev, int sms,
                               cudaStream_t st);
-cudaError_t mesh_snapshot_enqueue(const DeviceCtl* ctl, const VolumeBuffers& vb, uint32_t* keys, float2* vals,
+cudaError_t mesh_snapshot_enqueue(const DeviceCtl* ctl, const VolumeBuffers& vb, void* keys, float2* vals,
                                   size_t cap, unsigned int* n_dev, int sms, cudaStream_t st);
 
 // ------------------------------------------------------------------ ICP

@@ -36,10 +36,9 @@ namespace kifi {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr unsigned int kRows = 1u << 20;  // (z, y) rows of 10-bit fields
 
-__device__ __forceinline__ unsigned long long lower_bound_u32(const uint32_t* __restrict__ k,
-                                                              unsigned long long n, uint32_t t) {
+template <typename K>
+__device__ __forceinline__ unsigned long long lower_bound_key(const K* __restrict__ k, unsigned long long n, K t) {
     unsigned long long lo = 0, hi = n;
     while (lo < hi) {
         unsigned long long mid = (lo + hi) >> 1;
@@ -49,23 +48,25 @@ __device__ __forceinline__ unsigned long long lower_bound_u32(const uint32_t* __
     return lo;
 }
 
-// row_start[r] = first index whose key >> 10 >= r, for r in [0, 2^20]
-__global__ void k_row_directory(const uint32_t* __restrict__ keys, const unsigned int* __restrict__ n_dev,
+// row_start[r] = first index whose (z, y) row (key >> b) >= r, for r in [0, 2^2b]
+template <typename K>
+__global__ void k_row_directory(const K* __restrict__ keys, const unsigned int* __restrict__ n_dev, int b,
                                 unsigned int* __restrict__ row_start) {
     const unsigned long long n = *n_dev;
-    for (unsigned int r = blockIdx.x * blockDim.x + threadIdx.x; r <= kRows;
-         r += gridDim.x * blockDim.x)
-        row_start[r] = (unsigned int)lower_bound_u32(keys, n, r << 10);
+    const unsigned int rows = 1u << (2 * b);
+    for (unsigned int r = blockIdx.x * blockDim.x + threadIdx.x; r <= rows; r += gridDim.x * blockDim.x)
+        row_start[r] = (unsigned int)lower_bound_key<K>(keys, n, (K)r << b);
 }
 
 // upper_bound(keys, t) using the row directory: keys of t's row lie in
 // [row_start[r], row_start[r+1]) sorted by x.
-__device__ __forceinline__ unsigned int upper_bound_row(const uint32_t* __restrict__ keys,
+template <typename K>
+__device__ __forceinline__ unsigned int upper_bound_row(const K* __restrict__ keys,
                                                         const unsigned int* __restrict__ rs,
-                                                        uint32_t t, unsigned int n) {
-    const unsigned int r = t >> 10;
+                                                        K t, unsigned int n, const Codec<K>& cd) {
+    const unsigned long long r = cd.row(t);
     // a neighbour of a voxel on the last z slice lies past every key
-    if (r >= kRows) return n;
+    if (r >= (1ull << (2 * cd.b))) return n;
     unsigned int lo = rs[r], hi = rs[r + 1];
     while (lo < hi) {
         unsigned int mid = (lo + hi) >> 1;
@@ -76,9 +77,10 @@ __device__ __forceinline__ unsigned int upper_bound_row(const uint32_t* __restri
 }
 
 // neighbour pointer position after the reference's walk (see file comment)
-__device__ __forceinline__ unsigned int walk_ptr(const uint32_t* keys, const unsigned int* rs,
-                                                 uint32_t t, unsigned int n) {
-    unsigned int p = upper_bound_row(keys, rs, t, n) - 1u;
+template <typename K>
+__device__ __forceinline__ unsigned int walk_ptr(const K* keys, const unsigned int* rs, K t, unsigned int n,
+                                                 const Codec<K>& cd) {
+    unsigned int p = upper_bound_row<K>(keys, rs, t, n, cd) - 1u;
     return p < n - 2 ? p : n - 2;
 }
 
@@ -92,33 +94,33 @@ struct Cube {
 // Corner lookups of Mesher.cpp:122-132 (corners 0,1,2,4) and, when
 // kTris, :174-181 (corners 3,5,6,7).  Corner c = (c&1, c>>1&1, c>>2) in the
 // reference's voxels[] numbering: self, +x, +y, +xy, +z, +xz, +yz, +xyz.
-template <bool kTris>
-__device__ __forceinline__ void load_cube(const uint32_t* __restrict__ keys,
+template <bool kTris, typename K>
+__device__ __forceinline__ void load_cube(const K* __restrict__ keys,
                                           const float2* __restrict__ vals,
                                           const unsigned int* __restrict__ rs, unsigned int n,
-                                          unsigned int i, Cube& c) {
-    const uint32_t key = keys[i];
+                                          unsigned int i, Cube& c, const Codec<K>& cd) {
+    const K key = keys[i];
     const float2 zero = make_float2(0.0f, 0.0f);
     c.idx[0] = i;
     c.val[0] = vals[i];
     c.idx[1] = i + 1;
-    c.val[1] = keys[i + 1] == key + pack30(1, 0, 0) ? vals[i + 1] : zero;
-    const unsigned int iTop = walk_ptr(keys, rs, key + pack30(0, 1, 0), n);
-    const unsigned int iFront = walk_ptr(keys, rs, key + pack30(0, 0, 1), n);
+    c.val[1] = keys[i + 1] == key + cd.pack(1, 0, 0) ? vals[i + 1] : zero;
+    const unsigned int iTop = walk_ptr<K>(keys, rs, key + cd.pack(0, 1, 0), n, cd);
+    const unsigned int iFront = walk_ptr<K>(keys, rs, key + cd.pack(0, 0, 1), n, cd);
     c.idx[2] = iTop;
-    c.val[2] = keys[iTop] == key + pack30(0, 1, 0) ? vals[iTop] : zero;
+    c.val[2] = keys[iTop] == key + cd.pack(0, 1, 0) ? vals[iTop] : zero;
     c.idx[4] = iFront;
-    c.val[4] = keys[iFront] == key + pack30(0, 0, 1) ? vals[iFront] : zero;
+    c.val[4] = keys[iFront] == key + cd.pack(0, 0, 1) ? vals[iFront] : zero;
     if (kTris) {
-        const unsigned int iFT = walk_ptr(keys, rs, key + pack30(0, 1, 1), n);
+        const unsigned int iFT = walk_ptr<K>(keys, rs, key + cd.pack(0, 1, 1), n, cd);
         c.idx[6] = iFT;
-        c.val[6] = keys[iFT] == key + pack30(0, 1, 1) ? vals[iFT] : zero;
+        c.val[6] = keys[iFT] == key + cd.pack(0, 1, 1) ? vals[iFT] : zero;
         c.idx[3] = iTop + 1;
-        c.val[3] = keys[iTop + 1] == key + pack30(1, 1, 0) ? vals[iTop + 1] : zero;
+        c.val[3] = keys[iTop + 1] == key + cd.pack(1, 1, 0) ? vals[iTop + 1] : zero;
         c.idx[5] = iFront + 1;
-        c.val[5] = keys[iFront + 1] == key + pack30(1, 0, 1) ? vals[iFront + 1] : zero;
+        c.val[5] = keys[iFront + 1] == key + cd.pack(1, 0, 1) ? vals[iFront + 1] : zero;
         c.idx[7] = iFT + 1;
-        c.val[7] = keys[iFT + 1] == key + pack30(1, 1, 1) ? vals[iFT + 1] : zero;
+        c.val[7] = keys[iFT + 1] == key + cd.pack(1, 1, 1) ? vals[iFT + 1] : zero;
     }
 }
 
@@ -144,19 +146,20 @@ __device__ __forceinline__ int cube_case(const Cube& c) {
 }
 
 // flags per voxel: bits 0-2 vertex axes, bits 8-15 index count, 16-23 case
-template <bool kTris>
-__global__ void __launch_bounds__(kThreads) k_mesh_classify(const uint32_t* __restrict__ keys,
+template <bool kTris, typename K>
+__global__ void __launch_bounds__(kThreads) k_mesh_classify(const K* __restrict__ keys, int kb,
                                                             const float2* __restrict__ vals,
                                                             const unsigned int* __restrict__ rs,
                                                             const unsigned int* __restrict__ n_dev,
                                                             unsigned int* __restrict__ flags,
                                                             unsigned long long* __restrict__ counts) {
     const unsigned int n = *n_dev;
+    const Codec<K> cd(kb);
     for (unsigned int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
         unsigned int f = 0, nv = 0, ni = 0;
         if (i + 1 < n && vals[i].y != 0.0f) {
             Cube c;
-            load_cube<kTris>(keys, vals, rs, n, i, c);
+            load_cube<kTris, K>(keys, vals, rs, n, i, c, cd);
             const unsigned int axes = vertex_axes(c);
             nv = __popc(axes);
             f = axes;
@@ -180,8 +183,8 @@ __global__ void __launch_bounds__(kThreads) k_mesh_classify(const uint32_t* __re
 __constant__ unsigned char kEdgeCorner[12] = {4, 0, 0, 1, 6, 2, 2, 3, 5, 4, 0, 1};
 __constant__ unsigned char kEdgeAxis[12] = {0, 2, 0, 2, 0, 2, 0, 2, 1, 1, 1, 1};
 
-template <bool kTris>
-__global__ void __launch_bounds__(kThreads) k_mesh_emit(const uint32_t* __restrict__ keys,
+template <bool kTris, typename K>
+__global__ void __launch_bounds__(kThreads) k_mesh_emit(const K* __restrict__ keys, int kb,
                                                         const float2* __restrict__ vals,
                                                         const unsigned int* __restrict__ rs,
                                                         const unsigned int* __restrict__ n_dev, Geom g,
@@ -189,24 +192,25 @@ __global__ void __launch_bounds__(kThreads) k_mesh_emit(const uint32_t* __restri
                                                         const unsigned long long* __restrict__ scan,
                                                         unsigned long long n_verts,
                                                         unsigned long long n_idx,
-                                                        unsigned int missing_bound,
-                                                        const unsigned int* __restrict__ missing_bound_dev,
+                                                        unsigned long long missing_bound,
+                                                        const unsigned long long* __restrict__ missing_bound_dev,
                                                         float* __restrict__ verts,
                                                         uint32_t* __restrict__ idx,
-                                                        unsigned int* __restrict__ missing_min) {
+                                                        unsigned long long* __restrict__ missing_min) {
     const unsigned int n = *n_dev;
+    const Codec<K> cd(kb);
     // a re-run for the index mapping's stop rule takes its bound from the first run, and only
     // when that run found a missing vertex
     if (missing_bound_dev) {
         missing_bound = *missing_bound_dev;
-        if (missing_bound == 0xffffffffu) return;
+        if (missing_bound == ~0ull) return;
     }
     for (unsigned int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
         const unsigned int f = flags[i];
         if (f == 0) continue;
         Cube c;
-        load_cube<kTris>(keys, vals, rs, n, i, c);
-        const uint32_t key = keys[i];
+        load_cube<kTris, K>(keys, vals, rs, n, i, c, cd);
+        const K key = keys[i];
         const unsigned long long s = scan[i];
         const unsigned int vbase = (unsigned int)(s & 0xffffffffu);
         const unsigned int axes = f & 7u;
@@ -215,9 +219,9 @@ __global__ void __launch_bounds__(kThreads) k_mesh_emit(const uint32_t* __restri
             const unsigned int nv = __popc(axes);
             const unsigned long long first =
                 kTris ? vbase : n_verts - vbase - nv;  // ascending ids / generation order
-            const float cx = fadd(fmul((float)(int)key_x(key), g.vlen), g.center_off);
-            const float cy = fadd(fmul((float)(int)key_y(key), g.vlen), g.center_off);
-            const float cz = fadd(fmul((float)(int)key_z(key), g.vlen), g.center_off);
+            const float cx = fadd(fmul((float)(int)cd.x(key), g.vlen), g.center_off);
+            const float cy = fadd(fmul((float)(int)cd.y(key), g.vlen), g.center_off);
+            const float cz = fadd(fmul((float)(int)cd.z(key), g.vlen), g.center_off);
             const float dself = vdist(c.val[0]);
             const int nb[3] = {1, 2, 4};
             unsigned int r = 0;
@@ -241,24 +245,27 @@ __global__ void __launch_bounds__(kThreads) k_mesh_emit(const uint32_t* __restri
         const int lut = (int)(f >> 16 & 0xffu);
         const unsigned int ibase = (unsigned int)(s >> 32);
         const unsigned long long first = n_idx - ibase - ni;  // generation order
-        unsigned int local_min = 0xffffffffu;
+        unsigned long long local_min = ~0ull;
         for (unsigned int t = 0; t < ni; ++t) {
             const int e = mc_tri_edge(lut, (int)t);
             const int corner = kEdgeCorner[e], axis = kEdgeAxis[e];
             const unsigned int ci = c.idx[corner];
-            const uint32_t id = 3u * keys[ci] + (uint32_t)axis;
+            // the edge id 3 * key + axis: 32 bits wide for 30-bit keys (as in the
+            // reference); for 64-bit keys the stop rule compares full ids and an id
+            // written in place of a missing vertex keeps its low 32 bits
+            const unsigned long long id = 3ull * (unsigned long long)keys[ci] + (unsigned long long)axis;
             const unsigned int cf = flags[ci];
             uint32_t outv;
             if (cf >> axis & 1u) {
                 outv = (unsigned int)(scan[ci] & 0xffffffffu) + __popc(cf & 7u & ((1u << axis) - 1u));
             } else {
-                outv = id;
+                outv = (uint32_t)id;
                 local_min = min(local_min, id);
             }
-            if (id >= missing_bound) outv = id;
+            if (id >= missing_bound) outv = (uint32_t)id;
             idx[first + t] = outv;
         }
-        if (local_min != 0xffffffffu && missing_min) atomicMin(missing_min, local_min);
+        if (local_min != ~0ull && missing_min) atomicMin(missing_min, local_min);
     }
 }
 
@@ -332,7 +339,7 @@ __global__ void __launch_bounds__(kThreads) k_scan_sums(unsigned long long* __re
     if (threadIdx.x == 0) {
         counts->n_verts = carry & 0xffffffffull;
         counts->n_idx = carry >> 32;
-        counts->missing_min = 0xffffffffu;
+        counts->missing_min = ~0ull;
     }
 }
 
@@ -348,8 +355,10 @@ __global__ void __launch_bounds__(kThreads) k_scan_add(unsigned long long* __res
 
 }  // namespace
 
-cudaError_t mesh_scratch_reserve(MeshScratch* m, size_t n) {
-    if (m->cap >= n && m->vflags) return cudaSuccess;
+cudaError_t mesh_scratch_reserve(MeshScratch* m, size_t n, int kb) {
+    const size_t rows = ((size_t)1 << (2 * kb)) + 1;
+    if (m->cap >= n && m->vflags && m->rows_cap >= rows) return cudaSuccess;
+    if (n < m->cap) n = m->cap;
     mesh_scratch_free(m);
     size_t cap = n < 1024 ? 1024 : n;
     cudaError_t e;
@@ -357,7 +366,8 @@ cudaError_t mesh_scratch_reserve(MeshScratch* m, size_t n) {
     if ((e = cudaMalloc(&m->vscan, cap * sizeof(unsigned long long)))) return e;
     if ((e = cudaMalloc(&m->tscan, cap * sizeof(unsigned long long)))) return e;
     if ((e = cudaMalloc(&m->block_sums, ((cap + kScanTile - 1) / kScanTile + 1) * 8))) return e;
-    if ((e = cudaMalloc(&m->rows, (kRows + 1) * sizeof(unsigned int)))) return e;
+    if ((e = cudaMalloc(&m->rows, rows * sizeof(unsigned int)))) return e;
+    m->rows_cap = rows;
     if ((e = cudaMalloc(&m->counts, sizeof(MeshCounts)))) return e;
     if ((e = cudaMalloc(&m->n_dev, sizeof(unsigned int)))) return e;
     m->cap = cap;
@@ -383,57 +393,78 @@ static int grid_for(size_t n, int sms) {
 
 // The voxel count is read on the device from ms.n_dev (<= n_cap, which sizes
 // the grids), so the passes can be enqueued before the count is known.
-cudaError_t mesh_count_enqueue(const uint32_t* keys, const float2* vals, size_t n_cap, int with_indices,
-                               MeshScratch& ms, int sms, cudaStream_t st) {
+template <typename K>
+static void mesh_count_t(const K* keys, const float2* vals, size_t n_cap, int kb, int with_indices, MeshScratch& ms,
+                         int sms, cudaStream_t st) {
     // vscan holds the per-voxel packed counts, tscan their exclusive scan
     unsigned long long* cnt = ms.vscan;
     unsigned long long* scan = ms.tscan;
-    k_row_directory<<<grid_for(kRows + 1, sms), kThreads, 0, st>>>(keys, ms.n_dev, ms.rows);
+    k_row_directory<K><<<grid_for(((size_t)1 << (2 * kb)) + 1, sms), kThreads, 0, st>>>(keys, ms.n_dev, kb, ms.rows);
     if (with_indices)
-        k_mesh_classify<true><<<grid_for(n_cap, sms), kThreads, 0, st>>>(keys, vals, ms.rows, ms.n_dev, ms.vflags,
-                                                                          cnt);
+        k_mesh_classify<true, K><<<grid_for(n_cap, sms), kThreads, 0, st>>>(keys, kb, vals, ms.rows, ms.n_dev,
+                                                                             ms.vflags, cnt);
     else
-        k_mesh_classify<false><<<grid_for(n_cap, sms), kThreads, 0, st>>>(keys, vals, ms.rows, ms.n_dev, ms.vflags,
-                                                                           cnt);
+        k_mesh_classify<false, K><<<grid_for(n_cap, sms), kThreads, 0, st>>>(keys, kb, vals, ms.rows, ms.n_dev,
+                                                                              ms.vflags, cnt);
     const unsigned int n_tiles = (unsigned int)((n_cap + kScanTile - 1) / kScanTile);
     k_scan_tiles<<<n_tiles ? n_tiles : 1, kThreads, 0, st>>>(cnt, scan, ms.block_sums, ms.n_dev);
     k_scan_sums<<<1, kThreads, 0, st>>>(ms.block_sums, n_tiles ? n_tiles : 1, ms.n_dev, ms.counts);
     k_scan_add<<<n_tiles ? n_tiles : 1, kThreads, 0, st>>>(scan, ms.block_sums, ms.n_dev);
+}
+
+cudaError_t mesh_count_enqueue(const void* keys, int key_bytes, const float2* vals, size_t n_cap, int kb,
+                               int with_indices, MeshScratch& ms, int sms, cudaStream_t st) {
+    if (key_bytes == 8) mesh_count_t<uint64_t>((const uint64_t*)keys, vals, n_cap, kb, with_indices, ms, sms, st);
+    else mesh_count_t<uint32_t>((const uint32_t*)keys, vals, n_cap, 10, with_indices, ms, sms, st);
     return cudaGetLastError();
 }
 
 // Both emit passes: the first records the smallest edge id without a vertex
 // in ms.counts->missing_min; the second (the index mapping's stop rule)
 // re-emits with that bound and does nothing when the first found none.
-cudaError_t mesh_emit_enqueue(const Geom& g, const uint32_t* keys, const float2* vals, size_t n_cap,
+template <typename K>
+static void mesh_emit_t(const Geom& g, const K* keys, const float2* vals, size_t n_cap, int with_indices,
+                        MeshScratch& ms, unsigned long long n_verts, unsigned long long n_idx, float* verts_dev,
+                        uint32_t* idx_dev, int sms, cudaStream_t st) {
+    const unsigned long long* scan = ms.tscan;
+    unsigned long long* mm = &ms.counts->missing_min;
+    const int kb = sizeof(K) == 4 ? 10 : g.kb;
+    if (with_indices) {
+        k_mesh_emit<true, K><<<grid_for(n_cap, sms), kThreads, 0, st>>>(keys, kb, vals, ms.rows, ms.n_dev, g,
+                                                                         ms.vflags, scan, n_verts, n_idx,
+                                                                         ~0ull, nullptr, verts_dev, idx_dev, mm);
+        k_mesh_emit<true, K><<<grid_for(n_cap, sms), kThreads, 0, st>>>(keys, kb, vals, ms.rows, ms.n_dev, g,
+                                                                         ms.vflags, scan, n_verts, n_idx, 0ull, mm,
+                                                                         verts_dev, idx_dev, nullptr);
+    } else {
+        k_mesh_emit<false, K><<<grid_for(n_cap, sms), kThreads, 0, st>>>(keys, kb, vals, ms.rows, ms.n_dev, g,
+                                                                          ms.vflags, scan, n_verts, n_idx,
+                                                                          ~0ull, nullptr, verts_dev, idx_dev, mm);
+    }
+}
+
+cudaError_t mesh_emit_enqueue(const Geom& g, const void* keys, int key_bytes, const float2* vals, size_t n_cap,
                               int with_indices, MeshScratch& ms, unsigned long long n_verts,
                               unsigned long long n_idx, float* verts_dev, uint32_t* idx_dev, int sms,
                               cudaStream_t st) {
-    const unsigned long long* scan = ms.tscan;
-    unsigned int* mm = &ms.counts->missing_min;
-    if (with_indices) {
-        k_mesh_emit<true><<<grid_for(n_cap, sms), kThreads, 0, st>>>(keys, vals, ms.rows, ms.n_dev, g, ms.vflags,
-                                                                      scan, n_verts, n_idx, 0xffffffffu, nullptr,
-                                                                      verts_dev, idx_dev, mm);
-        k_mesh_emit<true><<<grid_for(n_cap, sms), kThreads, 0, st>>>(keys, vals, ms.rows, ms.n_dev, g, ms.vflags,
-                                                                      scan, n_verts, n_idx, 0u, mm, verts_dev,
-                                                                      idx_dev, nullptr);
-    } else {
-        k_mesh_emit<false><<<grid_for(n_cap, sms), kThreads, 0, st>>>(keys, vals, ms.rows, ms.n_dev, g, ms.vflags,
-                                                                       scan, n_verts, n_idx, 0xffffffffu, nullptr,
-                                                                       verts_dev, idx_dev, mm);
-    }
+    if (key_bytes == 8)
+        mesh_emit_t<uint64_t>(g, (const uint64_t*)keys, vals, n_cap, with_indices, ms, n_verts, n_idx, verts_dev,
+                              idx_dev, sms, st);
+    else
+        mesh_emit_t<uint32_t>(g, (const uint32_t*)keys, vals, n_cap, with_indices, ms, n_verts, n_idx, verts_dev,
+                              idx_dev, sms, st);
     return cudaGetLastError();
 }
 
 // Copy of the resident voxels (buffer ctl->cur, ctl->n[cur] of them) for a
 // mesh that runs while fusion goes on; the count goes to *n_dev.
-__global__ void k_mesh_snapshot(const DeviceCtl* __restrict__ ctl, VolumeBuffers vb, uint32_t* __restrict__ keys,
+template <typename K>
+__global__ void k_mesh_snapshot(const DeviceCtl* __restrict__ ctl, VolumeBuffers vb, K* __restrict__ keys,
                                 float2* __restrict__ vals, unsigned long long cap, unsigned int* __restrict__ n_dev) {
     const unsigned int cur = ctl->cur;
     unsigned long long n = ctl->n[cur];
     if (n > cap) n = cap;
-    const uint32_t* sk = cur ? vb.keys[1] : vb.keys[0];
+    const K* sk = (const K*)(cur ? vb.keys[1] : vb.keys[0]);
     const float2* sv = cur ? vb.vals[1] : vb.vals[0];
     for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (unsigned long long)gridDim.x * blockDim.x) {
@@ -443,9 +474,12 @@ __global__ void k_mesh_snapshot(const DeviceCtl* __restrict__ ctl, VolumeBuffers
     if (blockIdx.x == 0 && threadIdx.x == 0) *n_dev = (unsigned int)n;
 }
 
-cudaError_t mesh_snapshot_enqueue(const DeviceCtl* ctl, const VolumeBuffers& vb, uint32_t* keys, float2* vals,
+cudaError_t mesh_snapshot_enqueue(const DeviceCtl* ctl, const VolumeBuffers& vb, void* keys, float2* vals,
                                   size_t cap, unsigned int* n_dev, int sms, cudaStream_t st) {
-    k_mesh_snapshot<<<sms * 4, 256, 0, st>>>(ctl, vb, keys, vals, cap, n_dev);
+    if (vb.key_bytes == 8)
+        k_mesh_snapshot<uint64_t><<<sms * 4, 256, 0, st>>>(ctl, vb, (uint64_t*)keys, vals, cap, n_dev);
+    else
+        k_mesh_snapshot<uint32_t><<<sms * 4, 256, 0, st>>>(ctl, vb, (uint32_t*)keys, vals, cap, n_dev);
     return cudaGetLastError();
 }
 

@@ -42,29 +42,28 @@ constexpr unsigned long long kFlagAggregate = 1ull << 30;
 constexpr unsigned long long kFlagInclusive = 2ull << 30;
 constexpr unsigned long long kCountMask = (1ull << 30) - 1;
 
-__global__ void k_sort_prepare(SortScratch s) {
-    for (int i = threadIdx.x; i < 4 * kRadix; i += blockDim.x) s.hist[i] = 0u;
-    if (threadIdx.x < 4) s.tile_counter[threadIdx.x] = 0u;
+__global__ void k_sort_prepare(SortScratch s, int passes) {
+    for (int i = threadIdx.x; i < passes * kRadix; i += blockDim.x) s.hist[i] = 0u;
+    if (threadIdx.x < passes) s.tile_counter[threadIdx.x] = 0u;
     if (threadIdx.x == 0) *s.epoch += 1ull;
 }
 
-__global__ void __launch_bounds__(kThreads) k_sort_histogram(const uint32_t* __restrict__ keys,
+// all `passes` digit histograms in one read of the keys
+template <typename K>
+__global__ void __launch_bounds__(kThreads) k_sort_histogram(const K* __restrict__ keys,
                                                              const unsigned int* __restrict__ n_ptr,
-                                                             SortScratch s) {
-    __shared__ unsigned int h[4][kRadix];
-    for (int i = threadIdx.x; i < 4 * kRadix; i += kThreads) (&h[0][0])[i] = 0u;
+                                                             SortScratch s, int passes) {
+    __shared__ unsigned int h[kSortMaxPasses][kRadix];
+    for (int i = threadIdx.x; i < passes * kRadix; i += kThreads) (&h[0][0])[i] = 0u;
     __syncthreads();
     const size_t n = min((size_t)*n_ptr, s.max_n);
     for (size_t i = (size_t)blockIdx.x * kThreads + threadIdx.x; i < n;
          i += (size_t)gridDim.x * kThreads) {
-        uint32_t k = keys[i];
-        atomicAdd(&h[0][k & 0xffu], 1u);
-        atomicAdd(&h[1][(k >> 8) & 0xffu], 1u);
-        atomicAdd(&h[2][(k >> 16) & 0xffu], 1u);
-        atomicAdd(&h[3][k >> 24], 1u);
+        const K k = keys[i];
+        for (int p = 0; p < passes; ++p) atomicAdd(&h[p][(unsigned int)(k >> (8 * p)) & 0xffu], 1u);
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < 4 * kRadix; i += kThreads) {
+    for (int i = threadIdx.x; i < passes * kRadix; i += kThreads) {
         unsigned int c = (&h[0][0])[i];
         if (c) atomicAdd(&s.hist[i], c);
     }
@@ -85,9 +84,9 @@ __device__ __forceinline__ void st_volatile_u64(unsigned long long* p, unsigned 
     asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
-template <bool kWithValues>
-__global__ void __launch_bounds__(kThreads) k_sort_pass(const uint32_t* __restrict__ keys_in,
-                                                        uint32_t* __restrict__ keys_out,
+template <bool kWithValues, typename K>
+__global__ void __launch_bounds__(kThreads) k_sort_pass(const K* __restrict__ keys_in,
+                                                        K* __restrict__ keys_out,
                                                         const uint32_t* __restrict__ vals_in,
                                                         uint32_t* __restrict__ vals_out,
                                                         const unsigned int* __restrict__ n_ptr,
@@ -130,16 +129,17 @@ __global__ void __launch_bounds__(kThreads) k_sort_pass(const uint32_t* __restri
         if (tile >= n_tiles) break;
 
         const unsigned int base = tile * kTile + warp * (32 * kKeysPerThread);
-        uint32_t k[kKeysPerThread], v[kKeysPerThread];
+        K k[kKeysPerThread];
+        uint32_t v[kKeysPerThread];
         unsigned int rank[kKeysPerThread];
         int dig[kKeysPerThread];
 #pragma unroll
         for (int j = 0; j < kKeysPerThread; ++j) {
             unsigned int i = base + j * 32 + lane;
             bool ok = i < n;
-            k[j] = ok ? keys_in[i] : 0u;
+            k[j] = ok ? keys_in[i] : (K)0;
             if (kWithValues) v[j] = ok ? vals_in[i] : 0u;
-            dig[j] = ok ? (int)((k[j] >> shift) & 0xffu) : kRadix;
+            dig[j] = ok ? (int)((unsigned int)(k[j] >> shift) & 0xffu) : kRadix;
         }
         // stable warp-local ranks: lanes with equal digits, in (j, lane) order
 #pragma unroll
@@ -210,14 +210,14 @@ cudaError_t sort_scratch_alloc(SortScratch* s, size_t max_n) {
     s->max_tiles = sort_max_tiles(max_n);
     s->max_n = max_n;
     cudaError_t e;
-    if ((e = cudaMalloc(&s->hist, 4 * kRadix * sizeof(unsigned int) + 64))) return e;
+    if ((e = cudaMalloc(&s->hist, kSortMaxPasses * kRadix * sizeof(unsigned int) + 64))) return e;
     if ((e = cudaMalloc(&s->tile_counter, 8 * sizeof(unsigned int)))) return e;
     if ((e = cudaMalloc(&s->epoch, sizeof(unsigned long long)))) return e;
     if ((e = cudaMemset(s->epoch, 0, sizeof(unsigned long long)))) return e;
-    size_t lb = 4 * s->max_tiles * kRadix * sizeof(unsigned long long);
+    size_t lb = kSortMaxPasses * s->max_tiles * kRadix * sizeof(unsigned long long);
     if ((e = cudaMalloc(&s->lookback, lb))) return e;
     if ((e = cudaMemset(s->lookback, 0, lb))) return e;
-    if ((e = cudaMalloc(&s->alt_keys, (max_n + 64) * sizeof(uint32_t)))) return e;
+    if ((e = cudaMalloc(&s->alt_keys, (max_n + 64) * sizeof(uint64_t)))) return e;
     if ((e = cudaMalloc(&s->alt_vals, (max_n + 64) * sizeof(uint32_t)))) return e;
     return cudaSuccess;
 }
@@ -232,24 +232,46 @@ void sort_scratch_free(SortScratch* s) {
     *s = SortScratch{};
 }
 
-// Sorts keys[0..*n_dev) (and vals, when not null) in place.  *n_dev must not
-// exceed s->max_n.  Four passes leave the result in the caller's buffers.
-cudaError_t sort_u32(uint32_t* keys, uint32_t* vals, const unsigned int* n_dev, SortScratch& s,
-                     unsigned int* status, int grid_ctas, cudaStream_t st) {
+template <typename K>
+static cudaError_t sort_t(K* keys, int passes, uint32_t* vals, const unsigned int* n_dev, SortScratch& s,
+                          unsigned int* status, int grid_ctas, cudaStream_t st) {
     s.status = status;
-    k_sort_prepare<<<1, 256, 0, st>>>(s);
-    k_sort_histogram<<<grid_ctas, kThreads, 0, st>>>(keys, n_dev, s);
-    uint32_t *ki = keys, *ko = s.alt_keys, *vi = vals, *vo = s.alt_vals;
-    for (int pass = 0; pass < 4; ++pass) {
+    k_sort_prepare<<<1, 256, 0, st>>>(s, passes);
+    k_sort_histogram<K><<<grid_ctas, kThreads, 0, st>>>(keys, n_dev, s, passes);
+    K *ki = keys, *ko = (K*)s.alt_keys;
+    uint32_t *vi = vals, *vo = s.alt_vals;
+    for (int pass = 0; pass < passes; ++pass) {
         if (vals)
-            k_sort_pass<true><<<grid_ctas, kThreads, 0, st>>>(ki, ko, vi, vo, n_dev, s, pass);
+            k_sort_pass<true, K><<<grid_ctas, kThreads, 0, st>>>(ki, ko, vi, vo, n_dev, s, pass);
         else
-            k_sort_pass<false><<<grid_ctas, kThreads, 0, st>>>(ki, ko, nullptr, nullptr, n_dev, s,
-                                                               pass);
-        uint32_t* t = ki; ki = ko; ko = t;
-        t = vi; vi = vo; vo = t;
+            k_sort_pass<false, K><<<grid_ctas, kThreads, 0, st>>>(ki, ko, nullptr, nullptr, n_dev, s, pass);
+        K* t = ki;
+        ki = ko;
+        ko = t;
+        uint32_t* tv = vi;
+        vi = vo;
+        vo = tv;
     }
     return cudaGetLastError();
+}
+
+// Sorts keys[0..*n_dev) (and vals, when not null) in place.  *n_dev must not
+// exceed s.max_n.  An even number of passes leaves the result in the
+// caller's buffers.
+cudaError_t sort_u32(uint32_t* keys, uint32_t* vals, const unsigned int* n_dev, SortScratch& s,
+                     unsigned int* status, int grid_ctas, cudaStream_t st) {
+    return sort_t<uint32_t>(keys, 4, vals, n_dev, s, status, grid_ctas, st);
+}
+
+cudaError_t sort_keys(void* keys, int key_bytes, int key_bits, uint32_t* vals, const unsigned int* n_dev,
+                      SortScratch& s, unsigned int* status, int grid_ctas, cudaStream_t st) {
+    int passes = (key_bits + 7) / 8;
+    passes += passes & 1;
+    if (passes < 2) passes = 2;
+    if (key_bytes == 8)
+        return sort_t<uint64_t>((uint64_t*)keys, passes > kSortMaxPasses ? kSortMaxPasses : passes, vals, n_dev, s,
+                                status, grid_ctas, st);
+    return sort_t<uint32_t>((uint32_t*)keys, passes > 4 ? 4 : passes, vals, n_dev, s, status, grid_ctas, st);
 }
 
 }  // namespace kifi

@@ -82,10 +82,12 @@ class Volume:
 
     ``Volume(resolution, sideLength, truncationMargin)``; the cube is centred
     at the world origin.  Voxels are (distance-sum, weight) pairs keyed by
-    30-bit linear keys z<<20 | y<<10 | x."""
+    30-bit linear keys z<<20 | y<<10 | x up to 1024 voxels per axis, and by
+    64-bit keys z<<2b | y<<b | x (b = max(10, log2 resolution)) beyond, or
+    when ``key_bits=64``."""
 
     def __init__(self, resolution, side_length, truncation_margin, device=0, capacity=0,
-                 stream=None):
+                 stream=None, key_bits=0):
         self._h = None
         d = VolumeDesc()
         d.resolution = int(resolution)
@@ -94,9 +96,13 @@ class Volume:
         d.initial_capacity = int(capacity)
         d.device = int(device)
         d.stream = stream
+        d.key_bits = int(key_bits)
         h = C.c_void_p()
         check(_lib.load().kifi_volume_create(C.byref(d), C.byref(h)), "Volume")
         self._h = h
+        kb, b = C.c_int(), C.c_int()
+        check(_lib.load().kifi_volume_key_bits(h, C.byref(kb), C.byref(b)), "key_bits")
+        self.key_bits, self.bits_per_axis = kb.value, b.value
         self._res = int(resolution)
         self._side = np.float32(side_length)
         self._trunc = np.float32(truncation_margin)
@@ -137,22 +143,26 @@ class Volume:
         check(_lib.load().kifi_volume_size(self._h, C.byref(n)), "size")
         return n.value
 
-    def export(self):
-        """(keys uint32 (n,), values float32 (n, 2) = (distance-sum, weight))."""
+    def export(self, key_bits=None):
+        """(keys (n,), values float32 (n, 2) = (distance-sum, weight)); keys
+        uint32 or uint64 (``key_bits``, default the volume's own width)."""
+        wide = (key_bits or self.key_bits) == 64
         n = self.size()
-        keys = np.zeros(n + 1, np.uint32)
+        keys = np.zeros(n + 1, np.uint64 if wide else np.uint32)
         vals = np.zeros((n + 1, 2), np.float32)
         got = C.c_size_t()
-        check(_lib.load().kifi_volume_export(self._h, _ptr(keys), _ptr(vals), n + 1,
-                                             C.byref(got)), "export")
+        fn = _lib.load().kifi_volume_export64 if wide else _lib.load().kifi_volume_export
+        check(fn(self._h, _ptr(keys), _ptr(vals), n + 1, C.byref(got)), "export")
         return keys[:got.value].copy(), vals[:got.value].copy()
 
     def insert(self, keys, values=None):
-        """flat_map::insert: union with sorted unique keys; resident voxels win."""
-        k = np.ascontiguousarray(keys, dtype=np.uint32)
+        """flat_map::insert: union with sorted unique keys; resident voxels win.
+        uint64 keys go through the 64-bit entry point, others as uint32."""
+        wide = np.asarray(keys).dtype == np.uint64
+        k = np.ascontiguousarray(keys, dtype=np.uint64 if wide else np.uint32)
         v = None if values is None else np.ascontiguousarray(values, dtype=np.float32)
-        check(_lib.load().kifi_volume_insert(self._h, _ptr(k), None if v is None else _ptr(v),
-                                             k.size), "insert")
+        fn = _lib.load().kifi_volume_insert64 if wide else _lib.load().kifi_volume_insert
+        check(fn(self._h, _ptr(k), None if v is None else _ptr(v), k.size), "insert")
 
     def clear(self):
         check(_lib.load().kifi_volume_clear(self._h), "clear")
@@ -194,6 +204,9 @@ class Volume:
         self._res = int(np.frombuffer(hdr[8:12], np.int32)[0])
         self._side = np.frombuffer(hdr[12:16], np.float32)[0]
         self._trunc = np.frombuffer(hdr[16:20], np.float32)[0]
+        kb, b = C.c_int(), C.c_int()
+        check(lib.kifi_volume_key_bits(h, C.byref(kb), C.byref(b)), "key_bits")
+        self.key_bits, self.bits_per_axis = kb.value, b.value
         return self
 
 
@@ -334,14 +347,18 @@ class Renderer:
 
 
 def radix_sort(keys, values=None):
-    """util::radix_sort on the GPU (algorithm.h:63-134)."""
-    k = np.ascontiguousarray(keys, dtype=np.uint32).copy()
+    """util::radix_sort on the GPU (algorithm.h:63-134); uint64 keys sort
+    with the 64-bit variant, anything else as uint32."""
+    wide = np.asarray(keys).dtype == np.uint64
+    k = np.ascontiguousarray(keys, dtype=np.uint64 if wide else np.uint32).copy()
     lib = _lib.load()
     if values is None:
-        check(lib.kifi_radix_sort_u32(_ptr(k), k.size), "radix_sort")
+        fn = lib.kifi_radix_sort_u64 if wide else lib.kifi_radix_sort_u32
+        check(fn(_ptr(k), k.size), "radix_sort")
         return k
     v = np.ascontiguousarray(values, dtype=np.uint32).copy()
-    check(lib.kifi_radix_sort_pairs_u32(_ptr(k), _ptr(v), k.size), "radix_sort")
+    fn = lib.kifi_radix_sort_pairs_u64 if wide else lib.kifi_radix_sort_pairs_u32
+    check(fn(_ptr(k), _ptr(v), k.size), "radix_sort")
     return k, v
 
 

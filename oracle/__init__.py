@@ -1,7 +1,8 @@
 """Test infrastructure: the CPU oracle for the depth-fusion path.
 
-* ``oracle/kifi_oracle.c`` -- the C restatement of the reference algorithm
-  (built into ``oracle/_build/libkifi_oracle.so``), wrapped by
+* ``oracle/kifi_oracle.c`` -- the C restatement of the reference algorithm,
+  and ``oracle/kifi_oracle_k64.c``, its fusion path with 64-bit voxel keys
+  (both built into ``oracle/_build/libkifi_oracle.so``), wrapped by
   ``oracle.cpu``.
 * ``oracle/_ref`` -- the reference's own CPU code compiled by
   ``oracle/build_ref.py``, wrapped by ``oracle.ref``.
@@ -19,9 +20,9 @@ ORACLE_LIB = os.path.join(BUILD, "libkifi_oracle.so")
 
 def build_oracle():
     os.makedirs(BUILD, exist_ok=True)
-    src = os.path.join(HERE, "kifi_oracle.c")
+    srcs = [os.path.join(HERE, f) for f in ("kifi_oracle.c", "kifi_oracle_k64.c")]
     cmd = ["gcc", "-std=c11", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
-           "-Wall", "-Wno-unused-function", "-o", ORACLE_LIB, src, "-lm"]
+           "-Wall", "-Wno-unused-function", "-o", ORACLE_LIB] + srcs + ["-lm"]
     subprocess.check_call(cmd)
     return ORACLE_LIB
 

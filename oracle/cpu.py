@@ -41,6 +41,8 @@ def lib():
         _lib.or_set_union_i32.restype = C.c_size_t
         _lib.or_insert.restype = C.c_size_t
         _lib.or_kahan_sum.restype = C.c_float
+        for f in ("or64_splat", "or64_unique", "or64_expand", "or64_insert", "or64_integrate"):
+            getattr(_lib, f).restype = C.c_size_t
     return _lib
 
 
@@ -161,6 +163,70 @@ class Volume:
         rc = lib().or_mesh(C.byref(self.g), _p(self.keys), _p(self.values), C.c_size_t(n),
                            C.c_int(1 if with_indices else 0), _p(verts), C.c_size_t(vcap), _p(idx),
                            C.c_size_t(icap), C.byref(nv), C.byref(ni))
+        assert rc == 0
+        return verts[:nv.value].copy(), idx[:ni.value].copy()
+
+
+def key_bits_per_axis(res):
+    """b of the 64-bit keys z<<2b | y<<b | x: max(10, log2 res)."""
+    b = 10
+    while (1 << b) < res:
+        b += 1
+    return b
+
+
+def splat64(res, side, trunc, depth, cam, world_to_eye):
+    depth, w2e = f32(depth), f32(world_to_eye)
+    out = np.zeros(cam[0] * cam[1] + 1, np.uint64)
+    g = geom(res, side, trunc)
+    n = lib().or64_splat(C.byref(g), C.c_int(key_bits_per_axis(res)), _p(depth), C.byref(cam_struct(cam)),
+                         _p(w2e), _p(out))
+    return out[:n].copy()
+
+
+def radix_sort64(keys):
+    k = np.ascontiguousarray(keys, dtype=np.uint64).copy()
+    lib().or64_radix_sort(_p(k), C.c_size_t(k.size))
+    return k
+
+
+def expand64(sorted_unique_keys, b):
+    k = np.ascontiguousarray(sorted_unique_keys, dtype=np.uint64)
+    out = np.zeros(8 * k.size + 1, np.uint64)
+    n = lib().or64_expand(_p(k), C.c_size_t(k.size), C.c_int(b), _p(out))
+    return out[:n].copy()
+
+
+class Volume64(Volume):
+    """The same volume keyed by 64-bit keys z<<2b | y<<b | x."""
+
+    def __init__(self, res, side, trunc):
+        super().__init__(res, side, trunc)
+        self.b = key_bits_per_axis(res)
+        self.keys = np.zeros(0, np.uint64)
+
+    def integrate(self, depth, cam, world_to_eye):
+        depth, w2e = f32(depth), f32(world_to_eye)
+        n0 = self.keys.size
+        cap = n0 + 8 * cam[0] * cam[1] + 1
+        ok = np.zeros(cap, np.uint64)
+        ov = np.zeros((cap, 2), np.float32)
+        rk = np.ascontiguousarray(self.keys)
+        rv = np.ascontiguousarray(self.values)
+        n1 = lib().or64_integrate(C.byref(self.g), C.c_int(self.b), _p(depth), C.byref(cam_struct(cam)), _p(w2e),
+                                  _p(rk), _p(rv), C.c_size_t(n0), _p(ok), _p(ov))
+        self.keys = ok[:n1].copy()
+        self.values = ov[:n1].copy()
+
+    def mesh(self, with_indices=True):
+        n = self.keys.size
+        vcap, icap = 3 * n + 1, 15 * n + 1
+        verts = np.zeros((vcap, 3), np.float32)
+        idx = np.zeros(icap, np.uint32)
+        nv, ni = C.c_size_t(), C.c_size_t()
+        rc = lib().or64_mesh(C.byref(self.g), C.c_int(self.b), _p(self.keys), _p(self.values), C.c_size_t(n),
+                             C.c_int(1 if with_indices else 0), _p(verts), C.c_size_t(vcap), _p(idx),
+                             C.c_size_t(icap), C.byref(nv), C.byref(ni))
         assert rc == 0
         return verts[:nv.value].copy(), idx[:ni.value].copy()
 

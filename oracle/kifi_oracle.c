@@ -25,6 +25,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include "kifi_oracle.h"
+
 /* ------------------------------------------------------------------ math */
 
 /* float4x4 * float4: (c0*x + c1*y) + (c2*z + c3*w), lane by lane.
@@ -65,11 +67,6 @@ void or_invert_transform(const float* in, float* out) {
     memcpy(out, m, 64);
 }
 
-typedef struct {
-    int width, height;
-    float fx, fy, cx, cy;
-    float znear, zfar;
-} or_camera;
 
 /* DepthSensorParams::EyeToClipRH -- DepthSensorParams.cpp:47-63 */
 void or_eye_to_clip(const or_camera* c, float* out) {
@@ -87,14 +84,6 @@ void or_eye_to_clip(const or_camera* c, float* out) {
 
 /* --------------------------------------------------------------- volume */
 
-typedef struct {
-    int res;
-    float side, trunc;
-    float vlen;         /* side / res                     Volume.cpp:28 */
-    float center_off;   /* vlen * 0.5 + min               Volume.cpp:29 */
-    float vlen_inv;     /* 1 / vlen                       Volume.cpp:34 */
-    float index_off;    /* vlen_inv * -min                Volume.cpp:36 */
-} or_geom;
 
 void or_geom_init(or_geom* g, int res, float side, float trunc) {
     g->res = res;

@@ -39,8 +39,13 @@ def test_volume_create_rejects_bad_resolution(kifi_lib):
     d.resolution, d.side_length_m, d.truncation_m = 100, 2.0, 0.02  # not a power of two
     h = C.c_void_p()
     assert kifi_lib.kifi_volume_create(C.byref(d), C.byref(h)) == 1
-    d.resolution = 2048  # above the 10-bit key fields
+    d.resolution, d.key_bits = 2048, 32  # above the 10-bit fields of 32-bit keys
     assert kifi_lib.kifi_volume_create(C.byref(d), C.byref(h)) == 1
+    d.resolution, d.key_bits = 16384, 0  # above the 13-bit fields of 64-bit keys
+    assert kifi_lib.kifi_volume_create(C.byref(d), C.byref(h)) == 1
+    d.resolution, d.key_bits = 256, 48  # key width neither 32 nor 64
+    assert kifi_lib.kifi_volume_create(C.byref(d), C.byref(h)) == 1
+    d.key_bits = 0
     d.resolution, d.truncation_m = 256, 0.0
     assert kifi_lib.kifi_volume_create(C.byref(d), C.byref(h)) == 1
 
