@@ -263,6 +263,16 @@ KIFI_API kifi_status kifi_icp_create(int device, void* stream, kifi_icp** out);
 KIFI_API kifi_status kifi_icp_destroy(kifi_icp* icp);
 KIFI_API void* kifi_icp_stream(kifi_icp* icp);
 
+/* Diagnostics of ICP::AlignStep's association (ICP.cpp:66-131; no reference
+ * accessor).  While recording is on, every iteration stores per source
+ * pixel (rows, then every 4th column) the linear index y1 * width + x1 of
+ * its nearest target point, or -1 when it has none (also for pixels without
+ * depth), and that point's squared distance (0.01 when none).
+ * kifi_icp_associations reads back the last iteration's; *n = sources. */
+KIFI_API kifi_status kifi_icp_record_associations(kifi_icp* icp, int on);
+KIFI_API kifi_status kifi_icp_associations(kifi_icp* icp, int64_t* target_index, float* len2, size_t capacity,
+                                           size_t* n);
+
 /* The synthetic target of ICP::Align (ICP.h:23-24): a width x height
  * row-major buffer of world points (3 floats each, (0,0,0) = no point) and
  * the eye-to-world pose of the camera that produced it. */

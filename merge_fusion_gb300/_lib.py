@@ -57,6 +57,8 @@ SIGNATURES = {
                                        C.POINTER(C.c_size_t)]),
     "kifi_volume_insert64": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t]),
     "kifi_volume_key_bits": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "kifi_icp_record_associations": (C.c_int, [C.c_void_p, C.c_int]),
+    "kifi_icp_associations": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)]),
     "kifi_radix_sort_u64": (C.c_int, [C.c_void_p, C.c_size_t]),
     "kifi_radix_sort_pairs_u64": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "kifi_volume_clear": (C.c_int, [C.c_void_p]),

@@ -7,12 +7,11 @@ concurrently; the host never waits inside a step.
     python -m merge_fusion_gb300.batched [--scenes 64] [--seed 7]
 
 Scene i draws its frame size from {320x240, 512x424, 640x480, 1024x848},
-its voxel size from {2, 4, 8} mm (truncation 5 voxels; cube side 1024 voxels
-for 2 and 4 mm, 512 for 8 mm) and its trajectory length from [50, 300]
-frames.  The 30-bit keys allow 1024 voxels per axis, a 2.048 m cube at 2 mm,
-so 2 mm scenes use the generator's half-scale room (2 x 1.5 x 2 m).  To
-bound the rendering time a scene renders at most `unique` frames of its
-trajectory and plays them forward and back.  Reported: frames
+its voxel size from {2, 4, 8} mm (truncation 5 voxels; a 4.096 m cube of
+2048, 1024 or 512 voxels per axis, so 2 mm scenes use 64-bit keys) and its
+trajectory length from [50, 300] frames.  To bound the rendering time a
+scene renders at most `unique` frames of its trajectory and plays them
+forward and back.  Reported: frames
 per second over all scenes and the per-scene step latency (p50, p99), from
 CUDA events on each scene's volume and ICP streams."""
 import argparse
@@ -35,9 +34,9 @@ def scene_specs(n, seed):
     for i in range(n):
         w, h, f = SIZES[int(rng.integers(len(SIZES)))]
         vox = VOXELS_MM[int(rng.integers(len(VOXELS_MM)))]
-        res = 512 if vox == 8 else 1024
+        res = {2: 2048, 4: 1024, 8: 512}[vox]
         out.append({"seed": seed * 1000 + i, "width": w, "height": h, "f": f, "voxel_mm": vox, "res": res,
-                    "scale": 0.5 if vox == 2 else 1.0, "frames": int(rng.integers(50, 301))})
+                    "scale": 1.0, "frames": int(rng.integers(50, 301))})
     return out
 
 

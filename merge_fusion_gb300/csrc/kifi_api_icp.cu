@@ -23,6 +23,10 @@ struct kifi_icp {
     Mat4 synth_e2w{};
     bool have_target = false;
     int last_iters = 0;
+    bool record = false;             // keep the last iteration's association
+    long long* pairs = nullptr;      // per source: target index, or -1
+    float* pairs_len2 = nullptr;     // per source: len^2
+    size_t pairs_cap = 0, pairs_n = 0;
 };
 
 namespace {
@@ -46,8 +50,7 @@ kifi_status reserve_bytes(void** p, size_t* cap, size_t bytes, cudaStream_t st) 
 }
 
 kifi_status reserve_target(kifi_icp* c, int w, int h) {
-    return reserve_bytes((void**)&c->synth, &c->synth_cap, (size_t)w * h * sizeof(float4),
-                         c->stream);
+    return reserve_bytes((void**)&c->synth, &c->synth_cap, (size_t)w * h * sizeof(float4), c->stream);
 }
 
 kifi_status enqueue_align(kifi_icp* c, const void* depth_dev, bool u16, const kifi_camera* cam,
@@ -71,6 +74,22 @@ kifi_status enqueue_align(kifi_icp* c, const void* depth_dev, bool u16, const ki
     a.synth = c->synth;
     a.synth_w = c->sw;
     a.synth_h = c->sh;
+    if (c->record) {
+        if (n_src > c->pairs_cap) {
+            KIFI_CUDA(cudaStreamSynchronize(c->stream));
+            cudaFree(c->pairs);
+            cudaFree(c->pairs_len2);
+            c->pairs = nullptr;
+            c->pairs_len2 = nullptr;
+            c->pairs_cap = 0;
+            KIFI_CUDA(cudaMalloc(&c->pairs, n_src * sizeof(long long)));
+            KIFI_CUDA(cudaMalloc(&c->pairs_len2, n_src * sizeof(float)));
+            c->pairs_cap = n_src;
+        }
+        a.pairs = c->pairs;
+        a.pairs_len2 = c->pairs_len2;
+        c->pairs_n = n_src;
+    }
     KIFI_CUDA(icp_align_enqueue(a, c->st, load_mat(guess), iterations, icp_ctas(c, n_src),
                                 c->stream));
     c->last_iters = iterations;
@@ -133,6 +152,8 @@ kifi_status kifi_icp_destroy(kifi_icp* c) {
     cudaFree(c->st);
     cudaFree(c->depth_dev);
     cudaFree(c->synth);
+    cudaFree(c->pairs);
+    cudaFree(c->pairs_len2);
     cudaFree(c->staging);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -140,6 +161,26 @@ kifi_status kifi_icp_destroy(kifi_icp* c) {
 }
 
 void* kifi_icp_stream(kifi_icp* c) { return c ? (void*)c->stream : nullptr; }
+
+kifi_status kifi_icp_record_associations(kifi_icp* c, int on) {
+    if (!c) return fail(KIFI_ERR_INVALID_ARGUMENT, "null ICP");
+    c->record = on != 0;
+    return KIFI_OK;
+}
+
+kifi_status kifi_icp_associations(kifi_icp* c, int64_t* target_index, float* len2, size_t capacity, size_t* n) {
+    if (!c || !n) return fail(KIFI_ERR_INVALID_ARGUMENT, "null argument");
+    KIFI_CUDA(cudaSetDevice(c->device));
+    *n = c->pairs_n;
+    if (c->pairs_n > capacity) return fail(KIFI_ERR_CAPACITY, "association buffers too small");
+    if (c->pairs_n) {
+        if (target_index)
+            KIFI_CUDA(cudaMemcpyAsync(target_index, c->pairs, c->pairs_n * 8, cudaMemcpyDeviceToHost, c->stream));
+        if (len2) KIFI_CUDA(cudaMemcpyAsync(len2, c->pairs_len2, c->pairs_n * 4, cudaMemcpyDeviceToHost, c->stream));
+    }
+    KIFI_CUDA(cudaStreamSynchronize(c->stream));
+    return KIFI_OK;
+}
 
 kifi_status kifi_icp_set_target(kifi_icp* c, const float* points, int width, int height,
                                 const float synth_eye_to_world[16]) {

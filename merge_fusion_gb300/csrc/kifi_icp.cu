@@ -400,6 +400,11 @@ __global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step(IcpArgs a, IcpSta
                 bq = make_float3(q.x, q.y, q.z);
             }
             const bool hit = mine && rc >= 0;
+            if (a.pairs && mine) {
+                const size_t k = (size_t)y * n_cols + col;
+                a.pairs[k] = hit ? (long long)(v + (rc >> 5)) * a.synth_w + (u + (rc & 31)) : -1ll;
+                a.pairs_len2[k] = hit ? best : 0.01f;
+            }
             // this source's pair for the tile's moments (zeros when none)
             const int sidx = wcol * 32 + lane;
             s_rec[0][sidx] = hit ? wp[0] : 0.f;

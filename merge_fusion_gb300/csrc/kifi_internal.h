@@ -121,6 +121,8 @@ struct IcpArgs {
     float proj[16];         // EyeToClipRH * inverse(synth eye-to-world), kifi order
     const float4* synth;    // target world points (w unused), synth_w * synth_h
     int synth_w, synth_h;
+    long long* pairs;       // optional: per source the winner's target index (-1: none) ...
+    float* pairs_len2;      // ... and its len^2, overwritten by every iteration
 };
 
 struct IcpIterStats {
@@ -150,6 +152,7 @@ cudaError_t icp_align_enqueue(const IcpArgs& a, IcpState* st, const Mat4& guess,
 cudaError_t backproject_enqueue(const void* depth, bool u16, const kifi_camera& cam,
                                 const Mat4& eye_to_world, float4* out, int ctas, cudaStream_t st);
 cudaError_t expand_target_enqueue(const float* in, int n, float4* out, int ctas, cudaStream_t st);
+
 cudaError_t bin_enqueue(const float* pts, unsigned int n, const Mat4& w2c, int width, int height,
                         unsigned long long* zbuf, float* out, int ctas, cudaStream_t st);
 

@@ -321,6 +321,20 @@ class ICP:
                                          _ptr(out)), "Align")
         return out
 
+    def RecordAssociations(self, on=True):
+        check(_lib.load().kifi_icp_record_associations(self._h, 1 if on else 0), "RecordAssociations")
+
+    def Associations(self):
+        """The last iteration's association per source (rows, every 4th
+        column): (target index int64, -1 for none; len^2 float32)."""
+        lib = _lib.load()
+        n = C.c_size_t()
+        lib.kifi_icp_associations(self._h, None, None, 0, C.byref(n))  # the count (capacity error ignored)
+        idx = np.zeros(n.value, np.int64)
+        l2 = np.zeros(n.value, np.float32)
+        check(lib.kifi_icp_associations(self._h, _ptr(idx), _ptr(l2), n.value, C.byref(n)), "Associations")
+        return idx, l2
+
     def Result(self):
         """(pose float (16,), pose double (16,), n_assoc per iteration, rms per iteration)."""
         pf = np.zeros(16, np.float32)

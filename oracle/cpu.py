@@ -248,6 +248,19 @@ def icp_align(depth, cam, e2w_guess, synth, synth_e2w, iters, fp64=False):
     return out, outd, st.n_assoc
 
 
+def icp_associate(depth, cam, e2w, synth, synth_e2w):
+    """One AlignStep's association under pose e2w: per source (rows, every
+    4th column) the winner's linear target index (-1: none) and len^2."""
+    depth, pose, se2w, synth = f32(depth), f32(e2w), f32(synth_e2w), f32(synth)
+    sh, sw = synth.shape[0], synth.shape[1]
+    n = ((cam[0] + 3) // 4) * cam[1]
+    at = np.zeros(n, np.int64)
+    l2 = np.zeros(n, np.float32)
+    lib().or_icp_associate(_p(depth), C.byref(cam_struct(cam)), _p(pose), _p(synth), C.c_int(sw), C.c_int(sh),
+                           _p(se2w), _p(at), _p(l2))
+    return at, l2
+
+
 def bin_points(points, world_to_clip, w, h):
     pts = f32(points)
     w2c = f32(world_to_clip)

@@ -538,6 +538,33 @@ static void or_quat_to_rot(const double* q, double* R) {
 static int g_icp_fp64 = 0;
 void or_icp_set_fp64(int on) { g_icp_fp64 = on; }
 
+/* The association search of one source (ICP.cpp:100-131): the first strict
+ * minimum of len^2 < 0.01 over the window at (u, v), clamped to columns
+ * [0, 640) and rows [0, 480); returns len^2 (0.01 when none) and the
+ * winner's linear target index in *at (-1 when none). */
+static float icp_search(const float* synth, size_t nsynth, int sw, int32_t u, int32_t v, const float* wp,
+                        int64_t* at_out) {
+    float mind = 0.01f;
+    int64_t best = -1;
+    /* any u >= 640 or v >= 480 leaves the window empty, so the
+     * reference's wrapping u + 21 / v + 21 cannot matter */
+    int64_t yend = (int64_t)v + 21 < 480 ? (int64_t)v + 21 : 480;
+    int64_t xend = (int64_t)u + 21 < 640 ? (int64_t)u + 21 : 640;
+    for (int64_t y1 = v; y1 < yend; ++y1)
+        for (int64_t x1 = u; x1 < xend; ++x1) {
+            size_t at = (size_t)y1 * (size_t)sw + (size_t)x1;
+            if (at >= nsynth) continue;
+            const float* q = synth + 3 * at;
+            if (q[0] == 0.0f && q[1] == 0.0f && q[2] == 0.0f) continue;
+            float dx = q[0] - wp[0], dy = q[1] - wp[1], dz = q[2] - wp[2];
+            float dw = 1.0f - wp[3];
+            float l2 = (dx * dx + dy * dy) + (dz * dz + dw * dw);
+            if (l2 < mind) { mind = l2; best = (int64_t)at; }
+        }
+    *at_out = best;
+    return mind;
+}
+
 /* One ICP::AlignStep (ICP.cpp:35-265) with the Horn solve in double.
  *
  * Association, Kahan centroid and cross-covariance sums follow the reference
@@ -580,22 +607,9 @@ int or_icp_step(const float* depth, const or_camera* cam, const float* e2w_guess
             int32_t v = wrap_sub(wrap_sub((int32_t)sh - 1, cvt_i32_x86(uvy * half_h + half_h)), 10);
             if (u < 0) u = 0;
             if (v < 0) v = 0;
-            float mind = 0.01f, p2[3] = {0, 0, 0};
-            /* any u >= 640 or v >= 480 leaves the window empty, so the
-             * reference's wrapping u + 21 / v + 21 cannot matter */
-            int64_t yend = (int64_t)v + 21 < 480 ? (int64_t)v + 21 : 480;
-            int64_t xend = (int64_t)u + 21 < 640 ? (int64_t)u + 21 : 640;
-            for (int64_t y1 = v; y1 < yend; ++y1)
-                for (int64_t x1 = u; x1 < xend; ++x1) {
-                    size_t at = (size_t)y1 * (size_t)sw + (size_t)x1;
-                    if (at >= nsynth) continue;
-                    const float* q = synth + 3 * at;
-                    if (q[0] == 0.0f && q[1] == 0.0f && q[2] == 0.0f) continue;
-                    float dx = q[0] - wp[0], dy = q[1] - wp[1], dz = q[2] - wp[2];
-                    float dw = 1.0f - wp[3];
-                    float l2 = (dx * dx + dy * dy) + (dz * dz + dw * dw);
-                    if (l2 < mind) { mind = l2; p2[0] = q[0]; p2[1] = q[1]; p2[2] = q[2]; }
-                }
+            int64_t at;
+            float mind = icp_search(synth, nsynth, sw, u, v, wp, &at), p2[3] = {0, 0, 0};
+            if (at >= 0) memcpy(p2, synth + 3 * at, 12);
             if (mind < 0.01f) {
                 float* a = assoc + 6 * na++;
                 a[0] = wp[0]; a[1] = wp[1]; a[2] = wp[2];
@@ -698,6 +712,42 @@ int or_icp_step(const float* depth, const or_camera* cam, const float* e2w_guess
  * step is the double pose rounded to float.  Poses are eye-to-world,
  * in/out as kifi float4x4 (column-major); pose_d gets the double result
  * column-major. */
+/* The association of one AlignStep under pose e2w, per source in the
+ * reference's order (rows, every 4th column; ICP.cpp:66-131): the winner's
+ * linear target index (-1 when none, also for pixels without depth) and
+ * its len^2 (0.01 when none). */
+void or_icp_associate(const float* depth, const or_camera* cam, const float* e2w, const float* synth, int sw,
+                      int sh, const float* synth_e2w, int64_t* out_at, float* out_l2) {
+    float dst_w2e[16], e2c[16], m[16];
+    or_invert_transform(synth_e2w, dst_w2e);
+    or_eye_to_clip(cam, e2c);
+    or_mat_mul(e2c, dst_w2e, m);
+    float fl[4] = {1.0f / cam->fx, 1.0f / cam->fy, 1.0f, 1.0f};
+    float pp[4] = {(0.5f - cam->cx) * fl[0], (cam->cy - 0.5f) * fl[1], 0.0f * fl[2], 0.0f * fl[3]};
+    float half_w = (float)sw * 0.5f, half_h = (float)sh * 0.5f;
+    const size_t nsynth = (size_t)sw * sh;
+    size_t k = 0;
+    for (int y = 0; y < cam->height; ++y)
+        for (int x = 0; x < cam->width; x += 4, ++k) {
+            out_at[k] = -1;
+            out_l2[k] = 0.01f;
+            float d = depth[(size_t)y * cam->width + x];
+            if (0.0f == d) continue;
+            float pt[4] = {(float)x, -(float)y, -1.0f, 0.0f};
+            for (int l = 0; l < 4; ++l) pt[l] = (pt[l] * fl[l] + pp[l]) * d;
+            pt[3] = 1.0f;
+            float wp[4], cl[4];
+            or_mat_vec(e2w, pt, wp);
+            or_mat_vec(m, wp, cl);
+            float uvx = cl[0] / cl[3], uvy = cl[1] / cl[3];
+            int32_t u = wrap_sub(cvt_i32_x86(uvx * half_w + half_w), 10);
+            int32_t v = wrap_sub(wrap_sub((int32_t)sh - 1, cvt_i32_x86(uvy * half_h + half_h)), 10);
+            if (u < 0) u = 0;
+            if (v < 0) v = 0;
+            out_l2[k] = icp_search(synth, nsynth, sw, u, v, wp, &out_at[k]);
+        }
+}
+
 void or_icp_align(const float* depth, const or_camera* cam, const float* e2w_guess,
                   const float* synth, int sw, int sh, const float* synth_e2w, int iters,
                   float* out_pose, double* pose_d, or_icp_stats* stats) {

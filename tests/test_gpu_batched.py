@@ -13,11 +13,11 @@ def _export(lib, pipe):
     vol = lib.kifi_pipeline_volume(pipe)
     n = C.c_size_t()
     assert lib.kifi_volume_size(vol, C.byref(n)) == 0
-    k = np.zeros(n.value + 1, np.uint32)
+    k = np.zeros(n.value + 1, np.uint64)
     v = np.zeros((n.value + 1, 2), np.float32)
     got = C.c_size_t()
-    assert lib.kifi_volume_export(vol, k.ctypes.data_as(C.c_void_p), v.ctypes.data_as(C.c_void_p), n.value + 1,
-                                  C.byref(got)) == 0
+    assert lib.kifi_volume_export64(vol, k.ctypes.data_as(C.c_void_p), v.ctypes.data_as(C.c_void_p),
+                                    n.value + 1, C.byref(got)) == 0
     pose = np.zeros(16, np.float32)
     assert lib.kifi_pipeline_sync(pipe, pose.ctypes.data_as(C.c_void_p)) == 0
     return k[:got.value], v[:got.value], pose
@@ -29,8 +29,7 @@ def test_batched_scenes_equal_single_runs(gpu):
     lib = _lib.load()
     specs = [{"seed": 11, "width": 320, "height": 240, "f": 292.5, "voxel_mm": 8, "res": 512, "frames": 9},
              {"seed": 12, "width": 512, "height": 424, "f": 365.0, "voxel_mm": 4, "res": 1024, "frames": 7},
-             {"seed": 13, "width": 640, "height": 480, "f": 585.0, "voxel_mm": 2, "res": 1024, "scale": 0.5,
-              "frames": 8}]
+             {"seed": 13, "width": 640, "height": 480, "f": 585.0, "voxel_mm": 2, "res": 2048, "frames": 8}]
     together = [batched.Scene(s, 6, 10, 0) for s in specs]
     while any(not s.done() for s in together):
         for s in together:

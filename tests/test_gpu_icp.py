@@ -145,3 +145,39 @@ def test_icp_error_vs_fp64_oracle(gpu, oracle_cpu, golden):
         _, od, _ = oracle_cpu.icp_align(seq.depth_m(i), rc, prev, tgt, prev, 15, fp64=True)
         worst = max(worst, float(np.abs(pd - od).max()))
     assert worst < POSE_TOL, worst
+
+
+def test_association_is_exact(gpu, oracle_cpu, golden):
+    # The association of the first iteration (pose = the guess, identical on
+    # both sides) must be the reference's pair for pair: same winner (first
+    # strict minimum in scan order), same len^2 bits, for 640x480 targets
+    # and for 512x424 ones, whose 640x480 window clamp wraps into the next
+    # target row.
+    from merge_fusion_gb300 import kifi, scenes
+    icp = kifi.ICP()
+    icp.RecordAssociations(True)
+    cases = []
+    depth, view, cam = golden["depth"], golden["view"], golden["camera"]
+    e2w = oracle_cpu.invert_transform(view)
+    target = oracle_cpu.backproject(depth, cam, e2w)
+    for off in ((0.0, 0.0, 0.0), (0.01, -0.006, 0.004), (-0.03, 0.02, 0.01)):
+        cases.append((depth, cam, posed(e2w, off), target, e2w))
+    for seq in (scenes.room_scene(n_frames=3, seed=6), scenes.sphere_scene(n_frames=3, seed=6),
+                scenes.room_scene(n_frames=2, seed=7, width=512, height=424, f=365.0, scale=2.0)):
+        rc = seq.camera
+        for i in (1, 2):
+            if i >= len(seq.frames):
+                continue
+            prev = seq.eye_to_world_f32(i - 1)
+            tgt = oracle_cpu.backproject(seq.depth_m(i - 1), rc, prev)
+            cases.append((seq.depth_m(i), rc, prev, tgt, prev))
+            cases.append((seq.depth_m(i), rc, seq.eye_to_world_f32(i), tgt, prev))
+    for n, (d, c, guess, tgt, se2w) in enumerate(cases):
+        icp.Align(d, guess, tgt, se2w, cam_params(c), 1)
+        gi, gl = icp.Associations()
+        oi, ol = oracle_cpu.icp_associate(d, c, guess, tgt, se2w)
+        assert gi.size == oi.size, n
+        bad = np.nonzero(gi != oi)[0]
+        assert bad.size == 0, (n, bad[:5], gi[bad[:5]], oi[bad[:5]], gl[bad[:5]], ol[bad[:5]])
+        assert np.array_equal(gl.view(np.uint32), ol.view(np.uint32)), n
+        assert (gi >= 0).sum() > 1000, n
