@@ -446,7 +446,7 @@ __global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step(IcpArgs a, IcpSta
     if (!last_cta(&st->done)) return;
     __shared__ FF tot[kMoments];
     moments_total<kMoments>(st, tot);
-    if (threadIdx.x == 0) finish_step(st, tot);
+    if (threadIdx.x < 32) finish_step(st, tot);
 }
 
 // ------------------------------------------------------------- Horn solve
@@ -582,47 +582,79 @@ __device__ __forceinline__ void sym_mul_shift(const float* n, const float* p, fl
         }
 }
 
-// Thread 0 of the last CTA of an AlignStep: from the totals of the raw
+// Warp 0 of the last CTA of an AlignStep: from the totals of the raw
 // moments, the centroids and S (ICP.cpp:166-197), N (:199-213), its dominant
 // eigenvector (above), R and t (:215-256) and pose <- (T R) pose (:20-28).
+// The work is spread over the lanes entry by entry -- centroids, S, N,
+// the four minors and cofactors, R, t and the twelve pose entries -- and
+// joined by shuffles; the float characteristic polynomial and its Newton
+// search run on every lane alike.  Symmetric matrices indexed by a lane go
+// through shared memory (a register array indexed by a lane would live in
+// local memory).
+__device__ __forceinline__ FF shfl_ff(FF v, int src) {
+    return FF{__shfl_sync(0xffffffffu, v.hi, src), __shfl_sync(0xffffffffu, v.lo, src)};
+}
+// minor3 of rows {0..3} \ {rx} and columns {0..3} \ {cx} of n - s I, n in
+// shared memory (upper triangle), for lane-dependent rx, cx
+template <typename T>
+__device__ __forceinline__ T minor_excl(const T* n, T s, int rx, int cx) {
+    const int r0 = rx == 0 ? 1 : 0, r1 = rx <= 1 ? 2 : 1, r2 = rx <= 2 ? 3 : 2;
+    const int k0 = cx == 0 ? 1 : 0, k1 = cx <= 1 ? 2 : 1, k2 = cx <= 2 ? 3 : 2;
+    return minor3(n, s, r0, r1, r2, k0, k1, k2);
+}
+// N's entry k (upper triangle, row by row) as (S[i1] s2 S[i2]) s3 S[i3]:
+// N = [[Sxx+Syy+Szz, Syz-Szy, Szx-Sxz, Sxy-Syx], [., Sxx-Syy-Szz, Sxy+Syx,
+// Szx+Sxz], [., ., Syy-Sxx-Szz, Syz+Szy], [., ., ., Szz-Sxx-Syy]] (:199-213)
+__device__ __forceinline__ void n_terms(int k, int& i1, int& i2, int& i3, bool& m2, bool& m3, bool& t3) {
+    // per k (4 bits each): i1, i2, i3; flags: minus second, minus third, has third
+    constexpr unsigned long long kI1 = 0x8546101650ull, kI2 = 0x0702343274ull, kI3 = 0x4080080008ull;
+    constexpr unsigned int kM2 = 0x29e, kM3 = 0x290, kT3 = 0x291;
+    i1 = (int)(kI1 >> (4 * k)) & 15;
+    i2 = (int)(kI2 >> (4 * k)) & 15;
+    i3 = (int)(kI3 >> (4 * k)) & 15;
+    m2 = (kM2 >> k) & 1u;
+    m3 = (kM3 >> k) & 1u;
+    t3 = (kT3 >> k) & 1u;
+}
+
 __device__ __noinline__ void finish_step(IcpState* __restrict__ st, const FF* __restrict__ tot) {
-    // 1. centroids, S and N in FF
+    __shared__ float s_f[10];
+    __shared__ FF s_nf[10];
+    const int lane = threadIdx.x & 31;
+    // 1. centroids (lanes 0-5), S (lanes 0-8), N (lanes 0-9) in FF
     const float n = fadd(tot[0].hi, tot[0].lo);  // an exact count below 2^24
-    FF mu[6];
-#pragma unroll
-    for (int i = 0; i < 6; ++i) {
-        const float h = fdiv(tot[1 + i].hi, n);
-        const float r = fadd(__fmaf_rn(-h, n, tot[1 + i].hi), tot[1 + i].lo);  // exact remainder + lo
-        mu[i] = ff_norm(h, fdiv(r, n));
+    FF my_mu{0.0f, 0.0f};
+    if (lane < 6) {
+        const float h = fdiv(tot[1 + lane].hi, n);
+        const float r = fadd(__fmaf_rn(-h, n, tot[1 + lane].hi), tot[1 + lane].lo);  // exact remainder + lo
+        my_mu = ff_norm(h, fdiv(r, n));
     }
-    FF S[9];
+    const int sl = lane < 9 ? lane : 0;
+    const FF mu_c = shfl_ff(my_mu, 3 + sl % 3);
+    const FF my_s = tot[7 + sl] - tot[1 + sl / 3] * mu_c;
+    int i1, i2, i3;
+    bool m2, m3, t3;
+    n_terms(lane < 10 ? lane : 0, i1, i2, i3, m2, m3, t3);
+    const FF a1 = shfl_ff(my_s, i1), a2 = shfl_ff(my_s, i2), a3 = shfl_ff(my_s, i3);
+    FF my_n = m2 ? a1 - a2 : a1 + a2;
+    if (t3) my_n = m3 ? my_n - a3 : my_n + a3;
+    const bool diag = lane == 0 || lane == 4 || lane == 7 || lane == 9;
+    float f2 = lane < 10 ? fmul(diag ? my_n.hi : 2.0f * my_n.hi, my_n.hi) : 0.0f;
 #pragma unroll
-    for (int r = 0; r < 3; ++r)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) S[3 * r + c] = tot[7 + 3 * r + c] - tot[1 + r] * mu[3 + c];
-    const FF Sxx = S[0], Sxy = S[1], Sxz = S[2], Syx = S[3], Syy = S[4], Syz = S[5],
-             Szx = S[6], Szy = S[7], Szz = S[8];
-    FF nf[10] = {Sxx + Syy + Szz, Syz - Szy,       Szx - Sxz,       Sxy - Syx,
-                 Sxx - Syy - Szz, Sxy + Syx,       Szx + Sxz,
-                 Syy - Sxx - Szz, Syz + Szy,
-                 Szz - Sxx - Syy};
-    float f2 = 0.0f;
-#pragma unroll
-    for (int i = 0; i < 10; ++i) {
-        const bool diag = i == 0 || i == 4 || i == 7 || i == 9;
-        f2 = fmaf(diag ? nf[i].hi : 2.0f * nf[i].hi, nf[i].hi, f2);
-    }
+    for (int o = 16; o > 0; o >>= 1) f2 = fadd(f2, __shfl_xor_sync(0xffffffffu, f2, o));
     // power-of-two scale 2^-e/2 with f2 = m 2^e: N's Frobenius norm lands in [0.5, 1.5)
     const int e = ((__float_as_int(f2) >> 23) & 0xff) - 127;
     const float sc = __int_as_float((127 - (e >> 1)) << 23);
     const bool finite = f2 > 1e-30f && f2 < 1e30f;
+    if (lane < 10) {
+        s_nf[lane] = FF{my_n.hi * sc, my_n.lo * sc};
+        s_f[lane] = my_n.hi * sc;
+    }
+    __syncwarp();
     float f[10];
 #pragma unroll
-    for (int i = 0; i < 10; ++i) {
-        nf[i] = FF{nf[i].hi * sc, nf[i].lo * sc};
-        f[i] = nf[i].hi;
-    }
-    // 2. float search
+    for (int i = 0; i < 10; ++i) f[i] = s_f[i];
+    // 2. float search (every lane)
     float gmax = -1e30f;  // Gershgorin: the largest row bound
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
@@ -655,88 +687,116 @@ __device__ __noinline__ void finish_step(IcpState* __restrict__ st, const FF* __
         l -= step;
         if (step <= 1e-7f * fabsf(l)) break;
     }
-    const float d0 = fabsf(minor3(f, l, 1, 2, 3, 1, 2, 3)), d1 = fabsf(minor3(f, l, 0, 2, 3, 0, 2, 3));
-    const float d2 = fabsf(minor3(f, l, 0, 1, 3, 0, 1, 3)), d3 = fabsf(minor3(f, l, 0, 1, 2, 0, 1, 2));
+    // the principal minors (lanes 0-3); j = the first largest
+    const int q4 = lane & 3;
+    const float my_d = fabsf(minor_excl(s_f, l, q4, q4));
     int j = 0;
-    float dj = d0;
-    if (d1 > dj) { j = 1; dj = d1; }
-    if (d2 > dj) { j = 2; dj = d2; }
-    if (d3 > dj) { j = 3; dj = d3; }
-    FF q[4];
+    float dj = __shfl_sync(0xffffffffu, my_d, 0);
+#pragma unroll
+    for (int i = 1; i < 4; ++i) {
+        const float di = __shfl_sync(0xffffffffu, my_d, i);
+        if (di > dj) {
+            j = i;
+            dj = di;
+        }
+    }
+    // cofactor (i, j) of a symmetric matrix: lane i takes q[i] = (-1)^(i+j) minor(rows != j, cols != i)
+    const bool neg = ((q4 + j) & 1) != 0;
+    FF my_q{0.0f, 0.0f};
     int solver = 0;
     if (finite && dj > 1e-4f) {
         // 3. Rayleigh-quotient inverse iteration in FF
-        float qf[4];
-        adj_column(f, l, j, qf);
+        float my_qf = minor_excl(s_f, l, j, q4);
+        if (neg) my_qf = -my_qf;
         const int steps = dj < 1e-2f ? 2 : 1;
         for (int s = 0; s < steps; ++s) {
-            FF num{0.0f, 0.0f}, qq{0.0f, 0.0f};
+            // lane r: row r of N times qf, then the Rayleigh quotient num / qq over lanes 0-3
+            FF t{0.0f, 0.0f};
 #pragma unroll
-            for (int r = 0; r < 4; ++r) {
-                FF t{0.0f, 0.0f};
+            for (int c = 0; c < 4; ++c) t = t + s_nf[sym(q4, c)] * __shfl_sync(0xffffffffu, my_qf, c);
+            FF num = lane < 4 ? t * my_qf : FF{0.0f, 0.0f};
+            FF qq = lane < 4 ? FF{my_qf, 0.0f} * my_qf : FF{0.0f, 0.0f};
 #pragma unroll
-                for (int c = 0; c < 4; ++c) t = t + nf[sym(r, c)] * qf[c];
-                num = num + t * qf[r];
-                qq = qq + FF{qf[r], 0.0f} * qf[r];
+            for (int o = 1; o < 4; o <<= 1) {
+                num = num + shfl_ff(num, lane ^ o);
+                qq = qq + shfl_ff(qq, lane ^ o);
             }
-            adj_column(nf, ff_div(num, qq), j, q);
-#pragma unroll
-            for (int i = 0; i < 4; ++i) qf[i] = q[i].hi;
+            num = shfl_ff(num, 0);
+            qq = shfl_ff(qq, 0);
+            my_q = minor_excl(s_nf, ff_div(num, qq), j, q4);
+            if (neg) my_q = -my_q;
+            my_qf = my_q.hi;
         }
     } else {
         // 4. nearly repeated largest eigenvalue (or no finite solution)
         solver = 1;
-        double A[16], V[16];
-        for (int r = 0; r < 4; ++r)
-            for (int c = 0; c < 4; ++c) A[4 * r + c] = (double)nf[sym(r, c)].hi + (double)nf[sym(r, c)].lo;
-        jacobi4(A, V);
-        int imax = 0;
-        for (int i = 1; i < 4; ++i)
-            if (A[i] > A[imax]) imax = i;
-        for (int i = 0; i < 4; ++i) {
-            const double v = V[4 * i + imax];
-            q[i] = FF{(float)v, (float)(v - (double)(float)v)};
+        if (lane == 0) {
+            double A[16], V[16];
+            for (int r = 0; r < 4; ++r)
+                for (int c = 0; c < 4; ++c) A[4 * r + c] = (double)s_nf[sym(r, c)].hi + (double)s_nf[sym(r, c)].lo;
+            jacobi4(A, V);
+            int imax = 0;
+            for (int i = 1; i < 4; ++i)
+                if (A[i] > A[imax]) imax = i;
+            for (int i = 0; i < 4; ++i) {
+                const double vi = V[4 * i + imax];
+                s_nf[i] = FF{(float)vi, (float)(vi - (double)(float)vi)};  // N is not needed any more
+            }
         }
+        __syncwarp();
+        my_q = s_nf[q4];
     }
     // q = normalize(q) (:231): 1/sqrt(q'q) from a float estimate and one FF Newton step
-    const FF qq = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
+    FF qq = lane < 4 ? my_q * my_q : FF{0.0f, 0.0f};
+#pragma unroll
+    for (int o = 1; o < 4; o <<= 1) qq = qq + shfl_ff(qq, lane ^ o);
+    qq = shfl_ff(qq, 0);
     const float r0 = rsqrtf(qq.hi);
     const FF corr = (FF{1.0f, 0.0f} - qq * r0 * r0) * (0.5f * r0);
-    const FF ri = FF{r0, 0.0f} + corr;
+    my_q = my_q * (FF{r0, 0.0f} + corr);
+    // R from the quaternion, x = scalar part (:233-254), in FF: lane k < 9 takes entry k
+    //   diagonal k = 0, 4, 8:  1 - 2 (q_a q_a + q_b q_b)
+    //   off-diagonal:          2 (q_a q_b +- q_c q_d)
+    const int rk = lane < 9 ? lane : 0;
+    // (a, b, c, d) per entry, 4 bits each: (2,2,3,3) (1,2,0,3) (1,3,0,2) (1,2,0,3) (1,1,3,3)
+    // (2,3,0,1) (1,3,0,2) (2,3,0,1) (1,1,2,2)
+    constexpr unsigned long long kA = 0x121211112ull, kB = 0x133312322ull, kC = 0x200030003ull,
+                                 kD = 0x212133233ull;
+    const int ia = (int)(kA >> (4 * rk)) & 15, ib = (int)(kB >> (4 * rk)) & 15;
+    const int ic = (int)(kC >> (4 * rk)) & 15, id = (int)(kD >> (4 * rk)) & 15;
+    const FF qa = shfl_ff(my_q, ia), qb = shfl_ff(my_q, ib), qc = shfl_ff(my_q, ic), qd = shfl_ff(my_q, id);
+    const FF pab = qa * qb, pcd = qc * qd;
+    const bool rdiag = rk == 0 || rk == 4 || rk == 8;
+    const bool rminus = rk == 1 || rk == 5 || rk == 6;
+    const FF my_r = rdiag ? FF{1.0f, 0.0f} - (pab + pcd) * 2.0f : (rminus ? pab - pcd : pab + pcd) * 2.0f;
+    // t = dstMedian - R srcMedian (:256): lane r < 3
+    const int tr3 = lane < 3 ? lane : 0;
+    const FF mu0 = shfl_ff(my_mu, 0), mu1 = shfl_ff(my_mu, 1), mu2 = shfl_ff(my_mu, 2);
+    const FF mud = shfl_ff(my_mu, 3 + tr3);
+    const FF my_t = mud - (shfl_ff(my_r, 3 * tr3) * mu0 + shfl_ff(my_r, 3 * tr3 + 1) * mu1 +
+                           shfl_ff(my_r, 3 * tr3 + 2) * mu2);
+    // pose <- [R t; 0 1] pose (:259-263, :20-28): lane k < 12 takes row r = k % 3 of column c = k / 3
+    const int pk = lane < 12 ? lane : 0, pc = pk / 3, pr = pk - 3 * pc;
+    FF P[4];
 #pragma unroll
-    for (int i = 0; i < 4; ++i) q[i] = q[i] * ri;
-    // R from the quaternion, x = scalar part (:233-254), in FF
-    const FF xy = q[0] * q[1], xz = q[0] * q[2], xw = q[0] * q[3];
-    const FF yy = q[1] * q[1], yz = q[1] * q[2], yw = q[1] * q[3];
-    const FF zz = q[2] * q[2], zw = q[2] * q[3], ww = q[3] * q[3];
-    const FF one{1.0f, 0.0f};
-    const FF R[9] = {one - (zz + ww) * 2.0f, (yz - xw) * 2.0f,       (yw + xz) * 2.0f,
-                     (yz + xw) * 2.0f,       one - (yy + ww) * 2.0f, (zw - xy) * 2.0f,
-                     (yw - xz) * 2.0f,       (zw + xy) * 2.0f,       one - (yy + zz) * 2.0f};
-    // t = dstMedian - R srcMedian (:256); pose <- [R t; 0 1] pose (:259-263, :20-28)
-    FF t[3];
-#pragma unroll
-    for (int r = 0; r < 3; ++r) t[r] = mu[3 + r] - (R[3 * r] * mu[0] + R[3 * r + 1] * mu[1] + R[3 * r + 2] * mu[2]);
-    FF P[16];  // kifi order: entry (row r, column c) at 4c + r
-#pragma unroll
-    for (int i = 0; i < 16; ++i) P[i] = FF{st->pose_f[i], st->pose_lo[i]};
-#pragma unroll
-    for (int c = 0; c < 4; ++c)
-#pragma unroll
-        for (int r = 0; r < 3; ++r) {
-            const FF v = R[3 * r] * P[4 * c] + R[3 * r + 1] * P[4 * c + 1] + R[3 * r + 2] * P[4 * c + 2] +
-                         t[r] * P[4 * c + 3];
-            st->pose_f[4 * c + r] = v.hi;
-            st->pose_lo[4 * c + r] = v.lo;
-        }
-    const float mp[3] = {fadd(mu[0].hi, mu[0].lo), fadd(mu[1].hi, mu[1].lo), fadd(mu[2].hi, mu[2].lo)};
+    for (int i = 0; i < 4; ++i) P[i] = FF{st->pose_f[4 * pc + i], st->pose_lo[4 * pc + i]};
+    const FF v = shfl_ff(my_r, 3 * pr) * P[0] + shfl_ff(my_r, 3 * pr + 1) * P[1] + shfl_ff(my_r, 3 * pr + 2) * P[2] +
+                 shfl_ff(my_t, pr) * P[3];
+    __syncwarp();  // every lane has read its column before any entry is replaced
+    if (lane < 12) {
+        st->pose_f[4 * pc + pr] = v.hi;
+        st->pose_lo[4 * pc + pr] = v.lo;
+    }
+    const FF md0 = shfl_ff(my_mu, 3), md1 = shfl_ff(my_mu, 4), md2 = shfl_ff(my_mu, 5);
+    if (lane != 0) return;
     st->n_assoc = (int)n;
     st->sum_l2 = (double)fadd(tot[16].hi, tot[16].lo);
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        st->mu_s[i] = mp[i];
-        st->mu_d[i] = fadd(mu[3 + i].hi, mu[3 + i].lo);
-    }
+    st->mu_s[0] = fadd(mu0.hi, mu0.lo);
+    st->mu_s[1] = fadd(mu1.hi, mu1.lo);
+    st->mu_s[2] = fadd(mu2.hi, mu2.lo);
+    st->mu_d[0] = fadd(md0.hi, md0.lo);
+    st->mu_d[1] = fadd(md1.hi, md1.lo);
+    st->mu_d[2] = fadd(md2.hi, md2.lo);
     const int it = st->iter;
     if (it < kIcpMaxStats) {
         st->stats[it].n_assoc = (int)n;
