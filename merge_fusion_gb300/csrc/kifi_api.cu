@@ -28,6 +28,12 @@ kifi_status cuda_fail(cudaError_t e, const char* what) {
     return KIFI_ERR_CUDA;
 }
 
+void tracking_launch_shape(LaunchShape* ls) {
+    ls->splat_ctas = ls->sms * 16;
+    ls->sort_ctas = ls->sms * 16;
+    ls->merge_ctas = ls->sms * 32;
+}
+
 kifi_status launch_shape(int device, LaunchShape* ls) {
     int sms = 0;
     KIFI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));

@@ -123,7 +123,11 @@ kifi_status kifi_icp_create(int device, void* stream, kifi_icp** out) {
     if (!e) {
         if (stream) c->stream = (cudaStream_t)stream;
         else {
-            e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+            // the highest priority: tracking is the pipeline's critical path,
+            // and its CTAs are placed ahead of pending fusion CTAs
+            int lowest = 0, greatest = 0;
+            e = cudaDeviceGetStreamPriorityRange(&lowest, &greatest);
+            if (!e) e = cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, greatest);
             c->own_stream = !e;
         }
     }

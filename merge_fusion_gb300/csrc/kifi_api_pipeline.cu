@@ -251,6 +251,10 @@ kifi_status kifi_pipeline_create(const kifi_pipeline_desc* d, kifi_pipeline** ou
     vd.device = d->device;
     vd.key_bits = d->key_bits;
     kifi_status s = kifi_volume_create(&vd, &p->vol);
+    if (!s && d->icp_iterations > 0) {
+        p->vol->tracking_grids = true;
+        tracking_launch_shape(&p->vol->ls);
+    }
     if (!s) s = kifi_icp_create(d->device, nullptr, &p->icp);
     if (s) {
         kifi_pipeline_destroy(p);

@@ -17,6 +17,12 @@ kifi_status fail(kifi_status s, const char* what);
 // maps a CUDA error to a status and records it
 kifi_status cuda_fail(cudaError_t e, const char* what);
 kifi_status launch_shape(int device, LaunchShape* ls);
+// Fusion launch shape for a volume whose frames are also tracked on a
+// higher-priority stream: many CTAs per SM that each finish quickly, so the
+// tracking kernels reclaim SMs between CTAs instead of waiting for
+// persistent fusion CTAs to drain.
+void tracking_launch_shape(LaunchShape* ls);
+
 bool camera_ok(const kifi_camera* c);
 
 constexpr size_t kPad = 64;  // slack elements behind every device array
@@ -45,6 +51,9 @@ struct kifi_volume {
     kifi::SortScratch ss{};
     kifi::MeshScratch ms{};
     kifi::LaunchShape ls{};
+    // fusion beside a tracking stream: grids of short-lived CTAs (see
+    // tracking_launch_shape), also the only shapes the autotuner tries
+    bool tracking_grids = false;
     void* depth_dev = nullptr;
     size_t depth_dev_bytes = 0;
     void* depth_pinned = nullptr;

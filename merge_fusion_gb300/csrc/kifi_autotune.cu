@@ -35,7 +35,7 @@ std::mutex g_mu;
 std::map<std::string, LaunchShape> g_cache;
 bool g_loaded = false;
 
-std::string cache_key(int device, int res, int key_bits, int w, int h) {
+std::string cache_key(int device, int res, int key_bits, bool tracking, int w, int h) {
     cudaDeviceProp prop;
     if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) {
         cudaGetLastError();
@@ -43,11 +43,9 @@ std::string cache_key(int device, int res, int key_bits, int w, int h) {
         prop.multiProcessorCount = 0;
     }
     char buf[512];
-    // 30-bit keys keep the key format of caches written before 64-bit keys
-    if (key_bits == 64)
-        std::snprintf(buf, sizeof buf, "%s|%d|%d|k64|%dx%d", prop.name, prop.multiProcessorCount, res, w, h);
-    else
-        std::snprintf(buf, sizeof buf, "%s|%d|%d|%dx%d", prop.name, prop.multiProcessorCount, res, w, h);
+    // 30-bit keys of a stand-alone volume keep the key format of earlier caches
+    std::snprintf(buf, sizeof buf, "%s|%d|%d|%s%s%dx%d", prop.name, prop.multiProcessorCount, res,
+                  key_bits == 64 ? "k64|" : "", tracking ? "trk|" : "", w, h);
     for (char* c = buf; *c; ++c)
         if (*c == ' ') *c = '_';
     return buf;
@@ -99,7 +97,7 @@ extern "C" kifi_status kifi_volume_autotune(kifi_volume* v, const void* depth_de
     if (!v || !depth_dev || !camera_ok(cam) || !world_to_eye)
         return fail(KIFI_ERR_INVALID_ARGUMENT, "autotune: bad argument");
     KIFI_CUDA(cudaSetDevice(v->device));
-    const std::string key = cache_key(v->device, v->g.res, 8 * v->vb.key_bytes, cam->width, cam->height);
+    const std::string key = cache_key(v->device, v->g.res, 8 * v->vb.key_bytes, v->tracking_grids, cam->width, cam->height);
     {
         std::lock_guard<std::mutex> lock(g_mu);
         load_file();
@@ -167,7 +165,12 @@ extern "C" kifi_status kifi_volume_autotune(kifi_volume* v, const void* depth_de
     if ((s = run(base, bt))) goto done;
     {
         const int sms = base.sms;
-        for (int m : {1, 2, 4, 8}) {  // splat + emit (stage 0)
+        // beside a tracking stream only short-lived grids (tracking_launch_shape)
+        const bool tr = v->tracking_grids;
+        const std::vector<int> splat_m = tr ? std::vector<int>{8, 16, 32} : std::vector<int>{1, 2, 4, 8};
+        const std::vector<int> sort_m = tr ? std::vector<int>{8, 16, 32} : std::vector<int>{2, 4, 8};
+        const std::vector<int> merge_m = tr ? std::vector<int>{16, 32, 64} : std::vector<int>{1, 2};
+        for (int m : splat_m) {  // splat + emit (stage 0)
             LaunchShape c = best;
             c.splat_ctas = m * sms;
             double t[4];
@@ -177,7 +180,7 @@ extern "C" kifi_status kifi_volume_autotune(kifi_volume* v, const void* depth_de
                 bt[0] = t[0];
             }
         }
-        for (int m : {2, 4, 8}) {  // sort passes (stage 1)
+        for (int m : sort_m) {  // sort passes (stage 1)
             LaunchShape c = best;
             c.sort_ctas = m * sms;
             double t[4];
@@ -187,9 +190,9 @@ extern "C" kifi_status kifi_volume_autotune(kifi_volume* v, const void* depth_de
                 bt[1] = t[1];
             }
         }
-        for (int m : {1, 2}) {  // merge + update (stage 3)
+        for (int m : merge_m) {  // merge + update (stage 3)
             LaunchShape c = best;
-            c.merge_ctas = m * (base.merge_ctas);
+            c.merge_ctas = tr ? m * sms : m * base.merge_ctas;
             double t[4];
             if ((s = run(c, t))) goto done;
             if (t[3] < bt[3]) {
