@@ -257,6 +257,10 @@ __global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step(IcpArgs a, IcpSta
     __shared__ FF s_acc[kMoments];             // this CTA's moments (index 0 unused: s_count)
     __shared__ float s_rec[7][kTileCols * 32];  // per source: p xyz, q xyz, len^2 (0 when no pair)
     __shared__ unsigned int s_count;
+    // Steps are launched programmatically behind one another: this grid may
+    // start while the previous step's last CTA still updates the pose.  Wait
+    // for that grid (and its memory) before touching the ICP state.
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     const int n_cols = (a.width + 3) / 4;
     const int tiles_x = (n_cols + kTileCols - 1) / kTileCols;
     const int tiles_y = (a.height + kTileRows - 1) / kTileRows;
@@ -437,6 +441,8 @@ __global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step(IcpArgs a, IcpSta
         }
         __syncthreads();  // staging buffer, half results and records are reused by the next tile
     }
+    // association done: the next step's grid may be scheduled (it waits above)
+    asm volatile("griddepcontrol.launch_dependents;");
     if (threadIdx.x < kMoments) {
         const FF t = threadIdx.x == 0 ? FF{(float)s_count, 0.0f} : s_acc[threadIdx.x];
         st->part[(size_t)(2 * threadIdx.x) * kIcpMaxCtas + blockIdx.x] = t.hi;
@@ -903,7 +909,23 @@ cudaError_t icp_align_enqueue(const IcpArgs& a, IcpState* st, const Mat4& guess,
     const int tiles = ((n_cols + kTileCols - 1) / kTileCols) * ((a.height + kTileRows - 1) / kTileRows);
     const int ctas = tiles < kIcpMaxCtas ? tiles : kIcpMaxCtas;
     const size_t smem = kStagePixels * sizeof(float4);
-    for (int it = 0; it < iterations; ++it) k_icp_step<<<ctas, kAssocThreads, smem, stream>>>(a, st);
+    // programmatic dependent launch: each step's grid is scheduled as soon as
+    // every CTA of the one before has finished its association, overlapping
+    // its launch with the previous finisher (k_icp_step waits for it)
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(ctas);
+    cfg.blockDim = dim3(kAssocThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    for (int it = 0; it < iterations; ++it) {
+        const cudaError_t e = cudaLaunchKernelEx(&cfg, k_icp_step, a, st);
+        if (e != cudaSuccess) return e;
+    }
     return cudaGetLastError();
 }
 
