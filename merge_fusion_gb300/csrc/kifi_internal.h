@@ -89,6 +89,7 @@ struct MeshCounts {
 
 struct MeshScratch {
     unsigned int* vflags = nullptr;        // per voxel: vertex axes | index count<<8 | case<<16
+    uint4* corners = nullptr;              // per flagged voxel: indices of its +y, +z, +yz lookups
     unsigned long long* vscan = nullptr;   // per voxel packed (index count << 32 | vertex count)
     unsigned long long* tscan = nullptr;   // exclusive scan of vscan
     unsigned long long* block_sums = nullptr;

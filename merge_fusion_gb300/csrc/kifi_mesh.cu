@@ -59,15 +59,27 @@ __global__ void k_row_directory(const K* __restrict__ keys, const unsigned int* 
 }
 
 // upper_bound(keys, t) using the row directory: keys of t's row lie in
-// [row_start[r], row_start[r+1]) sorted by x.
+// [row_start[r], row_start[r+1]) sorted by x.  `hint` is where t probably
+// sits within its row -- the searching voxel's own offset within its row,
+// since neighbouring rows of a surface hold similar runs of x.  Two probes
+// around the guess settle most lookups; otherwise a binary search of the
+// side the probes leave.  The result does not depend on the hint.
 template <typename K>
 __device__ __forceinline__ unsigned int upper_bound_row(const K* __restrict__ keys,
                                                         const unsigned int* __restrict__ rs,
-                                                        K t, unsigned int n, const Codec<K>& cd) {
+                                                        K t, unsigned int n, const Codec<K>& cd,
+                                                        unsigned int hint) {
     const unsigned long long r = cd.row(t);
     // a neighbour of a voxel on the last z slice lies past every key
     if (r >= (1ull << (2 * cd.b))) return n;
     unsigned int lo = rs[r], hi = rs[r + 1];
+    if (lo == hi) return lo;
+    const unsigned int g = hint < hi - lo ? lo + hint : hi;
+    const bool right = g < hi && keys[g] <= t;   // the answer lies above g
+    const bool left = g > lo && keys[g - 1] > t;  // ... or below g
+    if (right) lo = g + 1;
+    else if (left) hi = g - 1;  // keys[g - 1] > t: the answer is at most g - 1
+    else return g;
     while (lo < hi) {
         unsigned int mid = (lo + hi) >> 1;
         if (keys[mid] <= t) lo = mid + 1;
@@ -79,12 +91,25 @@ __device__ __forceinline__ unsigned int upper_bound_row(const K* __restrict__ ke
 // neighbour pointer position after the reference's walk (see file comment)
 template <typename K>
 __device__ __forceinline__ unsigned int walk_ptr(const K* keys, const unsigned int* rs, K t, unsigned int n,
-                                                 const Codec<K>& cd) {
-    unsigned int p = upper_bound_row<K>(keys, rs, t, n, cd) - 1u;
+                                                 const Codec<K>& cd, unsigned int hint) {
+    unsigned int p = upper_bound_row<K>(keys, rs, t, n, cd, hint) - 1u;
     return p < n - 2 ? p : n - 2;
 }
 
 __device__ __forceinline__ float vdist(float2 v) { return fdiv(v.x, v.y); }  // Voxel::Distance
+
+// per-voxel packed counts are scanned in tiles of kScanTile
+constexpr int kScanItems = 4;
+constexpr int kScanTile = kThreads * kScanItems;
+
+// A voxel's exclusive prefix of the packed counts: its offset within its
+// scan tile plus the tile's offset.
+__device__ __forceinline__ unsigned long long scan_at(const unsigned long long* __restrict__ scan,
+                                                      const unsigned long long* __restrict__ tile_offsets,
+                                                      unsigned int i) {
+    return scan[i] + tile_offsets[i / kScanTile];
+}
+
 
 struct Cube {
     unsigned int idx[8];  // voxel index of each corner (valid where found)
@@ -101,18 +126,20 @@ __device__ __forceinline__ void load_cube(const K* __restrict__ keys,
                                           unsigned int i, Cube& c, const Codec<K>& cd) {
     const K key = keys[i];
     const float2 zero = make_float2(0.0f, 0.0f);
+    // this voxel's offset within its row, where its neighbours likely sit in theirs
+    const unsigned int hint = i - rs[cd.row(key)];
     c.idx[0] = i;
     c.val[0] = vals[i];
     c.idx[1] = i + 1;
     c.val[1] = keys[i + 1] == key + cd.pack(1, 0, 0) ? vals[i + 1] : zero;
-    const unsigned int iTop = walk_ptr<K>(keys, rs, key + cd.pack(0, 1, 0), n, cd);
-    const unsigned int iFront = walk_ptr<K>(keys, rs, key + cd.pack(0, 0, 1), n, cd);
+    const unsigned int iTop = walk_ptr<K>(keys, rs, key + cd.pack(0, 1, 0), n, cd, hint);
+    const unsigned int iFront = walk_ptr<K>(keys, rs, key + cd.pack(0, 0, 1), n, cd, hint);
     c.idx[2] = iTop;
     c.val[2] = keys[iTop] == key + cd.pack(0, 1, 0) ? vals[iTop] : zero;
     c.idx[4] = iFront;
     c.val[4] = keys[iFront] == key + cd.pack(0, 0, 1) ? vals[iFront] : zero;
     if (kTris) {
-        const unsigned int iFT = walk_ptr<K>(keys, rs, key + cd.pack(0, 1, 1), n, cd);
+        const unsigned int iFT = walk_ptr<K>(keys, rs, key + cd.pack(0, 1, 1), n, cd, hint);
         c.idx[6] = iFT;
         c.val[6] = keys[iFT] == key + cd.pack(0, 1, 1) ? vals[iFT] : zero;
         c.idx[3] = iTop + 1;
@@ -152,7 +179,13 @@ __global__ void __launch_bounds__(kThreads) k_mesh_classify(const K* __restrict_
                                                             const unsigned int* __restrict__ rs,
                                                             const unsigned int* __restrict__ n_dev,
                                                             unsigned int* __restrict__ flags,
-                                                            unsigned long long* __restrict__ counts) {
+                                                            unsigned long long* __restrict__ counts,
+                                                            uint4* __restrict__ corners) {
+    __shared__ uint64_t s_mc[256];
+    if (kTris) {
+        mc_table_to_shared(s_mc);
+        __syncthreads();
+    }
     const unsigned int n = *n_dev;
     const Codec<K> cd(kb);
     for (unsigned int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
@@ -169,19 +202,39 @@ __global__ void __launch_bounds__(kThreads) k_mesh_classify(const K* __restrict_
                 for (int q = 1; q < 8; ++q) skip |= (0.0f == c.val[q].y);
                 if (!skip) {
                     const int lut = cube_case(c);
-                    ni = 3u * mc_tri_count(lut);
+                    ni = 3u * mc_tri_count_of(s_mc[lut]);
                     f |= ni << 8 | (unsigned int)lut << 16;
                 }
             }
+            // emission reuses these lookups instead of searching again
+            if (f) corners[i] = make_uint4(c.idx[2], c.idx[4], kTris ? c.idx[6] : 0u, 0u);
         }
         flags[i] = f;
         counts[i] = (unsigned long long)ni << 32 | nv;
     }
 }
 
-// edge e of the cube -> (corner, axis), from localToGlobal (Mesher.cpp:206-218)
-__constant__ unsigned char kEdgeCorner[12] = {4, 0, 0, 1, 6, 2, 2, 3, 5, 4, 0, 1};
-__constant__ unsigned char kEdgeAxis[12] = {0, 2, 0, 2, 0, 2, 0, 2, 1, 1, 1, 1};
+// The corners of a flagged voxel from its stored lookups: +x, +xy, +xz and
+// +xyz sit one index past self, +y, +z and +yz (load_cube's walk).  Values
+// are loaded where emission reads them.
+__device__ __forceinline__ void stored_cube(unsigned int i, uint4 cr, unsigned int* idx) {
+    idx[0] = i;
+    idx[1] = i + 1;
+    idx[2] = cr.x;
+    idx[3] = cr.x + 1;
+    idx[4] = cr.y;
+    idx[5] = cr.y + 1;
+    idx[6] = cr.z;
+    idx[7] = cr.z + 1;
+}
+
+// edge e of the cube -> (corner, axis), from localToGlobal (Mesher.cpp:206-218):
+// corners {4, 0, 0, 1, 6, 2, 2, 3, 5, 4, 0, 1} (4 bits each) and axes
+// {0, 2, 0, 2, 0, 2, 0, 2, 1, 1, 1, 1} (2 bits each), decoded in registers
+constexpr unsigned long long kEdgeCorners = 0x104532261004ull;
+constexpr unsigned int kEdgeAxes = 0x558888u;
+__device__ __forceinline__ int edge_corner(int e) { return (int)((kEdgeCorners >> (4 * e)) & 15u); }
+__device__ __forceinline__ int edge_axis(int e) { return (int)((kEdgeAxes >> (2 * e)) & 3u); }
 
 template <bool kTris, typename K>
 __global__ void __launch_bounds__(kThreads) k_mesh_emit(const K* __restrict__ keys, int kb,
@@ -189,7 +242,9 @@ __global__ void __launch_bounds__(kThreads) k_mesh_emit(const K* __restrict__ ke
                                                         const unsigned int* __restrict__ rs,
                                                         const unsigned int* __restrict__ n_dev, Geom g,
                                                         const unsigned int* __restrict__ flags,
+                                                        const uint4* __restrict__ corners,
                                                         const unsigned long long* __restrict__ scan,
+                                                        const unsigned long long* __restrict__ tile_offsets,
                                                         unsigned long long n_verts,
                                                         unsigned long long n_idx,
                                                         unsigned long long missing_bound,
@@ -197,6 +252,11 @@ __global__ void __launch_bounds__(kThreads) k_mesh_emit(const K* __restrict__ ke
                                                         float* __restrict__ verts,
                                                         uint32_t* __restrict__ idx,
                                                         unsigned long long* __restrict__ missing_min) {
+    __shared__ uint64_t s_mc[256];
+    if (kTris) {
+        mc_table_to_shared(s_mc);
+        __syncthreads();
+    }
     const unsigned int n = *n_dev;
     const Codec<K> cd(kb);
     // a re-run for the index mapping's stop rule takes its bound from the first run, and only
@@ -208,10 +268,10 @@ __global__ void __launch_bounds__(kThreads) k_mesh_emit(const K* __restrict__ ke
     for (unsigned int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
         const unsigned int f = flags[i];
         if (f == 0) continue;
-        Cube c;
-        load_cube<kTris, K>(keys, vals, rs, n, i, c, cd);
+        unsigned int cidx[8];
+        stored_cube(i, corners[i], cidx);
         const K key = keys[i];
-        const unsigned long long s = scan[i];
+        const unsigned long long s = scan_at(scan, tile_offsets, i);
         const unsigned int vbase = (unsigned int)(s & 0xffffffffu);
         const unsigned int axes = f & 7u;
         // vertices (Mesher.cpp:134-168)
@@ -222,13 +282,13 @@ __global__ void __launch_bounds__(kThreads) k_mesh_emit(const K* __restrict__ ke
             const float cx = fadd(fmul((float)(int)cd.x(key), g.vlen), g.center_off);
             const float cy = fadd(fmul((float)(int)cd.y(key), g.vlen), g.center_off);
             const float cz = fadd(fmul((float)(int)cd.z(key), g.vlen), g.center_off);
-            const float dself = vdist(c.val[0]);
+            const float dself = vdist(vals[i]);
             const int nb[3] = {1, 2, 4};
             unsigned int r = 0;
 #pragma unroll
             for (int a = 0; a < 3; ++a) {
                 if (!(axes >> a & 1u)) continue;
-                const float dn = vdist(c.val[nb[a]]);
+                const float dn = vdist(vals[cidx[nb[a]]]);  // a flagged axis: the neighbour exists
                 const float t = fmul(fdiv(fabsf(dself), fadd(fabsf(dself), fabsf(dn))), g.vlen);
                 float p[3] = {cx, cy, cz};
                 p[a] = fadd(p[a], t);
@@ -242,14 +302,14 @@ __global__ void __launch_bounds__(kThreads) k_mesh_emit(const K* __restrict__ ke
         if (!kTris) continue;
         const unsigned int ni = (f >> 8) & 0xffu;
         if (!ni) continue;
-        const int lut = (int)(f >> 16 & 0xffu);
+        const uint64_t mcw = s_mc[(f >> 16) & 0xffu];  // the case's triangle edges
         const unsigned int ibase = (unsigned int)(s >> 32);
         const unsigned long long first = n_idx - ibase - ni;  // generation order
         unsigned long long local_min = ~0ull;
         for (unsigned int t = 0; t < ni; ++t) {
-            const int e = mc_tri_edge(lut, (int)t);
-            const int corner = kEdgeCorner[e], axis = kEdgeAxis[e];
-            const unsigned int ci = c.idx[corner];
+            const int e = mc_tri_edge_of(mcw, (int)t);
+            const int corner = edge_corner(e), axis = edge_axis(e);
+            const unsigned int ci = cidx[corner];
             // the edge id 3 * key + axis: 32 bits wide for 30-bit keys (as in the
             // reference); for 64-bit keys the stop rule compares full ids and an id
             // written in place of a missing vertex keeps its low 32 bits
@@ -257,7 +317,8 @@ __global__ void __launch_bounds__(kThreads) k_mesh_emit(const K* __restrict__ ke
             const unsigned int cf = flags[ci];
             uint32_t outv;
             if (cf >> axis & 1u) {
-                outv = (unsigned int)(scan[ci] & 0xffffffffu) + __popc(cf & 7u & ((1u << axis) - 1u));
+                outv = (unsigned int)(scan_at(scan, tile_offsets, ci) & 0xffffffffu) +
+                       __popc(cf & 7u & ((1u << axis) - 1u));
             } else {
                 outv = (uint32_t)id;
                 local_min = min(local_min, id);
@@ -272,8 +333,6 @@ __global__ void __launch_bounds__(kThreads) k_mesh_emit(const K* __restrict__ ke
 // -------------------------------------------------------- exclusive scan
 // Two-level exclusive scan of packed 64-bit (index count << 32 | vertex
 // count) values; both halves stay below 2^32 for volumes under 2^28 voxels.
-constexpr int kScanItems = 4;
-constexpr int kScanTile = kThreads * kScanItems;
 
 __device__ __forceinline__ unsigned long long block_exclusive_scan(unsigned long long x,
                                                                    unsigned long long* total) {
@@ -320,7 +379,9 @@ __global__ void __launch_bounds__(kThreads) k_scan_tiles(const unsigned long lon
     if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
 }
 
-// single CTA: exclusive scan of the tile sums, total to counts
+// single CTA: exclusive scan of the tile sums (in place), total to counts;
+// each thread takes kSumItems consecutive sums per round
+constexpr int kSumItems = 8;
 __global__ void __launch_bounds__(kThreads) k_scan_sums(unsigned long long* __restrict__ sums,
                                                         unsigned int n_tiles,
                                                         const unsigned int* __restrict__ n_dev,
@@ -329,11 +390,21 @@ __global__ void __launch_bounds__(kThreads) k_scan_sums(unsigned long long* __re
     const unsigned int used = (*n_dev + kScanTile - 1) / kScanTile;
     if (used < n_tiles) n_tiles = used;
     unsigned long long carry = 0;
-    for (unsigned int b = 0; b < n_tiles; b += kThreads) {
-        const unsigned int i = b + threadIdx.x;
-        unsigned long long x = i < n_tiles ? sums[i] : 0ull, total;
-        unsigned long long ex = block_exclusive_scan(x, &total);
-        if (i < n_tiles) sums[i] = carry + ex;
+    for (unsigned int b = 0; b < n_tiles; b += kThreads * kSumItems) {
+        const unsigned int i0 = b + threadIdx.x * kSumItems;
+        unsigned long long v[kSumItems], s = 0;
+#pragma unroll
+        for (int q = 0; q < kSumItems; ++q) {
+            v[q] = i0 + q < n_tiles ? sums[i0 + q] : 0ull;
+            s += v[q];
+        }
+        unsigned long long total;
+        unsigned long long run = carry + block_exclusive_scan(s, &total);
+#pragma unroll
+        for (int q = 0; q < kSumItems; ++q) {
+            if (i0 + q < n_tiles) sums[i0 + q] = run;
+            run += v[q];
+        }
         carry += total;
     }
     if (threadIdx.x == 0) {
@@ -341,16 +412,6 @@ __global__ void __launch_bounds__(kThreads) k_scan_sums(unsigned long long* __re
         counts->n_idx = carry >> 32;
         counts->missing_min = ~0ull;
     }
-}
-
-__global__ void __launch_bounds__(kThreads) k_scan_add(unsigned long long* __restrict__ out,
-                                                       const unsigned long long* __restrict__ sums,
-                                                       const unsigned int* __restrict__ n_dev) {
-    const unsigned int n = *n_dev;
-    const unsigned int base = blockIdx.x * kScanTile;
-    const unsigned long long add = sums[blockIdx.x];
-    for (int q = threadIdx.x; q < kScanTile; q += kThreads)
-        if (base + q < n) out[base + q] += add;
 }
 
 }  // namespace
@@ -363,6 +424,7 @@ cudaError_t mesh_scratch_reserve(MeshScratch* m, size_t n, int kb) {
     size_t cap = n < 1024 ? 1024 : n;
     cudaError_t e;
     if ((e = cudaMalloc(&m->vflags, cap * sizeof(unsigned int)))) return e;
+    if ((e = cudaMalloc(&m->corners, cap * sizeof(uint4)))) return e;
     if ((e = cudaMalloc(&m->vscan, cap * sizeof(unsigned long long)))) return e;
     if ((e = cudaMalloc(&m->tscan, cap * sizeof(unsigned long long)))) return e;
     if ((e = cudaMalloc(&m->block_sums, ((cap + kScanTile - 1) / kScanTile + 1) * 8))) return e;
@@ -376,6 +438,7 @@ cudaError_t mesh_scratch_reserve(MeshScratch* m, size_t n, int kb) {
 
 void mesh_scratch_free(MeshScratch* m) {
     cudaFree(m->vflags);
+    cudaFree(m->corners);
     cudaFree(m->vscan);
     cudaFree(m->tscan);
     cudaFree(m->block_sums);
@@ -402,14 +465,13 @@ static void mesh_count_t(const K* keys, const float2* vals, size_t n_cap, int kb
     k_row_directory<K><<<grid_for(((size_t)1 << (2 * kb)) + 1, sms), kThreads, 0, st>>>(keys, ms.n_dev, kb, ms.rows);
     if (with_indices)
         k_mesh_classify<true, K><<<grid_for(n_cap, sms), kThreads, 0, st>>>(keys, kb, vals, ms.rows, ms.n_dev,
-                                                                             ms.vflags, cnt);
+                                                                             ms.vflags, cnt, ms.corners);
     else
         k_mesh_classify<false, K><<<grid_for(n_cap, sms), kThreads, 0, st>>>(keys, kb, vals, ms.rows, ms.n_dev,
-                                                                              ms.vflags, cnt);
+                                                                              ms.vflags, cnt, ms.corners);
     const unsigned int n_tiles = (unsigned int)((n_cap + kScanTile - 1) / kScanTile);
     k_scan_tiles<<<n_tiles ? n_tiles : 1, kThreads, 0, st>>>(cnt, scan, ms.block_sums, ms.n_dev);
     k_scan_sums<<<1, kThreads, 0, st>>>(ms.block_sums, n_tiles ? n_tiles : 1, ms.n_dev, ms.counts);
-    k_scan_add<<<n_tiles ? n_tiles : 1, kThreads, 0, st>>>(scan, ms.block_sums, ms.n_dev);
 }
 
 cudaError_t mesh_count_enqueue(const void* keys, int key_bytes, const float2* vals, size_t n_cap, int kb,
@@ -431,14 +493,14 @@ static void mesh_emit_t(const Geom& g, const K* keys, const float2* vals, size_t
     const int kb = sizeof(K) == 4 ? 10 : g.kb;
     if (with_indices) {
         k_mesh_emit<true, K><<<grid_for(n_cap, sms), kThreads, 0, st>>>(keys, kb, vals, ms.rows, ms.n_dev, g,
-                                                                         ms.vflags, scan, n_verts, n_idx,
+                                                                         ms.vflags, ms.corners, scan, ms.block_sums, n_verts, n_idx,
                                                                          ~0ull, nullptr, verts_dev, idx_dev, mm);
         k_mesh_emit<true, K><<<grid_for(n_cap, sms), kThreads, 0, st>>>(keys, kb, vals, ms.rows, ms.n_dev, g,
-                                                                         ms.vflags, scan, n_verts, n_idx, 0ull, mm,
+                                                                         ms.vflags, ms.corners, scan, ms.block_sums, n_verts, n_idx, 0ull, mm,
                                                                          verts_dev, idx_dev, nullptr);
     } else {
         k_mesh_emit<false, K><<<grid_for(n_cap, sms), kThreads, 0, st>>>(keys, kb, vals, ms.rows, ms.n_dev, g,
-                                                                          ms.vflags, scan, n_verts, n_idx,
+                                                                          ms.vflags, ms.corners, scan, ms.block_sums, n_verts, n_idx,
                                                                           ~0ull, nullptr, verts_dev, idx_dev, mm);
     }
 }
