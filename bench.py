@@ -66,6 +66,28 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(x, world, device="cuda"):
+    """The largest x over the ranks of the process group (x itself alone)."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(world, steps, seconds):
+    """Whole-job frames/s: every rank fuses `steps` frames of its own scene,
+    timed by the slowest rank."""
+    return world * steps / seconds
+
+
+def rank_seed(rank):
+    """Each rank fuses its own seeded scene (replicas, weak scaling)."""
+    return SEED + rank
+
+
 def measured_peak():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -213,7 +235,7 @@ def run_gpu(args, rank, world, local):
     K, Wu, Fp = args.steps, args.warmup, args.prefill
     n_frames = Fp + Wu + 2 * K + 1
     # independent scene per rank (replicas; weak scaling)
-    seed = SEED + rank
+    seed = rank_seed(rank)
     frames, poses = scenes.render_room_torch(n_frames, seed=seed, device="cuda")
     torch.cuda.synchronize()
     frames_host = frames.cpu().numpy().view(np.uint16)
@@ -293,10 +315,7 @@ def run_gpu(args, rank, world, local):
     check(lib.kifi_volume_frame_log(vol, ptr(n0), ptr(ne), ptr(n1), 64, C.byref(cnt)))
     m = min(cnt.value, K)
     n0, ne, n1 = n0[cnt.value - m:cnt.value], ne[cnt.value - m:cnt.value], n1[cnt.value - m:cnt.value]
-    ms_t = torch.tensor([ms], device="cuda")
-    if world > 1:
-        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
-    ms = float(ms_t.item())
+    ms = max_over_ranks(ms, world)
 
     # ---- end to end through the public ABI from pinned host memory
     out_pose = np.zeros(16, np.float32)
@@ -309,10 +328,7 @@ def run_gpu(args, rank, world, local):
         check(lib.kifi_pipeline_integrate(pipe, C.c_void_p(pinned[K + j].data_ptr()), 1,
                                           ptr(w2e[i]), ptr(out_pose)), "e2e frame %d" % i)
     e2e_s = time.perf_counter() - te0
-    e2e_t = torch.tensor([e2e_s], device="cuda")
-    if world > 1:
-        dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
-    e2e_s = float(e2e_t.item())
+    e2e_s = max_over_ranks(e2e_s, world)
     nv, ni = C.c_size_t(), C.c_size_t()
     check(lib.kifi_pipeline_mesh_counts(pipe, C.byref(nv), C.byref(ni)))
     gb, gu = C.c_longlong(), C.c_longlong()
@@ -325,7 +341,7 @@ def run_gpu(args, rank, world, local):
             dist.destroy_process_group()
         return
 
-    value = world * K / (ms / 1e3)
+    value = job_throughput(world, K, ms / 1e3)
     P = W * H
     algo_bytes = (12.0 * n0.astype(np.float64) + 4.0 * ne + 12.0 * n1 + 2.0 * P)
     merge_ms = ms_stage[3] / max(nst.value, 1)
@@ -360,7 +376,7 @@ def run_gpu(args, rank, world, local):
                                "sort": ms_stage[1] / max(nst.value, 1),
                                "merge_partition": ms_stage[2] / max(nst.value, 1),
                                "merge_update": merge_ms},
-        "e2e": {"value": world * K / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 2 * P + 64,
+        "e2e": {"value": job_throughput(world, K, e2e_s), "unit": UNIT, "h2d_bytes_per_step": 2 * P + 64,
                 "d2h_bytes_per_step": 64 + 1024},
         "gpu_launches": gpu_launches,
         "graphs": {"on": bool(args.graphs), "instantiated": int(gb.value), "updated": int(gu.value)},
