@@ -148,7 +148,7 @@ kifi_status reserve_new(kifi_volume* v, size_t n_new) {
     sort_scratch_free(&v->ss);
     KIFI_CUDA(cudaMalloc(&v->vb.new_keys, (n_new + kPad) * vb_key_bytes(v->vb)));
     KIFI_CUDA(cudaMalloc(&v->vb.new_idx, (n_new + kPad) * sizeof(uint32_t)));
-    KIFI_CUDA(sort_scratch_alloc(&v->ss, n_new));
+    KIFI_CUDA(sort_scratch_alloc(&v->ss, n_new, v->stream));
     v->vb.new_cap = n_new;
     return KIFI_OK;
 }
@@ -330,13 +330,15 @@ kifi_status kifi_volume_create(const kifi_volume_desc* d, kifi_volume** out) {
     if ((s = launch_shape(v->device, &v->ls))) return bail(s);
     cudaError_t e;
     if ((e = cudaMalloc(&v->ctl, sizeof(DeviceCtl)))) return bail(cuda_fail(e, "control block"));
-    if ((e = cudaMemset(v->ctl, 0, sizeof(DeviceCtl)))) return bail(cuda_fail(e, "control block"));
+    // zeroing on the volume's stream: the library's streams are non-blocking and would not wait
+    // for a memset on the legacy default stream
+    if ((e = cudaMemsetAsync(v->ctl, 0, sizeof(DeviceCtl), v->stream))) return bail(cuda_fail(e, "control block"));
     if ((e = cudaMallocHost(&v->ctl_host, sizeof(DeviceCtl)))) return bail(cuda_fail(e, "pinned"));
     std::memset(v->ctl_host, 0, sizeof(DeviceCtl));
     const size_t r = (size_t)d->resolution;
     v->vb.bitmap_words = (r * r * r + 31) / 32;
     if ((e = cudaMalloc(&v->vb.bitmap, v->vb.bitmap_words * 4))) return bail(cuda_fail(e, "bitmap"));
-    if ((e = cudaMemset(v->vb.bitmap, 0, v->vb.bitmap_words * 4))) return bail(cuda_fail(e, "bitmap"));
+    if ((e = cudaMemsetAsync(v->vb.bitmap, 0, v->vb.bitmap_words * 4, v->stream))) return bail(cuda_fail(e, "bitmap"));
     size_t cap = d->initial_capacity;
     if (cap == 0) cap = r * r * r < ((size_t)1 << 22) ? r * r * r : ((size_t)1 << 22);
     for (int i = 0; i < 2; ++i) {
@@ -689,7 +691,7 @@ static kifi_status radix_sort_host(void* keys, int key_bytes, uint32_t* values, 
     const unsigned int n32 = (unsigned int)n;
     const size_t kb = (size_t)key_bytes;
     unsigned int status = 0;
-    cudaError_t e = sort_scratch_alloc(&ss, n);
+    cudaError_t e = sort_scratch_alloc(&ss, n, st);
     if (!e) e = cudaMalloc(&dk, (n + kPad) * kb);
     if (!e && values) e = cudaMalloc(&dv, (n + kPad) * 4);
     if (!e) e = cudaMalloc(&dn, 4);

@@ -132,7 +132,7 @@ kifi_status kifi_icp_create(int device, void* stream, kifi_icp** out) {
         }
     }
     if (!e) e = cudaMalloc(&c->st, sizeof(IcpState));
-    if (!e) e = cudaMemset(c->st, 0, sizeof(IcpState));
+    if (!e) e = cudaMemsetAsync(c->st, 0, sizeof(IcpState), c->stream);  // ordered before the context's work
     if (e) {
         kifi_icp_destroy(c);
         return cuda_fail(e, "ICP context");

@@ -26,7 +26,9 @@ struct SortScratch {
 };
 
 size_t sort_max_tiles(size_t max_n);
-cudaError_t sort_scratch_alloc(SortScratch* s, size_t max_n);
+// zeroes its look-back words on `st`: the sorts that use it must run on st
+// (or after it)
+cudaError_t sort_scratch_alloc(SortScratch* s, size_t max_n, cudaStream_t st);
 void sort_scratch_free(SortScratch* s);
 cudaError_t sort_u32(uint32_t* keys, uint32_t* vals, const unsigned int* n_dev, SortScratch& s,
                      unsigned int* status, int grid_ctas, cudaStream_t st);

@@ -475,7 +475,9 @@ kifi_status kifi_proposer_create(int device, int max_batch, kifi_proposer** out)
                 if (t == 11) on = i < (size_t)kOut;
                 m[kLayout.off[t] + i] = on ? 1 : 0;
             }
-        e = cudaMemcpy(pr->mask, m.data(), P, cudaMemcpyHostToDevice);
+        // on the proposer's stream (non-blocking: it would not wait for the legacy default stream)
+        e = cudaMemcpyAsync(pr->mask, m.data(), P, cudaMemcpyHostToDevice, pr->stream);
+        if (!e) e = cudaStreamSynchronize(pr->stream);
     }
     if (e) {
         kifi_proposer_destroy(pr);

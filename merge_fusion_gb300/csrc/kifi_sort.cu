@@ -205,7 +205,7 @@ __global__ void __launch_bounds__(kThreads) k_sort_pass(const K* __restrict__ ke
 
 size_t sort_max_tiles(size_t max_n) { return (max_n + kTile - 1) / kTile + 1; }
 
-cudaError_t sort_scratch_alloc(SortScratch* s, size_t max_n) {
+cudaError_t sort_scratch_alloc(SortScratch* s, size_t max_n, cudaStream_t st) {
     *s = SortScratch{};
     s->max_tiles = sort_max_tiles(max_n);
     s->max_n = max_n;
@@ -213,10 +213,10 @@ cudaError_t sort_scratch_alloc(SortScratch* s, size_t max_n) {
     if ((e = cudaMalloc(&s->hist, kSortMaxPasses * kRadix * sizeof(unsigned int) + 64))) return e;
     if ((e = cudaMalloc(&s->tile_counter, 8 * sizeof(unsigned int)))) return e;
     if ((e = cudaMalloc(&s->epoch, sizeof(unsigned long long)))) return e;
-    if ((e = cudaMemset(s->epoch, 0, sizeof(unsigned long long)))) return e;
+    if ((e = cudaMemsetAsync(s->epoch, 0, sizeof(unsigned long long), st))) return e;
     size_t lb = kSortMaxPasses * s->max_tiles * kRadix * sizeof(unsigned long long);
     if ((e = cudaMalloc(&s->lookback, lb))) return e;
-    if ((e = cudaMemset(s->lookback, 0, lb))) return e;
+    if ((e = cudaMemsetAsync(s->lookback, 0, lb, st))) return e;
     if ((e = cudaMalloc(&s->alt_keys, (max_n + 64) * sizeof(uint64_t)))) return e;
     if ((e = cudaMalloc(&s->alt_vals, (max_n + 64) * sizeof(uint32_t)))) return e;
     return cudaSuccess;
