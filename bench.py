@@ -353,9 +353,10 @@ def run_gpu(args, rank, world, local):
         traffic = float(tr["bytes_per_voxel"] * float((n0 + n1).mean()) + tr.get("bytes_fixed", 0.0))
     # per frame: frame set-up, splat+emit, sort (prepare, histogram, 4 passes),
     # merge partition, merge+update; ICP: begin, one step per iteration, the
-    # next target's back-projection; a mesh call is 6 launches
+    # next target's back-projection; a mesh is 7 launches (snapshot, row
+    # directory, classification, two scan kernels, two emission passes)
     launches_per_frame = 10 + (ICP_ITERS + 2)
-    gpu_launches = K * launches_per_frame + (K // MESH_EVERY) * 6
+    gpu_launches = K * launches_per_frame + (K // MESH_EVERY) * 7
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
         "warmup": Wu, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
