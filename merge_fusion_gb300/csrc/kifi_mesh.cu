@@ -265,17 +265,32 @@ __global__ void __launch_bounds__(kThreads) k_mesh_emit(const K* __restrict__ ke
         missing_bound = *missing_bound_dev;
         if (missing_bound == ~0ull) return;
     }
-    for (unsigned int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
-        const unsigned int f = flags[i];
-        if (f == 0) continue;
+    // Indices are emitted warp-cooperatively: the warp's 32 voxels stage their
+    // case word, corner indices and first output slot in shared memory, and
+    // all lanes walk the warp's indices together (a lane finds its voxel by a
+    // search over the prefix of the voxels' index counts), so a warp does
+    // not wait on its lane with the most triangles.
+    constexpr int kWarps = kThreads / 32;
+    __shared__ unsigned int s_cidx[kWarps][8][32];
+    __shared__ uint64_t s_mcw[kWarps][32];
+    __shared__ unsigned int s_first[kWarps][32];
+    __shared__ unsigned int s_excl[kWarps][33];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned int warps = gridDim.x * kWarps;
+    for (unsigned int base = (blockIdx.x * kWarps + warp) * 32u; base < n; base += warps * 32u) {
+        const unsigned int i = base + lane;
+        const unsigned int f = i < n ? flags[i] : 0u;
         unsigned int cidx[8];
-        stored_cube(i, corners[i], cidx);
-        const K key = keys[i];
-        const unsigned long long s = scan_at(scan, tile_offsets, i);
-        const unsigned int vbase = (unsigned int)(s & 0xffffffffu);
+        unsigned long long s = 0;
+        if (f) {
+            stored_cube(i, corners[i], cidx);
+            s = scan_at(scan, tile_offsets, i);
+        }
         const unsigned int axes = f & 7u;
-        // vertices (Mesher.cpp:134-168)
+        // vertices (Mesher.cpp:134-168): at most three per voxel, by the voxel's lane
         if (axes) {
+            const K key = keys[i];
+            const unsigned int vbase = (unsigned int)(s & 0xffffffffu);
             const unsigned int nv = __popc(axes);
             const unsigned long long first =
                 kTris ? vbase : n_verts - vbase - nv;  // ascending ids / generation order
@@ -299,34 +314,59 @@ __global__ void __launch_bounds__(kThreads) k_mesh_emit(const K* __restrict__ ke
                 ++r;
             }
         }
-        if (!kTris) continue;
-        const unsigned int ni = (f >> 8) & 0xffu;
-        if (!ni) continue;
-        const uint64_t mcw = s_mc[(f >> 16) & 0xffu];  // the case's triangle edges
-        const unsigned int ibase = (unsigned int)(s >> 32);
-        const unsigned long long first = n_idx - ibase - ni;  // generation order
-        unsigned long long local_min = ~0ull;
-        for (unsigned int t = 0; t < ni; ++t) {
-            const int e = mc_tri_edge_of(mcw, (int)t);
-            const int corner = edge_corner(e), axis = edge_axis(e);
-            const unsigned int ci = cidx[corner];
-            // the edge id 3 * key + axis: 32 bits wide for 30-bit keys (as in the
-            // reference); for 64-bit keys the stop rule compares full ids and an id
-            // written in place of a missing vertex keeps its low 32 bits
-            const unsigned long long id = 3ull * (unsigned long long)keys[ci] + (unsigned long long)axis;
-            const unsigned int cf = flags[ci];
-            uint32_t outv;
-            if (cf >> axis & 1u) {
-                outv = (unsigned int)(scan_at(scan, tile_offsets, ci) & 0xffffffffu) +
-                       __popc(cf & 7u & ((1u << axis) - 1u));
-            } else {
-                outv = (uint32_t)id;
-                local_min = min(local_min, id);
+        if constexpr (kTris) {
+            const unsigned int ni = (f >> 8) & 0xffu;
+            unsigned int inc = ni;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned int y = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += y;
             }
-            if (id >= missing_bound) outv = (uint32_t)id;
-            idx[first + t] = outv;
+            const unsigned int total = __shfl_sync(0xffffffffu, inc, 31);
+            if (total == 0u) continue;  // warp-uniform
+            __syncwarp();  // the previous round's readers are done with the staging
+            s_excl[warp][lane] = inc - ni;
+            if (lane == 31) s_excl[warp][32] = inc;
+            if (ni) {
+                s_mcw[warp][lane] = s_mc[(f >> 16) & 0xffu];  // the case's triangle edges
+                s_first[warp][lane] = (unsigned int)(n_idx - (s >> 32) - ni);  // generation order
+#pragma unroll
+                for (int k = 0; k < 8; ++k) s_cidx[warp][k][lane] = cidx[k];
+            }
+            __syncwarp();
+            unsigned long long local_min = ~0ull;
+            for (unsigned int j = lane; j < total; j += 32u) {
+                // v = the last voxel whose exclusive prefix is <= j (it has ni > 0)
+                int v = 0;
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1)
+                    if (s_excl[warp][v + step] <= j) v += step;
+                const unsigned int t = j - s_excl[warp][v];
+                const int e = mc_tri_edge_of(s_mcw[warp][v], (int)t);
+                const int corner = edge_corner(e), axis = edge_axis(e);
+                const unsigned int ci = s_cidx[warp][corner][v];
+                const unsigned int cf = flags[ci];
+                const bool has = (cf >> axis & 1u) != 0u;
+                // the edge id 3 * key + axis, needed for a missing vertex and on the
+                // stop rule's re-run: 32 bits wide for 30-bit keys (as in the reference);
+                // for 64-bit keys the stop rule compares full ids and an id written in
+                // place of a missing vertex keeps its low 32 bits
+                const bool need_id = !has || missing_bound != ~0ull;
+                const unsigned long long id =
+                    need_id ? 3ull * (unsigned long long)keys[ci] + (unsigned long long)axis : 0ull;
+                uint32_t outv;
+                if (has) {
+                    outv = (unsigned int)(scan_at(scan, tile_offsets, ci) & 0xffffffffu) +
+                           __popc(cf & 7u & ((1u << axis) - 1u));
+                } else {
+                    outv = (uint32_t)id;
+                    local_min = min(local_min, id);
+                }
+                if (need_id && id >= missing_bound) outv = (uint32_t)id;
+                idx[(unsigned long long)s_first[warp][v] + t] = outv;
+            }
+            if (local_min != ~0ull && missing_min) atomicMin(missing_min, local_min);
         }
-        if (local_min != ~0ull && missing_min) atomicMin(missing_min, local_min);
     }
 }
 
