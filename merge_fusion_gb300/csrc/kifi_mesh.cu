@@ -9,15 +9,18 @@
 // a closed form that depends on voxel i alone, so every voxel is handled by
 // its own thread:
 //
-//  k_row_directory  start index of every (y, z) key row (key >> 10); a
-//                   neighbour search then only scans one row of keys.
+//  k_row_directory  start index of every (y, z) key row (key >> b, b key bits
+//                   per axis); a neighbour search then only scans one row,
+//                   starting where the searching voxel sits in its own row.
 //  k_mesh_classify  per voxel i in [0, n-2] with weight > 0: which of its
 //                   +x/+y/+z edges carry a vertex (Mesher.cpp:140-168) and,
 //                   for Mesh(verts, indices), the cube's marching-cubes case
-//                   and triangle count (:172-226).
-//  (scan)           one exclusive scan of the packed (vertex, index) counts
-//                   in ascending voxel order.
-//  k_mesh_emit      writes the vertices and the triangle indices.
+//                   and triangle count (:172-226); a voxel with any output
+//                   keeps its +y, +z and +yz lookups for emission.
+//  k_scan_tiles,    one exclusive scan of the packed (vertex, index) counts
+//  k_scan_sums      in ascending voxel order (per tile, then the tile sums).
+//  k_mesh_emit      writes the vertices (by the voxel's lane) and the
+//                   triangle indices (spread over the warp's lanes).
 //
 // Output order equals the reference's:
 //  * Mesh(verts): vertices in generation order -- voxels descending, axes
@@ -27,8 +30,9 @@
 //    descending, table order), each index mapped to its vertex's rank
 //    (:28-44).  That mapping walk stops at the first index id that has no
 //    vertex; every index id at or above it keeps its raw id.  k_mesh_emit
-//    reproduces this: it records the smallest missing id, and when one exists
-//    the host runs it again with that bound.
+//    reproduces this: its first pass records the smallest missing id, and a
+//    second pass reads that bound on the device and rewrites the indices at
+//    or above it (it returns at once when no id was missing).
 #include "kifi_internal.h"
 #include "mc_table.cuh"
 
