@@ -16,12 +16,16 @@
 //  moments       the associated pairs are not stored: count, sum p, sum q,
 //                sum p q^T and the squared distances are accumulated per
 //                CTA in float-float, each product split exactly by an FMA.
-//  finisher      the last CTA totals the per-CTA partials, and one thread
+//  finisher      the last CTA totals the per-CTA partials, and one warp
 //                forms the centroids and the centred cross-covariance
 //                (:166-197), Horn's matrix (:199-213), its dominant
 //                eigenvector (:215-231), R and t (:233-261) and the pose
 //                update (:20-28), without double precision (see the Horn
 //                solve below).
+//
+// Consecutive steps are programmatic dependent launches: the next step's
+// grid is scheduled once every CTA has finished its association, and waits
+// (griddepcontrol.wait) for the finisher before it reads the pose.
 //
 // The per-point arithmetic follows the reference's float expression order
 // and x86 float-to-int conversion (CVTTSS2SI: truncation, INT_MIN for NaN or
