@@ -177,28 +177,38 @@ __device__ __forceinline__ float scan_staged(const float4* __restrict__ sp, int 
                                              float dw2, int* best_rc) {
     float b0 = 0.01f, b1 = 0.01f, b2 = 0.01f;
     int i0 = 0x7fffffff, i1 = 0x7fffffff, i2 = 0x7fffffff;
-    auto cand = [&](int at, int rc, float& b, int& bi) {
+    // a candidate records only its column (a constant of the unrolled row);
+    // the row is folded in once per row for the chains whose best moved
+    auto cand = [&](int at, int c, float& b, int& bc) {
         const float4 q = sp[at];
         const float dx = fsub(q.x, px), dy = fsub(q.y, py), dz = fsub(q.z, pz);
         const float zz = kW ? fadd(fmul(dz, dz), dw2) : fmul(dz, dz);
         const float l2 = fadd(fadd(fmul(dx, dx), fmul(dy, dy)), zz);
         if (l2 < b) {
             b = l2;
-            bi = rc;
+            bc = c;
         }
     };
     if (nc == 21) {
         for (int r = 0; r < nr; ++r, base += pitch) {
+            int c0 = -1, c1 = -1, c2 = -1;
 #pragma unroll
             for (int c = 0; c < 21; c += 3) {
-                cand(base + c, r * 32 + c, b0, i0);
-                cand(base + c + 1, r * 32 + c + 1, b1, i1);
-                cand(base + c + 2, r * 32 + c + 2, b2, i2);
+                cand(base + c, c, b0, c0);
+                cand(base + c + 1, c + 1, b1, c1);
+                cand(base + c + 2, c + 2, b2, c2);
             }
+            const int r32 = r * 32;
+            if (c0 >= 0) i0 = r32 + c0;
+            if (c1 >= 0) i1 = r32 + c1;
+            if (c2 >= 0) i2 = r32 + c2;
         }
     } else {
-        for (int r = 0; r < nr; ++r, base += pitch)
-            for (int c = 0; c < nc; ++c) cand(base + c, r * 32 + c, b0, i0);
+        for (int r = 0; r < nr; ++r, base += pitch) {
+            int c0 = -1;
+            for (int c = 0; c < nc; ++c) cand(base + c, c, b0, c0);
+            if (c0 >= 0) i0 = r * 32 + c0;
+        }
     }
     if (b1 < b0 || (b1 == b0 && i1 < i0)) {
         b0 = b1;
