@@ -98,20 +98,20 @@ __device__ __forceinline__ float load_depth(const void* depth, size_t i, bool u1
     return __ldg((const float*)depth + i);
 }
 
-// Last CTA to arrive returns true; resets the counter.  Thread 0's fences
-// order the whole CTA's earlier stores (the barrier makes them visible to it)
-// before the count, and the count before the last CTA's reads.
+// Last CTA to arrive returns true; resets the counter.  Thread 0's atomic
+// orders the whole CTA's earlier stores (the barrier makes them visible to
+// it) before the count, and the count before the last CTA's reads.
 __device__ __forceinline__ bool last_cta(unsigned int* counter) {
     __shared__ bool last;
     __syncthreads();
     if (threadIdx.x == 0) {
-        __threadfence();
-        const unsigned int prev = atomicAdd(counter, 1u);
+        // one acquire-release atomic at gpu scope: the release (cumulative
+        // over the CTA's writes ordered before it by the barrier) publishes
+        // this CTA's partials; the acquire lets the last CTA read everyone's
+        unsigned int prev;
+        asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(prev) : "l"(counter) : "memory");
         last = (prev == gridDim.x - 1);
-        if (last) {
-            *counter = 0u;
-            __threadfence();
-        }
+        if (last) *counter = 0u;  // read again only by the next launch
     }
     __syncthreads();
     return last;
