@@ -162,6 +162,40 @@ constexpr int kTileCols = 8, kTileRows = 32;
 constexpr int kSplitRow = 10;   // window rows [0, 10) to the lower half-warp set, [10, 21) to the upper
 constexpr int kStageBatch = 4;  // staging loads in flight per thread
 constexpr int kStagePixels = 3840;  // float4 per pixel: 60 KB
+constexpr int kPredMargin = 2;      // pixels added around a predicted window box
+
+// The target pixels [x0, x0 + w) x [y0, y0 + h) (linear index y * synth_w + x,
+// as the reference reads them) into `stage` with row pitch `pitch`, by the
+// whole CTA: kStageBatch independent loads in flight per thread, then the
+// stores.  (0,0,0) is no point (ICP.cpp:112) and is staged as NaN; indices
+// past the buffer's end are invalid points too.
+__device__ __forceinline__ void stage_region(float4* __restrict__ stage, const float4* __restrict__ synth,
+                                             size_t n_synth, int synth_w, int x0, int y0, int w, int h,
+                                             int pitch) {
+    const int total = w * h;
+    for (int i0 = threadIdx.x; i0 < total; i0 += kStageBatch * blockDim.x) {
+        float4 q[kStageBatch];
+#pragma unroll
+        for (int k = 0; k < kStageBatch; ++k) {
+            const int i = i0 + k * blockDim.x;
+            q[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (i < total) {
+                const int ry = i / w, rx = i - ry * w;
+                const size_t at = (size_t)(y0 + ry) * synth_w + (x0 + rx);
+                if (at < n_synth) q[k] = __ldg(synth + at);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kStageBatch; ++k) {
+            const int i = i0 + k * blockDim.x;
+            if (i < total) {
+                const int ry = i / w, rx = i - ry * w;
+                if (q[k].x == 0.0f && q[k].y == 0.0f && q[k].z == 0.0f) q[k].x = __int_as_float(0x7fffffff);
+                stage[ry * pitch + rx] = q[k];
+            }
+        }
+    }
+}
 
 // Scan of one thread's window in the staged region (float4 per pixel,
 // `base` = its first candidate, odd row pitch).  Invalid target points were
@@ -274,14 +308,45 @@ __global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step(IcpArgs a, IcpSta
     // Steps are launched programmatically behind one another: this grid may
     // start while the previous step's last CTA still updates the pose.  Wait
     // for that grid (and its memory) before touching the ICP state.
-    asm volatile("griddepcontrol.wait;" ::: "memory");
     const int n_cols = (a.width + 3) / 4;
     const int tiles_x = (n_cols + kTileCols - 1) / kTileCols;
     const int tiles_y = (a.height + kTileRows - 1) / kTileRows;
+    const size_t n_synth = (size_t)a.synth_w * a.synth_h;
+    // While the previous step may still be finishing: stage the box this
+    // CTA's first tile covered then, plus a margin -- windows move little
+    // between steps.  The box is read by one thread (it may be stale or
+    // half-updated; any box is only a guess) and shared, so every thread
+    // stages the same region; after the wait the guess is used only if it
+    // holds every window.
+    __shared__ int s_pred[4];
+    if (threadIdx.x == 0) {
+        int p[4] = {0, 0, 0, 0};
+        if (blockIdx.x < tiles_x * tiles_y) {
+            const volatile int* tb = st->tile_box + 4 * blockIdx.x;
+            const int b0 = tb[0], b1 = tb[1], b2 = tb[2], b3 = tb[3];
+            if (b2 > b0 && b3 > b1 && b0 >= 0 && b1 >= 0) {
+                const int x0 = max(b0 - kPredMargin, 0), y0 = max(b1 - kPredMargin, 0);
+                const int w = b2 + kPredMargin - x0, h = b3 + kPredMargin - y0;
+                if (w <= kStagePixels && h <= kStagePixels && (w | 1) * h <= kStagePixels) {
+                    p[0] = x0;
+                    p[1] = y0;
+                    p[2] = w;
+                    p[3] = h;
+                }
+            }
+        }
+        s_pred[0] = p[0];
+        s_pred[1] = p[1];
+        s_pred[2] = p[2];
+        s_pred[3] = p[3];
+    }
+    __syncthreads();
+    const int px0 = s_pred[0], py0 = s_pred[1], pw = s_pred[2], ph = s_pred[3];
+    if (pw > 0) stage_region(stage, a.synth, n_synth, a.synth_w, px0, py0, pw, ph, pw | 1);
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int wcol = warp >> 1, half = warp & 1;
     const float half_w = fmul((float)a.synth_w, 0.5f), half_h = fmul((float)a.synth_h, 0.5f);
-    const size_t n_synth = (size_t)a.synth_w * a.synth_h;
     if (threadIdx.x < kMoments) s_acc[threadIdx.x] = FF{0.0f, 0.0f};
     if (threadIdx.x == 0) s_count = 0u;
     if (threadIdx.x == 0) atomicMin(&st->t_start, global_ns());
@@ -331,36 +396,27 @@ __global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step(IcpArgs a, IcpSta
             }
         }
         __syncthreads();
-        const int bx0 = s_box[0], by0 = s_box[1], bx1 = s_box[2], by1 = s_box[3];
-        const int bw = bx1 - bx0, bh = by1 - by0;
-        const int pitch = bw | 1;  // odd pitch: vertically adjacent windows hit distinct banks
-        const bool staged = bx1 >= 0 && pitch * bh <= kStagePixels;
-        if (staged) {
-            // kStageBatch independent loads in flight per thread, then the stores
-            const int total = bw * bh;
-            for (int i0 = threadIdx.x; i0 < total; i0 += kStageBatch * kAssocThreads) {
-                float4 q[kStageBatch];
-#pragma unroll
-                for (int k = 0; k < kStageBatch; ++k) {
-                    const int i = i0 + k * kAssocThreads;
-                    q[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-                    if (i < total) {
-                        const int ry = i / bw, rx = i - ry * bw;
-                        const size_t at = (size_t)(by0 + ry) * a.synth_w + (bx0 + rx);
-                        if (at < n_synth) q[k] = __ldg(a.synth + at);
-                    }
-                }
-#pragma unroll
-                for (int k = 0; k < kStageBatch; ++k) {
-                    const int i = i0 + k * kAssocThreads;
-                    if (i < total) {
-                        const int ry = i / bw, rx = i - ry * bw;
-                        // (0,0,0) = no point (ICP.cpp:112): stage it as NaN
-                        if (q[k].x == 0.0f && q[k].y == 0.0f && q[k].z == 0.0f) q[k].x = __int_as_float(0x7fffffff);
-                        stage[ry * pitch + rx] = q[k];
-                    }
-                }
-            }
+        const int ax0 = s_box[0], ay0 = s_box[1], ax1 = s_box[2], ay1 = s_box[3];
+        // the prefetched region if it holds every window of the tile, else stage the box now
+        const bool use_pred = tile == (int)blockIdx.x && pw > 0 && ax1 >= 0 && ax0 >= px0 && ay0 >= py0 &&
+                              ax1 <= px0 + pw && ay1 <= py0 + ph;
+        int bx0 = ax0, by0 = ay0, pitch = (ax1 - ax0) | 1;  // odd pitch: adjacent windows hit distinct banks
+        bool staged;
+        if (use_pred) {
+            bx0 = px0;
+            by0 = py0;
+            pitch = pw | 1;
+            staged = true;
+        } else {
+            staged = ax1 >= 0 && pitch * (ay1 - ay0) <= kStagePixels;
+            if (staged) stage_region(stage, a.synth, n_synth, a.synth_w, ax0, ay0, ax1 - ax0, ay1 - ay0, pitch);
+        }
+        if (threadIdx.x == 0 && tile < kIcpMaxCtas && ax1 >= 0) {
+            int* tb = st->tile_box + 4 * tile;
+            tb[0] = ax0;
+            tb[1] = ay0;
+            tb[2] = ax1;
+            tb[3] = ay1;
         }
         __syncthreads();
         // this thread's rows of the window

@@ -147,6 +147,7 @@ struct IcpState {
     unsigned long long t_start, t_body;  // globaltimer stamps of the running step
     IcpIterStats stats[kIcpMaxStats];
     float part[34 * kIcpMaxCtas];   // per-CTA float-float partials: hi, lo rows of 17 components
+    int tile_box[4 * kIcpMaxCtas];  // each tile's window box in the last step: x0, y0, x1, y1
 };
 
 cudaError_t icp_init_device();
