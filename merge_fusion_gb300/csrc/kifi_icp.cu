@@ -343,6 +343,16 @@ __global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step(IcpArgs a, IcpSta
     __syncthreads();
     const int px0 = s_pred[0], py0 = s_pred[1], pw = s_pred[2], ph = s_pred[3];
     if (pw > 0) stage_region(stage, a.synth, n_synth, a.synth_w, px0, py0, pw, ph, pw | 1);
+    // this thread's source of the first tile in eye space (no pose needed yet)
+    const int lane0 = threadIdx.x & 31, wcol0 = (threadIdx.x >> 5) >> 1;
+    float pre_d = 0.0f;
+    {
+        const int t0 = blockIdx.x;
+        if (t0 < tiles_x * tiles_y) {
+            const int col = (t0 % tiles_x) * kTileCols + wcol0, y = (t0 / tiles_x) * kTileRows + lane0;
+            if (col < n_cols && y < a.height) pre_d = load_depth(a.depth, (size_t)y * a.width + col * 4, a.depth_u16);
+        }
+    }
     asm volatile("griddepcontrol.wait;" ::: "memory");
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int wcol = warp >> 1, half = warp & 1;
@@ -358,7 +368,7 @@ __global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step(IcpArgs a, IcpSta
         int u = 0, v = 0, nr = 0, nc = 0;
         if (mine) {
             const int x = col * 4;
-            const float d = load_depth(a.depth, (size_t)y * a.width + x, a.depth_u16);
+            const float d = tile == (int)blockIdx.x ? pre_d : load_depth(a.depth, (size_t)y * a.width + x, a.depth_u16);
             if (0.0f != d) {
                 float pt[4], cl[4];
                 pt[0] = fmul(fadd(fmul((float)x, a.fl_inv_x), a.pp_x), d);
