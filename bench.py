@@ -327,6 +327,8 @@ def run_gpu(args, rank, world, local):
         i = t0 + K + j
         check(lib.kifi_pipeline_integrate(pipe, C.c_void_p(pinned[K + j].data_ptr()), 1,
                                           ptr(w2e[i]), ptr(out_pose)), "e2e frame %d" % i)
+    # each call returns with its tracked pose; the last frames' fusion finishes inside the timing
+    check(lib.kifi_pipeline_sync(pipe, None), "e2e sync")
     e2e_s = time.perf_counter() - te0
     e2e_s = max_over_ranks(e2e_s, world)
     nv, ni = C.c_size_t(), C.c_size_t()

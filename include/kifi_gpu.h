@@ -440,9 +440,12 @@ KIFI_API kifi_icp* kifi_pipeline_icp(kifi_pipeline* p);
  * :32-35) and, when icp_iterations > 0, tracks it by ICP against the
  * previous frame's back-projection with the previous pose as the guess (the
  * reference's tracking path, :36-55); every mesh_every frames the mesh is
- * extracted on the device.  Host frame (uint16 mm or float m); returns when
- * done, with the tracked eye-to-world pose in out_eye_to_world (the given
- * pose's inverse for the first frame or when tracking is off; may be NULL). */
+ * extracted on the device.  Host frame (uint16 mm or float m).  Returns with
+ * the tracked eye-to-world pose in out_eye_to_world (the given pose's
+ * inverse for the first frame or when tracking is off; may be NULL) once the
+ * frame's tracking is done and `depth_host` may be reused; the frame's fusion
+ * may still be running -- every call that reads the volume (and
+ * kifi_pipeline_sync) waits for it and reports its device errors. */
 KIFI_API kifi_status kifi_pipeline_integrate(kifi_pipeline* p, const void* depth_host,
                                              int depth_is_u16, const float world_to_eye[16],
                                              float out_eye_to_world[16]);

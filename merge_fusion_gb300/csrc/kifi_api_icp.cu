@@ -23,6 +23,7 @@ struct kifi_icp {
     Mat4 synth_e2w{};
     bool have_target = false;
     int last_iters = 0;
+    IcpState* head = nullptr;        // pinned host copy of the state's head (poses, statistics)
     bool record = false;             // keep the last iteration's association
     long long* pairs = nullptr;      // per source: target index, or -1
     float* pairs_len2 = nullptr;     // per source: len^2
@@ -132,6 +133,7 @@ kifi_status kifi_icp_create(int device, void* stream, kifi_icp** out) {
         }
     }
     if (!e) e = cudaMalloc(&c->st, sizeof(IcpState));
+    if (!e) e = cudaMallocHost(&c->head, offsetof(IcpState, part));
     if (!e) e = cudaMemsetAsync(c->st, 0, sizeof(IcpState), c->stream);  // ordered before the context's work
     if (e) {
         kifi_icp_destroy(c);
@@ -154,6 +156,7 @@ kifi_status kifi_icp_destroy(kifi_icp* c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     cudaFree(c->st);
+    cudaFreeHost(c->head);
     cudaFree(c->depth_dev);
     cudaFree(c->synth);
     cudaFree(c->pairs);
@@ -259,16 +262,11 @@ kifi_status kifi_icp_result(kifi_icp* c, float out_eye_to_world[16], double out_
                             int* n_assoc, double* rms, int capacity, int* iterations) {
     if (!c) return fail(KIFI_ERR_INVALID_ARGUMENT, "null context");
     KIFI_CUDA(cudaSetDevice(c->device));
-    // read the head of the state: poses and per-iteration statistics
-    const size_t head = offsetof(IcpState, part);
-    IcpState* h = (IcpState*)std::malloc(head);
-    if (!h) return fail(KIFI_ERR_OUT_OF_MEMORY, "host allocation");
-    cudaError_t e = cudaMemcpyAsync(h, c->st, head, cudaMemcpyDeviceToHost, c->stream);
+    // read the head of the state: poses and per-iteration statistics (pinned)
+    IcpState* h = c->head;
+    cudaError_t e = cudaMemcpyAsync(h, c->st, offsetof(IcpState, part), cudaMemcpyDeviceToHost, c->stream);
     if (!e) e = cudaStreamSynchronize(c->stream);
-    if (e) {
-        std::free(h);
-        return cuda_fail(e, "ICP result");
-    }
+    if (e) return cuda_fail(e, "ICP result");
     if (out_eye_to_world) std::memcpy(out_eye_to_world, h->pose_f, 64);
     if (out_eye_to_world_d)
         for (int i = 0; i < 16; ++i) out_eye_to_world_d[i] = (double)h->pose_f[i] + (double)h->pose_lo[i];
@@ -278,7 +276,6 @@ kifi_status kifi_icp_result(kifi_icp* c, float out_eye_to_world[16], double out_
         if (n_assoc) n_assoc[i] = h->stats[i].n_assoc;
         if (rms) rms[i] = h->stats[i].rms;
     }
-    std::free(h);
     return KIFI_OK;
 }
 
@@ -286,22 +283,16 @@ kifi_status kifi_icp_iteration_times(kifi_icp* c, float* body_us, float* tail_us
                                      int* iterations) {
     if (!c) return fail(KIFI_ERR_INVALID_ARGUMENT, "null context");
     KIFI_CUDA(cudaSetDevice(c->device));
-    const size_t head = offsetof(IcpState, part);
-    IcpState* h = (IcpState*)std::malloc(head);
-    if (!h) return fail(KIFI_ERR_OUT_OF_MEMORY, "host allocation");
-    cudaError_t e = cudaMemcpyAsync(h, c->st, head, cudaMemcpyDeviceToHost, c->stream);
+    IcpState* h = c->head;
+    cudaError_t e = cudaMemcpyAsync(h, c->st, offsetof(IcpState, part), cudaMemcpyDeviceToHost, c->stream);
     if (!e) e = cudaStreamSynchronize(c->stream);
-    if (e) {
-        std::free(h);
-        return cuda_fail(e, "ICP timings");
-    }
+    if (e) return cuda_fail(e, "ICP timings");
     const int it = h->iter < kIcpMaxStats ? h->iter : kIcpMaxStats;
     if (iterations) *iterations = h->iter;
     for (int i = 0; i < it && i < capacity; ++i) {
         if (body_us) body_us[i] = h->stats[i].body_us;
         if (tail_us) tail_us[i] = h->stats[i].tail_us;
     }
-    std::free(h);
     return KIFI_OK;
 }
 

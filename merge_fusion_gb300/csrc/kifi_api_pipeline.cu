@@ -231,6 +231,22 @@ kifi_status frame_graph(kifi_pipeline* p, const void* host_src, size_t bytes, co
     return KIFI_OK;
 }
 
+// The caller's result of a host frame: the tracked pose.  Tracking waits for
+// the frame's upload, so once its result is in the host frame is free; the
+// frame's fusion may still run (every call that reads the volume waits for it
+// and reports its device errors, as after kifi_pipeline_integrate_device).
+kifi_status frame_result(kifi_pipeline* p, int k, float out_eye_to_world[16]) {
+    if (p->desc.icp_iterations > 0) {
+        if (p->frame > 1)
+            return kifi_icp_result(p->icp, out_eye_to_world, nullptr, nullptr, nullptr, 0, nullptr);
+        KIFI_CUDA(cudaStreamSynchronize(p->is));  // the first frame only sets the target
+    } else {
+        KIFI_CUDA(cudaEventSynchronize(p->uploaded[k]));
+    }
+    if (out_eye_to_world) std::memcpy(out_eye_to_world, p->prev_e2w, 64);
+    return KIFI_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -365,7 +381,7 @@ kifi_status kifi_pipeline_integrate(kifi_pipeline* p, const void* depth_host, in
     KIFI_CUDA(cudaEventRecord(p->uploaded[k], p->vs));
     kifi_status s = track_and_fuse(p, p->slot[k], depth_is_u16 != 0, k, world_to_eye);
     if (s) return s;
-    return kifi_pipeline_sync(p, out_eye_to_world);
+    return frame_result(p, k, out_eye_to_world);
 }
 
 kifi_status kifi_pipeline_sync(kifi_pipeline* p, float out_eye_to_world[16]) {
