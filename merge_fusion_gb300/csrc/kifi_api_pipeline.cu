@@ -145,9 +145,8 @@ kifi_status track_and_fuse(kifi_pipeline* p, const void* depth_dev, bool u16, in
     const kifi_camera& cam = p->desc.camera;
     kifi_status s = mesh_poll(p, false);
     if (s) return s;
-    // fusion on the volume's stream
-    if ((s = kifi_integrate_device(p->vol, depth_dev, u16 ? 1 : 0, &cam, world_to_eye))) return s;
-    // tracking on the ICP stream, once the frame is on the device
+    // tracking on the ICP stream, once the frame is on the device; enqueued
+    // first, as it is the frame's critical path
     const Mat4 e2w = invert_transform(load_mat(world_to_eye));
     if (p->desc.icp_iterations > 0) {
         if (k >= 0) KIFI_CUDA(cudaStreamWaitEvent(p->is, p->uploaded[k], 0));
@@ -160,6 +159,8 @@ kifi_status track_and_fuse(kifi_pipeline* p, const void* depth_dev, bool u16, in
             return s;
         if (k >= 0) KIFI_CUDA(cudaEventRecord(p->released[k], p->is));
     }
+    // fusion on the volume's stream
+    if ((s = kifi_integrate_device(p->vol, depth_dev, u16 ? 1 : 0, &cam, world_to_eye))) return s;
     std::memcpy(p->prev_e2w, e2w.m, 64);
     p->have_prev = true;
     ++p->frame;
