@@ -331,6 +331,24 @@ def run_gpu(args, rank, world, local):
     check(lib.kifi_pipeline_sync(pipe, None), "e2e sync")
     e2e_s = time.perf_counter() - te0
     e2e_s = max_over_ranks(e2e_s, world)
+
+    # the merge kernel with tracking idle: a few fusion-only frames after the
+    # timed regions (the last rendered frame again, on the pipeline's volume)
+    ISO = 5
+    check(lib.kifi_volume_set_profiling(vol, 1))
+    check(lib.kifi_volume_stage_times(vol, ptr(ms_stage), C.byref(nst)))  # reset
+    for _ in range(ISO):
+        check(lib.kifi_integrate_device(vol, C.c_void_p(frames[n_frames - 1].data_ptr()), 1, C.byref(cam),
+                                        ptr(w2e[n_frames - 1])), "isolated frame")
+    iso_stage = np.zeros(4)
+    check(lib.kifi_volume_stage_times(vol, ptr(iso_stage), C.byref(nst)))
+    check(lib.kifi_volume_set_profiling(vol, 0))
+    i0, ie, i1 = np.zeros(64, np.uint64), np.zeros(64, np.uint64), np.zeros(64, np.uint64)
+    check(lib.kifi_volume_frame_log(vol, ptr(i0), ptr(ie), ptr(i1), 64, C.byref(cnt)))
+    iso_bytes = float((12.0 * i0[cnt.value - ISO:cnt.value].astype(np.float64) + 4.0 * ie[cnt.value - ISO:cnt.value] +
+                       12.0 * i1[cnt.value - ISO:cnt.value] + 2.0 * W * H).mean())
+    iso_ms = iso_stage[3] / max(nst.value, 1)
+
     nv, ni = C.c_size_t(), C.c_size_t()
     check(lib.kifi_pipeline_mesh_counts(pipe, C.byref(nv), C.byref(ni)))
     gb, gu = C.c_longlong(), C.c_longlong()
@@ -374,7 +392,12 @@ def run_gpu(args, rank, world, local):
                      "kernel": "k_merge_update (fused merge-path union + TSDF update)",
                      "peak_source": peak_kind,
                      "bytes_per_launch": float(algo_bytes.mean()),
-                     "ms_per_launch": merge_ms},
+                     "ms_per_launch": merge_ms,
+                     "isolated": {"ms_per_launch": iso_ms, "achieved": iso_bytes / (iso_ms * 1e-3) / 1e9,
+                                  "frac": iso_bytes / (iso_ms * 1e-3) / 1e9 / peak, "bytes_per_launch": iso_bytes,
+                                  "frames": ISO,
+                                  "note": "fusion-only frames after the timed regions, tracking idle; inside the "
+                                          "pipeline the merge yields SMs to the higher-priority tracking steps"}},
         "stage_ms_per_frame": {"splat_emit": ms_stage[0] / max(nst.value, 1),
                                "sort": ms_stage[1] / max(nst.value, 1),
                                "merge_partition": ms_stage[2] / max(nst.value, 1),
