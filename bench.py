@@ -274,6 +274,7 @@ def run_gpu(args, rank, world, local):
                                        ptr(w2e[Fp + Wu]), 1, ptr(tuned)), "autotune")
     n_resident = C.c_size_t()
     check(lib.kifi_volume_size(vol, C.byref(n_resident)))
+    n_start = int(n_resident.value)  # resident voxels when the timed frames begin
 
     # bounded CPU baseline starts from the same resident volume
     resident = None
@@ -335,19 +336,22 @@ def run_gpu(args, rank, world, local):
     # the merge kernel with tracking idle: a few fusion-only frames after the
     # timed regions (the last rendered frame again, on the pipeline's volume)
     ISO = 5
+    iso_stage = np.zeros(4)
+    iso_n = C.c_int()
     check(lib.kifi_volume_set_profiling(vol, 1))
-    check(lib.kifi_volume_stage_times(vol, ptr(ms_stage), C.byref(nst)))  # reset
+    check(lib.kifi_volume_stage_times(vol, ptr(iso_stage), C.byref(iso_n)))  # reset
     for _ in range(ISO):
         check(lib.kifi_integrate_device(vol, C.c_void_p(frames[n_frames - 1].data_ptr()), 1, C.byref(cam),
                                         ptr(w2e[n_frames - 1])), "isolated frame")
-    iso_stage = np.zeros(4)
-    check(lib.kifi_volume_stage_times(vol, ptr(iso_stage), C.byref(nst)))
+    check(lib.kifi_volume_stage_times(vol, ptr(iso_stage), C.byref(iso_n)))
     check(lib.kifi_volume_set_profiling(vol, 0))
     i0, ie, i1 = np.zeros(64, np.uint64), np.zeros(64, np.uint64), np.zeros(64, np.uint64)
-    check(lib.kifi_volume_frame_log(vol, ptr(i0), ptr(ie), ptr(i1), 64, C.byref(cnt)))
-    iso_bytes = float((12.0 * i0[cnt.value - ISO:cnt.value].astype(np.float64) + 4.0 * ie[cnt.value - ISO:cnt.value] +
-                       12.0 * i1[cnt.value - ISO:cnt.value] + 2.0 * W * H).mean())
-    iso_ms = iso_stage[3] / max(nst.value, 1)
+    iso_cnt = C.c_int()
+    check(lib.kifi_volume_frame_log(vol, ptr(i0), ptr(ie), ptr(i1), 64, C.byref(iso_cnt)))
+    lo, hi = iso_cnt.value - ISO, iso_cnt.value
+    iso_bytes = float((12.0 * i0[lo:hi].astype(np.float64) + 4.0 * ie[lo:hi] + 12.0 * i1[lo:hi] +
+                       2.0 * W * H).mean())
+    iso_ms = iso_stage[3] / max(iso_n.value, 1)
 
     nv, ni = C.c_size_t(), C.c_size_t()
     check(lib.kifi_pipeline_mesh_counts(pipe, C.byref(nv), C.byref(ni)))
@@ -383,8 +387,9 @@ def run_gpu(args, rank, world, local):
         "vs_baseline": None, "dtype": "f32+u32", "data": "synthetic",
         "config": {"workload": "room 4x3x4 m, 40 boxes + 20 spheres, 640x480 uint16 depth, "
                                "res 1024 x 4 mm, trunc 2 cm, ICP 15 it/frame, mesh every 10",
-                   "prefill_frames": Fp, "resident_voxels_start": int(n0[0]) if m else None,
+                   "prefill_frames": Fp, "resident_voxels_start": n_start,
                    "resident_voxels_end": int(n1[-1]) if m else None,
+                   "roofline_frames": "the last %d timed frames (the device frame log's length)" % m,
                    "l2": "volume (>240 MB) larger than L2; every frame is a new depth image",
                    "parallelism": "replicas" if world > 1 else "single"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
