@@ -20,6 +20,7 @@ reference's own CPU code (oracle/_ref, else the C restatement in oracle/)
 on the same workload on the host cores.
 """
 import argparse
+import atexit
 import ctypes as C
 import json
 import os
@@ -116,26 +117,45 @@ class ClockSampler:
     def __init__(self, gpu_index):
         self.gpu = gpu_index
         self.proc = None
-        self.lines = []
+        self.lines = []  # (host time, csv line)
+        self.windows = []
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
-                 "--format=csv,noheader,nounits", "-lms", "50"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            atexit.register(self.__exit__, None, None, None)  # also when a timed region raises
+            # the timed regions are tens of milliseconds: start them only
+            # once nvidia-smi is producing samples
+            t_end = time.perf_counter() + 5.0
+            while not self.lines and time.perf_counter() < t_end and self.proc.poll() is None:
+                time.sleep(0.005)
         except OSError:
             self.proc = None
         return self
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
+
+    def window(self):
+        """Context manager marking one timed region on the host clock."""
+        sampler = self
+
+        class _W:
+            def __enter__(self):
+                self.t0 = time.perf_counter()
+
+            def __exit__(self, *a):
+                sampler.windows.append((self.t0, time.perf_counter()))
+        return _W()
 
     def __exit__(self, *a):
-        if self.proc:
+        if self.proc and self.proc.poll() is None:
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -143,9 +163,21 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
+        """Median SM clock and the active throttle reasons over the samples
+        taken inside the marked windows (all samples when none was marked;
+        a window shorter than the sampling period keeps the sample nearest
+        to it)."""
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        picked = self.lines
+        if self.windows:
+            picked = []
+            for a, b in self.windows:
+                inside = [x for x in self.lines if a <= x[0] <= b]
+                if not inside and self.lines:
+                    inside = [min(self.lines, key=lambda x: min(abs(x[0] - a), abs(x[0] - b)))]
+                picked += [x for x in inside if x not in picked]
+        for _, ln in picked:
             parts = [x.strip() for x in ln.split(",")]
             if len(parts) < 9:
                 continue
@@ -160,7 +192,7 @@ class ClockSampler:
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": smax, "reasons": [], "samples": 0}
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "regions_ms": [round((b - a) * 1e3, 1) for a, b in self.windows]}
 
 
 # ------------------------------------------------------------- CPU baseline
@@ -296,7 +328,9 @@ def run_gpu(args, rank, world, local):
         dist.barrier()
     torch.cuda.synchronize()
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as clocks:
+    # one sampler over both timed regions (device-resident, then end to end)
+    clocks = ClockSampler(local).__enter__()
+    with clocks.window():
         start.record(vs)
         ist.wait_event(start)
         for i in range(t0, t0 + K):
@@ -323,14 +357,16 @@ def run_gpu(args, rank, world, local):
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
-    te0 = time.perf_counter()
-    for j in range(K):
-        i = t0 + K + j
-        check(lib.kifi_pipeline_integrate(pipe, C.c_void_p(pinned[K + j].data_ptr()), 1,
-                                          ptr(w2e[i]), ptr(out_pose)), "e2e frame %d" % i)
-    # each call returns with its tracked pose; the last frames' fusion finishes inside the timing
-    check(lib.kifi_pipeline_sync(pipe, None), "e2e sync")
-    e2e_s = time.perf_counter() - te0
+    with clocks.window():
+        te0 = time.perf_counter()
+        for j in range(K):
+            i = t0 + K + j
+            check(lib.kifi_pipeline_integrate(pipe, C.c_void_p(pinned[K + j].data_ptr()), 1,
+                                              ptr(w2e[i]), ptr(out_pose)), "e2e frame %d" % i)
+        # each call returns with its tracked pose; the last frames' fusion finishes inside the timing
+        check(lib.kifi_pipeline_sync(pipe, None), "e2e sync")
+        e2e_s = time.perf_counter() - te0
+    clocks.__exit__(None, None, None)
     e2e_s = max_over_ranks(e2e_s, world)
 
     # the merge kernel with tracking idle: a few fusion-only frames after the
