@@ -199,11 +199,14 @@ __global__ void __launch_bounds__(kEmitThreads) k_splat_emit(DeviceCtl* __restri
     }
 }
 
-// UpdateVoxels for one voxel (Integrator.cpp:273-322 for one SSE lane).
-template <bool kU16, typename K>
-__device__ __forceinline__ void update_voxel(K key, float2& val, const FrameConst& fc,
-                                             const float (&w2c)[16], const Geom& g,
-                                             const void* depth) {
+// UpdateVoxels for one voxel (Integrator.cpp:273-322 for one SSE lane),
+// split in two: the projection and range tests give the depth pixel the
+// voxel reads (or -1 when it is not updated) and its clip w; apply_depth
+// then folds that pixel's depth into the voxel.  Callers project several
+// voxels before reading any depth, so the reads are in flight together.
+template <typename K>
+__device__ __forceinline__ int project_voxel(K key, const FrameConst& fc, const float (&w2c)[16],
+                                             const Geom& g, float& w_out) {
     const Codec<K> cd(g.kb);
     // VoxelCenter: index * (vlen, vlen, vlen, 1) + (off, off, off, 0)
     float c[4];
@@ -219,14 +222,14 @@ __device__ __forceinline__ void update_voxel(K key, float2& val, const FrameCons
     const float x = row(0), y = row(1), w = row(3);
     // lane w: (w/w) * 0 + 0 lies in [-FLT_MAX, FLT_MAX) iff w/w is finite,
     // i.e. iff w is finite and non-zero (w/w is then exactly 1).
-    if (!(isfinite(w) && w != 0.0f)) return;
+    if (!(isfinite(w) && w != 0.0f)) return -1;
     // lane z: (z/w) * 0 + 0 lies in [-1, 1) iff z/w is finite.  When the
     // host has bounded |z| by 1e18 over the whole volume (fc.z_bounded), any
     // |w| >= 1e-18 keeps the quotient finite and z need not be formed.
     if (!(fc.z_bounded && fabsf(w) >= 1e-18f)) {
         const float z = row(2);
-        if (!isfinite(z)) return;
-        if (!(fabsf(z) <= 1e18f && fabsf(w) >= 1e-18f) && !isfinite(fdiv(z, w))) return;
+        if (!isfinite(z)) return -1;
+        if (!(fabsf(z) <= 1e18f && fabsf(w) >= 1e-18f) && !isfinite(fdiv(z, w))) return -1;
     }
     // u = (x/w) * W/2 + W/2 and v likewise, IEEE-exact.  Only floor(u),
     // floor(v) and the range tests use them, so first try a fast reciprocal
@@ -240,22 +243,15 @@ __device__ __forceinline__ void update_voxel(K key, float2& val, const FrameCons
     if (!fc.fast_uv) {
         const float u = fadd(fmul(fdiv(x, w), fc.half_w), fc.half_w);
         const float v = fadd(fmul(fdiv(y, w), fc.half_h), fc.half_h);
-        if (!(u >= 0.0f && u < (float)fc.width && v >= 0.0f && v < (float)fc.height)) return;
-        const size_t px = (uint32_t)u;
-        const size_t py = (size_t)fc.height - (uint32_t)v - 1;
-        const float d = load_depth(depth, py * (size_t)fc.width + px, kU16);
-        const float sd = fsub(d, w);
-        if (d > 0.0f && sd >= -g.trunc) {
-            val.x = fadd(val.x, (g.trunc < sd) ? g.trunc : sd);
-            val.y = fadd(val.y, 1.0f);
-        }
-        return;
+        if (!(u >= 0.0f && u < (float)fc.width && v >= 0.0f && v < (float)fc.height)) return -1;
+        w_out = w;
+        return (fc.height - 1 - (int)(uint32_t)v) * fc.width + (int)(uint32_t)u;
     }
     const float rw = __fdividef(1.0f, w);
     const float ua = fadd(fmul(fmul(x, rw), fc.half_w), fc.half_w);
     const float va = fadd(fmul(fmul(y, rw), fc.half_h), fc.half_h);
     const float Wf = (float)fc.width, Hf = (float)fc.height;
-    if (!(ua >= -0.5f && ua <= Wf + 0.5f && va >= -0.5f && va <= Hf + 0.5f)) return;
+    if (!(ua >= -0.5f && ua <= Wf + 0.5f && va >= -0.5f && va <= Hf + 0.5f)) return -1;
     constexpr float kE = 1.0f / 256.0f;
     float u, v;
     {
@@ -265,16 +261,41 @@ __device__ __forceinline__ void update_voxel(K key, float2& val, const FrameCons
         u = su ? fu + 0.5f : fadd(fmul(fdiv(x, w), fc.half_w), fc.half_w);
         v = sv ? fv + 0.5f : fadd(fmul(fdiv(y, w), fc.half_h), fc.half_h);
     }
-    if (!(u >= 0.0f && u < Wf && v >= 0.0f && v < Hf)) return;
-    const size_t px = (uint32_t)u;
-    const size_t py = (size_t)fc.height - (uint32_t)v - 1;
-    const float d = load_depth(depth, py * (size_t)fc.width + px, kU16);
+    if (!(u >= 0.0f && u < Wf && v >= 0.0f && v < Hf)) return -1;
+    w_out = w;
+    return (fc.height - 1 - (int)(uint32_t)v) * fc.width + (int)(uint32_t)u;
+}
+
+// depth d at the voxel's pixel, w its clip w: signedDist = d - w, updated
+// when the depth is valid and signedDist >= -trunc,
+// Voxel::Update(std::min(signedDist, trunc)) (Voxel.h:53-57)
+__device__ __forceinline__ void apply_depth(float2& val, float d, float w, const Geom& g) {
     const float sd = fsub(d, w);
     if (d > 0.0f && sd >= -g.trunc) {
-        // Voxel::Update(std::min(signedDist, trunc)) (Voxel.h:53-57)
         val.x = fadd(val.x, (g.trunc < sd) ? g.trunc : sd);
         val.y = fadd(val.y, 1.0f);
     }
+}
+
+// The TSDF update of four output voxels: the voxels at positions >= upd_end
+// (outside the reference's update range, or no voxel) keep their values.
+template <bool kU16, typename K>
+__device__ __forceinline__ void update4(const K (&key)[4], float2 (&val)[4],
+                                        const unsigned long long (&pos)[4], unsigned long long upd_end,
+                                        const FrameConst& fc, const float (&w2c)[16], const Geom& g,
+                                        const void* depth) {
+    int ix[4];
+    float w[4], d[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        w[q] = 0.0f;
+        ix[q] = pos[q] < upd_end ? project_voxel<K>(key[q], fc, w2c, g, w[q]) : -1;
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) d[q] = ix[q] >= 0 ? load_depth(depth, (size_t)ix[q], kU16) : 0.0f;
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+        if (ix[q] >= 0) apply_depth(val[q], d[q], w[q], g);
 }
 
 // number of A elements among the first d outputs of merge(A, B); A and B
@@ -364,16 +385,6 @@ __global__ void __launch_bounds__(256) k_merge_partition(DeviceCtl* __restrict__
     }
 }
 
-// One output voxel: value from A or Voxel(), TSDF update when inside the
-// reference's update range.
-template <bool kU16, typename K>
-__device__ __forceinline__ void finish_voxel(K key, float2& val, unsigned long long pos,
-                                             unsigned long long upd_end, const FrameConst& fc,
-                                             const float (&w2c)[16], const Geom& g,
-                                             const void* depth) {
-    if (pos < upd_end) update_voxel<kU16, K>(key, val, fc, w2c, g, depth);
-}
-
 // four consecutive keys, streamed (p 16-byte aligned for 32-bit keys,
 // 32-byte aligned for 64-bit keys)
 __device__ __forceinline__ void ld4(const uint32_t* p, uint32_t (&k)[4]) {
@@ -428,45 +439,59 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_update(DeviceCtl* __res
         const unsigned long long a0 = splits[t], a1 = splits[t + 1];
         const int na = (int)(a1 - a0), nb = len - na;
         if (nb == 0) {
-            // only resident voxels in this tile: straight streaming, no barrier
+            // only resident voxels in this tile: straight streaming, no
+            // barrier.  Each thread loads all its groups of four first, then
+            // projects them, reads their depth pixels together and stores.
+            constexpr int kGroups = kItems / 4;
             const bool vec = (a0 & 3ull) == 0;
+            K kk[kGroups][4];
+            float2 vv[kGroups][4];
 #pragma unroll
-            for (int r = 0; r < kItems / 4; ++r) {
+            for (int r = 0; r < kGroups; ++r) {
                 const int j0 = threadIdx.x * 4 + r * kMergeThreads * 4;
-                if (j0 >= len) break;
-                K k0, k1, k2, k3;
-                float2 v0, v1, v2, v3;
                 const unsigned long long ia = a0 + j0;
-                if (vec && j0 + 4 <= len) {
-                    K kk[4];
-                    ld4(A + ia, kk);
+                if (j0 >= len) {
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        kk[r][q] = (K)0;
+                        vv[r][q] = make_float2(0.0f, 0.0f);
+                    }
+                } else if (vec && j0 + 4 <= len) {
+                    ld4(A + ia, kk[r]);
                     const float4 va = __ldcs((const float4*)(Av + ia));
                     const float4 vb4 = __ldcs((const float4*)(Av + ia + 2));
-                    k0 = kk[0]; k1 = kk[1]; k2 = kk[2]; k3 = kk[3];
-                    v0 = make_float2(va.x, va.y); v1 = make_float2(va.z, va.w);
-                    v2 = make_float2(vb4.x, vb4.y); v3 = make_float2(vb4.z, vb4.w);
+                    vv[r][0] = make_float2(va.x, va.y); vv[r][1] = make_float2(va.z, va.w);
+                    vv[r][2] = make_float2(vb4.x, vb4.y); vv[r][3] = make_float2(vb4.z, vb4.w);
                 } else {
                     const int m = len - j0;
-                    k0 = __ldcs(A + ia); v0 = __ldcs(Av + ia);
-                    k1 = m > 1 ? __ldcs(A + ia + 1) : (K)0; v1 = m > 1 ? __ldcs(Av + ia + 1) : v0;
-                    k2 = m > 2 ? __ldcs(A + ia + 2) : (K)0; v2 = m > 2 ? __ldcs(Av + ia + 2) : v0;
-                    k3 = m > 3 ? __ldcs(A + ia + 3) : (K)0; v3 = m > 3 ? __ldcs(Av + ia + 3) : v0;
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        kk[r][q] = q < m ? __ldcs(A + ia + q) : (K)0;
+                        vv[r][q] = q < m ? __ldcs(Av + ia + q) : make_float2(0.0f, 0.0f);
+                    }
                 }
+            }
+#pragma unroll
+            for (int r = 0; r < kGroups; ++r) {
+                const int j0 = threadIdx.x * 4 + r * kMergeThreads * 4;
+                if (j0 >= len) break;
                 const unsigned long long p = d0 + j0;
-                finish_voxel<kU16, K>(k0, v0, p, upd_end, fc, w2c, g, depth);
-                finish_voxel<kU16, K>(k1, v1, p + 1, upd_end, fc, w2c, g, depth);
-                finish_voxel<kU16, K>(k2, v2, p + 2, upd_end, fc, w2c, g, depth);
-                finish_voxel<kU16, K>(k3, v3, p + 3, upd_end, fc, w2c, g, depth);
+                // positions past the tile are past the update range too
+                // (only the last tile is ragged, and upd_end <= N1)
+                const unsigned long long pos[4] = {p, p + 1, p + 2, p + 3};
+                update4<kU16, K>(kk[r], vv[r], pos, upd_end, fc, w2c, g, depth);
                 if (j0 + 4 <= len) {
-                    const K kk[4] = {k0, k1, k2, k3};
-                    st4(outK + p, kk);
-                    __stcs((float4*)(outV + p), make_float4(v0.x, v0.y, v1.x, v1.y));
-                    __stcs((float4*)(outV + p + 2), make_float4(v2.x, v2.y, v3.x, v3.y));
+                    st4(outK + p, kk[r]);
+                    __stcs((float4*)(outV + p), make_float4(vv[r][0].x, vv[r][0].y, vv[r][1].x, vv[r][1].y));
+                    __stcs((float4*)(outV + p + 2), make_float4(vv[r][2].x, vv[r][2].y, vv[r][3].x, vv[r][3].y));
                 } else {
                     const int m = len - j0;
-                    outK[p] = k0; outV[p] = v0;
-                    if (m > 1) { outK[p + 1] = k1; outV[p + 1] = v1; }
-                    if (m > 2) { outK[p + 2] = k2; outV[p + 2] = v2; }
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+                        if (q < m) {
+                            outK[p + q] = kk[r][q];
+                            outV[p + q] = vv[r][q];
+                        }
                 }
             }
             continue;
@@ -504,22 +529,39 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_update(DeviceCtl* __res
             }
         }
         __syncthreads();
-        for (int j = threadIdx.x; j < len; j += kMergeThreads) {
-            const uint16_t src = sSrc[j];
-            K key;
-            float2 val;
-            if (!(src & kFromB)) {
-                key = sA_k[koff + src];
-                val = sA_v[voff + src];
-            } else {
-                const int ib = src & ~kFromB;
-                key = sB_k[ib];
-                if (in.b_vals) val = in.b_vals[in.b_index ? in.b_index[b0 + ib] : b0 + ib];
-                else val = make_float2(0.0f, 0.0f);
+        // outputs j, j + 256, j + 512, j + 768 of the tile per group of four
+        for (int j0 = threadIdx.x; j0 < len; j0 += 4 * kMergeThreads) {
+            K key[4];
+            float2 val[4];
+            unsigned long long pos[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int j = j0 + q * kMergeThreads;
+                key[q] = (K)0;
+                val[q] = make_float2(0.0f, 0.0f);
+                pos[q] = ~0ull;  // no voxel: never updated
+                if (j < len) {
+                    const uint16_t src = sSrc[j];
+                    pos[q] = d0 + j;
+                    if (!(src & kFromB)) {
+                        key[q] = sA_k[koff + src];
+                        val[q] = sA_v[voff + src];
+                    } else {
+                        const int ib = src & ~kFromB;
+                        key[q] = sB_k[ib];
+                        if (in.b_vals) val[q] = in.b_vals[in.b_index ? in.b_index[b0 + ib] : b0 + ib];
+                    }
+                }
             }
-            finish_voxel<kU16, K>(key, val, d0 + j, upd_end, fc, w2c, g, depth);
-            __stcs(outK + d0 + j, key);
-            __stcs(outV + d0 + j, val);
+            update4<kU16, K>(key, val, pos, upd_end, fc, w2c, g, depth);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int j = j0 + q * kMergeThreads;
+                if (j < len) {
+                    __stcs(outK + d0 + j, key[q]);
+                    __stcs(outV + d0 + j, val[q]);
+                }
+            }
         }
         __syncthreads();
     }
