@@ -75,6 +75,7 @@ kifi_status enqueue_align(kifi_icp* c, const void* depth_dev, bool u16, const ki
     a.synth = c->synth;
     a.synth_w = c->sw;
     a.synth_h = c->sh;
+    a.neg_zero = -0.0f;
     if (c->record) {
         if (n_src > c->pairs_cap) {
             KIFI_CUDA(cudaStreamSynchronize(c->stream));

@@ -161,15 +161,60 @@ __device__ __forceinline__ void moments_total(const IcpState* st, FF* out) {
 constexpr int kTileCols = 8, kTileRows = 32;
 constexpr int kSplitRow = 10;   // window rows [0, 10) to the lower half-warp set, [10, 21) to the upper
 constexpr int kStageBatch = 4;  // staging loads in flight per thread
-constexpr int kStagePixels = 3840;  // float4 per pixel: 60 KB
+constexpr int kStagePixels = 5120;  // three float planes (x, y, z): 60 KB
 constexpr int kPredMargin = 2;      // pixels added around a predicted window box
 
+// Row pitch of a staged region `w` pixels wide: even, so that a pair of
+// adjacent pixels is one aligned 64-bit load, with pitch/2 odd, so that the
+// 64-bit loads of lanes whose windows sit one row apart hit distinct banks.
+__host__ __device__ constexpr int stage_pitch(int w) {
+    return ((w + 1) & ~1) + ((((w + 1) & ~1) >> 1) & 1 ? 0 : 2);
+}
+
+// Packed float pairs (f32x2): each half is rounded exactly as the scalar
+// __fsub_rn / __fadd_rn of that half.  Products are formed as
+// fma(a, a, -0) with the -0 a kernel parameter: that is the rounded product
+// for every input (x + -0 = x, also for x = -0), and unlike a packed
+// multiply it cannot be fused into the add that consumes it -- ptxas does
+// fuse mul.rn.f32x2 into a following add.rn.f32x2, which would round the
+// sum of squares once instead of the reference's separate roundings.
+__device__ __forceinline__ unsigned long long f2_pack(float lo, float hi) {
+    unsigned long long d;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(lo), "f"(hi));
+    return d;
+}
+__device__ __forceinline__ void f2_unpack(unsigned long long v, float& lo, float& hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ unsigned long long f2_sub(unsigned long long a, unsigned long long b) {
+    unsigned long long d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ unsigned long long f2_sq(unsigned long long a, unsigned long long neg_zero) {
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %1, %2;" : "=l"(d) : "l"(a), "l"(neg_zero));
+    return d;
+}
+__device__ __forceinline__ unsigned long long f2_add(unsigned long long a, unsigned long long b) {
+    unsigned long long d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
+// The staging buffer: planes of x, y and z, kStagePixels floats each.
+struct Stage {
+    float* x;
+    float* y;
+    float* z;
+};
+
 // The target pixels [x0, x0 + w) x [y0, y0 + h) (linear index y * synth_w + x,
-// as the reference reads them) into `stage` with row pitch `pitch`, by the
-// whole CTA: kStageBatch independent loads in flight per thread, then the
-// stores.  (0,0,0) is no point (ICP.cpp:112) and is staged as NaN; indices
-// past the buffer's end are invalid points too.
-__device__ __forceinline__ void stage_region(float4* __restrict__ stage, const float4* __restrict__ synth,
+// as the reference reads them) into the planes of `stage` with row pitch
+// `pitch`, by the whole CTA: kStageBatch independent loads in flight per
+// thread, then the stores.  (0,0,0) is no point (ICP.cpp:112) and is staged
+// with x = NaN; indices past the buffer's end are invalid points too.
+__device__ __forceinline__ void stage_region(const Stage& stage, const float4* __restrict__ synth,
                                              size_t n_synth, int synth_w, int x0, int y0, int w, int h,
                                              int pitch) {
     const int total = w * h;
@@ -191,31 +236,35 @@ __device__ __forceinline__ void stage_region(float4* __restrict__ stage, const f
             if (i < total) {
                 const int ry = i / w, rx = i - ry * w;
                 if (q[k].x == 0.0f && q[k].y == 0.0f && q[k].z == 0.0f) q[k].x = __int_as_float(0x7fffffff);
-                stage[ry * pitch + rx] = q[k];
+                const int at = ry * pitch + rx;
+                stage.x[at] = q[k].x;
+                stage.y[at] = q[k].y;
+                stage.z[at] = q[k].z;
             }
         }
     }
 }
 
-// Scan of one thread's window in the staged region (float4 per pixel,
-// `base` = its first candidate, odd row pitch).  Invalid target points were
-// staged with x = NaN, which never passes `l2 < best`.  Three interleaved
-// chains (columns mod 3) keep their own first strict minimum so that the
-// compare/select dependencies overlap; the lexicographic (l2, candidate)
-// minimum of the chains is the first strict minimum of the row-major scan.
-// Returns the best squared distance (0.01 when none) and its candidate
-// number r * 32 + c (-1 when none).
+// Scan of one thread's window in the staged region (`base` = its first
+// candidate's plane index, even pitch).  Invalid target points were staged
+// with x = NaN, which never passes `l2 < best`.  A full 21-wide row is ten
+// aligned pairs of adjacent candidates, whose squared distances are formed
+// two at a time in packed float pairs (each half with the reference's
+// operations and rounding), plus the one candidate left over: the first when
+// the window starts on an odd plane index, else the last.  Three chains --
+// the pairs' first halves, their second halves and the leftovers -- keep
+// their own first strict minimum; the lexicographic (l2, candidate) minimum
+// of the chains is the first strict minimum of the row-major scan.  Returns
+// the best squared distance (0.01 when none) and its candidate number
+// r * 32 + c (-1 when none).
 template <bool kW>
-__device__ __forceinline__ float scan_staged(const float4* __restrict__ sp, int base, int pitch,
-                                             int nr, int nc, float px, float py, float pz,
-                                             float dw2, int* best_rc) {
+__device__ __forceinline__ float scan_staged(const Stage& sp, int base, int pitch, int nr, int nc, float px,
+                                             float py, float pz, float dw2, float neg_zero, int* best_rc) {
     float b0 = 0.01f, b1 = 0.01f, b2 = 0.01f;
     int i0 = 0x7fffffff, i1 = 0x7fffffff, i2 = 0x7fffffff;
-    // a candidate records only its column (a constant of the unrolled row);
-    // the row is folded in once per row for the chains whose best moved
+    // one candidate in scalar float, the reference's order: (dx^2 + dy^2) + (dz^2 + dw^2)
     auto cand = [&](int at, int c, float& b, int& bc) {
-        const float4 q = sp[at];
-        const float dx = fsub(q.x, px), dy = fsub(q.y, py), dz = fsub(q.z, pz);
+        const float dx = fsub(sp.x[at], px), dy = fsub(sp.y[at], py), dz = fsub(sp.z[at], pz);
         const float zz = kW ? fadd(fmul(dz, dz), dw2) : fmul(dz, dz);
         const float l2 = fadd(fadd(fmul(dx, dx), fmul(dy, dy)), zz);
         if (l2 < b) {
@@ -224,18 +273,46 @@ __device__ __forceinline__ float scan_staged(const float4* __restrict__ sp, int 
         }
     };
     if (nc == 21) {
+        const int o = base & 1;       // the pairs start at an even plane index
+        const int cs = o ? 0 : 20;    // the leftover candidate's column
+        const unsigned long long PX = f2_pack(px, px), PY = f2_pack(py, py), PZ = f2_pack(pz, pz);
+        const unsigned long long DW = f2_pack(dw2, dw2), NZ = f2_pack(neg_zero, neg_zero);
         for (int r = 0; r < nr; ++r, base += pitch) {
-            int c0 = -1, c1 = -1, c2 = -1;
+            // a candidate records only its pair number (a constant of the
+            // unrolled row); the row and the parity are folded in once per row
+            int c0 = -1, c1 = -1;
+            bool moved = false;
+            const int pb = base + o;
 #pragma unroll
-            for (int c = 0; c < 21; c += 3) {
-                cand(base + c, c, b0, c0);
-                cand(base + c + 1, c + 1, b1, c1);
-                cand(base + c + 2, c + 2, b2, c2);
+            for (int k = 0; k < 10; ++k) {
+                const int at = pb + 2 * k;
+                const unsigned long long X = *(const unsigned long long*)(sp.x + at);
+                const unsigned long long Y = *(const unsigned long long*)(sp.y + at);
+                const unsigned long long Z = *(const unsigned long long*)(sp.z + at);
+                const unsigned long long dx = f2_sub(X, PX), dy = f2_sub(Y, PY), dz = f2_sub(Z, PZ);
+                unsigned long long zz = f2_sq(dz, NZ);
+                if (kW) zz = f2_add(zz, DW);
+                const unsigned long long l2 = f2_add(f2_add(f2_sq(dx, NZ), f2_sq(dy, NZ)), zz);
+                float lo, hi;
+                f2_unpack(l2, lo, hi);
+                if (lo < b0) {
+                    b0 = lo;
+                    c0 = 2 * k;
+                }
+                if (hi < b1) {
+                    b1 = hi;
+                    c1 = 2 * k;
+                }
+            }
+            {
+                int cl = -1;
+                cand(base + cs, 0, b2, cl);
+                moved = cl >= 0;
             }
             const int r32 = r * 32;
-            if (c0 >= 0) i0 = r32 + c0;
-            if (c1 >= 0) i1 = r32 + c1;
-            if (c2 >= 0) i2 = r32 + c2;
+            if (c0 >= 0) i0 = r32 + o + c0;
+            if (c1 >= 0) i1 = r32 + o + c1 + 1;
+            if (moved) i2 = r32 + cs;
         }
     } else {
         for (int r = 0; r < nr; ++r, base += pitch) {
@@ -266,8 +343,10 @@ __device__ __noinline__ void finish_step(IcpState* __restrict__ st, const FF* __
 // one image row apart; the two warps of a column split each 21x21 window
 // into rows 0-10 and 11-20.  Each thread back-projects and projects its
 // source, the CTA stages the bounding box of the tile's windows in shared
-// memory (float4 per pixel, odd row pitch: lanes hit distinct banks) and each
-// thread scans its rows in the reference's loop order; the halves are merged
+// memory (planes of x, y and z; an even row pitch with pitch/2 odd: pairs of
+// pixels are aligned 64-bit loads, lanes hit distinct banks) and each
+// thread scans its rows in the reference's loop order, two candidates at a
+// time in packed float pairs; the halves are merged
 // by (len^2, scan position), so the first strict minimum wins as in the
 // reference.  A region too large for the staging buffer (fast motion) is
 // read from global memory instead.  Target pixel (y1, x1) is linear index
@@ -298,7 +377,8 @@ __device__ __forceinline__ FF two_prod(float a, float b) {
 }
 
 __global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step(IcpArgs a, IcpState* __restrict__ st) {
-    extern __shared__ float4 stage[];  // kStagePixels target points
+    extern __shared__ float4 stage_mem[];  // three planes of kStagePixels floats
+    const Stage stage{(float*)stage_mem, (float*)stage_mem + kStagePixels, (float*)stage_mem + 2 * kStagePixels};
     __shared__ int s_box[4];
     __shared__ float s_hb[kTileCols][32];  // lower half's best len^2 per source
     __shared__ int s_hi[kTileCols][32];    // and its candidate number
@@ -327,7 +407,7 @@ __global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step(IcpArgs a, IcpSta
             if (b2 > b0 && b3 > b1 && b0 >= 0 && b1 >= 0) {
                 const int x0 = max(b0 - kPredMargin, 0), y0 = max(b1 - kPredMargin, 0);
                 const int w = b2 + kPredMargin - x0, h = b3 + kPredMargin - y0;
-                if (w <= kStagePixels && h <= kStagePixels && (w | 1) * h <= kStagePixels) {
+                if (w <= kStagePixels && h <= kStagePixels && stage_pitch(w) * h <= kStagePixels) {
                     p[0] = x0;
                     p[1] = y0;
                     p[2] = w;
@@ -342,7 +422,7 @@ __global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step(IcpArgs a, IcpSta
     }
     __syncthreads();
     const int px0 = s_pred[0], py0 = s_pred[1], pw = s_pred[2], ph = s_pred[3];
-    if (pw > 0) stage_region(stage, a.synth, n_synth, a.synth_w, px0, py0, pw, ph, pw | 1);
+    if (pw > 0) stage_region(stage, a.synth, n_synth, a.synth_w, px0, py0, pw, ph, stage_pitch(pw));
     // this thread's source of the first tile in eye space (no pose needed yet)
     const int lane0 = threadIdx.x & 31, wcol0 = (threadIdx.x >> 5) >> 1;
     float pre_d = 0.0f;
@@ -410,12 +490,12 @@ __global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step(IcpArgs a, IcpSta
         // the prefetched region if it holds every window of the tile, else stage the box now
         const bool use_pred = tile == (int)blockIdx.x && pw > 0 && ax1 >= 0 && ax0 >= px0 && ay0 >= py0 &&
                               ax1 <= px0 + pw && ay1 <= py0 + ph;
-        int bx0 = ax0, by0 = ay0, pitch = (ax1 - ax0) | 1;  // odd pitch: adjacent windows hit distinct banks
+        int bx0 = ax0, by0 = ay0, pitch = stage_pitch(ax1 - ax0);
         bool staged;
         if (use_pred) {
             bx0 = px0;
             by0 = py0;
-            pitch = pw | 1;
+            pitch = stage_pitch(pw);
             staged = true;
         } else {
             staged = ax1 >= 0 && pitch * (ay1 - ay0) <= kStagePixels;
@@ -441,11 +521,13 @@ __global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step(IcpArgs a, IcpSta
                 const int base = (v + r0 - by0) * pitch + (u - bx0);
                 // dz^2 + dw^2 == dz^2 exactly when dw == 0 (dz^2 >= 0)
                 best = dw2 != 0.0f
-                           ? scan_staged<true>(stage, base, pitch, r1 - r0, nc, wp[0], wp[1], wp[2], dw2, &rc)
-                           : scan_staged<false>(stage, base, pitch, r1 - r0, nc, wp[0], wp[1], wp[2], dw2, &rc);
+                           ? scan_staged<true>(stage, base, pitch, r1 - r0, nc, wp[0], wp[1], wp[2], dw2,
+                                               a.neg_zero, &rc)
+                           : scan_staged<false>(stage, base, pitch, r1 - r0, nc, wp[0], wp[1], wp[2], dw2,
+                                                a.neg_zero, &rc);
                 if (rc >= 0) {
-                    const float4 q = stage[base + (rc >> 5) * pitch + (rc & 31)];
-                    bq = make_float3(q.x, q.y, q.z);
+                    const int at = base + (rc >> 5) * pitch + (rc & 31);
+                    bq = make_float3(stage.x[at], stage.y[at], stage.z[at]);
                     rc += r0 * 32;
                 }
             } else {
@@ -478,10 +560,13 @@ __global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step(IcpArgs a, IcpSta
             if (oi >= 0 && (rc < 0 || ob < best)) {
                 best = ob;
                 rc = oi;
-                const size_t at = (size_t)(v + (oi >> 5)) * a.synth_w + (u + (oi & 31));
-                const float4 q = staged ? stage[(v + (oi >> 5) - by0) * pitch + (u + (oi & 31) - bx0)]
-                                        : __ldg(a.synth + at);
-                bq = make_float3(q.x, q.y, q.z);
+                if (staged) {
+                    const int at = (v + (oi >> 5) - by0) * pitch + (u + (oi & 31) - bx0);
+                    bq = make_float3(stage.x[at], stage.y[at], stage.z[at]);
+                } else {
+                    const float4 q = __ldg(a.synth + (size_t)(v + (oi >> 5)) * a.synth_w + (u + (oi & 31)));
+                    bq = make_float3(q.x, q.y, q.z);
+                }
             }
             const bool hit = mine && rc >= 0;
             if (a.pairs && mine) {
@@ -988,7 +1073,7 @@ cudaError_t icp_align_enqueue(const IcpArgs& a, IcpState* st, const Mat4& guess,
     const int n_cols = (a.width + 3) / 4;
     const int tiles = ((n_cols + kTileCols - 1) / kTileCols) * ((a.height + kTileRows - 1) / kTileRows);
     const int ctas = tiles < kIcpMaxCtas ? tiles : kIcpMaxCtas;
-    const size_t smem = kStagePixels * sizeof(float4);
+    const size_t smem = 3 * kStagePixels * sizeof(float);
     // programmatic dependent launch: each step's grid is scheduled as soon as
     // every CTA of the one before has finished its association, overlapping
     // its launch with the previous finisher (k_icp_step waits for it)
@@ -1013,7 +1098,7 @@ cudaError_t icp_align_enqueue(const IcpArgs& a, IcpState* st, const Mat4& guess,
 // once per device, outside any stream capture.
 cudaError_t icp_init_device() {
     return cudaFuncSetAttribute(k_icp_step, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)(kStagePixels * sizeof(float4)));
+                                (int)(3 * kStagePixels * sizeof(float)));
 }
 
 cudaError_t expand_target_enqueue(const float* in, int n, float4* out, int ctas, cudaStream_t st) {

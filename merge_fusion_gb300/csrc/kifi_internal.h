@@ -126,6 +126,7 @@ struct IcpArgs {
     int synth_w, synth_h;
     long long* pairs;       // optional: per source the winner's target index (-1: none) ...
     float* pairs_len2;      // ... and its len^2, overwritten by every iteration
+    float neg_zero;         // -0.0f, a value the device code cannot see at compile time
 };
 
 struct IcpIterStats {
