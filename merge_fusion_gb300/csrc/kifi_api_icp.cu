@@ -1,5 +1,6 @@
 // kifi_api_icp.cu -- C ABI of the ICP context and of Renderer::Bin
 // (include/kifi_gpu.h).  Host code; the kernels live in kifi_icp.cu.
+#include <cmath>
 #include <cstring>
 #include <new>
 
@@ -275,7 +276,9 @@ kifi_status kifi_icp_result(kifi_icp* c, float out_eye_to_world[16], double out_
     if (iterations) *iterations = h->iter;
     for (int i = 0; i < it && i < capacity; ++i) {
         if (n_assoc) n_assoc[i] = h->stats[i].n_assoc;
-        if (rms) rms[i] = h->stats[i].rms;
+        // sqrt(sum / n) in float, as the device formed it before
+        const int n = h->stats[i].n_assoc;
+        if (rms) rms[i] = n > 0 ? (double)std::sqrt(h->stats[i].sum_l2 / (float)n) : 0.0;
     }
     return KIFI_OK;
 }

@@ -98,30 +98,40 @@ __device__ __forceinline__ float load_depth(const void* depth, size_t i, bool u1
     return __ldg((const float*)depth + i);
 }
 
-// Last CTA to arrive returns true; resets the counter.  Thread 0's atomic
-// orders the whole CTA's earlier stores (the barrier makes them visible to
-// it) before the count, and the count before the last CTA's reads.
-__device__ __forceinline__ bool last_cta(unsigned int* counter) {
+// Last CTA to arrive returns true and gets the grid's total of `mine` (an
+// association count, read after the barrier); resets the counter.  The
+// counter holds finished CTAs in its high 32 bits and the running total in
+// its low 32 bits, so one atomic does both.  Thread 0's atomic orders the
+// whole CTA's earlier stores (the barrier makes them visible to it) before
+// the count, and the count before the last CTA's reads.
+__device__ __forceinline__ bool last_cta(unsigned long long* counter, const unsigned int& mine,
+                                         unsigned int* total) {
     __shared__ bool last;
+    __shared__ unsigned int s_total;
     __syncthreads();
     if (threadIdx.x == 0) {
         // one acquire-release atomic at gpu scope: the release (cumulative
         // over the CTA's writes ordered before it by the barrier) publishes
         // this CTA's partials; the acquire lets the last CTA read everyone's
-        unsigned int prev;
-        asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(prev) : "l"(counter) : "memory");
-        last = (prev == gridDim.x - 1);
-        if (last) *counter = 0u;  // read again only by the next launch
+        const unsigned long long add = (1ull << 32) | mine;
+        unsigned long long prev;
+        asm volatile("atom.acq_rel.gpu.global.add.u64 %0, [%1], %2;"
+                     : "=l"(prev) : "l"(counter), "l"(add) : "memory");
+        last = (unsigned int)(prev >> 32) == gridDim.x - 1;
+        s_total = (unsigned int)prev + mine;
+        if (last) *counter = 0ull;  // read again only by the next launch
     }
     __syncthreads();
+    *total = s_total;
     return last;
 }
 
 // Totals of the per-CTA float-float partials, by the whole (last) CTA.  The
 // partials are stored component-major (hi row, then lo row, each
-// kIcpMaxCtas long), so warp w reduces components w and w + 16 with
-// coalesced loads: lane l adds CTAs l, l + 32, ... in float-float -- all of a
-// lane's loads (up to 320 CTAs) issued in one round -- then a shuffle tree.
+// kIcpMaxCtas long), so warp w reduces component w + 1 (the count, component
+// 0, comes with the last-CTA counter) with coalesced loads: lane l adds CTAs
+// l, l + 32, ... in float-float -- all of a lane's loads (up to 320 CTAs)
+// issued in one round -- then a shuffle tree.
 // Fixed order: independent of scheduling.  The loads bypass L1 (the partials
 // were written by other SMs during this launch).
 constexpr int kTotalsPerLane = 10;
@@ -139,21 +149,16 @@ __device__ __forceinline__ FF lane_partials(const float* ph, int b0, int G) {
     return acc;
 }
 template <int NV>
-__device__ __forceinline__ void moments_total(const IcpState* st, FF* out) {
-    const int lane = threadIdx.x & 31, c0 = threadIdx.x >> 5, c1 = c0 + (blockDim.x >> 5);
+__device__ __forceinline__ void moments_total(const IcpState* st, unsigned int count, FF* out) {
+    const int lane = threadIdx.x & 31, c = (threadIdx.x >> 5) + 1;
     const int G = gridDim.x;
-    if (c0 < NV) {
-        FF a0{0.0f, 0.0f}, a1{0.0f, 0.0f};
-        for (int b0 = lane; b0 < G; b0 += 32 * kTotalsPerLane) {
-            a0 = ff_add(a0, lane_partials(st->part + (size_t)(2 * c0) * kIcpMaxCtas, b0, G));
-            if (c1 < NV) a1 = ff_add(a1, lane_partials(st->part + (size_t)(2 * c1) * kIcpMaxCtas, b0, G));
-        }
-        a0 = warp_sum_ff(a0);
-        if (lane == 0) out[c0] = a0;
-        if (c1 < NV) {
-            a1 = warp_sum_ff(a1);
-            if (lane == 0) out[c1] = a1;
-        }
+    if (threadIdx.x == 0) out[0] = FF{(float)count, 0.0f};  // exact: at most 2^24 sources
+    if (c < NV) {
+        FF a{0.0f, 0.0f};
+        for (int b0 = lane; b0 < G; b0 += 32 * kTotalsPerLane)
+            a = ff_add(a, lane_partials(st->part + (size_t)(2 * c) * kIcpMaxCtas, b0, G));
+        a = warp_sum_ff(a);
+        if (lane == 0) out[c] = a;
     }
     __syncthreads();
 }
@@ -608,15 +613,16 @@ __global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step(IcpArgs a, IcpSta
     }
     // association done: the next step's grid may be scheduled (it waits above)
     asm volatile("griddepcontrol.launch_dependents;");
-    if (threadIdx.x < kMoments) {
-        const FF t = threadIdx.x == 0 ? FF{(float)s_count, 0.0f} : s_acc[threadIdx.x];
+    if (threadIdx.x >= 1 && threadIdx.x < kMoments) {
+        const FF t = s_acc[threadIdx.x];
         st->part[(size_t)(2 * threadIdx.x) * kIcpMaxCtas + blockIdx.x] = t.hi;
         st->part[(size_t)(2 * threadIdx.x + 1) * kIcpMaxCtas + blockIdx.x] = t.lo;
     }
     if (threadIdx.x == 0) atomicMax(&st->t_body, global_ns());
-    if (!last_cta(&st->done)) return;
+    unsigned int n_total;
+    if (!last_cta(&st->done, s_count, &n_total)) return;
     __shared__ FF tot[kMoments];
-    moments_total<kMoments>(st, tot);
+    moments_total<kMoments>(st, n_total, tot);
     if (threadIdx.x < 32) finish_step(st, tot);
 }
 
@@ -792,6 +798,16 @@ __device__ __noinline__ void finish_step(IcpState* __restrict__ st, const FF* __
     __shared__ float s_f[10];
     __shared__ FF s_nf[10];
     const int lane = threadIdx.x & 31;
+    // the step's counters for the statistics, read now so that no load is
+    // left behind the pose update (final: every CTA wrote them before its
+    // release of the last-CTA counter)
+    int step = 0;
+    unsigned long long t_start = 0ull, t_body = 0ull;
+    if (lane == 0) {
+        step = __ldcg(&st->iter);
+        t_start = __ldcg(&st->t_start);
+        t_body = __ldcg(&st->t_body);
+    }
     // 1. centroids (lanes 0-5), S (lanes 0-8), N (lanes 0-9) in FF
     const float n = fadd(tot[0].hi, tot[0].lo);  // an exact count below 2^24
     FF my_mu{0.0f, 0.0f};
@@ -961,25 +977,24 @@ __device__ __noinline__ void finish_step(IcpState* __restrict__ st, const FF* __
     const FF md0 = shfl_ff(my_mu, 3), md1 = shfl_ff(my_mu, 4), md2 = shfl_ff(my_mu, 5);
     if (lane != 0) return;
     st->n_assoc = (int)n;
-    st->sum_l2 = (double)fadd(tot[16].hi, tot[16].lo);
     st->mu_s[0] = fadd(mu0.hi, mu0.lo);
     st->mu_s[1] = fadd(mu1.hi, mu1.lo);
     st->mu_s[2] = fadd(mu2.hi, mu2.lo);
     st->mu_d[0] = fadd(md0.hi, md0.lo);
     st->mu_d[1] = fadd(md1.hi, md1.lo);
     st->mu_d[2] = fadd(md2.hi, md2.lo);
-    const int it = st->iter;
-    if (it < kIcpMaxStats) {
-        st->stats[it].n_assoc = (int)n;
-        st->stats[it].solver = solver;
-        st->stats[it].rms = n > 0.0f ? (double)sqrtf(fdiv(fadd(tot[16].hi, tot[16].lo), n)) : 0.0;
+    if (step < kIcpMaxStats) {
+        st->stats[step].n_assoc = (int)n;
+        st->stats[step].solver = solver;
+        st->stats[step].sum_l2 = fadd(tot[16].hi, tot[16].lo);
         const unsigned long long t_end = global_ns();
-        st->stats[it].body_us = (float)(st->t_body - st->t_start) * 1e-3f;
-        st->stats[it].tail_us = (float)(t_end - st->t_body) * 1e-3f;
+        // spans below 2^32 ns: the 32-bit conversions round as the 64-bit ones
+        st->stats[step].body_us = (float)(unsigned int)(t_body - t_start) * 1e-3f;
+        st->stats[step].tail_us = (float)(unsigned int)(t_end - t_body) * 1e-3f;
     }
     st->t_start = ~0ull;
     st->t_body = 0ull;
-    st->iter = it + 1;
+    st->iter = step + 1;
 }
 
 __global__ void k_icp_begin(IcpState* st, Mat4 guess) {
@@ -989,7 +1004,7 @@ __global__ void k_icp_begin(IcpState* st, Mat4 guess) {
         st->pose_lo[i] = 0.0f;
     }
     st->iter = 0;
-    st->done = 0u;
+    st->done = 0ull;
     st->t_start = ~0ull;
     st->t_body = 0ull;
 }

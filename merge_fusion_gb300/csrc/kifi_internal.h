@@ -132,7 +132,7 @@ struct IcpArgs {
 struct IcpIterStats {
     int n_assoc;
     int solver;       // Horn's eigenvector: 0 closed form, 1 Jacobi fallback
-    double rms;       // sqrt(mean of the associated squared distances)
+    float sum_l2;     // the associated squared distances' sum (the host forms the RMS)
     float body_us;    // first CTA start to last CTA end of the association
     float tail_us;    // last CTA end to the updated pose
 };
@@ -140,11 +140,10 @@ struct IcpIterStats {
 struct IcpState {
     float pose_f[16];   // eye-to-world estimate, kifi order (float-float high part)
     float pose_lo[16];  // and its low part
-    unsigned int done;  // last-CTA counter
+    unsigned long long done;  // CTAs finished (high 32 bits) and their associations (low 32 bits)
     float mu_s[4], mu_d[4];
     int n_assoc;
     int iter;
-    double sum_l2;
     unsigned long long t_start, t_body;  // globaltimer stamps of the running step
     IcpIterStats stats[kIcpMaxStats];
     float part[34 * kIcpMaxCtas];   // per-CTA float-float partials: hi, lo rows of 17 components
