@@ -222,29 +222,30 @@ struct Stage {
 __device__ __forceinline__ void stage_region(const Stage& stage, const float4* __restrict__ synth,
                                              size_t n_synth, int synth_w, int x0, int y0, int w, int h,
                                              int pitch) {
-    const int total = w * h;
-    for (int i0 = threadIdx.x; i0 < total; i0 += kStageBatch * blockDim.x) {
-        float4 q[kStageBatch];
+    // warps take rows (kStageBatch rows in flight each), lanes take columns
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, n_warps = blockDim.x >> 5;
+    for (int ry0 = warp; ry0 < h; ry0 += kStageBatch * n_warps) {
+        for (int rx = lane; rx < w; rx += 32) {
+            float4 q[kStageBatch];
 #pragma unroll
-        for (int k = 0; k < kStageBatch; ++k) {
-            const int i = i0 + k * blockDim.x;
-            q[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (i < total) {
-                const int ry = i / w, rx = i - ry * w;
-                const size_t at = (size_t)(y0 + ry) * synth_w + (x0 + rx);
-                if (at < n_synth) q[k] = __ldg(synth + at);
+            for (int k = 0; k < kStageBatch; ++k) {
+                const int ry = ry0 + k * n_warps;
+                q[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (ry < h) {
+                    const size_t at = (size_t)(y0 + ry) * synth_w + (x0 + rx);
+                    if (at < n_synth) q[k] = __ldg(synth + at);
+                }
             }
-        }
 #pragma unroll
-        for (int k = 0; k < kStageBatch; ++k) {
-            const int i = i0 + k * blockDim.x;
-            if (i < total) {
-                const int ry = i / w, rx = i - ry * w;
-                if (q[k].x == 0.0f && q[k].y == 0.0f && q[k].z == 0.0f) q[k].x = __int_as_float(0x7fffffff);
-                const int at = ry * pitch + rx;
-                stage.x[at] = q[k].x;
-                stage.y[at] = q[k].y;
-                stage.z[at] = q[k].z;
+            for (int k = 0; k < kStageBatch; ++k) {
+                const int ry = ry0 + k * n_warps;
+                if (ry < h) {
+                    if (q[k].x == 0.0f && q[k].y == 0.0f && q[k].z == 0.0f) q[k].x = __int_as_float(0x7fffffff);
+                    const int at = ry * pitch + rx;
+                    stage.x[at] = q[k].x;
+                    stage.y[at] = q[k].y;
+                    stage.z[at] = q[k].z;
+                }
             }
         }
     }
