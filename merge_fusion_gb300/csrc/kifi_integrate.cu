@@ -125,7 +125,9 @@ __global__ void __launch_bounds__(kEmitThreads) k_splat_emit(DeviceCtl* __restri
         K key = 0;
         bool valid = false;
         if (i < P) {
-            int u = (int)(i % (size_t)W), v = (int)(i / (size_t)W);
+            // frames hold at most 2^26 pixels: a 32-bit division, not a 64-bit one
+            const unsigned int iu = (unsigned int)i;
+            const int v = (int)(iu / (unsigned int)W), u = (int)(iu - (unsigned int)v * (unsigned int)W);
             valid = splat_pixel<K>(fc, e2w, g, cd, u, v, load_depth(depth, i, kU16), &key);
         }
         // the excluded key of the dilation: max splat + pack(1,1,1)
