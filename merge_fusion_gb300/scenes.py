@@ -206,114 +206,170 @@ def room_trajectory(n_frames, seed=0, scale=1.0):
 
 def room_scene(n_frames=300, seed=0, width=640, height=480, f=585.0, scale=1.0, dropout=0.02,
                first_frame=0):
-    """configs[1] (and, with scale=2 and 512x424, configs[2])."""
-    layout = room_layout(seed, scale)
-    poses = room_trajectory(first_frame + n_frames, seed, scale)[first_frame:]
-    fx = fy = f
-    cx, cy = width / 2.0, height / 2.0
-    rays = _rays(width, height, fx, fy, cx, cy)
-    frames = []
-    for i, pose in enumerate(poses):
-        rng = np.random.default_rng([seed, first_frame + i])
-        frames.append(_render(rays, pose, layout, rng, 0.4, 4.0, dropout))
-    return Sequence(width, height, fx, fy, cx, cy, 0.4, 4.0, frames, poses)
+    """configs[1] (and, with scale=2 and 512x424, configs[2]): the seeded room
+    rendered on the CPU by the same renderer the benchmark runs on the GPU
+    (render_room_torch; both devices give identical frames)."""
+    frames, poses = render_room_torch(n_frames, seed, width, height, f, scale, dropout, first_frame,
+                                      device="cpu")
+    frames = [fr for fr in frames.numpy().view(np.uint16)]
+    return Sequence(width, height, f, f, width / 2.0, height / 2.0, 0.4, 4.0, frames, poses)
 
 
 # ------------------------------------------------------------ torch renderer
-# Input generation for long sequences (benchmarks): the same scenes and
-# trajectories ray-cast with torch, on the GPU or the CPU.  Noise and
-# dropout come from a counter-based integer hash, so the random stream is
-# the same on either device.
+# The room scenes are ray-cast with torch, on the GPU (benchmarks, long
+# sequences) or on the CPU, and the two give the same frames bit for bit:
+# every floating-point step is one IEEE-rounded elementwise operation (add,
+# subtract, multiply, divide, square root, min/max, compare, round) applied
+# the same way on either device -- no matrix products or floating-point
+# sums, whose order and fusion differ between backends.  The Gaussian depth
+# noise and the dropout draw come from a counter-based integer hash of
+# (seed, frame, pixel), and the Box-Muller transform runs on the host in
+# float64, so no device's log or cos enters the frame.
 
 def _hash32(x):
-    """lowbias32-style integer hash of int64 tensors holding 32-bit values."""
-    def mul32(a, m):
-        lo = a & 0xFFFF
-        hi = a >> 16
-        return (lo * m + (((hi * m) & 0xFFFF) << 16)) & 0xFFFFFFFF
+    """lowbias32 integer hash of uint64 arrays holding 32-bit values."""
     x = x & 0xFFFFFFFF
     x = x ^ (x >> 16)
-    x = mul32(x, 0x7FEB352D)
+    x = (x * 0x7FEB352D) & 0xFFFFFFFF
     x = x ^ (x >> 15)
-    x = mul32(x, 0x846CA68B)
+    x = (x * 0x846CA68B) & 0xFFFFFFFF
     x = x ^ (x >> 16)
     return x
 
 
-def _uniform(torch, seed, frame, pix, stream):
-    key = _hash32(pix + _hash32(torch.full_like(pix, (seed * 7919 + frame * 104729 + stream * 31337)
-                                                & 0xFFFFFFFF)))
-    return (key.to(torch.float32) + 0.5) * (1.0 / 4294967296.0)
+def _uniform(seed, frame, n, stream):
+    """n uniforms in (0, 1] (float64) of one (seed, frame, stream)."""
+    salt = _hash32(np.uint64((seed * 7919 + frame * 104729 + stream * 31337) & 0xFFFFFFFF))
+    key = _hash32(np.arange(n, dtype=np.uint64) + salt)
+    return (key.astype(np.float64) + 0.5) * (1.0 / 4294967296.0)
+
+
+def room_noise(seed, frame, n):
+    """Per pixel a standard normal draw and a dropout uniform (float32)."""
+    u1, u2, u3 = (_uniform(seed, frame, n, k) for k in (1, 2, 3))
+    gauss = np.sqrt(-2.0 * np.log(u1)) * np.cos(6.283185307179586 * u2)
+    return gauss.astype(np.float32), u3.astype(np.float32)
+
+
+def _device_noise(torch, seed, frame, n, dev):
+    """room_noise's draws computed on `dev` with its own log and cos: fast,
+    but not bit-identical between devices (training data only)."""
+    def mul32(a, m):
+        lo, hi = a & 0xFFFF, a >> 16
+        return (lo * m + (((hi * m) & 0xFFFF) << 16)) & 0xFFFFFFFF
+
+    def h32(x):
+        x = x & 0xFFFFFFFF
+        x = x ^ (x >> 16)
+        x = mul32(x, 0x7FEB352D)
+        x = x ^ (x >> 15)
+        x = mul32(x, 0x846CA68B)
+        return x ^ (x >> 16)
+
+    pix = torch.arange(n, device=dev, dtype=torch.int64)
+    u = []
+    for k in (1, 2, 3):
+        salt = int(_hash32(np.uint64((seed * 7919 + frame * 104729 + k * 31337) & 0xFFFFFFFF)))
+        u.append((h32(pix + salt).to(torch.float64) + 0.5) * (1.0 / 4294967296.0))
+    g = torch.sqrt(-2.0 * torch.log(u[0])) * torch.cos(6.283185307179586 * u[1])
+    return g.to(torch.float32), u[2].to(torch.float32)
 
 
 def render_room_torch(n_frames, seed=0, width=640, height=480, f=585.0, scale=1.0, dropout=0.02,
-                      first_frame=0, device="cuda", chunk=1 << 16):
-    """Frames first_frame .. first_frame+n_frames-1 of room_scene(seed) as a
-    uint16 tensor (n, h, w) on `device`, and their eye-to-world poses."""
+                      first_frame=0, device="cuda", chunk=1 << 16, noise="host"):
+    """Frames first_frame .. first_frame+n_frames-1 of the seeded room as a
+    uint16 bit pattern in an int16 tensor (n, h, w) on `device`, and their
+    eye-to-world poses (float64 4x4).  noise="host" (the default) draws the
+    depth noise on the host so every device renders identical frames;
+    noise="device" draws it on `device` (faster, for large training sets)."""
     import torch
     layout = room_layout(seed, scale)
     poses = room_trajectory(first_frame + n_frames, seed, scale)[first_frame:]
     fx = fy = f
     cx, cy = width / 2.0, height / 2.0
     dev = torch.device(device)
-    u = torch.arange(width, device=dev, dtype=torch.float32)
-    v = torch.arange(height, device=dev, dtype=torch.float32)
-    vv, uu = torch.meshgrid(v, u, indexing="ij")
-    rays = torch.stack([(uu + 0.5 - cx) / fx, (cy - 0.5 - vv) / fy, -torch.ones_like(uu)], -1)
-    rays = rays.reshape(-1, 3)
-    half = torch.tensor(layout["half"], device=dev, dtype=torch.float32)
-    blo = torch.tensor(np.array(layout["box_lo"]), device=dev, dtype=torch.float32)
-    bhi = torch.tensor(np.array(layout["box_hi"]), device=dev, dtype=torch.float32)
-    sc = torch.tensor(np.array(layout["sph_c"]), device=dev, dtype=torch.float32)
-    sr = torch.tensor(np.array(layout["sph_r"]), device=dev, dtype=torch.float32)
-    pix = torch.arange(width * height, device=dev, dtype=torch.int64)
+    f32 = torch.float32
+
+    def t32(a):
+        return torch.tensor(np.asarray(a, np.float32), device=dev, dtype=f32)
+
+    # eye-space rays (u + 0.5 - cx) / fx, (cy - 0.5 - v) / fy, -1 from float64 on the host
+    u = np.arange(width, dtype=np.float64)
+    v = np.arange(height, dtype=np.float64)
+    uu, vv = np.meshgrid(u, v)
+    rx = t32(((uu + 0.5 - cx) / fx).reshape(-1))
+    ry = t32(((cy - 0.5 - vv) / fy).reshape(-1))
+    half = t32(layout["half"])
+    blo = t32(np.array(layout["box_lo"]))  # (B, 3)
+    bhi = t32(np.array(layout["box_hi"]))
+    sc = t32(np.array(layout["sph_c"]))    # (S, 3)
+    sr = t32(np.array(layout["sph_r"]))
+    sr2 = sr * sr
+    inf = torch.tensor(float("inf"), device=dev, dtype=f32)
+    tiny = torch.tensor(1e-30, device=dev, dtype=f32)
+    eps = torch.tensor(1e-6, device=dev, dtype=f32)
+    c_s0, c_s1, c_z0 = t32(0.0012), t32(0.0019), t32(0.4)
+    c_mm, zn, zf, c_drop = t32(1000.0), t32(0.4), t32(4.0), t32(dropout)
+    P = width * height
     out = torch.zeros((n_frames, height, width), dtype=torch.int16, device=dev)
-    inf = float("inf")
+    # host noise for the next frames is drawn on worker threads while the device ray-casts
+    from concurrent.futures import ThreadPoolExecutor
+    pool = ThreadPoolExecutor(max_workers=4)
+    ahead = 8 if noise == "host" else 0
+    pending = [pool.submit(room_noise, seed, first_frame + i, P) for i in range(min(ahead, n_frames))]
     for i, pose in enumerate(poses):
-        R = torch.tensor(pose[:3, :3], device=dev, dtype=torch.float32)
-        o = torch.tensor(pose[:3, 3], device=dev, dtype=torch.float32)
-        z = torch.empty(width * height, device=dev, dtype=torch.float32)
-        for s0 in range(0, width * height, chunk):
-            d = rays[s0:s0 + chunk] @ R.T
+        R = np.asarray(pose[:3, :3], np.float32)
+        o = t32(pose[:3, 3])
+        z = torch.empty(P, device=dev, dtype=f32)
+        for s0 in range(0, P, chunk):
+            x, y = rx[s0:s0 + chunk], ry[s0:s0 + chunk]
+            # world ray d = R (x, y, -1), one rounded multiply and add at a time
+            d = torch.stack([x * float(R[k, 0]) + y * float(R[k, 1]) - float(R[k, 2]) for k in range(3)], 1)
             # room walls from inside
-            tpos = torch.where(d > 0, (half - o) / d, torch.full_like(d, inf))
-            tneg = torch.where(d < 0, (-half - o) / d, torch.full_like(d, inf))
+            tpos = torch.where(d > 0, (half - o) / d, inf)
+            tneg = torch.where(d < 0, (-half - o) / d, inf)
             t = torch.minimum(tpos, tneg).amin(1)
             # boxes (slabs)
-            inv = 1.0 / torch.where(d == 0, torch.full_like(d, 1e-30), d)
+            inv = 1.0 / torch.where(d == 0, tiny, d)
             t1 = (blo[None] - o) * inv[:, None]
             t2 = (bhi[None] - o) * inv[:, None]
             tn = torch.minimum(t1, t2).amax(2)
             tf = torch.maximum(t1, t2).amin(2)
-            th = torch.where(tn > 1e-6, tn, tf)
-            hit = (tn <= tf) & (tf > 1e-6)
-            t = torch.minimum(t, torch.where(hit, th, torch.full_like(th, inf)).amin(1))
-            # spheres
-            oc = o[None] - sc                       # (S, 3)
-            b = d @ oc.T                            # (P, S)
-            cc = (oc * oc).sum(1) - sr * sr         # (S,)
-            a = (d * d).sum(1, keepdim=True)        # (P, 1)
+            th = torch.where(tn > eps, tn, tf)
+            hit = (tn <= tf) & (tf > eps)
+            t = torch.minimum(t, torch.where(hit, th, inf).amin(1))
+            # spheres: b = d.(o - c), cc = |o - c|^2 - r^2, a = |d|^2
+            oc = o[None] - sc
+            b = d[:, 0:1] * oc[None, :, 0] + d[:, 1:2] * oc[None, :, 1] + d[:, 2:3] * oc[None, :, 2]
+            cc = (oc[:, 0] * oc[:, 0] + oc[:, 1] * oc[:, 1] + oc[:, 2] * oc[:, 2]) - sr2
+            a = (d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1] + d[:, 2] * d[:, 2])[:, None]
             disc = b * b - a * cc[None]
             sq = torch.sqrt(torch.clamp(disc, min=0))
             t0 = (-b - sq) / a
             t1s = (-b + sq) / a
-            ts = torch.where(t0 > 1e-6, t0, t1s)
-            ok = (disc >= 0) & (ts > 1e-6)
-            t = torch.minimum(t, torch.where(ok, ts, torch.full_like(ts, inf)).amin(1))
-            z[s0:s0 + chunk] = t
-        gidx = first_frame + i
-        u1 = _uniform(torch, seed, gidx, pix, 1)
-        u2 = _uniform(torch, seed, gidx, pix, 2)
-        u3 = _uniform(torch, seed, gidx, pix, 3)
+            ts = torch.where(t0 > eps, t0, t1s)
+            ok = (disc >= 0) & (ts > eps)
+            t = torch.minimum(t, torch.where(ok, ts, inf).amin(1))
+            z[s0:s0 + chunk] = t  # the eye-space ray has z = -1: t is the planar depth
+        if noise == "host":
+            gauss, u3 = pending[i].result()
+            pending[i] = None
+            if i + ahead < n_frames:
+                pending.append(pool.submit(room_noise, seed, first_frame + i + ahead, P))
+            gauss = torch.from_numpy(gauss).to(dev)
+            u3 = torch.from_numpy(u3).to(dev)
+        else:
+            gauss, u3 = _device_noise(torch, seed, first_frame + i, P, dev)
         hitm = torch.isfinite(z)
         zz = torch.where(hitm, z, torch.zeros_like(z))
-        sigma = 0.0012 + 0.0019 * (zz - 0.4) ** 2
-        gauss = torch.sqrt(-2.0 * torch.log(u1)) * torch.cos(6.283185307179586 * u2)
+        dz = zz - c_z0
+        sigma = c_s0 + c_s1 * (dz * dz)
         zz = zz + sigma * gauss
-        mm = torch.round(zz * 1000.0)
-        valid = hitm & (zz >= 0.4) & (zz <= 4.0) & (u3 >= dropout)
+        mm = torch.round(zz * c_mm)
+        valid = hitm & (zz >= zn) & (zz <= zf) & (u3 >= c_drop)
         mm = torch.where(valid, torch.clamp(mm, 0, 65535), torch.zeros_like(mm))
         out[i] = mm.to(torch.int32).to(torch.int16).reshape(height, width)  # bit pattern of uint16
+    pool.shutdown()
     return out, poses
 
 
