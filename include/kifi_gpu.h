@@ -191,6 +191,11 @@ KIFI_API kifi_status kifi_mesh_device(kifi_volume* vol, int with_indices, size_t
  * the four stages and the number of frames, and resets the accumulation. */
 KIFI_API kifi_status kifi_volume_set_profiling(kifi_volume* vol, int on);
 KIFI_API kifi_status kifi_volume_stage_times(kifi_volume* vol, double out_ms[4], int* frames);
+/* No counterpart in the reference.  While profiling is on, kifi_mesh and
+ * kifi_mesh_device time the device work of each mesh (counting passes and
+ * emission); this returns their mean in milliseconds and their count, and
+ * resets them. */
+KIFI_API kifi_status kifi_volume_mesh_times(kifi_volume* v, double* out_ms, int* meshes);
 
 /* No counterpart in the reference.  Picks the persistent CTA counts of the
  * volume's splat+emit, sort and merge/update kernels by timing them on one
@@ -224,6 +229,16 @@ KIFI_API kifi_status kifi_radix_sort_pairs_u32(uint32_t* keys, uint32_t* values,
 KIFI_API kifi_status kifi_radix_sort_u64(uint64_t* keys, size_t n);
 KIFI_API kifi_status kifi_radix_sort_pairs_u64(uint64_t* keys, uint32_t* values, size_t n);
 
+/* No counterpart in the reference: fault injection for the failure-detection
+ * tests.  Every sort's digit passes resolve their offsets by a bounded wait
+ * on the look-back words of the tiles before them.  After this call, the
+ * sorts enqueued in this process hand out tile ids from skip_tiles on (so
+ * tiles below it are never processed and the waits on them cannot end) and
+ * give up a wait after spin_limit polls, raising KIFI_ERR_TIMEOUT; every
+ * store stays inside the output buffers.  (0, 0) restores the defaults (no
+ * skipped tile, 2^22 polls).  Not for production use. */
+KIFI_API kifi_status kifi_sort_set_fault_injection(unsigned int skip_tiles, unsigned long long spin_limit);
+
 /* No counterpart in the reference.  The radix sort of
  * kifi_radix_sort_pairs_u32 for callers that must not allocate device
  * memory: it sorts keys_dev[0..n) -- and values_dev[0..n) with them when
@@ -239,7 +254,10 @@ KIFI_API kifi_status kifi_radix_sort_pairs_u64(uint64_t* keys, uint32_t* values,
  *    KIFI_ERR_INVALID_ARGUMENT and does nothing.
  *  - The first call on a device (the device current at the call) looks up
  *    the scratch area's address; make that first call before any stream
- *    capture.
+ *    capture.  The address is kept for the life of the process:
+ *    cudaDeviceReset (or another context on that device) invalidates it.
+ *  - Every call waits on the host for its sort to finish and reads the
+ *    device status word back before it returns.
  *  - There is one scratch area per device: calls that overlap in time (from
  *    several host threads, or on several streams) race on it and corrupt
  *    each other's results.  Serialise them.  The call returns only when the
@@ -278,6 +296,16 @@ KIFI_API kifi_status kifi_icp_associations(kifi_icp* icp, int64_t* target_index,
  * the eye-to-world pose of the camera that produced it. */
 KIFI_API kifi_status kifi_icp_set_target(kifi_icp* icp, const float* points, int width, int height,
                                          const float synth_eye_to_world[16]);
+
+/* Renderer::Bin of device-resident world points (3 floats each) straight
+ * into the ICP target: the z-buffered splat through world_to_clip into a
+ * width x height target, as the reference's tracking pipeline renders its
+ * mesh for the next ICP::Align (Pipeline.cpp:48-52 then :38).  Asynchronous
+ * on the ICP stream: the points must stay valid until that stream has run
+ * it. */
+KIFI_API kifi_status kifi_icp_set_target_bin_device(kifi_icp* icp, const float* points_dev, size_t n,
+                                                    const float world_to_clip[16], int width, int height,
+                                                    const float synth_eye_to_world[16]);
 
 /* Target from a depth frame (host or device memory): every pixel
  * back-projected to world space with the frame's eye-to-world pose, using
@@ -372,7 +400,11 @@ KIFI_API kifi_status kifi_volume_load(const char* path, int device, kifi_volume*
  * C FP32 (row stride ldc), accumulated in FP32 on the tcgen05 tensor cores.
  * k, lda, ldb and k_split must be multiples of 8 and A, B 16-byte aligned;
  * k_split > 0 splits K across CTAs (requires accumulate).  Synchronous on
- * `stream`. */
+ * `stream`.  Its bounded waits report through one status word per device,
+ * shared by every call: calls that overlap on the GPU (from several host
+ * threads, or on several streams) race on that word and may report each
+ * other's KIFI_ERR_TIMEOUT; serialise them.  (The proposer's own GEMMs use
+ * the status word of their proposer handle.) */
 KIFI_API kifi_status kifi_gemm_bf16(const void* a_dev, const void* b_dev, float* c_dev, int m, int n, int k,
                                     int lda, int ldb, int ldc, int k_split, int accumulate, void* stream);
 
@@ -426,6 +458,9 @@ typedef struct kifi_pipeline_desc {
     size_t initial_capacity;
     int device;
     int key_bits;           /* as kifi_volume_desc::key_bits */
+    int closed_loop;        /* 0: open loop (fuse with the given poses); 1: the reference's
+                               tracking path (fuse with the tracked poses, track against the
+                               Bin of the model's mesh) -- see kifi_pipeline_integrate */
 } kifi_pipeline_desc;
 
 typedef struct kifi_pipeline kifi_pipeline;
@@ -436,16 +471,28 @@ KIFI_API kifi_volume* kifi_pipeline_volume(kifi_pipeline* p);
 KIFI_API kifi_icp* kifi_pipeline_icp(kifi_pipeline* p);
 
 /* kifi::Pipeline::Integrate(rawDepthMap, worldToEye) (Pipeline.h:31-35,
- * Pipeline.cpp:26-56): fuses the frame with its given pose (the live path,
- * :32-35) and, when icp_iterations > 0, tracks it by ICP against the
- * previous frame's back-projection with the previous pose as the guess (the
- * reference's tracking path, :36-55); every mesh_every frames the mesh is
- * extracted on the device.  Host frame (uint16 mm or float m).  Returns with
- * the tracked eye-to-world pose in out_eye_to_world (the given pose's
- * inverse for the first frame or when tracking is off; may be NULL) once the
- * frame's tracking is done and `depth_host` may be reused; the frame's fusion
- * may still be running -- every call that reads the volume (and
- * kifi_pipeline_sync) waits for it and reports its device errors. */
+ * Pipeline.cpp:26-56).  Host frame (uint16 mm or float m).
+ *
+ * Open loop (closed_loop = 0): fuses the frame with its given pose (the
+ * reference's live path, :32-35) and, when icp_iterations > 0, also tracks
+ * it: ICP against the previous frame's back-projection, with the previous
+ * given pose as the guess.  Fusion does not use the tracked pose; frame N+1's
+ * fusion overlaps frame N's tracking.
+ *
+ * Closed loop (closed_loop = 1): the reference's tracking path (:36-55).
+ * From the second frame on, ICP aligns the frame against the Bin of the
+ * model's mesh starting from the previous tracked pose; the frame is fused
+ * with the tracked pose; the volume is meshed (vertices) and binned through
+ * EyeToClipRH * worldToEye into a 1024 x 768 target for the next frame.  The
+ * first frame's pose is the given one (the reference's constructor fixes
+ * it); later given poses are ignored.
+ *
+ * Every mesh_every frames the output mesh is extracted on the device.
+ * Returns with the tracked eye-to-world pose in out_eye_to_world (the given
+ * pose's inverse for the first frame or when tracking is off; may be NULL)
+ * once the frame's tracking is done and `depth_host` may be reused; the
+ * frame's fusion may still be running -- every call that reads the volume
+ * (and kifi_pipeline_sync) waits for it and reports its device errors. */
 KIFI_API kifi_status kifi_pipeline_integrate(kifi_pipeline* p, const void* depth_host,
                                              int depth_is_u16, const float world_to_eye[16],
                                              float out_eye_to_world[16]);
@@ -456,24 +503,40 @@ KIFI_API kifi_status kifi_pipeline_integrate_device(kifi_pipeline* p, const void
                                                     int depth_is_u16,
                                                     const float world_to_eye[16]);
 
-/* Waits for all queued frames; reports device errors and the last tracked
- * pose (may be NULL). */
+/* Waits for all queued frames and meshes; reports device errors and the
+ * last tracked pose (may be NULL). */
 KIFI_API kifi_status kifi_pipeline_sync(kifi_pipeline* p, float out_eye_to_world[16]);
 
-/* Vertex and index counts of the last mesh the pipeline extracted. */
+/* No counterpart in the reference.  Makes `stream` (a cudaStream_t) wait for
+ * all work enqueued so far on the pipeline's streams -- fusion, tracking and
+ * meshing -- without blocking the host; e.g. to record one event after a
+ * run of frames. */
+KIFI_API kifi_status kifi_pipeline_join(kifi_pipeline* p, void* stream);
+
+/* No counterpart in the reference (its stop_watch telemetry).  While the
+ * pipeline's volume has profiling on (kifi_volume_set_profiling): the mean
+ * device span of an ICP alignment (out_ms[0], per aligned frame) and of an
+ * output mesh's counting and emission (out_ms[1], per mesh), with their
+ * counts; reading resets them. */
+KIFI_API kifi_status kifi_pipeline_stage_times(kifi_pipeline* p, double out_ms[2], int out_counts[2]);
+
 /* No counterpart in the reference.  With graphs on, each frame -- the upload
  * of a page-locked host frame, the fusion launches and the tracking launches
  * on both streams -- runs as one CUDA graph: captured, applied to the
  * instantiated graph with cudaGraphExecUpdate and launched once.  Results
  * are identical to graphs off.  Frames from pageable host memory are uploaded
  * outside the graph.  kifi_pipeline_graph_stats counts instantiations and
- * in-place updates. */
+ * in-place updates.  Not offered in closed-loop mode (KIFI_ERR_UNSUPPORTED). */
 KIFI_API kifi_status kifi_pipeline_set_graphs(kifi_pipeline* p, int on);
 KIFI_API kifi_status kifi_pipeline_graph_stats(kifi_pipeline* p, long long* instantiated,
                                                long long* updated);
 
+/* Vertex and index counts of the last output mesh (waits for it). */
 KIFI_API kifi_status kifi_pipeline_mesh_counts(kifi_pipeline* p, size_t* n_verts,
                                                size_t* n_indices);
+/* Output meshes completed, and how many of them had to be emitted a second
+ * time because they outgrew the buffers sized by earlier meshes. */
+KIFI_API kifi_status kifi_pipeline_mesh_stats(kifi_pipeline* p, long long* meshes, long long* reemitted);
 
 #ifdef __cplusplus
 }

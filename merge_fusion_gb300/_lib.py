@@ -17,6 +17,10 @@ STATUS_NAMES = {
 }
 
 
+# the status codes by name (KIFI_ERR_TIMEOUT, ...), as in include/kifi_gpu.h
+globals().update({_name: _code for _code, _name in STATUS_NAMES.items()})
+
+
 class KifiError(RuntimeError):
     def __init__(self, status, detail=""):
         self.status = status
@@ -33,7 +37,7 @@ class PipelineDesc(C.Structure):
     _fields_ = [("camera", Camera), ("resolution", C.c_int), ("side_length_m", C.c_float),
                 ("truncation_m", C.c_float), ("icp_iterations", C.c_int), ("mesh_every", C.c_int),
                 ("mesh_with_indices", C.c_int), ("initial_capacity", C.c_size_t),
-                ("device", C.c_int), ("key_bits", C.c_int)]
+                ("device", C.c_int), ("key_bits", C.c_int), ("closed_loop", C.c_int)]
 
 
 class VolumeDesc(C.Structure):
@@ -131,6 +135,13 @@ SIGNATURES = {
     "kifi_pipeline_sync": (C.c_int, [C.c_void_p, C.c_void_p]),
     "kifi_pipeline_mesh_counts": (C.c_int, [C.c_void_p, C.POINTER(C.c_size_t),
                                             C.POINTER(C.c_size_t)]),
+    "kifi_pipeline_mesh_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
+    "kifi_pipeline_join": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "kifi_sort_set_fault_injection": (C.c_int, [C.c_uint, C.c_ulonglong]),
+    "kifi_volume_mesh_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
+    "kifi_pipeline_stage_times": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "kifi_icp_set_target_bin_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_int,
+                                                 C.c_int, C.c_void_p]),
 }
 
 _lib = None

@@ -90,8 +90,14 @@ kifi_status take_device_status(kifi_volume* v) {
     unsigned int st = v->ctl_host->status;
     if (!st) return KIFI_OK;
     KIFI_CUDA(cudaMemsetAsync(&v->ctl->status, 0, sizeof(unsigned int), v->stream));
+    if (st & KIFI_DEV_ERR_TIMEOUT) {
+        // the frame was not merged, but its new keys' occupancy bits may have
+        // been set: derive the bitmap from the resident keys again
+        KIFI_CUDA(bitmap_rebuild_enqueue(v->ctl, v->g, v->vb, v->ls, v->stream));
+        KIFI_CUDA(cudaStreamSynchronize(v->stream));
+        return fail(KIFI_ERR_TIMEOUT, "a bounded device wait gave up; the frame was not fused");
+    }
     KIFI_CUDA(cudaStreamSynchronize(v->stream));
-    if (st & KIFI_DEV_ERR_TIMEOUT) return fail(KIFI_ERR_TIMEOUT, "a bounded device wait gave up");
     return fail(KIFI_ERR_CAPACITY, "volume capacity exceeded on the device");
 }
 
@@ -335,7 +341,8 @@ kifi_status kifi_volume_create(const kifi_volume_desc* d, kifi_volume** out) {
     if ((e = cudaMemsetAsync(v->ctl, 0, sizeof(DeviceCtl), v->stream))) return bail(cuda_fail(e, "control block"));
     if ((e = cudaMallocHost(&v->ctl_host, sizeof(DeviceCtl)))) return bail(cuda_fail(e, "pinned"));
     std::memset(v->ctl_host, 0, sizeof(DeviceCtl));
-    const size_t r = (size_t)d->resolution;
+    // the bitmap's 4x4x4 bricks need at least 4 voxels per axis
+    const size_t r = d->resolution < 4 ? 4 : (size_t)d->resolution;
     v->vb.bitmap_words = (r * r * r + 31) / 32;
     if ((e = cudaMalloc(&v->vb.bitmap, v->vb.bitmap_words * 4))) return bail(cuda_fail(e, "bitmap"));
     if ((e = cudaMemsetAsync(v->vb.bitmap, 0, v->vb.bitmap_words * 4, v->stream))) return bail(cuda_fail(e, "bitmap"));
@@ -373,6 +380,8 @@ kifi_status kifi_volume_destroy(kifi_volume* v) {
     cudaFree(v->mesh_idx);
     for (auto e : v->event_pool) cudaEventDestroy(e);
     for (auto& ev : v->pending)
+        for (auto e : ev) cudaEventDestroy(e);
+    for (auto& ev : v->mesh_pending)
         for (auto e : ev) cudaEventDestroy(e);
     if (v->own_stream && v->stream) cudaStreamDestroy(v->stream);
     delete v;
@@ -599,7 +608,10 @@ kifi_status kifi_volume_frame_log(kifi_volume* v, uint64_t* n_before, uint64_t* 
     return KIFI_OK;
 }
 
-// Meshes into the volume's device buffers; returns the counts.
+// Meshes into the volume's device buffers; returns the counts.  The
+// counting passes and the emission run back to back (the emission reads the
+// counts on the device); when the buffers turn out too small, they are grown
+// to the counts and the emission runs again.
 static kifi_status mesh_to_device(kifi_volume* v, int with_indices, size_t* n_verts,
                                   size_t* n_indices) {
     *n_verts = *n_indices = 0;
@@ -612,32 +624,72 @@ static kifi_status mesh_to_device(kifi_volume* v, int with_indices, size_t* n_ve
     KIFI_CUDA(mesh_scratch_reserve(&v->ms, n, v->g.kb));
     const unsigned int n32 = (unsigned int)n;
     KIFI_CUDA(cudaMemcpyAsync(v->ms.n_dev, &n32, sizeof n32, cudaMemcpyHostToDevice, v->stream));
+    std::array<cudaEvent_t, 2> ev{};
+    if (v->profiling) {
+        for (int k = 0; k < 2; ++k) {
+            if (v->event_pool.empty()) {
+                cudaEvent_t e;
+                KIFI_CUDA(cudaEventCreate(&e));
+                v->event_pool.push_back(e);
+            }
+            ev[k] = v->event_pool.back();
+            v->event_pool.pop_back();
+        }
+        KIFI_CUDA(cudaEventRecord(ev[0], v->stream));
+    }
     KIFI_CUDA(mesh_count_enqueue(v->vb.keys[cur], v->vb.key_bytes, v->vb.vals[cur], n, v->g.kb,
                                  with_indices ? 1 : 0, v->ms, v->ls.sms, v->stream));
     MeshCounts* mc = &v->ctl_host_mesh;
-    KIFI_CUDA(cudaMemcpyAsync(mc, v->ms.counts, sizeof(MeshCounts), cudaMemcpyDeviceToHost,
-                              v->stream));
-    KIFI_CUDA(cudaStreamSynchronize(v->stream));
-    const size_t nv = (size_t)mc->n_verts, ni = with_indices ? (size_t)mc->n_idx : 0;
-    if (nv > v->mesh_verts_cap) {
-        cudaFree(v->mesh_verts);
-        v->mesh_verts = nullptr;
-        v->mesh_verts_cap = 0;
-        KIFI_CUDA(cudaMalloc(&v->mesh_verts, (nv + kPad) * 12));
-        v->mesh_verts_cap = nv;
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        KIFI_CUDA(mesh_emit_enqueue(v->g, v->vb.keys[cur], v->vb.key_bytes, v->vb.vals[cur], n,
+                                    with_indices ? 1 : 0, v->ms, v->mesh_verts_cap, v->mesh_idx_cap, v->mesh_verts,
+                                    v->mesh_idx, v->ls.sms, v->stream));
+        if (attempt == 0 && ev[0]) {
+            KIFI_CUDA(cudaEventRecord(ev[1], v->stream));
+            v->mesh_pending.push_back(ev);
+        }
+        KIFI_CUDA(cudaMemcpyAsync(mc, v->ms.counts, sizeof(MeshCounts), cudaMemcpyDeviceToHost, v->stream));
+        KIFI_CUDA(cudaStreamSynchronize(v->stream));
+        if (!mc->overflow) break;
+        if (attempt == 1) return fail(KIFI_ERR_CUDA, "mesh emission overflowed buffers sized to its counts");
+        const size_t nv = (size_t)mc->n_verts, ni = with_indices ? (size_t)mc->n_idx : 0;
+        if (nv > v->mesh_verts_cap) {
+            cudaFree(v->mesh_verts);
+            v->mesh_verts = nullptr;
+            v->mesh_verts_cap = 0;
+            KIFI_CUDA(cudaMalloc(&v->mesh_verts, (nv + kPad) * 12));
+            v->mesh_verts_cap = nv;
+        }
+        if (ni > v->mesh_idx_cap) {
+            cudaFree(v->mesh_idx);
+            v->mesh_idx = nullptr;
+            v->mesh_idx_cap = 0;
+            KIFI_CUDA(cudaMalloc(&v->mesh_idx, (ni + kPad) * 4));
+            v->mesh_idx_cap = ni;
+        }
     }
-    if (ni > v->mesh_idx_cap) {
-        cudaFree(v->mesh_idx);
-        v->mesh_idx = nullptr;
-        v->mesh_idx_cap = 0;
-        KIFI_CUDA(cudaMalloc(&v->mesh_idx, (ni + kPad) * 4));
-        v->mesh_idx_cap = ni;
-    }
-    KIFI_CUDA(mesh_emit_enqueue(v->g, v->vb.keys[cur], v->vb.key_bytes, v->vb.vals[cur], n, with_indices ? 1 : 0,
-                                v->ms, nv, ni, v->mesh_verts, v->mesh_idx, v->ls.sms, v->stream));
-    *n_verts = nv;
-    *n_indices = ni;
+    *n_verts = (size_t)mc->n_verts;
+    *n_indices = with_indices ? (size_t)mc->n_idx : 0;
     v->mesh_counts_valid = true;
+    return KIFI_OK;
+}
+
+kifi_status kifi_volume_mesh_times(kifi_volume* v, double* out_ms, int* meshes) {
+    if (!v || !out_ms) return fail(KIFI_ERR_INVALID_ARGUMENT, "null argument");
+    KIFI_CUDA(cudaSetDevice(v->device));
+    double total = 0.0;
+    const int n = (int)v->mesh_pending.size();
+    for (auto& ev : v->mesh_pending) {
+        float ms = 0.0f;
+        KIFI_CUDA(cudaEventSynchronize(ev[1]));
+        KIFI_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+        total += ms;
+        v->event_pool.push_back(ev[0]);
+        v->event_pool.push_back(ev[1]);
+    }
+    v->mesh_pending.clear();
+    *out_ms = n ? total / n : 0.0;
+    if (meshes) *meshes = n;
     return KIFI_OK;
 }
 

@@ -29,6 +29,8 @@ struct kifi_icp {
     long long* pairs = nullptr;      // per source: target index, or -1
     float* pairs_len2 = nullptr;     // per source: len^2
     size_t pairs_cap = 0, pairs_n = 0;
+    void* zbuf = nullptr;            // Bin's z-buffer (8 bytes per target pixel)
+    size_t zbuf_cap = 0;
 };
 
 namespace {
@@ -164,6 +166,7 @@ kifi_status kifi_icp_destroy(kifi_icp* c) {
     cudaFree(c->pairs);
     cudaFree(c->pairs_len2);
     cudaFree(c->staging);
+    cudaFree(c->zbuf);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return KIFI_OK;
@@ -233,6 +236,25 @@ kifi_status kifi_icp_set_target_from_depth(kifi_icp* c, const void* depth, int o
     c->sw = cam->width;
     c->sh = cam->height;
     c->synth_e2w = e2w;
+    c->have_target = true;
+    return KIFI_OK;
+}
+
+kifi_status kifi_icp_set_target_bin_device(kifi_icp* c, const float* points_dev, size_t n,
+                                           const float world_to_clip[16], int width, int height,
+                                           const float synth_eye_to_world[16]) {
+    if (!c || (n && !points_dev) || !world_to_clip || width <= 0 || height <= 0 || !synth_eye_to_world)
+        return fail(KIFI_ERR_INVALID_ARGUMENT, "bad argument");
+    if (n >= ((size_t)1 << 32)) return fail(KIFI_ERR_UNSUPPORTED, "more than 2^32 points");
+    KIFI_CUDA(cudaSetDevice(c->device));
+    kifi_status s = reserve_target(c, width, height);
+    if (s) return s;
+    if ((s = reserve_bytes(&c->zbuf, &c->zbuf_cap, (size_t)width * height * 8, c->stream))) return s;
+    KIFI_CUDA(bin_target_enqueue(points_dev, (unsigned int)n, load_mat(world_to_clip), width, height,
+                                 (unsigned long long*)c->zbuf, c->synth, c->ls.sms * 4, c->stream));
+    c->sw = width;
+    c->sh = height;
+    c->synth_e2w = load_mat(synth_eye_to_world);
     c->have_target = true;
     return KIFI_OK;
 }

@@ -1,8 +1,21 @@
 // kifi_api_pipeline.cu -- kifi::Pipeline on the GPU (KinectFission/kifi/
-// Pipeline.h:16-56, Pipeline.cpp:26-56): per frame, fuse the depth frame with
-// its given pose (the live path, Pipeline.cpp:32-35) and track it with ICP
-// against the previous frame (the tracking path the reference keeps under
-// #else, :36-55), and extract the mesh every N frames.
+// Pipeline.h:16-56, Pipeline.cpp:26-56), in one of two modes:
+//
+//  open loop (default): per frame, fuse the depth frame with its given pose
+//    (the live path, Pipeline.cpp:32-35) and track it with ICP against the
+//    previous frame's back-projection, with the previous given pose as the
+//    guess; the tracked pose is reported, fusion does not use it.
+//  closed loop (kifi_pipeline_desc::closed_loop): the reference's tracking
+//    path (:36-55).  Per frame after the first, ICP aligns the frame
+//    against the Bin of the model's mesh, starting from the previous tracked
+//    pose; the frame is fused with the tracked pose; then the volume is
+//    meshed (vertices only, Mesher::Mesh(verts)) and the vertices are binned
+//    through EyeToClipRH * worldToEye into a 1024 x 768 target for the next
+//    frame.  Each stage needs the one before, so nothing overlaps across
+//    frames; the host reads the tracked pose back before it enqueues the
+//    fusion.
+//
+// The mesh every N frames (both modes) is the caller's output mesh.
 //
 // Fusion runs on the volume's stream and tracking on the ICP context's
 // stream, so the HBM-bound merge/update and the shared-memory-bound ICP
@@ -21,18 +34,27 @@
 //
 // Meshing every N frames never blocks the host: on a mesh frame a third
 // stream waits for that frame's fusion, copies the resident voxels into a
-// snapshot (count and buffer read on the device) and runs the counting
-// passes; the volume stream only waits for the copy before fusing the next
-// frame.  Later pipeline calls poll the counts without blocking and, once
-// they are in, size the outputs (stream-ordered allocation) and enqueue the
-// vertex/index emission on the mesh stream.  kifi_pipeline_mesh_counts waits
-// for the latest mesh.
+// snapshot (count and buffer read on the device), runs the counting passes
+// and the vertex/index emission, which reads the counts on the device; the
+// volume stream only waits for the copy before fusing the next frame.  The
+// emission writes into buffers sized by earlier meshes; when a mesh needs
+// more, it writes nothing and flags it, and the next pipeline call that sees
+// the counts grows the buffers (stream-ordered allocation) and emits again.
+// kifi_pipeline_mesh_counts, kifi_pipeline_sync and kifi_pipeline_join cover
+// the mesh stream.
+#include <array>
 #include <cstring>
 #include <new>
+#include <vector>
 
 #include "kifi_api_util.h"
 
 using namespace kifi;
+
+namespace {
+// the synthetic target the reference's tracking pipeline bins into (Pipeline.cpp:50)
+constexpr int kClosedLoopTargetW = 1024, kClosedLoopTargetH = 768;
+}  // namespace
 
 struct kifi_pipeline {
     kifi_pipeline_desc desc{};
@@ -64,49 +86,109 @@ struct kifi_pipeline {
     cudaGraphExec_t exec = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr, after = nullptr;
     long long graph_builds = 0, graph_updates = 0;
+    long long meshes = 0, mesh_reemits = 0;
+    bool closed = false;
+    cudaEvent_t vol_done = nullptr;     // closed loop: the frame's mesh is on the device
+    cudaEvent_t join_ev[3] = {nullptr, nullptr, nullptr};
+    // stage timers while the volume's profiling is on: ICP alignment spans
+    // on the tracking stream, mesh spans (counting + emission) on the mesh stream
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<std::array<cudaEvent_t, 2>> track_pending, mesh_pending;
+    double track_ms = 0.0, mesh_ms = 0.0;
+    int track_n = 0, mesh_n = 0;
 };
 
 namespace {
 
-// counts of the snapshot in: size the outputs and enqueue the emission
-kifi_status mesh_emit(kifi_pipeline* p) {
-    const MeshCounts& c = *p->counts_host;
-    const size_t nv = (size_t)c.n_verts, ni = p->desc.mesh_with_indices ? (size_t)c.n_idx : 0;
-    if (nv + kPad > p->mverts_cap) {
-        if (p->mverts) KIFI_CUDA(cudaFreeAsync(p->mverts, p->ms));
-        p->mverts_cap = (nv + kPad) + (nv + kPad) / 4;
-        KIFI_CUDA(cudaMallocAsync((void**)&p->mverts, p->mverts_cap * 12, p->ms));
+kifi_status take_event(kifi_pipeline* p, cudaEvent_t* e) {
+    if (p->ev_pool.empty()) {
+        cudaEvent_t x;
+        KIFI_CUDA(cudaEventCreate(&x));
+        p->ev_pool.push_back(x);
     }
-    if (ni + kPad > p->midx_cap) {
-        if (p->midx) KIFI_CUDA(cudaFreeAsync(p->midx, p->ms));
-        p->midx_cap = (ni + kPad) + (ni + kPad) / 4;
-        KIFI_CUDA(cudaMallocAsync((void**)&p->midx, p->midx_cap * 4, p->ms));
-    }
-    KIFI_CUDA(mesh_emit_enqueue(p->vol->g, p->snap_keys, p->vol->vb.key_bytes, p->snap_vals, p->snap_n,
-                                p->desc.mesh_with_indices, p->mscr, nv, ni, p->mverts, p->midx, p->vol->ls.sms,
-                                p->ms));
-    p->mesh_verts = nv;
-    p->mesh_indices = ni;
-    p->counting = false;
+    *e = p->ev_pool.back();
+    p->ev_pool.pop_back();
     return KIFI_OK;
 }
 
-// a mesh whose counts are in gets its emission; with `wait`, wait for them
-kifi_status mesh_poll(kifi_pipeline* p, bool wait) {
-    if (!p->counting) return KIFI_OK;
-    if (wait) {
-        KIFI_CUDA(cudaEventSynchronize(p->counts_ready));
-    } else {
-        const cudaError_t q = cudaEventQuery(p->counts_ready);
-        if (q == cudaErrorNotReady) return KIFI_OK;
-        if (q != cudaSuccess) return cuda_fail(q, "mesh counts");
-    }
-    return mesh_emit(p);
+// both events of a timed span, or none when profiling is off
+kifi_status span_begin(kifi_pipeline* p, std::array<cudaEvent_t, 2>& ev, cudaStream_t st) {
+    ev = {nullptr, nullptr};
+    if (!p->vol->profiling) return KIFI_OK;
+    kifi_status s = take_event(p, &ev[0]);
+    if (!s) s = take_event(p, &ev[1]);
+    if (s) return s;
+    KIFI_CUDA(cudaEventRecord(ev[0], st));
+    return KIFI_OK;
 }
 
-// snapshot + counting passes of the volume as of the frame just enqueued
+kifi_status span_end(std::vector<std::array<cudaEvent_t, 2>>& pending, std::array<cudaEvent_t, 2>& ev,
+                     cudaStream_t st) {
+    if (!ev[0]) return KIFI_OK;
+    KIFI_CUDA(cudaEventRecord(ev[1], st));
+    pending.push_back(ev);
+    return KIFI_OK;
+}
+
+// emission of the snapshot into the current buffers, then its counts to the host
+kifi_status mesh_emit(kifi_pipeline* p, std::array<cudaEvent_t, 2>* ev) {
+    KIFI_CUDA(mesh_emit_enqueue(p->vol->g, p->snap_keys, p->vol->vb.key_bytes, p->snap_vals, p->snap_n,
+                                p->desc.mesh_with_indices, p->mscr, p->mverts_cap, p->midx_cap, p->mverts, p->midx,
+                                p->vol->ls.sms, p->ms));
+    if (ev) {
+        kifi_status s = span_end(p->mesh_pending, *ev, p->ms);
+        if (s) return s;
+    }
+    KIFI_CUDA(cudaMemcpyAsync(p->counts_host, p->mscr.counts, sizeof(MeshCounts), cudaMemcpyDeviceToHost, p->ms));
+    KIFI_CUDA(cudaEventRecord(p->counts_ready, p->ms));
+    p->counting = true;
+    return KIFI_OK;
+}
+
+// A mesh whose emission has run: take its counts, or -- when its buffers
+// were too small -- grow them and emit again.  With `wait`, until it is done.
+kifi_status mesh_poll(kifi_pipeline* p, bool wait) {
+    for (int emitted = 0; p->counting; ++emitted) {
+        // buffers grown to the counts hold the mesh: a second overflow is an internal error
+        if (emitted > 1) return fail(KIFI_ERR_CUDA, "mesh emission overflowed buffers sized to its counts");
+        if (wait) {
+            KIFI_CUDA(cudaEventSynchronize(p->counts_ready));
+        } else {
+            const cudaError_t q = cudaEventQuery(p->counts_ready);
+            if (q == cudaErrorNotReady) return KIFI_OK;
+            if (q != cudaSuccess) return cuda_fail(q, "mesh counts");
+        }
+        const MeshCounts& c = *p->counts_host;
+        const size_t nv = (size_t)c.n_verts, ni = p->desc.mesh_with_indices ? (size_t)c.n_idx : 0;
+        if (!c.overflow) {
+            p->mesh_verts = nv;
+            p->mesh_indices = ni;
+            p->counting = false;
+            ++p->meshes;
+            return KIFI_OK;
+        }
+        if (nv > p->mverts_cap) {
+            if (p->mverts) KIFI_CUDA(cudaFreeAsync(p->mverts, p->ms));
+            p->mverts = nullptr;
+            p->mverts_cap = nv + nv / 4;
+            KIFI_CUDA(cudaMallocAsync((void**)&p->mverts, (p->mverts_cap + kPad) * 12, p->ms));
+        }
+        if (ni > p->midx_cap) {
+            if (p->midx) KIFI_CUDA(cudaFreeAsync(p->midx, p->ms));
+            p->midx = nullptr;
+            p->midx_cap = ni + ni / 4;
+            KIFI_CUDA(cudaMallocAsync((void**)&p->midx, (p->midx_cap + kPad) * 4, p->ms));
+        }
+        ++p->mesh_reemits;
+        kifi_status s = mesh_emit(p, nullptr);
+        if (s) return s;
+    }
+    return KIFI_OK;
+}
+
+// snapshot, counting passes and emission of the volume as of the frame just enqueued
 kifi_status mesh_begin(kifi_pipeline* p) {
-    kifi_status s = mesh_poll(p, true);  // one mesh at a time
+    kifi_status s = mesh_poll(p, true);  // one mesh at a time: the snapshot and buffers are shared
     if (s) return s;
     kifi_volume* v = p->vol;
     if (p->snap_cap < v->vb.cap) {
@@ -132,11 +214,65 @@ kifi_status mesh_begin(kifi_pipeline* p) {
                                     p->ms));
     KIFI_CUDA(cudaEventRecord(p->snap_done, p->ms));
     KIFI_CUDA(cudaStreamWaitEvent(p->vs, p->snap_done, 0));  // fusion may overwrite the buffers after the copy
+    std::array<cudaEvent_t, 2> ev;
+    if ((s = span_begin(p, ev, p->ms))) return s;
     KIFI_CUDA(mesh_count_enqueue(p->snap_keys, v->vb.key_bytes, p->snap_vals, p->snap_n, v->g.kb,
                                  p->desc.mesh_with_indices, p->mscr, v->ls.sms, p->ms));
-    KIFI_CUDA(cudaMemcpyAsync(p->counts_host, p->mscr.counts, sizeof(MeshCounts), cudaMemcpyDeviceToHost, p->ms));
-    KIFI_CUDA(cudaEventRecord(p->counts_ready, p->ms));
-    p->counting = true;
+    return mesh_emit(p, &ev);
+}
+
+// ICP alignment of a device frame, timed when profiling
+kifi_status align(kifi_pipeline* p, const void* depth_dev, bool u16, const float* guess) {
+    std::array<cudaEvent_t, 2> ev;
+    kifi_status s = span_begin(p, ev, p->is);
+    if (!s) s = kifi_icp_align_device(p->icp, depth_dev, u16 ? 1 : 0, &p->desc.camera, guess,
+                                      p->desc.icp_iterations);
+    if (!s) s = span_end(p->track_pending, ev, p->is);
+    return s;
+}
+
+// One frame of the reference's tracking pipeline (Pipeline.cpp:36-55; see
+// the file comment).  k: the upload slot of a host frame, or -1.
+kifi_status closed_loop_frame(kifi_pipeline* p, const void* depth_dev, bool u16, int k,
+                              const float* world_to_eye) {
+    const kifi_camera& cam = p->desc.camera;
+    kifi_status s = mesh_poll(p, false);
+    if (s) return s;
+    Mat4 e2w;
+    if (p->frame == 0 || p->desc.icp_iterations == 0) {
+        // the first pose is the caller's (the reference starts from the
+        // identity moved 2 m along z, Pipeline.cpp:20-21)
+        e2w = invert_transform(load_mat(world_to_eye));
+        if (k >= 0) KIFI_CUDA(cudaEventRecord(p->released[k], p->is));
+    } else {
+        // m_eyeToWorld = m_icp.Align(rawDepthMap, m_eyeToWorld, synth, m_eyeToWorld, cam) (:37-38)
+        if (k >= 0) KIFI_CUDA(cudaStreamWaitEvent(p->is, p->uploaded[k], 0));
+        if ((s = align(p, depth_dev, u16, p->prev_e2w))) return s;
+        if (k >= 0) KIFI_CUDA(cudaEventRecord(p->released[k], p->is));
+        float pose[16];
+        if ((s = kifi_icp_result(p->icp, pose, nullptr, nullptr, nullptr, 0, nullptr))) return s;
+        e2w = load_mat(pose);
+    }
+    // tmp = m_eyeToWorld; invert_transform(tmp); Integrate(volume, frame, cam, tmp) (:40-44)
+    const Mat4 w2e = invert_transform(e2w);
+    if ((s = kifi_integrate_device(p->vol, depth_dev, u16 ? 1 : 0, &cam, w2e.m))) return s;
+    if (p->desc.icp_iterations > 0) {
+        // m_mesher.Mesh(m_volume, m_tmpSynthPointCloud) (:46): vertices only
+        size_t nv = 0, ni = 0;
+        const float* verts = nullptr;
+        if ((s = kifi_mesh_device(p->vol, 0, &nv, &ni, &verts, nullptr))) return s;
+        // m_renderer.Bin(cloud, EyeToClipRH() * tmp, synth 1024 x 768) (:48-52)
+        KIFI_CUDA(cudaEventRecord(p->vol_done, p->vs));
+        KIFI_CUDA(cudaStreamWaitEvent(p->is, p->vol_done, 0));
+        const Mat4 w2c = mat_mul(eye_to_clip(cam), w2e);
+        if ((s = kifi_icp_set_target_bin_device(p->icp, verts, nv, w2c.m, kClosedLoopTargetW, kClosedLoopTargetH,
+                                                e2w.m)))
+            return s;
+    }
+    std::memcpy(p->prev_e2w, e2w.m, 64);
+    p->have_prev = true;
+    ++p->frame;
+    if (p->desc.mesh_every > 0 && p->frame % p->desc.mesh_every == 0 && (s = mesh_begin(p))) return s;
     return KIFI_OK;
 }
 
@@ -150,10 +286,7 @@ kifi_status track_and_fuse(kifi_pipeline* p, const void* depth_dev, bool u16, in
     const Mat4 e2w = invert_transform(load_mat(world_to_eye));
     if (p->desc.icp_iterations > 0) {
         if (k >= 0) KIFI_CUDA(cudaStreamWaitEvent(p->is, p->uploaded[k], 0));
-        if (p->have_prev &&
-            (s = kifi_icp_align_device(p->icp, depth_dev, u16 ? 1 : 0, &cam, p->prev_e2w,
-                                       p->desc.icp_iterations)))
-            return s;
+        if (p->have_prev && (s = align(p, depth_dev, u16, p->prev_e2w))) return s;
         // this frame becomes the next frame's target
         if ((s = kifi_icp_set_target_from_depth(p->icp, depth_dev, 1, u16 ? 1 : 0, &cam, e2w.m)))
             return s;
@@ -237,6 +370,10 @@ kifi_status frame_graph(kifi_pipeline* p, const void* host_src, size_t bytes, co
 // frame's fusion may still run (every call that reads the volume waits for it
 // and reports its device errors, as after kifi_pipeline_integrate_device).
 kifi_status frame_result(kifi_pipeline* p, int k, float out_eye_to_world[16]) {
+    if (p->closed) {  // the pose was read back before the frame's fusion
+        if (out_eye_to_world) std::memcpy(out_eye_to_world, p->prev_e2w, 64);
+        return KIFI_OK;
+    }
     if (p->desc.icp_iterations > 0) {
         if (p->frame > 1)
             return kifi_icp_result(p->icp, out_eye_to_world, nullptr, nullptr, nullptr, 0, nullptr);
@@ -257,9 +394,11 @@ kifi_status kifi_pipeline_create(const kifi_pipeline_desc* d, kifi_pipeline** ou
     *out = nullptr;
     if (d->icp_iterations < 0 || d->icp_iterations > kIcpMaxStats || d->mesh_every < 0)
         return fail(KIFI_ERR_INVALID_ARGUMENT, "bad iteration count or mesh period");
+    if (d->closed_loop != 0 && d->closed_loop != 1) return fail(KIFI_ERR_INVALID_ARGUMENT, "closed_loop must be 0 or 1");
     kifi_pipeline* p = new (std::nothrow) kifi_pipeline();
     if (!p) return fail(KIFI_ERR_OUT_OF_MEMORY, "host allocation");
     p->desc = *d;
+    p->closed = d->closed_loop == 1;
     kifi_volume_desc vd{};
     vd.resolution = d->resolution;
     vd.side_length_m = d->side_length_m;
@@ -268,7 +407,7 @@ kifi_status kifi_pipeline_create(const kifi_pipeline_desc* d, kifi_pipeline** ou
     vd.device = d->device;
     vd.key_bits = d->key_bits;
     kifi_status s = kifi_volume_create(&vd, &p->vol);
-    if (!s && d->icp_iterations > 0) {
+    if (!s && d->icp_iterations > 0 && !p->closed) {  // closed loop: fusion never runs beside tracking
         p->vol->tracking_grids = true;
         tracking_launch_shape(&p->vol->ls);
     }
@@ -294,6 +433,8 @@ kifi_status kifi_pipeline_create(const kifi_pipeline_desc* d, kifi_pipeline** ou
     if (!e) e = cudaHostAlloc((void**)&p->counts_host, sizeof(MeshCounts), cudaHostAllocDefault);
     if (!e) e = cudaEventCreateWithFlags(&p->join, cudaEventDisableTiming);
     if (!e) e = cudaEventCreateWithFlags(&p->after, cudaEventDisableTiming);
+    if (!e) e = cudaEventCreateWithFlags(&p->vol_done, cudaEventDisableTiming);
+    for (int i = 0; i < 3 && !e; ++i) e = cudaEventCreateWithFlags(&p->join_ev[i], cudaEventDisableTiming);
     if (e) {
         kifi_pipeline_destroy(p);
         return cuda_fail(e, "pipeline events");
@@ -315,6 +456,12 @@ kifi_status kifi_pipeline_destroy(kifi_pipeline* p) {
     if (p->fork) cudaEventDestroy(p->fork);
     if (p->join) cudaEventDestroy(p->join);
     if (p->after) cudaEventDestroy(p->after);
+    if (p->vol_done) cudaEventDestroy(p->vol_done);
+    for (int i = 0; i < 3; ++i)
+        if (p->join_ev[i]) cudaEventDestroy(p->join_ev[i]);
+    for (auto& a : p->track_pending) p->ev_pool.insert(p->ev_pool.end(), a.begin(), a.end());
+    for (auto& a : p->mesh_pending) p->ev_pool.insert(p->ev_pool.end(), a.begin(), a.end());
+    for (cudaEvent_t x : p->ev_pool) cudaEventDestroy(x);
     if (p->exec) cudaGraphExecDestroy(p->exec);
     if (p->ms) {
         cudaStreamSynchronize(p->ms);
@@ -343,6 +490,7 @@ kifi_status kifi_pipeline_integrate_device(kifi_pipeline* p, const void* depth_d
                                            const float world_to_eye[16]) {
     if (!p || !depth_dev || !world_to_eye) return fail(KIFI_ERR_INVALID_ARGUMENT, "bad argument");
     KIFI_CUDA(cudaSetDevice(p->desc.device));
+    if (p->closed) return closed_loop_frame(p, depth_dev, depth_is_u16 != 0, -1, world_to_eye);
     if (p->graphs) return frame_graph(p, nullptr, 0, depth_dev, depth_is_u16 != 0, world_to_eye);
     return track_and_fuse(p, depth_dev, depth_is_u16 != 0, -1, world_to_eye);
 }
@@ -380,7 +528,8 @@ kifi_status kifi_pipeline_integrate(kifi_pipeline* p, const void* depth_host, in
     }
     KIFI_CUDA(cudaMemcpyAsync(p->slot[k], depth_host, bytes, cudaMemcpyHostToDevice, p->vs));
     KIFI_CUDA(cudaEventRecord(p->uploaded[k], p->vs));
-    kifi_status s = track_and_fuse(p, p->slot[k], depth_is_u16 != 0, k, world_to_eye);
+    kifi_status s = p->closed ? closed_loop_frame(p, p->slot[k], depth_is_u16 != 0, k, world_to_eye)
+                              : track_and_fuse(p, p->slot[k], depth_is_u16 != 0, k, world_to_eye);
     if (s) return s;
     return frame_result(p, k, out_eye_to_world);
 }
@@ -390,8 +539,10 @@ kifi_status kifi_pipeline_sync(kifi_pipeline* p, float out_eye_to_world[16]) {
     KIFI_CUDA(cudaSetDevice(p->desc.device));
     kifi_status s = kifi_volume_sync(p->vol);
     if (s) return s;
+    if ((s = mesh_poll(p, true))) return s;
+    KIFI_CUDA(cudaStreamSynchronize(p->ms));
     if (out_eye_to_world) {
-        if (p->desc.icp_iterations > 0 && p->frame > 1)
+        if (!p->closed && p->desc.icp_iterations > 0 && p->frame > 1)
             return kifi_icp_result(p->icp, out_eye_to_world, nullptr, nullptr, nullptr, 0, nullptr);
         std::memcpy(out_eye_to_world, p->prev_e2w, 64);
     }
@@ -399,8 +550,47 @@ kifi_status kifi_pipeline_sync(kifi_pipeline* p, float out_eye_to_world[16]) {
     return KIFI_OK;
 }
 
+kifi_status kifi_pipeline_join(kifi_pipeline* p, void* stream) {
+    if (!p) return fail(KIFI_ERR_INVALID_ARGUMENT, "null pipeline");
+    KIFI_CUDA(cudaSetDevice(p->desc.device));
+    const cudaStream_t own[3] = {p->vs, p->is, p->ms};
+    for (int i = 0; i < 3; ++i) {
+        KIFI_CUDA(cudaEventRecord(p->join_ev[i], own[i]));
+        KIFI_CUDA(cudaStreamWaitEvent((cudaStream_t)stream, p->join_ev[i], 0));
+    }
+    return KIFI_OK;
+}
+
+kifi_status kifi_pipeline_stage_times(kifi_pipeline* p, double out_ms[2], int out_counts[2]) {
+    if (!p) return fail(KIFI_ERR_INVALID_ARGUMENT, "null pipeline");
+    KIFI_CUDA(cudaSetDevice(p->desc.device));
+    kifi_status s = mesh_poll(p, true);
+    if (s) return s;
+    std::vector<std::array<cudaEvent_t, 2>>* lists[2] = {&p->track_pending, &p->mesh_pending};
+    double* acc[2] = {&p->track_ms, &p->mesh_ms};
+    int* cnt[2] = {&p->track_n, &p->mesh_n};
+    for (int i = 0; i < 2; ++i) {
+        for (auto& a : *lists[i]) {
+            float ms = 0.0f;
+            KIFI_CUDA(cudaEventSynchronize(a[1]));
+            KIFI_CUDA(cudaEventElapsedTime(&ms, a[0], a[1]));
+            *acc[i] += ms;
+            ++*cnt[i];
+            p->ev_pool.push_back(a[0]);
+            p->ev_pool.push_back(a[1]);
+        }
+        lists[i]->clear();
+        if (out_ms) out_ms[i] = *cnt[i] ? *acc[i] / *cnt[i] : 0.0;
+        if (out_counts) out_counts[i] = *cnt[i];
+        *acc[i] = 0.0;
+        *cnt[i] = 0;
+    }
+    return KIFI_OK;
+}
+
 kifi_status kifi_pipeline_set_graphs(kifi_pipeline* p, int on) {
     if (!p) return fail(KIFI_ERR_INVALID_ARGUMENT, "null pipeline");
+    if (on && p->closed) return fail(KIFI_ERR_UNSUPPORTED, "graphs are not offered in closed-loop mode");
     p->graphs = on != 0;
     return KIFI_OK;
 }
@@ -420,6 +610,13 @@ kifi_status kifi_pipeline_mesh_counts(kifi_pipeline* p, size_t* n_verts, size_t*
     KIFI_CUDA(cudaStreamSynchronize(p->ms));
     *n_verts = p->mesh_verts;
     *n_indices = p->mesh_indices;
+    return KIFI_OK;
+}
+
+kifi_status kifi_pipeline_mesh_stats(kifi_pipeline* p, long long* meshes, long long* reemitted) {
+    if (!p) return fail(KIFI_ERR_INVALID_ARGUMENT, "null pipeline");
+    if (meshes) *meshes = p->meshes;
+    if (reemitted) *reemitted = p->mesh_reemits;
     return KIFI_OK;
 }
 

@@ -70,6 +70,7 @@ struct kifi_volume {
     bool profiling = false;
     std::vector<cudaEvent_t> event_pool;
     std::vector<std::array<cudaEvent_t, kStageEvents>> pending;
+    std::vector<std::array<cudaEvent_t, 2>> mesh_pending;  // counting + emission of kifi_mesh*
 };
 
 // integrate entry shared by the ABI translation units: enqueues one frame

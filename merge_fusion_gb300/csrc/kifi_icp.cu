@@ -1081,6 +1081,20 @@ __global__ void k_bin_resolve(const float* __restrict__ pts, const unsigned long
     }
 }
 
+// the same resolve into the association's float4 target layout
+__global__ void k_bin_resolve_target(const float* __restrict__ pts, const unsigned long long* __restrict__ zbuf,
+                                     int n_pix, float4* __restrict__ out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n_pix; i += gridDim.x * blockDim.x) {
+        const unsigned long long z = zbuf[i];
+        float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (z != ~0ull) {
+            const unsigned int j = (unsigned int)(z & 0xffffffffu);
+            o = make_float4(pts[3 * j], pts[3 * j + 1], pts[3 * j + 2], 0.f);
+        }
+        out[i] = o;
+    }
+}
+
 }  // namespace
 
 cudaError_t icp_align_enqueue(const IcpArgs& a, IcpState* st, const Mat4& guess, int iterations,
@@ -1137,6 +1151,15 @@ cudaError_t bin_enqueue(const float* pts, unsigned int n, const Mat4& w2c, int w
     if (e) return e;
     if (n) k_bin_splat<<<ctas, kThreads, 0, st>>>(pts, n, w2c, width, height, zbuf);
     k_bin_resolve<<<ctas, kThreads, 0, st>>>(pts, zbuf, width * height, out);
+    return cudaGetLastError();
+}
+
+cudaError_t bin_target_enqueue(const float* pts, unsigned int n, const Mat4& w2c, int width, int height,
+                               unsigned long long* zbuf, float4* out, int ctas, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(zbuf, 0xff, (size_t)width * height * 8, st);
+    if (e) return e;
+    if (n) k_bin_splat<<<ctas, kThreads, 0, st>>>(pts, n, w2c, width, height, zbuf);
+    k_bin_resolve_target<<<ctas, kThreads, 0, st>>>(pts, zbuf, width * height, out);
     return cudaGetLastError();
 }
 

@@ -23,6 +23,11 @@ struct SortScratch {
     uint32_t* alt_vals = nullptr;
     unsigned int* status = nullptr;         // where timeouts are reported
     size_t max_tiles = 0, max_n = 0;
+    // polls of a predecessor's look-back word before a pass gives up, and the
+    // first tile id the passes hand out (0; a test sets both through
+    // kifi_sort_set_fault_injection to make a look-back wait run out)
+    unsigned long long spin_limit = 0;
+    unsigned int first_tile = 0;
 };
 
 size_t sort_max_tiles(size_t max_n);
@@ -81,12 +86,16 @@ cudaError_t insert_filter_enqueue(DeviceCtl* ctl, const Geom& g, VolumeBuffers& 
                                   const LaunchShape& ls, cudaStream_t st);
 cudaError_t insert_merge_enqueue(DeviceCtl* ctl, const Geom& g, VolumeBuffers& vb,
                                  const float2* vals_dev, const LaunchShape& ls, cudaStream_t st);
+// clears the occupancy bitmap and sets the bits of the resident keys
+cudaError_t bitmap_rebuild_enqueue(const DeviceCtl* ctl, const Geom& g, const VolumeBuffers& vb,
+                                   const LaunchShape& ls, cudaStream_t st);
 
 // ---------------------------------------------------------------- mesher
 struct MeshCounts {
     unsigned long long n_verts;
     unsigned long long n_idx;
     unsigned long long missing_min;  // smallest triangle edge id without a vertex (or ~0)
+    unsigned long long overflow;     // emission skipped: the output buffers were too small
 };
 
 struct MeshScratch {
@@ -105,10 +114,13 @@ cudaError_t mesh_scratch_reserve(MeshScratch* m, size_t n, int kb);
 void mesh_scratch_free(MeshScratch* m);
 cudaError_t mesh_count_enqueue(const void* keys, int key_bytes, const float2* vals, size_t n_cap, int kb,
                                int with_indices, MeshScratch& ms, int sms, cudaStream_t st);
+// Emission reads the counts on the device (ms.counts, written by the
+// counting passes), so it can be enqueued right behind them.  The buffers
+// hold vert_cap vertices and idx_cap indices; when the mesh needs more, the
+// emission writes nothing and sets ms.counts->overflow instead.
 cudaError_t mesh_emit_enqueue(const Geom& g, const void* keys, int key_bytes, const float2* vals, size_t n_cap,
-                              int with_indices, MeshScratch& ms, unsigned long long n_verts,
-                              unsigned long long n_idx, float* verts_dev, uint32_t* idx_dev, int sms,
-                              cudaStream_t st);
+                              int with_indices, MeshScratch& ms, size_t vert_cap, size_t idx_cap,
+                              float* verts_dev, uint32_t* idx_dev, int sms, cudaStream_t st);
 cudaError_t mesh_snapshot_enqueue(const DeviceCtl* ctl, const VolumeBuffers& vb, void* keys, float2* vals,
                                   size_t cap, unsigned int* n_dev, int sms, cudaStream_t st);
 
@@ -159,6 +171,9 @@ cudaError_t expand_target_enqueue(const float* in, int n, float4* out, int ctas,
 
 cudaError_t bin_enqueue(const float* pts, unsigned int n, const Mat4& w2c, int width, int height,
                         unsigned long long* zbuf, float* out, int ctas, cudaStream_t st);
+// Bin straight into an ICP target (float4 per pixel, w unused)
+cudaError_t bin_target_enqueue(const float* pts, unsigned int n, const Mat4& w2c, int width, int height,
+                               unsigned long long* zbuf, float4* out, int ctas, cudaStream_t st);
 
 // C[M x N] (+)= A[M x K] * B[N x K]^T, BF16 in, FP32 out, on tcgen05 tensor
 // cores (kifi_tc_gemm.cu).  k_split > 0 splits K across CTAs that add into C

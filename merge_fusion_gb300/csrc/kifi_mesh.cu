@@ -249,8 +249,9 @@ __global__ void __launch_bounds__(kThreads) k_mesh_emit(const K* __restrict__ ke
                                                         const uint4* __restrict__ corners,
                                                         const unsigned long long* __restrict__ scan,
                                                         const unsigned long long* __restrict__ tile_offsets,
-                                                        unsigned long long n_verts,
-                                                        unsigned long long n_idx,
+                                                        MeshCounts* __restrict__ mc,
+                                                        unsigned long long vert_cap,
+                                                        unsigned long long idx_cap,
                                                         unsigned long long missing_bound,
                                                         const unsigned long long* __restrict__ missing_bound_dev,
                                                         float* __restrict__ verts,
@@ -263,6 +264,13 @@ __global__ void __launch_bounds__(kThreads) k_mesh_emit(const K* __restrict__ ke
     }
     const unsigned int n = *n_dev;
     const Codec<K> cd(kb);
+    // the counts of the counting passes; outputs that do not fit are not written
+    // (every CTA sees the same counts and returns alike; the host grows and re-emits)
+    const unsigned long long n_verts = mc->n_verts, n_idx = mc->n_idx;
+    const bool overflow = n_verts > vert_cap || (kTris && n_idx > idx_cap);
+    // the flag describes this emission (an earlier one into smaller buffers may have set it)
+    if (blockIdx.x == 0 && threadIdx.x == 0) mc->overflow = overflow ? 1ull : 0ull;
+    if (overflow) return;
     // a re-run for the index mapping's stop rule takes its bound from the first run, and only
     // when that run found a missing vertex
     if (missing_bound_dev) {
@@ -455,6 +463,7 @@ __global__ void __launch_bounds__(kThreads) k_scan_sums(unsigned long long* __re
         counts->n_verts = carry & 0xffffffffull;
         counts->n_idx = carry >> 32;
         counts->missing_min = ~0ull;
+        counts->overflow = 0ull;
     }
 }
 
@@ -530,34 +539,33 @@ cudaError_t mesh_count_enqueue(const void* keys, int key_bytes, const float2* va
 // re-emits with that bound and does nothing when the first found none.
 template <typename K>
 static void mesh_emit_t(const Geom& g, const K* keys, const float2* vals, size_t n_cap, int with_indices,
-                        MeshScratch& ms, unsigned long long n_verts, unsigned long long n_idx, float* verts_dev,
-                        uint32_t* idx_dev, int sms, cudaStream_t st) {
+                        MeshScratch& ms, size_t vert_cap, size_t idx_cap, float* verts_dev, uint32_t* idx_dev,
+                        int sms, cudaStream_t st) {
     const unsigned long long* scan = ms.tscan;
     unsigned long long* mm = &ms.counts->missing_min;
     const int kb = sizeof(K) == 4 ? 10 : g.kb;
     if (with_indices) {
         k_mesh_emit<true, K><<<grid_for(n_cap, sms), kThreads, 0, st>>>(keys, kb, vals, ms.rows, ms.n_dev, g,
-                                                                         ms.vflags, ms.corners, scan, ms.block_sums, n_verts, n_idx,
-                                                                         ~0ull, nullptr, verts_dev, idx_dev, mm);
+                                                                         ms.vflags, ms.corners, scan, ms.block_sums, ms.counts,
+                                                                         vert_cap, idx_cap, ~0ull, nullptr, verts_dev, idx_dev, mm);
         k_mesh_emit<true, K><<<grid_for(n_cap, sms), kThreads, 0, st>>>(keys, kb, vals, ms.rows, ms.n_dev, g,
-                                                                         ms.vflags, ms.corners, scan, ms.block_sums, n_verts, n_idx, 0ull, mm,
-                                                                         verts_dev, idx_dev, nullptr);
+                                                                         ms.vflags, ms.corners, scan, ms.block_sums, ms.counts,
+                                                                         vert_cap, idx_cap, 0ull, mm, verts_dev, idx_dev, nullptr);
     } else {
         k_mesh_emit<false, K><<<grid_for(n_cap, sms), kThreads, 0, st>>>(keys, kb, vals, ms.rows, ms.n_dev, g,
-                                                                          ms.vflags, ms.corners, scan, ms.block_sums, n_verts, n_idx,
-                                                                          ~0ull, nullptr, verts_dev, idx_dev, mm);
+                                                                          ms.vflags, ms.corners, scan, ms.block_sums, ms.counts,
+                                                                          vert_cap, idx_cap, ~0ull, nullptr, verts_dev, idx_dev, mm);
     }
 }
 
 cudaError_t mesh_emit_enqueue(const Geom& g, const void* keys, int key_bytes, const float2* vals, size_t n_cap,
-                              int with_indices, MeshScratch& ms, unsigned long long n_verts,
-                              unsigned long long n_idx, float* verts_dev, uint32_t* idx_dev, int sms,
-                              cudaStream_t st) {
+                              int with_indices, MeshScratch& ms, size_t vert_cap, size_t idx_cap,
+                              float* verts_dev, uint32_t* idx_dev, int sms, cudaStream_t st) {
     if (key_bytes == 8)
-        mesh_emit_t<uint64_t>(g, (const uint64_t*)keys, vals, n_cap, with_indices, ms, n_verts, n_idx, verts_dev,
+        mesh_emit_t<uint64_t>(g, (const uint64_t*)keys, vals, n_cap, with_indices, ms, vert_cap, idx_cap, verts_dev,
                               idx_dev, sms, st);
     else
-        mesh_emit_t<uint32_t>(g, (const uint32_t*)keys, vals, n_cap, with_indices, ms, n_verts, n_idx, verts_dev,
+        mesh_emit_t<uint32_t>(g, (const uint32_t*)keys, vals, n_cap, with_indices, ms, vert_cap, idx_cap, verts_dev,
                               idx_dev, sms, st);
     return cudaGetLastError();
 }

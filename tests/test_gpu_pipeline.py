@@ -55,6 +55,10 @@ def test_pipeline_matches_components_and_oracle(gpu, oracle_cpu):
         check(lib.kifi_pipeline_mesh_counts(pipe, C.byref(nv), C.byref(ni)))
         vb, ib = ov.mesh(True)
         assert (nv.value, ni.value) == (vb.shape[0], ib.size)
+        # two meshes (frames 2 and 4); the first found no buffers and was emitted again
+        meshes, reemitted = C.c_longlong(), C.c_longlong()
+        check(lib.kifi_pipeline_mesh_stats(pipe, C.byref(meshes), C.byref(reemitted)))
+        assert meshes.value == 2 and 1 <= reemitted.value <= 2, (meshes.value, reemitted.value)
     finally:
         lib.kifi_pipeline_destroy(pipe)
 
