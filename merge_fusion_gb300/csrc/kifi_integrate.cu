@@ -63,9 +63,39 @@ __device__ __forceinline__ float load_depth(const void* depth, size_t i, bool u1
     return __ldg((const float*)depth + i);
 }
 
+// The occupancy bitmap is laid out in 4x4x4 bricks: one 64-bit word per
+// brick (bricks x-fastest, then y, then z), bit (x&3) | (y&3)<<2 | (z&3)<<4
+// within it.  A voxel's {0,1}^3 dilation then lies in one word unless it
+// crosses a brick face (1.95 words on average instead of four x-rows), and
+// a 32-byte sector covers 16 x 4 x 4 voxels of a surface instead of one row.
+__host__ __device__ constexpr int bitmap_res(int res) { return res < 4 ? 4 : res; }
+
+__device__ __forceinline__ size_t brick_word(uint32_t x, uint32_t y, uint32_t z, int res) {
+    const size_t nb = (size_t)(bitmap_res(res) >> 2);
+    return (size_t)(x >> 2) + nb * ((size_t)(y >> 2) + nb * (size_t)(z >> 2));
+}
+
+// bit position of a key in the bitmap (as 32-bit words: b >> 5, bit b & 31)
 template <typename K>
 __device__ __forceinline__ size_t bit_index(K key, const Codec<K>& cd, int res) {
-    return (size_t)cd.x(key) + (size_t)res * ((size_t)cd.y(key) + (size_t)res * cd.z(key));
+    const uint32_t x = cd.x(key), y = cd.y(key), z = cd.z(key);
+    return brick_word(x, y, z, res) * 64 + ((x & 3u) | (y & 3u) << 2 | (z & 3u) << 4);
+}
+
+// the bits of coordinates [c, c+1] of one axis inside brick `side` (0: c's
+// brick, 1: the next one when c is the brick's last coordinate), as a 4-bit set
+__device__ __forceinline__ uint32_t pair_bits(uint32_t c, int side) {
+    const uint32_t l = c & 3u;
+    if (l != 3u) return side ? 0u : 3u << l;
+    return side ? 1u : 8u;
+}
+// {0..3} bit set -> spread by `stride` (4 for y rows, 16 for z planes)
+__device__ __forceinline__ uint64_t spread(uint32_t set4, int stride) {
+    uint64_t r = 0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+        if (set4 >> i & 1u) r |= 1ull << (i * stride);
+    return r;
 }
 
 // maximum over the warp
@@ -136,44 +166,44 @@ __global__ void __launch_bounds__(kEmitThreads) k_splat_emit(DeviceCtl* __restri
         // neighbouring pixels often land in one voxel: one emitter per key
         unsigned int peers = __match_any_sync(0xffffffffu, valid ? key : ~(K)0);
         const bool emitter = valid && (lane == __ffs(peers) - 1);
-        // The dilation's 8 keys are 4 (y, z) rows of an (x, x+1) pair.  The
-        // pair's bits are adjacent in the bitmap, so one word probe covers
-        // both unless x is the last bit of its word.  All probes are issued
-        // before any decision; atomics only for bits still clear.
-        uint32_t got[4] = {0u, 0u, 0u, 0u};   // bit 0: key + dx=0 new, bit 1: dx=1 new
+        // The dilation's 8 keys lie in the brick words of the bitmap: one
+        // word, or 2, 4 or 8 where the cube crosses brick faces.  All probes
+        // are issued before any decision; atomics only for bits still clear.
+        // A thread owns the bits its atomicOr flipped.
+        uint64_t got[8];     // per word slot: the bits this thread flipped
+        uint32_t wbase[3];   // the first brick's coordinates
         if (emitter) {
-            uint32_t* wp[4];
-            uint32_t* wq[4];
-            uint32_t m0[4], m1[4], pre0[4], pre1[4];
-            const size_t kb0 = bit_index(key, cd, g.res);
-            const size_t res = (size_t)g.res;
+            const uint32_t x = cd.x(key), y = cd.y(key), z = cd.z(key);
+            wbase[0] = x >> 2; wbase[1] = y >> 2; wbase[2] = z >> 2;
+            const size_t nb = (size_t)(bitmap_res(g.res) >> 2);
+            unsigned long long* words = (unsigned long long*)bitmap;
+            const size_t w0 = brick_word(x, y, z, g.res);
+            uint64_t mask[8], pre[8];
 #pragma unroll
-            for (int o = 0; o < 4; ++o) {
-                const size_t b = kb0 + (size_t)(o & 1) * res + (size_t)(o >> 1) * res * res;
-                const uint32_t sh = (uint32_t)(b & 31);
-                wp[o] = bitmap + (b >> 5);
-                wq[o] = bitmap + ((b + 1) >> 5);
-                m0[o] = sh == 31 ? 0x80000000u : (3u << sh);
-                m1[o] = sh == 31 ? 1u : 0u;
-                pre0[o] = __ldcg(wp[o]);
-                pre1[o] = sh == 31 ? __ldcg(wq[o]) : 0u;
+            for (int o = 0; o < 8; ++o) {
+                const int i = o & 1, j = (o >> 1) & 1, k = o >> 2;
+                const uint32_t xm = pair_bits(x, i), ym = pair_bits(y, j), zm = pair_bits(z, k);
+                // xm < 16 and the spreads leave room: the products do not carry
+                mask[o] = (uint64_t)xm * spread(ym, 4) * spread(zm, 16);
+                pre[o] = mask[o] ? __ldcg(words + w0 + i + nb * (j + nb * k)) : ~0ull;
             }
 #pragma unroll
-            for (int o = 0; o < 4; ++o) {
-                const uint32_t sh = m0[o] == 0x80000000u && m1[o] ? 31u : (uint32_t)(__ffs(m0[o]) - 1);
-                uint32_t need0 = m0[o] & ~pre0[o];
-                uint32_t need1 = m1[o] & ~pre1[o];
-                uint32_t flipped0 = 0u, flipped1 = 0u;
-                if (need0) flipped0 = need0 & ~atomicOr(wp[o], need0);
-                if (need1) flipped1 = need1 & ~atomicOr(wq[o], need1);
-                // dx = 0 is bit sh of word 0; dx = 1 is bit sh+1 of word 0, or bit 0 of word 1
-                const uint32_t n0 = (flipped0 >> sh) & 1u;
-                const uint32_t n1 = m1[o] ? (flipped1 & 1u) : ((flipped0 >> (sh + 1)) & 1u);
-                got[o] = n0 | (n1 << 1);
+            for (int o = 0; o < 8; ++o) {
+                const int i = o & 1, j = (o >> 1) & 1, k = o >> 2;
+                const uint64_t need = mask[o] & ~pre[o];
+                got[o] = need ? need & ~(uint64_t)atomicOr(words + w0 + i + nb * (j + nb * k),
+                                                           (unsigned long long)need)
+                              : 0ull;
             }
+        } else {
+#pragma unroll
+            for (int o = 0; o < 8; ++o) got[o] = 0ull;
+            wbase[0] = wbase[1] = wbase[2] = 0u;
         }
         // warp-aggregated append: one atomic per warp
-        const unsigned int cnt = __popc(got[0] | (got[1] << 2) | (got[2] << 4) | (got[3] << 6));
+        unsigned int cnt = 0;
+#pragma unroll
+        for (int o = 0; o < 8; ++o) cnt += __popcll(got[o]);
         unsigned int incl = cnt;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
@@ -187,12 +217,14 @@ __global__ void __launch_bounds__(kEmitThreads) k_splat_emit(DeviceCtl* __restri
             base = __shfl_sync(0xffffffffu, base, 31);
             unsigned int at = base + incl - cnt;
 #pragma unroll
-            for (int o = 0; o < 4; ++o) {
-                const K k0 = key + cd.pack(0, o & 1, o >> 1);
-#pragma unroll
-                for (int dx = 0; dx < 2; ++dx) {
-                    if (!((got[o] >> dx) & 1u)) continue;
-                    if (at < new_cap) new_keys[at] = k0 + (K)dx;
+            for (int o = 0; o < 8; ++o) {
+                uint64_t m = got[o];
+                const uint32_t bx = (wbase[0] + (o & 1)) << 2, by = (wbase[1] + ((o >> 1) & 1)) << 2,
+                               bz = (wbase[2] + (o >> 2)) << 2;
+                while (m) {
+                    const uint32_t b = (uint32_t)__ffsll((long long)m) - 1u;
+                    m &= m - 1ull;
+                    if (at < new_cap) new_keys[at] = cd.pack(bx + (b & 3u), by + ((b >> 2) & 3u), bz + (b >> 4));
                     else atomicOr(&ctl->status, KIFI_DEV_ERR_CAPACITY);
                     ++at;
                 }
@@ -347,12 +379,15 @@ __global__ void __launch_bounds__(256) k_merge_partition(DeviceCtl* __restrict__
     // would force the array into local memory
     const K* __restrict__ A = (const K*)(cur ? vb.keys[1] : vb.keys[0]);
     const K* __restrict__ B = in.b_keys;
+    // a sort that gave up on a bounded wait leaves its keys unordered: the
+    // volume stays as it was (the host rebuilds the occupancy bits)
+    const bool timed_out = (ctl->status & KIFI_DEV_ERR_TIMEOUT) != 0u;
     if (threadIdx.x == 0) {
         unsigned long long e = *in.b_count;
         const K excluded = (K)ctl->excluded_key;
-        const bool drop = e > 0 && excluded != 0 && B[e - 1] == excluded;
+        const bool drop = !timed_out && e > 0 && excluded != 0 && B[e - 1] == excluded;
         if (drop) --e;
-        const bool ok = N0 + e <= vb.cap;
+        const bool ok = !timed_out && N0 + e <= vb.cap;
         s_e = e;
         s_n1 = N0 + e;
         s_ok = ok;
@@ -364,12 +399,13 @@ __global__ void __launch_bounds__(256) k_merge_partition(DeviceCtl* __restrict__
                 size_t b = bit_index(excluded, cd, g.res);
                 atomicAnd(vb.bitmap + (b >> 5), ~(1u << (b & 31)));
             }
-            if (!ok) atomicOr(&ctl->status, KIFI_DEV_ERR_CAPACITY);
+            if (!ok && !timed_out) atomicOr(&ctl->status, KIFI_DEV_ERR_CAPACITY);
         }
     }
     __syncthreads();
     const unsigned long long e = s_e, N1 = s_n1;
     if (!s_ok) {
+        if (timed_out) return;
         // no room: leave the volume as it was and take the new keys back out
         // of the occupancy bitmap; the host grows the buffers and retries.
         for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < e;
@@ -498,7 +534,98 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_update(DeviceCtl* __res
             }
             continue;
         }
-        // mixed tile: stage both ranges in shared memory and merge there
+        if (nb <= kMergeThreads && (int)(a0 & 3ull) + na <= kTile) {
+            // Few new keys (the common mixed tile: a median of 16-25 per
+            // 2048 outputs).  Each thread keeps its resident entries in
+            // registers (aligned 128-bit loads from a0 rounded down to 4) and
+            // places each at its A index plus the number of new keys below
+            // it, found in the tile's staged new keys; a new key goes to its
+            // B index plus the number of resident keys below it.  Resident
+            // keys are staged too, for that second search.
+            const unsigned long long ka = a0 & ~3ull;
+            const int koff = (int)(a0 - ka);
+            const unsigned long long b0 = d0 - a0;
+            if ((int)threadIdx.x < nb) sB_k[threadIdx.x] = B[b0 + threadIdx.x];
+            K kk[2][4];
+            float2 vv[2][4];
+            int li0[2];
+#pragma unroll
+            for (int r = 0; r < 2; ++r) {
+                const int ls = (int)threadIdx.x * 4 + r * kMergeThreads * 4;
+                li0[r] = ls - koff;
+                if (ka + (unsigned long long)ls < a1) {  // reads at most 3 entries past a1 (array padding)
+                    ld4(A + ka + ls, kk[r]);
+                    const float4 x0 = __ldcs((const float4*)(Av + ka + ls));
+                    const float4 x1 = __ldcs((const float4*)(Av + ka + ls + 2));
+                    vv[r][0] = make_float2(x0.x, x0.y); vv[r][1] = make_float2(x0.z, x0.w);
+                    vv[r][2] = make_float2(x1.x, x1.y); vv[r][3] = make_float2(x1.z, x1.w);
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        kk[r][q] = (K)0;
+                        vv[r][q] = make_float2(0.0f, 0.0f);
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int li = li0[r] + q;
+                    if (li >= 0 && li < na) sA_k[li] = kk[r][q];
+                }
+            }
+            __syncthreads();
+#pragma unroll
+            for (int r = 0; r < 2; ++r) {
+                unsigned long long pos[4];
+                int rank = -1;  // new keys below the current resident key
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int li = li0[r] + q;
+                    pos[q] = ~0ull;  // not this tile's: never updated or stored
+                    if (li >= 0 && li < na) {
+                        const K a = kk[r][q];
+                        if (rank < 0) {
+                            int lo = 0, hi = nb;
+                            while (lo < hi) {
+                                const int mid = (lo + hi) >> 1;
+                                if (sB_k[mid] < a) lo = mid + 1;
+                                else hi = mid;
+                            }
+                            rank = lo;
+                        } else {
+                            while (rank < nb && sB_k[rank] < a) ++rank;
+                        }
+                        pos[q] = d0 + (unsigned long long)(li + rank);
+                    }
+                }
+                update4<kU16, K>(kk[r], vv[r], pos, upd_end, fc, w2c, g, depth);
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    if (pos[q] != ~0ull) {
+                        __stcs(outK + pos[q], kk[r][q]);
+                        __stcs(outV + pos[q], vv[r][q]);
+                    }
+            }
+            if ((int)threadIdx.x < nb) {
+                const int j = (int)threadIdx.x;
+                K key[4] = {sB_k[j], (K)0, (K)0, (K)0};
+                float2 val[4] = {make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f),
+                                 make_float2(0.0f, 0.0f)};
+                if (in.b_vals) val[0] = in.b_vals[in.b_index ? in.b_index[b0 + j] : b0 + j];
+                int lo = 0, hi = na;
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (sA_k[mid] < key[0]) lo = mid + 1;
+                    else hi = mid;
+                }
+                const unsigned long long pos[4] = {d0 + (unsigned long long)(j + lo), ~0ull, ~0ull, ~0ull};
+                update4<kU16, K>(key, val, pos, upd_end, fc, w2c, g, depth);
+                __stcs(outK + pos[0], key[0]);
+                __stcs(outV + pos[0], val[0]);
+            }
+            __syncthreads();
+            continue;
+        }
+        // mixed tile with many new keys: stage both ranges in shared memory and merge there
         const unsigned long long b0 = d0 - a0;
         const unsigned long long ka = a0 & ~3ull;
         const int koff = (int)(a0 - ka);
@@ -618,6 +745,20 @@ __global__ void k_insert_filter(DeviceCtl* ctl, Geom g, uint32_t* bitmap, const 
     }
 }
 
+// the occupancy bits of the resident keys (after the bitmap was cleared)
+template <typename K>
+__global__ void k_bitmap_from_keys(const DeviceCtl* __restrict__ ctl, Geom g, VolumeBuffers vb) {
+    const Codec<K> cd(g.kb);
+    const unsigned int cur = ctl->cur;
+    const unsigned long long n = ctl->n[cur];
+    const K* __restrict__ keys = (const K*)(cur ? vb.keys[1] : vb.keys[0]);
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        const size_t b = bit_index(keys[i], cd, g.res);
+        atomicOr(vb.bitmap + (b >> 5), 1u << (b & 31));
+    }
+}
+
 __global__ void k_reset_new(DeviceCtl* ctl) {
     ctl->n_new = 0u;
     ctl->excluded_key = 0ull;
@@ -694,6 +835,15 @@ cudaError_t integrate_enqueue(DeviceCtl* ctl, const Geom& g, VolumeBuffers& vb, 
         return integrate_enqueue_t<uint64_t>(ctl, g, vb, ss, depth_dev, depth_u16, cam, world_to_eye, ls, st,
                                              events);
     return integrate_enqueue_t<uint32_t>(ctl, g, vb, ss, depth_dev, depth_u16, cam, world_to_eye, ls, st, events);
+}
+
+cudaError_t bitmap_rebuild_enqueue(const DeviceCtl* ctl, const Geom& g, const VolumeBuffers& vb,
+                                   const LaunchShape& ls, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(vb.bitmap, 0, vb.bitmap_words * 4, st);
+    if (e) return e;
+    if (vb.key_bytes == 8) k_bitmap_from_keys<uint64_t><<<ls.sms * 8, 256, 0, st>>>(ctl, g, vb);
+    else k_bitmap_from_keys<uint32_t><<<ls.sms * 8, 256, 0, st>>>(ctl, g, vb);
+    return cudaGetLastError();
 }
 
 cudaError_t insert_filter_enqueue(DeviceCtl* ctl, const Geom& g, VolumeBuffers& vb, const void* keys_dev,

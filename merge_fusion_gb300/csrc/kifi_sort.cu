@@ -23,10 +23,13 @@
 // The look-back words pack {generation:32 | status:2 | count:30}, so the
 // count and its flag are one atomic 64-bit store and stale words of an
 // earlier sort are ignored without clearing.  Every wait on a predecessor is
-// bounded: after kSpinLimit polls the kernel raises KIFI_DEV_ERR_TIMEOUT in
-// the volume's status word and carries on with what it has, so a broken
+// bounded: after kSpinLimit polls (or the limit a test sets) the kernel
+// raises KIFI_DEV_ERR_TIMEOUT in the caller's status word and carries on with
+// what it has -- every store stays inside the output buffers -- so a broken
 // invariant can never hang the GPU.
-#include "kifi_internal.h"
+#include <atomic>
+
+#include "kifi_api_util.h"
 
 namespace kifi {
 namespace {
@@ -37,6 +40,7 @@ constexpr int kKeysPerThread = 8;
 constexpr int kTile = kThreads * kKeysPerThread;  // 2048
 constexpr int kRadix = 256;
 constexpr unsigned long long kSpinLimit = 1ull << 22;
+constexpr int kLookAhead = 8;  // predecessor look-back words fetched per round
 
 constexpr unsigned long long kFlagAggregate = 1ull << 30;
 constexpr unsigned long long kFlagInclusive = 2ull << 30;
@@ -44,7 +48,7 @@ constexpr unsigned long long kCountMask = (1ull << 30) - 1;
 
 __global__ void k_sort_prepare(SortScratch s, int passes) {
     for (int i = threadIdx.x; i < passes * kRadix; i += blockDim.x) s.hist[i] = 0u;
-    if (threadIdx.x < passes) s.tile_counter[threadIdx.x] = 0u;
+    if (threadIdx.x < passes) s.tile_counter[threadIdx.x] = s.first_tile;
     if (threadIdx.x == 0) *s.epoch += 1ull;
 }
 
@@ -167,21 +171,39 @@ __global__ void __launch_bounds__(kThreads) k_sort_pass(const K* __restrict__ ke
             digit_base[d] = pass_offset[d];
         } else {
             st_volatile_u64(my, gen | kFlagAggregate | tile_count);
+            // Walk back kLookAhead predecessor words per round: the loads of a
+            // round are independent, so a chain of aggregate-only tiles costs
+            // one memory latency per kLookAhead tiles, not one per tile.
             unsigned int excl = 0;
             int t = (int)tile - 1;
             unsigned long long spins = 0;
             while (t >= 0) {
-                unsigned long long w = ld_volatile_u64(lb + (size_t)t * kRadix + d);
-                if ((w & 0xffffffff00000000ull) != gen || (w & (3ull << 30)) == 0) {
-                    if (++spins > kSpinLimit) {
-                        atomicOr(s.status, KIFI_DEV_ERR_TIMEOUT);
-                        break;
+                unsigned long long w[kLookAhead];
+#pragma unroll
+                for (int q = 0; q < kLookAhead; ++q)
+                    w[q] = t - q >= 0 ? ld_volatile_u64(lb + (size_t)(t - q) * kRadix + d) : 0ull;
+                // consume the round's words in order, up to the first inclusive one
+                // or the first one not yet published
+                int used = 0;
+                bool done = false, stalled = false;
+#pragma unroll
+                for (int q = 0; q < kLookAhead; ++q) {
+                    if (done || stalled || t - q < 0) continue;
+                    const unsigned long long x = w[q];
+                    if ((x & 0xffffffff00000000ull) != gen || (x & (3ull << 30)) == 0) {
+                        stalled = true;
+                        continue;
                     }
-                    continue;
+                    excl += (unsigned int)(x & kCountMask);
+                    ++used;
+                    done = (x & kFlagInclusive) != 0;
                 }
-                excl += (unsigned int)(w & kCountMask);
-                if (w & kFlagInclusive) break;
-                --t;
+                t -= used;
+                if (done) break;
+                if (stalled && ++spins > s.spin_limit) {
+                    atomicOr(s.status, KIFI_DEV_ERR_TIMEOUT);
+                    break;
+                }
             }
             st_volatile_u64(my, gen | kFlagInclusive | ((excl + tile_count) & kCountMask));
             digit_base[d] = pass_offset[d] + excl;
@@ -200,6 +222,10 @@ __global__ void __launch_bounds__(kThreads) k_sort_pass(const K* __restrict__ ke
         }
     }
 }
+
+// process-wide look-back limits (kifi_sort_set_fault_injection)
+std::atomic<unsigned long long> g_spin_limit{kSpinLimit};
+std::atomic<unsigned int> g_first_tile{0u};
 
 }  // namespace
 
@@ -236,6 +262,8 @@ template <typename K>
 static cudaError_t sort_t(K* keys, int passes, uint32_t* vals, const unsigned int* n_dev, SortScratch& s,
                           unsigned int* status, int grid_ctas, cudaStream_t st) {
     s.status = status;
+    s.spin_limit = g_spin_limit.load();
+    s.first_tile = g_first_tile.load();
     k_sort_prepare<<<1, 256, 0, st>>>(s, passes);
     k_sort_histogram<K><<<grid_ctas, kThreads, 0, st>>>(keys, n_dev, s, passes);
     K *ki = keys, *ko = (K*)s.alt_keys;
@@ -275,3 +303,9 @@ cudaError_t sort_keys(void* keys, int key_bytes, int key_bits, uint32_t* vals, c
 }
 
 }  // namespace kifi
+
+extern "C" kifi_status kifi_sort_set_fault_injection(unsigned int skip_tiles, unsigned long long spin_limit) {
+    kifi::g_first_tile.store(skip_tiles);
+    kifi::g_spin_limit.store(spin_limit ? spin_limit : kifi::kSpinLimit);
+    return KIFI_OK;
+}
