@@ -1,31 +1,37 @@
 """Benchmark: fused frames/s at 640x480 and 4 mm voxels (the kifi fusion
 path of denniskb/merge_fusion on one GB300).
 
-Workload (one step = one frame): a seeded synthetic room (4 x 3 x 4 m, 40 boxes,
-20 spheres) ray-cast to 640x480 uint16 millimetre depth (f = 585, 2% dropout,
-depth noise 0.0012 + 0.0019 (z-0.4)^2 m) along a smooth trajectory; volume
-res 1024 x 4 mm (4.096 m cube), truncation 2 cm.  Every frame is fused with
-its given pose (splat + sort + merge/TSDF update) and tracked by 15 ICP
+Workload: a seeded synthetic room (4 x 3 x 4 m, 40 boxes, 20 spheres)
+ray-cast to 640x480 uint16 millimetre depth (f = 585, 2% dropout, depth
+noise 0.0012 + 0.0019 (z-0.4)^2 m) along a smooth trajectory; volume res
+1024 x 4 mm (4.096 m cube), truncation 2 cm.  Every frame is fused with its
+given pose (splat + sort + merge/TSDF update) and tracked by 15 ICP
 iterations against the previous frame; the mesh (vertices + indices) is
-extracted every 10 frames.  Before the warm-up, `--prefill` frames build
-the resident volume so that the timed frames run at a realistic size.
+extracted every 10 frames.  One step is one mesh period: ten frames and the
+mesh that ends it.  Before the warm-up, `--prefill` frames build the
+resident volume so that the timed frames run at a realistic size.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
-Prints one JSON line.  `value` times K frames with the frames already in
-device memory; `e2e` times K further frames through the public C ABI
-(kifi_pipeline_integrate) from pinned host memory, each call uploading its
-frame and reading its tracked pose back.  `--impl reference` times the
-reference's own CPU code (oracle/_ref, else the C restatement in oracle/)
-on the same workload on the host cores.
+Prints one JSON line.  `value` times K steps with the frames already in
+device memory: CUDA events on the volume stream, with the tracking and
+meshing streams joined before the end event.  `e2e` times K further steps
+through the public C ABI (kifi_pipeline_integrate) from pinned host memory,
+each call uploading its frame and reading its tracked pose back, ending
+with kifi_pipeline_sync (fusion, tracking and meshing done).
+`--impl reference` times the reference's own CPU code (oracle/_ref, else the
+C restatement in oracle/) on a bounded sample of the same workload.
 """
 import argparse
 import atexit
 import ctypes as C
+import datetime
 import json
 import os
+import platform
 import subprocess
 import sys
+import tempfile
 import threading
 import time
 
@@ -39,16 +45,29 @@ UNIT = "frames/s"
 W, H, F_PX = 640, 480, 585.0
 RES, SIDE, TRUNC = 1024, 4.096, 0.02
 ICP_ITERS, MESH_EVERY = 15, 10
+FRAMES_PER_STEP = MESH_EVERY  # a step is one mesh period
 SEED = 0
 CAM = (W, H, F_PX, F_PX, W / 2.0, H / 2.0, 0.4, 4.0)
+WORKLOAD = ("room 4x3x4 m, 40 boxes + 20 spheres, 640x480 uint16 depth, res 1024 x 4 mm, trunc 2 cm, "
+            "ICP 15 it/frame, mesh every 10")
+# kernels launched per frame: frame set-up, splat+emit, the sort (prepare,
+# histogram, 4 digit passes), merge partition, merge+update; tracking: ICP
+# begin, one step per iteration, the next target's back-projection; per mesh:
+# snapshot, row directory, classification, two scan kernels, two emission passes
+LAUNCHES_FUSION, LAUNCHES_TRACKING, LAUNCHES_MESH = 10, ICP_ITERS + 2, 7
+# bytes the host reads back per tracked frame: the head of the ICP state
+# (float and float-float pose, counters, 64 iteration records of 20 bytes)
+ICP_HEAD_BYTES = 192 + 64 * 20
+MESH_COUNTS_BYTES = 32
+FP32_LANES_PER_SM = 128  # FP32 FMA lanes of a Blackwell SM: 2 flop per lane per clock
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=95)
-    ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--prefill", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=20, help="timed steps (one mesh period of 10 frames each)")
+    ap.add_argument("--warmup", type=int, default=5, help="untimed steps before the timed ones")
+    ap.add_argument("--prefill", type=int, default=100, help="frames fused before the warm-up")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0,
                     help="bounded CPU-baseline sample (seconds of CPU work)")
@@ -57,6 +76,8 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
     ap.add_argument("--graphs", action="store_true",
                     help="one CUDA graph per frame (kifi_pipeline_set_graphs) instead of plain launches")
+    ap.add_argument("--capacity-mvox", type=int, default=48,
+                    help="volume capacity preset, millions of voxels (small cases for profiling use less)")
     return ap.parse_args()
 
 
@@ -78,10 +99,10 @@ def max_over_ranks(x, world, device="cuda"):
     return float(t.item())
 
 
-def job_throughput(world, steps, seconds):
-    """Whole-job frames/s: every rank fuses `steps` frames of its own scene,
+def job_throughput(world, frames, seconds):
+    """Whole-job frames/s: every rank fuses `frames` frames of its own scene,
     timed by the slowest rank."""
-    return world * steps / seconds
+    return world * frames / seconds
 
 
 def rank_seed(rank):
@@ -89,35 +110,80 @@ def rank_seed(rank):
     return SEED + rank
 
 
-def measured_peak():
+def workload_config(prefill, frames_per_step):
+    return {"workload": WORKLOAD, "prefill_frames": prefill, "frames_per_step": frames_per_step,
+            "l2": "volume (>240 MB) larger than L2; every frame is a new depth image"}
+
+
+def measured_peaks():
+    """(HBM GB/s, SM max MHz, source) from MEASURED_PEAKS.json, else the fallback."""
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
         with open(p) as f:
-            return float(json.load(f)["hbm_gbs"]), "measured"
-    return 6800.0, "fallback"
+            d = json.load(f)
+        return float(d["hbm_gbs"]), float(d.get("sm_max_mhz", 2070.0)), "measured"
+    return 6800.0, 2070.0, "fallback"
 
 
-def ncu_traffic_per_voxel():
-    """DRAM bytes per (N0 + N1) voxel of the merge+update kernel from the
-    committed ncu summary, or None."""
-    p = os.path.join(ROOT, "profiles", "merge_update_traffic.json")
+def ncu_traffic(name):
+    """DRAM bytes per unit of a kernel from a committed ncu summary, or None."""
+    p = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(p):
         return None
     with open(p) as f:
         return json.load(f)
 
 
-class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during a timed region."""
+def host_cpu():
+    """CPU model and logical core count of this host."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.startswith("Model name:"):
+                model = ln.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if not model:
+        try:
+            with open("/proc/cpuinfo") as f:
+                for ln in f:
+                    if ln.lower().startswith("model name"):
+                        model = ln.split(":", 1)[1].strip()
+                        break
+        except OSError:
+            pass
+    try:
+        usable = len(os.sched_getaffinity(0))  # the cores this process may run on
+    except (AttributeError, OSError):
+        usable = os.cpu_count()
+    return {"cpu_model": model or platform.processor() or platform.machine(), "nproc": usable,
+            "cpu_count": os.cpu_count(), "machine": platform.machine()}
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+
+def _smi_time(stamp):
+    """nvidia-smi's sample timestamp ("YYYY/MM/DD HH:MM:SS.mmm", local time)
+    as seconds since the epoch, or None."""
+    try:
+        return datetime.datetime.strptime(stamp.strip(), "%Y/%m/%d %H:%M:%S.%f").timestamp()
+    except ValueError:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during a timed region.
+    Samples are placed by nvidia-smi's own timestamp, not by when their line
+    reached this process (output may arrive in batches)."""
+
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, gpu_index):
         self.gpu = gpu_index
         self.proc = None
-        self.lines = []  # (host time, csv line)
+        self.lines = []  # (sample time, csv line without the timestamp)
         self.windows = []
 
     def __enter__(self):
@@ -129,10 +195,9 @@ class ClockSampler:
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
             atexit.register(self.__exit__, None, None, None)  # also when a timed region raises
-            # the timed regions are tens of milliseconds: start them only
-            # once nvidia-smi is producing samples
-            t_end = time.perf_counter() + 5.0
-            while not self.lines and time.perf_counter() < t_end and self.proc.poll() is None:
+            # start the timed regions only once nvidia-smi is producing samples
+            t_end = time.time() + 5.0
+            while not self.lines and time.time() < t_end and self.proc.poll() is None:
                 time.sleep(0.005)
         except OSError:
             self.proc = None
@@ -140,18 +205,23 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append((time.perf_counter(), line.strip()))
+            self.add(line, time.time())
+
+    def add(self, line, arrival):
+        stamp, _, rest = line.strip().partition(",")
+        t = _smi_time(stamp)
+        self.lines.append((arrival if t is None else t, rest.strip()))
 
     def window(self):
-        """Context manager marking one timed region on the host clock."""
+        """Context manager marking one timed region on the host's wall clock."""
         sampler = self
 
         class _W:
             def __enter__(self):
-                self.t0 = time.perf_counter()
+                self.t0 = time.time()
 
             def __exit__(self, *a):
-                sampler.windows.append((self.t0, time.perf_counter()))
+                sampler.windows.append((self.t0, time.time()))
         return _W()
 
     def __exit__(self, *a):
@@ -197,41 +267,41 @@ class ClockSampler:
 
 # ------------------------------------------------------------- CPU baseline
 
-def cpu_baseline(frames_u16, poses, start, n_max, seconds, resident=None):
-    """The reference's CPU path (oracle/_ref, else the oracle port) on the
-    same frames: integrate + 15 ICP iterations against the previous frame,
-    plus one mesh per 10 frames.  Runs until `seconds` of work or n_max
-    frames.  Returns (frames/s, kind, frames timed, mesh seconds)."""
-    from oracle import build_ref
-    kind = "reference"
+def _cpu_impl(resident):
+    """The reference's CPU code (oracle/_ref) with a volume holding `resident`,
+    else the oracle's C restatement.  Returns (kind, integrate, icp, mesh)."""
+    from oracle import build_ref, cpu
     try:
         from oracle import ref as impl
         if not impl.available():
             build_ref.build()
         if not impl.available():
             raise OSError("reference CPU build unavailable")
-    except Exception:
-        kind = "port"
-        impl = None
-    from oracle import cpu
-    if impl is not None:
         vol = impl.Volume(RES, SIDE, TRUNC)
         if resident is not None and resident[0].size:
             vol.insert(resident[0], resident[1])
-        icp = lambda d, g, t, tp: impl.icp_align(d, CAM, g, t, tp, ICP_ITERS)  # noqa: E731
-        mesh = lambda: vol.mesh(True)  # noqa: E731
-        integ = lambda d, m: vol.integrate(d, CAM, m)  # noqa: E731
-    else:
+        kind = "reference"
+        icp = impl.icp_align
+    except Exception:
         vol = cpu.Volume(RES, SIDE, TRUNC)
         if resident is not None:
             vol.keys, vol.values = resident[0].copy(), resident[1].copy()
-        icp = lambda d, g, t, tp: cpu.icp_align(d, CAM, g, t, tp, ICP_ITERS)  # noqa: E731
-        mesh = lambda: vol.mesh(True)  # noqa: E731
-        integ = lambda d, m: vol.integrate(d, CAM, m)  # noqa: E731
+        kind = "port"
+        icp = cpu.icp_align
+    return (kind, lambda d, m: vol.integrate(d, CAM, m),
+            lambda d, g, t, tp: icp(d, CAM, g, t, tp, ICP_ITERS), lambda: vol.mesh(True))
+
+
+def cpu_frames(frames_u16, poses, start, n_max, seconds, resident, with_mesh=True):
+    """The reference's CPU path on the same frames: integrate + 15 ICP
+    iterations against the previous frame, plus one mesh per 10 frames.
+    Runs until `seconds` of work or n_max frames.  Returns (frames/s, kind,
+    frames timed, mesh seconds)."""
+    from oracle import cpu
     from merge_fusion_gb300.scenes import kifi_matrix
+    kind, integ, icp, mesh = _cpu_impl(resident)
     t_total, n = 0.0, 0
     target = None
-    t_mesh = None
     while n < n_max and t_total < seconds:
         i = start + n
         depth = frames_u16[i].astype(np.float32) * np.float32(0.001)  # DepthStream conversion
@@ -246,14 +316,51 @@ def cpu_baseline(frames_u16, poses, start, n_max, seconds, resident=None):
         target = cpu.backproject(depth, CAM, kifi_matrix(poses[i]))
         t_total += time.perf_counter() - t0
         n += 1
-    t0 = time.perf_counter()
-    mesh()
-    t_mesh = time.perf_counter() - t0
+    t_mesh = 0.0
+    if with_mesh:
+        t0 = time.perf_counter()
+        mesh()
+        t_mesh = time.perf_counter() - t0
     per_frame = t_total / max(n, 1) + t_mesh / MESH_EVERY
     return 1.0 / per_frame, kind, n, t_mesh
 
 
+def _cpu_worker(path, seconds):
+    """One process of the multi-core aggregate: the same bounded sample from
+    the same resident volume (inputs in the npz file at `path`)."""
+    d = np.load(path)
+    poses = list(d["poses"])
+    fps, kind, n, tm = cpu_frames(d["frames"], poses, 1, d["frames"].shape[0] - 1, seconds,
+                                  (d["keys"], d["values"]))
+    return fps, kind, n, tm
+
+
+def cpu_aggregate(frames_u16, poses, start, n_max, seconds, resident, procs):
+    """One scene per core: `procs` processes each run the single-core sample
+    at once; the aggregate is the sum of their frames/s."""
+    import multiprocessing as mp
+    fd, path = tempfile.mkstemp(suffix=".npz", prefix="kifi_cpu_")
+    os.close(fd)
+    try:
+        np.savez(path, frames=frames_u16[start - 1:start + n_max], poses=np.asarray(poses[start - 1:start + n_max]),
+                 keys=resident[0], values=resident[1])
+        with mp.get_context("spawn").Pool(procs) as pool:
+            res = pool.starmap(_cpu_worker, [(path, seconds)] * procs)
+    finally:
+        os.unlink(path)
+    return sum(r[0] for r in res), res
+
+
 # ------------------------------------------------------------------ GPU arm
+
+def roofline_entry(bound, achieved, peak, unit, per_launch, ms, peak_source, extra=None):
+    e = {"bound": bound, "achieved": achieved, "peak": peak, "unit": unit, "frac": achieved / peak,
+         "ms_per_launch": ms, "peak_source": peak_source}
+    e.update(per_launch)
+    if extra:
+        e.update(extra)
+    return e
+
 
 def run_gpu(args, rank, world, local):
     import torch
@@ -264,30 +371,35 @@ def run_gpu(args, rank, world, local):
     if world > 1:
         dist.init_process_group("nccl")
     lib = _lib.load()
-    K, Wu, Fp = args.steps, args.warmup, args.prefill
-    n_frames = Fp + Wu + 2 * K + 1
+    K, Wu, Fp, FS = args.steps, args.warmup, args.prefill, FRAMES_PER_STEP
+    KF = K * FS
+    n_frames = Fp + (Wu + 2 * K) * FS + 1
     # independent scene per rank (replicas; weak scaling)
     seed = rank_seed(rank)
     frames, poses = scenes.render_room_torch(n_frames, seed=seed, device="cuda")
     torch.cuda.synchronize()
     frames_host = frames.cpu().numpy().view(np.uint16)
-    pinned = torch.empty((2 * K + 1, H, W), dtype=torch.int16).pin_memory()
-    pinned.copy_(frames[Fp + Wu:Fp + Wu + 2 * K + 1].cpu())
+    t0 = Fp + Wu * FS
+    pinned = torch.empty((KF, H, W), dtype=torch.int16).pin_memory()
+    pinned.copy_(frames[t0 + KF:t0 + 2 * KF].cpu())
     w2e = [scenes.kifi_matrix(np.linalg.inv(p)) for p in poses]
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
 
     cam = Camera(W, H, F_PX, F_PX, W / 2.0, H / 2.0, 0.4, 4.0)
     d = PipelineDesc()
     d.camera = cam
     d.resolution, d.side_length_m, d.truncation_m = RES, SIDE, TRUNC
     d.icp_iterations, d.mesh_every, d.mesh_with_indices = ICP_ITERS, MESH_EVERY, 1
-    d.initial_capacity = 48 << 20
+    d.initial_capacity = args.capacity_mvox << 20
     d.device = local
     pipe = C.c_void_p()
     check(lib.kifi_pipeline_create(C.byref(d), C.byref(pipe)), "pipeline")
     check(lib.kifi_pipeline_set_graphs(pipe, 1 if args.graphs else 0))
     vol = lib.kifi_pipeline_volume(pipe)
-    vs = torch.cuda.ExternalStream(lib.kifi_volume_stream(vol))
-    ist = torch.cuda.ExternalStream(lib.kifi_icp_stream(lib.kifi_pipeline_icp(pipe)))
+    icp = lib.kifi_pipeline_icp(pipe)
+    vs_handle = lib.kifi_volume_stream(vol)
+    vs = torch.cuda.ExternalStream(vs_handle)
+    ist = torch.cuda.ExternalStream(lib.kifi_icp_stream(icp))
 
     def ptr(a):
         return a.ctypes.data_as(C.c_void_p)
@@ -296,19 +408,29 @@ def run_gpu(args, rank, world, local):
         check(lib.kifi_pipeline_integrate_device(pipe, C.c_void_p(frames[i].data_ptr()), 1,
                                                  ptr(w2e[i])), "frame %d" % i)
 
-    for i in range(Fp + Wu):
+    def mesh_stats():
+        m, r = C.c_longlong(), C.c_longlong()
+        check(lib.kifi_pipeline_mesh_stats(pipe, C.byref(m), C.byref(r)))
+        return m.value, r.value
+
+    def mesh_counts():
+        nv, ni = C.c_size_t(), C.c_size_t()
+        check(lib.kifi_pipeline_mesh_counts(pipe, C.byref(nv), C.byref(ni)))
+        return nv.value, ni.value
+
+    for i in range(t0):  # prefill, then the warm-up steps
         step_device(i)
     check(lib.kifi_pipeline_sync(pipe, None))
     # launch shape of the fusion kernels, measured on the next frame (the volume is left unchanged)
     tuned = np.zeros(3, np.int32)
     if not args.no_autotune:
-        check(lib.kifi_volume_autotune(vol, C.c_void_p(frames[Fp + Wu].data_ptr()), 1, C.byref(cam),
-                                       ptr(w2e[Fp + Wu]), 1, ptr(tuned)), "autotune")
+        check(lib.kifi_volume_autotune(vol, C.c_void_p(frames[t0].data_ptr()), 1, C.byref(cam),
+                                       ptr(w2e[t0]), 1, ptr(tuned)), "autotune")
     n_resident = C.c_size_t()
     check(lib.kifi_volume_size(vol, C.byref(n_resident)))
     n_start = int(n_resident.value)  # resident voxels when the timed frames begin
 
-    # bounded CPU baseline starts from the same resident volume
+    # the CPU baseline starts from the same resident volume
     resident = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         nvox = n_resident.value
@@ -320,10 +442,13 @@ def run_gpu(args, rank, world, local):
 
     # ---- device-resident timed region
     check(lib.kifi_volume_set_profiling(vol, 1))
-    t0 = Fp + Wu
     ms_stage = np.zeros(4)
+    pipe_ms = np.zeros(2)
+    pipe_n = np.zeros(2, np.int32)
     nst = C.c_int()
     check(lib.kifi_volume_stage_times(vol, ptr(ms_stage), C.byref(nst)))  # reset
+    check(lib.kifi_pipeline_stage_times(pipe, ptr(pipe_ms), ptr(pipe_n)))  # reset
+    meshes0, reemit0 = mesh_stats()
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
@@ -333,23 +458,27 @@ def run_gpu(args, rank, world, local):
     with clocks.window():
         start.record(vs)
         ist.wait_event(start)
-        for i in range(t0, t0 + K):
+        for i in range(t0, t0 + KF):
             step_device(i)
-        fin = torch.cuda.Event()
-        fin.record(ist)
-        vs.wait_event(fin)
+        # the end event follows every stream of the pipeline: fusion, tracking, meshing
+        check(lib.kifi_pipeline_join(pipe, C.c_void_p(vs_handle)))
         end.record(vs)
         end.synchronize()
     ms = start.elapsed_time(end)
+    region_mesh = mesh_counts()  # the last mesh of the region, complete at the end event
     check(lib.kifi_volume_stage_times(vol, ptr(ms_stage), C.byref(nst)))
+    check(lib.kifi_pipeline_stage_times(pipe, ptr(pipe_ms), ptr(pipe_n)))
     check(lib.kifi_volume_set_profiling(vol, 0))
+    check(lib.kifi_pipeline_sync(pipe, None))
+    synced_mesh = mesh_counts()
+    meshes1, reemit1 = mesh_stats()
     n0 = np.zeros(64, np.uint64)
     ne = np.zeros(64, np.uint64)
     n1 = np.zeros(64, np.uint64)
     cnt = C.c_int()
     check(lib.kifi_volume_frame_log(vol, ptr(n0), ptr(ne), ptr(n1), 64, C.byref(cnt)))
-    m = min(cnt.value, K)
-    n0, ne, n1 = n0[cnt.value - m:cnt.value], ne[cnt.value - m:cnt.value], n1[cnt.value - m:cnt.value]
+    m = min(cnt.value, KF)
+    n0, ne, n1 = (a[cnt.value - m:cnt.value].astype(np.float64) for a in (n0, ne, n1))
     ms = max_over_ranks(ms, world)
 
     # ---- end to end through the public ABI from pinned host memory
@@ -359,18 +488,18 @@ def run_gpu(args, rank, world, local):
     torch.cuda.synchronize()
     with clocks.window():
         te0 = time.perf_counter()
-        for j in range(K):
-            i = t0 + K + j
-            check(lib.kifi_pipeline_integrate(pipe, C.c_void_p(pinned[K + j].data_ptr()), 1,
+        for j in range(KF):
+            i = t0 + KF + j
+            check(lib.kifi_pipeline_integrate(pipe, C.c_void_p(pinned[j].data_ptr()), 1,
                                               ptr(w2e[i]), ptr(out_pose)), "e2e frame %d" % i)
-        # each call returns with its tracked pose; the last frames' fusion finishes inside the timing
+        # each call returns with its tracked pose; the last frames' fusion and mesh finish inside the timing
         check(lib.kifi_pipeline_sync(pipe, None), "e2e sync")
         e2e_s = time.perf_counter() - te0
     clocks.__exit__(None, None, None)
     e2e_s = max_over_ranks(e2e_s, world)
 
-    # the merge kernel with tracking idle: a few fusion-only frames after the
-    # timed regions (the last rendered frame again, on the pipeline's volume)
+    # ---- isolated kernels, after the timed regions
+    # fusion-only frames (the last rendered frame again, on the pipeline's volume), tracking idle
     ISO = 5
     iso_stage = np.zeros(4)
     iso_n = C.c_int()
@@ -380,20 +509,41 @@ def run_gpu(args, rank, world, local):
         check(lib.kifi_integrate_device(vol, C.c_void_p(frames[n_frames - 1].data_ptr()), 1, C.byref(cam),
                                         ptr(w2e[n_frames - 1])), "isolated frame")
     check(lib.kifi_volume_stage_times(vol, ptr(iso_stage), C.byref(iso_n)))
+    # a mesh of the whole volume alone (the first call sizes the volume's mesh buffers)
+    iso_mesh_ms, iso_meshes = C.c_double(), C.c_int()
+    nvi, nii = C.c_size_t(), C.c_size_t()
+    for k in range(3):
+        if k == 1:
+            check(lib.kifi_volume_mesh_times(vol, C.byref(iso_mesh_ms), C.byref(iso_meshes)))  # reset
+        check(lib.kifi_mesh_device(vol, 1, C.byref(nvi), C.byref(nii), None, None), "isolated mesh")
+    check(lib.kifi_volume_mesh_times(vol, C.byref(iso_mesh_ms), C.byref(iso_meshes)))
     check(lib.kifi_volume_set_profiling(vol, 0))
     i0, ie, i1 = np.zeros(64, np.uint64), np.zeros(64, np.uint64), np.zeros(64, np.uint64)
     iso_cnt = C.c_int()
     check(lib.kifi_volume_frame_log(vol, ptr(i0), ptr(ie), ptr(i1), 64, C.byref(iso_cnt)))
     lo, hi = iso_cnt.value - ISO, iso_cnt.value
-    iso_bytes = float((12.0 * i0[lo:hi].astype(np.float64) + 4.0 * ie[lo:hi] + 12.0 * i1[lo:hi] +
-                       2.0 * W * H).mean())
-    iso_ms = iso_stage[3] / max(iso_n.value, 1)
+    i0, ie, i1 = (a[lo:hi].astype(np.float64) for a in (i0, ie, i1))
+    n_mesh_vox = C.c_size_t()
+    check(lib.kifi_volume_size(vol, C.byref(n_mesh_vox)))
+    # one ICP alignment alone (the pipeline's last target), after a first one that keeps the GPU busy
+    ia0, ia1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    last = n_frames - 1
+    guess = scenes.kifi_matrix(poses[last - 1])
+    check(lib.kifi_icp_align_device(icp, C.c_void_p(frames[last].data_ptr()), 1, C.byref(cam), ptr(guess),
+                                    ICP_ITERS))
+    ia0.record(ist)
+    check(lib.kifi_icp_align_device(icp, C.c_void_p(frames[last].data_ptr()), 1, C.byref(cam), ptr(guess),
+                                    ICP_ITERS))
+    ia1.record(ist)
+    ia1.synchronize()
+    iso_icp_ms = ia0.elapsed_time(ia1)
+    body = np.zeros(64, np.float32)
+    tail = np.zeros(64, np.float32)
+    nit = C.c_int()
+    check(lib.kifi_icp_iteration_times(icp, ptr(body), ptr(tail), 64, C.byref(nit)))
 
-    nv, ni = C.c_size_t(), C.c_size_t()
-    check(lib.kifi_pipeline_mesh_counts(pipe, C.byref(nv), C.byref(ni)))
     gb, gu = C.c_longlong(), C.c_longlong()
     check(lib.kifi_pipeline_graph_stats(pipe, C.byref(gb), C.byref(gu)))
-    check(lib.kifi_volume_size(vol, C.byref(n_resident)))
 
     if rank != 0:
         lib.kifi_pipeline_destroy(pipe)
@@ -401,64 +551,118 @@ def run_gpu(args, rank, world, local):
             dist.destroy_process_group()
         return
 
-    value = job_throughput(world, K, ms / 1e3)
     P = W * H
-    algo_bytes = (12.0 * n0.astype(np.float64) + 4.0 * ne + 12.0 * n1 + 2.0 * P)
-    merge_ms = ms_stage[3] / max(nst.value, 1)
-    achieved = float(algo_bytes.mean()) / (merge_ms / 1e3) / 1e9
-    peak, peak_kind = measured_peak()
+    peak, sm_mhz_max, peak_kind = measured_peaks()
+    fp32_peak = sms * FP32_LANES_PER_SM * 2 * sm_mhz_max * 1e6 / 1e12  # TFLOP/s
+    fp32_src = "computed: %d SMs x %d FP32 lanes x 2 flop x %.0f MHz" % (sms, FP32_LANES_PER_SM, sm_mhz_max)
+    per = max(nst.value, 1)
+
+    def gbs(nbytes, ms_):
+        return nbytes / (ms_ * 1e-3) / 1e9 if ms_ > 0 else 0.0
+
+    # algorithmic bytes per launch (each input read once, each output written once)
+    merge_bytes = float((12.0 * n0 + 4.0 * ne + 12.0 * n1 + 2.0 * P).mean())
+    splat_bytes = float((2.0 * P + 4.0 * ne).mean())
+    sort_bytes = float((8.0 * ne).mean())
+    merge_ms = ms_stage[3] / per
+    iso_per = max(iso_n.value, 1)
+    iso_merge_bytes = float((12.0 * i0 + 4.0 * ie + 12.0 * i1 + 2.0 * P).mean())
+    iso_splat_bytes = float((2.0 * P + 4.0 * ie).mean())
+    iso_sort_bytes = float((8.0 * ie).mean())
+    mv, mi = region_mesh
+    mesh_bytes = 12.0 * float(n1[-1]) + 12.0 * mv + 4.0 * mi  # keys+values, vertices, triangles (12 B each)
+    iso_mesh_bytes = 12.0 * n_mesh_vox.value + 12.0 * nvi.value + 4.0 * nii.value
+    icp_flops = (P / 4.0) * 441.0 * 10.0  # per iteration: P/4 sources x 441 candidates x 10 flop
+    track_step_ms = pipe_ms[0] / ICP_ITERS
+    iso_step_ms = iso_icp_ms / ICP_ITERS
+    tr_merge = ncu_traffic("merge_update_traffic.json")
     traffic = None
-    tr = ncu_traffic_per_voxel()
-    if tr:
-        traffic = float(tr["bytes_per_voxel"] * float((n0 + n1).mean()) + tr.get("bytes_fixed", 0.0))
-    # per frame: frame set-up, splat+emit, sort (prepare, histogram, 4 passes),
-    # merge partition, merge+update; ICP: begin, one step per iteration, the
-    # next target's back-projection; a mesh is 7 launches (snapshot, row
-    # directory, classification, two scan kernels, two emission passes)
-    launches_per_frame = 10 + (ICP_ITERS + 2)
-    gpu_launches = K * launches_per_frame + (K // MESH_EVERY) * 7
+    if tr_merge:
+        traffic = float(tr_merge["bytes_per_voxel"] * float((n0 + n1).mean()) + tr_merge.get("bytes_fixed", 0.0))
+
+    kernels = {
+        "k_splat_emit": roofline_entry(
+            "hbm", gbs(splat_bytes, ms_stage[0] / per), peak, "GB/s",
+            {"bytes_per_launch": splat_bytes, "bytes_rule": "2 B per pixel + 4 B per new key"},
+            ms_stage[0] / per, peak_kind,
+            {"isolated": {"ms_per_launch": iso_stage[0] / iso_per,
+                          "frac": gbs(iso_splat_bytes, iso_stage[0] / iso_per) / peak}}),
+        "sort (prepare, histogram, digit passes)": roofline_entry(
+            "hbm", gbs(sort_bytes, ms_stage[1] / per), peak, "GB/s",
+            {"bytes_per_launch": sort_bytes, "bytes_rule": "8 B per new key"}, ms_stage[1] / per, peak_kind,
+            {"isolated": {"ms_per_launch": iso_stage[1] / iso_per,
+                          "frac": gbs(iso_sort_bytes, iso_stage[1] / iso_per) / peak}}),
+        "k_merge_update": roofline_entry(
+            "hbm", gbs(merge_bytes, merge_ms), peak, "GB/s",
+            {"bytes_per_launch": merge_bytes, "bytes_rule": "12 B per resident voxel in and out + 4 B per new key "
+                                                            "+ 2 B per pixel"}, merge_ms, peak_kind,
+            {"traffic": traffic,
+             "isolated": {"ms_per_launch": iso_stage[3] / iso_per,
+                          "frac": gbs(iso_merge_bytes, iso_stage[3] / iso_per) / peak}}),
+        "mesher (row directory, classify, scan, emit)": roofline_entry(
+            "hbm", gbs(mesh_bytes, pipe_ms[1]), peak, "GB/s",
+            {"bytes_per_launch": mesh_bytes, "bytes_rule": "12 B per voxel + 12 B per vertex + 12 B per triangle",
+             "per": "mesh"}, pipe_ms[1], peak_kind,
+            {"meshes": int(pipe_n[1]),
+             "isolated": {"ms_per_launch": iso_mesh_ms.value, "voxels": n_mesh_vox.value,
+                          "frac": gbs(iso_mesh_bytes, iso_mesh_ms.value) / peak}}),
+        "k_icp_step": roofline_entry(
+            "fp32", icp_flops / (track_step_ms * 1e-3) / 1e12 if track_step_ms > 0 else 0.0, fp32_peak, "TFLOP/s",
+            {"flop_per_launch": icp_flops, "flop_rule": "P/4 sources x 441 window candidates x 10 flop"},
+            track_step_ms, fp32_src,
+            {"isolated": {"ms_per_launch": iso_step_ms,
+                          "frac": icp_flops / (iso_step_ms * 1e-3) / 1e12 / fp32_peak if iso_step_ms > 0 else 0.0,
+                          "association_us_median": float(np.median(body[:min(nit.value, 64)])),
+                          "finisher_us_median": float(np.median(tail[:min(nit.value, 64)]))}}),
+    }
+    value = job_throughput(world, KF, ms / 1e3)
+    steps_launches = K * (FS * (LAUNCHES_FUSION + LAUNCHES_TRACKING) + LAUNCHES_MESH)
+    cfg = workload_config(Fp, FS)
+    cfg.update({"resident_voxels_start": n_start, "resident_voxels_end": int(n1[-1]) if m else None,
+                "roofline_frames": "the last %d timed frames (the device frame log's length)" % m,
+                "trajectory_frames": n_frames,
+                "parallelism": "replicas" if world > 1 else "single"})
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
         "warmup": Wu, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+u32", "data": "synthetic",
-        "config": {"workload": "room 4x3x4 m, 40 boxes + 20 spheres, 640x480 uint16 depth, "
-                               "res 1024 x 4 mm, trunc 2 cm, ICP 15 it/frame, mesh every 10",
-                   "prefill_frames": Fp, "resident_voxels_start": n_start,
-                   "resident_voxels_end": int(n1[-1]) if m else None,
-                   "roofline_frames": "the last %d timed frames (the device frame log's length)" % m,
-                   "l2": "volume (>240 MB) larger than L2; every frame is a new depth image",
-                   "parallelism": "replicas" if world > 1 else "single"},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic,
-                     "kernel": "k_merge_update (fused merge-path union + TSDF update)",
-                     "peak_source": peak_kind,
-                     "bytes_per_launch": float(algo_bytes.mean()),
-                     "ms_per_launch": merge_ms,
-                     "isolated": {"ms_per_launch": iso_ms, "achieved": iso_bytes / (iso_ms * 1e-3) / 1e9,
-                                  "frac": iso_bytes / (iso_ms * 1e-3) / 1e9 / peak, "bytes_per_launch": iso_bytes,
-                                  "frames": ISO,
-                                  "note": "fusion-only frames after the timed regions, tracking idle; inside the "
-                                          "pipeline the merge yields SMs to the higher-priority tracking steps"}},
-        "stage_ms_per_frame": {"splat_emit": ms_stage[0] / max(nst.value, 1),
-                               "sort": ms_stage[1] / max(nst.value, 1),
-                               "merge_partition": ms_stage[2] / max(nst.value, 1),
-                               "merge_update": merge_ms},
-        "e2e": {"value": job_throughput(world, K, e2e_s), "unit": UNIT, "h2d_bytes_per_step": 2 * P + 64,
-                "d2h_bytes_per_step": 64 + 1024},
-        "gpu_launches": gpu_launches,
+        "config": cfg,
+        "roofline": dict(kernels["k_merge_update"], kernel="k_merge_update (fused merge-path union + TSDF update)",
+                         kernels=kernels),
+        "stage_ms_per_frame": {"splat_emit": ms_stage[0] / per, "sort": ms_stage[1] / per,
+                               "merge_partition": ms_stage[2] / per, "merge_update": merge_ms,
+                               "icp_alignment": pipe_ms[0], "mesh_per_10_frames": pipe_ms[1]},
+        "e2e": {"value": job_throughput(world, KF, e2e_s), "unit": UNIT,
+                "h2d_bytes_per_step": FS * (2 * P + 64),
+                "d2h_bytes_per_step": FS * ICP_HEAD_BYTES + MESH_COUNTS_BYTES},
+        "gpu_launches": steps_launches,
+        "mesh": {"meshes_in_region": meshes1 - meshes0, "reemitted_in_region": reemit1 - reemit0,
+                 "vertices": region_mesh[0], "indices": region_mesh[1],
+                 "same_after_sync": region_mesh == synced_mesh,
+                 "joined": "the device region's end event follows the mesh stream (kifi_pipeline_join)"},
         "graphs": {"on": bool(args.graphs), "instantiated": int(gb.value), "updated": int(gu.value)},
         "autotune": None if args.no_autotune else {"splat_ctas": int(tuned[0]), "sort_ctas": int(tuned[1]),
                                                    "merge_ctas": int(tuned[2])},
-        "mesh": {"vertices": nv.value, "indices": ni.value},
     }
     line["clocks"] = clocks.summary()
     if resident is not None:
-        v, kind, nfr, tmesh = cpu_baseline(frames_host, poses, t0, K, args.cpu_seconds, resident)
-        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": 1, "kind": kind,
-                                "sample": "%d frames (integrate + 15 ICP iterations each) from the "
-                                          "same resident volume, plus one mesh (%.2f s) amortised "
-                                          "over 10 frames; single-threaded, as the reference is"
-                                          % (nfr, tmesh)}
+        v, kind, nfr, tmesh = cpu_frames(frames_host, poses, t0, KF, args.cpu_seconds, resident)
+        hc = host_cpu()
+        cb = {"value": v, "unit": UNIT, "cores": 1, "kind": kind,
+              "sample": "%d frames (integrate + 15 ICP iterations each) from the same resident volume, plus one "
+                        "mesh (%.2f s) amortised over 10 frames; single-threaded, as the reference is"
+                        % (nfr, tmesh)}
+        cb.update(hc)
+        procs = max(1, int(hc["nproc"] or 1))
+        try:
+            agg, res = cpu_aggregate(frames_host, poses, t0, KF, args.cpu_seconds, resident, procs)
+            cb["aggregate"] = {"value": agg, "unit": UNIT, "processes": procs,
+                               "sample": "one scene per core: %d processes each run the same bounded sample "
+                                         "at once (%d-%d frames each); frames/s summed" %
+                                         (procs, min(r[2] for r in res), max(r[2] for r in res))}
+        except Exception as e:  # the aggregate is context, not the baseline
+            cb["aggregate"] = {"unavailable": str(e)[:200]}
+        line["cpu_baseline"] = cb
     lib.kifi_pipeline_destroy(pipe)
     if not args.no_learned:
         line["icp_iterations"] = learned_vs_plain()
@@ -486,10 +690,14 @@ def learned_vs_plain():
     seeds = [SEED + 21000, SEED + 21001]
     res = mp.evaluate(net, mean, std, seeds, 40, max_pairs=96)
     net.close()
-    return {"plain": res["plain_iterations"], "learned": res["learned_iterations"], "ratio": res["ratio"],
-            "pairs": res["pairs"], "fallbacks": res["fallbacks"], "criterion": "RMS change < 1e-4 m",
-            "held_out": "room trajectories %d-%d, pairs (a, a+k), k = 1..3" % (seeds[0], seeds[-1]),
-            "median_pose_diff": res["median_pose_diff"], "plain_spread_median": res["plain_spread_median"]}
+    out = {"plain": res["plain_iterations"], "learned": res["learned_iterations"], "ratio": res["ratio"],
+           "pairs": res["pairs"], "fallbacks": res["fallbacks"], "criterion": "RMS change < 1e-4 m",
+           "held_out": "room trajectories %d-%d, pairs (a, a+k), k = 1..3" % (seeds[0], seeds[-1]),
+           "median_pose_diff": res["median_pose_diff"], "plain_spread_median": res["plain_spread_median"]}
+    for k in ("plain_error_median", "learned_error_median", "same_pose_1e-5"):
+        if k in res:
+            out[k] = res[k]
+    return out
 
 
 def run_reference(args, rank, world):
@@ -497,7 +705,8 @@ def run_reference(args, rank, world):
         return
     from merge_fusion_gb300 import scenes
     # a bounded sample of the same workload: the first frames of the timed range
-    K, Wu, Fp = min(args.steps, REF_MAX_TIMED_FRAMES), min(args.warmup, 3), args.prefill
+    K = min(args.steps * FRAMES_PER_STEP, REF_MAX_TIMED_FRAMES)
+    Wu, Fp = min(args.warmup, 3), args.prefill
     n_frames = Fp + Wu + K + 1
     frames, poses = scenes.render_room_torch(n_frames, seed=SEED, device="cpu")
     frames = frames.numpy().view(np.uint16)
@@ -534,18 +743,18 @@ def run_reference(args, rank, world):
         times.append(time.perf_counter() - t0)
     tt = sum(times[Wu:])
     value = K / tt
+    hc = host_cpu()
+    cb = {"value": value, "unit": UNIT, "cores": 1, "kind": kind,
+          "sample": "%d timed frames (of the %d requested) after %d warm-up frames and %d fusion-only prefill "
+                    "frames; single-threaded: the reference fuses one scene on one thread"
+                    % (K, args.steps * FRAMES_PER_STEP, Wu, Fp)}
+    cb.update(hc)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-            "steps": K, "warmup": Wu, "ms_per_step": 1e3 * tt / K, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32+u32", "data": "synthetic",
-            "config": {"workload": "room 4x3x4 m, 40 boxes + 20 spheres, 640x480 uint16 depth, "
-                                   "res 1024 x 4 mm, trunc 2 cm, ICP 15 it/frame, mesh every 10",
-                       "prefill_frames": Fp},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": kind,
-                             "sample": "%d timed frames (of the %d requested) after %d warm-up "
-                                       "frames and %d fusion-only prefill frames; single-threaded "
-                                       "like the reference" % (K, args.steps, Wu, Fp)},
-            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": 0}}
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tt / K * FRAMES_PER_STEP,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+u32",
+            "data": "synthetic", "config": workload_config(Fp, FRAMES_PER_STEP),
+            "cpu_baseline": cb,
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 

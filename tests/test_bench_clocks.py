@@ -50,3 +50,19 @@ def test_malformed_lines_are_skipped():
     s = sampler([(1.0, "0, [N/A], 2070"), (1.1, "garbage"), (1.2, IDLE)], [(0.9, 1.3)])
     r = s.summary()
     assert r["samples"] == 1 and r["sm_mhz"] == 2070.0
+
+
+def test_samples_are_placed_by_their_own_timestamp():
+    """A line that reaches the reader late still counts where nvidia-smi
+    took it; a line without a readable timestamp falls back to its arrival."""
+    import datetime
+    s = bench.ClockSampler(0)
+    t = datetime.datetime(2026, 12, 4, 13, 0, 0, 250000)
+    stamp = t.strftime("%Y/%m/%d %H:%M:%S.%f")[:-3]
+    s.add(stamp + ", " + THERMAL, arrival=t.timestamp() + 5.0)
+    s.add("not a time, " + IDLE, arrival=t.timestamp() + 6.0)
+    assert abs(s.lines[0][0] - t.timestamp()) < 1e-3
+    assert s.lines[1][0] == t.timestamp() + 6.0
+    s.windows = [(t.timestamp() - 0.1, t.timestamp() + 0.1)]
+    r = s.summary()
+    assert r["samples"] == 1 and r["reasons"] == ["hw_thermal_slowdown"]

@@ -63,3 +63,20 @@ def test_two_gloo_ranks():
         assert value == pytest.approx(2 * 95 / 0.015)
         assert seeds[0] != seeds[1]
         assert printed == ""
+
+
+def test_cpu_aggregate_runs_one_sample_per_process():
+    """The multi-core CPU aggregate: each spawned process runs the bounded
+    single-core sample from the same resident volume; frames/s are summed."""
+    import numpy as np
+    sys.path.insert(0, ROOT)
+    import bench
+    from merge_fusion_gb300 import scenes
+    frames, poses = scenes.render_room_torch(3, seed=0, device="cpu")
+    frames = frames.numpy().view(np.uint16)
+    resident = (np.zeros(0, np.uint32), np.zeros((0, 2), np.float32))
+    total, res = bench.cpu_aggregate(frames, poses, 1, 1, 0.01, resident, 2)
+    assert len(res) == 2 and all(r[2] == 1 for r in res)
+    assert abs(total - sum(r[0] for r in res)) < 1e-9 and total > 0
+    info = bench.host_cpu()
+    assert info["nproc"] >= 1 and info["cpu_model"]
