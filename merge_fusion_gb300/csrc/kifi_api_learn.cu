@@ -7,6 +7,8 @@
 using namespace kifi;
 
 namespace {
+// where the GEMM's bounded waits report; one per device, shared by every
+// call of kifi_gemm_bf16 (overlapping calls race on it, as the header says)
 __device__ unsigned int g_gemm_status;
 }
 

@@ -175,6 +175,15 @@ class _Icp:
         return pd.reshape(4, 4).T.copy(), pf, rms[:it.value].copy()
 
 
+def pose_error(T, truth):
+    """(translation error in metres, rotation error in radians) of an
+    eye-to-world pose against the ground truth."""
+    T, truth = np.asarray(T, np.float64), np.asarray(truth, np.float64)
+    dR = T[:3, :3].T @ truth[:3, :3]
+    c = max(-1.0, min(1.0, (np.trace(dR) - 1.0) / 2.0))
+    return float(np.linalg.norm(T[:3, 3] - truth[:3, 3])), math.acos(c)
+
+
 def iterations_to_converge(rms, tol=1e-4):
     """First iteration whose RMS residual changed by less than tol (metres)
     from the previous one; len(rms) when none did."""
@@ -192,7 +201,7 @@ def make_pairs(proposer, seeds, frames_per_traj, steps=(1, 2, 3), icp_iters=40, 
     xs, ys, meta = [], [], []
     try:
         for seed in seeds:
-            frames, poses = scenes.render_room_torch(frames_per_traj, seed=seed, device=device)
+            frames, poses = scenes.render_room_torch(frames_per_traj, seed=seed, device=device, noise="device")
             e2w = [scenes.kifi_matrix(p) for p in poses]
             n = frames_per_traj - max(steps)
             x = torch.zeros((n * len(steps), IN_H, IN_W, 2), dtype=torch.float16, device=device)
@@ -234,14 +243,17 @@ def train(proposer, x, y, steps=3000, batch=256, lr=1e-3, seed=0, log_every=250)
 def evaluate(proposer, mean, std, seeds, frames_per_traj, steps=(1, 2, 3), icp_iters=60, max_pairs=1000,
              device="cuda"):
     """Plain vs learned-warm-started ICP on held-out trajectories: iterations
-    to converge (RMS change < 1e-4 m), the final pose difference, fallbacks."""
+    to converge (RMS change < 1e-4 m), the final pose difference, the final
+    pose error against the generator's ground truth (translation in metres,
+    rotation in radians) of either start, fallbacks."""
     import torch
     icp = _Icp()
     it_plain, it_learned, diffs, spread, fallbacks, n = [], [], [], [], 0, 0
+    err_plain, err_learned = [], []
     rng = np.random.default_rng(12345)
     try:
         for seed in seeds:
-            frames, poses = scenes.render_room_torch(frames_per_traj, seed=seed, device=device)
+            frames, poses = scenes.render_room_torch(frames_per_traj, seed=seed, device=device, noise="device")
             e2w = [scenes.kifi_matrix(p) for p in poses]
             na = frames_per_traj - max(steps)
             x = torch.zeros((8, IN_H, IN_W, 2), dtype=torch.float16, device=device)
@@ -270,6 +282,8 @@ def evaluate(proposer, mean, std, seeds, frames_per_traj, steps=(1, 2, 3), icp_i
                     it_plain.append(kp)
                     it_learned.append(kl)
                     diffs.append(float(np.abs(Tl - Tp).max()))
+                    err_plain.append(pose_error(Tp, poses[b]))
+                    err_learned.append(pose_error(Tl, poses[b]))
                     n += 1
             del frames
             if n >= max_pairs:
@@ -277,7 +291,13 @@ def evaluate(proposer, mean, std, seeds, frames_per_traj, steps=(1, 2, 3), icp_i
     finally:
         icp.close()
     diffs = np.asarray(diffs)
+    ep, el = np.asarray(err_plain), np.asarray(err_learned)
     return {"pairs": n, "plain_iterations": float(np.mean(it_plain)),
+            "plain_error_median": {"m": float(np.median(ep[:, 0])), "rad": float(np.median(ep[:, 1]))},
+            "learned_error_median": {"m": float(np.median(el[:, 0])), "rad": float(np.median(el[:, 1]))},
+            "plain_error_p90": {"m": float(np.percentile(ep[:, 0], 90)), "rad": float(np.percentile(ep[:, 1], 90))},
+            "learned_error_p90": {"m": float(np.percentile(el[:, 0], 90)),
+                                  "rad": float(np.percentile(el[:, 1], 90))},
             "learned_iterations": float(np.mean(it_learned)),
             "ratio": float(np.mean(it_learned) / max(np.mean(it_plain), 1e-12)),
             "fallbacks": fallbacks, "max_pose_diff": float(diffs.max()),

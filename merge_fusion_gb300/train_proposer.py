@@ -20,10 +20,12 @@ import numpy as np
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", required=True)
-    ap.add_argument("--train-trajectories", type=int, default=60)
+    # the defaults give 500 x (134 - 3) x 3 = 196,500 training pairs and 8
+    # held-out trajectories for the 1000 evaluation pairs
+    ap.add_argument("--train-trajectories", type=int, default=500)
     ap.add_argument("--eval-trajectories", type=int, default=8)
-    ap.add_argument("--frames", type=int, default=80)
-    ap.add_argument("--steps", type=int, default=4000)
+    ap.add_argument("--frames", type=int, default=134)
+    ap.add_argument("--steps", type=int, default=8000)
     ap.add_argument("--eval-pairs", type=int, default=1000)
     ap.add_argument("--seed", type=int, default=1000)
     ap.add_argument("--eval-only", help="evaluate saved weights instead of training")

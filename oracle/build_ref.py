@@ -29,7 +29,18 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = os.environ.get("KIFI_REFERENCE_ROOT", "/root/reference")
+
+
+def reference_root():
+    """The read-only reference checkout: $KIFI_REFERENCE_ROOT when set, else a
+    directory named ``reference`` beside this repository's root."""
+    env = os.environ.get("KIFI_REFERENCE_ROOT")
+    if env:
+        return env
+    return os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+
+
+REF_ROOT = reference_root()
 REF_KIFI = os.path.join(REF_ROOT, "KinectFission", "kifi")
 OUT = os.path.join(HERE, "_ref")
 SRC = os.path.join(OUT, "src")

@@ -97,3 +97,32 @@ def test_training_reduces_loss(gpu):
     p = pr.get_params()
     from oracle import proposer as op
     assert np.all(p[~op.trainable_mask()] == 0)
+
+
+def test_batch256_forward_and_training_step(gpu):
+    """Batch 256 (the training batch): three warm-up rounds of one training
+    step and one forward pass, then two of each, timed on the host; every
+    loss finite.  Its GEMM launches are the ones the proposer's ncu profile
+    captures."""
+    import time
+    import torch
+    from merge_fusion_gb300 import proposer as mp
+    net = mp.PoseProposer(max_batch=256)
+    net.set_params(mp.init_params(0))
+    rng = np.random.default_rng(0)
+    x = torch.from_numpy(rng.uniform(0.4, 4, (256, 60, 80, 2)).astype(np.float16)).cuda()
+    t = torch.from_numpy(rng.normal(size=(256, 6)).astype(np.float32)).cuda()
+    for _ in range(3):
+        assert np.isfinite(net.train_step(x, t, 1e-4))
+        net.predict(x)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(2):
+        out = net.predict(x)
+    t1 = time.perf_counter()
+    for _ in range(2):
+        assert np.isfinite(net.train_step(x, t, 1e-4))
+    t2 = time.perf_counter()
+    assert np.isfinite(out).all()
+    print("batch 256: forward %.3f ms, training step %.3f ms" % ((t1 - t0) / 2 * 1e3, (t2 - t1) / 2 * 1e3))
+    net.close()

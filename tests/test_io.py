@@ -64,7 +64,8 @@ def test_depthstream_matches_reference(kifi_lib, oracle_ref, tmp_path, version, 
 
 def test_depthstream_reference_fixtures(kifi_lib, oracle_ref):
     from merge_fusion_gb300 import _lib, kifi
-    root = "/root/reference/KinectFission/content"
+    from oracle import build_ref
+    root = os.path.join(build_ref.reference_root(), "KinectFission", "content")
     if not os.path.isdir(root):
         pytest.skip("reference fixtures absent")
     # imrod_v1.depth declares 18 frames but holds one: the reference returns

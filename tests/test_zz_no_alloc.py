@@ -79,6 +79,19 @@ def test_static_sort_in_a_fresh_process(gpu):
             "    assert lib.kifi_radix_sort_pairs_u32_static(C.c_void_p(d.data_ptr()), None, 100000, None) == 0\n"
             "    assert np.array_equal(d.cpu().numpy().view(np.uint32), np.sort(keys))\n"
             "    d.copy_(torch.from_numpy(keys.view(np.int32)))\n"
+            "# keys with values, the last tile partial (n not a multiple of 2048)\n"
+            "n = 77777\n"
+            "keys = rng.integers(0, 1 << 12, n, dtype=np.uint32)\n"
+            "vals = np.arange(n, dtype=np.uint32)\n"
+            "wk, wv = keys.copy(), vals.copy()\n"
+            "assert lib.kifi_radix_sort_pairs_u32(wk.ctypes.data_as(C.c_void_p), wv.ctypes.data_as(C.c_void_p), n) == 0\n"
+            "for _ in range(2):\n"
+            "    dk = torch.from_numpy(keys.view(np.int32)).cuda()\n"
+            "    dv = torch.from_numpy(vals.view(np.int32)).cuda()\n"
+            "    torch.cuda.synchronize()\n"
+            "    assert lib.kifi_radix_sort_pairs_u32_static(C.c_void_p(dk.data_ptr()), C.c_void_p(dv.data_ptr()), n, None) == 0\n"
+            "    assert np.array_equal(dk.cpu().numpy().view(np.uint32), wk)\n"
+            "    assert np.array_equal(dv.cpu().numpy().view(np.uint32), wv)\n"
             "print('ok')\n" % ROOT)
     r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0 and r.stdout.strip().endswith("ok"), r.stderr[-2000:]
