@@ -74,6 +74,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-vs-plain ICP measurement")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the 64-scene batched run (uneven frame sizes, voxel sizes and lengths)")
     ap.add_argument("--graphs", action="store_true",
                     help="one CUDA graph per frame (kifi_pipeline_set_graphs) instead of plain launches")
     ap.add_argument("--capacity-mvox", type=int, default=48,
@@ -666,6 +668,8 @@ def run_gpu(args, rank, world, local):
     lib.kifi_pipeline_destroy(pipe)
     if not args.no_learned:
         line["icp_iterations"] = learned_vs_plain()
+    if not args.no_batched:
+        line["batched"] = batched_scenes()
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
@@ -698,6 +702,20 @@ def learned_vs_plain():
         if k in res:
             out[k] = res[k]
     return out
+
+
+def batched_scenes():
+    """64 seeded scenes with uneven frame sizes ({320x240, 512x424, 640x480,
+    1024x848}), voxel sizes ({2, 4, 8} mm, truncation 5 voxels) and
+    trajectory lengths (50-300 frames) through one kifi_batch: each step is
+    one launch per stage for every scene that still has frames."""
+    from merge_fusion_gb300 import batched as bt
+    specs = bt.scene_specs(64, 7)
+    res = bt.run_batch(specs, unique=40, icp_iters=ICP_ITERS)
+    res["mix"] = {"sizes": {"%dx%d" % (w, h): sum(1 for s in specs if s["width"] == w) for w, h, _ in bt.SIZES},
+                  "voxels_mm": {str(v): sum(1 for s in specs if s["voxel_mm"] == v) for v in bt.VOXELS_MM},
+                  "trajectory_frames": [min(s["frames"] for s in specs), max(s["frames"] for s in specs)]}
+    return res
 
 
 def run_reference(args, rank, world):

@@ -538,6 +538,41 @@ KIFI_API kifi_status kifi_pipeline_mesh_counts(kifi_pipeline* p, size_t* n_verts
  * time because they outgrew the buffers sized by earlier meshes. */
 KIFI_API kifi_status kifi_pipeline_mesh_stats(kifi_pipeline* p, long long* meshes, long long* reemitted);
 
+/* -------------------------------------------------------------- batches */
+
+/* No counterpart in the reference, which runs one kifi::Pipeline at a time.
+ * A batch fuses and tracks many independent depth sequences together: one
+ * volume and one ICP context per scene (descs[i]: camera, volume, ICP
+ * iterations; mesh_every and closed_loop must be 0; one device; every
+ * tracked scene uses the same iteration count).  A step takes one device
+ * frame (uint16 mm) per scene and enqueues each stage of the path once for
+ * all scenes -- splat, sort, merge partition, merge + TSDF update on one
+ * stream, ICP begin, the AlignSteps and the next targets' back-projection on
+ * another -- each launch sharing its CTAs out among the scenes.  Per scene
+ * the results equal kifi_pipeline (open loop) on the same frames. */
+typedef struct kifi_batch kifi_batch;
+KIFI_API kifi_status kifi_batch_create(const kifi_pipeline_desc* descs, int n, kifi_batch** out);
+KIFI_API kifi_status kifi_batch_destroy(kifi_batch* b);
+/* one step: depth_dev[i] is scene i's frame (NULL: the scene sits this step
+ * out), world_to_eye its pose (16 floats per scene, kifi order).
+ * Asynchronous: the frames must stay valid until kifi_batch_sync. */
+KIFI_API kifi_status kifi_batch_step_device(kifi_batch* b, const void* const* depth_dev,
+                                            const float* world_to_eye);
+/* waits for every queued step; reports device errors */
+KIFI_API kifi_status kifi_batch_sync(kifi_batch* b);
+/* scene i's volume (for kifi_volume_size / export; valid until destroy) */
+KIFI_API kifi_volume* kifi_batch_volume(kifi_batch* b, int scene);
+/* scene i's last tracked eye-to-world pose (the given one before its first alignment) */
+KIFI_API kifi_status kifi_batch_pose(kifi_batch* b, int scene, float out_eye_to_world[16]);
+/* the fusion stream (a cudaStream_t): steps end on it */
+KIFI_API void* kifi_batch_stream(kifi_batch* b);
+/* step timers: while on, every step records its device span (upload of its
+ * argument tables to the end of fusion and tracking); kifi_batch_step_times
+ * waits for them, returns up to `capacity` spans (ms) and their count, and
+ * resets them */
+KIFI_API kifi_status kifi_batch_set_profiling(kifi_batch* b, int on);
+KIFI_API kifi_status kifi_batch_step_times(kifi_batch* b, float* out_ms, int capacity, int* steps);
+
 #ifdef __cplusplus
 }
 #endif

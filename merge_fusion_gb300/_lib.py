@@ -138,6 +138,15 @@ SIGNATURES = {
     "kifi_pipeline_mesh_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
     "kifi_pipeline_join": (C.c_int, [C.c_void_p, C.c_void_p]),
     "kifi_sort_set_fault_injection": (C.c_int, [C.c_uint, C.c_ulonglong]),
+    "kifi_batch_create": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]),
+    "kifi_batch_destroy": (C.c_int, [C.c_void_p]),
+    "kifi_batch_step_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "kifi_batch_sync": (C.c_int, [C.c_void_p]),
+    "kifi_batch_volume": (C.c_void_p, [C.c_void_p, C.c_int]),
+    "kifi_batch_pose": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "kifi_batch_stream": (C.c_void_p, [C.c_void_p]),
+    "kifi_batch_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
+    "kifi_batch_step_times": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
     "kifi_volume_mesh_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
     "kifi_pipeline_stage_times": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "kifi_icp_set_target_bin_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_int,

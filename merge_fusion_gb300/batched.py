@@ -1,10 +1,14 @@
 """Many independent scenes fused at once: seeded rooms with uneven frame
-sizes, voxel sizes and trajectory lengths, each a kifi_pipeline (its own
-volume, ICP context and CUDA streams).  Every step enqueues the next frame
-of every scene that still has frames, so the GPU runs the scenes' kernels
-concurrently; the host never waits inside a step.
+sizes, voxel sizes and trajectory lengths.  Two ways to run them:
 
-    python -m merge_fusion_gb300.batched [--scenes 64] [--seed 7]
+  * batch (default): one kifi_batch -- every step is one launch per stage of
+    the path for all scenes, each launch sharing its CTAs out among the
+    scenes (kifi_batch_step_device);
+  * streams: each scene a kifi_pipeline (its own volume, ICP context and
+    CUDA streams); every step enqueues the next frame of every scene, so the
+    GPU runs the scenes' kernels concurrently.
+
+    python -m merge_fusion_gb300.batched [--scenes 64] [--seed 7] [--mode batch|streams]
 
 Scene i draws its frame size from {320x240, 512x424, 640x480, 1024x848},
 its voxel size from {2, 4, 8} mm (truncation 5 voxels; a 4.096 m cube of
@@ -95,6 +99,93 @@ class Scene:
         lib.kifi_pipeline_destroy(self.pipe)
 
 
+def _desc(spec, icp_iters, mesh_every):
+    d = PipelineDesc()
+    w, h, f = spec["width"], spec["height"], spec["f"]
+    d.camera = Camera(w, h, f, f, w / 2.0, h / 2.0, 0.4, 4.0)
+    vox = spec["voxel_mm"] * 1e-3
+    d.resolution, d.side_length_m, d.truncation_m = spec["res"], spec["res"] * vox, 5 * vox
+    d.icp_iterations, d.mesh_every, d.mesh_with_indices = icp_iters, mesh_every, 1
+    d.device = 0
+    return d
+
+
+def run_batch(specs, unique=40, icp_iters=15, warmup_steps=3):
+    """All scenes through one kifi_batch: a step is one launch per stage for
+    every scene that still has frames.  Returns the same summary as run()."""
+    import torch
+    lib = _lib.load()
+    t0 = time.perf_counter()
+    data = []
+    for spec in specs:
+        n_unique = min(unique, spec["frames"])
+        fr, poses = scenes.render_room_torch(n_unique, seed=spec["seed"], width=spec["width"],
+                                             height=spec["height"], f=spec["f"], scale=spec.get("scale", 1.0),
+                                             device="cuda", noise="device")
+        data.append((fr, np.stack([scenes.kifi_matrix(np.linalg.inv(p)) for p in poses]),
+                     frame_order(n_unique, spec["frames"])))
+    torch.cuda.synchronize()
+    t_render = time.perf_counter() - t0
+    n = len(specs)
+    descs = (PipelineDesc * n)(*[_desc(s, icp_iters, 0) for s in specs])
+    for d, s in zip(descs, specs):
+        # room for the scene's volume plus a frame's worth of new voxels, so
+        # the steps need no host-side capacity checks that wait for the device
+        d.initial_capacity = {2: 64 << 20, 4: 16 << 20, 8: 6 << 20}[s["voxel_mm"]] + 8 * s["width"] * s["height"]
+    b = C.c_void_p()
+    check(lib.kifi_batch_create(descs, n, C.byref(b)), "batch")
+    try:
+        steps = max(s["frames"] for s in specs)
+        ptrs = (C.c_void_p * n)()
+        poses = np.zeros((n, 16), np.float32)
+
+        def step(t):
+            active = 0
+            for i, (fr, w2e, order) in enumerate(data):
+                if t < len(order):
+                    ptrs[i] = fr[order[t]].data_ptr()
+                    poses[i] = w2e[order[t]]
+                    active += 1
+                else:
+                    ptrs[i] = None
+            check(lib.kifi_batch_step_device(b, ptrs, poses.ctypes.data_as(C.c_void_p)), "step %d" % t)
+            return active
+
+        for t in range(warmup_steps):
+            step(t)
+        check(lib.kifi_batch_sync(b), "sync")
+        check(lib.kifi_batch_set_profiling(b, 1))
+        stream = torch.cuda.ExternalStream(lib.kifi_batch_stream(b))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        frames = 0
+        for t in range(warmup_steps, steps):
+            frames += step(t)
+        e1.record(stream)
+        check(lib.kifi_batch_sync(b), "sync")
+        e1.synchronize()
+        elapsed = e0.elapsed_time(e1) / 1e3
+        lat = np.zeros(steps, np.float32)
+        nl = C.c_int()
+        check(lib.kifi_batch_step_times(b, lat.ctypes.data_as(C.c_void_p), steps, C.byref(nl)))
+        lat = lat[:nl.value]
+        total = 0
+        for i in range(n):
+            nv = C.c_size_t()
+            check(lib.kifi_volume_size(lib.kifi_batch_volume(b, i), C.byref(nv)))
+            total += nv.value
+    finally:
+        lib.kifi_batch_destroy(b)
+    return {"mode": "batch", "scenes": n, "frames": int(frames), "seconds": elapsed,
+            "frames_per_s": frames / elapsed, "steps": int(nl.value),
+            "step_latency_ms_p50": float(np.percentile(lat, 50)), "step_latency_ms_p99": float(np.percentile(lat, 99)),
+            "resident_voxels_total": int(total), "render_seconds": t_render, "icp_iterations": icp_iters,
+            "unique_frames_per_scene": unique,
+            "latency_note": "a step runs every active scene's frame in one launch per stage, so each scene's "
+                            "step latency is the step's (device span from the argument upload to the end of "
+                            "fusion and tracking)"}
+
+
 def run(specs, unique=40, icp_iters=15, mesh_every=0, warmup_steps=3):
     import torch
     lib = _lib.load()
@@ -129,7 +220,8 @@ def run(specs, unique=40, icp_iters=15, mesh_every=0, warmup_steps=3):
         sizes[s.spec["seed"]] = n.value
     for s in sc:
         s.close(lib)
-    return {"scenes": len(specs), "frames": int(frames), "seconds": elapsed, "frames_per_s": frames / elapsed,
+    return {"mode": "streams", "scenes": len(specs), "frames": int(frames), "seconds": elapsed,
+            "frames_per_s": frames / elapsed,
             "step_latency_ms_p50": float(np.percentile(lat, 50)), "step_latency_ms_p99": float(np.percentile(lat, 99)),
             "per_scene_p50_ms": {"min": min(per_scene_p50), "max": max(per_scene_p50)},
             "resident_voxels_total": int(sum(sizes.values())), "render_seconds": t_render,
@@ -142,11 +234,15 @@ def main():
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--unique", type=int, default=40)
     ap.add_argument("--icp-iterations", type=int, default=15)
+    ap.add_argument("--mode", default="batch", choices=["batch", "streams"])
     args = ap.parse_args()
     import torch
     torch.cuda.set_device(0)
     specs = scene_specs(args.scenes, args.seed)
-    res = run(specs, unique=args.unique, icp_iters=args.icp_iterations)
+    if args.mode == "batch":
+        res = run_batch(specs, unique=args.unique, icp_iters=args.icp_iterations)
+    else:
+        res = run(specs, unique=args.unique, icp_iters=args.icp_iterations)
     res["mix"] = {"sizes": {"%dx%d" % (w, h): sum(1 for s in specs if s["width"] == w) for w, h, _ in SIZES},
                   "voxels_mm": {str(v): sum(1 for s in specs if s["voxel_mm"] == v) for v in VOXELS_MM},
                   "trajectory_frames": [min(s["frames"] for s in specs), max(s["frames"] for s in specs)]}

@@ -21,7 +21,7 @@ OBJDIR = os.path.join(LIBDIR, "obj")
 LIB = os.path.join(LIBDIR, "libkifi_gpu.so")
 
 SOURCES = ["kifi_api.cu", "kifi_api_icp.cu", "kifi_api_pipeline.cu", "kifi_integrate.cu",
-           "kifi_sort.cu", "kifi_sort_static.cu", "kifi_api_io.cu", "kifi_api_learn.cu", "kifi_tc_gemm.cu", "kifi_proposer.cu", "kifi_autotune.cu", "kifi_mesh.cu", "kifi_icp.cu"]
+           "kifi_sort.cu", "kifi_sort_static.cu", "kifi_api_batch.cu", "kifi_api_io.cu", "kifi_api_learn.cu", "kifi_tc_gemm.cu", "kifi_proposer.cu", "kifi_autotune.cu", "kifi_mesh.cu", "kifi_icp.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [
     "-O3", "-lineinfo", "-std=c++17", "-prec-div=true",

@@ -103,6 +103,45 @@ kifi_status enqueue_align(kifi_icp* c, const void* depth_dev, bool u16, const ki
 
 }  // namespace
 
+// The arguments of one frame pair's alignment for a batched launch (the
+// single-pair path's IcpArgs, without association recording).
+kifi_status kifi_icp_batch_args(kifi_icp* c, const void* depth_dev, const kifi_camera* cam, IcpArgs* a,
+                                IcpState** st, int iterations) {
+    if (!c->have_target) return fail(KIFI_ERR_INVALID_ARGUMENT, "ICP target not set");
+    *a = IcpArgs{};
+    a->depth = depth_dev;
+    a->depth_u16 = 1;
+    a->width = cam->width;
+    a->height = cam->height;
+    a->fl_inv_x = fdiv(1.0f, cam->fx);
+    a->fl_inv_y = fdiv(1.0f, cam->fy);
+    a->pp_x = fmul(fsub(0.5f, cam->cx), a->fl_inv_x);
+    a->pp_y = fmul(fsub(cam->cy, 0.5f), a->fl_inv_y);
+    const Mat4 proj = mat_mul(eye_to_clip(*cam), invert_transform(c->synth_e2w));
+    std::memcpy(a->proj, proj.m, 64);
+    a->synth = c->synth;
+    a->synth_w = c->sw;
+    a->synth_h = c->sh;
+    a->neg_zero = -0.0f;
+    *st = c->st;
+    c->last_iters = iterations;
+    return KIFI_OK;
+}
+
+// Room for a target of the camera's size; records that the next target is
+// this frame's back-projection (written by a batched launch) and returns
+// where it goes.
+kifi_status kifi_icp_batch_target(kifi_icp* c, const kifi_camera* cam, const float* eye_to_world, float4** out) {
+    kifi_status s = reserve_target(c, cam->width, cam->height);
+    if (s) return s;
+    c->sw = cam->width;
+    c->sh = cam->height;
+    c->synth_e2w = load_mat(eye_to_world);
+    c->have_target = true;
+    *out = c->synth;
+    return KIFI_OK;
+}
+
 // Everything an alignment against a target of the camera's size may need to
 // allocate, done ahead (outside any stream capture).
 kifi_status kifi_icp_prepare_frame(kifi_icp* c, const kifi_camera* cam) {

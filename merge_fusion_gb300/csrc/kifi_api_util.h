@@ -79,6 +79,10 @@ struct kifi_volume {
 // ahead of enqueueing it -- nothing in kifi_volume_enqueue_frame then waits.
 kifi_status kifi_volume_prepare_frame(kifi_volume* v, const kifi_camera* cam);
 kifi_status kifi_icp_prepare_frame(kifi_icp* c, const kifi_camera* cam);
+// batched alignment (kifi_api_batch.cu): one pair's arguments, and the next target's slot
+kifi_status kifi_icp_batch_args(kifi_icp* c, const void* depth_dev, const kifi_camera* cam, kifi::IcpArgs* a,
+                                kifi::IcpState** st, int iterations);
+kifi_status kifi_icp_batch_target(kifi_icp* c, const kifi_camera* cam, const float* eye_to_world, float4** out);
 kifi_status kifi_volume_enqueue_frame(kifi_volume* v, const void* depth_dev, bool u16,
                                       const kifi_camera* cam, const float* world_to_eye);
 

@@ -105,7 +105,7 @@ __device__ __forceinline__ float load_depth(const void* depth, size_t i, bool u1
 // whole CTA's earlier stores (the barrier makes them visible to it) before
 // the count, and the count before the last CTA's reads.
 __device__ __forceinline__ bool last_cta(unsigned long long* counter, const unsigned int& mine,
-                                         unsigned int* total) {
+                                         unsigned int* total, unsigned int nblk) {
     __shared__ bool last;
     __shared__ unsigned int s_total;
     __syncthreads();
@@ -117,7 +117,7 @@ __device__ __forceinline__ bool last_cta(unsigned long long* counter, const unsi
         unsigned long long prev;
         asm volatile("atom.acq_rel.gpu.global.add.u64 %0, [%1], %2;"
                      : "=l"(prev) : "l"(counter), "l"(add) : "memory");
-        last = (unsigned int)(prev >> 32) == gridDim.x - 1;
+        last = (unsigned int)(prev >> 32) == nblk - 1;
         s_total = (unsigned int)prev + mine;
         if (last) *counter = 0ull;  // read again only by the next launch
     }
@@ -149,9 +149,8 @@ __device__ __forceinline__ FF lane_partials(const float* ph, int b0, int G) {
     return acc;
 }
 template <int NV>
-__device__ __forceinline__ void moments_total(const IcpState* st, unsigned int count, FF* out) {
+__device__ __forceinline__ void moments_total(const IcpState* st, unsigned int count, FF* out, int G) {
     const int lane = threadIdx.x & 31, c = (threadIdx.x >> 5) + 1;
-    const int G = gridDim.x;
     if (threadIdx.x == 0) out[0] = FF{(float)count, 0.0f};  // exact: at most 2^24 sources
     if (c < NV) {
         FF a{0.0f, 0.0f};
@@ -382,7 +381,11 @@ __device__ __forceinline__ FF two_prod(float a, float b) {
     return FF{p, __fmaf_rn(a, b, -p)};  // exact remainder of the product
 }
 
-__global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step(IcpArgs a, IcpState* __restrict__ st) {
+// One AlignStep of one frame pair; `blk` / `nblk`: this CTA's index among
+// the nblk CTAs that work on the pair (the launch's own grid, or a share of
+// a batched launch over several pairs).
+__device__ __forceinline__ void icp_step_body(const IcpArgs& a, IcpState* __restrict__ st, unsigned int blk,
+                                              unsigned int nblk) {
     extern __shared__ float4 stage_mem[];  // three planes of kStagePixels floats
     const Stage stage{(float*)stage_mem, (float*)stage_mem + kStagePixels, (float*)stage_mem + 2 * kStagePixels};
     __shared__ int s_box[4];
@@ -407,8 +410,8 @@ __global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step(IcpArgs a, IcpSta
     __shared__ int s_pred[4];
     if (threadIdx.x == 0) {
         int p[4] = {0, 0, 0, 0};
-        if (blockIdx.x < tiles_x * tiles_y) {
-            const volatile int* tb = st->tile_box + 4 * blockIdx.x;
+        if (blk < tiles_x * tiles_y) {
+            const volatile int* tb = st->tile_box + 4 * blk;
             const int b0 = tb[0], b1 = tb[1], b2 = tb[2], b3 = tb[3];
             if (b2 > b0 && b3 > b1 && b0 >= 0 && b1 >= 0) {
                 const int x0 = max(b0 - kPredMargin, 0), y0 = max(b1 - kPredMargin, 0);
@@ -433,7 +436,7 @@ __global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step(IcpArgs a, IcpSta
     const int lane0 = threadIdx.x & 31, wcol0 = (threadIdx.x >> 5) >> 1;
     float pre_d = 0.0f;
     {
-        const int t0 = blockIdx.x;
+        const int t0 = blk;
         if (t0 < tiles_x * tiles_y) {
             const int col = (t0 % tiles_x) * kTileCols + wcol0, y = (t0 / tiles_x) * kTileRows + lane0;
             if (col < n_cols && y < a.height) pre_d = load_depth(a.depth, (size_t)y * a.width + col * 4, a.depth_u16);
@@ -446,7 +449,7 @@ __global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step(IcpArgs a, IcpSta
     if (threadIdx.x < kMoments) s_acc[threadIdx.x] = FF{0.0f, 0.0f};
     if (threadIdx.x == 0) s_count = 0u;
     if (threadIdx.x == 0) atomicMin(&st->t_start, global_ns());
-    for (int tile = blockIdx.x; tile < tiles_x * tiles_y; tile += gridDim.x) {
+    for (int tile = blk; tile < tiles_x * tiles_y; tile += nblk) {
         const int tx = tile % tiles_x, ty = tile / tiles_x;
         const int col = tx * kTileCols + wcol, y = ty * kTileRows + lane;
         const bool mine = col < n_cols && y < a.height;
@@ -454,7 +457,7 @@ __global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step(IcpArgs a, IcpSta
         int u = 0, v = 0, nr = 0, nc = 0;
         if (mine) {
             const int x = col * 4;
-            const float d = tile == (int)blockIdx.x ? pre_d : load_depth(a.depth, (size_t)y * a.width + x, a.depth_u16);
+            const float d = tile == (int)blk ? pre_d : load_depth(a.depth, (size_t)y * a.width + x, a.depth_u16);
             if (0.0f != d) {
                 float pt[4], cl[4];
                 pt[0] = fmul(fadd(fmul((float)x, a.fl_inv_x), a.pp_x), d);
@@ -494,7 +497,7 @@ __global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step(IcpArgs a, IcpSta
         __syncthreads();
         const int ax0 = s_box[0], ay0 = s_box[1], ax1 = s_box[2], ay1 = s_box[3];
         // the prefetched region if it holds every window of the tile, else stage the box now
-        const bool use_pred = tile == (int)blockIdx.x && pw > 0 && ax1 >= 0 && ax0 >= px0 && ay0 >= py0 &&
+        const bool use_pred = tile == (int)blk && pw > 0 && ax1 >= 0 && ax0 >= px0 && ay0 >= py0 &&
                               ax1 <= px0 + pw && ay1 <= py0 + ph;
         int bx0 = ax0, by0 = ay0, pitch = stage_pitch(ax1 - ax0);
         bool staged;
@@ -616,15 +619,19 @@ __global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step(IcpArgs a, IcpSta
     asm volatile("griddepcontrol.launch_dependents;");
     if (threadIdx.x >= 1 && threadIdx.x < kMoments) {
         const FF t = s_acc[threadIdx.x];
-        st->part[(size_t)(2 * threadIdx.x) * kIcpMaxCtas + blockIdx.x] = t.hi;
-        st->part[(size_t)(2 * threadIdx.x + 1) * kIcpMaxCtas + blockIdx.x] = t.lo;
+        st->part[(size_t)(2 * threadIdx.x) * kIcpMaxCtas + blk] = t.hi;
+        st->part[(size_t)(2 * threadIdx.x + 1) * kIcpMaxCtas + blk] = t.lo;
     }
     if (threadIdx.x == 0) atomicMax(&st->t_body, global_ns());
     unsigned int n_total;
-    if (!last_cta(&st->done, s_count, &n_total)) return;
+    if (!last_cta(&st->done, s_count, &n_total, nblk)) return;
     __shared__ FF tot[kMoments];
-    moments_total<kMoments>(st, n_total, tot);
+    moments_total<kMoments>(st, n_total, tot, (int)nblk);
     if (threadIdx.x < 32) finish_step(st, tot);
+}
+
+__global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step(IcpArgs a, IcpState* __restrict__ st) {
+    icp_step_body(a, st, blockIdx.x, gridDim.x);
 }
 
 // ------------------------------------------------------------- Horn solve
@@ -998,8 +1005,7 @@ __device__ __noinline__ void finish_step(IcpState* __restrict__ st, const FF* __
     st->iter = step + 1;
 }
 
-__global__ void k_icp_begin(IcpState* st, Mat4 guess) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__device__ __forceinline__ void icp_begin_body(IcpState* st, const Mat4& guess) {
     for (int i = 0; i < 16; ++i) {
         st->pose_f[i] = guess.m[i];
         st->pose_lo[i] = 0.0f;
@@ -1010,14 +1016,20 @@ __global__ void k_icp_begin(IcpState* st, Mat4 guess) {
     st->t_body = 0ull;
 }
 
+__global__ void k_icp_begin(IcpState* st, Mat4 guess) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    icp_begin_body(st, guess);
+}
+
 // World points of a depth frame: the back-projection of
 // DepthMap2PointCloud (Integrator.cpp:121-144) without the voxel step;
 // pixels without depth get (0,0,0), the reference's "invalid" target value.
-__global__ void k_backproject(const void* __restrict__ depth, int u16, int width, int height,
-                              float fl_inv_x, float fl_inv_y, float pp_x, float pp_y, Mat4 e2w,
-                              float4* __restrict__ out) {
+__device__ __forceinline__ void backproject_body(const void* __restrict__ depth, int u16, int width, int height,
+                                                 float fl_inv_x, float fl_inv_y, float pp_x, float pp_y,
+                                                 const Mat4& e2w, float4* __restrict__ out, unsigned int blk,
+                                                 unsigned int nblk) {
     const int n = width * height;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    for (int i = blk * blockDim.x + threadIdx.x; i < n; i += nblk * blockDim.x) {
         const int v = i / width, u = i - v * width;
         const float d = load_depth(depth, i, u16 != 0);
         float w[4] = {0.f, 0.f, 0.f, 0.f};
@@ -1031,6 +1043,12 @@ __global__ void k_backproject(const void* __restrict__ depth, int u16, int width
         }
         out[i] = make_float4(w[0], w[1], w[2], 0.0f);
     }
+}
+
+__global__ void k_backproject(const void* __restrict__ depth, int u16, int width, int height,
+                              float fl_inv_x, float fl_inv_y, float pp_x, float pp_y, Mat4 e2w,
+                              float4* __restrict__ out) {
+    backproject_body(depth, u16, width, height, fl_inv_x, fl_inv_y, pp_x, pp_y, e2w, out, blockIdx.x, gridDim.x);
 }
 
 // host float3 target -> the float4 layout the association reads (one
@@ -1081,6 +1099,27 @@ __global__ void k_bin_resolve(const float* __restrict__ pts, const unsigned long
     }
 }
 
+// ---- batched: several frame pairs per launch, each pair's CTAs running the
+// single-pair body on its arguments
+__global__ void k_icp_begin_batch(const IcpJob* __restrict__ jobs, int n) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v < n) icp_begin_body(jobs[v].st, jobs[v].guess);
+}
+
+__global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step_batch(const IcpJob* __restrict__ jobs, BlockMap m) {
+    const int v = block_owner(m, blockIdx.x);
+    const unsigned int b0 = m.first[v];
+    icp_step_body(jobs[v].a, jobs[v].st, blockIdx.x - b0, m.first[v + 1] - b0);
+}
+
+__global__ void k_backproject_batch(const BackprojectJob* __restrict__ jobs, BlockMap m) {
+    const int v = block_owner(m, blockIdx.x);
+    const BackprojectJob& j = jobs[v];
+    const unsigned int b0 = m.first[v];
+    backproject_body(j.depth, 1, j.width, j.height, j.fl_inv_x, j.fl_inv_y, j.pp_x, j.pp_y, j.e2w, j.out,
+                     blockIdx.x - b0, m.first[v + 1] - b0);
+}
+
 // the same resolve into the association's float4 target layout
 __global__ void k_bin_resolve_target(const float* __restrict__ pts, const unsigned long long* __restrict__ zbuf,
                                      int n_pix, float4* __restrict__ out) {
@@ -1127,8 +1166,49 @@ cudaError_t icp_align_enqueue(const IcpArgs& a, IcpState* st, const Mat4& guess,
 // The association's dynamic shared memory above the default 48 KB limit; set
 // once per device, outside any stream capture.
 cudaError_t icp_init_device() {
-    return cudaFuncSetAttribute(k_icp_step, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)(3 * kStagePixels * sizeof(float)));
+    cudaError_t e = cudaFuncSetAttribute(k_icp_step, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(3 * kStagePixels * sizeof(float)));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_icp_step_batch, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(3 * kStagePixels * sizeof(float)));
+    return e;
+}
+
+cudaError_t icp_align_batch_enqueue(const IcpJob* jobs, int n, const BlockMap& map, int iterations,
+                                    cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    k_icp_begin_batch<<<(n + 63) / 64, 64, 0, stream>>>(jobs, n);
+    const size_t smem = 3 * kStagePixels * sizeof(float);
+    // programmatic dependent launch, as for a single pair: each step's grid
+    // is scheduled once every CTA of the step before has finished its association
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(map.grid);
+    cfg.blockDim = dim3(kAssocThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    for (int it = 0; it < iterations; ++it) {
+        const cudaError_t e = cudaLaunchKernelEx(&cfg, k_icp_step_batch, jobs, map);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t backproject_batch_enqueue(const BackprojectJob* jobs, int n, const BlockMap& map, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_backproject_batch<<<map.grid, kThreads, 0, st>>>(jobs, map);
+    return cudaGetLastError();
+}
+
+// CTAs of one pair's association (its tiles, at most kIcpMaxCtas)
+int icp_tiles(int width, int height) {
+    const int n_cols = (width + 3) / 4;
+    const int tiles = ((n_cols + kTileCols - 1) / kTileCols) * ((height + kTileRows - 1) / kTileRows);
+    return tiles < kIcpMaxCtas ? tiles : kIcpMaxCtas;
 }
 
 cudaError_t expand_target_enqueue(const float* in, int n, float4* out, int ctas, cudaStream_t st) {

@@ -135,13 +135,14 @@ __device__ __forceinline__ bool splat_pixel(const FrameConst& fc, const float (&
     return true;
 }
 
+// Splat + dilation + new-key emission of one frame; `blk` / `nblk` are the
+// CTA's index and the CTA count working on this frame (the launch's own, or
+// a share of a batched launch over several volumes).
 template <bool kU16, typename K>
-__global__ void __launch_bounds__(kEmitThreads) k_splat_emit(DeviceCtl* __restrict__ ctl, Geom g,
-                                                             const void* __restrict__ depth,
-                                                             uint32_t* __restrict__ bitmap,
-                                                             K* __restrict__ new_keys,
-                                                             unsigned int new_cap,
-                                                             const FrameConst fc) {
+__device__ __forceinline__ void splat_emit_body(DeviceCtl* __restrict__ ctl, const Geom& g,
+                                                const void* __restrict__ depth, uint32_t* __restrict__ bitmap,
+                                                K* __restrict__ new_keys, unsigned int new_cap,
+                                                const FrameConst& fc, unsigned int blk, unsigned int nblk) {
     const Codec<K> cd(g.kb);
     const int W = fc.width, H = fc.height;
     const size_t P = (size_t)W * H;
@@ -149,9 +150,9 @@ __global__ void __launch_bounds__(kEmitThreads) k_splat_emit(DeviceCtl* __restri
     float e2w[16];
 #pragma unroll
     for (int i = 0; i < 16; ++i) e2w[i] = fc.eye_to_world.m[i];
-    const size_t stride = (size_t)gridDim.x * kEmitThreads;
+    const size_t stride = (size_t)nblk * kEmitThreads;
     const size_t P_round = (P + 31) / 32 * 32;  // warp-uniform trip count
-    for (size_t i = (size_t)blockIdx.x * kEmitThreads + threadIdx.x; i < P_round; i += stride) {
+    for (size_t i = (size_t)blk * kEmitThreads + threadIdx.x; i < P_round; i += stride) {
         K key = 0;
         bool valid = false;
         if (i < P) {
@@ -231,6 +232,16 @@ __global__ void __launch_bounds__(kEmitThreads) k_splat_emit(DeviceCtl* __restri
             }
         }
     }
+}
+
+template <bool kU16, typename K>
+__global__ void __launch_bounds__(kEmitThreads) k_splat_emit(DeviceCtl* __restrict__ ctl, Geom g,
+                                                             const void* __restrict__ depth,
+                                                             uint32_t* __restrict__ bitmap,
+                                                             K* __restrict__ new_keys,
+                                                             unsigned int new_cap,
+                                                             const FrameConst fc) {
+    splat_emit_body<kU16, K>(ctl, g, depth, bitmap, new_keys, new_cap, fc, blockIdx.x, gridDim.x);
 }
 
 // UpdateVoxels for one voxel (Integrator.cpp:273-322 for one SSE lane),
@@ -365,10 +376,10 @@ struct MergeInputs {
 // keys among the first t*kMergeTile outputs.  The binary searches of all
 // tiles run in parallel here instead of serialising the merge kernel's tiles.
 template <typename K>
-__global__ void __launch_bounds__(256) k_merge_partition(DeviceCtl* __restrict__ ctl, Geom g,
-                                                          VolumeBuffers vb, MergeInputs<K> in,
-                                                          unsigned long long* __restrict__ splits,
-                                                          unsigned int max_tiles) {
+__device__ __forceinline__ void merge_partition_body(DeviceCtl* __restrict__ ctl, const Geom& g,
+                                                     const VolumeBuffers& vb, const MergeInputs<K>& in,
+                                                     unsigned long long* __restrict__ splits,
+                                                     unsigned int max_tiles, unsigned int blk, unsigned int nblk) {
     constexpr int kTile = merge_tile<K>();
     const Codec<K> cd(g.kb);
     __shared__ unsigned long long s_e, s_n1;
@@ -391,7 +402,7 @@ __global__ void __launch_bounds__(256) k_merge_partition(DeviceCtl* __restrict__
         s_e = e;
         s_n1 = N0 + e;
         s_ok = ok;
-        if (blockIdx.x == 0) {
+        if (blk == 0) {
             ctl->merge_e = e;
             ctl->merge_n1 = N0 + e;
             ctl->merge_ok = ok ? 1u : 0u;
@@ -408,19 +419,27 @@ __global__ void __launch_bounds__(256) k_merge_partition(DeviceCtl* __restrict__
         if (timed_out) return;
         // no room: leave the volume as it was and take the new keys back out
         // of the occupancy bitmap; the host grows the buffers and retries.
-        for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < e;
-             i += (unsigned long long)gridDim.x * blockDim.x) {
+        for (unsigned long long i = (unsigned long long)blk * blockDim.x + threadIdx.x; i < e;
+             i += (unsigned long long)nblk * blockDim.x) {
             size_t b = bit_index(B[i], cd, g.res);
             atomicAnd(vb.bitmap + (b >> 5), ~(1u << (b & 31)));
         }
         return;
     }
     const unsigned long long n_tiles = (N1 + kTile - 1) / kTile;
-    for (unsigned long long t = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
-         t <= n_tiles && t < max_tiles; t += (unsigned long long)gridDim.x * blockDim.x) {
+    for (unsigned long long t = (unsigned long long)blk * blockDim.x + threadIdx.x;
+         t <= n_tiles && t < max_tiles; t += (unsigned long long)nblk * blockDim.x) {
         const unsigned long long d = t * kTile < N1 ? t * kTile : N1;
         splits[t] = merge_path(A, N0, B, e, d);
     }
+}
+
+template <typename K>
+__global__ void __launch_bounds__(256) k_merge_partition(DeviceCtl* __restrict__ ctl, Geom g,
+                                                          VolumeBuffers vb, MergeInputs<K> in,
+                                                          unsigned long long* __restrict__ splits,
+                                                          unsigned int max_tiles) {
+    merge_partition_body<K>(ctl, g, vb, in, splits, max_tiles, blockIdx.x, gridDim.x);
 }
 
 // four consecutive keys, streamed (p 16-byte aligned for 32-bit keys,
@@ -442,11 +461,11 @@ __device__ __forceinline__ void st4(uint64_t* p, const uint64_t (&k)[4]) {
 }
 
 template <bool kU16, typename K>
-__global__ void __launch_bounds__(kMergeThreads) k_merge_update(DeviceCtl* __restrict__ ctl, Geom g,
-                                                                VolumeBuffers vb, MergeInputs<K> in,
-                                                                const void* __restrict__ depth,
-                                                                const unsigned long long* __restrict__ splits,
-                                                                const FrameConst fc) {
+__device__ __forceinline__ void merge_update_body(DeviceCtl* __restrict__ ctl, const Geom& g,
+                                                  const VolumeBuffers& vb, const MergeInputs<K>& in,
+                                                  const void* __restrict__ depth,
+                                                  const unsigned long long* __restrict__ splits,
+                                                  const FrameConst& fc, unsigned int blk, unsigned int nblk) {
     constexpr int kTile = merge_tile<K>();
     constexpr int kItems = kTile / kMergeThreads;
     __shared__ __align__(16) K sA_k[kTile + 8];
@@ -470,7 +489,7 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_update(DeviceCtl* __res
 #pragma unroll
     for (int i = 0; i < 16; ++i) w2c[i] = fc.world_to_clip.m[i];
 
-    for (unsigned long long t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+    for (unsigned long long t = blk; t < n_tiles; t += nblk) {
         const unsigned long long d0 = t * kTile;
         const unsigned long long d1 = (d0 + kTile < N1) ? d0 + kTile : N1;
         const int len = (int)(d1 - d0);
@@ -699,7 +718,7 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_update(DeviceCtl* __res
     if (threadIdx.x == 0) {
         __threadfence();
         unsigned int prev = atomicAdd(&ctl->tile_counter[7], 1u);
-        if (prev == gridDim.x - 1) {
+        if (prev == nblk - 1) {
             ctl->n[out] = N1;
             ctl->cur = out;
             ctl->tile_counter[7] = 0u;
@@ -711,6 +730,15 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_update(DeviceCtl* __res
             __threadfence();
         }
     }
+}
+
+template <bool kU16, typename K>
+__global__ void __launch_bounds__(kMergeThreads) k_merge_update(DeviceCtl* __restrict__ ctl, Geom g,
+                                                                VolumeBuffers vb, MergeInputs<K> in,
+                                                                const void* __restrict__ depth,
+                                                                const unsigned long long* __restrict__ splits,
+                                                                const FrameConst fc) {
+    merge_update_body<kU16, K>(ctl, g, vb, in, depth, splits, fc, blockIdx.x, gridDim.x);
 }
 
 // inserts: keep keys not yet in the volume (flat_map::insert keeps resident
@@ -757,6 +785,44 @@ __global__ void k_bitmap_from_keys(const DeviceCtl* __restrict__ ctl, Geom g, Vo
         const size_t b = bit_index(keys[i], cd, g.res);
         atomicOr(vb.bitmap + (b >> 5), 1u << (b & 31));
     }
+}
+
+// ---- batched: one frame for each volume of a batch, one launch per stage;
+// each volume's CTAs run the single-volume kernel body on its arguments
+__global__ void k_frame_setup_batch(const FuseJob* __restrict__ jobs, int n) {
+    if ((int)blockIdx.x < n && threadIdx.x == 0) {
+        DeviceCtl* ctl = jobs[blockIdx.x].ctl;
+        ctl->n_new = 0u;
+        ctl->excluded_key = 0ull;
+    }
+}
+
+template <typename K>
+__global__ void __launch_bounds__(kEmitThreads) k_splat_emit_batch(const FuseJob* __restrict__ jobs, BlockMap m) {
+    const int v = block_owner(m, blockIdx.x);
+    const FuseJob& j = jobs[v];
+    const unsigned int b0 = m.first[v];
+    splat_emit_body<true, K>(j.ctl, j.g, j.depth, j.vb.bitmap, (K*)j.vb.new_keys, (unsigned int)j.vb.new_cap, j.fc,
+                             blockIdx.x - b0, m.first[v + 1] - b0);
+}
+
+template <typename K>
+__global__ void __launch_bounds__(256) k_merge_partition_batch(const FuseJob* __restrict__ jobs, BlockMap m) {
+    const int v = block_owner(m, blockIdx.x);
+    const FuseJob& j = jobs[v];
+    const unsigned int b0 = m.first[v];
+    const MergeInputs<K> in{(const K*)j.vb.new_keys, nullptr, nullptr, &j.ctl->n_new, true};
+    merge_partition_body<K>(j.ctl, j.g, j.vb, in, j.vb.splits, j.max_tiles, blockIdx.x - b0, m.first[v + 1] - b0);
+}
+
+template <typename K>
+__global__ void __launch_bounds__(kMergeThreads) k_merge_update_batch(const FuseJob* __restrict__ jobs, BlockMap m) {
+    const int v = block_owner(m, blockIdx.x);
+    const FuseJob& j = jobs[v];
+    const unsigned int b0 = m.first[v];
+    const MergeInputs<K> in{(const K*)j.vb.new_keys, nullptr, nullptr, &j.ctl->n_new, true};
+    merge_update_body<true, K>(j.ctl, j.g, j.vb, in, j.depth, j.vb.splits, j.fc, blockIdx.x - b0,
+                               m.first[v + 1] - b0);
 }
 
 __global__ void k_reset_new(DeviceCtl* ctl) {
@@ -835,6 +901,24 @@ cudaError_t integrate_enqueue(DeviceCtl* ctl, const Geom& g, VolumeBuffers& vb, 
         return integrate_enqueue_t<uint64_t>(ctl, g, vb, ss, depth_dev, depth_u16, cam, world_to_eye, ls, st,
                                              events);
     return integrate_enqueue_t<uint32_t>(ctl, g, vb, ss, depth_dev, depth_u16, cam, world_to_eye, ls, st, events);
+}
+
+template <typename K>
+static cudaError_t integrate_batch_t(const FuseJob* jobs, int n, int passes, const FuseMaps& m, cudaStream_t st) {
+    k_frame_setup_batch<<<n, 32, 0, st>>>(jobs, n);
+    k_splat_emit_batch<K><<<m.splat.grid, kEmitThreads, 0, st>>>(jobs, m.splat);
+    cudaError_t e = sort_batch_enqueue(jobs, n, sizeof(K), passes, m.hist, m.pass, st);
+    if (e != cudaSuccess) return e;
+    k_merge_partition_batch<K><<<m.partition.grid, 256, 0, st>>>(jobs, m.partition);
+    k_merge_update_batch<K><<<m.merge.grid, kMergeThreads, 0, st>>>(jobs, m.merge);
+    return cudaGetLastError();
+}
+
+cudaError_t integrate_batch_enqueue(const FuseJob* jobs, int n, int key_bytes, int passes, const FuseMaps& maps,
+                                    cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    if (key_bytes == 8) return integrate_batch_t<uint64_t>(jobs, n, passes, maps, st);
+    return integrate_batch_t<uint32_t>(jobs, n, passes, maps, st);
 }
 
 cudaError_t bitmap_rebuild_enqueue(const DeviceCtl* ctl, const Geom& g, const VolumeBuffers& vb,

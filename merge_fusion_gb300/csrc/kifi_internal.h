@@ -90,6 +90,58 @@ cudaError_t insert_merge_enqueue(DeviceCtl* ctl, const Geom& g, VolumeBuffers& v
 cudaError_t bitmap_rebuild_enqueue(const DeviceCtl* ctl, const Geom& g, const VolumeBuffers& vb,
                                    const LaunchShape& ls, cudaStream_t st);
 
+// ------------------------------------------------------------- batches
+// A batched launch runs one stage for several volumes (or ICP frame pairs)
+// at once: volume v owns the CTAs [first[v], first[v+1]) of the grid and
+// reads its arguments from a device table.
+struct BlockMap {
+    const unsigned int* first;  // device, n + 1 entries; first[n] = grid
+    int n;
+    unsigned int grid;          // the launch's CTAs (known on the host)
+};
+
+// One volume's frame in a batched fusion launch: the arguments of the
+// single-volume kernels.  Depth frames are uint16 millimetres.
+struct FuseJob {
+    DeviceCtl* ctl;
+    Geom g;
+    VolumeBuffers vb;
+    SortScratch ss;
+    const void* depth;
+    FrameConst fc;
+    unsigned int max_tiles;  // merge-path split slots of the volume
+};
+
+#ifdef __CUDACC__
+// the volume that owns CTA b of a batched launch
+__device__ __forceinline__ int block_owner(const BlockMap& m, unsigned int b) {
+    int lo = 0, hi = m.n;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (m.first[mid] <= b) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+#endif
+
+// The CTA shares of one batched fusion step, one map per stage; every
+// volume of the batch has the same key width.
+struct FuseMaps {
+    BlockMap splat, hist, pass, partition, merge;
+};
+
+// Enqueues Integrator::Integrate of one frame for each of the n volumes of
+// `jobs` (a device table) on `st`: one launch per stage for all of them.
+// key_bytes: the volumes' key width; passes: digit passes of the sort.
+// the sort of every volume's new keys (FuseJob::vb.new_keys, count in ctl->n_new)
+cudaError_t sort_batch_enqueue(const FuseJob* jobs, int n, int key_bytes, int passes, const BlockMap& hist,
+                               const BlockMap& pass, cudaStream_t st);
+// the look-back limits every sort applies (kifi_sort_set_fault_injection)
+void sort_limits(SortScratch* s);
+cudaError_t integrate_batch_enqueue(const FuseJob* jobs, int n, int key_bytes, int passes, const FuseMaps& maps,
+                                    cudaStream_t st);
+
 // ---------------------------------------------------------------- mesher
 struct MeshCounts {
     unsigned long long n_verts;
@@ -163,6 +215,30 @@ struct IcpState {
 };
 
 cudaError_t icp_init_device();
+// One ICP frame pair of a batched alignment: the arguments of the
+// single-pair kernels.
+struct IcpJob {
+    IcpArgs a;
+    IcpState* st;
+    Mat4 guess;
+};
+// `iterations` AlignSteps of the n pairs of `jobs` (a device table), one
+// launch per step for all of them; pair v's CTAs are map.first[v] ..
+// map.first[v+1] - 1, one per association tile.
+cudaError_t icp_align_batch_enqueue(const IcpJob* jobs, int n, const BlockMap& map, int iterations,
+                                    cudaStream_t stream);
+// Back-projection of one frame per pair into its target (the next frame's
+// ICP target), for the n entries of `jobs` (device table).
+struct BackprojectJob {
+    const void* depth;  // uint16 millimetres
+    int width, height;
+    float fl_inv_x, fl_inv_y, pp_x, pp_y;
+    Mat4 e2w;
+    float4* out;
+};
+cudaError_t backproject_batch_enqueue(const BackprojectJob* jobs, int n, const BlockMap& map, cudaStream_t st);
+// CTAs of one frame pair's association (one per tile)
+int icp_tiles(int width, int height);
 cudaError_t icp_align_enqueue(const IcpArgs& a, IcpState* st, const Mat4& guess, int iterations,
                               int ctas, cudaStream_t stream);
 cudaError_t backproject_enqueue(const void* depth, bool u16, const kifi_camera& cam,

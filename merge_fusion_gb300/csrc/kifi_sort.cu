@@ -46,23 +46,25 @@ constexpr unsigned long long kFlagAggregate = 1ull << 30;
 constexpr unsigned long long kFlagInclusive = 2ull << 30;
 constexpr unsigned long long kCountMask = (1ull << 30) - 1;
 
-__global__ void k_sort_prepare(SortScratch s, int passes) {
+__device__ __forceinline__ void sort_prepare_body(const SortScratch& s, int passes) {
     for (int i = threadIdx.x; i < passes * kRadix; i += blockDim.x) s.hist[i] = 0u;
     if (threadIdx.x < passes) s.tile_counter[threadIdx.x] = s.first_tile;
     if (threadIdx.x == 0) *s.epoch += 1ull;
 }
 
+__global__ void k_sort_prepare(SortScratch s, int passes) { sort_prepare_body(s, passes); }
+
 // all `passes` digit histograms in one read of the keys
 template <typename K>
-__global__ void __launch_bounds__(kThreads) k_sort_histogram(const K* __restrict__ keys,
-                                                             const unsigned int* __restrict__ n_ptr,
-                                                             SortScratch s, int passes) {
+__device__ __forceinline__ void sort_histogram_body(const K* __restrict__ keys, const unsigned int* __restrict__ n_ptr,
+                                                    const SortScratch& s, int passes, unsigned int blk,
+                                                    unsigned int nblk) {
     __shared__ unsigned int h[kSortMaxPasses][kRadix];
     for (int i = threadIdx.x; i < passes * kRadix; i += kThreads) (&h[0][0])[i] = 0u;
     __syncthreads();
     const size_t n = min((size_t)*n_ptr, s.max_n);
-    for (size_t i = (size_t)blockIdx.x * kThreads + threadIdx.x; i < n;
-         i += (size_t)gridDim.x * kThreads) {
+    for (size_t i = (size_t)blk * kThreads + threadIdx.x; i < n;
+         i += (size_t)nblk * kThreads) {
         const K k = keys[i];
         for (int p = 0; p < passes; ++p) atomicAdd(&h[p][(unsigned int)(k >> (8 * p)) & 0xffu], 1u);
     }
@@ -71,6 +73,13 @@ __global__ void __launch_bounds__(kThreads) k_sort_histogram(const K* __restrict
         unsigned int c = (&h[0][0])[i];
         if (c) atomicAdd(&s.hist[i], c);
     }
+}
+
+template <typename K>
+__global__ void __launch_bounds__(kThreads) k_sort_histogram(const K* __restrict__ keys,
+                                                             const unsigned int* __restrict__ n_ptr,
+                                                             SortScratch s, int passes) {
+    sort_histogram_body<K>(keys, n_ptr, s, passes, blockIdx.x, gridDim.x);
 }
 
 __device__ __forceinline__ unsigned int lanemask_lt() {
@@ -89,12 +98,10 @@ __device__ __forceinline__ void st_volatile_u64(unsigned long long* p, unsigned 
 }
 
 template <bool kWithValues, typename K>
-__global__ void __launch_bounds__(kThreads) k_sort_pass(const K* __restrict__ keys_in,
-                                                        K* __restrict__ keys_out,
-                                                        const uint32_t* __restrict__ vals_in,
-                                                        uint32_t* __restrict__ vals_out,
-                                                        const unsigned int* __restrict__ n_ptr,
-                                                        SortScratch s, int pass) {
+__device__ __forceinline__ void sort_pass_body(const K* __restrict__ keys_in, K* __restrict__ keys_out,
+                                               const uint32_t* __restrict__ vals_in, uint32_t* __restrict__ vals_out,
+                                               const unsigned int* __restrict__ n_ptr, const SortScratch& s,
+                                               int pass) {
     __shared__ unsigned int warp_hist[kWarps][kRadix + 1];  // last column: out-of-range keys
     __shared__ unsigned int digit_base[kRadix];
     __shared__ unsigned int pass_offset[kRadix];
@@ -223,6 +230,43 @@ __global__ void __launch_bounds__(kThreads) k_sort_pass(const K* __restrict__ ke
     }
 }
 
+template <bool kWithValues, typename K>
+__global__ void __launch_bounds__(kThreads) k_sort_pass(const K* __restrict__ keys_in,
+                                                        K* __restrict__ keys_out,
+                                                        const uint32_t* __restrict__ vals_in,
+                                                        uint32_t* __restrict__ vals_out,
+                                                        const unsigned int* __restrict__ n_ptr,
+                                                        SortScratch s, int pass) {
+    sort_pass_body<kWithValues, K>(keys_in, keys_out, vals_in, vals_out, n_ptr, s, pass);
+}
+
+// ---- batched: every volume of a batch sorts its frame's new keys, one
+// launch per stage; a volume's CTAs take its tiles from its own counter
+__global__ void k_sort_prepare_batch(const FuseJob* __restrict__ jobs, int n, int passes) {
+    if ((int)blockIdx.x < n) sort_prepare_body(jobs[blockIdx.x].ss, passes);
+}
+
+template <typename K>
+__global__ void __launch_bounds__(kThreads) k_sort_histogram_batch(const FuseJob* __restrict__ jobs, BlockMap m,
+                                                                   int passes) {
+    const int v = block_owner(m, blockIdx.x);
+    const FuseJob& j = jobs[v];
+    const unsigned int b0 = m.first[v];
+    sort_histogram_body<K>((const K*)j.vb.new_keys, &j.ctl->n_new, j.ss, passes, blockIdx.x - b0,
+                           m.first[v + 1] - b0);
+}
+
+template <typename K>
+__global__ void __launch_bounds__(kThreads) k_sort_pass_batch(const FuseJob* __restrict__ jobs, BlockMap m,
+                                                              int pass) {
+    const FuseJob& j = jobs[block_owner(m, blockIdx.x)];
+    K* keys = (K*)j.vb.new_keys;
+    K* alt = (K*)j.ss.alt_keys;
+    // passes alternate between the new-key buffer and the sort's spare one
+    sort_pass_body<false, K>(pass & 1 ? alt : keys, pass & 1 ? keys : alt, nullptr, nullptr, &j.ctl->n_new, j.ss,
+                             pass);
+}
+
 // process-wide look-back limits (kifi_sort_set_fault_injection)
 std::atomic<unsigned long long> g_spin_limit{kSpinLimit};
 std::atomic<unsigned int> g_first_tile{0u};
@@ -283,6 +327,20 @@ static cudaError_t sort_t(K* keys, int passes, uint32_t* vals, const unsigned in
     return cudaGetLastError();
 }
 
+void sort_limits(SortScratch* s) {
+    s->spin_limit = g_spin_limit.load();
+    s->first_tile = g_first_tile.load();
+}
+
+template <typename K>
+static cudaError_t sort_batch_t(const FuseJob* jobs, int n, int passes, const BlockMap& hist, const BlockMap& pass,
+                                unsigned int hist_ctas, unsigned int pass_ctas, cudaStream_t st) {
+    k_sort_prepare_batch<<<n, 256, 0, st>>>(jobs, n, passes);
+    k_sort_histogram_batch<K><<<hist_ctas, kThreads, 0, st>>>(jobs, hist, passes);
+    for (int p = 0; p < passes; ++p) k_sort_pass_batch<K><<<pass_ctas, kThreads, 0, st>>>(jobs, pass, p);
+    return cudaGetLastError();
+}
+
 // Sorts keys[0..*n_dev) (and vals, when not null) in place.  *n_dev must not
 // exceed s.max_n.  An even number of passes leaves the result in the
 // caller's buffers.
@@ -300,6 +358,12 @@ cudaError_t sort_keys(void* keys, int key_bytes, int key_bits, uint32_t* vals, c
         return sort_t<uint64_t>((uint64_t*)keys, passes > kSortMaxPasses ? kSortMaxPasses : passes, vals, n_dev, s,
                                 status, grid_ctas, st);
     return sort_t<uint32_t>((uint32_t*)keys, passes > 4 ? 4 : passes, vals, n_dev, s, status, grid_ctas, st);
+}
+
+cudaError_t sort_batch_enqueue(const FuseJob* jobs, int n, int key_bytes, int passes, const BlockMap& hist,
+                               const BlockMap& pass, cudaStream_t st) {
+    if (key_bytes == 8) return sort_batch_t<uint64_t>(jobs, n, passes, hist, pass, hist.grid, pass.grid, st);
+    return sort_batch_t<uint32_t>(jobs, n, passes, hist, pass, hist.grid, pass.grid, st);
 }
 
 }  // namespace kifi
