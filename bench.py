@@ -8,8 +8,10 @@ noise 0.0012 + 0.0019 (z-0.4)^2 m) along a smooth trajectory; volume res
 given pose (splat + sort + merge/TSDF update) and tracked by 15 ICP
 iterations against the previous frame; the mesh (vertices + indices) is
 extracted every 10 frames.  One step is one mesh period: ten frames and the
-mesh that ends it.  Before the warm-up, `--prefill` frames build the
-resident volume so that the timed frames run at a realistic size.
+mesh that ends it.  The sequence has 300 frames; a run that needs more
+plays it forward, then back (consecutive frames stay adjacent for ICP).
+Before the warm-up, `--prefill` frames build the resident volume so that the
+timed frames run at a realistic size.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -46,6 +48,14 @@ W, H, F_PX = 640, 480, 585.0
 RES, SIDE, TRUNC = 1024, 4.096, 0.02
 ICP_ITERS, MESH_EVERY = 15, 10
 FRAMES_PER_STEP = MESH_EVERY  # a step is one mesh period
+SEQ_FRAMES = 300  # the sequence's length; longer runs play it forward, then back
+
+
+def playback(t):
+    """Sequence frame of the t-th frame fused: 0, 1, .., 299, 298, .., 1, 0, 1, .."""
+    period = 2 * SEQ_FRAMES - 2
+    r = t % period
+    return r if r < SEQ_FRAMES else period - r
 SEED = 0
 CAM = (W, H, F_PX, F_PX, W / 2.0, H / 2.0, 0.4, 4.0)
 WORKLOAD = ("room 4x3x4 m, 40 boxes + 20 spheres, 640x480 uint16 depth, res 1024 x 4 mm, trunc 2 cm, "
@@ -375,15 +385,19 @@ def run_gpu(args, rank, world, local):
     lib = _lib.load()
     K, Wu, Fp, FS = args.steps, args.warmup, args.prefill, FRAMES_PER_STEP
     KF = K * FS
-    n_frames = Fp + (Wu + 2 * K) * FS + 1
+    n_frames = Fp + (Wu + 2 * K) * FS + 1  # frames fused, in playback order
     # independent scene per rank (replicas; weak scaling)
     seed = rank_seed(rank)
-    frames, poses = scenes.render_room_torch(n_frames, seed=seed, device="cuda")
+    seq_frames, seq_poses = scenes.render_room_torch(SEQ_FRAMES, seed=seed, device="cuda")
     torch.cuda.synchronize()
-    frames_host = frames.cpu().numpy().view(np.uint16)
+    order = [playback(t) for t in range(n_frames)]
+    frames = [seq_frames[j] for j in order]  # device views, in the order they are fused
+    poses = [seq_poses[j] for j in order]
+    seq_host = seq_frames.cpu().numpy().view(np.uint16)
     t0 = Fp + Wu * FS
     pinned = torch.empty((KF, H, W), dtype=torch.int16).pin_memory()
-    pinned.copy_(frames[t0 + KF:t0 + 2 * KF].cpu())
+    for j in range(KF):
+        pinned[j].copy_(frames[t0 + KF + j].cpu())
     w2e = [scenes.kifi_matrix(np.linalg.inv(p)) for p in poses]
     sms = torch.cuda.get_device_properties(local).multi_processor_count
 
@@ -622,7 +636,8 @@ def run_gpu(args, rank, world, local):
     cfg = workload_config(Fp, FS)
     cfg.update({"resident_voxels_start": n_start, "resident_voxels_end": int(n1[-1]) if m else None,
                 "roofline_frames": "the last %d timed frames (the device frame log's length)" % m,
-                "trajectory_frames": n_frames,
+                "sequence_frames": SEQ_FRAMES, "frames_fused": n_frames,
+                "playback": "frames 0-299 forward, then back (%d frames fused in all)" % n_frames,
                 "parallelism": "replicas" if world > 1 else "single"})
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
@@ -648,6 +663,7 @@ def run_gpu(args, rank, world, local):
     }
     line["clocks"] = clocks.summary()
     if resident is not None:
+        frames_host = seq_host[order[:t0 + KF + 1]]  # the playback order, up to the timed frames
         v, kind, nfr, tmesh = cpu_frames(frames_host, poses, t0, KF, args.cpu_seconds, resident)
         hc = host_cpu()
         cb = {"value": v, "unit": UNIT, "cores": 1, "kind": kind,

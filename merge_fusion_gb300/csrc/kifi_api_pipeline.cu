@@ -167,16 +167,17 @@ kifi_status mesh_poll(kifi_pipeline* p, bool wait) {
             ++p->meshes;
             return KIFI_OK;
         }
+        // half again as much: a growing volume's next meshes still fit
         if (nv > p->mverts_cap) {
             if (p->mverts) KIFI_CUDA(cudaFreeAsync(p->mverts, p->ms));
             p->mverts = nullptr;
-            p->mverts_cap = nv + nv / 4;
+            p->mverts_cap = nv + nv / 2;
             KIFI_CUDA(cudaMallocAsync((void**)&p->mverts, (p->mverts_cap + kPad) * 12, p->ms));
         }
         if (ni > p->midx_cap) {
             if (p->midx) KIFI_CUDA(cudaFreeAsync(p->midx, p->ms));
             p->midx = nullptr;
-            p->midx_cap = ni + ni / 4;
+            p->midx_cap = ni + ni / 2;
             KIFI_CUDA(cudaMallocAsync((void**)&p->midx, (p->midx_cap + kPad) * 4, p->ms));
         }
         ++p->mesh_reemits;

@@ -114,22 +114,7 @@ __device__ __forceinline__ void sort_pass_body(const K* __restrict__ keys_in, K*
     const unsigned long long gen = (*s.epoch & 0xffffffffull) << 32;
     unsigned long long* lb = s.lookback + (size_t)pass * s.max_tiles * kRadix;
 
-    // exclusive scan of this pass's global digit histogram (256 entries)
-    {
-        unsigned int c = s.hist[pass * kRadix + threadIdx.x];
-        unsigned int x = c;
-        for (int o = 1; o < 32; o <<= 1) {
-            unsigned int y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= o) x += y;
-        }
-        __shared__ unsigned int wsum[kWarps];
-        if (lane == 31) wsum[warp] = x;
-        __syncthreads();
-        unsigned int before = 0;
-        for (int w = 0; w < warp; ++w) before += wsum[w];
-        pass_offset[threadIdx.x] = before + x - c;
-    }
-
+    bool have_offsets = false;
     for (;;) {
         __syncthreads();
         if (threadIdx.x == 0) tile_id = atomicAdd(&s.tile_counter[pass], 1u);
@@ -137,7 +122,23 @@ __device__ __forceinline__ void sort_pass_body(const K* __restrict__ keys_in, K*
             (&warp_hist[0][0])[i] = 0u;
         __syncthreads();
         const unsigned int tile = tile_id;
-        if (tile >= n_tiles) break;
+        if (tile >= n_tiles) break;  // (CTAs without a tile leave before any other work)
+        if (!have_offsets) {
+            // exclusive scan of this pass's global digit histogram (256 entries)
+            const unsigned int c = s.hist[pass * kRadix + threadIdx.x];
+            unsigned int x = c;
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned int y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            __shared__ unsigned int wsum[kWarps];
+            if (lane == 31) wsum[warp] = x;
+            __syncthreads();
+            unsigned int before = 0;
+            for (int w = 0; w < warp; ++w) before += wsum[w];
+            pass_offset[threadIdx.x] = before + x - c;
+            have_offsets = true;  // read after the next barrier, before the scatter
+        }
 
         const unsigned int base = tile * kTile + warp * (32 * kKeysPerThread);
         K k[kKeysPerThread];
