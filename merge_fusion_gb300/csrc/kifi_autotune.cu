@@ -168,7 +168,8 @@ extern "C" kifi_status kifi_volume_autotune(kifi_volume* v, const void* depth_de
         // beside a tracking stream only short-lived grids (tracking_launch_shape)
         const bool tr = v->tracking_grids;
         const std::vector<int> splat_m = tr ? std::vector<int>{8, 16, 32} : std::vector<int>{1, 2, 4, 8};
-        const std::vector<int> sort_m = tr ? std::vector<int>{8, 16, 32} : std::vector<int>{2, 4, 8};
+        // a sort pass's CTAs leave as soon as the tiles run out, so small grids are candidates too
+        const std::vector<int> sort_m = tr ? std::vector<int>{2, 4, 8, 16, 32} : std::vector<int>{1, 2, 4, 8};
         const std::vector<int> merge_m = tr ? std::vector<int>{16, 32, 64} : std::vector<int>{1, 2};
         for (int m : splat_m) {  // splat + emit (stage 0)
             LaunchShape c = best;

@@ -168,12 +168,23 @@ __device__ __forceinline__ unsigned int vertex_axes(const Cube& c) {
     return axes;
 }
 
+// Voxel::Distance(v) < 0 without the division where its sign is certain:
+// for 2^-100 <= |x| and 2^-100 <= |w| <= 2^24 the quotient x / w is a
+// normal non-zero float (|x / w| >= 2^-124), so it is negative exactly when
+// x and w differ in sign.  Zeros, NaNs, infinities and the rest of the
+// range take the reference's division.
+__device__ __forceinline__ bool dist_negative(float2 v) {
+    const float ax = fabsf(v.x), aw = fabsf(v.y);
+    if (ax >= 0x1p-100f && aw >= 0x1p-100f && aw <= 0x1p24f) return (v.x < 0.0f) != (v.y < 0.0f);
+    return vdist(v) < 0.0f;
+}
+
 // marching-cubes case with the reference's corner bit order (Mesher.cpp:191-199)
 __device__ __forceinline__ int cube_case(const Cube& c) {
-    return (vdist(c.val[0]) < 0.0f) << 2 | (vdist(c.val[1]) < 0.0f) << 3 |
-           (vdist(c.val[2]) < 0.0f) << 6 | (vdist(c.val[3]) < 0.0f) << 7 |
-           (vdist(c.val[4]) < 0.0f) << 1 | (vdist(c.val[5]) < 0.0f) << 0 |
-           (vdist(c.val[6]) < 0.0f) << 5 | (vdist(c.val[7]) < 0.0f) << 4;
+    return dist_negative(c.val[0]) << 2 | dist_negative(c.val[1]) << 3 |
+           dist_negative(c.val[2]) << 6 | dist_negative(c.val[3]) << 7 |
+           dist_negative(c.val[4]) << 1 | dist_negative(c.val[5]) << 0 |
+           dist_negative(c.val[6]) << 5 | dist_negative(c.val[7]) << 4;
 }
 
 // flags per voxel: bits 0-2 vertex axes, bits 8-15 index count, 16-23 case
