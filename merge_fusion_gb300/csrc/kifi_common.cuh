@@ -174,6 +174,7 @@ struct FrameConst {
     int width, height;
     int z_bounded;             // |clip z| <= 1e18 for every voxel centre of the volume
     int fast_uv;               // frame small enough for the reciprocal fast path
+    float neg_zero;            // -0.0f, a value the device code cannot see at compile time
 };
 
 KIFI_HD FrameConst make_frame_const(const kifi_camera& cam, const Mat4& world_to_eye, int res) {
@@ -191,6 +192,7 @@ KIFI_HD FrameConst make_frame_const(const kifi_camera& cam, const Mat4& world_to
     f.height = cam.height;
     f.z_bounded = 0;
     f.fast_uv = (cam.width <= 4096 && cam.height <= 4096) ? 1 : 0;
+    f.neg_zero = -0.0f;
     return f;
 }
 

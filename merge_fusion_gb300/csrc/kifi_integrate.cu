@@ -244,27 +244,69 @@ __global__ void __launch_bounds__(kEmitThreads) k_splat_emit(DeviceCtl* __restri
     splat_emit_body<kU16, K>(ctl, g, depth, bitmap, new_keys, new_cap, fc, blockIdx.x, gridDim.x);
 }
 
+// Packed float pairs (f32x2): one instruction, each half rounded as the
+// scalar __fmul_rn / __fadd_rn of that half.  A product is fma(a, b, -0)
+// with the -0 a runtime value: the rounded product for every input, and
+// not fused by ptxas into the add that consumes it (a packed multiply
+// would be).
+__device__ __forceinline__ unsigned long long f2(float lo, float hi) {
+    unsigned long long d;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(lo), "f"(hi));
+    return d;
+}
+__device__ __forceinline__ void unf2(unsigned long long v, float& lo, float& hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ unsigned long long f2_mul(unsigned long long a, unsigned long long b,
+                                                     unsigned long long neg_zero) {
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(neg_zero));
+    return d;
+}
+__device__ __forceinline__ unsigned long long f2_add(unsigned long long a, unsigned long long b) {
+    unsigned long long d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
 // UpdateVoxels for one voxel (Integrator.cpp:273-322 for one SSE lane),
 // split in two: the projection and range tests give the depth pixel the
 // voxel reads (or -1 when it is not updated) and its clip w; apply_depth
 // then folds that pixel's depth into the voxel.  Callers project several
 // voxels before reading any depth, so the reads are in flight together.
+//
+// The projection of VoxelCenter(index) (Volume.cpp:75-78) through
+// worldToClip: rows 0, 1 and 3 in mat_vec's order for two voxels at once
+// (f32x2); row 2 is formed per voxel only when needed (pixel_of_clip).
+// The w lane of the centre is 1 * 1 + 0 = 1, and w2c[12 + i] * 1 is
+// w2c[12 + i] exactly.
 template <typename K>
-__device__ __forceinline__ int project_voxel(K key, const FrameConst& fc, const float (&w2c)[16],
-                                             const Geom& g, float& w_out) {
+__device__ __forceinline__ void clip_pair(K ka, K kb, const float (&w2c)[16], const Geom& g,
+                                          unsigned long long nz, float (&c)[2][3], float (&xyw)[2][3]) {
     const Codec<K> cd(g.kb);
-    // VoxelCenter: index * (vlen, vlen, vlen, 1) + (off, off, off, 0)
-    float c[4];
-    c[0] = fadd(fmul((float)cd.x(key), g.vlen), g.center_off);
-    c[1] = fadd(fmul((float)cd.y(key), g.vlen), g.center_off);
-    c[2] = fadd(fmul((float)cd.z(key), g.vlen), g.center_off);
-    c[3] = 1.0f;  // 1 * 1 + 0
-    // rows 0, 1, 3 of worldToClip * c (mat_vec's order); row 2 below
-    auto row = [&](int i) {
-        return fadd(fadd(fmul(w2c[i], c[0]), fmul(w2c[4 + i], c[1])),
-                    fadd(fmul(w2c[8 + i], c[2]), fmul(w2c[12 + i], c[3])));
-    };
-    const float x = row(0), y = row(1), w = row(3);
+    const unsigned long long vlen = f2(g.vlen, g.vlen), off = f2(g.center_off, g.center_off);
+    unsigned long long cc[3];
+    cc[0] = f2_add(f2_mul(f2((float)cd.x(ka), (float)cd.x(kb)), vlen, nz), off);
+    cc[1] = f2_add(f2_mul(f2((float)cd.y(ka), (float)cd.y(kb)), vlen, nz), off);
+    cc[2] = f2_add(f2_mul(f2((float)cd.z(ka), (float)cd.z(kb)), vlen, nz), off);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) unf2(cc[j], c[0][j], c[1][j]);
+    const int rows[3] = {0, 1, 3};
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        const int i = rows[r];
+        const unsigned long long a = f2_add(f2_mul(f2(w2c[i], w2c[i]), cc[0], nz),
+                                            f2_mul(f2(w2c[4 + i], w2c[4 + i]), cc[1], nz));
+        const unsigned long long b =
+            f2_add(f2_mul(f2(w2c[8 + i], w2c[8 + i]), cc[2], nz), f2(w2c[12 + i], w2c[12 + i]));
+        unf2(f2_add(a, b), xyw[0][r], xyw[1][r]);
+    }
+}
+
+// The depth pixel a voxel reads (or -1) from its clip x, y, w (and its
+// centre c, for row 2 when needed).
+__device__ __forceinline__ int pixel_of_clip(float x, float y, float w, const float (&c)[3], const FrameConst& fc,
+                                             const float (&w2c)[16], float& w_out) {
     // lane w: (w/w) * 0 + 0 lies in [-FLT_MAX, FLT_MAX) iff w/w is finite,
     // i.e. iff w is finite and non-zero (w/w is then exactly 1).
     if (!(isfinite(w) && w != 0.0f)) return -1;
@@ -272,7 +314,7 @@ __device__ __forceinline__ int project_voxel(K key, const FrameConst& fc, const 
     // host has bounded |z| by 1e18 over the whole volume (fc.z_bounded), any
     // |w| >= 1e-18 keeps the quotient finite and z need not be formed.
     if (!(fc.z_bounded && fabsf(w) >= 1e-18f)) {
-        const float z = row(2);
+        const float z = fadd(fadd(fmul(w2c[2], c[0]), fmul(w2c[6], c[1])), fadd(fmul(w2c[10], c[2]), w2c[14]));
         if (!isfinite(z)) return -1;
         if (!(fabsf(z) <= 1e18f && fabsf(w) >= 1e-18f) && !isfinite(fdiv(z, w))) return -1;
     }
@@ -331,10 +373,17 @@ __device__ __forceinline__ void update4(const K (&key)[4], float2 (&val)[4],
                                         const void* depth) {
     int ix[4];
     float w[4], d[4];
+    const unsigned long long nz = f2(fc.neg_zero, fc.neg_zero);
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-        w[q] = 0.0f;
-        ix[q] = pos[q] < upd_end ? project_voxel<K>(key[q], fc, w2c, g, w[q]) : -1;
+    for (int h = 0; h < 2; ++h) {
+        float c[2][3], xyw[2][3];
+        clip_pair<K>(key[2 * h], key[2 * h + 1], w2c, g, nz, c, xyw);
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const int q = 2 * h + j;
+            w[q] = 0.0f;
+            ix[q] = pos[q] < upd_end ? pixel_of_clip(xyw[j][0], xyw[j][1], xyw[j][2], c[j], fc, w2c, w[q]) : -1;
+        }
     }
 #pragma unroll
     for (int q = 0; q < 4; ++q) d[q] = ix[q] >= 0 ? load_depth(depth, (size_t)ix[q], kU16) : 0.0f;
