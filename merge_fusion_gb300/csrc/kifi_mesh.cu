@@ -187,6 +187,38 @@ __device__ __forceinline__ int cube_case(const Cube& c) {
            dist_negative(c.val[6]) << 5 | dist_negative(c.val[7]) << 4;
 }
 
+// One voxel's classification from its cube (live: the voxel is in [0, n-2]
+// with a non-zero weight, and c holds its corners): flags per voxel -- bits
+// 0-2 vertex axes, bits 8-15 index count, 16-23 case -- the packed
+// (index count, vertex count) for the scan, and, for a voxel with output,
+// its +y, +z and +yz lookups for emission.
+template <bool kTris>
+__device__ __forceinline__ void classify_voxel(const Cube& c, bool live, unsigned int i, const uint64_t* s_mc,
+                                               unsigned int* __restrict__ flags,
+                                               unsigned long long* __restrict__ counts,
+                                               uint4* __restrict__ corners) {
+    unsigned int f = 0, nv = 0, ni = 0;
+    if (live) {
+        const unsigned int axes = vertex_axes(c);
+        nv = __popc(axes);
+        f = axes;
+        if (kTris) {
+            bool skip = false;
+#pragma unroll
+            for (int q = 1; q < 8; ++q) skip |= (0.0f == c.val[q].y);
+            if (!skip) {
+                const int lut = cube_case(c);
+                ni = 3u * mc_tri_count_of(s_mc[lut]);
+                f |= ni << 8 | (unsigned int)lut << 16;
+            }
+        }
+        // emission reuses these lookups instead of searching again
+        if (f) corners[i] = make_uint4(c.idx[2], c.idx[4], kTris ? c.idx[6] : 0u, 0u);
+    }
+    flags[i] = f;
+    counts[i] = (unsigned long long)ni << 32 | nv;
+}
+
 // flags per voxel: bits 0-2 vertex axes, bits 8-15 index count, 16-23 case
 template <bool kTris, typename K>
 __global__ void __launch_bounds__(kThreads) k_mesh_classify(const K* __restrict__ keys, int kb,
@@ -204,28 +236,144 @@ __global__ void __launch_bounds__(kThreads) k_mesh_classify(const K* __restrict_
     const unsigned int n = *n_dev;
     const Codec<K> cd(kb);
     for (unsigned int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
-        unsigned int f = 0, nv = 0, ni = 0;
-        if (i + 1 < n && vals[i].y != 0.0f) {
-            Cube c;
-            load_cube<kTris, K>(keys, vals, rs, n, i, c, cd);
-            const unsigned int axes = vertex_axes(c);
-            nv = __popc(axes);
-            f = axes;
-            if (kTris) {
-                bool skip = false;
+        Cube c;
+        const bool live = i + 1 < n && vals[i].y != 0.0f;
+        if (live) load_cube<kTris, K>(keys, vals, rs, n, i, c, cd);
+        classify_voxel<kTris>(c, live, i, s_mc, flags, counts, corners);
+    }
+}
+
+// Classification by tiles of kClassTile consecutive voxels.  For a
+// neighbour offset d (+y, +z, +yz) the lookup positions walk_ptr(key_i + d)
+// are non-decreasing in i, so the tile's positions all lie between those of
+// its first and last voxel: six row-directory searches per tile (three
+// offsets, two ends) bound them, the keys in those ranges are staged in
+// shared memory, and each thread finds its four consecutive voxels'
+// positions by one search in the staged keys and a forward walk.  A tile
+// whose range is longer than the staging holds takes the per-voxel searches
+// of k_mesh_classify.  Results are identical.
+constexpr int kClassItems = 4;
+constexpr int kClassTile = kThreads * kClassItems;  // 1024 voxels
+template <typename K>
+__host__ __device__ constexpr int class_stage() { return sizeof(K) == 4 ? 2048 : 1536; }
+
+template <bool kTris, typename K>
+__global__ void __launch_bounds__(kThreads) k_mesh_classify_tiled(const K* __restrict__ keys, int kb,
+                                                                  const float2* __restrict__ vals,
+                                                                  const unsigned int* __restrict__ rs,
+                                                                  const unsigned int* __restrict__ n_dev,
+                                                                  unsigned int* __restrict__ flags,
+                                                                  unsigned long long* __restrict__ counts,
+                                                                  uint4* __restrict__ corners) {
+    constexpr int kD = kTris ? 3 : 2;  // offsets looked up: +y, +z (and +yz)
+    constexpr int kStage = class_stage<K>();
+    __shared__ uint64_t s_mc[256];
+    __shared__ K s_key[kD][kStage];
+    __shared__ unsigned int s_lo[kD], s_len[kD];
+    __shared__ int s_fits;
+    if (kTris) mc_table_to_shared(s_mc);
+    const unsigned int n = *n_dev;
+    const Codec<K> cd(kb);
+    const K delta[3] = {cd.pack(0, 1, 0), cd.pack(0, 0, 1), cd.pack(0, 1, 1)};
+    const float2 zero = make_float2(0.0f, 0.0f);
+    for (unsigned int i0 = blockIdx.x * kClassTile; i0 < n; i0 += gridDim.x * kClassTile) {
+        const unsigned int i1 = min(i0 + (unsigned int)kClassTile, n);
+        // voxels with a cube: i + 1 < n
+        const unsigned int last = min(i1, n - 1u);  // one past the tile's last such voxel
+        __syncthreads();  // the previous tile is done with the staging
+        if (threadIdx.x < kD) {
+            const int d = threadIdx.x;
+            unsigned int lo = 0, len = 0;
+            if (last > i0) {
+                // walk positions of the first and last voxel (unclamped), then
+                // the range [min(lo, n-2), min(hi + 1, n - 1)] holds every position
+                // of the tile and the one after it
+                const unsigned int p0 = upper_bound_row<K>(keys, rs, keys[i0] + delta[d], n, cd, 0u) - 1u;
+                const unsigned int p1 = upper_bound_row<K>(keys, rs, keys[last - 1] + delta[d], n, cd, 0u) - 1u;
+                lo = min(p0, n - 2u);
+                const unsigned int hi = min(p1 + 1u, n - 1u);
+                len = hi - lo + 1u;
+            }
+            s_lo[d] = lo;
+            s_len[d] = len;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int fits = 1;
 #pragma unroll
-                for (int q = 1; q < 8; ++q) skip |= (0.0f == c.val[q].y);
-                if (!skip) {
-                    const int lut = cube_case(c);
-                    ni = 3u * mc_tri_count_of(s_mc[lut]);
-                    f |= ni << 8 | (unsigned int)lut << 16;
+            for (int d = 0; d < kD; ++d) fits &= s_len[d] <= (unsigned int)kStage;
+            s_fits = fits;
+        }
+        __syncthreads();
+        const bool fits = s_fits != 0;
+        if (fits) {
+#pragma unroll
+            for (int d = 0; d < kD; ++d)
+                for (unsigned int j = threadIdx.x; j < s_len[d]; j += kThreads) s_key[d][j] = keys[s_lo[d] + j];
+        }
+        __syncthreads();
+        const unsigned int ib = i0 + threadIdx.x * kClassItems;
+        unsigned int pos[kD];  // running count of staged keys <= key + d
+#pragma unroll
+        for (int d = 0; d < kD; ++d) pos[d] = 0xffffffffu;
+#pragma unroll
+        for (int j = 0; j < kClassItems; ++j) {
+            const unsigned int i = ib + j;
+            if (i >= i1) break;
+            const bool live = i + 1 < n && vals[i].y != 0.0f;
+            Cube c;
+            if (live && !fits) {
+                load_cube<kTris, K>(keys, vals, rs, n, i, c, cd);
+            } else if (live) {
+                const K key = keys[i];
+                c.idx[0] = i;
+                c.val[0] = vals[i];
+                c.idx[1] = i + 1;
+                c.val[1] = keys[i + 1] == key + cd.pack(1, 0, 0) ? vals[i + 1] : zero;
+                unsigned int w[kD];
+#pragma unroll
+                for (int d = 0; d < kD; ++d) {
+                    const K t = key + delta[d];
+                    const unsigned int L = s_len[d];
+                    const K* sk = s_key[d];
+                    unsigned int p = pos[d];
+                    if (p == 0xffffffffu) {  // the thread's first live voxel: search
+                        unsigned int lo = 0, hi = L;
+                        while (lo < hi) {
+                            const unsigned int mid = (lo + hi) >> 1;
+                            if (sk[mid] <= t) lo = mid + 1;
+                            else hi = mid;
+                        }
+                        p = lo;
+                    } else {  // later voxels: the positions only move forward
+                        while (p < L && sk[p] <= t) ++p;
+                    }
+                    pos[d] = p;
+                    // walk_ptr = min(n - 2, upper_bound - 1), upper_bound = lo + p
+                    const unsigned int ub = s_lo[d] + p;
+                    w[d] = min(ub - 1u, n - 2u);
+                }
+                const unsigned int* lo_d = s_lo;
+                // corners: self, +x, +y, +xy, +z, +xz, +yz, +xyz (Mesher.cpp:122-132, 174-181)
+                c.idx[2] = w[0];
+                c.val[2] = s_key[0][w[0] - lo_d[0]] == key + delta[0] ? vals[w[0]] : zero;
+                c.idx[4] = w[1];
+                c.val[4] = s_key[1][w[1] - lo_d[1]] == key + delta[1] ? vals[w[1]] : zero;
+                if (kTris) {
+                    c.idx[6] = w[kD - 1];
+                    c.val[6] = s_key[kD - 1][w[kD - 1] - lo_d[kD - 1]] == key + delta[2] ? vals[w[kD - 1]] : zero;
+                    c.idx[3] = w[0] + 1;
+                    c.val[3] = s_key[0][w[0] + 1 - lo_d[0]] == key + cd.pack(1, 1, 0) ? vals[w[0] + 1] : zero;
+                    c.idx[5] = w[1] + 1;
+                    c.val[5] = s_key[1][w[1] + 1 - lo_d[1]] == key + cd.pack(1, 0, 1) ? vals[w[1] + 1] : zero;
+                    c.idx[7] = w[kD - 1] + 1;
+                    c.val[7] = s_key[kD - 1][w[kD - 1] + 1 - lo_d[kD - 1]] == key + cd.pack(1, 1, 1)
+                                   ? vals[w[kD - 1] + 1]
+                                   : zero;
                 }
             }
-            // emission reuses these lookups instead of searching again
-            if (f) corners[i] = make_uint4(c.idx[2], c.idx[4], kTris ? c.idx[6] : 0u, 0u);
+            classify_voxel<kTris>(c, live, i, s_mc, flags, counts, corners);
         }
-        flags[i] = f;
-        counts[i] = (unsigned long long)ni << 32 | nv;
     }
 }
 
@@ -528,11 +676,11 @@ static void mesh_count_t(const K* keys, const float2* vals, size_t n_cap, int kb
     unsigned long long* scan = ms.tscan;
     k_row_directory<K><<<grid_for(((size_t)1 << (2 * kb)) + 1, sms), kThreads, 0, st>>>(keys, ms.n_dev, kb, ms.rows);
     if (with_indices)
-        k_mesh_classify<true, K><<<grid_for(n_cap, sms), kThreads, 0, st>>>(keys, kb, vals, ms.rows, ms.n_dev,
-                                                                             ms.vflags, cnt, ms.corners);
+        k_mesh_classify_tiled<true, K><<<grid_for((n_cap + kClassItems - 1) / kClassItems, sms), kThreads, 0, st>>>(
+            keys, kb, vals, ms.rows, ms.n_dev, ms.vflags, cnt, ms.corners);
     else
-        k_mesh_classify<false, K><<<grid_for(n_cap, sms), kThreads, 0, st>>>(keys, kb, vals, ms.rows, ms.n_dev,
-                                                                              ms.vflags, cnt, ms.corners);
+        k_mesh_classify_tiled<false, K><<<grid_for((n_cap + kClassItems - 1) / kClassItems, sms), kThreads, 0, st>>>(
+            keys, kb, vals, ms.rows, ms.n_dev, ms.vflags, cnt, ms.corners);
     const unsigned int n_tiles = (unsigned int)((n_cap + kScanTile - 1) / kScanTile);
     k_scan_tiles<<<n_tiles ? n_tiles : 1, kThreads, 0, st>>>(cnt, scan, ms.block_sums, ms.n_dev);
     k_scan_sums<<<1, kThreads, 0, st>>>(ms.block_sums, n_tiles ? n_tiles : 1, ms.n_dev, ms.counts);
