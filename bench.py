@@ -526,13 +526,15 @@ def run_gpu(args, rank, world, local):
                                         ptr(w2e[n_frames - 1])), "isolated frame")
     check(lib.kifi_volume_stage_times(vol, ptr(iso_stage), C.byref(iso_n)))
     # a mesh of the whole volume alone (the first call sizes the volume's mesh buffers)
-    iso_mesh_ms, iso_meshes = C.c_double(), C.c_int()
+    iso_mesh = np.zeros(5)
+    iso_meshes = C.c_int()
     nvi, nii = C.c_size_t(), C.c_size_t()
     for k in range(3):
         if k == 1:
-            check(lib.kifi_volume_mesh_times(vol, C.byref(iso_mesh_ms), C.byref(iso_meshes)))  # reset
+            check(lib.kifi_volume_mesh_stage_times(vol, ptr(iso_mesh), C.byref(iso_meshes)))  # reset
         check(lib.kifi_mesh_device(vol, 1, C.byref(nvi), C.byref(nii), None, None), "isolated mesh")
-    check(lib.kifi_volume_mesh_times(vol, C.byref(iso_mesh_ms), C.byref(iso_meshes)))
+    check(lib.kifi_volume_mesh_stage_times(vol, ptr(iso_mesh), C.byref(iso_meshes)))
+    iso_mesh_ms = C.c_double(iso_mesh[4])
     check(lib.kifi_volume_set_profiling(vol, 0))
     i0, ie, i1 = np.zeros(64, np.uint64), np.zeros(64, np.uint64), np.zeros(64, np.uint64)
     iso_cnt = C.c_int()
@@ -621,7 +623,9 @@ def run_gpu(args, rank, world, local):
              "per": "mesh"}, pipe_ms[1], peak_kind,
             {"meshes": int(pipe_n[1]),
              "isolated": {"ms_per_launch": iso_mesh_ms.value, "voxels": n_mesh_vox.value,
-                          "frac": gbs(iso_mesh_bytes, iso_mesh_ms.value) / peak}}),
+                          "frac": gbs(iso_mesh_bytes, iso_mesh_ms.value) / peak,
+                          "stage_ms": {"row_directory": iso_mesh[0], "classification": iso_mesh[1],
+                                       "scan": iso_mesh[2], "emission": iso_mesh[3]}}}),
         "k_icp_step": roofline_entry(
             "fp32", icp_flops / (track_step_ms * 1e-3) / 1e12 if track_step_ms > 0 else 0.0, fp32_peak, "TFLOP/s",
             {"flop_per_launch": icp_flops, "flop_rule": "P/4 sources x 441 window candidates x 10 flop"},

@@ -196,6 +196,9 @@ KIFI_API kifi_status kifi_volume_stage_times(kifi_volume* vol, double out_ms[4],
  * emission); this returns their mean in milliseconds and their count, and
  * resets them. */
 KIFI_API kifi_status kifi_volume_mesh_times(kifi_volume* v, double* out_ms, int* meshes);
+/* The same per stage: out_ms = {row directory, classification, scan,
+ * emission, total} means in milliseconds. */
+KIFI_API kifi_status kifi_volume_mesh_stage_times(kifi_volume* v, double out_ms[5], int* meshes);
 
 /* No counterpart in the reference.  Picks the persistent CTA counts of the
  * volume's splat+emit, sort and merge/update kernels by timing them on one

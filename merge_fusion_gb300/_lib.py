@@ -148,6 +148,7 @@ SIGNATURES = {
     "kifi_batch_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
     "kifi_batch_step_times": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
     "kifi_volume_mesh_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
+    "kifi_volume_mesh_stage_times": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int)]),
     "kifi_pipeline_stage_times": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "kifi_icp_set_target_bin_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_int,
                                                  C.c_int, C.c_void_p]),

@@ -624,9 +624,9 @@ static kifi_status mesh_to_device(kifi_volume* v, int with_indices, size_t* n_ve
     KIFI_CUDA(mesh_scratch_reserve(&v->ms, n, v->g.kb));
     const unsigned int n32 = (unsigned int)n;
     KIFI_CUDA(cudaMemcpyAsync(v->ms.n_dev, &n32, sizeof n32, cudaMemcpyHostToDevice, v->stream));
-    std::array<cudaEvent_t, 2> ev{};
+    std::array<cudaEvent_t, 5> ev{};
     if (v->profiling) {
-        for (int k = 0; k < 2; ++k) {
+        for (int k = 0; k < 5; ++k) {
             if (v->event_pool.empty()) {
                 cudaEvent_t e;
                 KIFI_CUDA(cudaEventCreate(&e));
@@ -638,14 +638,15 @@ static kifi_status mesh_to_device(kifi_volume* v, int with_indices, size_t* n_ve
         KIFI_CUDA(cudaEventRecord(ev[0], v->stream));
     }
     KIFI_CUDA(mesh_count_enqueue(v->vb.keys[cur], v->vb.key_bytes, v->vb.vals[cur], n, v->g.kb,
-                                 with_indices ? 1 : 0, v->ms, v->ls.sms, v->stream));
+                                 with_indices ? 1 : 0, v->ms, v->ls.sms, v->stream, ev[0] ? &ev[1] : nullptr));
+    if (ev[0]) KIFI_CUDA(cudaEventRecord(ev[3], v->stream));
     MeshCounts* mc = &v->ctl_host_mesh;
     for (int attempt = 0; attempt < 2; ++attempt) {
         KIFI_CUDA(mesh_emit_enqueue(v->g, v->vb.keys[cur], v->vb.key_bytes, v->vb.vals[cur], n,
                                     with_indices ? 1 : 0, v->ms, v->mesh_verts_cap, v->mesh_idx_cap, v->mesh_verts,
                                     v->mesh_idx, v->ls.sms, v->stream));
         if (attempt == 0 && ev[0]) {
-            KIFI_CUDA(cudaEventRecord(ev[1], v->stream));
+            KIFI_CUDA(cudaEventRecord(ev[4], v->stream));
             v->mesh_pending.push_back(ev);
         }
         KIFI_CUDA(cudaMemcpyAsync(mc, v->ms.counts, sizeof(MeshCounts), cudaMemcpyDeviceToHost, v->stream));
@@ -674,23 +675,33 @@ static kifi_status mesh_to_device(kifi_volume* v, int with_indices, size_t* n_ve
     return KIFI_OK;
 }
 
-kifi_status kifi_volume_mesh_times(kifi_volume* v, double* out_ms, int* meshes) {
+kifi_status kifi_volume_mesh_stage_times(kifi_volume* v, double out_ms[5], int* meshes) {
     if (!v || !out_ms) return fail(KIFI_ERR_INVALID_ARGUMENT, "null argument");
     KIFI_CUDA(cudaSetDevice(v->device));
-    double total = 0.0;
+    double sum[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
     const int n = (int)v->mesh_pending.size();
     for (auto& ev : v->mesh_pending) {
-        float ms = 0.0f;
-        KIFI_CUDA(cudaEventSynchronize(ev[1]));
-        KIFI_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
-        total += ms;
-        v->event_pool.push_back(ev[0]);
-        v->event_pool.push_back(ev[1]);
+        KIFI_CUDA(cudaEventSynchronize(ev[4]));
+        for (int k = 0; k < 4; ++k) {
+            float ms = 0.0f;
+            KIFI_CUDA(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
+            sum[k] += ms;
+            sum[4] += ms;
+        }
+        for (int k = 0; k < 5; ++k) v->event_pool.push_back(ev[k]);
     }
     v->mesh_pending.clear();
-    *out_ms = n ? total / n : 0.0;
+    for (int k = 0; k < 5; ++k) out_ms[k] = n ? sum[k] / n : 0.0;
     if (meshes) *meshes = n;
     return KIFI_OK;
+}
+
+kifi_status kifi_volume_mesh_times(kifi_volume* v, double* out_ms, int* meshes) {
+    if (!v || !out_ms) return fail(KIFI_ERR_INVALID_ARGUMENT, "null argument");
+    double st[5];
+    kifi_status s = kifi_volume_mesh_stage_times(v, st, meshes);
+    *out_ms = st[4];
+    return s;
 }
 
 kifi_status kifi_mesh(kifi_volume* v, int with_indices, float* verts, size_t vert_capacity,

@@ -70,7 +70,9 @@ struct kifi_volume {
     bool profiling = false;
     std::vector<cudaEvent_t> event_pool;
     std::vector<std::array<cudaEvent_t, kStageEvents>> pending;
-    std::vector<std::array<cudaEvent_t, 2>> mesh_pending;  // counting + emission of kifi_mesh*
+    // kifi_mesh* timers: before the row directory, after it, after the
+    // classification, after the scan, after the emission
+    std::vector<std::array<cudaEvent_t, 5>> mesh_pending;
 };
 
 // integrate entry shared by the ABI translation units: enqueues one frame

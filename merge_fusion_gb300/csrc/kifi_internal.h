@@ -164,8 +164,11 @@ struct MeshScratch {
 
 cudaError_t mesh_scratch_reserve(MeshScratch* m, size_t n, int kb);
 void mesh_scratch_free(MeshScratch* m);
+// stage_events (optional, 2 entries): recorded after the row directory and
+// after the classification
 cudaError_t mesh_count_enqueue(const void* keys, int key_bytes, const float2* vals, size_t n_cap, int kb,
-                               int with_indices, MeshScratch& ms, int sms, cudaStream_t st);
+                               int with_indices, MeshScratch& ms, int sms, cudaStream_t st,
+                               cudaEvent_t* stage_events = nullptr);
 // Emission reads the counts on the device (ms.counts, written by the
 // counting passes), so it can be enqueued right behind them.  The buffers
 // hold vert_cap vertices and idx_cap indices; when the mesh needs more, the

@@ -670,26 +670,29 @@ static int grid_for(size_t n, int sms) {
 // the grids), so the passes can be enqueued before the count is known.
 template <typename K>
 static void mesh_count_t(const K* keys, const float2* vals, size_t n_cap, int kb, int with_indices, MeshScratch& ms,
-                         int sms, cudaStream_t st) {
+                         int sms, cudaStream_t st, cudaEvent_t* stage_events) {
     // vscan holds the per-voxel packed counts, tscan their exclusive scan
     unsigned long long* cnt = ms.vscan;
     unsigned long long* scan = ms.tscan;
     k_row_directory<K><<<grid_for(((size_t)1 << (2 * kb)) + 1, sms), kThreads, 0, st>>>(keys, ms.n_dev, kb, ms.rows);
+    if (stage_events) cudaEventRecord(stage_events[0], st);
     if (with_indices)
         k_mesh_classify_tiled<true, K><<<grid_for((n_cap + kClassItems - 1) / kClassItems, sms), kThreads, 0, st>>>(
             keys, kb, vals, ms.rows, ms.n_dev, ms.vflags, cnt, ms.corners);
     else
         k_mesh_classify_tiled<false, K><<<grid_for((n_cap + kClassItems - 1) / kClassItems, sms), kThreads, 0, st>>>(
             keys, kb, vals, ms.rows, ms.n_dev, ms.vflags, cnt, ms.corners);
+    if (stage_events) cudaEventRecord(stage_events[1], st);
     const unsigned int n_tiles = (unsigned int)((n_cap + kScanTile - 1) / kScanTile);
     k_scan_tiles<<<n_tiles ? n_tiles : 1, kThreads, 0, st>>>(cnt, scan, ms.block_sums, ms.n_dev);
     k_scan_sums<<<1, kThreads, 0, st>>>(ms.block_sums, n_tiles ? n_tiles : 1, ms.n_dev, ms.counts);
 }
 
 cudaError_t mesh_count_enqueue(const void* keys, int key_bytes, const float2* vals, size_t n_cap, int kb,
-                               int with_indices, MeshScratch& ms, int sms, cudaStream_t st) {
-    if (key_bytes == 8) mesh_count_t<uint64_t>((const uint64_t*)keys, vals, n_cap, kb, with_indices, ms, sms, st);
-    else mesh_count_t<uint32_t>((const uint32_t*)keys, vals, n_cap, 10, with_indices, ms, sms, st);
+                               int with_indices, MeshScratch& ms, int sms, cudaStream_t st, cudaEvent_t* stage_events) {
+    if (key_bytes == 8)
+        mesh_count_t<uint64_t>((const uint64_t*)keys, vals, n_cap, kb, with_indices, ms, sms, st, stage_events);
+    else mesh_count_t<uint32_t>((const uint32_t*)keys, vals, n_cap, 10, with_indices, ms, sms, st, stage_events);
     return cudaGetLastError();
 }
 
