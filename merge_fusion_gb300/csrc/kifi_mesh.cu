@@ -12,7 +12,7 @@
 //  k_row_directory  start index of every (y, z) key row (key >> b, b key bits
 //                   per axis); a neighbour search then only scans one row,
 //                   starting where the searching voxel sits in its own row.
-//  k_mesh_classify  per voxel i in [0, n-2] with weight > 0: which of its
+//  k_mesh_classify_tiled  per voxel i in [0, n-2] with weight > 0: which of its
 //                   +x/+y/+z edges carry a vertex (Mesher.cpp:140-168) and,
 //                   for Mesh(verts, indices), the cube's marching-cubes case
 //                   and triangle count (:172-226); a voxel with any output
@@ -219,43 +219,27 @@ __device__ __forceinline__ void classify_voxel(const Cube& c, bool live, unsigne
     counts[i] = (unsigned long long)ni << 32 | nv;
 }
 
-// flags per voxel: bits 0-2 vertex axes, bits 8-15 index count, 16-23 case
-template <bool kTris, typename K>
-__global__ void __launch_bounds__(kThreads) k_mesh_classify(const K* __restrict__ keys, int kb,
-                                                            const float2* __restrict__ vals,
-                                                            const unsigned int* __restrict__ rs,
-                                                            const unsigned int* __restrict__ n_dev,
-                                                            unsigned int* __restrict__ flags,
-                                                            unsigned long long* __restrict__ counts,
-                                                            uint4* __restrict__ corners) {
-    __shared__ uint64_t s_mc[256];
-    if (kTris) {
-        mc_table_to_shared(s_mc);
-        __syncthreads();
-    }
-    const unsigned int n = *n_dev;
-    const Codec<K> cd(kb);
-    for (unsigned int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
-        Cube c;
-        const bool live = i + 1 < n && vals[i].y != 0.0f;
-        if (live) load_cube<kTris, K>(keys, vals, rs, n, i, c, cd);
-        classify_voxel<kTris>(c, live, i, s_mc, flags, counts, corners);
-    }
-}
-
 // Classification by tiles of kClassTile consecutive voxels.  For a
 // neighbour offset d (+y, +z, +yz) the lookup positions walk_ptr(key_i + d)
 // are non-decreasing in i, so the tile's positions all lie between those of
 // its first and last voxel: six row-directory searches per tile (three
-// offsets, two ends) bound them, the keys in those ranges are staged in
-// shared memory, and each thread finds its four consecutive voxels'
-// positions by one search in the staged keys and a forward walk.  A tile
-// whose range is longer than the staging holds takes the per-voxel searches
-// of k_mesh_classify.  Results are identical.
+// offsets, two ends) bound them.  The keys and voxels of those ranges and of
+// the tile itself are staged in shared memory with independent coalesced
+// loads, and each thread builds its four consecutive voxels' cubes from the
+// staging: one search in the staged keys for its first voxel, a forward
+// walk for the others.  A tile whose ranges are longer than the staging
+// holds searches per voxel (load_cube).  Results are identical.
 constexpr int kClassItems = 4;
 constexpr int kClassTile = kThreads * kClassItems;  // 1024 voxels
 template <typename K>
-__host__ __device__ constexpr int class_stage() { return sizeof(K) == 4 ? 2048 : 1536; }
+__host__ __device__ constexpr int class_stage() { return 2048; }
+// dynamic shared memory of k_mesh_classify_tiled: per offset a staged range
+// of keys and voxels, the tile's own keys and voxels (plus the one after)
+template <typename K>
+__host__ __device__ constexpr size_t class_smem(int n_offsets) {
+    return (size_t)n_offsets * class_stage<K>() * (sizeof(K) + sizeof(float2)) +
+           (size_t)(kClassTile + 1) * (sizeof(K) + sizeof(float2));
+}
 
 template <bool kTris, typename K>
 __global__ void __launch_bounds__(kThreads) k_mesh_classify_tiled(const K* __restrict__ keys, int kb,
@@ -267,8 +251,12 @@ __global__ void __launch_bounds__(kThreads) k_mesh_classify_tiled(const K* __res
                                                                   uint4* __restrict__ corners) {
     constexpr int kD = kTris ? 3 : 2;  // offsets looked up: +y, +z (and +yz)
     constexpr int kStage = class_stage<K>();
+    extern __shared__ __align__(16) unsigned char class_mem[];
+    float2* s_val = (float2*)class_mem;                           // [kD][kStage]
+    float2* s_tval = s_val + kD * kStage;                          // [kClassTile + 1]
+    K* s_key = (K*)(s_tval + kClassTile + 1);                     // [kD][kStage]
+    K* s_tkey = s_key + kD * kStage;                              // [kClassTile + 1]
     __shared__ uint64_t s_mc[256];
-    __shared__ K s_key[kD][kStage];
     __shared__ unsigned int s_lo[kD], s_len[kD];
     __shared__ int s_fits;
     if (kTris) mc_table_to_shared(s_mc);
@@ -281,95 +269,121 @@ __global__ void __launch_bounds__(kThreads) k_mesh_classify_tiled(const K* __res
         // voxels with a cube: i + 1 < n
         const unsigned int last = min(i1, n - 1u);  // one past the tile's last such voxel
         __syncthreads();  // the previous tile is done with the staging
-        if (threadIdx.x < kD) {
-            const int d = threadIdx.x;
-            unsigned int lo = 0, len = 0;
-            if (last > i0) {
-                // walk positions of the first and last voxel (unclamped), then
-                // the range [min(lo, n-2), min(hi + 1, n - 1)] holds every position
-                // of the tile and the one after it
-                const unsigned int p0 = upper_bound_row<K>(keys, rs, keys[i0] + delta[d], n, cd, 0u) - 1u;
-                const unsigned int p1 = upper_bound_row<K>(keys, rs, keys[last - 1] + delta[d], n, cd, 0u) - 1u;
-                lo = min(p0, n - 2u);
-                const unsigned int hi = min(p1 + 1u, n - 1u);
-                len = hi - lo + 1u;
-            }
-            s_lo[d] = lo;
-            s_len[d] = len;
+        if (threadIdx.x < 2 * kD) {
+            // thread 2d + e: the walk position (unclamped) of the tile's first
+            // (e = 0) or last (e = 1) voxel for offset d
+            const int d = threadIdx.x >> 1, e = threadIdx.x & 1;
+            unsigned int p = 0;
+            if (last > i0)
+                p = upper_bound_row<K>(keys, rs, keys[e ? last - 1 : i0] + delta[d], n, cd, 0u) - 1u;
+            if (e == 0) s_lo[d] = p;
+            else s_len[d] = p;
         }
         __syncthreads();
         if (threadIdx.x == 0) {
             int fits = 1;
 #pragma unroll
-            for (int d = 0; d < kD; ++d) fits &= s_len[d] <= (unsigned int)kStage;
+            for (int d = 0; d < kD; ++d) {
+                // the range [min(p0, n-2), min(p1 + 1, n - 1)] holds every
+                // position of the tile and the one after it
+                unsigned int lo = 0, len = 0;
+                if (last > i0) {
+                    lo = min(s_lo[d], n - 2u);
+                    len = min(s_len[d] + 1u, n - 1u) - lo + 1u;
+                }
+                s_lo[d] = lo;
+                s_len[d] = len;
+                fits &= len <= (unsigned int)kStage;
+            }
             s_fits = fits;
         }
         __syncthreads();
         const bool fits = s_fits != 0;
         if (fits) {
+            // independent loads: the tile's own keys and voxels (and the one
+            // after), then each offset's range
+            for (unsigned int j = threadIdx.x; j <= (unsigned int)kClassTile; j += kThreads)
+                if (i0 + j < n) {
+                    s_tkey[j] = keys[i0 + j];
+                    s_tval[j] = vals[i0 + j];
+                }
 #pragma unroll
-            for (int d = 0; d < kD; ++d)
-                for (unsigned int j = threadIdx.x; j < s_len[d]; j += kThreads) s_key[d][j] = keys[s_lo[d] + j];
+            for (int d = 0; d < kD; ++d) {
+                const unsigned int lo = s_lo[d], len = s_len[d];
+                for (unsigned int j = threadIdx.x; j < len; j += kThreads) {
+                    s_key[d * kStage + j] = keys[lo + j];
+                    s_val[d * kStage + j] = vals[lo + j];
+                }
+            }
         }
         __syncthreads();
-        const unsigned int ib = i0 + threadIdx.x * kClassItems;
+        const unsigned int tb = threadIdx.x * kClassItems;  // this thread's first voxel in the tile
         unsigned int pos[kD];  // running count of staged keys <= key + d
 #pragma unroll
         for (int d = 0; d < kD; ++d) pos[d] = 0xffffffffu;
 #pragma unroll
         for (int j = 0; j < kClassItems; ++j) {
-            const unsigned int i = ib + j;
+            const unsigned int i = i0 + tb + j;
             if (i >= i1) break;
-            const bool live = i + 1 < n && vals[i].y != 0.0f;
             Cube c;
-            if (live && !fits) {
-                load_cube<kTris, K>(keys, vals, rs, n, i, c, cd);
-            } else if (live) {
-                const K key = keys[i];
-                c.idx[0] = i;
-                c.val[0] = vals[i];
-                c.idx[1] = i + 1;
-                c.val[1] = keys[i + 1] == key + cd.pack(1, 0, 0) ? vals[i + 1] : zero;
-                unsigned int w[kD];
+            bool live;
+            if (!fits) {
+                live = i + 1 < n && vals[i].y != 0.0f;
+                if (live) load_cube<kTris, K>(keys, vals, rs, n, i, c, cd);
+            } else {
+                const float2 v0 = s_tval[tb + j];
+                live = i + 1 < n && v0.y != 0.0f;
+                if (live) {
+                    const K key = s_tkey[tb + j];
+                    c.idx[0] = i;
+                    c.val[0] = v0;
+                    c.idx[1] = i + 1;
+                    c.val[1] = s_tkey[tb + j + 1] == key + cd.pack(1, 0, 0) ? s_tval[tb + j + 1] : zero;
+                    unsigned int w[kD];
 #pragma unroll
-                for (int d = 0; d < kD; ++d) {
-                    const K t = key + delta[d];
-                    const unsigned int L = s_len[d];
-                    const K* sk = s_key[d];
-                    unsigned int p = pos[d];
-                    if (p == 0xffffffffu) {  // the thread's first live voxel: search
-                        unsigned int lo = 0, hi = L;
-                        while (lo < hi) {
-                            const unsigned int mid = (lo + hi) >> 1;
-                            if (sk[mid] <= t) lo = mid + 1;
-                            else hi = mid;
+                    for (int d = 0; d < kD; ++d) {
+                        const K t = key + delta[d];
+                        const unsigned int L = s_len[d];
+                        const K* sk = s_key + d * kStage;
+                        unsigned int p = pos[d];
+                        if (p == 0xffffffffu) {  // the thread's first live voxel: search
+                            unsigned int lo = 0, hi = L;
+                            while (lo < hi) {
+                                const unsigned int mid = (lo + hi) >> 1;
+                                if (sk[mid] <= t) lo = mid + 1;
+                                else hi = mid;
+                            }
+                            p = lo;
+                        } else {  // later voxels: the positions only move forward
+                            while (p < L && sk[p] <= t) ++p;
                         }
-                        p = lo;
-                    } else {  // later voxels: the positions only move forward
-                        while (p < L && sk[p] <= t) ++p;
+                        pos[d] = p;
+                        // walk_ptr = min(n - 2, upper_bound - 1), upper_bound = lo + p;
+                        // w[d] is the staged index of that position
+                        w[d] = min(s_lo[d] + p - 1u, n - 2u) - s_lo[d];
                     }
-                    pos[d] = p;
-                    // walk_ptr = min(n - 2, upper_bound - 1), upper_bound = lo + p
-                    const unsigned int ub = s_lo[d] + p;
-                    w[d] = min(ub - 1u, n - 2u);
-                }
-                const unsigned int* lo_d = s_lo;
-                // corners: self, +x, +y, +xy, +z, +xz, +yz, +xyz (Mesher.cpp:122-132, 174-181)
-                c.idx[2] = w[0];
-                c.val[2] = s_key[0][w[0] - lo_d[0]] == key + delta[0] ? vals[w[0]] : zero;
-                c.idx[4] = w[1];
-                c.val[4] = s_key[1][w[1] - lo_d[1]] == key + delta[1] ? vals[w[1]] : zero;
-                if (kTris) {
-                    c.idx[6] = w[kD - 1];
-                    c.val[6] = s_key[kD - 1][w[kD - 1] - lo_d[kD - 1]] == key + delta[2] ? vals[w[kD - 1]] : zero;
-                    c.idx[3] = w[0] + 1;
-                    c.val[3] = s_key[0][w[0] + 1 - lo_d[0]] == key + cd.pack(1, 1, 0) ? vals[w[0] + 1] : zero;
-                    c.idx[5] = w[1] + 1;
-                    c.val[5] = s_key[1][w[1] + 1 - lo_d[1]] == key + cd.pack(1, 0, 1) ? vals[w[1] + 1] : zero;
-                    c.idx[7] = w[kD - 1] + 1;
-                    c.val[7] = s_key[kD - 1][w[kD - 1] + 1 - lo_d[kD - 1]] == key + cd.pack(1, 1, 1)
-                                   ? vals[w[kD - 1] + 1]
-                                   : zero;
+                    // corners: self, +x, +y, +xy, +z, +xz, +yz, +xyz (Mesher.cpp:122-132, 174-181)
+                    const K* ky = s_key;
+                    const K* kz = s_key + kStage;
+                    const float2* vy = s_val;
+                    const float2* vz = s_val + kStage;
+                    c.idx[2] = s_lo[0] + w[0];
+                    c.val[2] = ky[w[0]] == key + delta[0] ? vy[w[0]] : zero;
+                    c.idx[4] = s_lo[1] + w[1];
+                    c.val[4] = kz[w[1]] == key + delta[1] ? vz[w[1]] : zero;
+                    if (kTris) {
+                        const K* kyz = s_key + (kD - 1) * kStage;
+                        const float2* vyz = s_val + (kD - 1) * kStage;
+                        const unsigned int wy = w[kD - 1];
+                        c.idx[6] = s_lo[kD - 1] + wy;
+                        c.val[6] = kyz[wy] == key + delta[2] ? vyz[wy] : zero;
+                        c.idx[3] = c.idx[2] + 1;
+                        c.val[3] = ky[w[0] + 1] == key + cd.pack(1, 1, 0) ? vy[w[0] + 1] : zero;
+                        c.idx[5] = c.idx[4] + 1;
+                        c.val[5] = kz[w[1] + 1] == key + cd.pack(1, 0, 1) ? vz[w[1] + 1] : zero;
+                        c.idx[7] = c.idx[6] + 1;
+                        c.val[7] = kyz[wy + 1] == key + cd.pack(1, 1, 1) ? vyz[wy + 1] : zero;
+                    }
                 }
             }
             classify_voxel<kTris>(c, live, i, s_mc, flags, counts, corners);
@@ -676,12 +690,18 @@ static void mesh_count_t(const K* keys, const float2* vals, size_t n_cap, int kb
     unsigned long long* scan = ms.tscan;
     k_row_directory<K><<<grid_for(((size_t)1 << (2 * kb)) + 1, sms), kThreads, 0, st>>>(keys, ms.n_dev, kb, ms.rows);
     if (stage_events) cudaEventRecord(stage_events[0], st);
-    if (with_indices)
-        k_mesh_classify_tiled<true, K><<<grid_for((n_cap + kClassItems - 1) / kClassItems, sms), kThreads, 0, st>>>(
-            keys, kb, vals, ms.rows, ms.n_dev, ms.vflags, cnt, ms.corners);
-    else
-        k_mesh_classify_tiled<false, K><<<grid_for((n_cap + kClassItems - 1) / kClassItems, sms), kThreads, 0, st>>>(
-            keys, kb, vals, ms.rows, ms.n_dev, ms.vflags, cnt, ms.corners);
+    const int class_grid = grid_for((n_cap + kClassItems - 1) / kClassItems, sms);
+    if (with_indices) {
+        const size_t smem = class_smem<K>(3);
+        cudaFuncSetAttribute(k_mesh_classify_tiled<true, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_mesh_classify_tiled<true, K><<<class_grid, kThreads, smem, st>>>(keys, kb, vals, ms.rows, ms.n_dev,
+                                                                          ms.vflags, cnt, ms.corners);
+    } else {
+        const size_t smem = class_smem<K>(2);
+        cudaFuncSetAttribute(k_mesh_classify_tiled<false, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_mesh_classify_tiled<false, K><<<class_grid, kThreads, smem, st>>>(keys, kb, vals, ms.rows, ms.n_dev,
+                                                                           ms.vflags, cnt, ms.corners);
+    }
     if (stage_events) cudaEventRecord(stage_events[1], st);
     const unsigned int n_tiles = (unsigned int)((n_cap + kScanTile - 1) / kScanTile);
     k_scan_tiles<<<n_tiles ? n_tiles : 1, kThreads, 0, st>>>(cnt, scan, ms.block_sums, ms.n_dev);
