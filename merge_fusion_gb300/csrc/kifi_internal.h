@@ -157,6 +157,7 @@ struct MeshScratch {
     unsigned long long* tscan = nullptr;   // exclusive scan of vscan
     unsigned long long* block_sums = nullptr;
     unsigned int* rows = nullptr;          // start index of each (z, y) key row
+    uint2* tile_ranges = nullptr;          // per classification tile and offset: staged range (start, length)
     MeshCounts* counts = nullptr;
     unsigned int* n_dev = nullptr;         // the voxel count the passes read
     size_t cap = 0, rows_cap = 0;

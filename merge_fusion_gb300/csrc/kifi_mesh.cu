@@ -222,23 +222,50 @@ __device__ __forceinline__ void classify_voxel(const Cube& c, bool live, unsigne
 // Classification by tiles of kClassTile consecutive voxels.  For a
 // neighbour offset d (+y, +z, +yz) the lookup positions walk_ptr(key_i + d)
 // are non-decreasing in i, so the tile's positions all lie between those of
-// its first and last voxel: six row-directory searches per tile (three
-// offsets, two ends) bound them.  The keys and voxels of those ranges and of
-// the tile itself are staged in shared memory with independent coalesced
-// loads, and each thread builds its four consecutive voxels' cubes from the
-// staging: one search in the staged keys for its first voxel, a forward
-// walk for the others.  A tile whose ranges are longer than the staging
-// holds searches per voxel (load_cube).  Results are identical.
-constexpr int kClassItems = 4;
-constexpr int kClassTile = kThreads * kClassItems;  // 1024 voxels
-template <typename K>
-__host__ __device__ constexpr int class_stage() { return 2048; }
+// its first and last voxel.  k_mesh_tile_ranges finds those bounds for every
+// tile at once (six row-directory searches per tile, one thread each); the
+// classification then stages the tile's keys and voxels and each offset's
+// range in shared memory with independent coalesced loads and builds every
+// cube from the staging: one search in the staged keys for a thread's first
+// voxel, a forward walk for its next.  A tile whose ranges are longer than
+// the staging holds searches per voxel (load_cube).  Results are identical.
+constexpr int kClassItems = 2;
+constexpr int kClassTile = kThreads * kClassItems;  // 512 voxels
+constexpr int kClassStage = 1024;                    // staged keys per offset
 // dynamic shared memory of k_mesh_classify_tiled: per offset a staged range
 // of keys and voxels, the tile's own keys and voxels (plus the one after)
 template <typename K>
 __host__ __device__ constexpr size_t class_smem(int n_offsets) {
-    return (size_t)n_offsets * class_stage<K>() * (sizeof(K) + sizeof(float2)) +
-           (size_t)(kClassTile + 1) * (sizeof(K) + sizeof(float2));
+    return ((size_t)n_offsets * kClassStage + kClassTile + 1) * (sizeof(K) + sizeof(float2));
+}
+
+// per tile and offset d: the first staged position and the range length
+// (length 0: nothing to stage; longer than kClassStage: search per voxel)
+template <typename K>
+__global__ void k_mesh_tile_ranges(const K* __restrict__ keys, int kb, const unsigned int* __restrict__ rs,
+                                   const unsigned int* __restrict__ n_dev, int n_offsets,
+                                   uint2* __restrict__ ranges, unsigned int max_tiles) {
+    const unsigned int n = *n_dev;
+    const unsigned int tiles = min((n + kClassTile - 1) / kClassTile, max_tiles);
+    const Codec<K> cd(kb);
+    const K delta[3] = {cd.pack(0, 1, 0), cd.pack(0, 0, 1), cd.pack(0, 1, 1)};
+    for (unsigned int q = blockIdx.x * blockDim.x + threadIdx.x; q < tiles * n_offsets;
+         q += gridDim.x * blockDim.x) {
+        const unsigned int t = q / n_offsets;
+        const int d = (int)(q - t * n_offsets);
+        const unsigned int i0 = t * kClassTile;
+        const unsigned int last = min(min(i0 + (unsigned int)kClassTile, n), n - 1u);  // voxels with a cube: < last
+        uint2 r = make_uint2(0u, 0u);
+        if (last > i0) {
+            // walk positions (unclamped) of the first and last voxel; the range
+            // [min(p0, n-2), min(p1 + 1, n - 1)] holds every position and the one after
+            const unsigned int p0 = upper_bound_row<K>(keys, rs, keys[i0] + delta[d], n, cd, 0u) - 1u;
+            const unsigned int p1 = upper_bound_row<K>(keys, rs, keys[last - 1] + delta[d], n, cd, 0u) - 1u;
+            const unsigned int lo = min(p0, n - 2u);
+            r = make_uint2(lo, min(p1 + 1u, n - 1u) - lo + 1u);
+        }
+        ranges[(size_t)t * 3 + d] = r;
+    }
 }
 
 template <bool kTris, typename K>
@@ -246,59 +273,38 @@ __global__ void __launch_bounds__(kThreads) k_mesh_classify_tiled(const K* __res
                                                                   const float2* __restrict__ vals,
                                                                   const unsigned int* __restrict__ rs,
                                                                   const unsigned int* __restrict__ n_dev,
+                                                                  const uint2* __restrict__ ranges,
+                                                                  unsigned int max_tiles,
                                                                   unsigned int* __restrict__ flags,
                                                                   unsigned long long* __restrict__ counts,
                                                                   uint4* __restrict__ corners) {
     constexpr int kD = kTris ? 3 : 2;  // offsets looked up: +y, +z (and +yz)
-    constexpr int kStage = class_stage<K>();
+    constexpr int kStage = kClassStage;
     extern __shared__ __align__(16) unsigned char class_mem[];
     float2* s_val = (float2*)class_mem;                           // [kD][kStage]
     float2* s_tval = s_val + kD * kStage;                          // [kClassTile + 1]
     K* s_key = (K*)(s_tval + kClassTile + 1);                     // [kD][kStage]
     K* s_tkey = s_key + kD * kStage;                              // [kClassTile + 1]
     __shared__ uint64_t s_mc[256];
-    __shared__ unsigned int s_lo[kD], s_len[kD];
-    __shared__ int s_fits;
     if (kTris) mc_table_to_shared(s_mc);
     const unsigned int n = *n_dev;
     const Codec<K> cd(kb);
     const K delta[3] = {cd.pack(0, 1, 0), cd.pack(0, 0, 1), cd.pack(0, 1, 1)};
     const float2 zero = make_float2(0.0f, 0.0f);
-    for (unsigned int i0 = blockIdx.x * kClassTile; i0 < n; i0 += gridDim.x * kClassTile) {
+    const unsigned int tiles = min((n + kClassTile - 1) / kClassTile, max_tiles);
+    for (unsigned int t = blockIdx.x; t < tiles; t += gridDim.x) {
+        const unsigned int i0 = t * kClassTile;
         const unsigned int i1 = min(i0 + (unsigned int)kClassTile, n);
-        // voxels with a cube: i + 1 < n
-        const unsigned int last = min(i1, n - 1u);  // one past the tile's last such voxel
-        __syncthreads();  // the previous tile is done with the staging
-        if (threadIdx.x < 2 * kD) {
-            // thread 2d + e: the walk position (unclamped) of the tile's first
-            // (e = 0) or last (e = 1) voxel for offset d
-            const int d = threadIdx.x >> 1, e = threadIdx.x & 1;
-            unsigned int p = 0;
-            if (last > i0)
-                p = upper_bound_row<K>(keys, rs, keys[e ? last - 1 : i0] + delta[d], n, cd, 0u) - 1u;
-            if (e == 0) s_lo[d] = p;
-            else s_len[d] = p;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            int fits = 1;
+        unsigned int lo[kD], len[kD];
+        bool fits = true;
 #pragma unroll
-            for (int d = 0; d < kD; ++d) {
-                // the range [min(p0, n-2), min(p1 + 1, n - 1)] holds every
-                // position of the tile and the one after it
-                unsigned int lo = 0, len = 0;
-                if (last > i0) {
-                    lo = min(s_lo[d], n - 2u);
-                    len = min(s_len[d] + 1u, n - 1u) - lo + 1u;
-                }
-                s_lo[d] = lo;
-                s_len[d] = len;
-                fits &= len <= (unsigned int)kStage;
-            }
-            s_fits = fits;
+        for (int d = 0; d < kD; ++d) {
+            const uint2 r = ranges[(size_t)t * 3 + d];
+            lo[d] = r.x;
+            len[d] = r.y;
+            fits &= r.y <= (unsigned int)kStage;
         }
-        __syncthreads();
-        const bool fits = s_fits != 0;
+        __syncthreads();  // the previous tile is done with the staging
         if (fits) {
             // independent loads: the tile's own keys and voxels (and the one
             // after), then each offset's range
@@ -308,13 +314,11 @@ __global__ void __launch_bounds__(kThreads) k_mesh_classify_tiled(const K* __res
                     s_tval[j] = vals[i0 + j];
                 }
 #pragma unroll
-            for (int d = 0; d < kD; ++d) {
-                const unsigned int lo = s_lo[d], len = s_len[d];
-                for (unsigned int j = threadIdx.x; j < len; j += kThreads) {
-                    s_key[d * kStage + j] = keys[lo + j];
-                    s_val[d * kStage + j] = vals[lo + j];
+            for (int d = 0; d < kD; ++d)
+                for (unsigned int j = threadIdx.x; j < len[d]; j += kThreads) {
+                    s_key[d * kStage + j] = keys[lo[d] + j];
+                    s_val[d * kStage + j] = vals[lo[d] + j];
                 }
-            }
         }
         __syncthreads();
         const unsigned int tb = threadIdx.x * kClassItems;  // this thread's first voxel in the tile
@@ -342,40 +346,39 @@ __global__ void __launch_bounds__(kThreads) k_mesh_classify_tiled(const K* __res
                     unsigned int w[kD];
 #pragma unroll
                     for (int d = 0; d < kD; ++d) {
-                        const K t = key + delta[d];
-                        const unsigned int L = s_len[d];
+                        const K tk = key + delta[d];
                         const K* sk = s_key + d * kStage;
                         unsigned int p = pos[d];
                         if (p == 0xffffffffu) {  // the thread's first live voxel: search
-                            unsigned int lo = 0, hi = L;
-                            while (lo < hi) {
-                                const unsigned int mid = (lo + hi) >> 1;
-                                if (sk[mid] <= t) lo = mid + 1;
-                                else hi = mid;
+                            unsigned int a = 0, b = len[d];
+                            while (a < b) {
+                                const unsigned int mid = (a + b) >> 1;
+                                if (sk[mid] <= tk) a = mid + 1;
+                                else b = mid;
                             }
-                            p = lo;
+                            p = a;
                         } else {  // later voxels: the positions only move forward
-                            while (p < L && sk[p] <= t) ++p;
+                            while (p < len[d] && sk[p] <= tk) ++p;
                         }
                         pos[d] = p;
                         // walk_ptr = min(n - 2, upper_bound - 1), upper_bound = lo + p;
                         // w[d] is the staged index of that position
-                        w[d] = min(s_lo[d] + p - 1u, n - 2u) - s_lo[d];
+                        w[d] = min(lo[d] + p - 1u, n - 2u) - lo[d];
                     }
                     // corners: self, +x, +y, +xy, +z, +xz, +yz, +xyz (Mesher.cpp:122-132, 174-181)
                     const K* ky = s_key;
                     const K* kz = s_key + kStage;
                     const float2* vy = s_val;
                     const float2* vz = s_val + kStage;
-                    c.idx[2] = s_lo[0] + w[0];
+                    c.idx[2] = lo[0] + w[0];
                     c.val[2] = ky[w[0]] == key + delta[0] ? vy[w[0]] : zero;
-                    c.idx[4] = s_lo[1] + w[1];
+                    c.idx[4] = lo[1] + w[1];
                     c.val[4] = kz[w[1]] == key + delta[1] ? vz[w[1]] : zero;
                     if (kTris) {
                         const K* kyz = s_key + (kD - 1) * kStage;
                         const float2* vyz = s_val + (kD - 1) * kStage;
                         const unsigned int wy = w[kD - 1];
-                        c.idx[6] = s_lo[kD - 1] + wy;
+                        c.idx[6] = lo[kD - 1] + wy;
                         c.val[6] = kyz[wy] == key + delta[2] ? vyz[wy] : zero;
                         c.idx[3] = c.idx[2] + 1;
                         c.val[3] = ky[w[0] + 1] == key + cd.pack(1, 1, 0) ? vy[w[0] + 1] : zero;
@@ -655,6 +658,7 @@ cudaError_t mesh_scratch_reserve(MeshScratch* m, size_t n, int kb) {
     if ((e = cudaMalloc(&m->tscan, cap * sizeof(unsigned long long)))) return e;
     if ((e = cudaMalloc(&m->block_sums, ((cap + kScanTile - 1) / kScanTile + 1) * 8))) return e;
     if ((e = cudaMalloc(&m->rows, rows * sizeof(unsigned int)))) return e;
+    if ((e = cudaMalloc(&m->tile_ranges, ((cap + kClassTile - 1) / kClassTile + 1) * 3 * sizeof(uint2)))) return e;
     m->rows_cap = rows;
     if ((e = cudaMalloc(&m->counts, sizeof(MeshCounts)))) return e;
     if ((e = cudaMalloc(&m->n_dev, sizeof(unsigned int)))) return e;
@@ -669,6 +673,7 @@ void mesh_scratch_free(MeshScratch* m) {
     cudaFree(m->tscan);
     cudaFree(m->block_sums);
     cudaFree(m->rows);
+    cudaFree(m->tile_ranges);
     cudaFree(m->counts);
     cudaFree(m->n_dev);
     *m = MeshScratch{};
@@ -690,17 +695,24 @@ static void mesh_count_t(const K* keys, const float2* vals, size_t n_cap, int kb
     unsigned long long* scan = ms.tscan;
     k_row_directory<K><<<grid_for(((size_t)1 << (2 * kb)) + 1, sms), kThreads, 0, st>>>(keys, ms.n_dev, kb, ms.rows);
     if (stage_events) cudaEventRecord(stage_events[0], st);
-    const int class_grid = grid_for((n_cap + kClassItems - 1) / kClassItems, sms);
+    // tile ranges, then the classification (its grid: up to 8 CTAs per SM, each walking tiles)
+    const unsigned int max_tiles = (unsigned int)((n_cap + kClassTile - 1) / kClassTile);
+    const int offsets = with_indices ? 3 : 2;
+    k_mesh_tile_ranges<K><<<grid_for((size_t)max_tiles * offsets, sms), kThreads, 0, st>>>(
+        keys, kb, ms.rows, ms.n_dev, offsets, ms.tile_ranges, max_tiles);
+    const int class_grid = (int)(max_tiles < (unsigned int)(sms * 8) ? (max_tiles ? max_tiles : 1) : sms * 8);
     if (with_indices) {
         const size_t smem = class_smem<K>(3);
         cudaFuncSetAttribute(k_mesh_classify_tiled<true, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_mesh_classify_tiled<true, K><<<class_grid, kThreads, smem, st>>>(keys, kb, vals, ms.rows, ms.n_dev,
-                                                                          ms.vflags, cnt, ms.corners);
+                                                                          ms.tile_ranges, max_tiles, ms.vflags, cnt,
+                                                                          ms.corners);
     } else {
         const size_t smem = class_smem<K>(2);
         cudaFuncSetAttribute(k_mesh_classify_tiled<false, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_mesh_classify_tiled<false, K><<<class_grid, kThreads, smem, st>>>(keys, kb, vals, ms.rows, ms.n_dev,
-                                                                           ms.vflags, cnt, ms.corners);
+                                                                           ms.tile_ranges, max_tiles, ms.vflags,
+                                                                           cnt, ms.corners);
     }
     if (stage_events) cudaEventRecord(stage_events[1], st);
     const unsigned int n_tiles = (unsigned int)((n_cap + kScanTile - 1) / kScanTile);
