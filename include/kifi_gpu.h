@@ -411,6 +411,18 @@ KIFI_API kifi_status kifi_volume_load(const char* path, int device, kifi_volume*
 KIFI_API kifi_status kifi_gemm_bf16(const void* a_dev, const void* b_dev, float* c_dev, int m, int n, int k,
                                     int lda, int ldb, int ldc, int k_split, int accumulate, void* stream);
 
+/* No counterpart in the reference.  The proposer's convolution: a 3x3,
+ * stride 2, padding 1 convolution of x [batch][height][width][cin] (NHWC
+ * BF16, cin 32 or 64) with weights w [cout][kp] (BF16, k = (ky * 3 + kx) *
+ * cin + c, cout 64 or 128, kp >= 9 cin) as an implicit GEMM on the tcgen05
+ * tensor cores (TMA gathers the input windows; no im2col matrix):
+ * out [batch][(height+1)/2][(width+1)/2][cout] = bf16(relu?(conv + bias)),
+ * FP32 accumulation, bias FP32 [cout] or NULL.  Synchronous on `stream`;
+ * reports through the same status word as kifi_gemm_bf16. */
+KIFI_API kifi_status kifi_conv3x3s2_bf16(const void* x_dev, int batch, int height, int width, int cin,
+                                         const void* w_dev, int cout, int kp, const float* bias_dev, int relu,
+                                         void* out_dev, void* stream);
+
 /* No counterpart in the reference: the learned ICP pose proposer -- a small
  * convolutional network (4 conv 3x3/2 layers 32-64-64-128, global average
  * pool, MLP 128-64-6) mapping two depth frames box-downsampled to 80 x 60 to

@@ -91,6 +91,8 @@ SIGNATURES = {
                                   C.c_int, C.POINTER(C.c_int)]),
     "kifi_gemm_bf16": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
                                  C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p]),
+    "kifi_conv3x3s2_bf16": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int,
+                                      C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "kifi_volume_autotune": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.POINTER(Camera), C.c_void_p, C.c_int,
                                        C.c_void_p]),
     "kifi_proposer_create": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_void_p)]),

@@ -151,11 +151,17 @@ struct MeshCounts {
 };
 
 struct MeshScratch {
-    unsigned int* vflags = nullptr;        // per voxel: vertex axes | index count<<8 | case<<16
-    uint4* corners = nullptr;              // per flagged voxel: indices of its +y, +z, +yz lookups
-    unsigned long long* vscan = nullptr;   // per voxel packed (index count << 32 | vertex count)
-    unsigned long long* tscan = nullptr;   // exclusive scan of vscan
-    unsigned long long* block_sums = nullptr;
+    // per voxel: vertex axes | triangle count << 3 | marching-cubes case << 6 |
+    // the voxel's first vertex within its classification tile << 14
+    unsigned int* vflags = nullptr;
+    // per voxel with output: indices of its +y, +z, +yz lookups and its first
+    // index within its classification tile
+    uint4* corners = nullptr;
+    // per classification tile: packed (index count << 32 | vertex count),
+    // then (after the scan) their exclusive prefix
+    unsigned long long* tile_sums = nullptr;
+    unsigned int* tile_nflag = nullptr;    // per tile: its voxels with output
+    unsigned int* flagged = nullptr;       // per tile of 512 slots: those voxels, ascending
     unsigned int* rows = nullptr;          // start index of each (z, y) key row
     uint2* tile_ranges = nullptr;          // per classification tile and offset: staged range (start, length)
     MeshCounts* counts = nullptr;
@@ -255,10 +261,29 @@ cudaError_t bin_enqueue(const float* pts, unsigned int n, const Mat4& w2c, int w
 cudaError_t bin_target_enqueue(const float* pts, unsigned int n, const Mat4& w2c, int width, int height,
                                unsigned long long* zbuf, float4* out, int ctas, cudaStream_t st);
 
+// Optional epilogue of gemm_bf16_enqueue: C = acc + bias[n] (FP32), or with
+// out_bf16 set, out_bf16 = bf16(relu?(acc + bias[n])) (row stride ldc) in
+// place of C.
+struct GemmEpilogue {
+    const float* bias = nullptr;
+    bool relu = false;
+    void* out_bf16 = nullptr;
+};
+
 // C[M x N] (+)= A[M x K] * B[N x K]^T, BF16 in, FP32 out, on tcgen05 tensor
-// cores (kifi_tc_gemm.cu).  k_split > 0 splits K across CTAs that add into C
-// atomically (atomic must then be true and C pre-initialised).
+// cores with TMA-fed operands (kifi_tc_gemm.cu).  k_split > 0 splits K
+// across tiles that add into C atomically (atomic must then be true and C
+// pre-initialised; the split is rounded up to a multiple of 64).
 cudaError_t gemm_bf16_enqueue(const void* A, const void* B, float* C, int M, int N, int K, int lda, int ldb,
-                              int ldc, int k_split, bool atomic, unsigned int* status, cudaStream_t st);
+                              int ldc, int k_split, bool atomic, unsigned int* status, cudaStream_t st,
+                              const GemmEpilogue* epi = nullptr);
+
+// 3x3 / stride 2 / pad 1 convolution of an NHWC BF16 input [batch][H][W][Cin]
+// (Cin 32 or 64) with weights [Co][Kp] (k = (ky * 3 + kx) * Cin + c, Co 64 or
+// 128) as an implicit GEMM on the tensor cores: out_bf16 [batch][Ho][Wo][Co]
+// = bf16(relu?(conv + bias)), Ho = (H + 1) / 2, Wo = (W + 1) / 2.
+cudaError_t conv3x3s2_bf16_enqueue(const void* x, int batch, int H, int W, int Cin, const void* Wt, int Co, int Kp,
+                                   const float* bias, bool relu, void* out_bf16, unsigned int* status,
+                                   cudaStream_t st);
 
 }  // namespace kifi

@@ -12,15 +12,22 @@
 //  k_row_directory  start index of every (y, z) key row (key >> b, b key bits
 //                   per axis); a neighbour search then only scans one row,
 //                   starting where the searching voxel sits in its own row.
+//  k_mesh_tile_ranges  per tile of 512 voxels and neighbour offset, the
+//                   range of positions its voxels' lookups fall in.
 //  k_mesh_classify_tiled  per voxel i in [0, n-2] with weight > 0: which of its
 //                   +x/+y/+z edges carry a vertex (Mesher.cpp:140-168) and,
 //                   for Mesh(verts, indices), the cube's marching-cubes case
 //                   and triangle count (:172-226); a voxel with any output
-//                   keeps its +y, +z and +yz lookups for emission.
-//  k_scan_tiles,    one exclusive scan of the packed (vertex, index) counts
-//  k_scan_sums      in ascending voxel order (per tile, then the tile sums).
-//  k_mesh_emit      writes the vertices (by the voxel's lane) and the
-//                   triangle indices (spread over the warp's lanes).
+//                   keeps its +y, +z and +yz lookups for emission.  Per tile
+//                   it also scans the vertex and index counts (a voxel's
+//                   first vertex within the tile goes into its flags, its
+//                   first index beside its lookups), lists the tile's voxels
+//                   with output and writes the tile's packed (index, vertex)
+//                   totals.
+//  k_scan_tile_sums one CTA turns the tile totals into tile offsets.
+//  k_mesh_emit      per tile, over its list of voxels with output: writes the
+//                   vertices (by the voxel's lane) and the triangle indices
+//                   (spread over the warp's lanes).
 //
 // Output order equals the reference's:
 //  * Mesh(verts): vertices in generation order -- voxels descending, axes
@@ -102,18 +109,39 @@ __device__ __forceinline__ unsigned int walk_ptr(const K* keys, const unsigned i
 
 __device__ __forceinline__ float vdist(float2 v) { return fdiv(v.x, v.y); }  // Voxel::Distance
 
-// per-voxel packed counts are scanned in tiles of kScanTile
-constexpr int kScanItems = 4;
-constexpr int kScanTile = kThreads * kScanItems;
+// Packed per-voxel flags: bits 0-2 the vertex axes, 3-5 the triangle count,
+// 6-13 the marching-cubes case, 14-24 the voxel's first vertex within its
+// classification tile (at most 3 x 512 = 1536).
+__device__ __forceinline__ unsigned int f_axes(unsigned int f) { return f & 7u; }
+__device__ __forceinline__ unsigned int f_tris(unsigned int f) { return (f >> 3) & 7u; }
+__device__ __forceinline__ unsigned int f_case(unsigned int f) { return (f >> 6) & 0xffu; }
+__device__ __forceinline__ unsigned int f_vofs(unsigned int f) { return f >> 14; }
 
-// A voxel's exclusive prefix of the packed counts: its offset within its
-// scan tile plus the tile's offset.
-__device__ __forceinline__ unsigned long long scan_at(const unsigned long long* __restrict__ scan,
-                                                      const unsigned long long* __restrict__ tile_offsets,
-                                                      unsigned int i) {
-    return scan[i] + tile_offsets[i / kScanTile];
+// exclusive scan of one 64-bit value per thread over a CTA of kT threads;
+// the CTA's total to *total
+template <int kT>
+__device__ __forceinline__ unsigned long long block_exclusive_scan(unsigned long long x,
+                                                                   unsigned long long* total) {
+    __shared__ unsigned long long warp_sums[kT / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned long long inc = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        unsigned long long y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+    }
+    if (lane == 31) warp_sums[warp] = inc;
+    __syncthreads();
+    unsigned long long before = 0, all = 0;
+#pragma unroll
+    for (int w = 0; w < kT / 32; ++w) {
+        if (w < warp) before += warp_sums[w];
+        all += warp_sums[w];
+    }
+    __syncthreads();
+    *total = all;
+    return before + inc - x;
 }
-
 
 struct Cube {
     unsigned int idx[8];  // voxel index of each corner (valid where found)
@@ -156,14 +184,31 @@ __device__ __forceinline__ void load_cube(const K* __restrict__ keys,
 }
 
 // vertex axes of a voxel: bit a set when edge +a carries a vertex
+// Mesher.cpp:140-168's test Distance(self) * Distance(neighbour) <= 0
+// without the divisions where its outcome is certain: for 2^-30 <= |x|, |w|
+// <= 2^30 (both voxels) each quotient x / w is a float of magnitude in
+// [2^-60, 2^60], so their product is a normal non-zero float (magnitude in
+// [2^-120, 2^120]) whose sign is the product of the four operand signs; it
+// is <= 0 exactly when the two quotients differ in sign.  Zeros, NaNs,
+// infinities and the rest of the range take the reference's divisions.
+__device__ __forceinline__ bool in_sign_range(float2 v) {
+    const float ax = fabsf(v.x), aw = fabsf(v.y);
+    return ax >= 0x1p-30f && ax <= 0x1p30f && aw >= 0x1p-30f && aw <= 0x1p30f;
+}
 __device__ __forceinline__ unsigned int vertex_axes(const Cube& c) {
-    const float dself = vdist(c.val[0]);
+    const float2 sv = c.val[0];
+    const bool s_ok = in_sign_range(sv);
+    const bool s_neg = (sv.x < 0.0f) != (sv.y < 0.0f);
     unsigned int axes = 0;
     const int nb[3] = {1, 2, 4};
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         const float2 o = c.val[nb[a]];
-        if (o.y > 0.0f && fmul(dself, vdist(o)) <= 0.0f) axes |= 1u << a;
+        if (!(o.y > 0.0f)) continue;
+        bool crosses;
+        if (s_ok && in_sign_range(o)) crosses = s_neg != ((o.x < 0.0f) != (o.y < 0.0f));
+        else crosses = fmul(vdist(sv), vdist(o)) <= 0.0f;
+        if (crosses) axes |= 1u << a;
     }
     return axes;
 }
@@ -188,35 +233,25 @@ __device__ __forceinline__ int cube_case(const Cube& c) {
 }
 
 // One voxel's classification from its cube (live: the voxel is in [0, n-2]
-// with a non-zero weight, and c holds its corners): flags per voxel -- bits
-// 0-2 vertex axes, bits 8-15 index count, 16-23 case -- the packed
-// (index count, vertex count) for the scan, and, for a voxel with output,
-// its +y, +z and +yz lookups for emission.
+// with a non-zero weight, and c holds its corners): its flags without the
+// tile offset -- vertex axes, triangle count, case.
 template <bool kTris>
-__device__ __forceinline__ void classify_voxel(const Cube& c, bool live, unsigned int i, const uint64_t* s_mc,
-                                               unsigned int* __restrict__ flags,
-                                               unsigned long long* __restrict__ counts,
-                                               uint4* __restrict__ corners) {
-    unsigned int f = 0, nv = 0, ni = 0;
+__device__ __forceinline__ unsigned int classify_voxel(const Cube& c, bool live, const uint64_t* s_mc) {
+    unsigned int f = 0;
     if (live) {
-        const unsigned int axes = vertex_axes(c);
-        nv = __popc(axes);
-        f = axes;
+        f = vertex_axes(c);
         if (kTris) {
             bool skip = false;
 #pragma unroll
             for (int q = 1; q < 8; ++q) skip |= (0.0f == c.val[q].y);
             if (!skip) {
                 const int lut = cube_case(c);
-                ni = 3u * mc_tri_count_of(s_mc[lut]);
-                f |= ni << 8 | (unsigned int)lut << 16;
+                const unsigned int tris = mc_tri_count_of(s_mc[lut]);
+                if (tris) f |= tris << 3 | (unsigned int)lut << 6;
             }
         }
-        // emission reuses these lookups instead of searching again
-        if (f) corners[i] = make_uint4(c.idx[2], c.idx[4], kTris ? c.idx[6] : 0u, 0u);
     }
-    flags[i] = f;
-    counts[i] = (unsigned long long)ni << 32 | nv;
+    return f;
 }
 
 // Classification by tiles of kClassTile consecutive voxels.  For a
@@ -276,7 +311,9 @@ __global__ void __launch_bounds__(kThreads) k_mesh_classify_tiled(const K* __res
                                                                   const uint2* __restrict__ ranges,
                                                                   unsigned int max_tiles,
                                                                   unsigned int* __restrict__ flags,
-                                                                  unsigned long long* __restrict__ counts,
+                                                                  unsigned long long* __restrict__ tile_sums,
+                                                                  unsigned int* __restrict__ tile_nflag,
+                                                                  unsigned int* __restrict__ flagged,
                                                                   uint4* __restrict__ corners) {
     constexpr int kD = kTris ? 3 : 2;  // offsets looked up: +y, +z (and +yz)
     constexpr int kStage = kClassStage;
@@ -325,6 +362,10 @@ __global__ void __launch_bounds__(kThreads) k_mesh_classify_tiled(const K* __res
         unsigned int pos[kD];  // running count of staged keys <= key + d
 #pragma unroll
         for (int d = 0; d < kD; ++d) pos[d] = 0xffffffffu;
+        unsigned int fl[kClassItems];
+        uint3 look[kClassItems];  // the +y, +z, +yz lookups, kept for emission
+#pragma unroll
+        for (int j = 0; j < kClassItems; ++j) fl[j] = 0u;
 #pragma unroll
         for (int j = 0; j < kClassItems; ++j) {
             const unsigned int i = i0 + tb + j;
@@ -389,7 +430,42 @@ __global__ void __launch_bounds__(kThreads) k_mesh_classify_tiled(const K* __res
                     }
                 }
             }
-            classify_voxel<kTris>(c, live, i, s_mc, flags, counts, corners);
+            fl[j] = classify_voxel<kTris>(c, live, s_mc);
+            look[j] = make_uint3(c.idx[2], c.idx[4], kTris ? c.idx[6] : 0u);
+        }
+        // in-tile offsets of the vertices (into the flags), of the indices
+        // (beside the lookups) and of the voxels with output (their list),
+        // one CTA scan of (output voxels << 48 | indices << 24 | vertices)
+        unsigned int nv = 0, ni = 0, nf = 0;
+#pragma unroll
+        for (int j = 0; j < kClassItems; ++j) {
+            nv += __popc(f_axes(fl[j]));
+            ni += 3u * f_tris(fl[j]);
+            nf += fl[j] ? 1u : 0u;
+        }
+        unsigned long long total;
+        const unsigned long long ex = block_exclusive_scan<kThreads>(
+            (unsigned long long)nf << 48 | (unsigned long long)ni << 24 | nv, &total);
+        unsigned int vo = (unsigned int)(ex & 0xffffffu), io = (unsigned int)((ex >> 24) & 0xffffffu);
+        unsigned int fo = (unsigned int)(ex >> 48);
+#pragma unroll
+        for (int j = 0; j < kClassItems; ++j) {
+            const unsigned int i = i0 + tb + j;
+            if (i < i1) {
+                flags[i] = fl[j] | vo << 14;
+                if (fl[j]) {
+                    // emission reuses the lookups instead of searching again
+                    corners[i] = make_uint4(look[j].x, look[j].y, look[j].z, io);
+                    flagged[i0 + fo] = i;
+                    ++fo;
+                }
+            }
+            vo += __popc(f_axes(fl[j]));
+            io += 3u * f_tris(fl[j]);
+        }
+        if (threadIdx.x == 0) {
+            tile_sums[t] = (total >> 24 & 0xffffffull) << 32 | (total & 0xffffffull);
+            tile_nflag[t] = (unsigned int)(total >> 48);
         }
     }
 }
@@ -416,15 +492,20 @@ constexpr unsigned int kEdgeAxes = 0x558888u;
 __device__ __forceinline__ int edge_corner(int e) { return (int)((kEdgeCorners >> (4 * e)) & 15u); }
 __device__ __forceinline__ int edge_axis(int e) { return (int)((kEdgeAxes >> (2 * e)) & 3u); }
 
+// Emission: each warp takes the voxels with output of one classification
+// tile (their list, ascending), 32 at a time.  A voxel's first vertex is its
+// tile's vertex offset plus the in-tile offset in its flags, its first index
+// slot its tile's index offset plus the in-tile offset kept beside its
+// lookups.
 template <bool kTris, typename K>
 __global__ void __launch_bounds__(kThreads) k_mesh_emit(const K* __restrict__ keys, int kb,
                                                         const float2* __restrict__ vals,
-                                                        const unsigned int* __restrict__ rs,
                                                         const unsigned int* __restrict__ n_dev, Geom g,
                                                         const unsigned int* __restrict__ flags,
                                                         const uint4* __restrict__ corners,
-                                                        const unsigned long long* __restrict__ scan,
-                                                        const unsigned long long* __restrict__ tile_offsets,
+                                                        const unsigned long long* __restrict__ tile_ofs,
+                                                        const unsigned int* __restrict__ tile_nflag,
+                                                        const unsigned int* __restrict__ flagged,
                                                         MeshCounts* __restrict__ mc,
                                                         unsigned long long vert_cap,
                                                         unsigned long long idx_cap,
@@ -465,20 +546,25 @@ __global__ void __launch_bounds__(kThreads) k_mesh_emit(const K* __restrict__ ke
     __shared__ unsigned int s_excl[kWarps][33];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned int warps = gridDim.x * kWarps;
-    for (unsigned int base = (blockIdx.x * kWarps + warp) * 32u; base < n; base += warps * 32u) {
-        const unsigned int i = base + lane;
-        const unsigned int f = i < n ? flags[i] : 0u;
+    const unsigned int tiles = (n + kClassTile - 1) / kClassTile;
+    // each warp takes a tile's voxels with output, 32 at a time
+    for (unsigned int tile = blockIdx.x * kWarps + warp; tile < tiles; tile += warps)
+    for (unsigned int c0 = 0, cnt = tile_nflag[tile]; c0 < cnt; c0 += 32u) {
+        const unsigned long long tofs = tile_ofs[tile];
+        const unsigned int k = c0 + lane;
+        const unsigned int i = k < cnt ? flagged[tile * kClassTile + k] : 0u;
+        const unsigned int f = k < cnt ? flags[i] : 0u;
         unsigned int cidx[8];
-        unsigned long long s = 0;
+        uint4 cr = make_uint4(0u, 0u, 0u, 0u);
         if (f) {
-            stored_cube(i, corners[i], cidx);
-            s = scan_at(scan, tile_offsets, i);
+            cr = corners[i];
+            stored_cube(i, cr, cidx);
         }
-        const unsigned int axes = f & 7u;
+        const unsigned int axes = f_axes(f);
         // vertices (Mesher.cpp:134-168): at most three per voxel, by the voxel's lane
         if (axes) {
             const K key = keys[i];
-            const unsigned int vbase = (unsigned int)(s & 0xffffffffu);
+            const unsigned int vbase = (unsigned int)(tofs & 0xffffffffu) + f_vofs(f);
             const unsigned int nv = __popc(axes);
             const unsigned long long first =
                 kTris ? vbase : n_verts - vbase - nv;  // ascending ids / generation order
@@ -503,7 +589,7 @@ __global__ void __launch_bounds__(kThreads) k_mesh_emit(const K* __restrict__ ke
             }
         }
         if constexpr (kTris) {
-            const unsigned int ni = (f >> 8) & 0xffu;
+            const unsigned int ni = 3u * f_tris(f);
             unsigned int inc = ni;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
@@ -516,8 +602,9 @@ __global__ void __launch_bounds__(kThreads) k_mesh_emit(const K* __restrict__ ke
             s_excl[warp][lane] = inc - ni;
             if (lane == 31) s_excl[warp][32] = inc;
             if (ni) {
-                s_mcw[warp][lane] = s_mc[(f >> 16) & 0xffu];  // the case's triangle edges
-                s_first[warp][lane] = (unsigned int)(n_idx - (s >> 32) - ni);  // generation order
+                s_mcw[warp][lane] = s_mc[f_case(f)];  // the case's triangle edges
+                // generation order: voxels descending
+                s_first[warp][lane] = (unsigned int)(n_idx - ((tofs >> 32) + cr.w) - ni);
 #pragma unroll
                 for (int k = 0; k < 8; ++k) s_cidx[warp][k][lane] = cidx[k];
             }
@@ -544,8 +631,8 @@ __global__ void __launch_bounds__(kThreads) k_mesh_emit(const K* __restrict__ ke
                     need_id ? 3ull * (unsigned long long)keys[ci] + (unsigned long long)axis : 0ull;
                 uint32_t outv;
                 if (has) {
-                    outv = (unsigned int)(scan_at(scan, tile_offsets, ci) & 0xffffffffu) +
-                           __popc(cf & 7u & ((1u << axis) - 1u));
+                    outv = (unsigned int)(tile_ofs[ci / kClassTile] & 0xffffffffu) + f_vofs(cf) +
+                           __popc(f_axes(cf) & ((1u << axis) - 1u));
                 } else {
                     outv = (uint32_t)id;
                     local_min = min(local_min, id);
@@ -558,67 +645,16 @@ __global__ void __launch_bounds__(kThreads) k_mesh_emit(const K* __restrict__ ke
     }
 }
 
-// -------------------------------------------------------- exclusive scan
-// Two-level exclusive scan of packed 64-bit (index count << 32 | vertex
-// count) values; both halves stay below 2^32 for volumes under 2^28 voxels.
-
-__device__ __forceinline__ unsigned long long block_exclusive_scan(unsigned long long x,
-                                                                   unsigned long long* total) {
-    __shared__ unsigned long long warp_sums[kThreads / 32];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    unsigned long long inc = x;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        unsigned long long y = __shfl_up_sync(0xffffffffu, inc, o);
-        if (lane >= o) inc += y;
-    }
-    if (lane == 31) warp_sums[warp] = inc;
-    __syncthreads();
-    unsigned long long before = 0, all = 0;
-#pragma unroll
-    for (int w = 0; w < kThreads / 32; ++w) {
-        if (w < warp) before += warp_sums[w];
-        all += warp_sums[w];
-    }
-    __syncthreads();
-    *total = all;
-    return before + inc - x;
-}
-
-__global__ void __launch_bounds__(kThreads) k_scan_tiles(const unsigned long long* __restrict__ in,
-                                                         unsigned long long* __restrict__ out,
-                                                         unsigned long long* __restrict__ tile_sums,
-                                                         const unsigned int* __restrict__ n_dev) {
-    const unsigned int n = *n_dev;
-    const unsigned int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
-    unsigned long long v[kScanItems], s = 0;
-#pragma unroll
-    for (int q = 0; q < kScanItems; ++q) {
-        v[q] = base + q < n ? in[base + q] : 0ull;
-        s += v[q];
-    }
-    unsigned long long total;
-    unsigned long long run = block_exclusive_scan(s, &total);
-#pragma unroll
-    for (int q = 0; q < kScanItems; ++q) {
-        if (base + q < n) out[base + q] = run;
-        run += v[q];
-    }
-    if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
-}
-
-// single CTA: exclusive scan of the tile sums (in place), total to counts;
-// each thread takes kSumItems consecutive sums per round
-constexpr int kSumItems = 8;
-__global__ void __launch_bounds__(kThreads) k_scan_sums(unsigned long long* __restrict__ sums,
-                                                        unsigned int n_tiles,
-                                                        const unsigned int* __restrict__ n_dev,
-                                                        MeshCounts* __restrict__ counts) {
-    // only the tiles that hold voxels (the grid covers an upper bound)
-    const unsigned int used = (*n_dev + kScanTile - 1) / kScanTile;
-    if (used < n_tiles) n_tiles = used;
+// single CTA: exclusive scan (in place) of the classification tiles' packed
+// (index count << 32 | vertex count), the totals to *counts; both halves stay
+// below 2^32 for volumes under 2^28 voxels
+constexpr int kSumThreads = 1024, kSumItems = 8;
+__global__ void __launch_bounds__(kSumThreads) k_scan_tile_sums(unsigned long long* __restrict__ sums,
+                                                                const unsigned int* __restrict__ n_dev,
+                                                                MeshCounts* __restrict__ counts) {
+    const unsigned int n_tiles = (*n_dev + kClassTile - 1) / kClassTile;
     unsigned long long carry = 0;
-    for (unsigned int b = 0; b < n_tiles; b += kThreads * kSumItems) {
+    for (unsigned int b = 0; b < n_tiles; b += kSumThreads * kSumItems) {
         const unsigned int i0 = b + threadIdx.x * kSumItems;
         unsigned long long v[kSumItems], s = 0;
 #pragma unroll
@@ -627,7 +663,7 @@ __global__ void __launch_bounds__(kThreads) k_scan_sums(unsigned long long* __re
             s += v[q];
         }
         unsigned long long total;
-        unsigned long long run = carry + block_exclusive_scan(s, &total);
+        unsigned long long run = carry + block_exclusive_scan<kSumThreads>(s, &total);
 #pragma unroll
         for (int q = 0; q < kSumItems; ++q) {
             if (i0 + q < n_tiles) sums[i0 + q] = run;
@@ -651,14 +687,15 @@ cudaError_t mesh_scratch_reserve(MeshScratch* m, size_t n, int kb) {
     if (n < m->cap) n = m->cap;
     mesh_scratch_free(m);
     size_t cap = n < 1024 ? 1024 : n;
+    const size_t tiles = (cap + kClassTile - 1) / kClassTile + 1;
     cudaError_t e;
     if ((e = cudaMalloc(&m->vflags, cap * sizeof(unsigned int)))) return e;
     if ((e = cudaMalloc(&m->corners, cap * sizeof(uint4)))) return e;
-    if ((e = cudaMalloc(&m->vscan, cap * sizeof(unsigned long long)))) return e;
-    if ((e = cudaMalloc(&m->tscan, cap * sizeof(unsigned long long)))) return e;
-    if ((e = cudaMalloc(&m->block_sums, ((cap + kScanTile - 1) / kScanTile + 1) * 8))) return e;
+    if ((e = cudaMalloc(&m->tile_sums, tiles * sizeof(unsigned long long)))) return e;
+    if ((e = cudaMalloc(&m->tile_nflag, tiles * sizeof(unsigned int)))) return e;
+    if ((e = cudaMalloc(&m->flagged, tiles * kClassTile * sizeof(unsigned int)))) return e;
     if ((e = cudaMalloc(&m->rows, rows * sizeof(unsigned int)))) return e;
-    if ((e = cudaMalloc(&m->tile_ranges, ((cap + kClassTile - 1) / kClassTile + 1) * 3 * sizeof(uint2)))) return e;
+    if ((e = cudaMalloc(&m->tile_ranges, tiles * 3 * sizeof(uint2)))) return e;
     m->rows_cap = rows;
     if ((e = cudaMalloc(&m->counts, sizeof(MeshCounts)))) return e;
     if ((e = cudaMalloc(&m->n_dev, sizeof(unsigned int)))) return e;
@@ -669,9 +706,9 @@ cudaError_t mesh_scratch_reserve(MeshScratch* m, size_t n, int kb) {
 void mesh_scratch_free(MeshScratch* m) {
     cudaFree(m->vflags);
     cudaFree(m->corners);
-    cudaFree(m->vscan);
-    cudaFree(m->tscan);
-    cudaFree(m->block_sums);
+    cudaFree(m->tile_sums);
+    cudaFree(m->tile_nflag);
+    cudaFree(m->flagged);
     cudaFree(m->rows);
     cudaFree(m->tile_ranges);
     cudaFree(m->counts);
@@ -690,9 +727,6 @@ static int grid_for(size_t n, int sms) {
 template <typename K>
 static void mesh_count_t(const K* keys, const float2* vals, size_t n_cap, int kb, int with_indices, MeshScratch& ms,
                          int sms, cudaStream_t st, cudaEvent_t* stage_events) {
-    // vscan holds the per-voxel packed counts, tscan their exclusive scan
-    unsigned long long* cnt = ms.vscan;
-    unsigned long long* scan = ms.tscan;
     k_row_directory<K><<<grid_for(((size_t)1 << (2 * kb)) + 1, sms), kThreads, 0, st>>>(keys, ms.n_dev, kb, ms.rows);
     if (stage_events) cudaEventRecord(stage_events[0], st);
     // tile ranges, then the classification (its grid: up to 8 CTAs per SM, each walking tiles)
@@ -705,19 +739,19 @@ static void mesh_count_t(const K* keys, const float2* vals, size_t n_cap, int kb
         const size_t smem = class_smem<K>(3);
         cudaFuncSetAttribute(k_mesh_classify_tiled<true, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_mesh_classify_tiled<true, K><<<class_grid, kThreads, smem, st>>>(keys, kb, vals, ms.rows, ms.n_dev,
-                                                                          ms.tile_ranges, max_tiles, ms.vflags, cnt,
+                                                                          ms.tile_ranges, max_tiles, ms.vflags,
+                                                                          ms.tile_sums, ms.tile_nflag, ms.flagged,
                                                                           ms.corners);
     } else {
         const size_t smem = class_smem<K>(2);
         cudaFuncSetAttribute(k_mesh_classify_tiled<false, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_mesh_classify_tiled<false, K><<<class_grid, kThreads, smem, st>>>(keys, kb, vals, ms.rows, ms.n_dev,
                                                                            ms.tile_ranges, max_tiles, ms.vflags,
-                                                                           cnt, ms.corners);
+                                                                           ms.tile_sums, ms.tile_nflag, ms.flagged,
+                                                                           ms.corners);
     }
     if (stage_events) cudaEventRecord(stage_events[1], st);
-    const unsigned int n_tiles = (unsigned int)((n_cap + kScanTile - 1) / kScanTile);
-    k_scan_tiles<<<n_tiles ? n_tiles : 1, kThreads, 0, st>>>(cnt, scan, ms.block_sums, ms.n_dev);
-    k_scan_sums<<<1, kThreads, 0, st>>>(ms.block_sums, n_tiles ? n_tiles : 1, ms.n_dev, ms.counts);
+    k_scan_tile_sums<<<1, kSumThreads, 0, st>>>(ms.tile_sums, ms.n_dev, ms.counts);
 }
 
 cudaError_t mesh_count_enqueue(const void* keys, int key_bytes, const float2* vals, size_t n_cap, int kb,
@@ -735,20 +769,20 @@ template <typename K>
 static void mesh_emit_t(const Geom& g, const K* keys, const float2* vals, size_t n_cap, int with_indices,
                         MeshScratch& ms, size_t vert_cap, size_t idx_cap, float* verts_dev, uint32_t* idx_dev,
                         int sms, cudaStream_t st) {
-    const unsigned long long* scan = ms.tscan;
     unsigned long long* mm = &ms.counts->missing_min;
     const int kb = sizeof(K) == 4 ? 10 : g.kb;
+    const int grid = grid_for(n_cap, sms);
     if (with_indices) {
-        k_mesh_emit<true, K><<<grid_for(n_cap, sms), kThreads, 0, st>>>(keys, kb, vals, ms.rows, ms.n_dev, g,
-                                                                         ms.vflags, ms.corners, scan, ms.block_sums, ms.counts,
-                                                                         vert_cap, idx_cap, ~0ull, nullptr, verts_dev, idx_dev, mm);
-        k_mesh_emit<true, K><<<grid_for(n_cap, sms), kThreads, 0, st>>>(keys, kb, vals, ms.rows, ms.n_dev, g,
-                                                                         ms.vflags, ms.corners, scan, ms.block_sums, ms.counts,
-                                                                         vert_cap, idx_cap, 0ull, mm, verts_dev, idx_dev, nullptr);
+        k_mesh_emit<true, K><<<grid, kThreads, 0, st>>>(keys, kb, vals, ms.n_dev, g, ms.vflags, ms.corners,
+                                                          ms.tile_sums, ms.tile_nflag, ms.flagged, ms.counts, vert_cap, idx_cap, ~0ull, nullptr,
+                                                          verts_dev, idx_dev, mm);
+        k_mesh_emit<true, K><<<grid, kThreads, 0, st>>>(keys, kb, vals, ms.n_dev, g, ms.vflags, ms.corners,
+                                                          ms.tile_sums, ms.tile_nflag, ms.flagged, ms.counts, vert_cap, idx_cap, 0ull, mm,
+                                                          verts_dev, idx_dev, nullptr);
     } else {
-        k_mesh_emit<false, K><<<grid_for(n_cap, sms), kThreads, 0, st>>>(keys, kb, vals, ms.rows, ms.n_dev, g,
-                                                                          ms.vflags, ms.corners, scan, ms.block_sums, ms.counts,
-                                                                          vert_cap, idx_cap, ~0ull, nullptr, verts_dev, idx_dev, mm);
+        k_mesh_emit<false, K><<<grid, kThreads, 0, st>>>(keys, kb, vals, ms.n_dev, g, ms.vflags, ms.corners,
+                                                           ms.tile_sums, ms.tile_nflag, ms.flagged, ms.counts, vert_cap, idx_cap, ~0ull, nullptr,
+                                                           verts_dev, idx_dev, mm);
     }
 }
 
@@ -765,20 +799,49 @@ cudaError_t mesh_emit_enqueue(const Geom& g, const void* keys, int key_bytes, co
 }
 
 // Copy of the resident voxels (buffer ctl->cur, ctl->n[cur] of them) for a
-// mesh that runs while fusion goes on; the count goes to *n_dev.
+// mesh that runs while fusion goes on; the count goes to *n_dev.  16-byte
+// loads (four 32-bit or two 64-bit keys, two voxels), four in flight per
+// thread, streaming past L1; the buffers are cudaMalloc'd (256-byte aligned).
 template <typename K>
-__global__ void k_mesh_snapshot(const DeviceCtl* __restrict__ ctl, VolumeBuffers vb, K* __restrict__ keys,
-                                float2* __restrict__ vals, unsigned long long cap, unsigned int* __restrict__ n_dev) {
+__global__ void __launch_bounds__(256) k_mesh_snapshot(const DeviceCtl* __restrict__ ctl, VolumeBuffers vb,
+                                                       K* __restrict__ keys, float2* __restrict__ vals,
+                                                       unsigned long long cap, unsigned int* __restrict__ n_dev) {
+    constexpr unsigned int kPerVec = 16 / sizeof(K);  // keys per 16 bytes
     const unsigned int cur = ctl->cur;
     unsigned long long n = ctl->n[cur];
     if (n > cap) n = cap;
     const K* sk = (const K*)(cur ? vb.keys[1] : vb.keys[0]);
     const float2* sv = cur ? vb.vals[1] : vb.vals[0];
-    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += (unsigned long long)gridDim.x * blockDim.x) {
-        keys[i] = __ldcs(sk + i);
-        vals[i] = __ldcs(sv + i);
+    const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+    const unsigned long long t0 = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+    // keys: n / kPerVec vectors, then the tail
+    const unsigned long long nk = n / kPerVec;
+    const uint4* ks = reinterpret_cast<const uint4*>(sk);
+    uint4* kd = reinterpret_cast<uint4*>(keys);
+    for (unsigned long long i = t0; i < nk; i += 4 * stride) {
+        uint4 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (i + u * stride < nk) v[u] = __ldcs(ks + i + u * stride);
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (i + u * stride < nk) kd[i + u * stride] = v[u];
     }
+    for (unsigned long long i = nk * kPerVec + t0; i < n; i += stride) keys[i] = __ldcs(sk + i);
+    // voxels: two per vector
+    const unsigned long long nv = n / 2;
+    const float4* vs = reinterpret_cast<const float4*>(sv);
+    float4* vd = reinterpret_cast<float4*>(vals);
+    for (unsigned long long i = t0; i < nv; i += 4 * stride) {
+        float4 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (i + u * stride < nv) v[u] = __ldcs(vs + i + u * stride);
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (i + u * stride < nv) vd[i + u * stride] = v[u];
+    }
+    if ((n & 1) && t0 == 0) vals[n - 1] = __ldcs(sv + n - 1);
     if (blockIdx.x == 0 && threadIdx.x == 0) *n_dev = (unsigned int)n;
 }
 

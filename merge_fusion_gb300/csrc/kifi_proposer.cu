@@ -10,9 +10,12 @@
 //   global average pool        -> 128
 //   fc 128->64, ReLU; fc 64->6
 //
-// Activations are NHWC BF16; every product -- convolutions as im2col GEMMs,
-// the fully connected layers, and all their backward products -- runs on the
-// tcgen05 GEMM (kifi_tc_gemm.cu) with FP32 accumulation.  Parameters keep an
+// Activations are NHWC BF16; every product -- convolutions 2-4 as implicit
+// GEMMs whose A tiles TMA gathers straight from the previous activation,
+// convolution 1 through its im2col matrix, the fully connected layers, and
+// all the backward products -- runs on the TMA-fed tcgen05 GEMM
+// (kifi_tc_gemm.cu) with FP32 accumulation; forward products add the bias
+// and apply the ReLU in the GEMM epilogue.  Parameters keep an
 // FP32 master copy updated by Adam, which also writes the BF16 copies the
 // GEMMs read.  Padded parameter entries (conv 1's K = 18 padded to 32, the
 // output layer's 6 rows padded to 16) stay zero.
@@ -126,20 +129,6 @@ __global__ void k_transpose(const bf16* __restrict__ in, int R, int Cc, bf16* __
     for (int j = threadIdx.y; j < 32; j += 8) {
         const int c = c0 + j, r = r0 + threadIdx.x;
         if (r < R && c < Cc) out[(size_t)c * R + r] = t[threadIdx.x][j];
-    }
-}
-
-// act = bf16(relu?(y + bias)), y [M][C] FP32 with row stride ldy
-__global__ void k_bias_act(const float* __restrict__ y, int ldy, const float* __restrict__ bias, int M, int C,
-                           int relu, bf16* __restrict__ act, float* __restrict__ out_f32) {
-    const size_t n = (size_t)M * C;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        const int c = (int)(i % C);
-        const size_t m = i / C;
-        float v = y[m * ldy + c] + bias[c];
-        if (relu) v = fmaxf(v, 0.0f);
-        if (act) act[i] = __float2bfloat16_rn(v);
-        if (out_f32) out_f32[i] = v;
     }
 }
 
@@ -290,8 +279,8 @@ namespace {
 size_t conv_m(int l, int batch) { return (size_t)batch * kHout[l] * kWout[l]; }
 
 kifi_status gemm(kifi_proposer* pr, const void* A, const void* B, float* C, int M, int N, int K, int lda, int ldb,
-                 int ldc, int k_split, bool acc) {
-    KIFI_CUDA(gemm_bf16_enqueue(A, B, C, M, N, K, lda, ldb, ldc, k_split, acc, pr->status, pr->stream));
+                 int ldc, int k_split, bool acc, const GemmEpilogue* epi = nullptr) {
+    KIFI_CUDA(gemm_bf16_enqueue(A, B, C, M, N, K, lda, ldb, ldc, k_split, acc, pr->status, pr->stream, epi));
     return KIFI_OK;
 }
 kifi_status transpose(kifi_proposer* pr, const bf16* in, int R, int Cc, bf16* out) {
@@ -305,7 +294,10 @@ const bf16* wb(const kifi_proposer* pr, int t) { return pr->pb + kLayout.off[t];
 const float* pf(const kifi_proposer* pr, int t) { return pr->p + kLayout.off[t]; }
 float* gf(kifi_proposer* pr, int t) { return pr->g + kLayout.off[t]; }
 
-// forward pass; with `train` the transposed im2col matrices are kept
+// forward pass; with `train` the transposed im2col matrices are kept for the
+// weight gradients.  Convolutions 2-4 run as implicit GEMMs over the previous
+// activation; convolution 1 (Cin = 2) through its im2col matrix.  Bias and
+// ReLU are applied in the GEMM epilogue, which writes the BF16 activation.
 kifi_status forward(kifi_proposer* pr, int batch, bool train) {
     kifi_status s;
     cudaStream_t st = pr->stream;
@@ -315,24 +307,34 @@ kifi_status forward(kifi_proposer* pr, int batch, bool train) {
         if (l == 0)
             k_im2col<__half><<<grid, kThreads, 0, st>>>(pr->x, batch, kHin[0], kWin[0], kCin[0], kHout[0],
                                                         kWout[0], kKp[0], pr->col[0]);
-        else
+        else if (train)
             k_im2col<bf16><<<grid, kThreads, 0, st>>>(pr->act[l - 1], batch, kHin[l], kWin[l], kCin[l], kHout[l],
                                                       kWout[l], kKp[l], pr->col[l]);
         KIFI_CUDA(cudaGetLastError());
         if (train && (s = transpose(pr, pr->col[l], M, kKp[l], pr->colT[l]))) return s;
-        if ((s = gemm(pr, pr->col[l], wb(pr, 2 * l), pr->y, M, kCout[l], kKp[l], kKp[l], kKp[l], kCout[l], 0,
-                      false)))
-            return s;
-        k_bias_act<<<grid, kThreads, 0, st>>>(pr->y, kCout[l], pf(pr, 2 * l + 1), M, kCout[l], 1, pr->act[l],
-                                              nullptr);
+        GemmEpilogue epi;
+        epi.bias = pf(pr, 2 * l + 1);
+        epi.relu = true;
+        epi.out_bf16 = pr->act[l];
+        if (l == 0) {
+            if ((s = gemm(pr, pr->col[0], wb(pr, 0), nullptr, M, kCout[0], kKp[0], kKp[0], kKp[0], kCout[0], 0, false,
+                          &epi)))
+                return s;
+        } else {
+            KIFI_CUDA(conv3x3s2_bf16_enqueue(pr->act[l - 1], batch, kHin[l], kWin[l], kCin[l], wb(pr, 2 * l),
+                                             kCout[l], kKp[l], epi.bias, true, pr->act[l], pr->status, st));
+        }
     }
     k_gap<<<blocks((size_t)batch * 128), kThreads, 0, st>>>(pr->act[3], batch, kHout[3] * kWout[3], 128, pr->gap);
-    if ((s = gemm(pr, pr->gap, wb(pr, 8), pr->y, batch, kFc1, 128, 128, 128, kFc1, 0, false))) return s;
-    k_bias_act<<<blocks((size_t)batch * kFc1), kThreads, 0, st>>>(pr->y, kFc1, pf(pr, 9), batch, kFc1, 1, pr->h1,
-                                                                  nullptr);
-    if ((s = gemm(pr, pr->h1, wb(pr, 10), pr->y, batch, kOutPad, kFc1, kFc1, kFc1, kOutPad, 0, false))) return s;
-    k_bias_act<<<blocks((size_t)batch * kOutPad), kThreads, 0, st>>>(pr->y, kOutPad, pf(pr, 11), batch, kOutPad,
-                                                                     0, nullptr, pr->out);
+    GemmEpilogue e1;
+    e1.bias = pf(pr, 9);
+    e1.relu = true;
+    e1.out_bf16 = pr->h1;
+    if ((s = gemm(pr, pr->gap, wb(pr, 8), nullptr, batch, kFc1, 128, 128, 128, kFc1, 0, false, &e1))) return s;
+    GemmEpilogue e2;
+    e2.bias = pf(pr, 11);
+    if ((s = gemm(pr, pr->h1, wb(pr, 10), pr->out, batch, kOutPad, kFc1, kFc1, kFc1, kOutPad, 0, false, &e2)))
+        return s;
     KIFI_CUDA(cudaGetLastError());
     return KIFI_OK;
 }

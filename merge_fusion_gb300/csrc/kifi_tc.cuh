@@ -1,14 +1,17 @@
 // kifi_tc.cuh -- the sm_100-family tensor-core primitives the pose proposer's
 // GEMMs use, as inline PTX: TMEM allocation, tcgen05.mma (kind::f16, BF16
-// inputs, FP32 accumulator in TMEM), tcgen05.commit to an mbarrier, bounded
+// inputs, FP32 accumulator in TMEM), tcgen05.commit to an mbarrier, TMA
+// tensor loads (cp.async.bulk.tensor) completing on mbarriers, bounded
 // mbarrier waits and tcgen05.ld of the accumulator.
 //
-// Operand tiles live in shared memory in the canonical K-major layout
-// without swizzle: "core matrices" of 8 rows x 16 bytes (8 BF16), each row's
-// 16 bytes contiguous; the two core matrices that one MMA's K = 16 spans are
-// `lbo` bytes apart, and consecutive groups of 8 rows (M or N) `sbo` bytes
-// apart.  The shared-memory descriptor encodes start, lbo and sbo in units of
-// 16 bytes, the descriptor version (1) at bits 46-47 and swizzle mode 0.
+// Operand tiles live in shared memory in a K-major layout the MMA's shared-
+// memory descriptor describes: either without swizzle -- "core matrices" of
+// 8 rows x 16 bytes (8 BF16), each row's 16 bytes contiguous; the two core
+// matrices that one MMA's K = 16 spans `lbo` bytes apart, and consecutive
+// groups of 8 rows (M or N) `sbo` bytes apart -- or as a TMA load with
+// 128-byte swizzle writes it (smem_desc_sw128).  The descriptor encodes
+// start, lbo and sbo in units of 16 bytes, the descriptor version (1) at
+// bits 46-47 and the swizzle mode at bits 61-63.
 #pragma once
 
 #include <cstdint>
@@ -23,6 +26,17 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p) {
 __device__ __forceinline__ uint64_t smem_desc(uint32_t start, uint32_t lbo, uint32_t sbo) {
     return (uint64_t)((start >> 4) & 0x3fffu) | ((uint64_t)((lbo >> 4) & 0x3fffu) << 16) |
            ((uint64_t)((sbo >> 4) & 0x3fffu) << 32) | ((uint64_t)1 << 46);
+}
+
+// K-major operand tile written by a TMA load with 128-byte swizzle: rows of
+// 64 BF16 (128 bytes), groups of 8 rows 1024 bytes apart, the 16-byte
+// chunks of row r stored at chunk index c ^ (r & 7).  The tile base must be
+// 1024-byte aligned; one MMA's K = 16 slice starts 32 bytes further per step
+// (the swizzle is applied to the computed addresses).  Layout type 2 at bits
+// 61-63, stride between 8-row groups 1024 bytes, leading offset unused.
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t start) {
+    return (uint64_t)((start >> 4) & 0x3fffu) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+           ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
 }
 
 // kind::f16 instruction descriptor: D = F32, A = B = BF16, both K-major
@@ -85,6 +99,39 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32
     for (uint32_t i = 0; i < max_polls; ++i)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
+}
+// initialised barriers -> visible to the async proxy (TMA, tensor core)
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// one arrival that also announces `bytes` of asynchronous transfers
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// TMA: the box of a 2-D tensor map at (c0 innermost, c1) into shared memory
+// at dst; completion is counted in bytes on the mbarrier.  Out-of-range
+// elements of the box are written as zeros.  c0 * element size must be a
+// multiple of 16 bytes.
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const void* map, int c0, int c1, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            dst),
+        "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(smem_u32(bar))
+        : "memory");
+}
+// the same for a 4-D tensor map, coordinates innermost first
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const void* map, int c0, int c1, int c2, int c3,
+                                            uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+        "[%6];" ::"r"(dst),
+        "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+        : "memory");
 }
 
 // 32 lanes x 16 consecutive 32-bit columns of TMEM: lane l of the warp gets
