@@ -148,22 +148,35 @@ struct MeshCounts {
     unsigned long long n_idx;
     unsigned long long missing_min;  // smallest triangle edge id without a vertex (or ~0)
     unsigned long long overflow;     // emission skipped: the output buffers were too small
+    unsigned long long n_flagged;    // voxels with output (vertices or triangles)
+};
+
+// per classification tile: the voxels staged for its lookups -- region A,
+// from the tile's first voxel on (the tile itself and its +y lookups), and
+// region B (the +z and +yz lookups) in up to two ranges (lo, len), the second
+// for the tile's voxels from `split` on (split = the tile's end when there is
+// one range)
+struct MeshTileRange {
+    unsigned int a_len, b_lo[2], b_len[2], split;
 };
 
 struct MeshScratch {
     // per voxel: vertex axes | triangle count << 3 | marching-cubes case << 6 |
     // the voxel's first vertex within its classification tile << 14
     unsigned int* vflags = nullptr;
+    unsigned char* vstatus = nullptr;      // per voxel: the status byte classification reads
     // per voxel with output: indices of its +y, +z, +yz lookups and its first
     // index within its classification tile
     uint4* corners = nullptr;
     // per classification tile: packed (index count << 32 | vertex count),
     // then (after the scan) their exclusive prefix
     unsigned long long* tile_sums = nullptr;
-    unsigned int* tile_nflag = nullptr;    // per tile: its voxels with output
-    unsigned int* flagged = nullptr;       // per tile of 512 slots: those voxels, ascending
+    // per tile: its voxels with output, then (after the scan) their exclusive
+    // prefix, with the total at [tiles]
+    unsigned int* tile_nflag = nullptr;
+    unsigned int* flagged = nullptr;       // per tile, a slot per voxel: those voxels, ascending
     unsigned int* rows = nullptr;          // start index of each (z, y) key row
-    uint2* tile_ranges = nullptr;          // per classification tile and offset: staged range (start, length)
+    MeshTileRange* tile_ranges = nullptr;  // per classification tile: the staged regions
     MeshCounts* counts = nullptr;
     unsigned int* n_dev = nullptr;         // the voxel count the passes read
     size_t cap = 0, rows_cap = 0;

@@ -12,8 +12,9 @@
 //  k_row_directory  start index of every (y, z) key row (key >> b, b key bits
 //                   per axis); a neighbour search then only scans one row,
 //                   starting where the searching voxel sits in its own row.
-//  k_mesh_tile_ranges  per tile of 512 voxels and neighbour offset, the
-//                   range of positions its voxels' lookups fall in.
+//  k_mesh_tile_ranges  per tile of 1024 voxels and neighbour offset, the
+//                   ranges of positions its voxels' lookups fall in.
+//  k_mesh_status    one status byte per voxel (weight, distance sign).
 //  k_mesh_classify_tiled  per voxel i in [0, n-2] with weight > 0: which of its
 //                   +x/+y/+z edges carry a vertex (Mesher.cpp:140-168) and,
 //                   for Mesh(verts, indices), the cube's marching-cubes case
@@ -111,7 +112,7 @@ __device__ __forceinline__ float vdist(float2 v) { return fdiv(v.x, v.y); }  // 
 
 // Packed per-voxel flags: bits 0-2 the vertex axes, 3-5 the triangle count,
 // 6-13 the marching-cubes case, 14-24 the voxel's first vertex within its
-// classification tile (at most 3 x 512 = 1536).
+// classification tile (at most 3 x 1024 = 3072).
 __device__ __forceinline__ unsigned int f_axes(unsigned int f) { return f & 7u; }
 __device__ __forceinline__ unsigned int f_tris(unsigned int f) { return (f >> 3) & 7u; }
 __device__ __forceinline__ unsigned int f_case(unsigned int f) { return (f >> 6) & 0xffu; }
@@ -119,7 +120,7 @@ __device__ __forceinline__ unsigned int f_vofs(unsigned int f) { return f >> 14;
 
 // exclusive scan of one 64-bit value per thread over a CTA of kT threads;
 // the CTA's total to *total
-template <int kT>
+template <int kT, bool kTrailingSync = true>
 __device__ __forceinline__ unsigned long long block_exclusive_scan(unsigned long long x,
                                                                    unsigned long long* total) {
     __shared__ unsigned long long warp_sums[kT / 32];
@@ -138,7 +139,7 @@ __device__ __forceinline__ unsigned long long block_exclusive_scan(unsigned long
         if (w < warp) before += warp_sums[w];
         all += warp_sums[w];
     }
-    __syncthreads();
+    if (kTrailingSync) __syncthreads();  // warp_sums may be rewritten next
     *total = all;
     return before + inc - x;
 }
@@ -195,24 +196,6 @@ __device__ __forceinline__ bool in_sign_range(float2 v) {
     const float ax = fabsf(v.x), aw = fabsf(v.y);
     return ax >= 0x1p-30f && ax <= 0x1p30f && aw >= 0x1p-30f && aw <= 0x1p30f;
 }
-__device__ __forceinline__ unsigned int vertex_axes(const Cube& c) {
-    const float2 sv = c.val[0];
-    const bool s_ok = in_sign_range(sv);
-    const bool s_neg = (sv.x < 0.0f) != (sv.y < 0.0f);
-    unsigned int axes = 0;
-    const int nb[3] = {1, 2, 4};
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        const float2 o = c.val[nb[a]];
-        if (!(o.y > 0.0f)) continue;
-        bool crosses;
-        if (s_ok && in_sign_range(o)) crosses = s_neg != ((o.x < 0.0f) != (o.y < 0.0f));
-        else crosses = fmul(vdist(sv), vdist(o)) <= 0.0f;
-        if (crosses) axes |= 1u << a;
-    }
-    return axes;
-}
-
 // Voxel::Distance(v) < 0 without the division where its sign is certain:
 // for 2^-100 <= |x| and 2^-100 <= |w| <= 2^24 the quotient x / w is a
 // normal non-zero float (|x / w| >= 2^-124), so it is negative exactly when
@@ -224,31 +207,72 @@ __device__ __forceinline__ bool dist_negative(float2 v) {
     return vdist(v) < 0.0f;
 }
 
-// marching-cubes case with the reference's corner bit order (Mesher.cpp:191-199)
-__device__ __forceinline__ int cube_case(const Cube& c) {
-    return dist_negative(c.val[0]) << 2 | dist_negative(c.val[1]) << 3 |
-           dist_negative(c.val[2]) << 6 | dist_negative(c.val[3]) << 7 |
-           dist_negative(c.val[4]) << 1 | dist_negative(c.val[5]) << 0 |
-           dist_negative(c.val[6]) << 5 | dist_negative(c.val[7]) << 4;
+// Classification reads a voxel through one status byte, computed once per
+// staged voxel: E weight != 0 (the reference's skip test, :172-181), P
+// weight > 0 (the vertex test's neighbour condition, :140-168), N
+// Distance() < 0 (the case bit, :191-199, exact through dist_negative), R
+// operands in in_sign_range, S the quotient's sign (x < 0 != w < 0).  A
+// voxel that is not found reads as status 0, as Voxel() = (0, 0) does.
+constexpr unsigned int kStE = 1, kStP = 2, kStN = 4, kStR = 8, kStS = 16;
+__device__ __forceinline__ unsigned int voxel_status(float2 v) {
+    unsigned int s = 0;
+    if (v.y != 0.0f) s |= kStE;
+    if (v.y > 0.0f) s |= kStP;
+    if (dist_negative(v)) s |= kStN;
+    if (in_sign_range(v)) s |= kStR;
+    if ((v.x < 0.0f) != (v.y < 0.0f)) s |= kStS;
+    return s;
 }
 
-// One voxel's classification from its cube (live: the voxel is in [0, n-2]
-// with a non-zero weight, and c holds its corners): its flags without the
-// tile offset -- vertex axes, triangle count, case.
+// the status of every voxel (one byte each, four per 32-bit store)
+__global__ void __launch_bounds__(kThreads) k_mesh_status(const float2* __restrict__ vals,
+                                                          const unsigned int* __restrict__ n_dev,
+                                                          unsigned int* __restrict__ status4) {
+    const unsigned int n = *n_dev;
+    const float4* v2 = reinterpret_cast<const float4*>(vals);  // two voxels per vector
+    for (unsigned int q = blockIdx.x * blockDim.x + threadIdx.x; q < (n + 3u) / 4u; q += gridDim.x * blockDim.x) {
+        const unsigned int i = 4u * q;
+        unsigned int word = 0;
+        if (i + 4u <= n) {
+            const float4 a = __ldg(v2 + 2 * q), b = __ldg(v2 + 2 * q + 1);
+            word = voxel_status(make_float2(a.x, a.y)) | voxel_status(make_float2(a.z, a.w)) << 8 |
+                   voxel_status(make_float2(b.x, b.y)) << 16 | voxel_status(make_float2(b.z, b.w)) << 24;
+        } else {
+            for (unsigned int k = 0; i + k < n; ++k) word |= voxel_status(vals[i + k]) << (8u * k);
+        }
+        status4[q] = word;
+    }
+}
+
+// One live voxel's flags without the tile offset -- vertex axes, triangle
+// count, case -- from its corners' statuses st and indices idx (corner c =
+// (c&1, c>>1&1, c>>2): self, +x, +y, +xy, +z, +xz, +yz, +xyz).  A vertex
+// test whose operands are out of in_sign_range takes the reference's
+// divisions on the voxels themselves.
 template <bool kTris>
-__device__ __forceinline__ unsigned int classify_voxel(const Cube& c, bool live, const uint64_t* s_mc) {
+__device__ __forceinline__ unsigned int classify_status(const unsigned int (&st)[8], const unsigned int (&idx)[8],
+                                                        const float2* __restrict__ vals, const uint64_t* s_mc) {
     unsigned int f = 0;
-    if (live) {
-        f = vertex_axes(c);
-        if (kTris) {
-            bool skip = false;
+    const unsigned int s0 = st[0];
+    const int nb[3] = {1, 2, 4};
 #pragma unroll
-            for (int q = 1; q < 8; ++q) skip |= (0.0f == c.val[q].y);
-            if (!skip) {
-                const int lut = cube_case(c);
-                const unsigned int tris = mc_tri_count_of(s_mc[lut]);
-                if (tris) f |= tris << 3 | (unsigned int)lut << 6;
-            }
+    for (int a = 0; a < 3; ++a) {
+        const unsigned int o = st[nb[a]];
+        if (!(o & kStP)) continue;
+        bool cross;
+        if (s0 & o & kStR) cross = ((s0 ^ o) & kStS) != 0u;
+        else cross = fmul(vdist(vals[idx[0]]), vdist(vals[idx[nb[a]]])) <= 0.0f;
+        if (cross) f |= 1u << a;
+    }
+    if (kTris) {
+        const unsigned int all = st[1] & st[2] & st[3] & st[4] & st[5] & st[6] & st[7];
+        if (all & kStE) {
+            // the reference's corner bit order (Mesher.cpp:191-199)
+            auto neg = [&](int q) { return (st[q] & kStN) ? 1u : 0u; };
+            const unsigned int lut = neg(0) << 2 | neg(1) << 3 | neg(2) << 6 | neg(3) << 7 | neg(4) << 1 |
+                                     neg(5) << 0 | neg(6) << 5 | neg(7) << 4;
+            const unsigned int tris = mc_tri_count_of(s_mc[lut]);
+            if (tris) f |= tris << 3 | lut << 6;
         }
     }
     return f;
@@ -256,182 +280,220 @@ __device__ __forceinline__ unsigned int classify_voxel(const Cube& c, bool live,
 
 // Classification by tiles of kClassTile consecutive voxels.  For a
 // neighbour offset d (+y, +z, +yz) the lookup positions walk_ptr(key_i + d)
-// are non-decreasing in i, so the tile's positions all lie between those of
-// its first and last voxel.  k_mesh_tile_ranges finds those bounds for every
-// tile at once (six row-directory searches per tile, one thread each); the
-// classification then stages the tile's keys and voxels and each offset's
-// range in shared memory with independent coalesced loads and builds every
-// cube from the staging: one search in the staged keys for a thread's first
-// voxel, a forward walk for its next.  A tile whose ranges are longer than
-// the staging holds searches per voxel (load_cube).  Results are identical.
-constexpr int kClassItems = 2;
-constexpr int kClassTile = kThreads * kClassItems;  // 512 voxels
-constexpr int kClassStage = 1024;                    // staged keys per offset
-// dynamic shared memory of k_mesh_classify_tiled: per offset a staged range
-// of keys and voxels, the tile's own keys and voxels (plus the one after)
+// are non-decreasing in i, so the positions of a run of voxels all lie
+// between those of its first and last voxel.  The +y positions start at the
+// voxel itself, so the tile and its +y lookups are one region (A) from the
+// tile's first voxel on; the +yz positions start at or after the +z ones,
+// so those two offsets share region B.  A tile that spans two z slices gets
+// region B in two ranges, one per slice, since the lookups of the two parts
+// land a whole slice apart.  k_mesh_tile_ranges finds the regions of every
+// tile at once (one thread per tile, searches through the row directory).
+// The classification stages both regions in shared memory with independent
+// coalesced loads -- keys, and the status byte k_mesh_status wrote per voxel
+// in place of its value -- and builds every cube from the staging: one
+// search in the staged keys for a thread's first voxel in a range, a
+// forward walk for its next.  A tile whose regions are longer than the
+// staging holds searches per voxel (load_cube).  Results are identical.
+constexpr int kClassItems = 4;
+constexpr int kClassTile = kThreads * kClassItems;  // 1024 voxels
+constexpr int kStageA = 2048, kStageB = 2048;        // staged keys per region
+// dynamic shared memory of k_mesh_classify_tiled: keys of regions A and B,
+// then their status bytes
 template <typename K>
-__host__ __device__ constexpr size_t class_smem(int n_offsets) {
-    return ((size_t)n_offsets * kClassStage + kClassTile + 1) * (sizeof(K) + sizeof(float2));
+__host__ __device__ constexpr size_t class_smem() {
+    return (size_t)(kStageA + kStageB) * (sizeof(K) + 1);
 }
 
-// per tile and offset d: the first staged position and the range length
-// (length 0: nothing to stage; longer than kClassStage: search per voxel)
+typedef MeshTileRange TileRange;
+
 template <typename K>
 __global__ void k_mesh_tile_ranges(const K* __restrict__ keys, int kb, const unsigned int* __restrict__ rs,
-                                   const unsigned int* __restrict__ n_dev, int n_offsets,
-                                   uint2* __restrict__ ranges, unsigned int max_tiles) {
+                                   const unsigned int* __restrict__ n_dev, int with_yz,
+                                   TileRange* __restrict__ ranges, unsigned int max_tiles) {
     const unsigned int n = *n_dev;
     const unsigned int tiles = min((n + kClassTile - 1) / kClassTile, max_tiles);
     const Codec<K> cd(kb);
-    const K delta[3] = {cd.pack(0, 1, 0), cd.pack(0, 0, 1), cd.pack(0, 1, 1)};
-    for (unsigned int q = blockIdx.x * blockDim.x + threadIdx.x; q < tiles * n_offsets;
-         q += gridDim.x * blockDim.x) {
-        const unsigned int t = q / n_offsets;
-        const int d = (int)(q - t * n_offsets);
+    const K dy = cd.pack(0, 1, 0), dz = cd.pack(0, 0, 1), dyz = cd.pack(0, 1, 1);
+    // walk position (unclamped) of key + delta
+    auto wpos = [&](K t) { return upper_bound_row<K>(keys, rs, t, n, cd, 0u) - 1u; };
+    for (unsigned int t = blockIdx.x * blockDim.x + threadIdx.x; t < tiles; t += gridDim.x * blockDim.x) {
         const unsigned int i0 = t * kClassTile;
         const unsigned int last = min(min(i0 + (unsigned int)kClassTile, n), n - 1u);  // voxels with a cube: < last
-        uint2 r = make_uint2(0u, 0u);
+        TileRange r;
+        r.b_lo[0] = r.b_lo[1] = r.b_len[0] = r.b_len[1] = 0u;
+        // region A: the tile and the one after, and every +y position plus one
+        r.a_len = min(i0 + (unsigned int)kClassTile + 1u, n) - i0;
+        r.split = last;
         if (last > i0) {
-            // walk positions (unclamped) of the first and last voxel; the range
-            // [min(p0, n-2), min(p1 + 1, n - 1)] holds every position and the one after
-            const unsigned int p0 = upper_bound_row<K>(keys, rs, keys[i0] + delta[d], n, cd, 0u) - 1u;
-            const unsigned int p1 = upper_bound_row<K>(keys, rs, keys[last - 1] + delta[d], n, cd, 0u) - 1u;
-            const unsigned int lo = min(p0, n - 2u);
-            r = make_uint2(lo, min(p1 + 1u, n - 1u) - lo + 1u);
+            r.a_len = max(r.a_len, min(wpos(keys[last - 1] + dy) + 1u, n - 1u) + 1u - i0);
+            unsigned int split = last;
+            const unsigned int z0 = cd.z(keys[i0]), zl = cd.z(keys[last - 1]);
+            if (z0 != zl) {  // a range per z slice when the tile spans exactly two
+                const K bound = cd.pack(0, 0, z0 + 1);  // first key of the next slice
+                unsigned int a = i0 + 1, b = last - 1;  // keys[i0] < bound <= keys[last - 1]
+                while (a < b) {
+                    const unsigned int mid = (a + b) >> 1;
+                    if (keys[mid] < bound) a = mid + 1;
+                    else b = mid;
+                }
+                if (cd.z(keys[a]) == zl) split = a;
+            }
+            // region B: from the first +z position (clamped) to the last +z or +yz
+            // position plus one
+            unsigned int first = i0, end = split;
+#pragma unroll
+            for (int sg = 0; sg < 2; ++sg) {
+                if (first < end) {
+                    const unsigned int lo = min(wpos(keys[first] + dz), n - 2u);
+                    unsigned int hi = wpos(keys[end - 1] + dz);
+                    if (with_yz) hi = max(hi, wpos(keys[end - 1] + dyz));
+                    r.b_lo[sg] = lo;
+                    r.b_len[sg] = min(hi + 1u, n - 1u) - lo + 1u;
+                }
+                first = split;
+                end = last;
+            }
+            r.split = split;
         }
-        ranges[(size_t)t * 3 + d] = r;
+        ranges[t] = r;
     }
 }
 
 template <bool kTris, typename K>
-__global__ void __launch_bounds__(kThreads) k_mesh_classify_tiled(const K* __restrict__ keys, int kb,
-                                                                  const float2* __restrict__ vals,
-                                                                  const unsigned int* __restrict__ rs,
-                                                                  const unsigned int* __restrict__ n_dev,
-                                                                  const uint2* __restrict__ ranges,
-                                                                  unsigned int max_tiles,
-                                                                  unsigned int* __restrict__ flags,
-                                                                  unsigned long long* __restrict__ tile_sums,
-                                                                  unsigned int* __restrict__ tile_nflag,
-                                                                  unsigned int* __restrict__ flagged,
-                                                                  uint4* __restrict__ corners) {
+__global__ void __launch_bounds__(kThreads, 4) k_mesh_classify_tiled(const K* __restrict__ keys, int kb,
+                                                                     const float2* __restrict__ vals,
+                                                                     const unsigned char* __restrict__ status,
+                                                                     const unsigned int* __restrict__ rs,
+                                                                     const unsigned int* __restrict__ n_dev,
+                                                                     const TileRange* __restrict__ ranges,
+                                                                     unsigned int max_tiles,
+                                                                     unsigned int* __restrict__ flags,
+                                                                     unsigned long long* __restrict__ tile_sums,
+                                                                     unsigned int* __restrict__ tile_nflag,
+                                                                     unsigned int* __restrict__ flagged,
+                                                                     uint4* __restrict__ corners) {
     constexpr int kD = kTris ? 3 : 2;  // offsets looked up: +y, +z (and +yz)
-    constexpr int kStage = kClassStage;
     extern __shared__ __align__(16) unsigned char class_mem[];
-    float2* s_val = (float2*)class_mem;                           // [kD][kStage]
-    float2* s_tval = s_val + kD * kStage;                          // [kClassTile + 1]
-    K* s_key = (K*)(s_tval + kClassTile + 1);                     // [kD][kStage]
-    K* s_tkey = s_key + kD * kStage;                              // [kClassTile + 1]
+    K* s_ka = (K*)class_mem;                                     // [kStageA]: region A keys
+    K* s_kb = s_ka + kStageA;                                    // [kStageB]: region B keys
+    unsigned char* s_sa = (unsigned char*)(s_kb + kStageB);      // [kStageA]: statuses
+    unsigned char* s_sb = s_sa + kStageA;                        // [kStageB]
     __shared__ uint64_t s_mc[256];
     if (kTris) mc_table_to_shared(s_mc);
     const unsigned int n = *n_dev;
     const Codec<K> cd(kb);
     const K delta[3] = {cd.pack(0, 1, 0), cd.pack(0, 0, 1), cd.pack(0, 1, 1)};
-    const float2 zero = make_float2(0.0f, 0.0f);
     const unsigned int tiles = min((n + kClassTile - 1) / kClassTile, max_tiles);
     for (unsigned int t = blockIdx.x; t < tiles; t += gridDim.x) {
         const unsigned int i0 = t * kClassTile;
         const unsigned int i1 = min(i0 + (unsigned int)kClassTile, n);
-        unsigned int lo[kD], len[kD];
-        bool fits = true;
-#pragma unroll
-        for (int d = 0; d < kD; ++d) {
-            const uint2 r = ranges[(size_t)t * 3 + d];
-            lo[d] = r.x;
-            len[d] = r.y;
-            fits &= r.y <= (unsigned int)kStage;
-        }
+        const TileRange r = ranges[t];
+        const bool fits = r.a_len <= (unsigned int)kStageA && r.b_len[0] + r.b_len[1] <= (unsigned int)kStageB;
         __syncthreads();  // the previous tile is done with the staging
         if (fits) {
-            // independent loads: the tile's own keys and voxels (and the one
-            // after), then each offset's range
-            for (unsigned int j = threadIdx.x; j <= (unsigned int)kClassTile; j += kThreads)
-                if (i0 + j < n) {
-                    s_tkey[j] = keys[i0 + j];
-                    s_tval[j] = vals[i0 + j];
-                }
-#pragma unroll
-            for (int d = 0; d < kD; ++d)
-                for (unsigned int j = threadIdx.x; j < len[d]; j += kThreads) {
-                    s_key[d * kStage + j] = keys[lo[d] + j];
-                    s_val[d * kStage + j] = vals[lo[d] + j];
-                }
+            // independent loads: region A, then region B's ranges back to back
+            for (unsigned int j = threadIdx.x; j < r.a_len; j += kThreads) {
+                s_ka[j] = keys[i0 + j];
+                s_sa[j] = status[i0 + j];
+            }
+            const unsigned int nb = r.b_len[0] + r.b_len[1];
+            for (unsigned int j = threadIdx.x; j < nb; j += kThreads) {
+                const unsigned int g = j < r.b_len[0] ? r.b_lo[0] + j : r.b_lo[1] + (j - r.b_len[0]);
+                s_kb[j] = keys[g];
+                s_sb[j] = status[g];
+            }
         }
         __syncthreads();
         const unsigned int tb = threadIdx.x * kClassItems;  // this thread's first voxel in the tile
-        unsigned int pos[kD];  // running count of staged keys <= key + d
+        unsigned int pos[kD], seg[kD];  // running count of a range's staged keys <= key + d; its range
 #pragma unroll
-        for (int d = 0; d < kD; ++d) pos[d] = 0xffffffffu;
+        for (int d = 0; d < kD; ++d) {
+            pos[d] = 0u;
+            seg[d] = 2u;  // none yet: search
+        }
         unsigned int fl[kClassItems];
         uint3 look[kClassItems];  // the +y, +z, +yz lookups, kept for emission
 #pragma unroll
-        for (int j = 0; j < kClassItems; ++j) fl[j] = 0u;
+        for (int j = 0; j < kClassItems; ++j) {
+            fl[j] = 0u;
+            look[j] = make_uint3(0u, 0u, 0u);
+        }
 #pragma unroll
         for (int j = 0; j < kClassItems; ++j) {
             const unsigned int i = i0 + tb + j;
             if (i >= i1) break;
-            Cube c;
+            unsigned int st[8], idx[8];
             bool live;
             if (!fits) {
                 live = i + 1 < n && vals[i].y != 0.0f;
-                if (live) load_cube<kTris, K>(keys, vals, rs, n, i, c, cd);
-            } else {
-                const float2 v0 = s_tval[tb + j];
-                live = i + 1 < n && v0.y != 0.0f;
                 if (live) {
-                    const K key = s_tkey[tb + j];
-                    c.idx[0] = i;
-                    c.val[0] = v0;
-                    c.idx[1] = i + 1;
-                    c.val[1] = s_tkey[tb + j + 1] == key + cd.pack(1, 0, 0) ? s_tval[tb + j + 1] : zero;
-                    unsigned int w[kD];
+                    Cube c;
+                    load_cube<kTris, K>(keys, vals, rs, n, i, c, cd);
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        idx[q] = c.idx[q];
+                        st[q] = (kTris || q == 0 || q == 1 || q == 2 || q == 4) ? voxel_status(c.val[q]) : 0u;
+                    }
+                }
+            } else {
+                const unsigned int s0 = s_sa[tb + j];
+                live = i + 1 < n && (s0 & kStE);
+                if (live) {
+                    const K key = s_ka[tb + j];
+                    idx[0] = i;
+                    st[0] = s0;
+                    idx[1] = i + 1;
+                    st[1] = s_ka[tb + j + 1] == key + cd.pack(1, 0, 0) ? s_sa[tb + j + 1] : 0u;
+                    unsigned int w[kD];  // staged index of each lookup's position in its region
 #pragma unroll
                     for (int d = 0; d < kD; ++d) {
+                        // region A for +y (one range, from i0); region B for +z, +yz
+                        const unsigned int sg = d == 0 ? 0u : (i >= r.split ? 1u : 0u);
+                        const unsigned int base = sg ? r.b_len[0] : 0u;
+                        const unsigned int L = d == 0 ? r.a_len : (sg ? r.b_len[1] : r.b_len[0]);
+                        const unsigned int lod = d == 0 ? i0 : (sg ? r.b_lo[1] : r.b_lo[0]);
+                        const K* sk = (d == 0 ? s_ka : s_kb) + base;
                         const K tk = key + delta[d];
-                        const K* sk = s_key + d * kStage;
                         unsigned int p = pos[d];
-                        if (p == 0xffffffffu) {  // the thread's first live voxel: search
-                            unsigned int a = 0, b = len[d];
+                        if (seg[d] != sg) {  // the thread's first live voxel in this range: search
+                            unsigned int a = 0, b = L;
                             while (a < b) {
                                 const unsigned int mid = (a + b) >> 1;
                                 if (sk[mid] <= tk) a = mid + 1;
                                 else b = mid;
                             }
                             p = a;
+                            seg[d] = sg;
                         } else {  // later voxels: the positions only move forward
-                            while (p < len[d] && sk[p] <= tk) ++p;
+                            while (p < L && sk[p] <= tk) ++p;
                         }
                         pos[d] = p;
-                        // walk_ptr = min(n - 2, upper_bound - 1), upper_bound = lo + p;
-                        // w[d] is the staged index of that position
-                        w[d] = min(lo[d] + p - 1u, n - 2u) - lo[d];
+                        // walk_ptr = min(n - 2, upper_bound - 1), upper_bound = lo + p
+                        const unsigned int gp = min(lod + p - 1u, n - 2u);
+                        idx[d == 0 ? 2 : (d == 1 ? 4 : 6)] = gp;
+                        w[d] = base + (gp - lod);
                     }
-                    // corners: self, +x, +y, +xy, +z, +xz, +yz, +xyz (Mesher.cpp:122-132, 174-181)
-                    const K* ky = s_key;
-                    const K* kz = s_key + kStage;
-                    const float2* vy = s_val;
-                    const float2* vz = s_val + kStage;
-                    c.idx[2] = lo[0] + w[0];
-                    c.val[2] = ky[w[0]] == key + delta[0] ? vy[w[0]] : zero;
-                    c.idx[4] = lo[1] + w[1];
-                    c.val[4] = kz[w[1]] == key + delta[1] ? vz[w[1]] : zero;
+                    // corners: +y, +z (+yz) at the lookups, +xy, +xz (+xyz) one past
+                    st[2] = s_ka[w[0]] == key + delta[0] ? s_sa[w[0]] : 0u;
+                    st[4] = s_kb[w[1]] == key + delta[1] ? s_sb[w[1]] : 0u;
+                    idx[3] = idx[2] + 1;
+                    idx[5] = idx[4] + 1;
                     if (kTris) {
-                        const K* kyz = s_key + (kD - 1) * kStage;
-                        const float2* vyz = s_val + (kD - 1) * kStage;
-                        const unsigned int wy = w[kD - 1];
-                        c.idx[6] = lo[kD - 1] + wy;
-                        c.val[6] = kyz[wy] == key + delta[2] ? vyz[wy] : zero;
-                        c.idx[3] = c.idx[2] + 1;
-                        c.val[3] = ky[w[0] + 1] == key + cd.pack(1, 1, 0) ? vy[w[0] + 1] : zero;
-                        c.idx[5] = c.idx[4] + 1;
-                        c.val[5] = kz[w[1] + 1] == key + cd.pack(1, 0, 1) ? vz[w[1] + 1] : zero;
-                        c.idx[7] = c.idx[6] + 1;
-                        c.val[7] = kyz[wy + 1] == key + cd.pack(1, 1, 1) ? vyz[wy + 1] : zero;
+                        st[6] = s_kb[w[2]] == key + delta[2] ? s_sb[w[2]] : 0u;
+                        idx[7] = idx[6] + 1;
+                        st[3] = s_ka[w[0] + 1] == key + cd.pack(1, 1, 0) ? s_sa[w[0] + 1] : 0u;
+                        st[5] = s_kb[w[1] + 1] == key + cd.pack(1, 0, 1) ? s_sb[w[1] + 1] : 0u;
+                        st[7] = s_kb[w[2] + 1] == key + cd.pack(1, 1, 1) ? s_sb[w[2] + 1] : 0u;
+                    } else {
+                        idx[6] = idx[7] = 0u;
+                        st[3] = st[5] = st[6] = st[7] = 0u;
                     }
                 }
             }
-            fl[j] = classify_voxel<kTris>(c, live, s_mc);
-            look[j] = make_uint3(c.idx[2], c.idx[4], kTris ? c.idx[6] : 0u);
+            if (live) {
+                fl[j] = classify_status<kTris>(st, idx, vals, s_mc);
+                look[j] = make_uint3(idx[2], idx[4], kTris ? idx[6] : 0u);
+            }
         }
         // in-tile offsets of the vertices (into the flags), of the indices
         // (beside the lookups) and of the voxels with output (their list),
@@ -444,7 +506,8 @@ __global__ void __launch_bounds__(kThreads) k_mesh_classify_tiled(const K* __res
             nf += fl[j] ? 1u : 0u;
         }
         unsigned long long total;
-        const unsigned long long ex = block_exclusive_scan<kThreads>(
+        // (no trailing barrier: the next tile's first barrier orders the reuse)
+        const unsigned long long ex = block_exclusive_scan<kThreads, false>(
             (unsigned long long)nf << 48 | (unsigned long long)ni << 24 | nv, &total);
         unsigned int vo = (unsigned int)(ex & 0xffffffu), io = (unsigned int)((ex >> 24) & 0xffffffu);
         unsigned int fo = (unsigned int)(ex >> 48);
@@ -492,8 +555,8 @@ constexpr unsigned int kEdgeAxes = 0x558888u;
 __device__ __forceinline__ int edge_corner(int e) { return (int)((kEdgeCorners >> (4 * e)) & 15u); }
 __device__ __forceinline__ int edge_axis(int e) { return (int)((kEdgeAxes >> (2 * e)) & 3u); }
 
-// Emission: each warp takes the voxels with output of one classification
-// tile (their list, ascending), 32 at a time.  A voxel's first vertex is its
+// Emission over the voxels with output in ascending order (the tiles'
+// lists end to end), 32 per warp step.  A voxel's first vertex is its
 // tile's vertex offset plus the in-tile offset in its flags, its first index
 // slot its tile's index offset plus the in-tile offset kept beside its
 // lookups.
@@ -540,20 +603,43 @@ __global__ void __launch_bounds__(kThreads) k_mesh_emit(const K* __restrict__ ke
     // search over the prefix of the voxels' index counts), so a warp does
     // not wait on its lane with the most triangles.
     constexpr int kWarps = kThreads / 32;
-    __shared__ unsigned int s_cidx[kWarps][8][32];
+    __shared__ unsigned int s_cidx[kWarps][8][32];  // corner voxel
+    __shared__ unsigned int s_cvb[kWarps][8][32];   // corner voxel's first vertex
+    __shared__ unsigned char s_cax[kWarps][8][32];  // corner voxel's vertex axes
     __shared__ uint64_t s_mcw[kWarps][32];
     __shared__ unsigned int s_first[kWarps][32];
     __shared__ unsigned int s_excl[kWarps][33];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned int warps = gridDim.x * kWarps;
     const unsigned int tiles = (n + kClassTile - 1) / kClassTile;
-    // each warp takes a tile's voxels with output, 32 at a time
-    for (unsigned int tile = blockIdx.x * kWarps + warp; tile < tiles; tile += warps)
-    for (unsigned int c0 = 0, cnt = tile_nflag[tile]; c0 < cnt; c0 += 32u) {
-        const unsigned long long tofs = tile_ofs[tile];
-        const unsigned int k = c0 + lane;
-        const unsigned int i = k < cnt ? flagged[tile * kClassTile + k] : 0u;
-        const unsigned int f = k < cnt ? flags[i] : 0u;
+    // The voxels with output, counted across tiles (tile_nflag holds each tile's
+    // first position), are cut into chunks of 32; each warp takes a contiguous
+    // run of chunks and finds the tile of each position by walking forward.
+    const unsigned int n_out = (unsigned int)mc->n_flagged;
+    const unsigned int chunks = (n_out + 31u) / 32u;
+    const unsigned int wid = blockIdx.x * kWarps + warp;
+    const unsigned int cbeg = (unsigned int)((unsigned long long)chunks * wid / warps);
+    const unsigned int cend = (unsigned int)((unsigned long long)chunks * (wid + 1) / warps);
+    unsigned int tile = 0;
+    if (cbeg < cend) {  // the warp's first tile: the last with a first position <= 32 cbeg
+        unsigned int a = 0, b = tiles;
+        while (a + 1 < b) {
+            const unsigned int mid = (a + b) >> 1;
+            if (tile_nflag[mid] <= 32u * cbeg) a = mid;
+            else b = mid;
+        }
+        tile = a;
+    }
+    for (unsigned int ch = cbeg; ch < cend; ++ch) {
+        const unsigned int gpos = 32u * ch + lane;
+        const bool valid = gpos < n_out;
+        unsigned int tl = tile;
+        if (valid)
+            while (tile_nflag[tl + 1] <= gpos) ++tl;  // tile_nflag[tiles] = n_out > gpos
+        tile = __shfl_sync(0xffffffffu, tl, 31);      // positions only move forward
+        const unsigned int i = valid ? flagged[tl * kClassTile + (gpos - tile_nflag[tl])] : 0u;
+        const unsigned int f = valid ? flags[i] : 0u;
+        const unsigned long long tofs = valid ? tile_ofs[tl] : 0ull;
         unsigned int cidx[8];
         uint4 cr = make_uint4(0u, 0u, 0u, 0u);
         if (f) {
@@ -605,8 +691,20 @@ __global__ void __launch_bounds__(kThreads) k_mesh_emit(const K* __restrict__ ke
                 s_mcw[warp][lane] = s_mc[f_case(f)];  // the case's triangle edges
                 // generation order: voxels descending
                 s_first[warp][lane] = (unsigned int)(n_idx - ((tofs >> 32) + cr.w) - ni);
+                // each corner voxel's vertex axes and first vertex: independent loads
+                unsigned int cf[8];
+                unsigned long long co[8];
 #pragma unroll
-                for (int k = 0; k < 8; ++k) s_cidx[warp][k][lane] = cidx[k];
+                for (int k = 0; k < 8; ++k) {
+                    cf[k] = flags[cidx[k]];
+                    co[k] = tile_ofs[cidx[k] / kClassTile];
+                }
+#pragma unroll
+                for (int k = 0; k < 8; ++k) {
+                    s_cidx[warp][k][lane] = cidx[k];
+                    s_cax[warp][k][lane] = (unsigned char)f_axes(cf[k]);
+                    s_cvb[warp][k][lane] = (unsigned int)(co[k] & 0xffffffffu) + f_vofs(cf[k]);
+                }
             }
             __syncwarp();
             unsigned long long local_min = ~0ull;
@@ -619,20 +717,19 @@ __global__ void __launch_bounds__(kThreads) k_mesh_emit(const K* __restrict__ ke
                 const unsigned int t = j - s_excl[warp][v];
                 const int e = mc_tri_edge_of(s_mcw[warp][v], (int)t);
                 const int corner = edge_corner(e), axis = edge_axis(e);
-                const unsigned int ci = s_cidx[warp][corner][v];
-                const unsigned int cf = flags[ci];
-                const bool has = (cf >> axis & 1u) != 0u;
+                const unsigned int cax = s_cax[warp][corner][v];
+                const bool has = (cax >> axis & 1u) != 0u;
                 // the edge id 3 * key + axis, needed for a missing vertex and on the
                 // stop rule's re-run: 32 bits wide for 30-bit keys (as in the reference);
                 // for 64-bit keys the stop rule compares full ids and an id written in
                 // place of a missing vertex keeps its low 32 bits
                 const bool need_id = !has || missing_bound != ~0ull;
                 const unsigned long long id =
-                    need_id ? 3ull * (unsigned long long)keys[ci] + (unsigned long long)axis : 0ull;
+                    need_id ? 3ull * (unsigned long long)keys[s_cidx[warp][corner][v]] + (unsigned long long)axis
+                            : 0ull;
                 uint32_t outv;
                 if (has) {
-                    outv = (unsigned int)(tile_ofs[ci / kClassTile] & 0xffffffffu) + f_vofs(cf) +
-                           __popc(f_axes(cf) & ((1u << axis) - 1u));
+                    outv = s_cvb[warp][corner][v] + __popc(cax & ((1u << axis) - 1u));
                 } else {
                     outv = (uint32_t)id;
                     local_min = min(local_min, id);
@@ -645,37 +742,51 @@ __global__ void __launch_bounds__(kThreads) k_mesh_emit(const K* __restrict__ ke
     }
 }
 
-// single CTA: exclusive scan (in place) of the classification tiles' packed
-// (index count << 32 | vertex count), the totals to *counts; both halves stay
-// below 2^32 for volumes under 2^28 voxels
+// single CTA: exclusive scans (in place) of the classification tiles' packed
+// (index count << 32 | vertex count) and of their counts of voxels with
+// output (the total after the last), the totals to *counts; the packed
+// halves stay below 2^32 for volumes under 2^28 voxels
 constexpr int kSumThreads = 1024, kSumItems = 8;
 __global__ void __launch_bounds__(kSumThreads) k_scan_tile_sums(unsigned long long* __restrict__ sums,
+                                                                unsigned int* __restrict__ nflag,
                                                                 const unsigned int* __restrict__ n_dev,
                                                                 MeshCounts* __restrict__ counts) {
     const unsigned int n_tiles = (*n_dev + kClassTile - 1) / kClassTile;
-    unsigned long long carry = 0;
+    unsigned long long carry = 0, fcarry = 0;
     for (unsigned int b = 0; b < n_tiles; b += kSumThreads * kSumItems) {
         const unsigned int i0 = b + threadIdx.x * kSumItems;
-        unsigned long long v[kSumItems], s = 0;
+        unsigned long long v[kSumItems], s = 0, fs = 0;
+        unsigned int fv[kSumItems];
 #pragma unroll
         for (int q = 0; q < kSumItems; ++q) {
-            v[q] = i0 + q < n_tiles ? sums[i0 + q] : 0ull;
+            const bool in = i0 + q < n_tiles;
+            v[q] = in ? sums[i0 + q] : 0ull;
+            fv[q] = in ? nflag[i0 + q] : 0u;
             s += v[q];
+            fs += fv[q];
         }
-        unsigned long long total;
+        unsigned long long total, ftotal;
         unsigned long long run = carry + block_exclusive_scan<kSumThreads>(s, &total);
+        unsigned long long frun = fcarry + block_exclusive_scan<kSumThreads>(fs, &ftotal);
 #pragma unroll
         for (int q = 0; q < kSumItems; ++q) {
-            if (i0 + q < n_tiles) sums[i0 + q] = run;
+            if (i0 + q < n_tiles) {
+                sums[i0 + q] = run;
+                nflag[i0 + q] = (unsigned int)frun;
+            }
             run += v[q];
+            frun += fv[q];
         }
         carry += total;
+        fcarry += ftotal;
     }
     if (threadIdx.x == 0) {
+        nflag[n_tiles] = (unsigned int)fcarry;
         counts->n_verts = carry & 0xffffffffull;
         counts->n_idx = carry >> 32;
         counts->missing_min = ~0ull;
         counts->overflow = 0ull;
+        counts->n_flagged = fcarry;
     }
 }
 
@@ -690,12 +801,13 @@ cudaError_t mesh_scratch_reserve(MeshScratch* m, size_t n, int kb) {
     const size_t tiles = (cap + kClassTile - 1) / kClassTile + 1;
     cudaError_t e;
     if ((e = cudaMalloc(&m->vflags, cap * sizeof(unsigned int)))) return e;
+    if ((e = cudaMalloc(&m->vstatus, (cap + 4) / 4 * 4))) return e;
     if ((e = cudaMalloc(&m->corners, cap * sizeof(uint4)))) return e;
     if ((e = cudaMalloc(&m->tile_sums, tiles * sizeof(unsigned long long)))) return e;
     if ((e = cudaMalloc(&m->tile_nflag, tiles * sizeof(unsigned int)))) return e;
     if ((e = cudaMalloc(&m->flagged, tiles * kClassTile * sizeof(unsigned int)))) return e;
     if ((e = cudaMalloc(&m->rows, rows * sizeof(unsigned int)))) return e;
-    if ((e = cudaMalloc(&m->tile_ranges, tiles * 3 * sizeof(uint2)))) return e;
+    if ((e = cudaMalloc(&m->tile_ranges, tiles * sizeof(MeshTileRange)))) return e;
     m->rows_cap = rows;
     if ((e = cudaMalloc(&m->counts, sizeof(MeshCounts)))) return e;
     if ((e = cudaMalloc(&m->n_dev, sizeof(unsigned int)))) return e;
@@ -705,6 +817,7 @@ cudaError_t mesh_scratch_reserve(MeshScratch* m, size_t n, int kb) {
 
 void mesh_scratch_free(MeshScratch* m) {
     cudaFree(m->vflags);
+    cudaFree(m->vstatus);
     cudaFree(m->corners);
     cudaFree(m->tile_sums);
     cudaFree(m->tile_nflag);
@@ -731,27 +844,27 @@ static void mesh_count_t(const K* keys, const float2* vals, size_t n_cap, int kb
     if (stage_events) cudaEventRecord(stage_events[0], st);
     // tile ranges, then the classification (its grid: up to 8 CTAs per SM, each walking tiles)
     const unsigned int max_tiles = (unsigned int)((n_cap + kClassTile - 1) / kClassTile);
-    const int offsets = with_indices ? 3 : 2;
-    k_mesh_tile_ranges<K><<<grid_for((size_t)max_tiles * offsets, sms), kThreads, 0, st>>>(
-        keys, kb, ms.rows, ms.n_dev, offsets, ms.tile_ranges, max_tiles);
+    k_mesh_tile_ranges<K><<<grid_for((size_t)max_tiles, sms), kThreads, 0, st>>>(
+        keys, kb, ms.rows, ms.n_dev, with_indices, ms.tile_ranges, max_tiles);
     const int class_grid = (int)(max_tiles < (unsigned int)(sms * 8) ? (max_tiles ? max_tiles : 1) : sms * 8);
+    k_mesh_status<<<grid_for((n_cap + 3) / 4, sms), kThreads, 0, st>>>(vals, ms.n_dev, (unsigned int*)ms.vstatus);
     if (with_indices) {
-        const size_t smem = class_smem<K>(3);
+        const size_t smem = class_smem<K>();
         cudaFuncSetAttribute(k_mesh_classify_tiled<true, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_mesh_classify_tiled<true, K><<<class_grid, kThreads, smem, st>>>(keys, kb, vals, ms.rows, ms.n_dev,
+        k_mesh_classify_tiled<true, K><<<class_grid, kThreads, smem, st>>>(keys, kb, vals, ms.vstatus, ms.rows, ms.n_dev,
                                                                           ms.tile_ranges, max_tiles, ms.vflags,
                                                                           ms.tile_sums, ms.tile_nflag, ms.flagged,
                                                                           ms.corners);
     } else {
-        const size_t smem = class_smem<K>(2);
+        const size_t smem = class_smem<K>();
         cudaFuncSetAttribute(k_mesh_classify_tiled<false, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_mesh_classify_tiled<false, K><<<class_grid, kThreads, smem, st>>>(keys, kb, vals, ms.rows, ms.n_dev,
+        k_mesh_classify_tiled<false, K><<<class_grid, kThreads, smem, st>>>(keys, kb, vals, ms.vstatus, ms.rows, ms.n_dev,
                                                                            ms.tile_ranges, max_tiles, ms.vflags,
                                                                            ms.tile_sums, ms.tile_nflag, ms.flagged,
                                                                            ms.corners);
     }
     if (stage_events) cudaEventRecord(stage_events[1], st);
-    k_scan_tile_sums<<<1, kSumThreads, 0, st>>>(ms.tile_sums, ms.n_dev, ms.counts);
+    k_scan_tile_sums<<<1, kSumThreads, 0, st>>>(ms.tile_sums, ms.tile_nflag, ms.n_dev, ms.counts);
 }
 
 cudaError_t mesh_count_enqueue(const void* keys, int key_bytes, const float2* vals, size_t n_cap, int kb,
