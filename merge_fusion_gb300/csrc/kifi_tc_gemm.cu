@@ -395,33 +395,65 @@ bool matrix_map(CUtensorMap* map, const void* ptr, int rows, int K, int ld, int 
     return encode(map, ptr, 2, dims, strides, box, estr, CU_TENSOR_MAP_SWIZZLE_128B);
 }
 
+// per device: shared memory per SM and per block, reserved per block, SMs
+struct DeviceLimits {
+    int per_sm = 0, per_block = 0, reserved = 0, sms = 0;
+};
+
+cudaError_t device_limits(DeviceLimits* out) {
+    constexpr int kMaxDevices = 64;
+    static DeviceLimits cache[kMaxDevices];
+    static std::once_flag once[kMaxDevices];
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    static cudaError_t err[kMaxDevices];
+    std::call_once(once[dev], [&] {
+        DeviceLimits& L = cache[dev];
+        cudaError_t x = cudaDeviceGetAttribute(&L.per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+        if (!x) x = cudaDeviceGetAttribute(&L.per_block, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        if (!x) x = cudaDeviceGetAttribute(&L.reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+        if (!x) x = cudaDeviceGetAttribute(&L.sms, cudaDevAttrMultiProcessorCount, dev);
+        err[dev] = x;
+    });
+    *out = cache[dev];
+    return err[dev];
+}
+
 template <int BN>
 cudaError_t launch(const CUtensorMap& a, const CUtensorMap& b, Tiles T, int tiles, const Epilogue& ep,
                    unsigned int* status, cudaStream_t st) {
     constexpr uint32_t kBTile = BN * kBK * 2;
-    int dev = 0, per_sm = 0, per_block = 0, reserved = 0, sms = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (!e) e = cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
-    if (!e) e = cudaDeviceGetAttribute(&per_block, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    if (!e) e = cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
-    if (!e) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaFuncAttributes fa;
-    if (!e) e = cudaFuncGetAttributes(&fa, k_gemm_bf16_tma<BN>);
+    // the kernel's static shared memory (its barriers), the same on every device
+    static size_t static_smem = 0;
+    static std::once_flag once;
+    static cudaError_t fa_err = cudaSuccess;
+    std::call_once(once, [] {
+        cudaFuncAttributes fa;
+        fa_err = cudaFuncGetAttributes(&fa, k_gemm_bf16_tma<BN>);
+        if (!fa_err) static_smem = fa.sharedSizeBytes;
+    });
+    if (fa_err) return fa_err;
+    DeviceLimits L;
+    cudaError_t e = device_limits(&L);
     if (e) return e;
-    // B stays resident when the launch has one N tile, K is not split and B fits
+    // per-CTA shared memory budget at `occ` CTAs per SM (1024 bytes for the alignment of the ring)
+    auto budget = [&](int occ) -> long long {
+        const long long x = std::min<long long>((long long)L.per_sm / occ - L.reserved, L.per_block);
+        return x - (long long)static_smem - 1024;
+    };
+    // B stays resident when the launch has one N tile, K is not split and B
+    // fits beside four stages of A with two CTAs per SM; otherwise B is staged
+    // with A.  Two CTAs per SM where four stages fit, else one with a deeper ring.
     const int chunks = (T.k_split + kBK - 1) / kBK;
-    T.b_res = (T.nt == 1 && T.zs == 1 && (size_t)chunks * kBTile <= 72 * 1024) ? 1 : 0;
+    T.b_res = (T.nt == 1 && T.zs == 1 && (long long)chunks * kBTile + 4ll * kATile <= budget(2)) ? 1 : 0;
     T.nk_b = T.b_res ? chunks : 0;
     const size_t fixed = (size_t)T.nk_b * kBTile;
     const size_t stage = kATile + (T.b_res ? 0 : kBTile);
-    // per-CTA shared memory budget at `occ` CTAs per SM (1024 bytes for the alignment of the ring)
-    auto budget = [&](int occ) -> long long {
-        const long long b = std::min<long long>((long long)per_sm / occ - reserved, per_block);
-        return b - (long long)fa.sharedSizeBytes - 1024;
-    };
-    int occ = 2;  // two CTAs per SM where four stages fit, else one with a deeper ring
+    int occ = 2;
     if ((long long)(fixed + 4 * stage) > budget(2)) occ = 1;
-    long long fit = (budget(occ) - (long long)fixed) / (long long)stage;
+    const long long fit = (budget(occ) - (long long)fixed) / (long long)stage;
     if (fit < 2) return cudaErrorInvalidValue;
     T.stages = (int)std::min<long long>(kMaxStages, fit);
     const size_t smem = fixed + (size_t)T.stages * stage + 1024;
@@ -431,7 +463,7 @@ cudaError_t launch(const CUtensorMap& a, const CUtensorMap& b, Tiles T, int tile
         e = cudaFuncSetAttribute(k_gemm_bf16_tma<BN>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                  (int)cudaSharedmemCarveoutMaxShared);
     if (e) return e;
-    const int grid = std::min(tiles, std::max(sms, 1) * occ);
+    const int grid = std::min(tiles, std::max(L.sms, 1) * occ);
     k_gemm_bf16_tma<BN><<<grid, kGemmThreads, smem, st>>>(a, b, T, ep, status);
     return cudaGetLastError();
 }
