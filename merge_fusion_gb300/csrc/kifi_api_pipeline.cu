@@ -19,8 +19,10 @@
 //
 // Fusion runs on the volume's stream and tracking on the ICP context's
 // stream, so the HBM-bound merge/update and the shared-memory-bound ICP
-// window search overlap on the GPU.  Events order the shared inputs: a frame
-// slot is only overwritten after the tracking stream has finished reading it.
+// window search overlap on the GPU.  Host frames are uploaded on a third
+// stream into two device slots; events order the shared inputs: both
+// streams wait for a frame's upload, and a slot is only overwritten after
+// tracking and fusion have finished reading it.
 //
 // With graphs on (kifi_pipeline_set_graphs), a frame -- the upload of a host
 // frame, the fusion launches and the tracking launches on both streams -- is
@@ -61,10 +63,12 @@ struct kifi_pipeline {
     kifi_volume* vol = nullptr;
     kifi_icp* icp = nullptr;
     cudaStream_t vs = nullptr, is = nullptr;
+    cudaStream_t us = nullptr;  // uploads of host-fed frames
     void* slot[2] = {nullptr, nullptr};  // host-fed frames (uint16 or float)
     size_t slot_bytes = 0;
     cudaEvent_t uploaded[2] = {nullptr, nullptr};   // frame in slot k is on the device
     cudaEvent_t released[2] = {nullptr, nullptr};   // tracking no longer reads slot k
+    cudaEvent_t slot_fused[2] = {nullptr, nullptr}; // fusion no longer reads slot k
     cudaEvent_t fused = nullptr;
     long long frame = 0;
     float prev_e2w[16];
@@ -256,7 +260,9 @@ kifi_status closed_loop_frame(kifi_pipeline* p, const void* depth_dev, bool u16,
     }
     // tmp = m_eyeToWorld; invert_transform(tmp); Integrate(volume, frame, cam, tmp) (:40-44)
     const Mat4 w2e = invert_transform(e2w);
+    if (k >= 0) KIFI_CUDA(cudaStreamWaitEvent(p->vs, p->uploaded[k], 0));
     if ((s = kifi_integrate_device(p->vol, depth_dev, u16 ? 1 : 0, &cam, w2e.m))) return s;
+    if (k >= 0) KIFI_CUDA(cudaEventRecord(p->slot_fused[k], p->vs));
     if (p->desc.icp_iterations > 0) {
         // m_mesher.Mesh(m_volume, m_tmpSynthPointCloud) (:46): vertices only
         size_t nv = 0, ni = 0;
@@ -293,8 +299,10 @@ kifi_status track_and_fuse(kifi_pipeline* p, const void* depth_dev, bool u16, in
             return s;
         if (k >= 0) KIFI_CUDA(cudaEventRecord(p->released[k], p->is));
     }
-    // fusion on the volume's stream
+    // fusion on the volume's stream, once the frame is on the device
+    if (k >= 0) KIFI_CUDA(cudaStreamWaitEvent(p->vs, p->uploaded[k], 0));
     if ((s = kifi_integrate_device(p->vol, depth_dev, u16 ? 1 : 0, &cam, world_to_eye))) return s;
+    if (k >= 0) KIFI_CUDA(cudaEventRecord(p->slot_fused[k], p->vs));
     std::memcpy(p->prev_e2w, e2w.m, 64);
     p->have_prev = true;
     ++p->frame;
@@ -424,6 +432,12 @@ kifi_status kifi_pipeline_create(const kifi_pipeline_desc* d, kifi_pipeline** ou
         e = cudaEventCreateWithFlags(&p->uploaded[k], cudaEventDisableTiming);
         if (!e) e = cudaEventCreateWithFlags(&p->released[k], cudaEventDisableTiming);
         if (!e) e = cudaEventRecord(p->released[k], p->is);
+        if (!e) e = cudaEventCreateWithFlags(&p->slot_fused[k], cudaEventDisableTiming);
+    }
+    if (!e) {  // uploads run at the tracking stream's priority: they start each frame's critical path
+        int lowest = 0, greatest = 0;
+        e = cudaDeviceGetStreamPriorityRange(&lowest, &greatest);
+        if (!e) e = cudaStreamCreateWithPriority(&p->us, cudaStreamNonBlocking, greatest);
     }
     if (!e) e = cudaEventCreateWithFlags(&p->fused, cudaEventDisableTiming);
     if (!e) e = cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming);
@@ -448,11 +462,14 @@ kifi_status kifi_pipeline_destroy(kifi_pipeline* p) {
     if (!p) return KIFI_OK;
     if (p->vs) cudaStreamSynchronize(p->vs);
     if (p->is) cudaStreamSynchronize(p->is);
+    if (p->us) cudaStreamSynchronize(p->us);
     for (int k = 0; k < 2; ++k) {
         cudaFree(p->slot[k]);
         if (p->uploaded[k]) cudaEventDestroy(p->uploaded[k]);
         if (p->released[k]) cudaEventDestroy(p->released[k]);
+        if (p->slot_fused[k]) cudaEventDestroy(p->slot_fused[k]);
     }
+    if (p->us) cudaStreamDestroy(p->us);
     if (p->fused) cudaEventDestroy(p->fused);
     if (p->fork) cudaEventDestroy(p->fork);
     if (p->join) cudaEventDestroy(p->join);
@@ -514,8 +531,8 @@ kifi_status kifi_pipeline_integrate(kifi_pipeline* p, const void* depth_host, in
         p->slot_bytes = bytes;
     }
     const int k = (int)(p->frame & 1);
-    KIFI_CUDA(cudaStreamWaitEvent(p->vs, p->released[k], 0));
     if (p->graphs) {
+        KIFI_CUDA(cudaStreamWaitEvent(p->vs, p->released[k], 0));
         cudaPointerAttributes attr;
         const bool pinned = cudaPointerGetAttributes(&attr, depth_host) == cudaSuccess &&
                             attr.type == cudaMemoryTypeHost;
@@ -527,8 +544,13 @@ kifi_status kifi_pipeline_integrate(kifi_pipeline* p, const void* depth_host, in
             return kifi_pipeline_sync(p, out_eye_to_world);
         }
     }
-    KIFI_CUDA(cudaMemcpyAsync(p->slot[k], depth_host, bytes, cudaMemcpyHostToDevice, p->vs));
-    KIFI_CUDA(cudaEventRecord(p->uploaded[k], p->vs));
+    // the upload stream: slot k is free once the frame two back is no longer
+    // read by tracking or fusion; it does not queue behind the previous
+    // frame's fusion, so tracking starts as soon as the frame is on the device
+    KIFI_CUDA(cudaStreamWaitEvent(p->us, p->released[k], 0));
+    KIFI_CUDA(cudaStreamWaitEvent(p->us, p->slot_fused[k], 0));
+    KIFI_CUDA(cudaMemcpyAsync(p->slot[k], depth_host, bytes, cudaMemcpyHostToDevice, p->us));
+    KIFI_CUDA(cudaEventRecord(p->uploaded[k], p->us));
     kifi_status s = p->closed ? closed_loop_frame(p, p->slot[k], depth_is_u16 != 0, k, world_to_eye)
                               : track_and_fuse(p, p->slot[k], depth_is_u16 != 0, k, world_to_eye);
     if (s) return s;
