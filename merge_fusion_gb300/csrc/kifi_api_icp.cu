@@ -1,5 +1,7 @@
 // kifi_api_icp.cu -- C ABI of the ICP context and of Renderer::Bin
 // (include/kifi_gpu.h).  Host code; the kernels live in kifi_icp.cu.
+#include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -31,6 +33,10 @@ struct kifi_icp {
     size_t pairs_cap = 0, pairs_n = 0;
     void* zbuf = nullptr;            // Bin's z-buffer (8 bytes per target pixel)
     size_t zbuf_cap = 0;
+    IcpPoseMail* mail = nullptr;     // page-locked, mapped: the last step's pose ...
+    IcpPoseMail* mail_dev = nullptr; // ... its device address
+    unsigned long long mail_seq = 0; // ... and the number of the latest alignment
+    bool publish = false;            // alignments publish their pose (icp_publish_pose)
 };
 
 namespace {
@@ -95,8 +101,9 @@ kifi_status enqueue_align(kifi_icp* c, const void* depth_dev, bool u16, const ki
         a.pairs_len2 = c->pairs_len2;
         c->pairs_n = n_src;
     }
+    if (c->publish) ++c->mail_seq;
     KIFI_CUDA(icp_align_enqueue(a, c->st, load_mat(guess), iterations, icp_ctas(c, n_src),
-                                c->stream));
+                                c->stream, c->publish ? c->mail_dev : nullptr, c->mail_seq));
     c->last_iters = iterations;
     return KIFI_OK;
 }
@@ -177,6 +184,11 @@ kifi_status kifi_icp_create(int device, void* stream, kifi_icp** out) {
     }
     if (!e) e = cudaMalloc(&c->st, sizeof(IcpState));
     if (!e) e = cudaMallocHost(&c->head, offsetof(IcpState, part));
+    if (!e) e = cudaHostAlloc((void**)&c->mail, sizeof(IcpPoseMail), cudaHostAllocMapped);
+    if (!e) {
+        c->mail->seq = 0;
+        e = cudaHostGetDevicePointer((void**)&c->mail_dev, c->mail, 0);
+    }
     if (!e) e = cudaMemsetAsync(c->st, 0, sizeof(IcpState), c->stream);  // ordered before the context's work
     if (e) {
         kifi_icp_destroy(c);
@@ -200,6 +212,7 @@ kifi_status kifi_icp_destroy(kifi_icp* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     cudaFree(c->st);
     cudaFreeHost(c->head);
+    cudaFreeHost(c->mail);
     cudaFree(c->depth_dev);
     cudaFree(c->synth);
     cudaFree(c->pairs);
@@ -343,6 +356,35 @@ kifi_status kifi_icp_result(kifi_icp* c, float out_eye_to_world[16], double out_
     }
     return KIFI_OK;
 }
+
+}  // extern "C"
+
+// The pose of the latest alignment as its last step publishes it (see
+// IcpPoseMail), polled without synchronising the stream: the caller gets
+// it as soon as the final finisher has written it, not after the work
+// queued behind it.  Polls for at most two seconds, then takes the
+// synchronising path, which also reports device errors.
+void icp_publish_pose(kifi_icp* c, bool on) { c->publish = on; }
+
+kifi_status icp_wait_pose(kifi_icp* c, float out_eye_to_world[16]) {
+    if (c->last_iters > 0 && c->publish && c->mail) {
+        const unsigned long long want = c->mail_seq;
+        const volatile unsigned long long* seq = &c->mail->seq;
+        const auto t0 = std::chrono::steady_clock::now();
+        for (unsigned long long spins = 0;; ++spins) {
+            if (*seq == want) {
+                std::atomic_thread_fence(std::memory_order_acquire);
+                const volatile float* pose = c->mail->pose;
+                for (int i = 0; i < 16; ++i) out_eye_to_world[i] = pose[i];
+                return KIFI_OK;
+            }
+            if ((spins & 1023) == 1023 && std::chrono::steady_clock::now() - t0 > std::chrono::seconds(2)) break;
+        }
+    }
+    return kifi_icp_result(c, out_eye_to_world, nullptr, nullptr, nullptr, 0, nullptr);
+}
+
+extern "C" {
 
 kifi_status kifi_icp_iteration_times(kifi_icp* c, float* body_us, float* tail_us, int capacity,
                                      int* iterations) {

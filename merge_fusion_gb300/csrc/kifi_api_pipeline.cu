@@ -44,6 +44,7 @@
 // the counts grows the buffers (stream-ordered allocation) and emits again.
 // kifi_pipeline_mesh_counts, kifi_pipeline_sync and kifi_pipeline_join cover
 // the mesh stream.
+#include <algorithm>
 #include <array>
 #include <cstring>
 #include <new>
@@ -56,6 +57,19 @@ using namespace kifi;
 namespace {
 // the synthetic target the reference's tracking pipeline bins into (Pipeline.cpp:50)
 constexpr int kClosedLoopTargetW = 1024, kClosedLoopTargetH = 768;
+
+// A host frame in page-locked memory the device can address, read over the
+// host link into a frame slot: one 16-byte load per thread, all in flight
+// at once (a copy-engine transfer of a 600 KB frame takes several times as
+// long to start and finish); the bytes past the last full vector by CTA 0.
+__global__ void k_upload(const uint4* __restrict__ src, uint4* __restrict__ dst, size_t n16,
+                         const unsigned char* __restrict__ src_b, unsigned char* __restrict__ dst_b,
+                         size_t n_bytes) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = src[i];
+    if (blockIdx.x == 0)
+        for (size_t j = n16 * 16 + threadIdx.x; j < n_bytes; j += blockDim.x) dst_b[j] = src_b[j];
+}
 }  // namespace
 
 struct kifi_pipeline {
@@ -293,6 +307,8 @@ kifi_status track_and_fuse(kifi_pipeline* p, const void* depth_dev, bool u16, in
     const Mat4 e2w = invert_transform(load_mat(world_to_eye));
     if (p->desc.icp_iterations > 0) {
         if (k >= 0) KIFI_CUDA(cudaStreamWaitEvent(p->is, p->uploaded[k], 0));
+        // a host-fed frame's caller waits for the pose: published by the last step
+        icp_publish_pose(p->icp, k >= 0);
         if (p->have_prev && (s = align(p, depth_dev, u16, p->prev_e2w))) return s;
         // this frame becomes the next frame's target
         if ((s = kifi_icp_set_target_from_depth(p->icp, depth_dev, 1, u16 ? 1 : 0, &cam, e2w.m)))
@@ -384,8 +400,12 @@ kifi_status frame_result(kifi_pipeline* p, int k, float out_eye_to_world[16]) {
         return KIFI_OK;
     }
     if (p->desc.icp_iterations > 0) {
-        if (p->frame > 1)
-            return kifi_icp_result(p->icp, out_eye_to_world, nullptr, nullptr, nullptr, 0, nullptr);
+        if (p->frame > 1) {
+            float pose[16];
+            kifi_status s = icp_wait_pose(p->icp, pose);
+            if (!s && out_eye_to_world) std::memcpy(out_eye_to_world, pose, 64);
+            return s;
+        }
         KIFI_CUDA(cudaStreamSynchronize(p->is));  // the first frame only sets the target
     } else {
         KIFI_CUDA(cudaEventSynchronize(p->uploaded[k]));
@@ -549,7 +569,22 @@ kifi_status kifi_pipeline_integrate(kifi_pipeline* p, const void* depth_host, in
     // frame's fusion, so tracking starts as soon as the frame is on the device
     KIFI_CUDA(cudaStreamWaitEvent(p->us, p->released[k], 0));
     KIFI_CUDA(cudaStreamWaitEvent(p->us, p->slot_fused[k], 0));
-    KIFI_CUDA(cudaMemcpyAsync(p->slot[k], depth_host, bytes, cudaMemcpyHostToDevice, p->us));
+    cudaPointerAttributes attr;
+    const void* src_dev = nullptr;
+    if (cudaPointerGetAttributes(&attr, depth_host) == cudaSuccess && attr.type == cudaMemoryTypeHost &&
+        attr.devicePointer && ((uintptr_t)attr.devicePointer & 15u) == 0)
+        src_dev = attr.devicePointer;
+    cudaGetLastError();  // a pageable pointer is not an error here
+    if (src_dev) {
+        const size_t n16 = bytes / 16;
+        const int threads = 256;
+        const int blocks = (int)std::max<size_t>(1, std::min<size_t>((n16 + threads - 1) / threads, 4096));
+        k_upload<<<blocks, threads, 0, p->us>>>((const uint4*)src_dev, (uint4*)p->slot[k], n16,
+                                                (const unsigned char*)src_dev, (unsigned char*)p->slot[k], bytes);
+        KIFI_CUDA(cudaGetLastError());
+    } else {
+        KIFI_CUDA(cudaMemcpyAsync(p->slot[k], depth_host, bytes, cudaMemcpyHostToDevice, p->us));
+    }
     KIFI_CUDA(cudaEventRecord(p->uploaded[k], p->us));
     kifi_status s = p->closed ? closed_loop_frame(p, p->slot[k], depth_is_u16 != 0, k, world_to_eye)
                               : track_and_fuse(p, p->slot[k], depth_is_u16 != 0, k, world_to_eye);

@@ -81,6 +81,10 @@ struct kifi_volume {
 // ahead of enqueueing it -- nothing in kifi_volume_enqueue_frame then waits.
 kifi_status kifi_volume_prepare_frame(kifi_volume* v, const kifi_camera* cam);
 kifi_status kifi_icp_prepare_frame(kifi_icp* c, const kifi_camera* cam);
+// whether the context's alignments publish their final pose to its mailbox,
+// and that pose of the latest alignment, polled (kifi_api_icp.cu)
+void icp_publish_pose(kifi_icp* c, bool on);
+kifi_status icp_wait_pose(kifi_icp* c, float out_eye_to_world[16]);
 // batched alignment (kifi_api_batch.cu): one pair's arguments, and the next target's slot
 kifi_status kifi_icp_batch_args(kifi_icp* c, const void* depth_dev, const kifi_camera* cam, kifi::IcpArgs* a,
                                 kifi::IcpState** st, int iterations);

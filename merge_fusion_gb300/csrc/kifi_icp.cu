@@ -357,7 +357,8 @@ __device__ __forceinline__ float scan_staged(const Stage& sp, int base, int pitc
     return b0;
 }
 
-__device__ __noinline__ void finish_step(IcpState* __restrict__ st, const FF* __restrict__ tot);
+__device__ __noinline__ void finish_step(IcpState* __restrict__ st, const FF* __restrict__ tot,
+                                        IcpPoseMail* mail, unsigned long long mail_seq);
 
 // One ICP::AlignStep (ICP.cpp:35-265) as one kernel.
 //
@@ -646,7 +647,7 @@ __device__ __forceinline__ void icp_step_body(const IcpArgs& a, IcpState* __rest
     if (!last_cta(&st->done, s_count, &n_total, nblk)) return;
     __shared__ FF tot[kMoments];
     moments_total<kMoments>(st, n_total, tot, (int)nblk);
-    if (threadIdx.x < 32) finish_step(st, tot);
+    if (threadIdx.x < 32) finish_step(st, tot, a.mail, a.mail_seq);
 }
 
 __global__ void __launch_bounds__(kAssocThreads, 2) k_icp_step(IcpArgs a, IcpState* __restrict__ st) {
@@ -821,7 +822,8 @@ __device__ __forceinline__ void n_terms(int k, int& i1, int& i2, int& i3, bool& 
     t3 = (kT3 >> k) & 1u;
 }
 
-__device__ __noinline__ void finish_step(IcpState* __restrict__ st, const FF* __restrict__ tot) {
+__device__ __noinline__ void finish_step(IcpState* __restrict__ st, const FF* __restrict__ tot,
+                                        IcpPoseMail* mail, unsigned long long mail_seq) {
     __shared__ float s_f[10];
     __shared__ FF s_nf[10];
     const int lane = threadIdx.x & 31;
@@ -1002,6 +1004,18 @@ __device__ __noinline__ void finish_step(IcpState* __restrict__ st, const FF* __
         st->pose_lo[4 * pc + pr] = v.lo;
     }
     const FF md0 = shfl_ff(my_mu, 3), md1 = shfl_ff(my_mu, 4), md2 = shfl_ff(my_mu, 5);
+    // the alignment's last step publishes the pose to the host's mailbox (a
+    // launch argument, null in the other steps): lanes 0-11 their new entries,
+    // lanes 0, 3, 6, 9 their column's unchanged bottom entry, then lane 0 the number
+    if (mail) {
+        if (lane < 12) {
+            mail->pose[4 * pc + pr] = v.hi;
+            if (pr == 0) mail->pose[4 * pc + 3] = P[3].hi;
+        }
+        __threadfence_system();
+        __syncwarp();
+        if (lane == 0) *(volatile unsigned long long*)&mail->seq = mail_seq;
+    }
     if (lane != 0) return;
     st->n_assoc = (int)n;
     st->mu_s[0] = fadd(mu0.hi, mu0.lo);
@@ -1156,7 +1170,7 @@ __global__ void k_bin_resolve_target(const float* __restrict__ pts, const unsign
 }  // namespace
 
 cudaError_t icp_align_enqueue(const IcpArgs& a, IcpState* st, const Mat4& guess, int iterations,
-                              int /*ctas*/, cudaStream_t stream) {
+                              int /*ctas*/, cudaStream_t stream, IcpPoseMail* mail, unsigned long long seq) {
     k_icp_begin<<<1, 32, 0, stream>>>(st, guess);
     const int n_cols = (a.width + 3) / 4;
     const int tiles = ((n_cols + kTileCols - 1) / kTileCols) * ((a.height + kTileRows - 1) / kTileRows);
@@ -1175,8 +1189,13 @@ cudaError_t icp_align_enqueue(const IcpArgs& a, IcpState* st, const Mat4& guess,
     cfg.stream = stream;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
+    IcpArgs last = a;  // the last step publishes the pose
+    last.mail = mail;
+    last.mail_seq = seq;
+    IcpArgs other = a;
+    other.mail = nullptr;
     for (int it = 0; it < iterations; ++it) {
-        const cudaError_t e = cudaLaunchKernelEx(&cfg, k_icp_step, a, st);
+        const cudaError_t e = cudaLaunchKernelEx(&cfg, k_icp_step, it + 1 == iterations ? last : other, st);
         if (e != cudaSuccess) return e;
     }
     return cudaGetLastError();

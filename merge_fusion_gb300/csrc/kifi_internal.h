@@ -203,6 +203,14 @@ cudaError_t mesh_snapshot_enqueue(const DeviceCtl* ctl, const VolumeBuffers& vb,
 constexpr int kIcpMaxStats = 64;
 constexpr int kIcpMaxCtas = 2048;
 
+// Where the last step of an alignment publishes its pose for a host that
+// polls instead of synchronising (page-locked, mapped host memory): the pose
+// (kifi order), then the alignment's sequence number, written after it.
+struct IcpPoseMail {
+    float pose[16];
+    unsigned long long seq;
+};
+
 struct IcpArgs {
     const void* depth;      // source frame (float metres or uint16 mm)
     int depth_u16;
@@ -214,6 +222,8 @@ struct IcpArgs {
     long long* pairs;       // optional: per source the winner's target index (-1: none) ...
     float* pairs_len2;      // ... and its len^2, overwritten by every iteration
     float neg_zero;         // -0.0f, a value the device code cannot see at compile time
+    IcpPoseMail* mail;      // the step that publishes the final pose (the last): its
+    unsigned long long mail_seq;  // mailbox and the alignment's number; null otherwise
 };
 
 struct IcpIterStats {
@@ -262,8 +272,11 @@ struct BackprojectJob {
 cudaError_t backproject_batch_enqueue(const BackprojectJob* jobs, int n, const BlockMap& map, cudaStream_t st);
 // CTAs of one frame pair's association (one per tile)
 int icp_tiles(int width, int height);
+// mail (device address of mapped host memory, or null): the last step
+// publishes the final pose there with sequence number `seq`
 cudaError_t icp_align_enqueue(const IcpArgs& a, IcpState* st, const Mat4& guess, int iterations,
-                              int ctas, cudaStream_t stream);
+                              int ctas, cudaStream_t stream, IcpPoseMail* mail = nullptr,
+                              unsigned long long seq = 0);
 cudaError_t backproject_enqueue(const void* depth, bool u16, const kifi_camera& cam,
                                 const Mat4& eye_to_world, float4* out, int ctas, cudaStream_t st);
 cudaError_t expand_target_enqueue(const float* in, int n, float4* out, int ctas, cudaStream_t st);

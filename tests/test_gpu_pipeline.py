@@ -148,3 +148,19 @@ def test_pipeline_graphs_match_plain_launches(gpu, device_frames):
     # the first frame (no tracking) and the first tracked frame instantiate;
     # the rest update the instantiated graph in place
     assert built + updated == 6 and updated >= 3, (built, updated)
+
+
+def test_host_fed_frames_equal_device_frames(gpu):
+    """Frames fed from page-locked host memory (read by the upload kernel,
+    poses taken from the ICP mailbox) give the volume, poses and mesh of the
+    same frames fed from device memory."""
+    from merge_fusion_gb300 import _lib, scenes
+    lib = _lib.load()
+    seq = scenes.room_scene(n_frames=6, seed=8)
+    k0, v0, p0, m0, _ = _run_pipeline(lib, seq, False, True)
+    k1, v1, p1, m1, _ = _run_pipeline(lib, seq, False, False)
+    assert np.array_equal(k0, k1)
+    assert np.array_equal(canon_bits(v0), canon_bits(v1))
+    for a, b in zip(p0[1:], p1[1:]):  # from the first tracked frame on
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    assert m0 == m1
