@@ -278,22 +278,15 @@ __device__ __forceinline__ float scan_staged(const Stage& sp, int base, int pitc
         }
     };
     if (nc == 21) {
-        // Each row keeps only its smallest len^2 (fminf skips the NaNs of
-        // invalid points); the first row whose minimum is strictly below the
-        // best so far holds the winner, the first strict minimum of the
-        // row-major scan: its first candidate with that len^2, found by
-        // forming that row's candidates once more (the packed halves round
-        // exactly as the scalar operations do).
         const int o = base & 1;       // the pairs start at an even plane index
         const int cs = o ? 0 : 20;    // the leftover candidate's column
         const unsigned long long PX = f2_pack(px, px), PY = f2_pack(py, py), PZ = f2_pack(pz, pz);
         const unsigned long long DW = f2_pack(dw2, dw2), NZ = f2_pack(neg_zero, neg_zero);
-        const float inf = __int_as_float(0x7f800000);
-        float best = 0.01f;
-        int brow = -1;
-        const int base0 = base;
         for (int r = 0; r < nr; ++r, base += pitch) {
-            float m0 = inf, m1 = inf;
+            // a candidate records only its pair number (a constant of the
+            // unrolled row); the row and the parity are folded in once per row
+            int c0 = -1, c1 = -1;
+            bool moved = false;
             const int pb = base + o;
 #pragma unroll
             for (int k = 0; k < 10; ++k) {
@@ -307,37 +300,25 @@ __device__ __forceinline__ float scan_staged(const Stage& sp, int base, int pitc
                 const unsigned long long l2 = f2_add(f2_add(f2_sq(dx, NZ), f2_sq(dy, NZ)), zz);
                 float lo, hi;
                 f2_unpack(l2, lo, hi);
-                m0 = fminf(m0, lo);
-                m1 = fminf(m1, hi);
-            }
-            float ml = inf;
-            {
-                int cl = -1;
-                cand(base + cs, 0, ml, cl);
-            }
-            const float m = fminf(fminf(m0, m1), ml);
-            if (m < best) {
-                best = m;
-                brow = r;
-            }
-        }
-        if (brow >= 0) {
-            const int rb = base0 + brow * pitch;
-            int col = 0;
-            for (int c = 0; c < 21; ++c) {
-                const float dx = fsub(sp.x[rb + c], px), dy = fsub(sp.y[rb + c], py), dz = fsub(sp.z[rb + c], pz);
-                const float zz = kW ? fadd(fmul(dz, dz), dw2) : fmul(dz, dz);
-                const float l2 = fadd(fadd(fmul(dx, dx), fmul(dy, dy)), zz);
-                if (l2 == best) {
-                    col = c;
-                    break;
+                if (lo < b0) {
+                    b0 = lo;
+                    c0 = 2 * k;
+                }
+                if (hi < b1) {
+                    b1 = hi;
+                    c1 = 2 * k;
                 }
             }
-            *best_rc = brow * 32 + col;
-        } else {
-            *best_rc = -1;
+            {
+                int cl = -1;
+                cand(base + cs, 0, b2, cl);
+                moved = cl >= 0;
+            }
+            const int r32 = r * 32;
+            if (c0 >= 0) i0 = r32 + o + c0;
+            if (c1 >= 0) i1 = r32 + o + c1 + 1;
+            if (moved) i2 = r32 + cs;
         }
-        return best;
     } else {
         for (int r = 0; r < nr; ++r, base += pitch) {
             int c0 = -1;
