@@ -78,6 +78,7 @@ struct kifi_pipeline {
     kifi_icp* icp = nullptr;
     cudaStream_t vs = nullptr, is = nullptr;
     cudaStream_t us = nullptr;  // uploads of host-fed frames
+    cudaStream_t fs = nullptr;  // the volume's (fusion) stream, when the pipeline made it
     void* slot[2] = {nullptr, nullptr};  // host-fed frames (uint16 or float)
     size_t slot_bytes = 0;
     cudaEvent_t uploaded[2] = {nullptr, nullptr};   // frame in slot k is on the device
@@ -435,6 +436,17 @@ kifi_status kifi_pipeline_create(const kifi_pipeline_desc* d, kifi_pipeline** ou
     vd.initial_capacity = d->initial_capacity;
     vd.device = d->device;
     vd.key_bits = d->key_bits;
+    {
+        // fusion one priority step above the mesh stream (both below tracking), so
+        // a frame's fusion CTAs are scheduled ahead of a running mesh's (measured
+        // neutral to +0.4%: the mesh is background work)
+        int lowest = 0, greatest = 0;
+        if (cudaSetDevice(d->device) == cudaSuccess &&
+            cudaDeviceGetStreamPriorityRange(&lowest, &greatest) == cudaSuccess && greatest < lowest &&
+            cudaStreamCreateWithPriority(&p->fs, cudaStreamNonBlocking, lowest - 1) == cudaSuccess)
+            vd.stream = p->fs;
+        cudaGetLastError();
+    }
     kifi_status s = kifi_volume_create(&vd, &p->vol);
     if (!s && d->icp_iterations > 0 && !p->closed) {  // closed loop: fusion never runs beside tracking
         p->vol->tracking_grids = true;
@@ -516,7 +528,8 @@ kifi_status kifi_pipeline_destroy(kifi_pipeline* p) {
     if (p->snap_done) cudaEventDestroy(p->snap_done);
     if (p->counts_ready) cudaEventDestroy(p->counts_ready);
     kifi_icp_destroy(p->icp);
-    kifi_volume_destroy(p->vol);
+    kifi_volume_destroy(p->vol);  // synchronises the fusion stream first
+    if (p->fs) cudaStreamDestroy(p->fs);
     delete p;
     return KIFI_OK;
 }
