@@ -150,13 +150,16 @@ def test_pipeline_graphs_match_plain_launches(gpu, device_frames):
     assert built + updated == 6 and updated >= 3, (built, updated)
 
 
-def test_host_fed_frames_equal_device_frames(gpu):
+@pytest.mark.parametrize("size", [(640, 480, 585.0), (132, 97, 121.0)])
+def test_host_fed_frames_equal_device_frames(gpu, size):
     """Frames fed from page-locked host memory (read by the upload kernel,
     poses taken from the ICP mailbox) give the volume, poses and mesh of the
-    same frames fed from device memory."""
+    same frames fed from device memory.  132 x 97 uint16 is 25,608 bytes:
+    the upload's 16-byte vectors leave 8 bytes for its tail."""
     from merge_fusion_gb300 import _lib, scenes
     lib = _lib.load()
-    seq = scenes.room_scene(n_frames=6, seed=8)
+    w, h, f = size
+    seq = scenes.room_scene(n_frames=6, seed=8, width=w, height=h, f=f)
     k0, v0, p0, m0, _ = _run_pipeline(lib, seq, False, True)
     k1, v1, p1, m1, _ = _run_pipeline(lib, seq, False, False)
     assert np.array_equal(k0, k1)
