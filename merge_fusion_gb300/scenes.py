@@ -145,7 +145,7 @@ def _render(ray_eye, pose, scene, rng, znear, zfar, dropout):
 
 
 def sphere_scene(n_frames=10, seed=0, width=320, height=240):
-    """configs[0]: sphere on a plane, 320x240, f=292.5."""
+    """The small sphere-on-a-plane scene: 320x240, f=292.5."""
     rng = np.random.default_rng(seed)
     fx = fy = 292.5 * width / 320.0
     cx, cy = width / 2.0, height / 2.0
@@ -206,7 +206,8 @@ def room_trajectory(n_frames, seed=0, scale=1.0):
 
 def room_scene(n_frames=300, seed=0, width=640, height=480, f=585.0, scale=1.0, dropout=0.02,
                first_frame=0):
-    """configs[1] (and, with scale=2 and 512x424, configs[2]): the seeded room
+    """The 640x480 room workload (and, with scale=2 and 512x424, the large-volume
+    room of the 4096^3 study): the seeded room
     rendered on the CPU by the same renderer the benchmark runs on the GPU
     (render_room_torch; both devices give identical frames)."""
     frames, poses = render_room_torch(n_frames, seed, width, height, f, scale, dropout, first_frame,
