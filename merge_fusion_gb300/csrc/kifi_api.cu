@@ -651,6 +651,7 @@ static kifi_status mesh_to_device(kifi_volume* v, int with_indices, size_t* n_ve
         }
         KIFI_CUDA(cudaMemcpyAsync(mc, v->ms.counts, sizeof(MeshCounts), cudaMemcpyDeviceToHost, v->stream));
         KIFI_CUDA(cudaStreamSynchronize(v->stream));
+        if (mc->error) return fail(KIFI_ERR_TIMEOUT, "mesh classification: a bounded wait gave up");
         if (!mc->overflow) break;
         if (attempt == 1) return fail(KIFI_ERR_CUDA, "mesh emission overflowed buffers sized to its counts");
         const size_t nv = (size_t)mc->n_verts, ni = with_indices ? (size_t)mc->n_idx : 0;

@@ -178,6 +178,10 @@ kifi_status mesh_poll(kifi_pipeline* p, bool wait) {
             if (q != cudaSuccess) return cuda_fail(q, "mesh counts");
         }
         const MeshCounts& c = *p->counts_host;
+        if (c.error) {  // the classification gave up on a bounded wait: no mesh
+            p->counting = false;
+            return fail(KIFI_ERR_TIMEOUT, "mesh classification: a bounded wait gave up");
+        }
         const size_t nv = (size_t)c.n_verts, ni = p->desc.mesh_with_indices ? (size_t)c.n_idx : 0;
         if (!c.overflow) {
             p->mesh_verts = nv;

@@ -149,6 +149,7 @@ struct MeshCounts {
     unsigned long long missing_min;  // smallest triangle edge id without a vertex (or ~0)
     unsigned long long overflow;     // emission skipped: the output buffers were too small
     unsigned long long n_flagged;    // voxels with output (vertices or triangles)
+    unsigned long long error;        // non-zero: a bounded wait of the classification gave up
 };
 
 // per classification tile: the voxels staged for its lookups -- region A,

@@ -297,11 +297,120 @@ __device__ __forceinline__ unsigned int classify_status(const unsigned int (&st)
 constexpr int kClassItems = 4;
 constexpr int kClassTile = kThreads * kClassItems;  // 1024 voxels
 constexpr int kStageA = 2048, kStageB = 2048;        // staged keys per region
-// dynamic shared memory of k_mesh_classify_tiled: keys of regions A and B,
-// then their status bytes
+// One staging buffer: keys of region A, keys of region B (two ranges), then
+// the status bytes alike.  Copies start on 16-byte boundaries, so each part
+// has room for the alignment shifts and round-ups; every part starts on a
+// 16-byte boundary.  Two buffers: the next tile's copies land in one while
+// the current tile is classified from the other.
+constexpr int kKeyA = kStageA + 8, kKeyB = kStageB + 16, kStA = kStageA + 32, kStB = kStageB + 64;
+template <typename K>
+__host__ __device__ constexpr size_t class_buf_bytes() {
+    return (size_t)(kKeyA + kKeyB) * sizeof(K) + kStA + kStB;
+}
 template <typename K>
 __host__ __device__ constexpr size_t class_smem() {
-    return (size_t)(kStageA + kStageB) * (sizeof(K) + 1);
+    return 2 * class_buf_bytes<K>();
+}
+static_assert(class_buf_bytes<uint32_t>() % 16 == 0 && class_buf_bytes<uint64_t>() % 16 == 0, "16-byte parts");
+static_assert((kKeyA * 4) % 16 == 0 && (kKeyA * 8) % 16 == 0 && kStA % 16 == 0, "16-byte parts");
+
+constexpr unsigned int kStageSpinLimit = 1u << 24;  // polls before a staging wait gives up
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init1(uint64_t* bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+    for (unsigned int i = 0; i < kStageSpinLimit; ++i)
+        if (mbar_try(bar, parity)) return true;
+    return false;
+}
+// `bytes` (a multiple of 16) from global `src` to shared `dst`, both 16-byte
+// aligned, completing on `bar` by transaction bytes
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
+// Where a tile's staged regions sit in its buffer: per part, the element
+// offset of the aligned copy's start and of the range's first element.
+struct StagedTile {
+    unsigned int ka0, ka;        // region A keys
+    unsigned int sa0, sa;        // region A statuses
+    unsigned int kb0[2], kb[2];  // region B keys, per range
+    unsigned int sb0[2], sb[2];  // region B statuses, per range
+};
+__device__ __forceinline__ unsigned int up_to(unsigned int x, unsigned int m) { return (x + m - 1) / m * m; }
+template <typename K>
+__device__ __forceinline__ StagedTile staged_tile(const MeshTileRange& r, unsigned int i0) {
+    constexpr unsigned int kv = 16 / sizeof(K);  // keys per 16 bytes
+    StagedTile L;
+    L.ka0 = 0;
+    L.ka = i0 % kv;
+    L.sa0 = 0;
+    L.sa = i0 % 16u;
+    unsigned int ko = 0, so = 0;
+#pragma unroll
+    for (int sg = 0; sg < 2; ++sg) {
+        L.kb0[sg] = ko;
+        L.kb[sg] = ko + r.b_lo[sg] % kv;
+        L.sb0[sg] = so;
+        L.sb[sg] = so + r.b_lo[sg] % 16u;
+        if (r.b_len[sg]) {
+            ko = up_to(L.kb[sg] + r.b_len[sg], kv);
+            so = up_to(L.sb[sg] + r.b_len[sg], 16u);
+        }
+    }
+    return L;
+}
+// thread 0: the copies of tile (r, i0) into buffer `buf`, announced on `bar`
+template <typename K>
+__device__ __forceinline__ void stage_tile_async(unsigned char* buf, const K* keys, const unsigned char* status,
+                                                 const MeshTileRange& r, unsigned int i0, uint64_t* bar) {
+    const StagedTile L = staged_tile<K>(r, i0);
+    K* kA = (K*)buf;
+    K* kB = kA + kKeyA;
+    unsigned char* sA = (unsigned char*)(kB + kKeyB);
+    unsigned char* sB = sA + kStA;
+    // the buffer's earlier contents were read through the generic proxy
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    const uint32_t bka = up_to((L.ka + r.a_len) * (unsigned int)sizeof(K), 16u);
+    const uint32_t bsa = up_to(L.sa + r.a_len, 16u);
+    uint32_t bkb[2], bsb[2];
+    uint32_t total = bka + bsa;
+#pragma unroll
+    for (int sg = 0; sg < 2; ++sg) {
+        bkb[sg] = r.b_len[sg] ? up_to((L.kb[sg] - L.kb0[sg] + r.b_len[sg]) * (unsigned int)sizeof(K), 16u) : 0u;
+        bsb[sg] = r.b_len[sg] ? up_to(L.sb[sg] - L.sb0[sg] + r.b_len[sg], 16u) : 0u;
+        total += bkb[sg] + bsb[sg];
+    }
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(total)
+                 : "memory");
+    bulk_g2s(kA + L.ka0, keys + (i0 - L.ka), bka, bar);
+    bulk_g2s(sA + L.sa0, status + (i0 - L.sa), bsa, bar);
+#pragma unroll
+    for (int sg = 0; sg < 2; ++sg)
+        if (r.b_len[sg]) {
+            const unsigned int lo = r.b_lo[sg];
+            bulk_g2s(kB + L.kb0[sg], keys + (lo - (L.kb[sg] - L.kb0[sg])), bkb[sg], bar);
+            bulk_g2s(sB + L.sb0[sg], status + (lo - (L.sb[sg] - L.sb0[sg])), bsb[sg], bar);
+        }
+}
+__device__ __forceinline__ bool tile_fits(const MeshTileRange& r) {
+    return r.a_len <= (unsigned int)kStageA && r.b_len[0] + r.b_len[1] <= (unsigned int)kStageB;
 }
 
 typedef MeshTileRange TileRange;
@@ -371,39 +480,63 @@ __global__ void __launch_bounds__(kThreads, 4) k_mesh_classify_tiled(const K* __
                                                                      unsigned long long* __restrict__ tile_sums,
                                                                      unsigned int* __restrict__ tile_nflag,
                                                                      unsigned int* __restrict__ flagged,
-                                                                     uint4* __restrict__ corners) {
+                                                                     uint4* __restrict__ corners,
+                                                                     unsigned long long* __restrict__ error) {
     constexpr int kD = kTris ? 3 : 2;  // offsets looked up: +y, +z (and +yz)
     extern __shared__ __align__(16) unsigned char class_mem[];
-    K* s_ka = (K*)class_mem;                                     // [kStageA]: region A keys
-    K* s_kb = s_ka + kStageA;                                    // [kStageB]: region B keys
-    unsigned char* s_sa = (unsigned char*)(s_kb + kStageB);      // [kStageA]: statuses
-    unsigned char* s_sb = s_sa + kStageA;                        // [kStageB]
+    __shared__ __align__(8) uint64_t s_bar[2];  // a staging buffer's copies have landed
+    __shared__ int s_fail;
     __shared__ uint64_t s_mc[256];
     if (kTris) mc_table_to_shared(s_mc);
     const unsigned int n = *n_dev;
     const Codec<K> cd(kb);
     const K delta[3] = {cd.pack(0, 1, 0), cd.pack(0, 0, 1), cd.pack(0, 1, 1)};
     const unsigned int tiles = min((n + kClassTile - 1) / kClassTile, max_tiles);
-    for (unsigned int t = blockIdx.x; t < tiles; t += gridDim.x) {
+    unsigned int issued0 = 0u, issued1 = 0u;  // thread 0: batches of copies issued per buffer
+    if (threadIdx.x == 0) {
+        mbar_init1(&s_bar[0]);
+        mbar_init1(&s_bar[1]);
+        s_fail = 0;
+        // the first tile's copies
+        if (blockIdx.x < tiles && tile_fits(ranges[blockIdx.x])) {
+            stage_tile_async<K>(class_mem, keys, status, ranges[blockIdx.x], blockIdx.x * kClassTile, &s_bar[0]);
+            ++issued0;
+        }
+    }
+    __syncthreads();
+    uint32_t phase0 = 0u, phase1 = 0u;  // per buffer: the parity of its next batch of copies
+    unsigned int it = 0;
+    for (unsigned int t = blockIdx.x; t < tiles; t += gridDim.x, ++it) {
         const unsigned int i0 = t * kClassTile;
         const unsigned int i1 = min(i0 + (unsigned int)kClassTile, n);
         const TileRange r = ranges[t];
-        const bool fits = r.a_len <= (unsigned int)kStageA && r.b_len[0] + r.b_len[1] <= (unsigned int)kStageB;
-        __syncthreads();  // the previous tile is done with the staging
-        if (fits) {
-            // independent loads: region A, then region B's ranges back to back
-            for (unsigned int j = threadIdx.x; j < r.a_len; j += kThreads) {
-                s_ka[j] = keys[i0 + j];
-                s_sa[j] = status[i0 + j];
-            }
-            const unsigned int nb = r.b_len[0] + r.b_len[1];
-            for (unsigned int j = threadIdx.x; j < nb; j += kThreads) {
-                const unsigned int g = j < r.b_len[0] ? r.b_lo[0] + j : r.b_lo[1] + (j - r.b_len[0]);
-                s_kb[j] = keys[g];
-                s_sb[j] = status[g];
+        const bool fits = tile_fits(r);
+        const unsigned int b = it & 1u;
+        unsigned char* buf = class_mem + b * class_buf_bytes<K>();
+        // the next tile's copies into the other buffer (free: every thread has
+        // passed the previous tile's closing barrier)
+        const unsigned int tn = t + gridDim.x;
+        if (threadIdx.x == 0 && tn < tiles) {
+            const TileRange rn = ranges[tn];
+            if (tile_fits(rn)) {
+                stage_tile_async<K>(class_mem + (b ^ 1u) * class_buf_bytes<K>(), keys, status, rn, tn * kClassTile,
+                                    &s_bar[b ^ 1u]);
+                if (b) ++issued0;
+                else ++issued1;
             }
         }
-        __syncthreads();
+        if (fits) {
+            const bool ok = mbar_wait_bounded(&s_bar[b], b ? phase1 : phase0);
+            if (!ok) s_fail = 1;
+            if (b) phase1 ^= 1u;
+            else phase0 ^= 1u;
+        }
+        if (__syncthreads_or(s_fail)) break;  // a wait gave up: leave the tile loop (reported below)
+        const StagedTile L = staged_tile<K>(r, i0);
+        const K* s_ka = (const K*)buf + L.ka;                                   // key i0 of region A
+        const unsigned char* s_sa = buf + (kKeyA + kKeyB) * sizeof(K) + L.sa;   // its status
+        const K* kbase = (const K*)buf + kKeyA;
+        const unsigned char* sbase = buf + (kKeyA + kKeyB) * sizeof(K) + kStA;
         const unsigned int tb = threadIdx.x * kClassItems;  // this thread's first voxel in the tile
         unsigned int pos[kD], seg[kD];  // running count of a range's staged keys <= key + d; its range
 #pragma unroll
@@ -444,46 +577,49 @@ __global__ void __launch_bounds__(kThreads, 4) k_mesh_classify_tiled(const K* __
                     st[0] = s0;
                     idx[1] = i + 1;
                     st[1] = s_ka[tb + j + 1] == key + cd.pack(1, 0, 0) ? s_sa[tb + j + 1] : 0u;
-                    unsigned int w[kD];  // staged index of each lookup's position in its region
+                    unsigned int w[kD];  // each lookup's position within its staged range
+                    // region B's range of this voxel (+z, +yz): its keys and statuses
+                    const unsigned int sgb = i >= r.split ? 1u : 0u;
+                    const K* s_kbr = kbase + (sgb ? L.kb[1] : L.kb[0]);
+                    const unsigned char* s_sbr = sbase + (sgb ? L.sb[1] : L.sb[0]);
 #pragma unroll
                     for (int d = 0; d < kD; ++d) {
                         // region A for +y (one range, from i0); region B for +z, +yz
-                        const unsigned int sg = d == 0 ? 0u : (i >= r.split ? 1u : 0u);
-                        const unsigned int base = sg ? r.b_len[0] : 0u;
-                        const unsigned int L = d == 0 ? r.a_len : (sg ? r.b_len[1] : r.b_len[0]);
+                        const unsigned int sg = d == 0 ? 0u : sgb;
+                        const unsigned int Ln = d == 0 ? r.a_len : (sg ? r.b_len[1] : r.b_len[0]);
                         const unsigned int lod = d == 0 ? i0 : (sg ? r.b_lo[1] : r.b_lo[0]);
-                        const K* sk = (d == 0 ? s_ka : s_kb) + base;
+                        const K* sk = d == 0 ? s_ka : s_kbr;
                         const K tk = key + delta[d];
                         unsigned int p = pos[d];
                         if (seg[d] != sg) {  // the thread's first live voxel in this range: search
-                            unsigned int a = 0, b = L;
-                            while (a < b) {
-                                const unsigned int mid = (a + b) >> 1;
+                            unsigned int a = 0, e = Ln;
+                            while (a < e) {
+                                const unsigned int mid = (a + e) >> 1;
                                 if (sk[mid] <= tk) a = mid + 1;
-                                else b = mid;
+                                else e = mid;
                             }
                             p = a;
                             seg[d] = sg;
                         } else {  // later voxels: the positions only move forward
-                            while (p < L && sk[p] <= tk) ++p;
+                            while (p < Ln && sk[p] <= tk) ++p;
                         }
                         pos[d] = p;
                         // walk_ptr = min(n - 2, upper_bound - 1), upper_bound = lo + p
                         const unsigned int gp = min(lod + p - 1u, n - 2u);
                         idx[d == 0 ? 2 : (d == 1 ? 4 : 6)] = gp;
-                        w[d] = base + (gp - lod);
+                        w[d] = gp - lod;
                     }
                     // corners: +y, +z (+yz) at the lookups, +xy, +xz (+xyz) one past
                     st[2] = s_ka[w[0]] == key + delta[0] ? s_sa[w[0]] : 0u;
-                    st[4] = s_kb[w[1]] == key + delta[1] ? s_sb[w[1]] : 0u;
+                    st[4] = s_kbr[w[1]] == key + delta[1] ? s_sbr[w[1]] : 0u;
                     idx[3] = idx[2] + 1;
                     idx[5] = idx[4] + 1;
                     if (kTris) {
-                        st[6] = s_kb[w[2]] == key + delta[2] ? s_sb[w[2]] : 0u;
+                        st[6] = s_kbr[w[2]] == key + delta[2] ? s_sbr[w[2]] : 0u;
                         idx[7] = idx[6] + 1;
                         st[3] = s_ka[w[0] + 1] == key + cd.pack(1, 1, 0) ? s_sa[w[0] + 1] : 0u;
-                        st[5] = s_kb[w[1] + 1] == key + cd.pack(1, 0, 1) ? s_sb[w[1] + 1] : 0u;
-                        st[7] = s_kb[w[2] + 1] == key + cd.pack(1, 1, 1) ? s_sb[w[2] + 1] : 0u;
+                        st[5] = s_kbr[w[1] + 1] == key + cd.pack(1, 0, 1) ? s_sbr[w[1] + 1] : 0u;
+                        st[7] = s_kbr[w[2] + 1] == key + cd.pack(1, 1, 1) ? s_sbr[w[2] + 1] : 0u;
                     } else {
                         idx[6] = idx[7] = 0u;
                         st[3] = st[5] = st[6] = st[7] = 0u;
@@ -530,6 +666,13 @@ __global__ void __launch_bounds__(kThreads, 4) k_mesh_classify_tiled(const K* __
             tile_sums[t] = (total >> 24 & 0xffffffull) << 32 | (total & 0xffffffull);
             tile_nflag[t] = (unsigned int)(total >> 48);
         }
+    }
+    if (s_fail && threadIdx.x == 0) {
+        // a staging wait gave up: report it (the mesh is not emitted) and wait,
+        // bounded, for the copies still in flight before the CTA exits
+        atomicExch(error, 1ull);
+        if (issued0) mbar_wait_bounded(&s_bar[0], (issued0 - 1u) & 1u);
+        if (issued1) mbar_wait_bounded(&s_bar[1], (issued1 - 1u) & 1u);
     }
 }
 
@@ -587,6 +730,7 @@ __global__ void __launch_bounds__(kThreads) k_mesh_emit(const K* __restrict__ ke
     // the counts of the counting passes; outputs that do not fit are not written
     // (every CTA sees the same counts and returns alike; the host grows and re-emits)
     const unsigned long long n_verts = mc->n_verts, n_idx = mc->n_idx;
+    if (mc->error) return;  // the classification gave up: nothing to emit (the host reports it)
     const bool overflow = n_verts > vert_cap || (kTris && n_idx > idx_cap);
     // the flag describes this emission (an earlier one into smaller buffers may have set it)
     if (blockIdx.x == 0 && threadIdx.x == 0) mc->overflow = overflow ? 1ull : 0ull;
@@ -801,7 +945,7 @@ cudaError_t mesh_scratch_reserve(MeshScratch* m, size_t n, int kb) {
     const size_t tiles = (cap + kClassTile - 1) / kClassTile + 1;
     cudaError_t e;
     if ((e = cudaMalloc(&m->vflags, cap * sizeof(unsigned int)))) return e;
-    if ((e = cudaMalloc(&m->vstatus, (cap + 4) / 4 * 4))) return e;
+    if ((e = cudaMalloc(&m->vstatus, (cap + 4) / 4 * 4 + 32))) return e;  // 16-byte copies read past the end
     if ((e = cudaMalloc(&m->corners, cap * sizeof(uint4)))) return e;
     if ((e = cudaMalloc(&m->tile_sums, tiles * sizeof(unsigned long long)))) return e;
     if ((e = cudaMalloc(&m->tile_nflag, tiles * sizeof(unsigned int)))) return e;
@@ -840,6 +984,7 @@ static int grid_for(size_t n, int sms) {
 template <typename K>
 static void mesh_count_t(const K* keys, const float2* vals, size_t n_cap, int kb, int with_indices, MeshScratch& ms,
                          int sms, cudaStream_t st, cudaEvent_t* stage_events) {
+    cudaMemsetAsync(&ms.counts->error, 0, sizeof(unsigned long long), st);  // set by a staging wait that gives up
     k_row_directory<K><<<grid_for(((size_t)1 << (2 * kb)) + 1, sms), kThreads, 0, st>>>(keys, ms.n_dev, kb, ms.rows);
     if (stage_events) cudaEventRecord(stage_events[0], st);
     // tile ranges, then the classification (its grid: up to 8 CTAs per SM, each walking tiles)
@@ -854,14 +999,14 @@ static void mesh_count_t(const K* keys, const float2* vals, size_t n_cap, int kb
         k_mesh_classify_tiled<true, K><<<class_grid, kThreads, smem, st>>>(keys, kb, vals, ms.vstatus, ms.rows, ms.n_dev,
                                                                           ms.tile_ranges, max_tiles, ms.vflags,
                                                                           ms.tile_sums, ms.tile_nflag, ms.flagged,
-                                                                          ms.corners);
+                                                                          ms.corners, &ms.counts->error);
     } else {
         const size_t smem = class_smem<K>();
         cudaFuncSetAttribute(k_mesh_classify_tiled<false, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_mesh_classify_tiled<false, K><<<class_grid, kThreads, smem, st>>>(keys, kb, vals, ms.vstatus, ms.rows, ms.n_dev,
                                                                            ms.tile_ranges, max_tiles, ms.vflags,
                                                                            ms.tile_sums, ms.tile_nflag, ms.flagged,
-                                                                           ms.corners);
+                                                                           ms.corners, &ms.counts->error);
     }
     if (stage_events) cudaEventRecord(stage_events[1], st);
     k_scan_tile_sums<<<1, kSumThreads, 0, st>>>(ms.tile_sums, ms.tile_nflag, ms.n_dev, ms.counts);
