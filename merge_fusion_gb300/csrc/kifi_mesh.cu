@@ -415,6 +415,11 @@ __device__ __forceinline__ bool tile_fits(const MeshTileRange& r) {
 
 typedef MeshTileRange TileRange;
 
+// Eight lanes per tile.  The z-slice split needs no search: the first key of
+// slice z0 + 1 starts row (z0 + 1) << b of the row directory.  The tile's up
+// to seven neighbour searches are independent and run one per lane.
+constexpr int kRangeLanes = 8;
+
 template <typename K>
 __global__ void k_mesh_tile_ranges(const K* __restrict__ keys, int kb, const unsigned int* __restrict__ rs,
                                    const unsigned int* __restrict__ n_dev, int with_yz,
@@ -423,9 +428,10 @@ __global__ void k_mesh_tile_ranges(const K* __restrict__ keys, int kb, const uns
     const unsigned int tiles = min((n + kClassTile - 1) / kClassTile, max_tiles);
     const Codec<K> cd(kb);
     const K dy = cd.pack(0, 1, 0), dz = cd.pack(0, 0, 1), dyz = cd.pack(0, 1, 1);
-    // walk position (unclamped) of key + delta
-    auto wpos = [&](K t) { return upper_bound_row<K>(keys, rs, t, n, cd, 0u) - 1u; };
-    for (unsigned int t = blockIdx.x * blockDim.x + threadIdx.x; t < tiles; t += gridDim.x * blockDim.x) {
+    const unsigned int lane = threadIdx.x & (kRangeLanes - 1);
+    const unsigned int gmask = 0xFFu << ((threadIdx.x & 31u) & ~(unsigned int)(kRangeLanes - 1));
+    const unsigned int groups = gridDim.x * blockDim.x / kRangeLanes;
+    for (unsigned int t = (blockIdx.x * blockDim.x + threadIdx.x) / kRangeLanes; t < tiles; t += groups) {
         const unsigned int i0 = t * kClassTile;
         const unsigned int last = min(min(i0 + (unsigned int)kClassTile, n), n - 1u);  // voxels with a cube: < last
         TileRange r;
@@ -434,37 +440,42 @@ __global__ void k_mesh_tile_ranges(const K* __restrict__ keys, int kb, const uns
         r.a_len = min(i0 + (unsigned int)kClassTile + 1u, n) - i0;
         r.split = last;
         if (last > i0) {
-            r.a_len = max(r.a_len, min(wpos(keys[last - 1] + dy) + 1u, n - 1u) + 1u - i0);
+            const K k0 = keys[i0], kl = keys[last - 1];
             unsigned int split = last;
-            const unsigned int z0 = cd.z(keys[i0]), zl = cd.z(keys[last - 1]);
+            const unsigned int z0 = cd.z(k0), zl = cd.z(kl);
             if (z0 != zl) {  // a range per z slice when the tile spans exactly two
-                const K bound = cd.pack(0, 0, z0 + 1);  // first key of the next slice
-                unsigned int a = i0 + 1, b = last - 1;  // keys[i0] < bound <= keys[last - 1]
-                while (a < b) {
-                    const unsigned int mid = (a + b) >> 1;
-                    if (keys[mid] < bound) a = mid + 1;
-                    else b = mid;
-                }
+                const unsigned int a = rs[cd.row(cd.pack(0, 0, z0 + 1))];  // keys[i0] < keys[a] <= keys[last - 1]
                 if (cd.z(keys[a]) == zl) split = a;
             }
-            // region B: from the first +z position (clamped) to the last +z or +yz
-            // position plus one
-            unsigned int first = i0, end = split;
+            const bool two = split < last;
+            // region B per slice: from the first +z position (clamped) to the
+            // last +z or +yz position plus one
+            K q = kl + dy;
+            bool active = true;
+            switch (lane) {
+                case 1: q = k0 + dz; break;
+                case 2: q = keys[split - 1] + dz; break;
+                case 3: q = keys[split - 1] + dyz; active = with_yz; break;
+                case 4: q = keys[split] + dz; active = two; break;
+                case 5: q = kl + dz; active = two; break;
+                case 6: q = kl + dyz; active = two && with_yz; break;
+                case 7: active = false; break;
+                default: break;
+            }
+            const unsigned int p = active ? upper_bound_row<K>(keys, rs, q, n, cd, 0u) - 1u : 0u;
+            unsigned int w[7];
 #pragma unroll
-            for (int sg = 0; sg < 2; ++sg) {
-                if (first < end) {
-                    const unsigned int lo = min(wpos(keys[first] + dz), n - 2u);
-                    unsigned int hi = wpos(keys[end - 1] + dz);
-                    if (with_yz) hi = max(hi, wpos(keys[end - 1] + dyz));
-                    r.b_lo[sg] = lo;
-                    r.b_len[sg] = min(hi + 1u, n - 1u) - lo + 1u;
-                }
-                first = split;
-                end = last;
+            for (int j = 0; j < 7; ++j) w[j] = __shfl_sync(gmask, p, j, kRangeLanes);
+            r.a_len = max(r.a_len, min(w[0] + 1u, n - 1u) + 1u - i0);
+            r.b_lo[0] = min(w[1], n - 2u);
+            r.b_len[0] = min((with_yz ? max(w[2], w[3]) : w[2]) + 1u, n - 1u) - r.b_lo[0] + 1u;
+            if (two) {
+                r.b_lo[1] = min(w[4], n - 2u);
+                r.b_len[1] = min((with_yz ? max(w[5], w[6]) : w[5]) + 1u, n - 1u) - r.b_lo[1] + 1u;
             }
             r.split = split;
         }
-        ranges[t] = r;
+        if (lane == 0) ranges[t] = r;
     }
 }
 
@@ -890,22 +901,34 @@ __global__ void __launch_bounds__(kThreads) k_mesh_emit(const K* __restrict__ ke
 // (index count << 32 | vertex count) and of their counts of voxels with
 // output (the total after the last), the totals to *counts; the packed
 // halves stay below 2^32 for volumes under 2^28 voxels
-constexpr int kSumThreads = 1024, kSumItems = 8;
+constexpr int kSumThreads = 1024, kSumItems = 8, kSumRound = kSumThreads * kSumItems;
+// dynamic shared memory of k_scan_tile_sums: one round of both arrays
+constexpr size_t kSumSmem = (size_t)kSumRound * (sizeof(unsigned long long) + sizeof(unsigned int));
 __global__ void __launch_bounds__(kSumThreads) k_scan_tile_sums(unsigned long long* __restrict__ sums,
                                                                 unsigned int* __restrict__ nflag,
                                                                 const unsigned int* __restrict__ n_dev,
                                                                 MeshCounts* __restrict__ counts) {
+    extern __shared__ __align__(16) unsigned char sum_mem[];
+    unsigned long long* s_v = (unsigned long long*)sum_mem;  // [kSumRound]
+    unsigned int* s_f = (unsigned int*)(s_v + kSumRound);    // [kSumRound]
     const unsigned int n_tiles = (*n_dev + kClassTile - 1) / kClassTile;
     unsigned long long carry = 0, fcarry = 0;
-    for (unsigned int b = 0; b < n_tiles; b += kSumThreads * kSumItems) {
-        const unsigned int i0 = b + threadIdx.x * kSumItems;
+    for (unsigned int b = 0; b < n_tiles; b += kSumRound) {
+        // coalesced loads of the round into shared memory, then each thread
+        // takes kSumItems consecutive entries from there
+        for (unsigned int j = threadIdx.x; j < (unsigned int)kSumRound; j += kSumThreads) {
+            const bool in = b + j < n_tiles;
+            s_v[j] = in ? sums[b + j] : 0ull;
+            s_f[j] = in ? nflag[b + j] : 0u;
+        }
+        __syncthreads();
+        const unsigned int l0 = threadIdx.x * kSumItems;
         unsigned long long v[kSumItems], s = 0, fs = 0;
         unsigned int fv[kSumItems];
 #pragma unroll
         for (int q = 0; q < kSumItems; ++q) {
-            const bool in = i0 + q < n_tiles;
-            v[q] = in ? sums[i0 + q] : 0ull;
-            fv[q] = in ? nflag[i0 + q] : 0u;
+            v[q] = s_v[l0 + q];
+            fv[q] = s_f[l0 + q];
             s += v[q];
             fs += fv[q];
         }
@@ -914,15 +937,20 @@ __global__ void __launch_bounds__(kSumThreads) k_scan_tile_sums(unsigned long lo
         unsigned long long frun = fcarry + block_exclusive_scan<kSumThreads>(fs, &ftotal);
 #pragma unroll
         for (int q = 0; q < kSumItems; ++q) {
-            if (i0 + q < n_tiles) {
-                sums[i0 + q] = run;
-                nflag[i0 + q] = (unsigned int)frun;
-            }
+            s_v[l0 + q] = run;
+            s_f[l0 + q] = (unsigned int)frun;
             run += v[q];
             frun += fv[q];
         }
+        __syncthreads();
+        for (unsigned int j = threadIdx.x; j < (unsigned int)kSumRound; j += kSumThreads)
+            if (b + j < n_tiles) {
+                sums[b + j] = s_v[j];
+                nflag[b + j] = s_f[j];
+            }
         carry += total;
         fcarry += ftotal;
+        __syncthreads();  // the staging is reused by the next round
     }
     if (threadIdx.x == 0) {
         nflag[n_tiles] = (unsigned int)fcarry;
@@ -989,7 +1017,7 @@ static void mesh_count_t(const K* keys, const float2* vals, size_t n_cap, int kb
     if (stage_events) cudaEventRecord(stage_events[0], st);
     // tile ranges, then the classification (its grid: up to 8 CTAs per SM, each walking tiles)
     const unsigned int max_tiles = (unsigned int)((n_cap + kClassTile - 1) / kClassTile);
-    k_mesh_tile_ranges<K><<<grid_for((size_t)max_tiles, sms), kThreads, 0, st>>>(
+    k_mesh_tile_ranges<K><<<grid_for((size_t)max_tiles * kRangeLanes, sms), kThreads, 0, st>>>(
         keys, kb, ms.rows, ms.n_dev, with_indices, ms.tile_ranges, max_tiles);
     const int class_grid = (int)(max_tiles < (unsigned int)(sms * 8) ? (max_tiles ? max_tiles : 1) : sms * 8);
     k_mesh_status<<<grid_for((n_cap + 3) / 4, sms), kThreads, 0, st>>>(vals, ms.n_dev, (unsigned int*)ms.vstatus);
@@ -1009,7 +1037,8 @@ static void mesh_count_t(const K* keys, const float2* vals, size_t n_cap, int kb
                                                                            ms.corners, &ms.counts->error);
     }
     if (stage_events) cudaEventRecord(stage_events[1], st);
-    k_scan_tile_sums<<<1, kSumThreads, 0, st>>>(ms.tile_sums, ms.tile_nflag, ms.n_dev, ms.counts);
+    cudaFuncSetAttribute(k_scan_tile_sums, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSumSmem);
+    k_scan_tile_sums<<<1, kSumThreads, kSumSmem, st>>>(ms.tile_sums, ms.tile_nflag, ms.n_dev, ms.counts);
 }
 
 cudaError_t mesh_count_enqueue(const void* keys, int key_bytes, const float2* vals, size_t n_cap, int kb,
