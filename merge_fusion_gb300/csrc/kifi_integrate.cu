@@ -3,7 +3,8 @@
 //
 //  k_frame_setup   derive eyeToWorld / worldToClip and the projection
 //                  constants from the pose (Integrator.cpp:41-42), reset the
-//                  per-frame counters.
+//                  per-frame counters (k_frame_setup_sort for 30-bit keys also
+//                  prepares the sort's digit histograms and tile counters).
 //  k_splat_emit    DepthMap2PointCloud (Integrator.cpp:76-183) fused with
 //                  ExpandChunks (:186-250) and the de-duplication of
 //                  std::unique (:50-55): every valid pixel's voxel key and its
@@ -11,7 +12,10 @@
 //                  occupancy bitmap (one bit per voxel of the res^3 grid); the
 //                  thread whose atomicOr flips a bit owns that key and appends
 //                  it to the frame's list of keys NEW to the volume.
-//  (radix sort)    the new keys are sorted (kifi_sort.cu).
+//                  For 30-bit keys (k_splat_emit_hist) it also counts the
+//                  three 10-bit digits of every key it stores.
+//  (radix sort)    the new keys are sorted (kifi_sort.cu): three 10-bit
+//                  digit passes for 30-bit keys.
 //  k_merge_update  flat_map::insert (flat_map.h:164-197) as a merge-path
 //                  merge of the sorted resident keys with the sorted new keys
 //                  into the other half of the ping-pong buffers, fused with
@@ -35,6 +39,8 @@
 // n/4*4 voxels of the merged volume only -- the reference's 4-wide loop drops
 // the n%4 tail (Integrator.cpp:269) -- which the merge kernel can apply
 // directly because the merged size n = N0 + #new is known before it runs.
+#include <algorithm>
+
 #include "kifi_internal.h"
 
 namespace kifi {
@@ -53,6 +59,19 @@ __global__ void k_frame_setup(DeviceCtl* ctl) {
     if (threadIdx.x == 0 && blockIdx.x == 0) {
         ctl->n_new = 0u;
         ctl->excluded_key = 0ull;
+    }
+}
+
+// The same for 30-bit keys, plus the set-up of the frame's sort: its digit
+// histograms (filled by the splat) zeroed, its passes' tile counters at the
+// first tile and a new look-back generation.
+__global__ void k_frame_setup_sort(DeviceCtl* ctl, SortScratch ss) {
+    for (int i = threadIdx.x; i < kSortHistWords; i += blockDim.x) ss.hist[i] = 0u;
+    if (threadIdx.x < kFrameSortPasses) ss.tile_counter[threadIdx.x] = ss.first_tile;
+    if (threadIdx.x == 0) {
+        ctl->n_new = 0u;
+        ctl->excluded_key = 0ull;
+        *ss.epoch += 1ull;
     }
 }
 
@@ -137,12 +156,25 @@ __device__ __forceinline__ bool splat_pixel(const FrameConst& fc, const float (&
 
 // Splat + dilation + new-key emission of one frame; `blk` / `nblk` are the
 // CTA's index and the CTA count working on this frame (the launch's own, or
-// a share of a batched launch over several volumes).
-template <bool kU16, typename K>
+// a share of a batched launch over several volumes).  With kHist (30-bit
+// keys) the CTA also counts the three 10-bit digits of every key it stores,
+// in shared memory, and adds its counts to the sort's histograms `hist`.
+template <bool kU16, typename K, bool kHist = false>
 __device__ __forceinline__ void splat_emit_body(DeviceCtl* __restrict__ ctl, const Geom& g,
                                                 const void* __restrict__ depth, uint32_t* __restrict__ bitmap,
                                                 K* __restrict__ new_keys, unsigned int new_cap,
-                                                const FrameConst& fc, unsigned int blk, unsigned int nblk) {
+                                                const FrameConst& fc, unsigned int blk, unsigned int nblk,
+                                                unsigned int* __restrict__ hist = nullptr) {
+    static_assert(!kHist || sizeof(K) == 4, "digit counts of 30-bit keys");
+    unsigned int* s_hist = nullptr;
+    if constexpr (kHist) {
+        // a CTA without pixels has nothing to count
+        if ((size_t)blk * kEmitThreads >= (size_t)fc.width * fc.height) return;
+        __shared__ unsigned int s_counts[kSortHistWords];
+        s_hist = s_counts;
+        for (int i = threadIdx.x; i < kSortHistWords; i += blockDim.x) s_hist[i] = 0u;
+        __syncthreads();
+    }
     const Codec<K> cd(g.kb);
     const int W = fc.width, H = fc.height;
     const size_t P = (size_t)W * H;
@@ -225,11 +257,28 @@ __device__ __forceinline__ void splat_emit_body(DeviceCtl* __restrict__ ctl, con
                 while (m) {
                     const uint32_t b = (uint32_t)__ffsll((long long)m) - 1u;
                     m &= m - 1ull;
-                    if (at < new_cap) new_keys[at] = cd.pack(bx + (b & 3u), by + ((b >> 2) & 3u), bz + (b >> 4));
-                    else atomicOr(&ctl->status, KIFI_DEV_ERR_CAPACITY);
+                    if (at < new_cap) {
+                        const K key_out = cd.pack(bx + (b & 3u), by + ((b >> 2) & 3u), bz + (b >> 4));
+                        new_keys[at] = key_out;
+                        if constexpr (kHist) {
+                            const uint32_t ku = (uint32_t)key_out;
+                            atomicAdd(&s_hist[ku & (kFrameRadix - 1)], 1u);
+                            atomicAdd(&s_hist[kFrameRadix + ((ku >> kFrameDigitBits) & (kFrameRadix - 1))], 1u);
+                            atomicAdd(&s_hist[2 * kFrameRadix + (ku >> (2 * kFrameDigitBits))], 1u);
+                        }
+                    } else {
+                        atomicOr(&ctl->status, KIFI_DEV_ERR_CAPACITY);
+                    }
                     ++at;
                 }
             }
+        }
+    }
+    if constexpr (kHist) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < kSortHistWords; i += blockDim.x) {
+            const unsigned int c = s_hist[i];
+            if (c) atomicAdd(&hist[i], c);
         }
     }
 }
@@ -242,6 +291,18 @@ __global__ void __launch_bounds__(kEmitThreads) k_splat_emit(DeviceCtl* __restri
                                                              unsigned int new_cap,
                                                              const FrameConst fc) {
     splat_emit_body<kU16, K>(ctl, g, depth, bitmap, new_keys, new_cap, fc, blockIdx.x, gridDim.x);
+}
+
+// 30-bit keys: the splat also fills the frame sort's digit histograms
+template <bool kU16>
+__global__ void __launch_bounds__(kEmitThreads) k_splat_emit_hist(DeviceCtl* __restrict__ ctl, Geom g,
+                                                                  const void* __restrict__ depth,
+                                                                  uint32_t* __restrict__ bitmap,
+                                                                  uint32_t* __restrict__ new_keys,
+                                                                  unsigned int new_cap, const FrameConst fc,
+                                                                  unsigned int* __restrict__ hist) {
+    splat_emit_body<kU16, uint32_t, true>(ctl, g, depth, bitmap, new_keys, new_cap, fc, blockIdx.x, gridDim.x,
+                                          hist);
 }
 
 // Packed float pairs (f32x2): one instruction, each half rounded as the
@@ -924,19 +985,41 @@ static cudaError_t integrate_enqueue_t(DeviceCtl* ctl, const Geom& g, VolumeBuff
     FrameConst fc = make_frame_const(cam, world_to_eye, g.res);
     fc.z_bounded = clip_z_bounded(fc.world_to_clip, g.side);
     if (events) cudaEventRecord(events[0], st);
-    k_frame_setup<<<1, 32, 0, st>>>(ctl);
     const unsigned int new_cap = (unsigned int)vb.new_cap;
     K* nk = (K*)vb.new_keys;
-    if (depth_u16)
-        k_splat_emit<true, K><<<ls.splat_ctas, kEmitThreads, 0, st>>>(ctl, g, depth_dev, vb.bitmap, nk, new_cap, fc);
-    else
-        k_splat_emit<false, K><<<ls.splat_ctas, kEmitThreads, 0, st>>>(ctl, g, depth_dev, vb.bitmap, nk, new_cap, fc);
-    if (events) cudaEventRecord(events[1], st);
-    cudaError_t e = sort_keys(vb.new_keys, sizeof(K), 3 * g.kb, nullptr, &ctl->n_new, ss, &ctl->status,
-                              ls.sort_ctas, st);
+    const K* sorted = nk;
+    cudaError_t e;
+    if constexpr (sizeof(K) == 4) {
+        // 30-bit keys: set-up and digit counts ride on the set-up and splat
+        // kernels; the sort is its three digit passes.  The splat takes at
+        // most one CTA per kEmitThreads pixels (a CTA without pixels would
+        // only launch and leave).
+        const size_t pix_ctas = ((size_t)cam.width * cam.height + kEmitThreads - 1) / kEmitThreads;
+        const int splat_ctas = (int)std::min<size_t>((size_t)ls.splat_ctas, std::max<size_t>(pix_ctas, 1));
+        sort_limits(&ss);
+        k_frame_setup_sort<<<1, 256, 0, st>>>(ctl, ss);
+        if (depth_u16)
+            k_splat_emit_hist<true><<<splat_ctas, kEmitThreads, 0, st>>>(ctl, g, depth_dev, vb.bitmap, nk, new_cap,
+                                                                          fc, ss.hist);
+        else
+            k_splat_emit_hist<false><<<splat_ctas, kEmitThreads, 0, st>>>(ctl, g, depth_dev, vb.bitmap, nk, new_cap,
+                                                                           fc, ss.hist);
+        if (events) cudaEventRecord(events[1], st);
+        e = sort_frame_keys(nk, &ctl->n_new, ss, &ctl->status, ls.sort_ctas, st, &sorted);
+    } else {
+        k_frame_setup<<<1, 32, 0, st>>>(ctl);
+        if (depth_u16)
+            k_splat_emit<true, K><<<ls.splat_ctas, kEmitThreads, 0, st>>>(ctl, g, depth_dev, vb.bitmap, nk, new_cap,
+                                                                          fc);
+        else
+            k_splat_emit<false, K><<<ls.splat_ctas, kEmitThreads, 0, st>>>(ctl, g, depth_dev, vb.bitmap, nk,
+                                                                           new_cap, fc);
+        if (events) cudaEventRecord(events[1], st);
+        e = sort_keys(vb.new_keys, sizeof(K), 3 * g.kb, nullptr, &ctl->n_new, ss, &ctl->status, ls.sort_ctas, st);
+    }
     if (e != cudaSuccess) return e;
     if (events) cudaEventRecord(events[2], st);
-    MergeInputs<K> in{nk, nullptr, nullptr, &ctl->n_new, true};
+    MergeInputs<K> in{sorted, nullptr, nullptr, &ctl->n_new, true};
     e = merge_enqueue<K>(ctl, g, vb, in, depth_dev, depth_u16, fc, ls, st, events ? events[3] : nullptr);
     if (events) cudaEventRecord(events[4], st);
     return e;

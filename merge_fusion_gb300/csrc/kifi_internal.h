@@ -14,11 +14,21 @@ namespace kifi {
 // ------------------------------------------------------------ radix sort
 // up to 8 digit passes: keys of up to 64 bits
 constexpr int kSortMaxPasses = 8;
+// A frame's 30-bit new keys sort in three 10-bit digit passes.  The frame's
+// set-up kernel zeroes their histograms and tile counters, and the splat
+// counts the digits of every key it stores, so the sort itself is the three
+// passes (its result lands in SortScratch::alt_keys).
+constexpr int kFrameDigitBits = 10;
+constexpr int kFrameRadix = 1 << kFrameDigitBits;
+constexpr int kFrameSortPasses = 3;
+// counters of the largest digit set: 3 x 1024 (frame keys) or 8 x 256
+constexpr int kSortHistWords = kFrameSortPasses * kFrameRadix;
+static_assert(kSortHistWords >= kSortMaxPasses * 256, "histogram sized for both digit sets");
 struct SortScratch {
-    unsigned int* hist = nullptr;           // [passes][256] digit counts
+    unsigned int* hist = nullptr;           // [passes][radix] digit counts
     unsigned int* tile_counter = nullptr;   // [passes] dynamic tile ids per pass
     unsigned long long* epoch = nullptr;    // look-back generation tag
-    unsigned long long* lookback = nullptr; // [passes][max_tiles][256]
+    unsigned long long* lookback = nullptr; // [passes][max_tiles][radix]
     void* alt_keys = nullptr;               // ping-pong buffers, max_n (+pad), 8 bytes per key
     uint32_t* alt_vals = nullptr;
     unsigned int* status = nullptr;         // where timeouts are reported
@@ -42,6 +52,11 @@ cudaError_t sort_u32(uint32_t* keys, uint32_t* vals, const unsigned int* n_dev, 
 // even count so the result lands back in `keys`
 cudaError_t sort_keys(void* keys, int key_bytes, int key_bits, uint32_t* vals, const unsigned int* n_dev,
                       SortScratch& s, unsigned int* status, int grid_ctas, cudaStream_t st);
+// the frame path's three 10-bit passes over 30-bit keys whose histograms and
+// pass counters are already set (see kFrameDigitBits); *sorted receives the
+// buffer holding the result
+cudaError_t sort_frame_keys(uint32_t* keys, const unsigned int* n_dev, SortScratch& s, unsigned int* status,
+                            int grid_ctas, cudaStream_t st, const uint32_t** sorted);
 
 // ------------------------------------------------------------- integrate
 struct VolumeBuffers {

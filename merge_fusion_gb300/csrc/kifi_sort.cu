@@ -7,6 +7,10 @@
 // behind the kernel that produces the keys without a host round trip and
 // captured in a CUDA graph.
 //
+// A frame's 30-bit new keys take three 10-bit digit passes instead: the
+// frame's set-up kernel prepares them and the splat counts their digits
+// (kifi_integrate.cu), so that sort is three launches of k_sort_pass_frame.
+//
 // Structure (one "onesweep" kernel per digit pass):
 //  * k_sort_prepare: zero the digit histograms and the dynamic tile
 //    counters, bump the look-back generation tag.
@@ -97,48 +101,69 @@ __device__ __forceinline__ void st_volatile_u64(unsigned long long* p, unsigned 
     asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
-template <bool kWithValues, typename K>
+// One digit pass of kBits bits (radix R = 2^kBits, R / kThreads digits per
+// thread in the scans and the look-back: one for 8-bit digits, four for the
+// frame keys' 10-bit digits).
+template <bool kWithValues, typename K, int kBits>
 __device__ __forceinline__ void sort_pass_body(const K* __restrict__ keys_in, K* __restrict__ keys_out,
                                                const uint32_t* __restrict__ vals_in, uint32_t* __restrict__ vals_out,
                                                const unsigned int* __restrict__ n_ptr, const SortScratch& s,
-                                               int pass) {
-    __shared__ unsigned int warp_hist[kWarps][kRadix + 1];  // last column: out-of-range keys
-    __shared__ unsigned int digit_base[kRadix];
-    __shared__ unsigned int pass_offset[kRadix];
+                                               int pass, unsigned int blk) {
+    constexpr int R = 1 << kBits;
+    constexpr int D = R / kThreads;
+    constexpr int kLA = D == 1 ? kLookAhead : kLookAhead / 2;  // look-back words per digit and round
+    static_assert(D >= 1 && D * kThreads == R, "whole digits per thread");
+    __shared__ unsigned int warp_hist[kWarps][R + 1];  // last column: out-of-range keys
+    __shared__ unsigned int digit_base[R];
+    __shared__ unsigned int pass_offset[R];
+    __shared__ unsigned int wsum[kWarps];
     __shared__ unsigned int tile_id;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned int n = (unsigned int)min((size_t)*n_ptr, s.max_n);
     const unsigned int n_tiles = (n + kTile - 1) / kTile;
-    const int shift = pass * 8;
+    // Grids are sized before the key count exists.  CTAs beyond the tile
+    // count leave before the tile counter: n_tiles CTAs (or the whole grid,
+    // when smaller) take every tile, and the counter sees only them.
+    if (blk >= n_tiles) return;
+    const int shift = pass * kBits;
     const unsigned long long gen = (*s.epoch & 0xffffffffull) << 32;
-    unsigned long long* lb = s.lookback + (size_t)pass * s.max_tiles * kRadix;
+    unsigned long long* lb = s.lookback + (size_t)pass * s.max_tiles * R;
 
     bool have_offsets = false;
     for (;;) {
         __syncthreads();
         if (threadIdx.x == 0) tile_id = atomicAdd(&s.tile_counter[pass], 1u);
-        for (int i = threadIdx.x; i < kWarps * (kRadix + 1); i += kThreads)
-            (&warp_hist[0][0])[i] = 0u;
         __syncthreads();
         const unsigned int tile = tile_id;
         if (tile >= n_tiles) break;  // (CTAs without a tile leave before any other work)
+        for (int i = threadIdx.x; i < kWarps * (R + 1); i += kThreads) (&warp_hist[0][0])[i] = 0u;
         if (!have_offsets) {
-            // exclusive scan of this pass's global digit histogram (256 entries)
-            const unsigned int c = s.hist[pass * kRadix + threadIdx.x];
-            unsigned int x = c;
+            // exclusive scan of this pass's global digit histogram: thread t
+            // holds digits t*D .. t*D + D - 1
+            unsigned int c[D], sum = 0;
+#pragma unroll
+            for (int q = 0; q < D; ++q) {
+                c[q] = s.hist[pass * R + threadIdx.x * D + q];
+                sum += c[q];
+            }
+            unsigned int x = sum;
             for (int o = 1; o < 32; o <<= 1) {
                 const unsigned int y = __shfl_up_sync(0xffffffffu, x, o);
                 if (lane >= o) x += y;
             }
-            __shared__ unsigned int wsum[kWarps];
             if (lane == 31) wsum[warp] = x;
             __syncthreads();
-            unsigned int before = 0;
-            for (int w = 0; w < warp; ++w) before += wsum[w];
-            pass_offset[threadIdx.x] = before + x - c;
+            unsigned int run = x - sum;
+            for (int w = 0; w < warp; ++w) run += wsum[w];
+#pragma unroll
+            for (int q = 0; q < D; ++q) {
+                pass_offset[threadIdx.x * D + q] = run;
+                run += c[q];
+            }
             have_offsets = true;  // read after the next barrier, before the scatter
         }
+        __syncthreads();  // warp_hist cleared
 
         const unsigned int base = tile * kTile + warp * (32 * kKeysPerThread);
         K k[kKeysPerThread];
@@ -151,7 +176,7 @@ __device__ __forceinline__ void sort_pass_body(const K* __restrict__ keys_in, K*
             bool ok = i < n;
             k[j] = ok ? keys_in[i] : (K)0;
             if (kWithValues) v[j] = ok ? vals_in[i] : 0u;
-            dig[j] = ok ? (int)((unsigned int)(k[j] >> shift) & 0xffu) : kRadix;
+            dig[j] = ok ? (int)((unsigned int)(k[j] >> shift) & (unsigned int)(R - 1)) : R;
         }
         // stable warp-local ranks: lanes with equal digits, in (j, lane) order
 #pragma unroll
@@ -164,62 +189,97 @@ __device__ __forceinline__ void sort_pass_body(const K* __restrict__ keys_in, K*
             __syncwarp();
         }
         __syncthreads();
-        // per digit: counts across warps -> exclusive prefix over warps
-        const int d = threadIdx.x;
-        unsigned int tile_count = 0;
-        for (int w = 0; w < kWarps; ++w) {
-            unsigned int c = warp_hist[w][d];
-            warp_hist[w][d] = tile_count;
-            tile_count += c;
+        // per digit d = threadIdx.x + q * kThreads: counts across warps ->
+        // exclusive prefix over warps
+        unsigned int tile_count[D];
+#pragma unroll
+        for (int q = 0; q < D; ++q) {
+            const int d = threadIdx.x + q * kThreads;
+            unsigned int tc = 0;
+            for (int w = 0; w < kWarps; ++w) {
+                unsigned int c = warp_hist[w][d];
+                warp_hist[w][d] = tc;
+                tc += c;
+            }
+            tile_count[q] = tc;
         }
-        // decoupled look-back for digit d
-        unsigned long long* my = lb + (size_t)tile * kRadix + d;
+        // decoupled look-back for the thread's digits
         if (tile == 0) {
-            st_volatile_u64(my, gen | kFlagInclusive | tile_count);
-            digit_base[d] = pass_offset[d];
+#pragma unroll
+            for (int q = 0; q < D; ++q) {
+                const int d = threadIdx.x + q * kThreads;
+                st_volatile_u64(lb + d, gen | kFlagInclusive | tile_count[q]);
+                digit_base[d] = pass_offset[d];
+            }
         } else {
-            st_volatile_u64(my, gen | kFlagAggregate | tile_count);
-            // Walk back kLookAhead predecessor words per round: the loads of a
-            // round are independent, so a chain of aggregate-only tiles costs
-            // one memory latency per kLookAhead tiles, not one per tile.
-            unsigned int excl = 0;
-            int t = (int)tile - 1;
+#pragma unroll
+            for (int q = 0; q < D; ++q)
+                st_volatile_u64(lb + (size_t)tile * R + threadIdx.x + q * kThreads,
+                                gen | kFlagAggregate | tile_count[q]);
+            // Walk back kLA predecessor words per digit and round: the loads of
+            // a round are independent, so a chain of aggregate-only tiles
+            // costs one memory latency per kLA tiles, not one per tile.
+            unsigned int excl[D];
+            int t[D];
+            unsigned int pending = 0;
+#pragma unroll
+            for (int q = 0; q < D; ++q) {
+                excl[q] = 0;
+                t[q] = (int)tile - 1;
+                pending |= 1u << q;
+            }
             unsigned long long spins = 0;
-            while (t >= 0) {
-                unsigned long long w[kLookAhead];
+            while (pending) {
+                unsigned long long w[D][kLA];
 #pragma unroll
-                for (int q = 0; q < kLookAhead; ++q)
-                    w[q] = t - q >= 0 ? ld_volatile_u64(lb + (size_t)(t - q) * kRadix + d) : 0ull;
-                // consume the round's words in order, up to the first inclusive one
-                // or the first one not yet published
-                int used = 0;
-                bool done = false, stalled = false;
+                for (int q = 0; q < D; ++q) {
+                    const int d = threadIdx.x + q * kThreads;
 #pragma unroll
-                for (int q = 0; q < kLookAhead; ++q) {
-                    if (done || stalled || t - q < 0) continue;
-                    const unsigned long long x = w[q];
-                    if ((x & 0xffffffff00000000ull) != gen || (x & (3ull << 30)) == 0) {
-                        stalled = true;
-                        continue;
-                    }
-                    excl += (unsigned int)(x & kCountMask);
-                    ++used;
-                    done = (x & kFlagInclusive) != 0;
+                    for (int i = 0; i < kLA; ++i)
+                        w[q][i] = ((pending >> q) & 1u) && t[q] - i >= 0
+                                      ? ld_volatile_u64(lb + (size_t)(t[q] - i) * R + d)
+                                      : 0ull;
                 }
-                t -= used;
-                if (done) break;
-                if (stalled && ++spins > s.spin_limit) {
+                // consume each digit's words in order, up to the first inclusive
+                // one or the first one not yet published
+                bool stalled_any = false;
+#pragma unroll
+                for (int q = 0; q < D; ++q) {
+                    if (!((pending >> q) & 1u)) continue;
+                    int used = 0;
+                    bool done = false, stalled = false;
+#pragma unroll
+                    for (int i = 0; i < kLA; ++i) {
+                        if (done || stalled || t[q] - i < 0) continue;
+                        const unsigned long long x = w[q][i];
+                        if ((x & 0xffffffff00000000ull) != gen || (x & (3ull << 30)) == 0) {
+                            stalled = true;
+                            continue;
+                        }
+                        excl[q] += (unsigned int)(x & kCountMask);
+                        ++used;
+                        done = (x & kFlagInclusive) != 0;
+                    }
+                    t[q] -= used;
+                    if (done || t[q] < 0) pending &= ~(1u << q);
+                    else if (stalled) stalled_any = true;
+                }
+                if (stalled_any && ++spins > s.spin_limit) {
                     atomicOr(s.status, KIFI_DEV_ERR_TIMEOUT);
                     break;
                 }
             }
-            st_volatile_u64(my, gen | kFlagInclusive | ((excl + tile_count) & kCountMask));
-            digit_base[d] = pass_offset[d] + excl;
+#pragma unroll
+            for (int q = 0; q < D; ++q) {
+                const int d = threadIdx.x + q * kThreads;
+                st_volatile_u64(lb + (size_t)tile * R + d, gen | kFlagInclusive | ((excl[q] + tile_count[q]) & kCountMask));
+                digit_base[d] = pass_offset[d] + excl[q];
+            }
         }
         __syncthreads();
 #pragma unroll
         for (int j = 0; j < kKeysPerThread; ++j) {
-            if (dig[j] == kRadix) continue;
+            if (dig[j] == R) continue;
             unsigned int pos = digit_base[dig[j]] + warp_hist[warp][dig[j]] + rank[j];
             if (pos >= n) {  // only reachable after a timed-out look-back
                 atomicOr(s.status, KIFI_DEV_ERR_TIMEOUT);
@@ -238,7 +298,16 @@ __global__ void __launch_bounds__(kThreads) k_sort_pass(const K* __restrict__ ke
                                                         uint32_t* __restrict__ vals_out,
                                                         const unsigned int* __restrict__ n_ptr,
                                                         SortScratch s, int pass) {
-    sort_pass_body<kWithValues, K>(keys_in, keys_out, vals_in, vals_out, n_ptr, s, pass);
+    sort_pass_body<kWithValues, K, 8>(keys_in, keys_out, vals_in, vals_out, n_ptr, s, pass, blockIdx.x);
+}
+
+// a pass of the frame keys' 10-bit digits
+__global__ void __launch_bounds__(kThreads) k_sort_pass_frame(const uint32_t* __restrict__ keys_in,
+                                                              uint32_t* __restrict__ keys_out,
+                                                              const unsigned int* __restrict__ n_ptr,
+                                                              SortScratch s, int pass) {
+    sort_pass_body<false, uint32_t, kFrameDigitBits>(keys_in, keys_out, nullptr, nullptr, n_ptr, s, pass,
+                                                     blockIdx.x);
 }
 
 // ---- batched: every volume of a batch sorts its frame's new keys, one
@@ -260,12 +329,13 @@ __global__ void __launch_bounds__(kThreads) k_sort_histogram_batch(const FuseJob
 template <typename K>
 __global__ void __launch_bounds__(kThreads) k_sort_pass_batch(const FuseJob* __restrict__ jobs, BlockMap m,
                                                               int pass) {
-    const FuseJob& j = jobs[block_owner(m, blockIdx.x)];
+    const int v = block_owner(m, blockIdx.x);
+    const FuseJob& j = jobs[v];
     K* keys = (K*)j.vb.new_keys;
     K* alt = (K*)j.ss.alt_keys;
     // passes alternate between the new-key buffer and the sort's spare one
-    sort_pass_body<false, K>(pass & 1 ? alt : keys, pass & 1 ? keys : alt, nullptr, nullptr, &j.ctl->n_new, j.ss,
-                             pass);
+    sort_pass_body<false, K, 8>(pass & 1 ? alt : keys, pass & 1 ? keys : alt, nullptr, nullptr, &j.ctl->n_new,
+                                j.ss, pass, blockIdx.x - m.first[v]);
 }
 
 // process-wide look-back limits (kifi_sort_set_fault_injection)
@@ -281,11 +351,11 @@ cudaError_t sort_scratch_alloc(SortScratch* s, size_t max_n, cudaStream_t st) {
     s->max_tiles = sort_max_tiles(max_n);
     s->max_n = max_n;
     cudaError_t e;
-    if ((e = cudaMalloc(&s->hist, kSortMaxPasses * kRadix * sizeof(unsigned int) + 64))) return e;
+    if ((e = cudaMalloc(&s->hist, kSortHistWords * sizeof(unsigned int) + 64))) return e;
     if ((e = cudaMalloc(&s->tile_counter, 8 * sizeof(unsigned int)))) return e;
     if ((e = cudaMalloc(&s->epoch, sizeof(unsigned long long)))) return e;
     if ((e = cudaMemsetAsync(s->epoch, 0, sizeof(unsigned long long), st))) return e;
-    size_t lb = kSortMaxPasses * s->max_tiles * kRadix * sizeof(unsigned long long);
+    size_t lb = (size_t)kSortHistWords * s->max_tiles * sizeof(unsigned long long);
     if ((e = cudaMalloc(&s->lookback, lb))) return e;
     if ((e = cudaMemsetAsync(s->lookback, 0, lb, st))) return e;
     if ((e = cudaMalloc(&s->alt_keys, (max_n + 64) * sizeof(uint64_t)))) return e;
@@ -331,6 +401,18 @@ static cudaError_t sort_t(K* keys, int passes, uint32_t* vals, const unsigned in
 void sort_limits(SortScratch* s) {
     s->spin_limit = g_spin_limit.load();
     s->first_tile = g_first_tile.load();
+}
+
+// keys -> alt -> keys -> alt: the sorted keys end in s.alt_keys
+cudaError_t sort_frame_keys(uint32_t* keys, const unsigned int* n_dev, SortScratch& s, unsigned int* status,
+                            int grid_ctas, cudaStream_t st, const uint32_t** sorted) {
+    s.status = status;
+    uint32_t* alt = (uint32_t*)s.alt_keys;
+    for (int pass = 0; pass < kFrameSortPasses; ++pass)
+        k_sort_pass_frame<<<grid_ctas, kThreads, 0, st>>>(pass & 1 ? alt : keys, pass & 1 ? keys : alt, n_dev, s,
+                                                          pass);
+    *sorted = kFrameSortPasses & 1 ? alt : keys;
+    return cudaGetLastError();
 }
 
 template <typename K>
