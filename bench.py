@@ -519,16 +519,21 @@ def run_gpu(args, rank, world, local):
     e2e_s = max_over_ranks(e2e_s, world)
 
     # ---- isolated kernels, after the timed regions
-    # fusion-only frames (the last rendered frame again, on the pipeline's volume), tracking idle
+    # fusion-only frames (the last rendered frame again, on the pipeline's volume), tracking idle, with
+    # the volume's launch shape for fusion alone (persistent grids, the merge build with 4 CTAs per SM);
+    # one untimed frame first loads that shape's kernels
     ISO = 5
     iso_stage = np.zeros(4)
     iso_n = C.c_int()
+    check(lib.kifi_volume_set_launch_mode(vol, 0))
     check(lib.kifi_volume_set_profiling(vol, 1))
-    check(lib.kifi_volume_stage_times(vol, ptr(iso_stage), C.byref(iso_n)))  # reset
-    for _ in range(ISO):
+    for k in range(ISO + 1):
+        if k == 1:
+            check(lib.kifi_volume_stage_times(vol, ptr(iso_stage), C.byref(iso_n)))  # reset
         check(lib.kifi_integrate_device(vol, C.c_void_p(frames[n_frames - 1].data_ptr()), 1, C.byref(cam),
                                         ptr(w2e[n_frames - 1])), "isolated frame")
     check(lib.kifi_volume_stage_times(vol, ptr(iso_stage), C.byref(iso_n)))
+    check(lib.kifi_volume_set_launch_mode(vol, 1))
     # a mesh of the whole volume alone (the first call sizes the volume's mesh buffers)
     iso_mesh = np.zeros(5)
     iso_meshes = C.c_int()

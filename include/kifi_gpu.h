@@ -200,6 +200,15 @@ KIFI_API kifi_status kifi_volume_mesh_times(kifi_volume* v, double* out_ms, int*
  * emission, total} means in milliseconds. */
 KIFI_API kifi_status kifi_volume_mesh_stage_times(kifi_volume* v, double out_ms[5], int* meshes);
 
+/* No counterpart in the reference.  The volume's launch shape: beside
+ * tracking (beside_tracking != 0; what a pipeline gives its volume) the
+ * fusion kernels run as short-lived CTAs and the merge/update as its build
+ * that holds fewer SM resources, so that ICP steps find free SMs; alone
+ * (0, the default) as persistent CTAs and the merge/update build with more
+ * CTAs per SM.  Results are identical either way.  Resets any autotuned
+ * CTA counts. */
+KIFI_API kifi_status kifi_volume_set_launch_mode(kifi_volume* vol, int beside_tracking);
+
 /* No counterpart in the reference.  Picks the persistent CTA counts of the
  * volume's splat+emit, sort and merge/update kernels by timing them on one
  * frame (device memory) integrated from a snapshot of the volume, which is

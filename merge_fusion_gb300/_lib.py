@@ -125,6 +125,7 @@ SIGNATURES = {
     "kifi_mesh_device": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_size_t),
                                    C.POINTER(C.c_size_t), C.c_void_p, C.c_void_p]),
     "kifi_volume_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
+    "kifi_volume_set_launch_mode": (C.c_int, [C.c_void_p, C.c_int]),
     "kifi_volume_stage_times": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int)]),
     "kifi_volume_frame_log": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
                                         C.POINTER(C.c_int)]),

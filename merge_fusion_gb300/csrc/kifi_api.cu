@@ -32,6 +32,7 @@ void tracking_launch_shape(LaunchShape* ls) {
     ls->splat_ctas = ls->sms * 16;
     ls->sort_ctas = ls->sms * 16;
     ls->merge_ctas = ls->sms * 32;
+    ls->beside_tracking = true;
 }
 
 kifi_status launch_shape(int device, LaunchShape* ls) {
@@ -41,6 +42,7 @@ kifi_status launch_shape(int device, LaunchShape* ls) {
     ls->sort_ctas = sms * 4;
     ls->merge_ctas = sms * merge_blocks_per_sm();
     ls->splat_ctas = sms * 4;
+    ls->beside_tracking = false;
     return KIFI_OK;
 }
 
@@ -562,6 +564,15 @@ kifi_status kifi_integrate_device(kifi_volume* v, const void* depth_dev, int dep
     kifi_status s = frame_prologue(v, cam);
     if (s) return s;
     return kifi_volume_enqueue_frame(v, depth_dev, depth_is_u16 != 0, cam, world_to_eye);
+}
+
+kifi_status kifi_volume_set_launch_mode(kifi_volume* v, int beside_tracking) {
+    if (!v) return fail(KIFI_ERR_INVALID_ARGUMENT, "null volume");
+    KIFI_CUDA(cudaSetDevice(v->device));
+    kifi_status s = launch_shape(v->device, &v->ls);
+    if (s) return s;
+    if (beside_tracking) tracking_launch_shape(&v->ls);
+    return KIFI_OK;
 }
 
 kifi_status kifi_volume_set_profiling(kifi_volume* v, int on) {

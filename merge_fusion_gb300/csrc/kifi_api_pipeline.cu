@@ -453,7 +453,6 @@ kifi_status kifi_pipeline_create(const kifi_pipeline_desc* d, kifi_pipeline** ou
     }
     kifi_status s = kifi_volume_create(&vd, &p->vol);
     if (!s && d->icp_iterations > 0 && !p->closed) {  // closed loop: fusion never runs beside tracking
-        p->vol->tracking_grids = true;
         tracking_launch_shape(&p->vol->ls);
     }
     if (!s) s = kifi_icp_create(d->device, nullptr, &p->icp);

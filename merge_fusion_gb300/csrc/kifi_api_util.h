@@ -50,10 +50,10 @@ struct kifi_volume {
     kifi::VolumeBuffers vb{};
     kifi::SortScratch ss{};
     kifi::MeshScratch ms{};
+    // ls.beside_tracking: fusion beside a tracking stream, grids of
+    // short-lived CTAs (see tracking_launch_shape), also the only shapes the
+    // autotuner tries
     kifi::LaunchShape ls{};
-    // fusion beside a tracking stream: grids of short-lived CTAs (see
-    // tracking_launch_shape), also the only shapes the autotuner tries
-    bool tracking_grids = false;
     void* depth_dev = nullptr;
     size_t depth_dev_bytes = 0;
     void* depth_pinned = nullptr;

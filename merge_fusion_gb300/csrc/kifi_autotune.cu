@@ -97,13 +97,16 @@ extern "C" kifi_status kifi_volume_autotune(kifi_volume* v, const void* depth_de
     if (!v || !depth_dev || !camera_ok(cam) || !world_to_eye)
         return fail(KIFI_ERR_INVALID_ARGUMENT, "autotune: bad argument");
     KIFI_CUDA(cudaSetDevice(v->device));
-    const std::string key = cache_key(v->device, v->g.res, 8 * v->vb.key_bytes, v->tracking_grids, cam->width, cam->height);
+    const std::string key =
+        cache_key(v->device, v->g.res, 8 * v->vb.key_bytes, v->ls.beside_tracking, cam->width, cam->height);
     {
         std::lock_guard<std::mutex> lock(g_mu);
         load_file();
         auto it = g_cache.find(key);
         if (!force && it != g_cache.end() && it->second.sms == v->ls.sms) {
+            const bool beside = v->ls.beside_tracking;  // part of the key, not of the cached counts
             v->ls = it->second;
+            v->ls.beside_tracking = beside;
             if (out_ctas) {
                 out_ctas[0] = v->ls.splat_ctas;
                 out_ctas[1] = v->ls.sort_ctas;
@@ -170,11 +173,11 @@ extern "C" kifi_status kifi_volume_autotune(kifi_volume* v, const void* depth_de
         // longer-lived CTAs win, but in the pipeline such CTAs hold SMs the
         // higher-priority tracking steps wait for (measured: 1846 against
         // 1948 frames/s with 8/2/16 x the SM count for splat/sort/merge).
-        const bool tr = v->tracking_grids;
+        const bool tr = v->ls.beside_tracking;
         const std::vector<int> splat_m = tr ? std::vector<int>{16, 32} : std::vector<int>{1, 2, 4, 8};
         // a sort pass's CTAs leave as soon as the tiles run out, so small grids are candidates too
         const std::vector<int> sort_m = tr ? std::vector<int>{16, 32} : std::vector<int>{1, 2, 4, 8};
-        const std::vector<int> merge_m = tr ? std::vector<int>{32, 64} : std::vector<int>{1, 2};
+        const std::vector<int> merge_m = tr ? std::vector<int>{32, 64} : std::vector<int>{1, 2, 8};
         for (int m : splat_m) {  // splat + emit (stage 0)
             LaunchShape c = best;
             c.splat_ctas = m * sms;

@@ -842,12 +842,25 @@ __device__ __forceinline__ void merge_update_body(DeviceCtl* __restrict__ ctl, c
     }
 }
 
+// Two builds of the same merge: beside tracking, 76 registers and 3 CTAs
+// per SM, so that fewer SMs are held when the next ICP step starts; alone,
+// capped at 64 registers for a fourth CTA per SM (a few spilled words, in
+// L1).  Measured at ~21 M voxels, 10-frame runs: alone 122 -> 113 us; in the
+// pipeline the capped build gave 2000 against 2036 frames/s.
 template <bool kU16, typename K>
 __global__ void __launch_bounds__(kMergeThreads) k_merge_update(DeviceCtl* __restrict__ ctl, Geom g,
                                                                 VolumeBuffers vb, MergeInputs<K> in,
                                                                 const void* __restrict__ depth,
                                                                 const unsigned long long* __restrict__ splits,
                                                                 const FrameConst fc) {
+    merge_update_body<kU16, K>(ctl, g, vb, in, depth, splits, fc, blockIdx.x, gridDim.x);
+}
+template <bool kU16, typename K>
+__global__ void __launch_bounds__(kMergeThreads, 4) k_merge_update_alone(DeviceCtl* __restrict__ ctl, Geom g,
+                                                                         VolumeBuffers vb, MergeInputs<K> in,
+                                                                         const void* __restrict__ depth,
+                                                                         const unsigned long long* __restrict__ splits,
+                                                                         const FrameConst fc) {
     merge_update_body<kU16, K>(ctl, g, vb, in, depth, splits, fc, blockIdx.x, gridDim.x);
 }
 
@@ -944,7 +957,7 @@ __global__ void k_reset_new(DeviceCtl* ctl) {
 
 int merge_blocks_per_sm() {
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_merge_update<true, uint32_t>, kMergeThreads, 0) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_merge_update_alone<true, uint32_t>, kMergeThreads, 0) !=
             cudaSuccess ||
         n < 1)
         n = 4;
@@ -969,10 +982,19 @@ static cudaError_t merge_enqueue(DeviceCtl* ctl, const Geom& g, VolumeBuffers& v
     const unsigned int mt = max_tiles_of<K>(vb);
     k_merge_partition<K><<<(mt + 255) / 256, 256, 0, st>>>(ctl, g, vb, in, vb.splits, mt);
     if (after_partition) cudaEventRecord(after_partition, st);
-    if (u16)
-        k_merge_update<true, K><<<ls.merge_ctas, kMergeThreads, 0, st>>>(ctl, g, vb, in, depth, vb.splits, fc);
-    else
-        k_merge_update<false, K><<<ls.merge_ctas, kMergeThreads, 0, st>>>(ctl, g, vb, in, depth, vb.splits, fc);
+    if (ls.beside_tracking) {
+        if (u16)
+            k_merge_update<true, K><<<ls.merge_ctas, kMergeThreads, 0, st>>>(ctl, g, vb, in, depth, vb.splits, fc);
+        else
+            k_merge_update<false, K><<<ls.merge_ctas, kMergeThreads, 0, st>>>(ctl, g, vb, in, depth, vb.splits, fc);
+    } else {
+        if (u16)
+            k_merge_update_alone<true, K><<<ls.merge_ctas, kMergeThreads, 0, st>>>(ctl, g, vb, in, depth, vb.splits,
+                                                                                   fc);
+        else
+            k_merge_update_alone<false, K><<<ls.merge_ctas, kMergeThreads, 0, st>>>(ctl, g, vb, in, depth, vb.splits,
+                                                                                    fc);
+    }
     return cudaGetLastError();
 }
 

@@ -77,6 +77,11 @@ struct LaunchShape {
     int sort_ctas = 0;    // persistent CTAs of the sort passes
     int merge_ctas = 0;   // persistent CTAs of the merge/update kernel
     int splat_ctas = 0;
+    // beside tracking (a pipeline's volume): short-lived CTAs and the merge
+    // variant that leaves room on the SMs (3 CTAs of 256 threads per SM);
+    // alone: persistent CTAs and the merge variant capped at 64 registers
+    // (4 CTAs per SM)
+    bool beside_tracking = false;
 };
 
 // Enqueues one Integrator::Integrate on `st`.  depth_dev holds the frame

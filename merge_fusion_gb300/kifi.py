@@ -176,6 +176,11 @@ class Volume:
     def stream(self):
         return _lib.load().kifi_volume_stream(self._h)
 
+    def set_launch_mode(self, beside_tracking):
+        """Launch shape of the fusion kernels: beside a tracking stream (short-lived CTAs, the
+        merge build that holds fewer SM resources) or alone (the default).  Results are identical."""
+        check(_lib.load().kifi_volume_set_launch_mode(self._h, 1 if beside_tracking else 0), "set_launch_mode")
+
     def autotune(self, depth_dev_ptr, depth_is_u16, camera_params, world_to_eye, force=False):
         """Measures and sets the persistent CTA counts of the fusion kernels
         on one device frame (kifi_volume_autotune); the volume is unchanged.

@@ -1,5 +1,7 @@
 """kifi_volume_autotune: tuning leaves the volume untouched, every tuned
-launch shape gives bit-identical results, and choices are cached."""
+launch shape gives bit-identical results, and choices are cached.
+kifi_volume_set_launch_mode: both launch shapes (and merge builds) give
+bit-identical volumes."""
 import os
 
 import numpy as np
@@ -38,3 +40,21 @@ def test_autotune_is_invisible_and_cached(gpu, golden, tmp_path):
     # cached: the same choice without measuring, and written to the file
     assert b.autotune(d.data_ptr(), False, params, shifted) == shape
     assert cache.exists() and len(cache.read_text().split()) == 5
+
+
+def test_launch_modes_give_identical_volumes(gpu, golden):
+    from merge_fusion_gb300 import kifi
+    depth, view, cam = golden["depth"], golden["view"], golden["camera"]
+    params = cam_params(cam)
+    shifted = view.copy()
+    shifted[12] += np.float32(0.013)
+    vols = [kifi.Volume(256, 2.0, 0.02) for _ in range(2)]
+    vols[0].set_launch_mode(True)
+    vols[1].set_launch_mode(False)
+    for v in vols:
+        for w2e in (view, shifted, view):
+            kifi.Integrator().Integrate(v, depth, params, w2e)
+    ka, va = vols[0].export()
+    kb, vb = vols[1].export()
+    assert ka.size > 0
+    assert np.array_equal(ka, kb) and np.array_equal(va.view(np.uint32), vb.view(np.uint32))
