@@ -60,11 +60,12 @@ SEED = 0
 CAM = (W, H, F_PX, F_PX, W / 2.0, H / 2.0, 0.4, 4.0)
 WORKLOAD = ("room 4x3x4 m, 40 boxes + 20 spheres, 640x480 uint16 depth, res 1024 x 4 mm, trunc 2 cm, "
             "ICP 15 it/frame, mesh every 10")
-# kernels launched per frame: frame set-up, splat+emit, the sort (prepare,
-# histogram, 4 digit passes), merge partition, merge+update; tracking: ICP
-# begin, one step per iteration, the next target's back-projection; per mesh:
-# snapshot, row directory, classification, two scan kernels, two emission passes
-LAUNCHES_FUSION, LAUNCHES_TRACKING, LAUNCHES_MESH = 10, ICP_ITERS + 2, 7
+# kernels launched per frame: frame set-up (with the sort's set-up), splat+emit
+# (with the digit counts), three digit passes, merge partition, merge+update;
+# tracking: ICP begin, one step per iteration, the next target's
+# back-projection; per mesh: snapshot, row directory, tile ranges, status
+# bytes, classification, tile-sum scan, two emission passes
+LAUNCHES_FUSION, LAUNCHES_TRACKING, LAUNCHES_MESH = 7, ICP_ITERS + 2, 8
 # bytes the host reads back per tracked frame: the head of the ICP state
 # (float and float-float pose, counters, 64 iteration records of 20 bytes)
 ICP_HEAD_BYTES = 192 + 64 * 20

@@ -20,9 +20,11 @@
 // Fusion runs on the volume's stream and tracking on the ICP context's
 // stream, so the HBM-bound merge/update and the shared-memory-bound ICP
 // window search overlap on the GPU.  Host frames are uploaded on a third
-// stream into two device slots; events order the shared inputs: both
+// stream into kFrameSlots device slots; events order the shared inputs: both
 // streams wait for a frame's upload, and a slot is only overwritten after
-// tracking and fusion have finished reading it.
+// tracking and fusion have finished reading it.  With four slots a frame's
+// upload waits for the fusion of the frame four back, so fusion may lag
+// tracking by up to three frames before it holds tracking up.
 //
 // With graphs on (kifi_pipeline_set_graphs), a frame -- the upload of a host
 // frame, the fusion launches and the tracking launches on both streams -- is
@@ -72,6 +74,8 @@ __global__ void k_upload(const uint4* __restrict__ src, uint4* __restrict__ dst,
 }
 }  // namespace
 
+constexpr int kFrameSlots = 4;  // device slots of host-fed frames
+
 struct kifi_pipeline {
     kifi_pipeline_desc desc{};
     kifi_volume* vol = nullptr;
@@ -79,11 +83,11 @@ struct kifi_pipeline {
     cudaStream_t vs = nullptr, is = nullptr;
     cudaStream_t us = nullptr;  // uploads of host-fed frames
     cudaStream_t fs = nullptr;  // the volume's (fusion) stream, when the pipeline made it
-    void* slot[2] = {nullptr, nullptr};  // host-fed frames (uint16 or float)
+    void* slot[kFrameSlots] = {};  // host-fed frames (uint16 or float)
     size_t slot_bytes = 0;
-    cudaEvent_t uploaded[2] = {nullptr, nullptr};   // frame in slot k is on the device
-    cudaEvent_t released[2] = {nullptr, nullptr};   // tracking no longer reads slot k
-    cudaEvent_t slot_fused[2] = {nullptr, nullptr}; // fusion no longer reads slot k
+    cudaEvent_t uploaded[kFrameSlots] = {};    // frame in slot k is on the device
+    cudaEvent_t released[kFrameSlots] = {};    // tracking no longer reads slot k
+    cudaEvent_t slot_fused[kFrameSlots] = {};  // fusion no longer reads slot k
     cudaEvent_t fused = nullptr;
     long long frame = 0;
     float prev_e2w[16];
@@ -463,7 +467,7 @@ kifi_status kifi_pipeline_create(const kifi_pipeline_desc* d, kifi_pipeline** ou
     p->vs = (cudaStream_t)kifi_volume_stream(p->vol);
     p->is = (cudaStream_t)kifi_icp_stream(p->icp);
     cudaError_t e = cudaSuccess;
-    for (int k = 0; k < 2 && !e; ++k) {
+    for (int k = 0; k < kFrameSlots && !e; ++k) {
         e = cudaEventCreateWithFlags(&p->uploaded[k], cudaEventDisableTiming);
         if (!e) e = cudaEventCreateWithFlags(&p->released[k], cudaEventDisableTiming);
         if (!e) e = cudaEventRecord(p->released[k], p->is);
@@ -498,7 +502,7 @@ kifi_status kifi_pipeline_destroy(kifi_pipeline* p) {
     if (p->vs) cudaStreamSynchronize(p->vs);
     if (p->is) cudaStreamSynchronize(p->is);
     if (p->us) cudaStreamSynchronize(p->us);
-    for (int k = 0; k < 2; ++k) {
+    for (int k = 0; k < kFrameSlots; ++k) {
         cudaFree(p->slot[k]);
         if (p->uploaded[k]) cudaEventDestroy(p->uploaded[k]);
         if (p->released[k]) cudaEventDestroy(p->released[k]);
@@ -558,15 +562,15 @@ kifi_status kifi_pipeline_integrate(kifi_pipeline* p, const void* depth_host, in
     if (bytes > p->slot_bytes) {
         KIFI_CUDA(cudaStreamSynchronize(p->vs));
         KIFI_CUDA(cudaStreamSynchronize(p->is));
-        for (int k = 0; k < 2; ++k) {
+        for (int k = 0; k < kFrameSlots; ++k) {
             cudaFree(p->slot[k]);
             p->slot[k] = nullptr;
         }
         p->slot_bytes = 0;
-        for (int k = 0; k < 2; ++k) KIFI_CUDA(cudaMalloc(&p->slot[k], bytes));
+        for (int k = 0; k < kFrameSlots; ++k) KIFI_CUDA(cudaMalloc(&p->slot[k], bytes));
         p->slot_bytes = bytes;
     }
-    const int k = (int)(p->frame & 1);
+    const int k = (int)(p->frame % kFrameSlots);
     if (p->graphs) {
         KIFI_CUDA(cudaStreamWaitEvent(p->vs, p->released[k], 0));
         cudaPointerAttributes attr;
@@ -580,9 +584,9 @@ kifi_status kifi_pipeline_integrate(kifi_pipeline* p, const void* depth_host, in
             return kifi_pipeline_sync(p, out_eye_to_world);
         }
     }
-    // the upload stream: slot k is free once the frame two back is no longer
-    // read by tracking or fusion; it does not queue behind the previous
-    // frame's fusion, so tracking starts as soon as the frame is on the device
+    // the upload stream: slot k is free once the frame kFrameSlots back is no
+    // longer read by tracking or fusion; it does not queue behind the recent
+    // frames' fusion, so tracking starts as soon as the frame is on the device
     KIFI_CUDA(cudaStreamWaitEvent(p->us, p->released[k], 0));
     KIFI_CUDA(cudaStreamWaitEvent(p->us, p->slot_fused[k], 0));
     cudaPointerAttributes attr;
