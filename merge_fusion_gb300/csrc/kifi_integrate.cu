@@ -178,13 +178,22 @@ __device__ __forceinline__ void splat_emit_body(DeviceCtl* __restrict__ ctl, con
     const Codec<K> cd(g.kb);
     const int W = fc.width, H = fc.height;
     const size_t P = (size_t)W * H;
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     float e2w[16];
 #pragma unroll
     for (int i = 0; i < 16; ++i) e2w[i] = fc.eye_to_world.m[i];
+    // Per-frame counters are shared by every CTA: the excluded key's maximum
+    // and the new-key count take one global atomic per CTA (one per warp
+    // queued thousands of same-address atomics at one L2 slice).
+    constexpr int kEmitWarps = kEmitThreads / 32;
+    __shared__ unsigned long long s_ex;
+    __shared__ unsigned int s_wtot[kEmitWarps], s_wpre[kEmitWarps], s_base;
+    if (threadIdx.x == 0) s_ex = 0ull;
+    __syncthreads();
     const size_t stride = (size_t)nblk * kEmitThreads;
-    const size_t P_round = (P + 31) / 32 * 32;  // warp-uniform trip count
-    for (size_t i = (size_t)blk * kEmitThreads + threadIdx.x; i < P_round; i += stride) {
+    // CTA-uniform trip count: the append's barriers are reached by every thread
+    for (size_t c0 = (size_t)blk * kEmitThreads; c0 < P; c0 += stride) {
+        const size_t i = c0 + threadIdx.x;
         K key = 0;
         bool valid = false;
         if (i < P) {
@@ -195,7 +204,7 @@ __device__ __forceinline__ void splat_emit_body(DeviceCtl* __restrict__ ctl, con
         }
         // the excluded key of the dilation: max splat + pack(1,1,1)
         const K ex = warp_max(valid ? (K)(key + cd.pack(1, 1, 1)) : (K)0);
-        if (lane == 0 && ex) atomicMax(&ctl->excluded_key, (unsigned long long)ex);
+        if (lane == 0 && ex) atomicMax(&s_ex, (unsigned long long)ex);
         // neighbouring pixels often land in one voxel: one emitter per key
         unsigned int peers = __match_any_sync(0xffffffffu, valid ? key : ~(K)0);
         const bool emitter = valid && (lane == __ffs(peers) - 1);
@@ -233,7 +242,7 @@ __device__ __forceinline__ void splat_emit_body(DeviceCtl* __restrict__ ctl, con
             for (int o = 0; o < 8; ++o) got[o] = 0ull;
             wbase[0] = wbase[1] = wbase[2] = 0u;
         }
-        // warp-aggregated append: one atomic per warp
+        // append: each thread's keys follow the keys of the lanes before it
         unsigned int cnt = 0;
 #pragma unroll
         for (int o = 0; o < 8; ++o) cnt += __popcll(got[o]);
@@ -243,12 +252,22 @@ __device__ __forceinline__ void splat_emit_body(DeviceCtl* __restrict__ ctl, con
             const unsigned int y = __shfl_up_sync(0xffffffffu, incl, d);
             if (lane >= d) incl += y;
         }
-        const unsigned int total = __shfl_sync(0xffffffffu, incl, 31);
-        if (total) {
-            unsigned int base = 0;
-            if (lane == 31) base = atomicAdd(&ctl->n_new, total);
-            base = __shfl_sync(0xffffffffu, base, 31);
-            unsigned int at = base + incl - cnt;
+        // the CTA's keys take one range of the list: warp totals, their
+        // prefix and one atomic by thread 0
+        if (lane == 31) s_wtot[warp] = incl;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned int run = 0;
+#pragma unroll
+            for (int w = 0; w < kEmitWarps; ++w) {
+                s_wpre[w] = run;
+                run += s_wtot[w];
+            }
+            s_base = run ? atomicAdd(&ctl->n_new, run) : 0u;
+        }
+        __syncthreads();
+        if (cnt) {
+            unsigned int at = s_base + s_wpre[warp] + incl - cnt;
 #pragma unroll
             for (int o = 0; o < 8; ++o) {
                 uint64_t m = got[o];
@@ -274,8 +293,9 @@ __device__ __forceinline__ void splat_emit_body(DeviceCtl* __restrict__ ctl, con
             }
         }
     }
+    __syncthreads();
+    if (threadIdx.x == 0 && s_ex) atomicMax(&ctl->excluded_key, s_ex);
     if constexpr (kHist) {
-        __syncthreads();
         for (int i = threadIdx.x; i < kSortHistWords; i += blockDim.x) {
             const unsigned int c = s_hist[i];
             if (c) atomicAdd(&hist[i], c);
