@@ -738,10 +738,16 @@ def batched_scenes():
     """64 seeded scenes with uneven frame sizes ({320x240, 512x424, 640x480,
     1024x848}), voxel sizes ({2, 4, 8} mm, truncation 5 voxels) and
     trajectory lengths (50-300 frames) through one kifi_batch: each step is
-    one launch per stage for every scene that still has frames."""
+    one launch per stage for every scene that still has frames.  The same
+    frames again with the fusion as one persistent launch over a device work
+    queue (`persistent_queue`)."""
     from merge_fusion_gb300 import batched as bt
     specs = bt.scene_specs(64, 7)
-    res = bt.run_batch(specs, unique=40, icp_iters=ICP_ITERS)
+    rendered = bt.render_batch(specs, unique=40)
+    res = bt.run_batch(specs, unique=40, icp_iters=ICP_ITERS, rendered=rendered)
+    q = bt.run_batch(specs, unique=40, icp_iters=ICP_ITERS, persistent=True, queue_ctas_per_sm=1, rendered=rendered)
+    res["persistent_queue"] = {k: q[k] for k in ("mode", "frames", "seconds", "frames_per_s", "step_latency_ms_p50",
+                                                 "step_latency_ms_p99")}
     res["mix"] = {"sizes": {"%dx%d" % (w, h): sum(1 for s in specs if s["width"] == w) for w, h, _ in bt.SIZES},
                   "voxels_mm": {str(v): sum(1 for s in specs if s["voxel_mm"] == v) for v in bt.VOXELS_MM},
                   "trajectory_frames": [min(s["frames"] for s in specs), max(s["frames"] for s in specs)]}

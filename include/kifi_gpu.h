@@ -590,6 +590,14 @@ KIFI_API kifi_volume* kifi_batch_volume(kifi_batch* b, int scene);
 KIFI_API kifi_status kifi_batch_pose(kifi_batch* b, int scene, float out_eye_to_world[16]);
 /* the fusion stream (a cudaStream_t): steps end on it */
 KIFI_API void* kifi_batch_stream(kifi_batch* b);
+/* No counterpart in the reference.  With on != 0 each step's fusion of a
+ * key-width group (set-up, splat, digit histograms, digit passes, merge
+ * partition, merge + TSDF update of every scene) is one persistent launch of
+ * ctas_per_sm CTAs per SM (0: one) whose CTAs walk a device work queue of
+ * (stage, scene, chunk) items in stage order; an item first waits, bounded,
+ * for its scene's previous stage (KIFI_ERR_TIMEOUT past the bound).  Results
+ * equal the launch-per-stage path.  Tracking stays one launch per stage. */
+KIFI_API kifi_status kifi_batch_set_persistent(kifi_batch* b, int on, int ctas_per_sm);
 /* step timers: while on, every step records its device span (upload of its
  * argument tables to the end of fusion and tracking); kifi_batch_step_times
  * waits for them, returns up to `capacity` spans (ms) and their count, and

@@ -149,6 +149,7 @@ SIGNATURES = {
     "kifi_batch_pose": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
     "kifi_batch_stream": (C.c_void_p, [C.c_void_p]),
     "kifi_batch_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
+    "kifi_batch_set_persistent": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "kifi_batch_step_times": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
     "kifi_volume_mesh_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
     "kifi_volume_mesh_stage_times": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int)]),

@@ -110,11 +110,10 @@ def _desc(spec, icp_iters, mesh_every):
     return d
 
 
-def run_batch(specs, unique=40, icp_iters=15, warmup_steps=3):
-    """All scenes through one kifi_batch: a step is one launch per stage for
-    every scene that still has frames.  Returns the same summary as run()."""
+def render_batch(specs, unique=40):
+    """Each scene's unique frames on the device, its poses and its playback
+    order; and the seconds it took."""
     import torch
-    lib = _lib.load()
     t0 = time.perf_counter()
     data = []
     for spec in specs:
@@ -125,7 +124,19 @@ def run_batch(specs, unique=40, icp_iters=15, warmup_steps=3):
         data.append((fr, np.stack([scenes.kifi_matrix(np.linalg.inv(p)) for p in poses]),
                      frame_order(n_unique, spec["frames"])))
     torch.cuda.synchronize()
-    t_render = time.perf_counter() - t0
+    return data, time.perf_counter() - t0
+
+
+def run_batch(specs, unique=40, icp_iters=15, warmup_steps=3, persistent=False, queue_ctas_per_sm=1,
+              rendered=None):
+    """All scenes through one kifi_batch: a step is one launch per stage for
+    every scene that still has frames, or with `persistent` one persistent
+    fusion launch over a device work queue (kifi_batch_set_persistent) plus
+    the tracking launches.  `rendered`: render_batch's result, to reuse.
+    Returns the same summary as run()."""
+    import torch
+    lib = _lib.load()
+    data, t_render = rendered if rendered is not None else render_batch(specs, unique)
     n = len(specs)
     descs = (PipelineDesc * n)(*[_desc(s, icp_iters, 0) for s in specs])
     for d, s in zip(descs, specs):
@@ -135,6 +146,7 @@ def run_batch(specs, unique=40, icp_iters=15, warmup_steps=3):
     b = C.c_void_p()
     check(lib.kifi_batch_create(descs, n, C.byref(b)), "batch")
     try:
+        check(lib.kifi_batch_set_persistent(b, 1 if persistent else 0, queue_ctas_per_sm), "persistent")
         steps = max(s["frames"] for s in specs)
         ptrs = (C.c_void_p * n)()
         poses = np.zeros((n, 16), np.float32)
@@ -176,14 +188,14 @@ def run_batch(specs, unique=40, icp_iters=15, warmup_steps=3):
             total += nv.value
     finally:
         lib.kifi_batch_destroy(b)
-    return {"mode": "batch", "scenes": n, "frames": int(frames), "seconds": elapsed,
+    return {"mode": "batch, persistent fusion queue (%d CTAs per SM)" % queue_ctas_per_sm if persistent
+            else "batch, one launch per stage", "scenes": n, "frames": int(frames), "seconds": elapsed,
             "frames_per_s": frames / elapsed, "steps": int(nl.value),
             "step_latency_ms_p50": float(np.percentile(lat, 50)), "step_latency_ms_p99": float(np.percentile(lat, 99)),
             "resident_voxels_total": int(total), "render_seconds": t_render, "icp_iterations": icp_iters,
             "unique_frames_per_scene": unique,
-            "latency_note": "a step runs every active scene's frame in one launch per stage, so each scene's "
-                            "step latency is the step's (device span from the argument upload to the end of "
-                            "fusion and tracking)"}
+            "latency_note": "a step runs every active scene's frame together, so each scene's step latency is "
+                            "the step's (device span from the argument upload to the end of fusion and tracking)"}
 
 
 def run(specs, unique=40, icp_iters=15, mesh_every=0, warmup_steps=3):
@@ -234,13 +246,15 @@ def main():
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--unique", type=int, default=40)
     ap.add_argument("--icp-iterations", type=int, default=15)
-    ap.add_argument("--mode", default="batch", choices=["batch", "streams"])
+    ap.add_argument("--mode", default="batch", choices=["batch", "queue", "streams"])
+    ap.add_argument("--queue-ctas", type=int, default=1, help="persistent fusion CTAs per SM (--mode queue)")
     args = ap.parse_args()
     import torch
     torch.cuda.set_device(0)
     specs = scene_specs(args.scenes, args.seed)
-    if args.mode == "batch":
-        res = run_batch(specs, unique=args.unique, icp_iters=args.icp_iterations)
+    if args.mode in ("batch", "queue"):
+        res = run_batch(specs, unique=args.unique, icp_iters=args.icp_iterations, persistent=args.mode == "queue",
+                        queue_ctas_per_sm=args.queue_ctas)
     else:
         res = run(specs, unique=args.unique, icp_iters=args.icp_iterations)
     res["mix"] = {"sizes": {"%dx%d" % (w, h): sum(1 for s in specs if s["width"] == w) for w, h, _ in SIZES},

@@ -12,8 +12,11 @@
 // sized by the scene's frame or volume); a scene's CTAs run the
 // single-volume kernel body on that scene's arguments, read from a device
 // table uploaded once per step.  Scenes with 32-bit and 64-bit keys are two
-// groups, one fusion launch sequence each.  Results equal the scenes run one
-// by one (the same kernel bodies on the same inputs).
+// groups, one fusion launch sequence each.  With kifi_batch_set_persistent a
+// group's fusion is instead one persistent launch whose CTAs walk a device
+// work queue of (stage, scene, chunk) items (k_fuse_queue, kifi_integrate.cu).
+// Results equal the scenes run one by one (the same kernel bodies on the
+// same inputs).
 //
 // Tracking is the open-loop pipeline's: each frame against the previous
 // frame's back-projection, from the previous given pose.
@@ -59,6 +62,10 @@ struct kifi_batch {
     cudaEvent_t uploaded[2] = {nullptr, nullptr};  // the slot's host table has been copied
     cudaEvent_t tracked[2] = {nullptr, nullptr};   // the slot's step no longer reads its device table
     long long steps = 0;
+    // fusion as one persistent launch over a device work queue
+    // (kifi_batch_set_persistent), with this many CTAs per SM
+    bool persistent = false;
+    int queue_ctas_per_sm = 1;
     // step timers
     bool profiling = false;
     std::vector<cudaEvent_t> ev_pool;
@@ -256,15 +263,23 @@ kifi_status kifi_batch_step_device(kifi_batch* b, const void* const* depth_dev, 
         if (b->desc[i].icp_iterations != iters)
             return fail(KIFI_ERR_UNSUPPORTED, "the scenes of a batch track with one iteration count");
 
-    // one table: both groups' jobs and maps, the ICP jobs and map, the back-projections and map
+    // one table: both groups' jobs and maps (and, for the persistent fusion,
+    // the queue counter and per-scene stage counts, zero), the ICP jobs and
+    // map, the back-projections and map
     size_t off = 0;
-    size_t o_jobs[2], o_maps[2][5], o_ij = 0, o_im = 0, o_bj = 0, o_bm = 0;
+    size_t o_jobs[2], o_maps[2][5], o_queue[2] = {0, 0}, queue_words[2] = {0, 0}, o_ij = 0, o_im = 0, o_bj = 0,
+                                                         o_bm = 0;
     for (int gi = 0; gi < 2; ++gi) {
         o_jobs[gi] = off;
         off = up(off + grp[gi].jobs.size() * sizeof(FuseJob));
         for (int m = 0; m < 5; ++m) {
             o_maps[gi][m] = off;
             off = up(off + (grp[gi].jobs.size() + 1) * sizeof(unsigned int));
+        }
+        if (b->persistent && !grp[gi].jobs.empty()) {
+            o_queue[gi] = off;
+            queue_words[gi] = 1 + grp[gi].jobs.size() * (size_t)(5 + grp[gi].passes);
+            off = up(off + queue_words[gi] * sizeof(unsigned int));
         }
     }
     o_ij = off;
@@ -296,6 +311,7 @@ kifi_status kifi_batch_step_device(kifi_batch* b, const void* const* depth_dev, 
         std::memcpy(h + o_jobs[gi], g.jobs.data(), g.jobs.size() * sizeof(FuseJob));
         std::vector<unsigned int>* maps[5] = {&g.splat, &g.hist, &g.pass, &g.part, &g.merge};
         for (int m = 0; m < 5; ++m) std::memcpy(h + o_maps[gi][m], maps[m]->data(), maps[m]->size() * 4);
+        if (queue_words[gi]) std::memset(h + o_queue[gi], 0, queue_words[gi] * sizeof(unsigned int));
     }
     if (!ijobs.empty()) {
         std::memcpy(h + o_ij, ijobs.data(), ijobs.size() * sizeof(IcpJob));
@@ -334,7 +350,24 @@ kifi_status kifi_batch_step_device(kifi_batch* b, const void* const* depth_dev, 
             return BlockMap{(const unsigned int*)(dv + o_maps[gi][m]), n, f.back()};
         };
         FuseMaps fm{map(0, g.splat), map(1, g.hist), map(2, g.pass), map(3, g.part), map(4, g.merge)};
-        KIFI_CUDA(integrate_batch_enqueue((const FuseJob*)(dv + o_jobs[gi]), n, g.key_bytes, g.passes, fm, b->fs));
+        if (b->persistent) {
+            FuseQueuePlan q;
+            q.n = n;
+            q.passes = g.passes;
+            q.stages = 5 + g.passes;
+            const BlockMap* bm[5] = {&fm.splat, &fm.hist, &fm.pass, &fm.partition, &fm.merge};
+            for (int m = 0; m < 5; ++m) q.maps[m] = *bm[m];
+            q.first[0] = 0u;
+            for (int k = 0; k < q.stages; ++k)
+                q.first[k + 1] = q.first[k] + (k == 0 ? (unsigned int)n : q.maps[fuse_stage_map(k, q.passes)].grid);
+            unsigned int* qw = (unsigned int*)(dv + o_queue[gi]);
+            const int ctas = b->vol[g.scenes[0]]->ls.sms * b->queue_ctas_per_sm;
+            KIFI_CUDA(integrate_queue_enqueue((const FuseJob*)(dv + o_jobs[gi]), g.key_bytes, q, qw, qw + 1, ctas,
+                                              b->fs));
+        } else {
+            KIFI_CUDA(
+                integrate_batch_enqueue((const FuseJob*)(dv + o_jobs[gi]), n, g.key_bytes, g.passes, fm, b->fs));
+        }
     }
     KIFI_CUDA(cudaEventRecord(b->tracked[k], b->ts));
     if (e0) {
@@ -375,6 +408,13 @@ kifi_status kifi_batch_pose(kifi_batch* b, int scene, float out_eye_to_world[16]
         if (iters > 0) return KIFI_OK;
     }
     std::memcpy(out_eye_to_world, &b->prev_e2w[16 * scene], 64);
+    return KIFI_OK;
+}
+
+kifi_status kifi_batch_set_persistent(kifi_batch* b, int on, int ctas_per_sm) {
+    if (!b || ctas_per_sm < 0 || ctas_per_sm > 32) return fail(KIFI_ERR_INVALID_ARGUMENT, "bad argument");
+    b->persistent = on != 0;
+    b->queue_ctas_per_sm = ctas_per_sm > 0 ? ctas_per_sm : 1;
     return KIFI_OK;
 }
 

@@ -24,6 +24,11 @@
 //                  updated before it is written -- one read and one write of
 //                  the volume per frame.
 //
+// Batches (kifi_api_batch.cu) run the same bodies on many volumes: one
+// launch per stage whose CTAs are shared out by block maps, or k_fuse_queue,
+// one persistent launch whose CTAs walk a device work queue of (stage,
+// scene, chunk) items.
+//
 // Set semantics.  The reference dilates the sorted unique splat keys U with
 // three set unions: S2 = U + {0, dz, dy, dy+dz}, then the +x step adds s+1
 // for every s in S2 except the largest (its loop never emits the successor of
@@ -42,6 +47,7 @@
 #include <algorithm>
 
 #include "kifi_internal.h"
+#include "kifi_sort_body.cuh"
 
 namespace kifi {
 namespace {
@@ -159,19 +165,27 @@ __device__ __forceinline__ bool splat_pixel(const FrameConst& fc, const float (&
 // a share of a batched launch over several volumes).  With kHist (30-bit
 // keys) the CTA also counts the three 10-bit digits of every key it stores,
 // in shared memory, and adds its counts to the sort's histograms `hist`.
+constexpr int kEmitWarps = kEmitThreads / 32;
+struct SplatSmem {
+    unsigned long long ex;
+    unsigned int wtot[kEmitWarps], wpre[kEmitWarps], base;
+};
+template <bool kHist>
+struct SplatSmemHist : SplatSmem {
+    unsigned int counts[kHist ? kSortHistWords : 1];
+};
 template <bool kU16, typename K, bool kHist = false>
 __device__ __forceinline__ void splat_emit_body(DeviceCtl* __restrict__ ctl, const Geom& g,
                                                 const void* __restrict__ depth, uint32_t* __restrict__ bitmap,
                                                 K* __restrict__ new_keys, unsigned int new_cap,
                                                 const FrameConst& fc, unsigned int blk, unsigned int nblk,
-                                                unsigned int* __restrict__ hist = nullptr) {
+                                                SplatSmemHist<kHist>& sm, unsigned int* __restrict__ hist = nullptr) {
     static_assert(!kHist || sizeof(K) == 4, "digit counts of 30-bit keys");
     unsigned int* s_hist = nullptr;
     if constexpr (kHist) {
         // a CTA without pixels has nothing to count
         if ((size_t)blk * kEmitThreads >= (size_t)fc.width * fc.height) return;
-        __shared__ unsigned int s_counts[kSortHistWords];
-        s_hist = s_counts;
+        s_hist = sm.counts;
         for (int i = threadIdx.x; i < kSortHistWords; i += blockDim.x) s_hist[i] = 0u;
         __syncthreads();
     }
@@ -185,9 +199,10 @@ __device__ __forceinline__ void splat_emit_body(DeviceCtl* __restrict__ ctl, con
     // Per-frame counters are shared by every CTA: the excluded key's maximum
     // and the new-key count take one global atomic per CTA (one per warp
     // queued thousands of same-address atomics at one L2 slice).
-    constexpr int kEmitWarps = kEmitThreads / 32;
-    __shared__ unsigned long long s_ex;
-    __shared__ unsigned int s_wtot[kEmitWarps], s_wpre[kEmitWarps], s_base;
+    unsigned long long& s_ex = sm.ex;
+    unsigned int(&s_wtot)[kEmitWarps] = sm.wtot;
+    unsigned int(&s_wpre)[kEmitWarps] = sm.wpre;
+    unsigned int& s_base = sm.base;
     if (threadIdx.x == 0) s_ex = 0ull;
     __syncthreads();
     const size_t stride = (size_t)nblk * kEmitThreads;
@@ -310,7 +325,8 @@ __global__ void __launch_bounds__(kEmitThreads) k_splat_emit(DeviceCtl* __restri
                                                              K* __restrict__ new_keys,
                                                              unsigned int new_cap,
                                                              const FrameConst fc) {
-    splat_emit_body<kU16, K>(ctl, g, depth, bitmap, new_keys, new_cap, fc, blockIdx.x, gridDim.x);
+    __shared__ SplatSmemHist<false> sm;
+    splat_emit_body<kU16, K>(ctl, g, depth, bitmap, new_keys, new_cap, fc, blockIdx.x, gridDim.x, sm);
 }
 
 // 30-bit keys: the splat also fills the frame sort's digit histograms
@@ -321,8 +337,9 @@ __global__ void __launch_bounds__(kEmitThreads) k_splat_emit_hist(DeviceCtl* __r
                                                                   uint32_t* __restrict__ new_keys,
                                                                   unsigned int new_cap, const FrameConst fc,
                                                                   unsigned int* __restrict__ hist) {
+    __shared__ SplatSmemHist<true> sm;
     splat_emit_body<kU16, uint32_t, true>(ctl, g, depth, bitmap, new_keys, new_cap, fc, blockIdx.x, gridDim.x,
-                                          hist);
+                                          sm, hist);
 }
 
 // Packed float pairs (f32x2): one instruction, each half rounded as the
@@ -499,6 +516,11 @@ struct MergeInputs {
     bool update;              // run UpdateVoxels on the merged volume
 };
 
+struct PartitionSmem {
+    unsigned long long e, n1;
+    int ok;
+};
+
 // Merge set-up and partition.  Thread 0 settles the merge: drops the
 // dilation's excluded key when it is the largest new key (clearing its
 // occupancy bit), checks the capacity and publishes (e, N1).  Every thread t
@@ -509,11 +531,13 @@ template <typename K>
 __device__ __forceinline__ void merge_partition_body(DeviceCtl* __restrict__ ctl, const Geom& g,
                                                      const VolumeBuffers& vb, const MergeInputs<K>& in,
                                                      unsigned long long* __restrict__ splits,
-                                                     unsigned int max_tiles, unsigned int blk, unsigned int nblk) {
+                                                     unsigned int max_tiles, unsigned int blk, unsigned int nblk,
+                                                     PartitionSmem& sm) {
     constexpr int kTile = merge_tile<K>();
     const Codec<K> cd(g.kb);
-    __shared__ unsigned long long s_e, s_n1;
-    __shared__ int s_ok;
+    unsigned long long& s_e = sm.e;
+    unsigned long long& s_n1 = sm.n1;
+    int& s_ok = sm.ok;
     const unsigned int cur = ctl->cur;
     const unsigned long long N0 = ctl->n[cur];
     // select rather than index: a runtime index into a parameter array
@@ -569,7 +593,8 @@ __global__ void __launch_bounds__(256) k_merge_partition(DeviceCtl* __restrict__
                                                           VolumeBuffers vb, MergeInputs<K> in,
                                                           unsigned long long* __restrict__ splits,
                                                           unsigned int max_tiles) {
-    merge_partition_body<K>(ctl, g, vb, in, splits, max_tiles, blockIdx.x, gridDim.x);
+    __shared__ PartitionSmem sm;
+    merge_partition_body<K>(ctl, g, vb, in, splits, max_tiles, blockIdx.x, gridDim.x, sm);
 }
 
 // four consecutive keys, streamed (p 16-byte aligned for 32-bit keys,
@@ -590,18 +615,27 @@ __device__ __forceinline__ void st4(uint64_t* p, const uint64_t (&k)[4]) {
     __stcs((ulonglong2*)(p + 2), make_ulonglong2(k[2], k[3]));
 }
 
+template <typename K>
+struct MergeSmem {
+    alignas(16) K sA_k[merge_tile<K>() + 8];
+    float2 sA_v[merge_tile<K>() + 4];
+    K sB_k[merge_tile<K>()];
+    uint16_t sSrc[merge_tile<K>()];
+};
+
 template <bool kU16, typename K>
 __device__ __forceinline__ void merge_update_body(DeviceCtl* __restrict__ ctl, const Geom& g,
                                                   const VolumeBuffers& vb, const MergeInputs<K>& in,
                                                   const void* __restrict__ depth,
                                                   const unsigned long long* __restrict__ splits,
-                                                  const FrameConst& fc, unsigned int blk, unsigned int nblk) {
+                                                  const FrameConst& fc, unsigned int blk, unsigned int nblk,
+                                                  MergeSmem<K>& sm) {
     constexpr int kTile = merge_tile<K>();
     constexpr int kItems = kTile / kMergeThreads;
-    __shared__ __align__(16) K sA_k[kTile + 8];
-    __shared__ float2 sA_v[kTile + 4];
-    __shared__ K sB_k[kTile];
-    __shared__ uint16_t sSrc[kTile];
+    K* const sA_k = sm.sA_k;
+    float2* const sA_v = sm.sA_v;
+    K* const sB_k = sm.sB_k;
+    uint16_t* const sSrc = sm.sSrc;
 
     if (!ctl->merge_ok) return;
     const unsigned int cur = ctl->cur, out = cur ^ 1u;
@@ -873,7 +907,8 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_update(DeviceCtl* __res
                                                                 const void* __restrict__ depth,
                                                                 const unsigned long long* __restrict__ splits,
                                                                 const FrameConst fc) {
-    merge_update_body<kU16, K>(ctl, g, vb, in, depth, splits, fc, blockIdx.x, gridDim.x);
+    __shared__ MergeSmem<K> sm;
+    merge_update_body<kU16, K>(ctl, g, vb, in, depth, splits, fc, blockIdx.x, gridDim.x, sm);
 }
 template <bool kU16, typename K>
 __global__ void __launch_bounds__(kMergeThreads, 4) k_merge_update_alone(DeviceCtl* __restrict__ ctl, Geom g,
@@ -881,7 +916,8 @@ __global__ void __launch_bounds__(kMergeThreads, 4) k_merge_update_alone(DeviceC
                                                                          const void* __restrict__ depth,
                                                                          const unsigned long long* __restrict__ splits,
                                                                          const FrameConst fc) {
-    merge_update_body<kU16, K>(ctl, g, vb, in, depth, splits, fc, blockIdx.x, gridDim.x);
+    __shared__ MergeSmem<K> sm;
+    merge_update_body<kU16, K>(ctl, g, vb, in, depth, splits, fc, blockIdx.x, gridDim.x, sm);
 }
 
 // inserts: keep keys not yet in the volume (flat_map::insert keeps resident
@@ -945,8 +981,9 @@ __global__ void __launch_bounds__(kEmitThreads) k_splat_emit_batch(const FuseJob
     const int v = block_owner(m, blockIdx.x);
     const FuseJob& j = jobs[v];
     const unsigned int b0 = m.first[v];
+    __shared__ SplatSmemHist<false> sm;
     splat_emit_body<true, K>(j.ctl, j.g, j.depth, j.vb.bitmap, (K*)j.vb.new_keys, (unsigned int)j.vb.new_cap, j.fc,
-                             blockIdx.x - b0, m.first[v + 1] - b0);
+                             blockIdx.x - b0, m.first[v + 1] - b0, sm);
 }
 
 template <typename K>
@@ -955,7 +992,9 @@ __global__ void __launch_bounds__(256) k_merge_partition_batch(const FuseJob* __
     const FuseJob& j = jobs[v];
     const unsigned int b0 = m.first[v];
     const MergeInputs<K> in{(const K*)j.vb.new_keys, nullptr, nullptr, &j.ctl->n_new, true};
-    merge_partition_body<K>(j.ctl, j.g, j.vb, in, j.vb.splits, j.max_tiles, blockIdx.x - b0, m.first[v + 1] - b0);
+    __shared__ PartitionSmem sm;
+    merge_partition_body<K>(j.ctl, j.g, j.vb, in, j.vb.splits, j.max_tiles, blockIdx.x - b0, m.first[v + 1] - b0,
+                            sm);
 }
 
 template <typename K>
@@ -964,8 +1003,127 @@ __global__ void __launch_bounds__(kMergeThreads) k_merge_update_batch(const Fuse
     const FuseJob& j = jobs[v];
     const unsigned int b0 = m.first[v];
     const MergeInputs<K> in{(const K*)j.vb.new_keys, nullptr, nullptr, &j.ctl->n_new, true};
+    __shared__ MergeSmem<K> sm;
     merge_update_body<true, K>(j.ctl, j.g, j.vb, in, j.depth, j.vb.splits, j.fc, blockIdx.x - b0,
-                               m.first[v + 1] - b0);
+                               m.first[v + 1] - b0, sm);
+}
+
+// ---- batched fusion as one persistent launch over a device work queue
+//
+// The items of a step are (stage, scene, chunk): the frame set-up, the
+// splat chunks, the histogram chunks, each digit pass's chunks, the
+// partition chunks and the merge chunks of every scene, numbered stage by
+// stage (a stage's chunks per scene are its block map's shares).  CTAs take
+// item numbers from one counter.  Before its body an item waits until every
+// item of the scene's previous stage has finished; those items have smaller
+// numbers, so they were handed out before it, to CTAs that are running: the
+// wait always ends, whatever CTAs are resident.  A wait is bounded: past the
+// limit the scene's status takes KIFI_DEV_ERR_TIMEOUT, the item is skipped
+// (the partition then leaves the volume as it was) and still counts as done.
+template <typename K>
+union QueueSmem {
+    SplatSmemHist<false> splat;
+    sort_detail::SortHistSmem hist;
+    sort_detail::SortPassSmem<8> pass;
+    PartitionSmem part;
+    MergeSmem<K> merge;
+};
+
+__device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int* p) {
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// chunks of stage k for scene v (stage 0, the set-up: one)
+__device__ __forceinline__ unsigned int stage_chunks(const FuseQueuePlan& q, int k, int v) {
+    if (k == 0) return 1u;
+    const BlockMap& m = q.maps[fuse_stage_map(k, q.passes)];
+    return m.first[v + 1] - m.first[v];
+}
+
+template <typename K>
+__global__ void __launch_bounds__(kMergeThreads) k_fuse_queue(const FuseJob* __restrict__ jobs, FuseQueuePlan q,
+                                                               unsigned int* __restrict__ next,
+                                                               unsigned int* __restrict__ done,
+                                                               unsigned long long spin_limit) {
+    __shared__ QueueSmem<K> sm;
+    __shared__ unsigned int s_item;
+    __shared__ int s_go;
+    const unsigned int total = q.first[q.stages];
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(next, 1u);
+        __syncthreads();
+        const unsigned int i = s_item;
+        __syncthreads();  // read by every thread before thread 0 takes the next item
+        if (i >= total) break;
+        int k = 0;
+        while (i >= q.first[k + 1]) ++k;
+        const unsigned int local = i - q.first[k];
+        int v;
+        unsigned int c, nb;
+        if (k == 0) {
+            v = (int)local;
+            c = 0u;
+            nb = 1u;
+        } else {
+            const BlockMap& m = q.maps[fuse_stage_map(k, q.passes)];
+            v = block_owner(m, local);
+            c = local - m.first[v];
+            nb = m.first[v + 1] - m.first[v];
+        }
+        const FuseJob& j = jobs[v];
+        if (k > 0) {
+            if (threadIdx.x == 0) {
+                const unsigned int want = stage_chunks(q, k - 1, v);
+                const unsigned int* d = done + (size_t)v * q.stages + (k - 1);
+                unsigned long long spins = 0;
+                bool ok = true;
+                while (ld_acquire_u32(d) < want) {
+                    if (++spins > spin_limit) {
+                        ok = false;
+                        atomicOr(&j.ctl->status, KIFI_DEV_ERR_TIMEOUT);
+                        break;
+                    }
+                    __nanosleep(64);
+                }
+                s_go = ok;
+            }
+            __syncthreads();
+        }
+        if (k == 0 || s_go) {
+            const int pass = k - 3;
+            if (k == 0) {
+                if (threadIdx.x == 0) {
+                    j.ctl->n_new = 0u;
+                    j.ctl->excluded_key = 0ull;
+                }
+                sort_detail::sort_prepare_body(j.ss, q.passes);
+            } else if (k == 1) {
+                splat_emit_body<true, K>(j.ctl, j.g, j.depth, j.vb.bitmap, (K*)j.vb.new_keys,
+                                         (unsigned int)j.vb.new_cap, j.fc, c, nb, sm.splat);
+            } else if (k == 2) {
+                sort_detail::sort_histogram_body<K>((const K*)j.vb.new_keys, &j.ctl->n_new, j.ss, q.passes, c, nb,
+                                                    sm.hist);
+            } else if (pass < q.passes) {
+                K* keys = (K*)j.vb.new_keys;
+                K* alt = (K*)j.ss.alt_keys;
+                sort_detail::sort_pass_body<false, K, 8>(pass & 1 ? alt : keys, pass & 1 ? keys : alt, nullptr,
+                                                         nullptr, &j.ctl->n_new, j.ss, pass, c, sm.pass);
+            } else {
+                const MergeInputs<K> in{(const K*)j.vb.new_keys, nullptr, nullptr, &j.ctl->n_new, true};
+                if (pass == q.passes)
+                    merge_partition_body<K>(j.ctl, j.g, j.vb, in, j.vb.splits, j.max_tiles, c, nb, sm.part);
+                else
+                    merge_update_body<true, K>(j.ctl, j.g, j.vb, in, j.depth, j.vb.splits, j.fc, c, nb, sm.merge);
+            }
+        }
+        __syncthreads();  // the item's stores are done
+        if (threadIdx.x == 0) {
+            __threadfence();
+            atomicAdd(done + (size_t)v * q.stages + k, 1u);
+        }
+    }
 }
 
 __global__ void k_reset_new(DeviceCtl* ctl) {
@@ -1093,6 +1251,22 @@ cudaError_t integrate_batch_enqueue(const FuseJob* jobs, int n, int key_bytes, i
     if (n <= 0) return cudaSuccess;
     if (key_bytes == 8) return integrate_batch_t<uint64_t>(jobs, n, passes, maps, st);
     return integrate_batch_t<uint32_t>(jobs, n, passes, maps, st);
+}
+
+cudaError_t integrate_queue_enqueue(const FuseJob* jobs, int key_bytes, const FuseQueuePlan& plan,
+                                    unsigned int* next, unsigned int* done, int ctas, cudaStream_t st) {
+    if (plan.n <= 0) return cudaSuccess;
+    unsigned long long limit = 0;
+    {
+        SortScratch probe{};
+        sort_limits(&probe);
+        limit = probe.spin_limit;
+    }
+    if (key_bytes == 8)
+        k_fuse_queue<uint64_t><<<ctas, kMergeThreads, 0, st>>>(jobs, plan, next, done, limit);
+    else
+        k_fuse_queue<uint32_t><<<ctas, kMergeThreads, 0, st>>>(jobs, plan, next, done, limit);
+    return cudaGetLastError();
 }
 
 cudaError_t bitmap_rebuild_enqueue(const DeviceCtl* ctl, const Geom& g, const VolumeBuffers& vb,

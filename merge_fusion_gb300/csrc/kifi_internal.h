@@ -151,6 +151,23 @@ struct FuseMaps {
     BlockMap splat, hist, pass, partition, merge;
 };
 
+// The batched fusion of a step as one persistent launch over a device work
+// queue (integrate_queue_enqueue): stages 0 set-up, 1 splat, 2 histogram,
+// 3 .. 2 + passes the digit passes, then the partition and the merge; first[k]
+// is the number of stage k's first item, first[stages] the item count.
+constexpr int kQueueMaxStages = 5 + kSortMaxPasses;
+struct FuseQueuePlan {
+    int n = 0;       // scenes
+    int passes = 0;  // digit passes
+    int stages = 0;  // 5 + passes
+    unsigned int first[kQueueMaxStages + 1] = {};
+    BlockMap maps[5] = {};  // splat, histogram, pass, partition, merge
+};
+// the block map of stage k (k >= 1)
+KIFI_HD int fuse_stage_map(int k, int passes) {
+    return k == 1 ? 0 : k == 2 ? 1 : k < 3 + passes ? 2 : k == 3 + passes ? 3 : 4;
+}
+
 // Enqueues Integrator::Integrate of one frame for each of the n volumes of
 // `jobs` (a device table) on `st`: one launch per stage for all of them.
 // key_bytes: the volumes' key width; passes: digit passes of the sort.
@@ -161,6 +178,10 @@ cudaError_t sort_batch_enqueue(const FuseJob* jobs, int n, int key_bytes, int pa
 void sort_limits(SortScratch* s);
 cudaError_t integrate_batch_enqueue(const FuseJob* jobs, int n, int key_bytes, int passes, const FuseMaps& maps,
                                     cudaStream_t st);
+// the same as one persistent launch of `ctas` CTAs; next (1 word) and done
+// (plan.n x plan.stages words) must be zero
+cudaError_t integrate_queue_enqueue(const FuseJob* jobs, int key_bytes, const FuseQueuePlan& plan,
+                                    unsigned int* next, unsigned int* done, int ctas, cudaStream_t st);
 
 // ---------------------------------------------------------------- mesher
 struct MeshCounts {

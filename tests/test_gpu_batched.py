@@ -72,11 +72,14 @@ def _pipeline_alone(lib, spec, frames, w2e, iters):
         lib.kifi_pipeline_destroy(pipe)
 
 
-def test_batch_launches_equal_single_pipelines(gpu):
+@pytest.mark.parametrize("queue_ctas", [0, 1, 2])
+def test_batch_launches_equal_single_pipelines(gpu, queue_ctas):
     """kifi_batch (one launch per stage for all scenes, CTAs shared out by
-    block maps): every scene's volume and tracked pose equal the scene run
-    alone through kifi_pipeline -- 32- and 64-bit keys, three frame sizes,
-    scenes of different lengths (a scene sits out the steps after its end)."""
+    block maps; or, queue_ctas > 0, the persistent fusion launch over a device
+    work queue with that many CTAs per SM): every scene's volume and tracked
+    pose equal the scene run alone through kifi_pipeline -- 32- and 64-bit
+    keys, three frame sizes, scenes of different lengths (a scene sits out the
+    steps after its end)."""
     import torch
     from merge_fusion_gb300 import _lib, scenes
     from merge_fusion_gb300._lib import Camera, PipelineDesc, check
@@ -100,6 +103,7 @@ def test_batch_launches_equal_single_pipelines(gpu):
     b = C.c_void_p()
     check(lib.kifi_batch_create(descs, len(specs), C.byref(b)))
     try:
+        check(lib.kifi_batch_set_persistent(b, 1 if queue_ctas else 0, queue_ctas))
         check(lib.kifi_batch_set_profiling(b, 1))
         steps = max(s["frames"] for s in specs)
         for t in range(steps):
