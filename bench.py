@@ -615,7 +615,7 @@ def run_gpu(args, rank, world, local):
             ms_stage[0] / per, peak_kind,
             {"isolated": {"ms_per_launch": iso_stage[0] / iso_per,
                           "frac": gbs(iso_splat_bytes, iso_stage[0] / iso_per) / peak}}),
-        "sort (prepare, histogram, digit passes)": roofline_entry(
+        "sort (three 10-bit digit passes; set-up and digit counts ride on the set-up and splat kernels)": roofline_entry(
             "hbm", gbs(sort_bytes, ms_stage[1] / per), peak, "GB/s",
             {"bytes_per_launch": sort_bytes, "bytes_rule": "8 B per new key"}, ms_stage[1] / per, peak_kind,
             {"isolated": {"ms_per_launch": iso_stage[1] / iso_per,
