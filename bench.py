@@ -647,17 +647,18 @@ def run_gpu(args, rank, world, local):
     }
     value = job_throughput(world, KF, ms / 1e3)
     steps_launches = K * (FS * (LAUNCHES_FUSION + LAUNCHES_TRACKING) + LAUNCHES_MESH)
+    # `config` names the workload (the reference arm prints the same dict); `run` describes this run
     cfg = workload_config(Fp, FS)
-    cfg.update({"resident_voxels_start": n_start, "resident_voxels_end": int(n1[-1]) if m else None,
-                "roofline_frames": "the last %d timed frames (the device frame log's length)" % m,
-                "sequence_frames": SEQ_FRAMES, "frames_fused": n_frames,
-                "playback": "frames 0-299 forward, then back (%d frames fused in all)" % n_frames,
-                "parallelism": "replicas" if world > 1 else "single"})
+    run = {"resident_voxels_start": n_start, "resident_voxels_end": int(n1[-1]) if m else None,
+           "roofline_frames": "the last %d timed frames (the device frame log's length)" % m,
+           "sequence_frames": SEQ_FRAMES, "frames_fused": n_frames,
+           "playback": "frames 0-299 forward, then back (%d frames fused in all)" % n_frames,
+           "parallelism": "replicas" if world > 1 else "single"}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
         "warmup": Wu, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+u32", "data": "synthetic",
-        "config": cfg,
+        "config": cfg, "run": run,
         "roofline": dict(kernels["k_merge_update"], kernel="k_merge_update (fused merge-path union + TSDF update)",
                          kernels=kernels),
         "stage_ms_per_frame": {"splat_emit": ms_stage[0] / per, "sort": ms_stage[1] / per,
