@@ -4,11 +4,13 @@ sizes, voxel sizes and trajectory lengths.  Two ways to run them:
   * batch (default): one kifi_batch -- every step is one launch per stage of
     the path for all scenes, each launch sharing its CTAs out among the
     scenes (kifi_batch_step_device);
+  * queue: the same batch with each step's fusion as one persistent launch
+    whose CTAs walk a device work queue (kifi_batch_set_persistent);
   * streams: each scene a kifi_pipeline (its own volume, ICP context and
     CUDA streams); every step enqueues the next frame of every scene, so the
     GPU runs the scenes' kernels concurrently.
 
-    python -m merge_fusion_gb300.batched [--scenes 64] [--seed 7] [--mode batch|streams]
+    python -m merge_fusion_gb300.batched [--scenes 64] [--seed 7] [--mode batch|queue|streams]
 
 Scene i draws its frame size from {320x240, 512x424, 640x480, 1024x848},
 its voxel size from {2, 4, 8} mm (truncation 5 voxels; a 4.096 m cube of
