@@ -55,6 +55,8 @@ def test_null_arguments_are_rejected(kifi_lib):
     assert kifi_lib.kifi_integrate_f32(None, None, None, None) == 1
     assert kifi_lib.kifi_radix_sort_u32(None, 5) == 1
     assert kifi_lib.kifi_radix_sort_u32(None, 0) == 0  # empty sort is a no-op
+    assert kifi_lib.kifi_volume_set_launch_mode(None, 0) == 1
+    assert kifi_lib.kifi_batch_set_persistent(None, 1, 1) == 1
 
 
 def test_no_device_is_reported_not_faked(kifi_lib):
